@@ -1,0 +1,270 @@
+/*
+ * thorin_gpu.h -- C ABI of the GB300 (sm_103a) FP64 implementation of the
+ * FARGO_THORIN per-timestep hydrodynamics loop.
+ *
+ * The reference has no plugin/FFI layer: its driver calls
+ *   void AlgoGas(PolarGrid *Rho, *Vrad, *Vtheta, *Energy, *Label,
+ *                PlanetarySystem *sys, struct reb_simulation *rsim)
+ * once per DT (src_main/main.c:201, src_main/SourceEuler.c:210-317), and the
+ * physics routines communicate through globals (src_main/global.h,
+ * src_main/param.h).  This header replaces that link-level interface with
+ * plain C entry points (no C++/torch types): parameters are passed in one
+ * struct that mirrors the in.par variables (src_main/var.c:17-141) and the
+ * switches derived from them (src_main/Interpret.c:149-265); fields are passed
+ * as host double arrays in the reference's PolarGrid layout
+ * (l = j + i*nsec, rows 0..nrad, src_main/LowTasks.c:73-103).
+ *
+ * All entry points return a status code (THORIN_OK == 0).  Device memory is
+ * owned by the library; host arrays are owned by the caller.
+ */
+#ifndef THORIN_GPU_H
+#define THORIN_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define THORIN_OK               0
+#define THORIN_ERR_ARG          1   /* bad argument or unsupported option      */
+#define THORIN_ERR_CUDA         2   /* a CUDA call failed                       */
+#define THORIN_ERR_CRASH        3   /* negative density/energy (DetectCrash)    */
+#define THORIN_ERR_SOR_MAXIT    4   /* SOR hit its iteration cap                */
+#define THORIN_ERR_TIMEOUT      5   /* a bounded device wait gave up            */
+#define THORIN_ERR_STATE        6   /* call out of order                        */
+#define THORIN_ERR_NOMEM        7   /* allocation failed                        */
+#define THORIN_ERR_OMEGA        8   /* SOR omega calibration did not converge   */
+
+#define THORIN_MAXPLANETS     120   /* src_main/types.h:67 */
+
+/* Opacity laws (src_main/Interpret.c:250-265). */
+#define THORIN_OPA_BL94   0
+#define THORIN_OPA_ZHU12  1
+#define THORIN_OPA_LP85   2
+#define THORIN_OPA_CONST  3
+
+/* Field identifiers for upload/download.  Sizes are (nrad+1)*nsec doubles
+ * (the reference allocates nrad+1 rows; row nrad is the outer v_rad face). */
+enum thorin_field {
+  THORIN_DENS = 0,        /* gas surface density Sigma                 */
+  THORIN_VRAD,            /* gas radial velocity (inner face of cell)  */
+  THORIN_VTHETA,          /* gas azimuthal velocity (left face of cell)*/
+  THORIN_ENERGY,          /* gas internal energy per unit area         */
+  THORIN_PEBDENS,         /* pebble surface density                    */
+  THORIN_PEBVRAD,
+  THORIN_PEBVTHETA,
+  THORIN_PEBSIZE,         /* dominant pebble size (code units)         */
+  THORIN_TEMPER,          /* temperature (output only)                 */
+  THORIN_SOUNDSPEED,      /* sound speed (output only)                 */
+  THORIN_PRESSURE,        /* pressure (output only)                    */
+  THORIN_STOKES,          /* Stokes number (output only)               */
+  THORIN_QPLUS,           /* viscous heating (output only)             */
+  THORIN_DIVV,            /* velocity divergence (output only)         */
+  THORIN_OPACITY,         /* opacity in code units (output only)       */
+  THORIN_QMINUS,          /* radiative cooling term (output only)      */
+  THORIN_NFIELDS
+};
+
+/* Ring (1D radial) profiles kept by the reference as globals and used as
+ * damping targets / ring means.  Each has nrad entries. */
+enum thorin_profile {
+  THORIN_SIGMAMED = 0,    /* SigmaMed   (Theo.c:25, RefillSigma Theo.c:33) */
+  THORIN_SIGMAINF,        /* SigmaInf                                      */
+  THORIN_ENERGYMED,       /* EnergyMed  (Theo.c:76, RefillEnergy Theo.c:82)*/
+  THORIN_VTHETAMED,       /* VthetaMed  (Theo.c:132)                       */
+  THORIN_PEBDENSINIT,     /* PebDensInit   (Pebbles.c:182,208)             */
+  THORIN_PEBVRADINIT,     /* PebVradInit                                   */
+  THORIN_PEBVTHETAINIT,   /* PebVthetaInit                                 */
+  THORIN_NPROFILES
+};
+
+/* Parameters: the in.par variables (src_main/var.c) and derived switches
+ * (src_main/Interpret.c:149-265) read by the hydro loop.  Integers are 0/1
+ * switches unless noted.  thorin_params_default() fills the reference's
+ * defaults. */
+typedef struct thorin_params {
+  /* mesh */
+  int    nrad, nsec;
+  int    log_grid;               /* RadialSpacing Logarithmic           */
+  double rmin, rmax;
+  /* disk profiles */
+  double sigma0, sigma_slope, aspect_ratio, flaring_index;
+  double scaling_factor;         /* -f command-line factor (main.c:100) */
+  double cavity_radius, cavity_ratio, cavity_width, lambda_doubling;
+  double transition_radius, transition_ratio, transition_width;
+  /* viscosity */
+  double viscosity, alpha_viscosity;
+  int    viscosity_alpha;        /* ALPHAVISCOSITY != 0                 */
+  int    alpha_flock;
+  double alpha_mri, alpha_dead, tmri, twidth;
+  /* energy equation */
+  int    energy_eq;
+  double adiabind;
+  double cooling_time;           /* > 0 selects parametric cooling      */
+  int    parametric_cooling;
+  int    stellar_irradiation;
+  double opacity_drop, effective_temperature, stellar_radius, disc_albedo;
+  double parametric_opacity;
+  int    opacity_law;            /* THORIN_OPA_*                        */
+  /* planets and disk forces */
+  double thickness_smoothing;
+  int    exclude_hill;
+  double hillcut;
+  int    indirect_term;
+  double mass_taper;             /* MASSTAPER                           */
+  double vertical_damping;
+  int    feel_disk;
+  double accretion_rate;         /* ACCRETIONRATE (gas accretion)       */
+  int    gas_accret_heating;
+  double planetary_density;
+  int    aerodynamic_drag;
+  /* frame and transport */
+  double omega_frame;
+  int    fast_transport;         /* FARGO (1) or standard (0)           */
+  /* boundaries */
+  int    damping, damp_vrad, damp_init, damp_flux;
+  double damping_rmin_frac, damping_rmax_frac, damping_period_frac;
+  double gasflux;
+  int    open_inner, open_outer, non_reflecting, outer_source_mass;
+  double imposed_disk_drift;
+  /* time stepping */
+  double dt;                     /* DT                                  */
+  double first_step, minimum_step, maximum_step;
+  int    sloppy_cfl;
+  /* pebbles */
+  int    pebbles, back_reaction, accret_heating, diffusive_particles, pebble_gravity;
+  double pebble_alpha, pebble_bulk_dens, schmidt_number;
+  double pebble_flux, pebble_coagulation, pebble_to_gas_max;
+  double fragment_factor, fragment_threshold, fragment_alpha;
+  double evaporation_rate, evaporation_temperature;
+  int    heating_delay;
+  double parametric_accretion;
+  int    prescribed_accretion;
+  /* SOR (EnergySources.c:22-27; the tolerance is a compile-time constant
+   * there and a parameter here) */
+  double sor_eps;                /* SOREPS                              */
+  int    sor_maxiters;           /* SORMAXITERS                         */
+} thorin_params;
+
+/* The planetary system as seen by the hydro loop (src_main/types.h:96-115). */
+typedef struct thorin_planets {
+  int    nb;
+  double mass[THORIN_MAXPLANETS], gas[THORIN_MAXPLANETS], solid[THORIN_MAXPLANETS];
+  double x[THORIN_MAXPLANETS], y[THORIN_MAXPLANETS], z[THORIN_MAXPLANETS];
+  double vx[THORIN_MAXPLANETS], vy[THORIN_MAXPLANETS], vz[THORIN_MAXPLANETS];
+  double ax[THORIN_MAXPLANETS], ay[THORIN_MAXPLANETS], az[THORIN_MAXPLANETS];
+  double acc[THORIN_MAXPLANETS];
+  int    feel_disk[THORIN_MAXPLANETS];
+} thorin_planets;
+
+/* Run statistics of the last call. */
+typedef struct thorin_stats {
+  int    substeps;               /* hydro substeps done in the last DT          */
+  int    sor_calls;              /* SOR solves so far                           */
+  long long sor_sweeps;          /* SOR sweeps so far (sum of Niter)            */
+  int    sor_last_niter;         /* Niter of the last solve                     */
+  double sor_omega;              /* omega used by the last solve                */
+  int    crashed;                /* DetectCrash result of the last substep      */
+  double physical_time;
+  double last_dt;
+} thorin_stats;
+
+/* Fill p with the reference defaults of src_main/var.c and nrad x nsec. */
+void thorin_params_default(thorin_params *p, int nrad, int nsec);
+
+typedef struct thorin_disk thorin_disk;   /* one disk resident on one GPU */
+
+/* Allocate all device state for one disk on the current CUDA device.
+ * Replaces InitEuler's allocations (SourceEuler.c:133-175) and
+ * CreatePolarGrid (LowTasks.c:73). */
+int thorin_gpu_create(const thorin_params *p, thorin_disk **out);
+int thorin_gpu_destroy(thorin_disk *d);
+
+/* Build the 1D grid arrays (FillPolar1DArrays, SourceEuler.c:68-131), the
+ * default initial state (FillSigma/FillEnergy/InitGasDensityEnergy,
+ * ComputeSoundSpeed/Pressure/Temperature, InitGasVelocity,
+ * SetWaveKillingZones: SourceEuler.c:133-175, Pframeforce.c:620-751,
+ * SideEuler.c:341-362) and, with pebbles, the flux-equilibrium pebble disk
+ * (EquilPebbleDisk, Pebbles.c:58-204).  Fields are left on the device. */
+int thorin_gpu_init_default(thorin_disk *d);
+
+/* Host<->device copies of one field, (nrad+1)*nsec doubles. */
+int thorin_gpu_upload(thorin_disk *d, int field, const double *host);
+int thorin_gpu_download(thorin_disk *d, int field, double *host);
+
+/* After fields were uploaded (the InitializeFromFile / restart paths of
+ * Init.c:81-136 and Pebbles.c:66-75): recompute c_s, P, T and the ring means
+ * from the resident fields.  flags: THORIN_REFILL_GAS redoes RefillSigma,
+ * RefillEnergy and FillVtheta (Theo.c:33-151); THORIN_REFILL_PEBBLES redoes
+ * BckpFieldsForBC (Pebbles.c:208-232). */
+#define THORIN_REFILL_GAS     1
+#define THORIN_REFILL_PEBBLES 2
+int thorin_gpu_refresh(thorin_disk *d, int flags);
+
+/* Ring profiles (nrad doubles each). */
+int thorin_gpu_set_profile(thorin_disk *d, int profile, const double *host);
+int thorin_gpu_get_profile(thorin_disk *d, int profile, double *host);
+
+/* Simulation clock (PhysicalTime / PhysicalTimeInitial, main.c:166). */
+int thorin_gpu_set_time(thorin_disk *d, double physical_time);
+
+/* ---- phase API: the pieces of one AlgoGas substep, for a host driver that
+ * keeps REBOUND on the host (SourceEuler.c:229-315). ---- */
+
+/* PebbleStokesNumbers + CriticalCharTime + ConditionCFL
+ * (Pebbles.c:280,729; SourceEuler.c:589-712).  invdtreb_sq comes from
+ * MinStepForRebound (ReboundInterface.c:360).  Returns the substep count
+ * for the remaining interval dt_remaining. */
+int thorin_gpu_cfl(thorin_disk *d, double dt_remaining, double invdtreb_sq, int *n_sub);
+
+/* InitHeating + AccretePebblesOntoPlanets + Heating1 + EvaporatePebbles
+ * (Planet.c:222-258, Pebbles.c:353-539, Pebbles.c:834-864).  Updates the
+ * planets' masses and velocities in sys. */
+int thorin_gpu_accrete(thorin_disk *d, thorin_planets *sys, double dt);
+
+/* FillForcesArrays (Pframeforce.c:43-510) incl. ThicknessSmoothing
+ * (Force.c:75): fills the disk accelerations on the device and returns the
+ * disk-on-planet accelerations in sys->ax/ay, the indirect term in
+ * indirect[2] and, for DampingTW04 (Pframeforce.c:571), the ring means of
+ * Sigma and c_s at each planet (ring_rho/ring_cs, may be NULL). */
+int thorin_gpu_forces(thorin_disk *d, thorin_planets *sys, double mass_taper,
+                      double indirect[2], double *ring_rho, double *ring_cs);
+
+/* Everything after the planet update in one substep: boundaries, crash test,
+ * pressure, pebble sources, SubStep1/2/3, implicit radiative diffusion with
+ * SOR, transport, EOS refresh, pebble transport (SourceEuler.c:270-313).
+ * Advances the clock by dt. */
+int thorin_gpu_hydro(thorin_disk *d, double dt);
+
+/* ---- whole-DT driver ---- */
+
+/* One call of AlgoGas (SourceEuler.c:210-317) with the planets integrated on
+ * the host by the library's own N-body integrator (standing in for
+ * REBOUND's IAS15, ReboundInterface.c:262-325).  sys is updated in place. */
+int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys);
+
+/* Conservation integrals (SideEuler.c:26-80,523-565), summed on the device. */
+int thorin_gpu_integrals(thorin_disk *d, double *mass, double *momentum,
+                         double *energy, double *peb_mass, double *peb_momentum);
+
+/* Per-ring FARGO shifts of the last gas transport (TransportEuler.c:70-111),
+ * nrad ints. */
+int thorin_gpu_get_nshift(thorin_disk *d, int *host);
+
+int thorin_gpu_get_stats(thorin_disk *d, thorin_stats *s);
+
+/* Last CUDA error string (thread-local, for diagnostics). */
+const char *thorin_gpu_last_error(void);
+
+/* ---- host N-body (stands in for REBOUND) ---- */
+
+/* reb_tools_orbit_to_particle semantics: planet k from orbital elements
+ * (degrees), heliocentric.  mass etc. are read as float like
+ * SetupReboundSimulation does (ReboundInterface.c:137-170). */
+int thorin_planet_from_elements(thorin_planets *sys, int k, float mass, float gas,
+                                float solid, float a, float e, float inc,
+                                float Omega, float omega, float f);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* THORIN_GPU_H */

@@ -1,0 +1,155 @@
+"""Generate golden fixtures from the reference FARGO_THORIN binary.
+
+Builds the reference's sequential binary from its sources with
+oracle/ref.mk (into oracle/_ref/), runs it on small disk set-ups and stores
+its outputs as .npz fixtures next to this script.  Needs the reference tree
+(default /root/reference, or $THORIN_REFERENCE); the fixtures it writes are
+committed so that the tests never need the reference at run time.
+
+Each case runs the reference twice, like the measured workloads prescribe:
+``thorin -0`` dumps the default initial state, that state is perturbed
+(Sigma (1 + 1e-4 u), v_r = 0, and for pebble cases Sigma_p = 0.01 Sigma with
+Stokes number 0.1), and the perturbed state is fed back through the
+reference's own InitializeFromFile (gas only) or restart (-s 0, pebbles)
+path.  Recorded: the initial dump, field dumps after chosen DTs, the -a
+integrals after every DT, the -d SOR iteration counts and CFL substep counts,
+and the planet state of the torque log (tqwk0.dat, written every DT).
+
+Usage: python tests/golden/make_golden.py [case ...]
+"""
+from __future__ import annotations
+
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from fargo_thorin_gb300 import workloads  # noqa: E402
+
+REF = os.environ.get("THORIN_REFERENCE", "/root/reference")
+THORIN = os.path.join(ROOT, "oracle", "_ref", "thorin")
+
+# name: (kind, nrad, nsec, ntot, ninterm, extra in.par lines, full-field snapshots?)
+CASES = {
+    "disk0_24x72": ("disk0", 24, 72, 4, 1, "", True),
+    "disk1_32x96": ("disk1", 32, 96, 3, 1, "", True),
+    "disk0_128x384_200": ("disk0", 128, 384, 200, 100, "", False),
+    "disk1_64x192_40": ("disk1", 64, 192, 40, 20, "", False),
+}
+GAS = ["dens", "vrad", "vtheta", "temper"]
+PEB = ["pebbledens", "pebblevrad", "pebblevtheta"]
+SAMPLE_ROWS_FRAC = [0.0, 0.3, 0.5, 0.75, 1.0]
+
+
+def build_reference():
+    subprocess.run(["make", "-s", "-f", os.path.join(ROOT, "oracle", "ref.mk"), f"REF={REF}"], check=True)
+
+
+def read_dump(out, name, k, nr, ns):
+    return np.fromfile(os.path.join(out, f"gas{name}{k}.dat"), dtype="<f8").reshape(nr, ns)
+
+
+def run(cmd, cwd):
+    r = subprocess.run(cmd, cwd=cwd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{cmd} failed: {r.stdout[-2000:]} {r.stderr[-2000:]}")
+    return r.stdout
+
+
+def parse_log(text):
+    """Per-DT integrals, SOR Niter per solve, CFL substeps per DT."""
+    mom, mass, ener, niter, subs = [], [], [], [], []
+    cfl_calls = 0
+    for line in text.splitlines():
+        if "Limit time step adopted" in line:
+            cfl_calls += 1
+        m = re.search(r"SOR: Niter = (\d+)", line)
+        if m and "omega" not in line:
+            niter.append(int(m.group(1)))
+        if line.startswith("Gas Momentum"):
+            mom.append(float(line.split(":")[1]))
+            subs.append(cfl_calls)
+            cfl_calls = 0
+        elif line.startswith("Gas total Mass"):
+            mass.append(float(line.split(":")[1]))
+        elif line.startswith("Gas total Energy"):
+            ener.append(float(line.split(":")[1]))
+    return dict(momentum=np.array(mom), mass=np.array(mass), energy=np.array(ener),
+                sor_niter=np.array(niter, dtype=np.int64), substeps=np.array(subs, dtype=np.int64))
+
+
+def make_case(name):
+    kind, nr, ns, ntot, ninterm, extra, full = CASES[name]
+    work = tempfile.mkdtemp(prefix="thorin_golden_")
+    try:
+        out = os.path.join(work, "out")
+        par = workloads.inpar_text(kind, nr, ns) + extra
+        par = re.sub(r"Ntot \d+", f"Ntot {ntot}", par)
+        par = re.sub(r"Ninterm \d+", f"Ninterm {ninterm}", par)
+        par = par.replace("OutputDir out", f"OutputDir {out}")
+        planet = workloads.PLANET1 if kind == "disk1" else workloads.PLANET0
+        with open(os.path.join(work, "planet.cfg"), "w") as f:
+            f.write("Embryo1 " + " ".join(repr(v) for v in planet) + "\n")
+        par += f"PlanetConfig {os.path.join(work, 'planet.cfg')}\n"
+        with open(os.path.join(work, "in.par"), "w") as f:
+            f.write(par)
+        run([THORIN, "-0", "in.par"], work)
+        init = {k: read_dump(out, k, 0, nr, ns) for k in GAS}
+        if kind == "disk1":
+            for k in PEB + ["pebblesize", "pebblestokes"]:
+                init[k] = read_dump(out, k, 0, nr, ns)
+        params = workloads.params_for(kind, nr, ns)
+        st = workloads.perturbed_state(params, {"dens": init["dens"].ravel(), "temper": init["temper"].ravel()})
+        if kind == "disk0":
+            files = {"DensInfile": st["dens"], "VradInfile": st["vrad"],
+                     "VthetaInfile": init["vtheta"].ravel(), "TemperInfile": init["temper"].ravel()}
+            for key, arr in files.items():
+                path = os.path.join(work, key + ".txt")
+                np.savetxt(path, arr, fmt="%.17g")
+                par += f"{key} {path}\n"
+            par += "InitializeFromFile YES\n"
+            with open(os.path.join(work, "in.par"), "w") as f:
+                f.write(par)
+            log = run([THORIN, "-ad", "in.par"], work)
+        else:
+            st["dens"].astype("<f8").tofile(os.path.join(out, "gasdens0.dat"))
+            st["vrad"].astype("<f8").tofile(os.path.join(out, "gasvrad0.dat"))
+            st["pebdens"].astype("<f8").tofile(os.path.join(out, "gaspebbledens0.dat"))
+            st["pebsize"].astype("<f8").tofile(os.path.join(out, "gaspebblesize0.dat"))
+            log = run([THORIN, "-ad", "-s", "0", "in.par"], work)
+        res = {"inpar": np.array(par), "planet": np.array(planet), "nrad": nr, "nsec": ns,
+               "ntot": ntot, "ninterm": ninterm, "kind": np.array(kind)}
+        for k, v in init.items():
+            res["init_" + k] = v
+        res.update(parse_log(log))
+        names = GAS + (PEB if kind == "disk1" else [])
+        rows = sorted({min(nr - 1, int(round(f * (nr - 1)))) for f in SAMPLE_ROWS_FRAC})
+        res["sample_rows"] = np.array(rows)
+        for k in range(1, ntot // ninterm + 1):
+            for fname in names:
+                arr = read_dump(out, fname, k, nr, ns)
+                if full:
+                    res[f"out{k}_{fname}"] = arr
+                else:
+                    res[f"out{k}_{fname}_ringmean"] = arr.mean(axis=1)
+                    res[f"out{k}_{fname}_rows"] = arr[rows]
+                    res[f"out{k}_{fname}_l2"] = np.sqrt(np.sum(arr * arr))
+        tq = np.loadtxt(os.path.join(out, "tqwk0.dat"), ndmin=2)
+        res["tqwk"] = tq                      # t, tq, tq_norm, x, y, ax, ay (one line per DT)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+        print(name, "substeps", res["substeps"].tolist()[:10], "sor", res["sor_niter"].tolist()[:10])
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
+if __name__ == "__main__":
+    build_reference()
+    for name in (sys.argv[1:] or list(CASES)):
+        make_case(name)

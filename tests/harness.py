@@ -1,0 +1,49 @@
+"""Shared set-up for the parity tests: golden cases and initial states."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+from fargo_thorin_gb300 import workloads
+from fargo_thorin_gb300.params import derive, read_inpar
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+FIELD_IDS = {"dens": 0, "vrad": 1, "vtheta": 2, "energy": 3, "pebbledens": 4, "pebblevrad": 5,
+             "pebblevtheta": 6, "pebblesize": 7, "temper": 8, "soundspeed": 9, "pressure": 10,
+             "pebblestokes": 11, "qplus": 12, "divv": 13, "opacity": 14, "qminus": 15}
+GAS = ["dens", "vrad", "vtheta", "temper"]
+PEB = ["pebbledens", "pebblevrad", "pebblevtheta"]
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+def case_params(g, **kw):
+    return derive(read_inpar(str(g["inpar"])), **kw)
+
+
+def start_state(disk, params, init_fields, seed=0):
+    """Apply the measured initial state (perturbed Sigma, v_r = 0, pebble
+    overrides) on top of a disk that holds the default initial fields, then
+    refresh derived quantities like the reference's InitializeFromFile
+    (gas-only) or restart (pebbles) path."""
+    st = workloads.perturbed_state(params, init_fields, seed=seed)
+    disk.set(FIELD_IDS["dens"], st["dens"])
+    disk.set(FIELD_IDS["vrad"], st["vrad"])
+    disk.set(FIELD_IDS["energy"], st["energy"])
+    if params.pebbles:
+        disk.set(FIELD_IDS["pebbledens"], st["pebdens"])
+        disk.set(FIELD_IDS["pebblesize"], st["pebsize"])
+        disk.refresh(2)
+    else:
+        disk.refresh(1)
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
