@@ -1,0 +1,845 @@
+// kernels_aux.cu -- ring means, viscosity per ring, CFL, pebble source terms,
+// damping boundaries, disk forces with their reductions, pebble accretion,
+// conservation integrals.
+#include "thorin_kernels.cuh"
+
+static inline dim3 grid2d(int ns, int rows, int bx) { return dim3((ns + bx - 1) / bx, rows); }
+static const int BX = 128;
+
+#define CELL_LOOP_2D                                                        \
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;                      \
+  const int i = blockIdx.y;                                                 \
+  if (j >= ns) return;                                                      \
+  const int l = j + i * ns;
+
+// ---------------------------------------------------------------------------
+// Ring means summed in order (mpi_make1Dprofile, mpiTasks.c:12-36): one
+// warp per ring.
+__global__ void k_ring_mean(int nr, int ns, const double *__restrict__ f, double *__restrict__ out)
+{
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= nr) return;
+  const double s = warp_seq_sum(f + (size_t)w * ns, ns);
+  if ((threadIdx.x & 31) == 0) out[w] = s / (double)ns;
+}
+
+void aux_ring_mean(const DevGrid &g, const double *f, double *out, cudaStream_t s)
+{
+  const int threads = 256, warps = threads / 32;
+  k_ring_mean<<<(g.nr + warps - 1) / warps, threads, 0, s>>>(g.nr, g.ns, f, out);
+}
+
+// Ring mean of one ring (e.g. the ring holding a planet).
+__global__ void k_ring_mean_at(int ns, const double *__restrict__ f, int ring, double *out)
+{
+  const double s = warp_seq_sum(f + (size_t)ring * ns, ns);
+  if (threadIdx.x == 0) *out = s / (double)ns;
+}
+
+void aux_ring_mean_at(const DevGrid &g, const double *f, int ring, double *out, cudaStream_t s)
+{
+  k_ring_mean_at<<<1, 32, 0, s>>>(g.ns, f, ring, out);
+}
+
+// FViscosity at Rmed[i] and Rinf[i] (Viscosity.c:26-54).  The ring index
+// found by the reference's linear search is i for both radii; pow(r, 1.5)
+// comes precomputed from the host.
+
+__device__ __forceinline__ double fvisc(const ViscParams &v, double rad, double cs, double tmean, double r15)
+{
+  double nu = v.viscosity;
+  if (v.viscosity_alpha) nu = v.alpha * cs * cs * r15;
+  if (v.alpha_flock) {
+    double a = (v.alpha_mri - v.alpha_dead) * (1.0 - tanh((v.tmri - tmean * v.t2si) / v.twidth)) / 2.0 + v.alpha_dead;
+    nu = a * cs * cs * r15;
+  }
+  if (rad < v.cav_rmin) nu *= v.cav_ratio;
+  if ((rad >= v.cav_rmin) && (rad <= v.cav_rmax)) nu *= exp((v.cav_rmax - rad) / (v.cav_rmax - v.cav_rmin) * v.log_cav_ratio);
+  return nu;
+}
+
+__global__ void k_viscosity_rings(DevGrid g, ViscParams v)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.nr) return;
+  const double cs = g.r.csmean[i], tm = g.r.tempmean[i];
+  g.r.nu_med[i] = fvisc(v, g.r.Rmed[i], cs, tm, g.r.Rmed15[i]);
+  g.r.nu_inf[i] = fvisc(v, g.r.Rinf[i], cs, tm, g.r.Rinf15[i]);
+}
+
+void aux_viscosity_rings(const DevGrid &g, const ViscParams &v, cudaStream_t s)
+{
+  k_viscosity_rings<<<(g.nr + 127) / 128, 128, 0, s>>>(g, v);
+}
+
+// ---------------------------------------------------------------------------
+// PebbleStokesNumbers (Pebbles.c:280-300).
+__global__ void k_stokes(DevGrid g, const double *__restrict__ rho, const double *__restrict__ psize,
+                         double *__restrict__ tau)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  tau[l] = 2.0 * g.k.pebbulkdens * psize[l] / rho[l] * g.k.sqrt_adiabind_inv;
+}
+
+void aux_stokes(const DevGrid &g, const double *rho, const double *psize, double *tau, cudaStream_t s)
+{
+  k_stokes<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, psize, tau);
+}
+
+// ---------------------------------------------------------------------------
+// CFL: ConditionCFL (SourceEuler.c:589-712) and CriticalCharTime
+// (Pebbles.c:729-767).  Because x -> CFLSECURITY/sqrt((x + a) + b) is
+// monotone, the minimum over cells of the per-cell step equals the step of
+// the cell with the largest sum of squared rates, so block maxima of that
+// sum are reduced (exactly, in any order) and the step is formed once.
+
+__global__ void k_cfl_means(DevGrid g, const double *__restrict__ vt, const double *__restrict__ pvt, CflRings cr,
+                            int pebbles_fast)
+{
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= g.nr) return;
+  const double s = warp_seq_sum(vt + (size_t)w * g.ns, g.ns);
+  double p = 0.0;
+  if (pebbles_fast) p = warp_seq_sum(pvt + (size_t)w * g.ns, g.ns);
+  if ((threadIdx.x & 31) == 0) {
+    cr.vmoy[w] = s / (double)g.ns;
+    if (pebbles_fast) cr.pvtmed[w] = p / (double)g.ns;
+  }
+}
+
+__global__ void k_cfl_cells(DevGrid g, const double *__restrict__ vr, const double *__restrict__ vt,
+                            const double *__restrict__ cs, const double *__restrict__ pvr,
+                            const double *__restrict__ pvt, CflRings cr, int pebbles, int fast, int viscous,
+                            double *__restrict__ part)
+{
+  const int ns = g.ns;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y + 1;                    // rings One_or_active .. Max_or_active-1
+  double gas = 0.0, peb = -1.0e30;
+  if (j < ns) {
+    const int l = j + i * ns, lip = l + ns;
+    const int ljp = (j == ns - 1) ? i * ns : l + 1;
+    const double dxrad = cr.dxrad[i], dxtheta = cr.dxtheta[i];
+    const double vres = fast ? vt[l] - cr.vmoy[i] : vt[l];
+    const double invdt1 = cs[l] / cr.mindx[i];
+    const double invdt2 = fabs(vr[l]) / dxrad;
+    const double invdt3 = fabs(vres) / dxtheta;
+    double dvr = vr[lip] - vr[l], dvt = vt[ljp] - vt[l];
+    dvr = (dvr >= 0.0) ? 1e-10 : -dvr;
+    dvt = (dvt >= 0.0) ? 1e-10 : -dvt;
+    const double a = dvr / dxrad, b = dvt / dxtheta;
+    double invdt4 = (b > a) ? b : a;
+    invdt4 *= 4.0 * TH_CVNR * TH_CVNR;
+    const double invdt5 = viscous ? g.r.nu_med[i] * 4. / cr.den5[i] : 1e-30;
+    gas = invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4 + invdt5 * invdt5;
+    if (pebbles) {
+      const double p1 = fabs(pvr[l]) / dxrad;
+      const double vrp = fast ? pvt[l] - cr.pvtmed[i] : pvt[l];
+      const double p2 = fabs(vrp) / dxtheta;
+      const double p3 = fabs(pvr[l] - vr[l]) / dxrad;
+      const double p4 = fabs(pvt[l] - vt[l]) / dxtheta;
+      peb = p1 * p1 + p2 * p2 + p3 * p3 + p4 * p4;
+    }
+  }
+  const double mg = block_reduce(gas, OpMax(), 0.0);
+  const double mp = block_reduce(peb, OpMax(), -1.0e30);
+  if (threadIdx.x == 0) {
+    const int b = blockIdx.x + blockIdx.y * gridDim.x;
+    part[2 * b] = mg;
+    part[2 * b + 1] = mp;
+  }
+}
+
+
+__global__ void k_cfl_final(DevGrid g, const double *__restrict__ part, CflRings cr, CflFinal f,
+                            double *__restrict__ scal, int *__restrict__ iscal)
+{
+  double mg = 0.0, mp = -1.0e30, shear = 1e30;
+  for (int b = threadIdx.x; b < f.nb; b += blockDim.x) {
+    const double a = part[2 * b], c = part[2 * b + 1];
+    if (a > mg) mg = a;
+    if (c > mp) mp = c;
+  }
+  for (int i = threadIdx.x; i < g.nr - 1; i += blockDim.x) {
+    const double dt = f.twopi_cfl_ns / fabs(cr.vmoy[i] * g.r.InvRmed[i] - cr.vmoy[i + 1] * g.r.InvRmed[i + 1]);
+    if (dt < shear) shear = dt;
+  }
+  mg = block_reduce(mg, OpMax(), 0.0);
+  mp = block_reduce(mp, OpMax(), -1.0e30);
+  shear = block_reduce(shear, OpMin(), 1e30);
+  if (threadIdx.x == 0) {
+    double newdt;
+    if (!f.pebbles) newdt = TH_CFLSECURITY / sqrt(mg + f.invdtreb_sq);
+    else newdt = TH_CFLSECURITY / sqrt(mg + mp + f.invdtreb_sq);
+    if (newdt > 1e30) newdt = 1e30;
+    if (shear < newdt) newdt = shear;
+    const double dts = scal[SC_DTSTELLAR];
+    if (newdt > dts) {
+      const double m = (1.0 * dts > f.minimum_step) ? 1.0 * dts : f.minimum_step;
+      newdt = (newdt < m) ? newdt : m;
+    }
+    newdt = (newdt < f.maximum_step) ? newdt : f.maximum_step;
+    if (f.first_call && f.first_step > 0.0) newdt = f.first_step;
+    if (f.deltaT < newdt) newdt = f.deltaT;
+    scal[SC_NEWDT] = newdt;
+    scal[SC_INVDTPEB] = mp;
+    iscal[IS_NSUB] = (int)(ceil(f.deltaT / newdt));
+  }
+}
+
+void aux_cfl(const DevGrid &g, const double *vr, const double *vt, const double *cs, const double *pvr, const double *pvt,
+             const CflRings &cr, int pebbles, int fast, int viscous, double *part, const CflFinal &f0, double *scal,
+             int *iscal, cudaStream_t s)
+{
+  const int threads = 256, warps = threads / 32;
+  k_cfl_means<<<(g.nr + warps - 1) / warps, threads, 0, s>>>(g, vt, pvt, cr, pebbles && fast);
+  dim3 grid = grid2d(g.ns, g.nr - 1, 256);
+  k_cfl_cells<<<grid, 256, 0, s>>>(g, vr, vt, cs, pvr, pvt, cr, pebbles, fast, viscous, part);
+  CflFinal f = f0;
+  f.nb = grid.x * grid.y;
+  k_cfl_final<<<1, 1024, 0, s>>>(g, part, cr, f, scal, iscal);
+}
+
+// ---------------------------------------------------------------------------
+// EvaporatePebbles (Pebbles.c:834-864).
+__global__ void k_evaporate(DevGrid g, const double *__restrict__ T, double *__restrict__ pdens, double facc)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  if (T[l] > g.k.evaptemp) {
+    double d = pdens[l] * (1.0 - facc);
+    if (d < 1.0e-8) d = 1.0e-8;
+    pdens[l] = d;
+  }
+}
+
+void aux_evaporate(const DevGrid &g, const double *T, double *pdens, double facc, cudaStream_t s)
+{
+  k_evaporate<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, T, pdens, facc);
+}
+
+// ---------------------------------------------------------------------------
+// Damping boundaries (DampingBoundary, SideEuler.c:368-419, and DampPebbles,
+// SideEuler.c:423-456).  Only rings inside the damping zones are launched.
+__global__ void k_damp_gas(DevGrid g, double *__restrict__ vrad, double *__restrict__ rho, double *__restrict__ vtheta,
+                           double *__restrict__ energy, const int *__restrict__ rings, double dt, double omega_frame,
+                           int damp_init, int energy_eq)
+{
+  const int ns = g.ns;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ns) return;
+  const int i = rings[blockIdx.y];
+  const int l = j + i * ns;
+  const double lambda = g.r.WaveKiller[i] * dt;
+  vrad[l] = (vrad[l] + lambda * 0.0) / (1.0 + lambda);
+  if (damp_init) {
+    const double rho0 = g.r.SigmaMed[i], e0 = g.r.EnergyMed[i];
+    const double vt0 = g.r.VthetaMed[i] - g.r.Rmed[i] * omega_frame;
+    rho[l] = (rho[l] + lambda * rho0) / (1.0 + lambda);
+    vtheta[l] = (vtheta[l] + lambda * vt0) / (1.0 + lambda);
+    if (energy_eq) energy[l] = (energy[l] + lambda * e0) / (1.0 + lambda);
+  }
+}
+
+void aux_damp_gas(const DevGrid &g, double *vrad, double *rho, double *vtheta, double *energy, const int *rings,
+                  int nrings, double dt, double omega_frame, int damp_init, int energy_eq, cudaStream_t s)
+{
+  if (nrings <= 0) return;
+  k_damp_gas<<<grid2d(g.ns, nrings, BX), BX, 0, s>>>(g, vrad, rho, vtheta, energy, rings, dt, omega_frame, damp_init,
+                                                     energy_eq);
+}
+
+__global__ void k_damp_peb(DevGrid g, double *__restrict__ pd, double *__restrict__ pvr, double *__restrict__ pvt,
+                           const int *__restrict__ rings, double dt, double omega_frame)
+{
+  const int ns = g.ns;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ns) return;
+  const int i = rings[blockIdx.y];
+  const int l = j + i * ns;
+  const double lambda = g.r.WaveKiller[i] * dt;
+  const double d0 = g.r.PebDensInit[i], vr0 = g.r.PebVradInit[i];
+  const double vt0 = g.r.PebVthetaInit[i] - g.r.Rmed[i] * omega_frame;
+  pd[l] = (pd[l] + lambda * d0) / (1.0 + lambda);
+  pvr[l] = (pvr[l] + lambda * vr0) / (1.0 + lambda);
+  pvt[l] = (pvt[l] + lambda * vt0) / (1.0 + lambda);
+}
+
+void aux_damp_peb(const DevGrid &g, double *pd, double *pvr, double *pvt, const int *rings, int nrings, double dt,
+                  double omega_frame, cudaStream_t s)
+{
+  if (nrings <= 0) return;
+  k_damp_peb<<<grid2d(g.ns, nrings, BX), BX, 0, s>>>(g, pd, pvr, pvt, rings, dt, omega_frame);
+}
+
+// DetectCrash (SourceEuler.c:48-66): any negative value in rows 0..nr-1.
+__global__ void k_crash(int n, const double *__restrict__ f, int *flag)
+{
+  int bad = 0;
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n; l += gridDim.x * blockDim.x)
+    if (f[l] < 0.0) bad = 1;
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+void aux_crash(const DevGrid &g, const double *f, int *flag, cudaStream_t s)
+{
+  const int n = g.nr * g.ns;
+  int blocks = (n + 255) / 256;
+  if (blocks > 1216) blocks = 1216;
+  k_crash<<<blocks, 256, 0, s>>>(n, f, flag);
+}
+
+// ---------------------------------------------------------------------------
+// SourceTermsPebbles (Pebbles.c:550-613), after DampPebbles.
+__global__ void k_pebble_sources(DevGrid g, const double *__restrict__ pd, const double *__restrict__ pvr,
+                                 const double *__restrict__ pvt, const double *__restrict__ tau,
+                                 const double *__restrict__ vr, const double *__restrict__ vt,
+                                 const double *__restrict__ pagr, const double *__restrict__ pagt,
+                                 double *__restrict__ paccr, double *__restrict__ pacct, double *__restrict__ dragr,
+                                 double *__restrict__ dragt, double omega_frame, int back_reaction)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  const double Omega = 1.0 / g.r.OmegaInv[i];
+  const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+  if (i >= 1) {
+    const int lim = l - ns;
+    const int ljp = (j == ns - 1) ? i * ns : l + 1;
+    double vt2 = pvt[l] + pvt[ljp] + pvt[lim] + pvt[ljp - ns];
+    vt2 = vt2 / 4.0 + g.r.Rinf[i] * omega_frame;
+    vt2 = vt2 * vt2;
+    paccr[l] = vt2 * g.r.InvRinf[i] + 0.5 * (pagr[l] + pagr[lim]);
+    if (back_reaction) {
+      const double drag = Omega * (pvr[l] - vr[l]) / tau[l];
+      dragr[l] = 0.5 * (pd[l] + pd[lim]) * drag;
+    }
+  }
+  pacct[l] = 0.5 * (pagt[l] + pagt[ljm]);
+  if (back_reaction) {
+    const double drag = Omega * (pvt[l] - vt[l]) / tau[l];
+    dragt[l] = 0.5 * (pd[l] + pd[ljm]) * drag;
+  }
+}
+
+void aux_pebble_sources(const DevGrid &g, const double *pd, const double *pvr, const double *pvt, const double *tau,
+                        const double *vr, const double *vt, const double *pagr, const double *pagt, double *paccr,
+                        double *pacct, double *dragr, double *dragt, double omega_frame, int back_reaction,
+                        cudaStream_t s)
+{
+  k_pebble_sources<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, pd, pvr, pvt, tau, vr, vt, pagr, pagt, paccr, pacct, dragr,
+                                                         dragt, omega_frame, back_reaction);
+}
+
+// SubStep1Pebbles (Pebbles.c:617-652) followed by ParticleDiffusion
+// (Pebbles.c:656-698): both only change the pebble velocities of cell l.
+__global__ void k_pebble_substep1(DevGrid g, double *__restrict__ pvr, double *__restrict__ pvt,
+                                  const double *__restrict__ tau, const double *__restrict__ vr,
+                                  const double *__restrict__ vt, const double *__restrict__ paccr,
+                                  const double *__restrict__ pacct, const double *__restrict__ gaccr,
+                                  const double *__restrict__ gacct, const double *__restrict__ rho,
+                                  const double *__restrict__ pd, double dt, int diffusion, double schmidt,
+                                  const double *__restrict__ invdxtheta_r)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  const double Omega = 1.0 / g.r.OmegaInv[i];
+  const double t = tau[l];
+  const double efac = exp(-dt * Omega / t);
+  double a = pvr[l], b = pvt[l];
+  if (i > 0) a = a * efac + gaccr[l] * dt + (vr[l] + (paccr[l] - gaccr[l]) * t / Omega) * (1.0 - efac);
+  b = b * efac + gacct[l] * dt + (vt[l] + (pacct[l] - gacct[l]) * t / Omega) * (1.0 - efac);
+  if (diffusion) {
+    if (i >= 1) {
+      const int lim = l - ns;
+      double corr = -g.r.nu_inf[i] / schmidt;
+      corr *= (rho[l] + rho[lim]) / (pd[l] + pd[lim]);
+      corr *= (pd[l] / rho[l] - pd[lim] / rho[lim]) * g.r.InvDiffRmed[i];
+      a += corr;
+    }
+    const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+    double corr = -g.r.nu_med[i] / schmidt;
+    corr *= (rho[l] + rho[ljm]) / (pd[l] + pd[ljm]);
+    corr *= (pd[l] / rho[l] - pd[ljm] / rho[ljm]) * invdxtheta_r[i];
+    b += corr;
+  }
+  pvr[l] = a;
+  pvt[l] = b;
+}
+
+void aux_pebble_substep1(const DevGrid &g, double *pvr, double *pvt, const double *tau, const double *vr, const double *vt,
+                         const double *paccr, const double *pacct, const double *gaccr, const double *gacct,
+                         const double *rho, const double *pd, double dt, int diffusion, double schmidt,
+                         const double *invdxtheta_r, cudaStream_t s)
+{
+  k_pebble_substep1<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, pvr, pvt, tau, vr, vt, paccr, pacct, gaccr, gacct, rho, pd,
+                                                          dt, diffusion, schmidt, invdxtheta_r);
+}
+
+// ---------------------------------------------------------------------------
+// FillForcesArrays (Pframeforce.c:43-510).  Per ring: the azimuthal mean
+// sound speed and Stokes number (sums in order) and the 10-node vertical
+// averages of the star's pull for the ring-mean scale height.
+
+__global__ void k_force_rings(DevGrid g, const double *__restrict__ cs, const double *__restrict__ tau, ForceRings fr,
+                              int pebbles, double pebble_alpha)
+{
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= g.nr) return;
+  const int i = w;
+  const double csum = warp_seq_sum(cs + (size_t)i * g.ns, g.ns);
+  double tsum = 0.0;
+  if (pebbles) tsum = warp_seq_sum(tau + (size_t)i * g.ns, g.ns);
+  if ((threadIdx.x & 31) != 0) return;
+  const double cs_avr = csum / (double)g.ns;
+  const double H_avr = cs_avr * g.r.OmegaInv[i] * g.k.sqrt_adiabind_inv;
+  double tau_avr = 0.0, p_H_avr = 0.0, p_int = 0.0;
+  if (pebbles) {
+    tau_avr = tsum / (double)g.ns;
+    p_H_avr = H_avr * sqrt(pebble_alpha / tau_avr);
+  }
+  const double r2 = g.r.Rmed2[i];
+  const double H2 = H_avr * H_avr, zmax = 3.0 * H_avr, deltaz = zmax / 10.0;
+  double sig = 0.0, ist = 0.0;
+  for (int m = 1; m <= 10; m++) {
+    const double znode = ((double)m - 0.5) * deltaz;
+    double znode2 = znode * znode;
+    const double sum = exp(-(0.5 * znode2 / H2));
+    sig += sum;
+    double d2 = r2 + znode2, d = sqrt(d2), denom = d * d2;
+    ist += sum / denom;
+    if (pebbles) {
+      znode2 *= pebble_alpha / tau_avr;
+      d2 = r2 + znode2; d = sqrt(d2); denom = d * d2;
+      p_int += sum / denom;
+    }
+  }
+  fr.H_avr[i] = H_avr;
+  fr.sigma_avr[i] = sig;
+  fr.integstar_avr[i] = ist;
+  fr.p_H_avr[i] = p_H_avr;
+  fr.p_integstar_avr[i] = p_int;
+}
+
+
+
+
+__global__ void k_forces(DevGrid g, ForceArgs a, ForceRings fr)
+{
+  const int ns = g.ns;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  const int npl = a.npl, peb = a.pebbles;
+  double acc[2 + 2 * MAXPL_DEV];
+  for (int q = 0; q < 2 + 2 * npl; q++) acc[q] = 0.0;
+  if (j < ns) {
+    const int l = j + i * ns;
+    const double omegainv = g.r.OmegaInv[i], r2 = g.r.Rmed2[i];
+    double Rsup_Rinf2 = g.r.Rsup[i] - g.r.Rinf[i];
+    Rsup_Rinf2 *= Rsup_Rinf2;
+    const double x = g.r.Rmed[i] * g.r.costab[j];
+    const double y = g.r.Rmed[i] * g.r.sintab[j];
+    const double mcell = a.rho[l] * g.r.Surf[i];
+    const double H = a.cs[l] * omegainv * g.k.sqrt_adiabind_inv;
+    const double H2 = H * H;
+    const double H_avr = fr.H_avr[i];
+    int local = (fabs(H - H_avr) / H_avr > 0.05) ? 1 : 0;
+    double Hcorr = 0.0, pH = 0.0, pmcell = 0.0;
+    if (peb) {
+      pmcell = a.pdens[l] * g.r.Surf[i];
+      Hcorr = sqrt(a.pebble_alpha / a.tau[l]);
+      pH = H * Hcorr;
+      const double p_H_avr = fr.p_H_avr[i];
+      if (fabs(pH - p_H_avr) / p_H_avr > 0.05) local = 1;
+    }
+    double s2[MAXPL_DEV], integpl[MAXPL_DEV], p_integpl[MAXPL_DEV], hillcut[MAXPL_DEV];
+    int with[MAXPL_DEV];
+    int Nvert = 10;
+    for (int k = 0; k < npl; k++) {
+      const DevPlanet P = a.pl[k];
+      s2[k] = (x - P.x) * (x - P.x) + (y - P.y) * (y - P.y);
+      double c1 = 10.0 * P.Hpl; c1 *= c1;
+      double c2 = 5.0 * P.rhill; c2 *= c2;
+      hillcut[k] = 1.0;
+      integpl[k] = 0.0;
+      p_integpl[k] = 0.0;
+      if (a.mass_taper == 1.0 && (s2[k] < c1 || s2[k] < c2)) {
+        local = 1;
+        with[k] = 1;
+        if (a.exclude_hill) {
+          const double d2 = s2[k] + P.z * P.z;
+          hillcut[k] = 1.0 / (exp(-(sqrt(d2) / P.rhill - a.hillcut) / a.hillcut * 10.0) + 1.0);
+        }
+      } else {
+        with[k] = 0;
+      }
+      if (s2[k] < P.rmorevert2) Nvert = 30;
+    }
+    double sigma, integstar, p_integstar = 0.0;
+    if (local) {
+      const double zmax = 3.0 * H, deltaz = zmax / (double)Nvert;
+      sigma = 0.0;
+      integstar = 0.0;
+      for (int m = 1; m <= Nvert; m++) {
+        const double znode = ((double)m - 0.5) * deltaz, znode2 = znode * znode;
+        const double sum = exp(-(0.5 * znode2 / H2));
+        sigma += sum;
+        double d2 = r2 + znode2, d = sqrt(d2), denom = d * d2;
+        integstar += sum / denom;
+        if (peb) {
+          d2 = r2 + znode2 * Hcorr * Hcorr; d = sqrt(d2); denom = d * d2;
+          p_integstar += sum / denom;
+        }
+        for (int k = 0; k < npl; k++) {
+          if (!with[k]) continue;
+          const DevPlanet P = a.pl[k];
+          const double mx = (P.rsm2 > Rsup_Rinf2) ? P.rsm2 : Rsup_Rinf2;
+          double taper, dd;
+          d2 = s2[k] + (znode - P.z) * (znode - P.z);
+          if (d2 < P.rst2) { dd = sqrt(d2); taper = -3.0 * d2 * d2 / P.rst4 + 4.0 * dd * d2 / P.rst3; } else taper = 1.0;
+          d2 += mx; dd = sqrt(d2); denom = dd * d2;
+          integpl[k] += sum / denom * taper;
+          if (P.z < -0.05 * H || P.z > 0.05 * H) {
+            d2 = s2[k] + (-znode - P.z) * (-znode - P.z);
+            if (d2 < P.rst2) { dd = sqrt(d2); taper = -3.0 * d2 * d2 / P.rst4 + 4.0 * dd * d2 / P.rst3; } else taper = 1.0;
+            d2 += mx; dd = sqrt(d2); denom = dd * d2;
+            integpl[k] += sum / denom * taper;
+          }
+          if (peb) {
+            d2 = s2[k] + (znode * Hcorr - P.z) * (znode * Hcorr - P.z);
+            if (d2 < P.rst2) { dd = sqrt(d2); taper = -3.0 * d2 * d2 / P.rst4 + 4.0 * dd * d2 / P.rst3; } else taper = 1.0;
+            d2 += mx; dd = sqrt(d2); denom = dd * d2;
+            p_integpl[k] += sum / denom * taper;
+            if (P.z < -0.05 * pH || P.z > 0.05 * pH) {
+              d2 = s2[k] + (-znode * Hcorr - P.z) * (-znode * Hcorr - P.z);
+              if (d2 < P.rst2) { dd = sqrt(d2); taper = -3.0 * d2 * d2 / P.rst4 + 4.0 * dd * d2 / P.rst3; } else taper = 1.0;
+              d2 += mx; dd = sqrt(d2); denom = dd * d2;
+              p_integpl[k] += sum / denom * taper;
+            }
+          }
+        }
+      }
+    } else {
+      sigma = fr.sigma_avr[i];
+      integstar = fr.integstar_avr[i];
+      if (peb) p_integstar = fr.p_integstar_avr[i];
+    }
+    double tmp = integstar / sigma;
+    double agr = -g.r.Rmed[i] * tmp;            // 0.0 + ar
+    acc[0] = mcell * tmp * x;
+    acc[1] = mcell * tmp * y;
+    double pagr = 0.0;
+    if (peb) { const double pt = p_integstar / sigma; pagr = -g.r.Rmed[i] * pt; }
+    double ax = 0.0, ay = 0.0, pax = 0.0, pay = 0.0;
+    for (int k = 0; k < npl; k++) {
+      const DevPlanet P = a.pl[k];
+      double mpl = P.m;
+      if (with[k]) {
+        const bool off = (P.z < -0.05 * H || P.z > 0.05 * H);
+        tmp = off ? (x - P.x) * integpl[k] / (2.0 * sigma) : (x - P.x) * integpl[k] / sigma;
+        ax += -mpl * tmp;
+        if (a.exclude_hill) tmp *= hillcut[k];
+        acc[2 + 2 * k] += mcell * tmp;
+        tmp = off ? (y - P.y) * integpl[k] / (2.0 * sigma) : (y - P.y) * integpl[k] / sigma;
+        ay += -mpl * tmp;
+        if (a.exclude_hill) tmp *= hillcut[k];
+        acc[3 + 2 * k] += mcell * tmp;
+        if (peb) {
+          const bool poff = (P.z < -0.05 * pH || P.z > 0.05 * pH);
+          tmp = poff ? (x - P.x) * p_integpl[k] / (2.0 * sigma) : (x - P.x) * p_integpl[k] / sigma;
+          pax += -mpl * tmp;
+          if (a.pebble_gravity) { if (a.exclude_hill) tmp *= hillcut[k]; acc[2 + 2 * k] += pmcell * tmp; }
+          tmp = poff ? (y - P.y) * p_integpl[k] / (2.0 * sigma) : (y - P.y) * p_integpl[k] / sigma;
+          pay += -mpl * tmp;
+          if (a.pebble_gravity) { if (a.exclude_hill) tmp *= hillcut[k]; acc[3 + 2 * k] += pmcell * tmp; }
+        }
+      } else {
+        mpl *= a.mass_taper;
+        double d2 = s2[k] + P.z * P.z + P.smoothing2, d = sqrt(d2), denom = d * d2;
+        tmp = (x - P.x) / denom;
+        ax += -mpl * tmp;
+        if (a.exclude_hill) tmp *= hillcut[k];
+        acc[2 + 2 * k] += mcell * tmp;
+        tmp = (y - P.y) / denom;
+        ay += -mpl * tmp;
+        if (a.exclude_hill) tmp *= hillcut[k];
+        acc[3 + 2 * k] += mcell * tmp;
+        if (peb) {
+          d2 += -P.smoothing2 + P.smoothing2 * Hcorr * Hcorr;
+          d = sqrt(d2); denom = d * d2;
+          tmp = (x - P.x) / denom;
+          pax += -mpl * tmp;
+          if (a.pebble_gravity) { if (a.exclude_hill) tmp *= hillcut[k]; acc[2 + 2 * k] += pmcell * tmp; }
+          tmp = (y - P.y) / denom;
+          pay += -mpl * tmp;
+          if (a.pebble_gravity) { if (a.exclude_hill) tmp *= hillcut[k]; acc[3 + 2 * k] += pmcell * tmp; }
+        }
+      }
+    }
+    const double ir = g.r.InvRmed[i];
+    a.agr[l] = agr + (x * ax + y * ay) * ir;
+    a.agt[l] = 0.0 + (x * ay - y * ax) * ir;
+    if (peb) {
+      a.pagr[l] = pagr + (x * pax + y * pay) * ir;
+      a.pagt[l] = 0.0 + (x * pay - y * pax) * ir;
+    }
+  }
+  const int nq = 2 + 2 * npl;
+  const int b = blockIdx.x + blockIdx.y * gridDim.x;
+  for (int q = 0; q < nq; q++) {
+    const double v = block_reduce(acc[q], OpAdd(), 0.0);
+    if (threadIdx.x == 0) a.part[(size_t)b * nq + q] = v;
+  }
+}
+
+__global__ void k_forces_final(const double *__restrict__ part, int nb, int nq, double *__restrict__ scal)
+{
+  // one block; quantity q summed over blocks in a fixed order
+  for (int q = 0; q < nq; q++) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += part[(size_t)b * nq + q];
+    s = block_reduce(s, OpAdd(), 0.0);
+    if (threadIdx.x == 0) {
+      if (q == 0) scal[SC_INDX] = -s;
+      else if (q == 1) scal[SC_INDY] = -s;
+      else scal[SC_PLANET_A + (q - 2)] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// Indirect term added to every cell (Pframeforce.c:488-509).
+__global__ void k_forces_indirect(DevGrid g, double *__restrict__ agr, double *__restrict__ agt,
+                                  double *__restrict__ pagr, double *__restrict__ pagt, const double *__restrict__ scal,
+                                  double indx_pl, double indy_pl, int pebbles)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  const double axi = scal[SC_INDX] + indx_pl, ayi = scal[SC_INDY] + indy_pl;
+  const double x = g.r.Rmed[i] * g.r.costab[j], y = g.r.Rmed[i] * g.r.sintab[j];
+  const double ar = (x * axi + y * ayi) * g.r.InvRmed[i];
+  const double at = (x * ayi - y * axi) * g.r.InvRmed[i];
+  agr[l] += ar;
+  agt[l] += at;
+  if (pebbles) { pagr[l] += ar; pagt[l] += at; }
+}
+
+void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr, double indx_pl, double indy_pl,
+                double *scal, cudaStream_t s)
+{
+  const int threads = 256, warps = threads / 32;
+  k_force_rings<<<(g.nr + warps - 1) / warps, threads, 0, s>>>(g, a0.cs, a0.tau, fr, a0.pebbles, a0.pebble_alpha);
+  dim3 grid = grid2d(g.ns, g.nr, 128);
+  k_forces<<<grid, 128, 0, s>>>(g, a0, fr);
+  k_forces_final<<<1, 1024, 0, s>>>(a0.part, grid.x * grid.y, 2 + 2 * a0.npl, scal);
+  k_forces_indirect<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, a0.agr, a0.agt, a0.pagr, a0.pagt, scal, indx_pl, indy_pl,
+                                                          a0.pebbles);
+}
+
+// ---------------------------------------------------------------------------
+// AccretePebblesOntoPlanets for one planet (Pebbles.c:353-539), one block.
+// The annulus [imin, imax] holding the Hill sphere is searched; cells within
+// the effective accretion radius give up pebbles up to the model rate.
+
+__device__ double trapzd_col(int n, double a, double b, double H2, double *state)
+{
+  if (n == 1) {
+    *state = 0.5 * (b - a) * (exp(-0.5 * a * a / H2) + exp(-0.5 * b * b / H2));
+    return *state;
+  }
+  int it = 1;
+  for (int j = 1; j < n - 1; j++) it <<= 1;
+  const double iter = it, spacing = (b - a) / iter;
+  double x = a + 0.5 * spacing, sum = 0.0;
+  for (int j = 1; j <= it; j++) { sum += exp(-0.5 * x * x / H2); x += spacing; }
+  *state = 0.5 * (*state + (b - a) * sum / iter);
+  return *state;
+}
+
+__device__ double column_mass(double a, double b, double Hpeb)
+{
+  double integral = 0.0, iold = 0.0, st = 0.0;
+  const double H2 = Hpeb * Hpeb;
+  for (int n = 1; n <= 16; n++) {
+    integral = trapzd_col(n, a, b, H2, &st);
+    if (n > 5)
+      if (fabs(integral - iold) < 1.0e-4 * fabs(iold) || (integral == 0.0 && iold == 0.0)) return integral;
+    iold = integral;
+  }
+  return __longlong_as_double(0x7ff8000000000000ULL);   // the reference aborts here
+}
+
+__global__ void k_accrete(DevGrid g, AccArgs a, double *__restrict__ scal)
+{
+  const int ns = g.ns;
+  __shared__ double sh[8];
+  // vt1D at the two rings bracketing the planet (mpi_make1Dprofile of v_theta)
+  if (threadIdx.x < 32) {
+    const double s0 = warp_seq_sum(a.vt + (size_t)a.iflow * ns, ns);
+    double s1 = 0.0;                         // vt1D[nrad] is zero in the reference
+    if (a.iflow + 1 < g.nr) s1 = warp_seq_sum(a.vt + (size_t)(a.iflow + 1) * ns, ns);
+    if (threadIdx.x == 0) { sh[0] = s0 / (double)ns; sh[1] = s1 / (double)ns; }
+  }
+  // STEP 1: mean tau over the annulus
+  double ts = 0.0;
+  const int ncells = (a.imax - a.imin + 1) * ns;
+  for (int q = threadIdx.x; q < ncells; q += blockDim.x) ts += a.tau[(size_t)a.imin * ns + q];
+  ts = block_reduce(ts, OpAdd(), 0.0);
+  if (threadIdx.x == 0) {
+    const double tau_mean = ts / (double)ncells;
+    const double flow = sh[0] * (1.0 - a.frac) + sh[1] * a.frac + a.Rp * a.omega_frame;
+    const double flowx = -flow * a.Yp / a.Rp, flowy = flow * a.Xp / a.Rp;
+    const double vrel = sqrt((a.VXp - flowx) * (a.VXp - flowx) + (a.VYp - flowy) * (a.VYp - flowy) + a.VZp * a.VZp);
+    const double Mt = sqrt(1.0 / 3.0) * cube_rn(vrel) / a.Omegap;
+    double Reff;
+    if (a.Mp < Mt) {
+      const double Rbondi = a.Mp / vrel / vrel, tbondi = Rbondi / vrel;
+      Reff = Rbondi * sqrt(tau_mean * a.Rp15 / tbondi);
+    } else {
+      Reff = a.Rhill * pow(tau_mean / 0.1, 1.0 / 3.0);
+    }
+    if (Reff > a.Rhill) Reff = a.Rhill;
+    sh[2] = Reff;
+    sh[3] = vrel;
+    sh[4] = Mt;
+  }
+  __syncthreads();
+  const double Reff = sh[2], Reff2 = Reff * Reff;
+  // STEP 3: upper limit per cell within Reff
+  double dmu = 0.0, hpm = 0.0, pdm = 0.0;
+  int nc = 0;
+  for (int q = threadIdx.x; q < ncells; q += blockDim.x) {
+    const int i = a.imin + q / ns, j = q % ns, l = j + i * ns;
+    const double xc = g.r.Rmed[i] * g.r.costab[j], yc = g.r.Rmed[i] * g.r.sintab[j];
+    const double R2 = (xc - a.Xp) * (xc - a.Xp) + (yc - a.Yp) * (yc - a.Yp);
+    if (R2 <= Reff2) {
+      const double H = a.cs[l] * g.r.OmegaInv[i] * g.k.sqrt_adiabind_inv;
+      const double Hpeb = H * sqrt(a.pebble_alpha / a.tau[l]);
+      const double zmin = a.Zp - sqrt(Reff2 - R2), zmax = a.Zp + sqrt(Reff2 - R2);
+      const double mcell = g.r.Surf[i] * a.pdens[l];
+      const double vdp = a.pdens[l] / Hpeb * g.k.sqrt2pi_inv;
+      double dM = vdp * g.r.Surf[i] * column_mass(zmin, zmax, Hpeb);
+      if (dM > mcell) dM = 0.99999999 * mcell;
+      a.macc[l] = dM;
+      dmu += dM; hpm += Hpeb; pdm += a.pdens[l]; nc++;
+    }
+  }
+  dmu = block_reduce(dmu, OpAdd(), 0.0);
+  hpm = block_reduce(hpm, OpAdd(), 0.0);
+  pdm = block_reduce(pdm, OpAdd(), 0.0);
+  nc = block_reduce(nc, OpAddI(), 0);
+  if (threadIdx.x == 0) {
+    double Hpeb_mean = hpm, pdens_mean = pdm;
+    if (nc > 0) { Hpeb_mean /= (double)nc; pdens_mean /= (double)nc; }
+    const double vrel = sh[3], Mt = sh[4];
+    const double veloc = (a.Mp < Mt) ? vrel : Reff * a.Omegap;
+    double dM_model;
+    if (Hpeb_mean < Reff) dM_model = 2.0 * Reff * veloc * pdens_mean;
+    else dM_model = TH_PI * Reff * Reff * veloc * pdens_mean / Hpeb_mean * g.k.sqrt2pi_inv;
+    dM_model *= a.dt;
+    sh[5] = (dmu > dM_model) ? dM_model / dmu : 1.0;
+  }
+  __syncthreads();
+  const double limiter = sh[5];
+  double dM_s = 0.0, dPx = 0.0, dPy = 0.0;
+  for (int q = threadIdx.x; q < ncells; q += blockDim.x) {
+    const int i = a.imin + q / ns, j = q % ns, l = j + i * ns;
+    if (a.macc[l] > 0.0) {
+      const double xc = g.r.Rmed[i] * g.r.costab[j], yc = g.r.Rmed[i] * g.r.sintab[j];
+      const double vtcorr = g.r.Rmed[i] * a.omega_frame;
+      const double vrc = a.pvr[l], vtc = a.pvt[l] + vtcorr;
+      const double vxc = (vrc * xc - vtc * yc) * g.r.InvRmed[i], vyc = (vrc * yc + vtc * xc) * g.r.InvRmed[i];
+      const double dM = a.macc[l] * limiter;
+      a.macc[l] = 0.0;
+      const double mcell = g.r.Surf[i] * a.pdens[l];
+      double pd = (mcell - dM) / g.r.Surf[i];
+      if (pd < 0.0) pd = 1.e-20;
+      a.pdens[l] = pd;
+      dM_s += dM; dPx += dM * vxc; dPy += dM * vyc;
+    }
+  }
+  dM_s = block_reduce(dM_s, OpAdd(), 0.0);
+  dPx = block_reduce(dPx, OpAdd(), 0.0);
+  dPy = block_reduce(dPy, OpAdd(), 0.0);
+  if (threadIdx.x == 0) { scal[SC_ACC_DM] = dM_s; scal[SC_ACC_DPX] = dPx; scal[SC_ACC_DPY] = dPy; }
+}
+
+void aux_accrete(const DevGrid &g, const AccArgs &a, double *scal, cudaStream_t s)
+{
+  k_accrete<<<1, 1024, 0, s>>>(g, a, scal);
+}
+
+// ---------------------------------------------------------------------------
+// Conservation integrals (GasTotalMass, GasMomentum, GasTotalEnergy,
+// SideEuler.c:26-80,523-565) and the same mass/momentum sums for pebbles.
+__global__ void k_integrals(DevGrid g, const double *__restrict__ rho, const double *__restrict__ vr,
+                            const double *__restrict__ vt, const double *__restrict__ e, const double *__restrict__ pd,
+                            const double *__restrict__ pvt, double omega_frame, int pebbles, double *__restrict__ part)
+{
+  const int ns = g.ns;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  double m = 0, am = 0, en = 0, pm = 0, pam = 0;
+  if (j < ns) {
+    const int l = j + i * ns;
+    const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+    const int ljp = (j == ns - 1) ? i * ns : l + 1;
+    const double S = g.r.Surf[i], rm = g.r.Rmed[i];
+    m = S * rho[l];
+    am = S * (rho[l] + rho[ljm]) * rm * (vt[l] + omega_frame * rm);
+    double vrc = (rm - g.r.Rinf[i]) * vr[l + ns] + (g.r.Rsup[i] - rm) * vr[l];
+    vrc /= (g.r.Rsup[i] - g.r.Rinf[i]);
+    const double vtc = 0.5 * (vt[l] + vt[ljp]) + rm * omega_frame;
+    en = 0.5 * S * rho[l] * (vrc * vrc + vtc * vtc) + S * e[l];
+    if (pebbles) {
+      pm = S * pd[l];
+      pam = S * (pd[l] + pd[ljm]) * rm * (pvt[l] + omega_frame * rm);
+    }
+  }
+  m = block_reduce(m, OpAdd(), 0.0);
+  am = block_reduce(am, OpAdd(), 0.0);
+  en = block_reduce(en, OpAdd(), 0.0);
+  pm = block_reduce(pm, OpAdd(), 0.0);
+  pam = block_reduce(pam, OpAdd(), 0.0);
+  if (threadIdx.x == 0) {
+    const int b = blockIdx.x + blockIdx.y * gridDim.x;
+    part[5 * b + 0] = m; part[5 * b + 1] = am; part[5 * b + 2] = en; part[5 * b + 3] = pm; part[5 * b + 4] = pam;
+  }
+}
+
+__global__ void k_integrals_final(const double *__restrict__ part, int nb, double *__restrict__ scal)
+{
+  for (int q = 0; q < 5; q++) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += part[5 * b + q];
+    s = block_reduce(s, OpAdd(), 0.0);
+    if (threadIdx.x == 0) {
+      if (q == 1 || q == 4) s *= 0.5;
+      scal[SC_MASS + q] = s;
+    }
+    __syncthreads();
+  }
+}
+
+void aux_integrals(const DevGrid &g, const double *rho, const double *vr, const double *vt, const double *e,
+                   const double *pd, const double *pvt, double omega_frame, int pebbles, double *part, double *scal,
+                   cudaStream_t s)
+{
+  dim3 grid = grid2d(g.ns, g.nr, 256);
+  k_integrals<<<grid, 256, 0, s>>>(g, rho, vr, vt, e, pd, pvt, omega_frame, pebbles, part);
+  k_integrals_final<<<1, 1024, 0, s>>>(part, grid.x * grid.y, scal);
+}
+
+// Final minimum of block partials (DiffusionTimestep's MPI_MIN).
+__global__ void k_min_final(const double *__restrict__ part, int nb, double *__restrict__ out)
+{
+  double m = 1.0e38;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) m = (part[b] < m) ? part[b] : m;
+  m = block_reduce(m, OpMin(), 1.0e38);
+  if (threadIdx.x == 0) *out = m;
+}
+
+void aux_min_final(const double *part, int nb, double *out, cudaStream_t s)
+{
+  k_min_final<<<1, 1024, 0, s>>>(part, nb, out);
+}

@@ -1,0 +1,1005 @@
+// kernels_hydro.cu -- source terms, viscosity, energy equation, SOR and
+// transport of the AlgoGas substep (src_main/SourceEuler.c:319-586,
+// Viscosity.c:85-260, EnergySources.c:75-856, TransportEuler.c:34-505).
+//
+// Each kernel keeps the reference's per-cell operation order (products and
+// sums associate left to right exactly as written in the C source) so that,
+// compiled without FMA contraction, results match the reference bit for bit
+// wherever no transcendental function is involved.
+#include "thorin_kernels.cuh"
+
+#define CELL_LOOP_2D                                                        \
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;                      \
+  const int i = blockIdx.y;                                                 \
+  if (j >= ns) return;                                                      \
+  const int l = j + i * ns;
+
+static inline dim3 grid2d(int ns, int rows, int bx) { return dim3((ns + bx - 1) / bx, rows); }
+static const int BX = 128;
+
+// ---------------------------------------------------------------------------
+// SubStep1 velocity predictor (SourceEuler.c:319-407), pressure from the
+// energy (ComputePressureField, SourceEuler.c:740-762).
+__global__ void k_substep1(DevGrid g, const double *__restrict__ rho, const double *__restrict__ vrad,
+                           const double *__restrict__ vtheta, const double *__restrict__ energy,
+                           const double *__restrict__ agr, const double *__restrict__ agt,
+                           const double *__restrict__ dragr, const double *__restrict__ dragt,
+                           double *__restrict__ vradint, double *__restrict__ vthetaint,
+                           double *__restrict__ gaccr, double *__restrict__ gacct,
+                           double dt, double omega_frame, double gm1, int pebbles, int back_reaction,
+                           const double *__restrict__ supp_torque, const double *__restrict__ invdxtheta_r)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+  const int ljp = (j == ns - 1) ? i * ns : l + 1;
+  const double pl = gm1 * energy[l];
+  if (i >= 1) {
+    const int lim = l - ns;
+    const double plim = gm1 * energy[lim];
+    double gradp = (pl - plim) * 2.0 / (rho[l] + rho[lim]) * g.r.InvDiffRmed[i];
+    double vt2 = vtheta[l] + vtheta[ljp] + vtheta[lim] + vtheta[ljp - ns];
+    vt2 = vt2 / 4.0 + g.r.Rinf[i] * omega_frame;
+    vt2 = vt2 * vt2;
+    double tmp = -gradp + 0.5 * (agr[l] + agr[lim]) + vt2 * g.r.InvRinf[i];
+    double v = vrad[l] + dt * tmp;
+    if (pebbles) {
+      double acc = tmp;
+      if (back_reaction) {
+        tmp = dragr[l] * 2.0 / (rho[l] + rho[lim]);
+        v += dt * tmp;
+        acc += tmp;
+      }
+      gaccr[l] = acc;
+    }
+    vradint[l] = v;
+  }
+  {
+    const double invdxtheta = invdxtheta_r[i];
+    const double pljm = gm1 * energy[ljm];
+    double gradp = (pl - pljm) * 2.0 / (rho[l] + rho[ljm]) * invdxtheta;
+    double tmp = -gradp + 0.5 * (agt[l] + agt[ljm]);
+    double v = vtheta[l] + dt * tmp;
+    v += dt * supp_torque[i];
+    if (pebbles) {
+      double acc = tmp + supp_torque[i];
+      if (back_reaction) {
+        tmp = dragt[l] * 2.0 / (rho[l] + rho[ljm]);
+        v += dt * tmp;
+        acc += tmp;
+      }
+      gacct[l] = acc;
+    }
+    vthetaint[l] = v;
+  }
+}
+
+// UpdateDivVelocAndStressTensor (Viscosity.c:85-162): divergence and the
+// three stress components at cell l from the staggered velocities.
+struct Stress { double divv, trr, tpp, trp; };
+
+__device__ __forceinline__ Stress stress_at(const DevGrid &g, const double *vr, const double *vt, const double *rho,
+                                            int i, int j, double invdphi)
+{
+  const int ns = g.ns, l = j + i * ns, lip = l + ns;
+  const int ljp = (j == ns - 1) ? i * ns : l + 1;
+  const double onethird = 1.0 / 3.0;
+  Stress s;
+  double Drr = (vr[lip] - vr[l]) * g.r.InvDiffRsup[i];
+  double Dpp = (vt[ljp] - vt[l]) * invdphi * g.r.InvRmed[i] + 0.5 * (vr[lip] + vr[l]) * g.r.InvRmed[i];
+  double dv = (vr[lip] * g.r.Rsup[i] - vr[l] * g.r.Rinf[i]) * g.r.InvDiffRsup[i] * g.r.InvRmed[i];
+  dv += (vt[ljp] - vt[l]) * invdphi * g.r.InvRmed[i];
+  s.divv = dv;
+  const double nu = g.r.nu_med[i];
+  s.trr = 2.0 * rho[l] * nu * (Drr - onethird * dv);
+  s.tpp = 2.0 * rho[l] * nu * (Dpp - onethird * dv);
+  if (i >= 1) {
+    const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1, lim = l - ns, ljmim = ljm - ns;
+    double Drp = 0.5 * (g.r.Rinf[i] * (vt[l] * g.r.InvRmed[i] - vt[lim] * g.r.InvRmed[i - 1]) * g.r.InvDiffRmed[i] +
+                        (vr[l] - vr[ljm]) * invdphi * g.r.InvRinf[i]);
+    s.trp = 2.0 * 0.25 * (rho[l] + rho[lim] + rho[ljm] + rho[ljmim]) * g.r.nu_inf[i] * Drp;
+  } else {
+    s.trp = 0.0;
+  }
+  return s;
+}
+
+__global__ void k_stress(DevGrid g, const double *__restrict__ vr, const double *__restrict__ vt,
+                         const double *__restrict__ rho, double *__restrict__ divv, double *__restrict__ trr,
+                         double *__restrict__ tpp, double *__restrict__ trp, double invdphi)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  Stress s = stress_at(g, vr, vt, rho, i, j, invdphi);
+  divv[l] = s.divv;
+  trr[l] = s.trr;
+  tpp[l] = s.tpp;
+  trp[l] = s.trp;
+}
+
+// UpdateVelocityWithViscousTerms (Viscosity.c:165-218) and
+// ImposeKeplerianEdges (Viscosity.c:221-260).
+__global__ void k_visc_update(DevGrid g, double *__restrict__ vr, double *__restrict__ vt,
+                              const double *__restrict__ rho, const double *__restrict__ trr,
+                              const double *__restrict__ tpp, const double *__restrict__ trp, double dt,
+                              double invdphi, int kepler_edges, double vkep_in, double vkep_out)
+{
+  const int ns = g.ns, nr = g.nr;
+  CELL_LOOP_2D
+  const int ljp = (j == ns - 1) ? i * ns : l + 1;
+  const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+  if (i >= 1 && i < nr - 1) {
+    const int lip = l + ns;
+    vt[l] += dt * g.r.InvRmed[i] *
+             ((g.r.Rsup[i] * trp[lip] - g.r.Rinf[i] * trp[l]) * g.r.InvDiffRsup[i] + (tpp[l] - tpp[ljm]) * invdphi +
+              0.5 * (trp[l] + trp[lip])) /
+             (0.5 * (rho[l] + rho[ljm]));
+  }
+  if (i >= 1) {
+    const int lim = l - ns;
+    vr[l] += dt * g.r.InvRinf[i] *
+             ((g.r.Rmed[i] * trr[l] - g.r.Rmed[i - 1] * trr[lim]) * g.r.InvDiffRmed[i] + (trp[ljp] - trp[l]) * invdphi -
+              0.5 * (tpp[l] + tpp[lim])) /
+             (0.5 * (rho[l] + rho[lim]));
+  }
+  if (kepler_edges) {
+    if (i == 0) vt[l] = vkep_in;
+    if (i == nr - 1) vt[l] = vkep_out;
+  }
+}
+
+// SubStep2 (SourceEuler.c:417-504): von Neumann-Richtmyer artificial
+// viscosity, velocity and energy updates.  q_r, q_theta are recomputed at
+// the neighbouring cells instead of being stored.
+__device__ __forceinline__ double avisc(double dv, double rho)
+{
+  return (dv < 0.0) ? TH_CVNR * TH_CVNR * rho * dv * dv : 0.0;
+}
+
+__global__ void k_substep2(DevGrid g, const double *__restrict__ rho, const double *__restrict__ vr,
+                           const double *__restrict__ vt, const double *__restrict__ energy,
+                           double *__restrict__ vrnew, double *__restrict__ vtnew, double *__restrict__ eint,
+                           double dt, int energy_eq, const double *__restrict__ invdxtheta_r)
+{
+  const int ns = g.ns, nr = g.nr;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= ns) return;
+  const int l = j + i * ns;
+  if (i == nr) {                       // rows the reference never writes stay zero
+    vrnew[l] = 0.0;
+    vtnew[l] = 0.0;
+    return;
+  }
+  const int lip = l + ns;
+  const int ljp = (j == ns - 1) ? i * ns : l + 1;
+  const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+  const double qr = avisc(vr[lip] - vr[l], rho[l]);
+  const double qt = avisc(vt[ljp] - vt[l], rho[l]);
+  if (i >= 1) {
+    const int lim = l - ns;
+    const double qrm = avisc(vr[l] - vr[lim], rho[lim]);
+    vrnew[l] = vr[l] - dt * 2.0 / (rho[l] + rho[lim]) * (qr - qrm) * g.r.InvDiffRmed[i];
+  } else {
+    vrnew[l] = 0.0;
+  }
+  const double invdxtheta = invdxtheta_r[i];
+  const double qtm = avisc(vt[l] - vt[ljm], rho[ljm]);
+  vtnew[l] = vt[l] - dt * 2.0 / (rho[l] + rho[ljm]) * (qt - qtm) * invdxtheta;
+  if (energy_eq)
+    eint[l] = energy[l] - dt * qr * (vr[lip] - vr[l]) * g.r.InvDiffRsup[i] - dt * qt * (vt[ljp] - vt[l]) * invdxtheta;
+}
+
+// SubStep3 viscous heating (SourceEuler.c:541-554) from the stress of the
+// updated velocities (the second UpdateDivVelocAndStressTensor call,
+// SourceEuler.c:302).
+__global__ void k_qplus(DevGrid g, const double *__restrict__ vr, const double *__restrict__ vt,
+                        const double *__restrict__ rho, double *__restrict__ divv, double *__restrict__ qplus,
+                        double invdphi)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  Stress s = stress_at(g, vr, vt, rho, i, j, invdphi);
+  divv[l] = s.divv;
+  if (i >= 1) {
+    const double nu = g.r.nu_med[i];
+    double q;
+    if (nu != 0.0) {
+      q = 0.5 / nu / rho[l] * (s.trr * s.trr + 2.0 * s.trp * s.trp + s.tpp * s.tpp);
+      q += (2.0 / 9.0) * nu * rho[l] * s.divv * s.divv;
+    } else {
+      q = 0.0;
+    }
+    qplus[l] = q;
+  }
+}
+
+// Power-law extrapolation of Q+ into ring 0 (SourceEuler.c:556-567).
+__global__ void k_qplus_row0(DevGrid g, double *__restrict__ qplus, double lr01, double lr12)
+{
+  const int ns = g.ns;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ns) return;
+  double q1 = qplus[j + ns], q2 = qplus[j + 2 * ns];
+  qplus[j] = (g.r.nu_med[0] != 0.0) ? q1 * exp(log(q1 / q2) * lr01 / lr12) : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Energy equation (EnergySources.c)
+// ComputeTemperatureField + ComputeSoundSpeed (SourceEuler.c:715-792).
+__global__ void k_eos(DevGrid g, const double *__restrict__ rho, const double *__restrict__ energy,
+                      double *__restrict__ temper, double *__restrict__ cs, double gm1, double gg1)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  const double r = rho[l], e = energy[l];
+  double tmp2 = 1.0 / (r * 1.0);
+  double tmp1 = e * 1.0 * gm1;
+  temper[l] = tmp1 * tmp2;
+  cs[l] = sqrt(gg1 * fabs(e) / r);
+}
+
+// Opacity laws, Opacity.c.
+__device__ double opacity_BL94(double rho, double T)
+{
+  const double kappa[8] = {2.0e-4, 2.0e16, 0.1, 2.0e81, 1.0e-8, 1.0e-36, 1.5e20, 0.348};
+  const double a[8] = {0.0, 0.0, 0.0, 1.0, 2.0 / 3.0, 1.0 / 3.0, 1.0, 0.0};
+  const double b[8] = {2.0, -7.0, 0.5, -24.0, 3.0, 10.0, -2.5, 0.0};
+#define TEMPB(i, j) pow(kappa[j] / kappa[i] * pow(rho, a[j] - a[i]), 1.0 / (b[i] - b[j]))
+  double k;
+  if (T <= TEMPB(2, 3)) {
+    double k1 = kappa[0] * pow(T, b[0]);
+    double k2 = kappa[1] * pow(T, b[1]);
+    double k3 = kappa[2] * pow(T, b[2]);
+    double t1 = 1.0 / (k1 * k1) + 1.0 / (k2 * k2);
+    t1 = 1.0 / (t1 * t1);
+    double t2 = pow(k3 / (1.0 + 1.0e22 * pow(T, -10.0)), 4.0);
+    k = pow(t1 + t2, 0.25);
+  } else if ((T > TEMPB(2, 3)) && (T <= TEMPB(3, 4))) {
+    k = kappa[3] * pow(rho, a[3]) * pow(T, b[3]);
+  } else if ((T > TEMPB(3, 4)) && (T <= TEMPB(4, 5))) {
+    k = kappa[4] * pow(rho, a[4]) * pow(T, b[4]);
+  } else if ((T > TEMPB(4, 5)) && (T <= TEMPB(5, 6))) {
+    k = kappa[5] * pow(rho, a[5]) * pow(T, b[5]);
+  } else if ((T > TEMPB(5, 6)) && (T <= TEMPB(6, 7))) {
+    k = kappa[6] * pow(rho, a[6]) * pow(T, b[6]);
+  } else {
+    k = kappa[7];
+  }
+#undef TEMPB
+  return k;
+}
+
+__device__ double opacity_ZHU12(double rho, double T)
+{
+  double xlop, pre = 8.3144598 * 1.0e7 / 2.4 * rho * T;
+  double xlp = log10(pre), xlt = log10(T);
+  if (xlt < 2.23567 + 0.01899 * (xlp - 5.)) xlop = 1.5 * (xlt - 1.16331) - 0.736364;
+  else if (xlt < 2.30713 + 0.01899 * (xlp - 5.)) xlop = -3.53154212 * xlt + 8.767726 - (7.24786 - 8.767726) * (xlp - 5.) / 16.;
+  else if (xlt < (17.7 - 0.62 + 1.5 * 2.30713) / (1.5 + 5.832)) xlop = 1.5 * (xlt - 2.30713) + 0.62;
+  else if (xlt < (5.9398 + 17.7) / (5.832 + 2.129)) xlop = -5.832 * xlt + 17.7;
+  else if (xlt < (129.88071 + 5.9398 + (142.996475 - 129.88071) * 0.1 * (xlp + 4.)) / (2.129 + 42.98075)) xlop = 2.129 * xlt - 5.9398;
+  else if (xlt < (129.88071 + 15.0125 + (142.996475 - 129.88071) * 0.1 * (xlp + 4.)) / (4.0625 + 42.98075)) xlop = 129.88071 - 42.98075 * xlt + (142.996475 - 129.88071) * 0.1 * (xlp + 4.0);
+  else if (xlt < 3.28 + xlp / 4. * 0.12) xlop = -15.0125 + 4.0625 * xlt;
+  else if (xlt < 3.41 + 0.03328 * xlp / 4.) xlop = 58.9294 - 18.4808 * xlt + (61.6346 - 58.9294) * xlp / 4.;
+  else if (xlt < 3.76 + (xlp - 4) / 2. * 0.03) xlop = -12.002 + 2.90477 * xlt + (xlp - 4) / 4. * (13.9953 - 12.002);
+  else if (xlt < 4.07 + (xlp - 4) / 2. * 0.08) xlop = -39.4077 + 10.1935 * xlt + (xlp - 4) / 2. * (40.1719 - 39.4077);
+  else if (xlt < 5.3715 + (xlp - 6) / 2. * 0.5594) xlop = 17.5935 - 3.3647 * xlt + (xlp - 6) / 2. * (17.5935 - 15.7376);
+  else xlop = -0.48;
+  if (xlop < 3.586 * xlt - 16.85 && xlt < 4.) xlop = 3.586 * xlt - 16.85;
+  return pow(10., xlop);
+}
+
+__device__ double opacity_LP85(double rho, double T)
+{
+  if (T < pow(2.0e-4 / 2.0e16, -1.0 / 9.0)) return 2.0e-4 * T * T;
+  if (T < pow(2.0e16 / 5.0e-3, 1.0 / 8.0)) return 2.0e16 * pow(T, -7.0);
+  if (T < pow(5.0e-3 / 2.0e34, -1.0 / 10.0) * pow(rho, 1.0 / 15.0)) return 5.0e-3 * T;
+  if (T < pow(2.0e34 / 2.0e-8, 1.0 / 12.0)) return 2.0e34 * pow(rho, 2.0 / 3.0) * pow(T, -9.0);
+  if (T < pow(2.0e-8 / 1.0e-36, 1.0 / 7.0) * pow(rho, 1.0 / 21.0)) return 2.0e-8 * pow(rho, 2.0 / 3.0) * T * T * T;
+  if (T < pow(1.0e-36 / 1.5e20, -1.0 / 12.5) * pow(rho, 4.0 / 75.0)) return 1.0e-36 * pow(rho, 1.0 / 3.0) * pow(T, 10.0);
+  return 1.5e20 * rho * pow(T, -5.0 / 2.0);
+}
+
+__device__ __forceinline__ double opacity_law(int law, double rho, double T, double parametric)
+{
+  switch (law) {
+  case THORIN_OPA_ZHU12: return opacity_ZHU12(rho, T);
+  case THORIN_OPA_LP85: return opacity_LP85(rho, T);
+  case THORIN_OPA_CONST: return parametric;
+  default: return opacity_BL94(rho, T);
+  }
+}
+
+// |grad T| at a cell centre (TemperatureGradient, EnergySources.c:609-653).
+__device__ __forceinline__ double gradt_mag(const DevGrid &g, const double *T, int i, int j, const double *invdxtheta_r)
+{
+  const int ns = g.ns, l = j + i * ns, lip = l + ns, lim = l - ns;
+  const int ljp = (j == ns - 1) ? i * ns : l + 1;
+  const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+  const double invdx = invdxtheta_r[i];
+  double gr_l = (T[l] - T[lim]) * g.r.InvDiffRmed[i];
+  double gr_lip = (T[lip] - T[l]) * g.r.InvDiffRmed[i + 1];
+  double gt_l = (T[l] - T[ljm]) * invdx;
+  double gt_ljp = (T[ljp] - T[l]) * invdx;
+  double r = 0.5 * (gr_lip + gr_l);
+  double t = 0.5 * (gt_ljp + gt_l);
+  return sqrt(r * r + t * t);
+}
+
+__device__ __forceinline__ double flux_limiter(double s)
+{
+  if (s <= 2.0) return 2.0 / (3.0 + sqrt(9.0 + 10.0 * s * s));
+  return 10.0 / (10.0 * s + 9.0 + sqrt(81.0 + 180.0 * s));
+}
+
+// MidplaneVolumeDensity, OpacityProfile, CalculateQminus and the centred
+// diffusion coefficient of DiffusionCoefs (EnergySources.c:556-592,
+// 658-711, Opacity.c:231-266); block partial minima of DiffusionTimestep
+// (EnergySources.c:833-856).
+__global__ void k_diffcoef(DevGrid g, const double *__restrict__ rho, const double *__restrict__ T,
+                           const double *__restrict__ cs, double *__restrict__ opacity, double *__restrict__ qminus,
+                           double *__restrict__ dcen, double *__restrict__ dtmin_part, int law, double parametric_cu,
+                           double parametric_raw, double opacity_drop, double taueff_c, const double *__restrict__ invdxtheta_r,
+                           const double *__restrict__ deltar2_r)
+{
+  const int ns = g.ns, nr = g.nr;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  double dtl = 1.0e38;
+  if (j < ns) {
+    const int l = j + i * ns;
+    const double H = cs[l] * g.r.OmegaInv[i] * g.k.sqrt_adiabind_inv;
+    const double vd = rho[l] / H * g.k.sqrt2pi_inv;
+    const double Tl = T[l];
+    double kap;
+    if (parametric_raw > 0.0) kap = parametric_cu;
+    else kap = opacity_law(law, vd * g.k.rho2cgs, Tl * g.k.t2si, parametric_raw) * g.k.opa2cu;
+    opacity[l] = kap;
+    const double tau = opacity_drop * 0.5 * kap * rho[l];
+    const double taueff = 0.375 * tau + taueff_c + 0.25 / tau;
+    const double T3 = cube_rn(Tl);
+    qminus[l] = 2.0 * g.k.sigma_sb * T3 / taueff;
+    const int ig = (i == 0) ? 1 : (i == nr - 1 ? nr - 2 : i);
+    const double gradt = gradt_mag(g, T, ig, j, invdxtheta_r);
+    const double fac = 1.0 / (vd * kap);
+    const double s = 4.0 * gradt * fac / Tl;
+    const double D = flux_limiter(s) * 16.0 * g.k.sigma_sb * T3 * fac;
+    dcen[l] = D;
+    dtl = deltar2_r[i] / D;
+  }
+  const double m = block_reduce(dtl, OpMin(), 1.0e38);
+  if (threadIdx.x == 0) dtmin_part[blockIdx.x + blockIdx.y * gridDim.x] = m;
+}
+
+// Stellar irradiation: CalculateFlaring + CalculateQirr
+// (EnergySources.c:103-198).
+__global__ void k_irradiation(DevGrid g, const double *__restrict__ rho, const double *__restrict__ cs,
+                              const double *__restrict__ opacity, double *__restrict__ flaring, double *__restrict__ qirr,
+                              double rstar, double tirr4fac, double opacity_drop, double taueff_c,
+                              const double *__restrict__ rinf15, const double *__restrict__ rsup15)
+{
+  const int ns = g.ns, nr = g.nr;
+  CELL_LOOP_2D
+  const double sqi = g.k.sqrt_adiabind_inv;
+  // flaring at (i, j): interior rings use their own derivative, rings 0 and
+  // nr-1 adopt the derivative of rings 1 and nr-2.
+  int ic = (i == 0) ? 1 : (i == nr - 1 ? nr - 2 : i);
+  if (nr >= 3) {
+    const int lc = j + ic * ns;
+    const double csin = 0.5 * (cs[lc] + cs[lc - ns]);
+    const double csout = 0.5 * (cs[lc] + cs[lc + ns]);
+    const double Hin = csin * rinf15[ic] * sqi;
+    const double Hout = csout * rsup15[ic] * sqi;
+    const double dHdr = (Hout - Hin) * g.r.InvDiffRsup[ic];
+    const double H = cs[l] * g.r.OmegaInv[i] * sqi;
+    double f;
+    if (i == ic) f = atan(dHdr) - atan((H - 0.4 * rstar) * g.r.InvRmed[i]);
+    else f = atan(dHdr) - atan((H - 0.4 * rstar) / g.r.Rmed[i]);
+    f = (f >= 0.0) ? sin(f) : 0.0;
+    flaring[l] = f;
+    double q = 0.0;
+    if (f > 0.0) {
+      const double tau = opacity_drop * 0.5 * opacity[l] * rho[l];
+      const double taueff = 0.375 * tau + taueff_c + 0.25 / tau;
+      const double r2inv = 1.0 / g.r.Rmed2[i];
+      q = 2.0 * g.k.sigma_sb * (tirr4fac * r2inv * f) / taueff;
+    }
+    qirr[l] = q;
+  }
+}
+
+// Matrix of the linearised implicit energy equation
+// (ImplicitRadiativeDiffusion, EnergySources.c:256-297).
+__global__ void k_matrix(DevGrid g, const double *__restrict__ rho, const double *__restrict__ T,
+                         const double *__restrict__ cs, const double *__restrict__ dcen, const double *__restrict__ divv,
+                         const double *__restrict__ qminus, const double *__restrict__ qplus, const double *__restrict__ qirr,
+                         double *__restrict__ ml, double *__restrict__ mlip, double *__restrict__ mlim,
+                         double *__restrict__ mljp, double *__restrict__ mljm, double *__restrict__ rhs, double dt,
+                         double gm1, const double *__restrict__ invdxtheta2_r, int irradiation, int nheat,
+                         const int *__restrict__ heat_idx, const double *__restrict__ heat_val)
+{
+  const int ns = g.ns;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y + 1;                   // rings 1 .. nr-2
+  if (j >= ns) return;
+  const int l = j + i * ns, lip = l + ns, lim = l - ns;
+  const int ljp = (j == ns - 1) ? i * ns : l + 1;
+  const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+  const double sqi = g.k.sqrt_adiabind_inv;
+  const double oi = g.r.OmegaInv[i];
+  const double idx2 = invdxtheta2_r[i];
+  // A at faces i and i+1, B at faces j and j+1
+  const double Dr_l = 0.5 * (dcen[l] + dcen[lim]);
+  const double Dr_lip = 0.5 * (dcen[lip] + dcen[l]);
+  const double A_l = Dr_l * g.r.Rinf[i] * g.r.InvDiffRmed[i];
+  const double A_lip = Dr_lip * g.r.Rinf[i + 1] * g.r.InvDiffRmed[i + 1];
+  const double H = cs[l] * oi * sqi;
+  const double Dt_l = 0.5 * (dcen[l] + dcen[ljm]);
+  const double B_l = Dt_l * idx2 * 2.0 * H;
+  const double Hjp = cs[ljp] * oi * sqi;
+  const double Dt_ljp = 0.5 * (dcen[ljp] + dcen[l]);
+  const double B_ljp = Dt_ljp * idx2 * 2.0 * Hjp;
+  const double bfac = dt / (rho[l] * g.k.cv);
+  const double afac = bfac * g.r.InvDiffRsup[i] * 2.0 * H / g.r.Rmed[i];
+  const double Tl = T[l], qm = qminus[l];
+  ml[l] = 1.0 + divv[l] * gm1 * dt + 4.0 * bfac * qm + afac * (A_lip + A_l) + bfac * (B_ljp + B_l);
+  mlip[l] = -afac * A_lip;
+  mlim[l] = -afac * A_l;
+  mljp[l] = -bfac * B_ljp;
+  mljm[l] = -bfac * B_l;
+  double r = Tl + bfac * (qplus[l] + 3.0 * qm * Tl);
+  if (irradiation) r += bfac * qirr[l];
+  for (int k = 0; k < nheat; k++)
+    if (l == heat_idx[k]) r += bfac * heat_val[k];
+  rhs[l] = r;
+}
+
+// ---------------------------------------------------------------------------
+// Red-black SOR (SuccessiveOverrelaxation, EnergySources.c:406-511).
+// Rings 1 .. nr-2 are updated; pass 1 visits j = (i-1) mod 2, 1 + ..., pass 2
+// the other colour (jchess1st = 0, jchess2nd = 1 on one rank, :431-432).
+// Per-block partial L1 residual sums and "changed" counts go to scratch; the
+// last block of pass 2 (ticketed with an atomic counter, no waiting) sums
+// both passes in a fixed order and evaluates the three exit tests.
+
+__device__ __forceinline__ double sor_resid(const double *T, const double *ml, const double *mlip, const double *mlim,
+                                            const double *mljp, const double *mljm, const double *rhs, int l, int lip,
+                                            int lim, int ljp, int ljm)
+{
+  return T[l] * ml[l] + T[lip] * mlip[l] + T[lim] * mlim[l] + T[ljp] * mljp[l] + T[ljm] * mljm[l] - rhs[l];
+}
+
+__global__ void k_sor_resid0(DevGrid g, const double *__restrict__ T, const double *__restrict__ ml,
+                             const double *__restrict__ mlip, const double *__restrict__ mlim,
+                             const double *__restrict__ mljp, const double *__restrict__ mljm,
+                             const double *__restrict__ rhs, SorCtl c)
+{
+  const int ns = g.ns;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y + 1;
+  double a = 0.0;
+  if (j < ns) {
+    const int l = j + i * ns;
+    const int ljp = (j == ns - 1) ? i * ns : l + 1;
+    const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+    a = fabs(sor_resid(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm));
+  }
+  a = block_reduce(a, OpAdd(), 0.0);
+  const int nb = gridDim.x * gridDim.y;
+  const int b = blockIdx.x + blockIdx.y * gridDim.x;
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    c.part[b] = a;
+    __threadfence();
+    unsigned t = atomicAdd(c.ticket, 1u);
+    last = (t == (unsigned)nb - 1);
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    double s = 0.0;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) s += ((volatile double *)c.part)[k];
+    s = block_reduce(s, OpAdd(), 0.0);
+    if (threadIdx.x == 0) {
+      *c.normres0 = s;
+      *c.done = 0;
+      *c.niter = 0;
+      *c.ticket = 0u;
+    }
+  }
+}
+
+// One colour pass of sweep n.  Threads map to the cells of one colour:
+// k in [0, ns/2) of ring i gives j = 2k + parity(i, pass).
+__global__ void k_sor_pass(DevGrid g, double *__restrict__ T, const double *__restrict__ ml,
+                           const double *__restrict__ mlip, const double *__restrict__ mlim,
+                           const double *__restrict__ mljp, const double *__restrict__ mljm,
+                           const double *__restrict__ rhs, SorCtl c, double omega, double eps, int pass, int n,
+                           int maxiters)
+{
+  if (*((volatile int *)c.done)) return;
+  const int ns = g.ns, half = ns >> 1;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y + 1;
+  double a = 0.0;
+  int ch = 0;
+  if (k < half) {
+    const int par = (pass == 1) ? ((i - 1) & 1) : (i & 1);
+    const int j = 2 * k + par;
+    const int l = j + i * ns;
+    const int ljp = (j == ns - 1) ? i * ns : l + 1;
+    const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+    const double resid = sor_resid(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm);
+    a = fabs(resid);
+    const double delta = omega * resid / ml[l];
+    const double tn = T[l] - delta;
+    T[l] = tn;
+    ch = (delta > tn * TH_SORPRECISION) ? 1 : 0;
+  }
+  a = block_reduce(a, OpAdd(), 0.0);
+  int chs = block_reduce(ch, OpAddI(), 0);
+  const int nb = gridDim.x * gridDim.y;
+  const int b = blockIdx.x + blockIdx.y * gridDim.x;
+  const int slot = (pass - 1) * nb + b;
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    c.part[slot] = a;
+    c.ipart[slot] = chs;
+    last = false;
+    if (pass == 2) {
+      __threadfence();
+      unsigned t = atomicAdd(c.ticket, 1u);
+      last = (t == (unsigned)nb - 1);
+    }
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    double s = 0.0;
+    int cs = 0;
+    for (int q = threadIdx.x; q < 2 * nb; q += blockDim.x) {
+      s += ((volatile double *)c.part)[q];
+      cs += ((volatile int *)c.ipart)[q];
+    }
+    s = block_reduce(s, OpAdd(), 0.0);
+    cs = block_reduce(cs, OpAddI(), 0);
+    if (threadIdx.x == 0) {
+      const double r0 = *c.normres0;
+      *c.normres = s;
+      *c.changed = cs;
+      *c.niter = n;
+      if (s < eps * r0 || s < TH_SORMIN || cs == 0) *c.done = 1;
+      else if (n >= maxiters) *c.done = 2;
+      *c.ticket = 0u;
+    }
+  }
+}
+
+// After SOR: boundary rings adopt their neighbours' temperature and the
+// energy is rebuilt, E = rho T c_v (EnergySources.c:319-334).
+__global__ void k_energy_from_t(DevGrid g, const double *__restrict__ rho, double *__restrict__ T,
+                                double *__restrict__ enew)
+{
+  const int ns = g.ns, nr = g.nr;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= ns) return;
+  const int l = j + i * ns;
+  if (i == nr) { enew[l] = 0.0; return; }
+  double t;
+  if (i == 0) { t = T[l + ns]; T[l] = t; }
+  else if (i == nr - 1) { t = T[l - ns]; T[l] = t; }
+  else t = T[l];
+  enew[l] = rho[l] * t * g.k.cv;
+}
+
+// ---------------------------------------------------------------------------
+// Transport (TransportEuler.c).  Radial step: the six (gas) or five
+// (pebbles) transported quantities are updated out of place from the old
+// state, in four cell-parallel passes: quotients by the density, van Leer
+// slopes, upwind face values, flux divergence.
+
+// ComputeLRMomenta (TransportEuler.c:318-347) + DivisePolarGrid quotients.
+__global__ void k_rad_prep(DevGrid g, int nq, const double *__restrict__ rho, const double *__restrict__ vr,
+                           const double *__restrict__ vt, const double *__restrict__ energy, double *rmp, double *rmm,
+                           double *tmp_, double *tmm, double *w0, double *w1, double *w2, double *w3, double *we,
+                           double *wr, double omega_frame)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  const int ljp = (j == ns - 1) ? i * ns : l + 1;
+  const double r = rho[l], rm = g.r.Rmed[i];
+  const double a = r * vr[l + ns];
+  const double b = r * vr[l];
+  const double c = r * (vt[ljp] + rm * omega_frame) * rm;
+  const double d = r * (vt[l] + rm * omega_frame) * rm;
+  rmp[l] = a; rmm[l] = b; tmp_[l] = c; tmm[l] = d;
+  const double den = r + 1e-20;
+  w0[l] = a / den; w1[l] = b / den; w2[l] = c / den; w3[l] = d / den;
+  if (nq == 6) we[l] = energy[l] / den;
+  wr[l] = r / den;
+}
+
+__device__ __forceinline__ double vl_slope_r(const DevGrid &g, const double *q, int i, int l)
+{
+  const int nr = g.nr, ns = g.ns;
+  if (i == 0 || i == nr - 1) return 0.0;
+  const double dqm = (q[l] - q[l - ns]) * g.r.InvDiffRmed[i];
+  const double dqp = (q[l + ns] - q[l]) * g.r.InvDiffRmed[i + 1];
+  return (dqp * dqm > 0.0) ? 2.0 * dqp * dqm / (dqp + dqm) : 0.0;
+}
+
+
+__global__ void k_rad_slope(DevGrid g, PtrPack7 pk)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  for (int q = 0; q < pk.n; q++) pk.dst[q][l] = vl_slope_r(g, pk.src[q], i, l);
+}
+
+// ComputeStarRad (TransportEuler.c:232-273): upwind face values at the inner
+// face of ring i (faces 0 and nr are zero).
+__global__ void k_rad_face(DevGrid g, PtrPack7 w, PtrPack7 dq, const double *__restrict__ vr, double dt)
+{
+  const int ns = g.ns, nr = g.nr;
+  CELL_LOOP_2D
+  if (i == 0 || i == nr) {
+    for (int q = 0; q < w.n; q++) w.dst[q][l] = 0.0;
+    return;
+  }
+  const double v = vr[l];
+  if (v > 0.0) {
+    const double c = (g.r.Rmed[i] - g.r.Rmed[i - 1] - v * dt) * 0.5;
+    for (int q = 0; q < w.n; q++) w.dst[q][l] = w.src[q][l - ns] + c * dq.src[q][l - ns];
+  } else {
+    const double c = (g.r.Rmed[i + 1] - g.r.Rmed[i] + v * dt) * 0.5;
+    for (int q = 0; q < w.n; q++) w.dst[q][l] = w.src[q][l] - c * dq.src[q][l];
+  }
+}
+
+// VanLeerRadial update (TransportEuler.c:384-415).
+__global__ void k_rad_update(DevGrid g, PtrPack7 qf, const double *__restrict__ rhos, const double *__restrict__ vr,
+                             PtrPack7 io, double dt)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  const int lip = l + ns;
+  const double dtheta = 2.0 * TH_PI / (double)ns;
+  const double ci = dt * dtheta * g.r.Rinf[i];
+  const double co = dt * dtheta * g.r.Rsup[i];
+  for (int q = 0; q < io.n; q++) {
+    double varq = ci * qf.src[q][l] * rhos[l] * vr[l];
+    varq -= co * qf.src[q][lip] * rhos[lip] * vr[lip];
+    io.dst[q][l] = io.src[q][l] + varq * g.r.InvSurf[i];
+  }
+}
+
+// Azimuthal step (OneWindTheta + QuantitiesAdvection + AdvectSHIFT,
+// TransportEuler.c:70-175): one block per ring with the ring in shared
+// memory.  ComputeResiduals' ring mean of v_theta is summed in order, the
+// integer FARGO shift and the fractional uniform velocity follow, then the
+// residual pass, the uniform pass and the cyclic shift.
+__device__ __forceinline__ void azi_star(double *s_out, const double *s_q, const double *s_dq, int ns, double dxtheta,
+                                         double dt, const double *vt_row, double vsub, double vconst, int uniform)
+{
+  // s_out[j] = ComputeStarTheta face value at the left face of cell j
+  for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+    const int jm = (j == 0) ? ns - 1 : j - 1;
+    const double v = uniform ? vconst : (vt_row[j] - vsub);
+    const double ksi = v * dt;
+    if (ksi > 0.0) s_out[j] = s_q[jm] + (dxtheta - ksi) * s_dq[jm];
+    else s_out[j] = s_q[j] - (dxtheta + ksi) * s_dq[j];
+  }
+}
+
+__device__ __forceinline__ void azi_slope(double *s_dq, const double *s_q, int ns, double invdxtheta)
+{
+  for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+    const int jm = (j == 0) ? ns - 1 : j - 1, jp = (j == ns - 1) ? 0 : j + 1;
+    const double dqm = s_q[j] - s_q[jm], dqp = s_q[jp] - s_q[j];
+    s_dq[j] = ((dqp * dqm > 0.0) && (dqp + dqm != 0.0)) ? dqp * dqm / (dqp + dqm) * invdxtheta : 0.0;
+  }
+}
+
+
+__global__ void k_azimuthal(DevGrid g, AziQ Q, const double *__restrict__ vt, double dt, int fast, int *nshift_out,
+                            double *vmed_out)
+{
+  extern __shared__ double sm[];
+  const int ns = g.ns, i = blockIdx.x;
+  double *s_rho = sm, *s_rhos = sm + ns, *s_w = sm + 2 * ns, *s_dq = sm + 3 * ns;
+  __shared__ double sh_vmed, sh_vtemp;
+  __shared__ int sh_shift;
+  const double *vt_row = vt + (size_t)i * ns;
+  const double rmed = g.r.Rmed[i];
+  const double dxtheta = 2.0 * TH_PI / (double)ns * rmed;
+  const double invdxtheta = 1.0 / dxtheta;
+  const double dxrad = (g.r.Rsup[i] - g.r.Rinf[i]) * dt;
+  const double invsurf = 1.0 / g.r.Surf[i];
+  // ComputeResiduals (TransportEuler.c:70-111)
+  if (threadIdx.x < 32) {
+    const double moy = warp_seq_sum(vt_row, ns);
+    if (threadIdx.x == 0) {
+      const double vm = moy / (double)ns;
+      const double Ntilde = vm * g.r.InvRmed[i] * dt * (double)ns / 2.0 / TH_PI;
+      const double Nround = floor(Ntilde + 0.5);
+      sh_vmed = vm;
+      sh_shift = (int)(long long)Nround;
+      const double invdt = 1.0 / dt, dpinvns = 2.0 * TH_PI / (double)ns;
+      sh_vtemp = (Ntilde - Nround) * rmed * invdt * dpinvns;
+      nshift_out[i] = sh_shift;
+      vmed_out[i] = vm;
+    }
+  }
+  double *rho_g = Q.q[Q.n - 1] + (size_t)i * ns;
+  for (int j = threadIdx.x; j < ns; j += blockDim.x) s_rho[j] = rho_g[j];
+  __syncthreads();
+  const double vmed = sh_vmed, vtemp = sh_vtemp;
+  const int npass = fast ? 2 : 1;
+  for (int pass = 0; pass < npass; pass++) {
+    const int uniform = (pass == 1);
+    const double vsub = fast ? vmed : 0.0;        // residual velocity = vt - VMed (FARGO) or vt
+    // RhoStar from the current density; RhoInt = current density (s_rho)
+    azi_slope(s_dq, s_rho, ns, invdxtheta);
+    __syncthreads();
+    azi_star(s_rhos, s_rho, s_dq, ns, dxtheta, dt, vt_row, vsub, vtemp, uniform);
+    __syncthreads();
+    for (int q = 0; q < Q.n; q++) {
+      double *row = Q.q[q] + (size_t)i * ns;
+      const bool isrho = (q == Q.n - 1);
+      // Work = Q / (RhoInt + 1e-20) into s_w
+      for (int j = threadIdx.x; j < ns; j += blockDim.x) s_w[j] = (isrho ? s_rho[j] : row[j]) / (s_rho[j] + 1e-20);
+      __syncthreads();
+      azi_slope(s_dq, s_w, ns, invdxtheta);
+      __syncthreads();
+      // flux difference with face values computed on the fly
+      double upd[64];
+      int cnt = 0;
+      for (int j = threadIdx.x; j < ns; j += blockDim.x, cnt++) {
+        const int jp = (j == ns - 1) ? 0 : j + 1;
+        const int jm = (j == 0) ? ns - 1 : j - 1;
+        const double v0 = uniform ? vtemp : (vt_row[j] - vsub);
+        const double v1 = uniform ? vtemp : (vt_row[jp] - vsub);
+        const double k0 = v0 * dt, k1 = v1 * dt;
+        const double qs0 = (k0 > 0.0) ? s_w[jm] + (dxtheta - k0) * s_dq[jm] : s_w[j] - (dxtheta + k0) * s_dq[j];
+        const double qs1 = (k1 > 0.0) ? s_w[j] + (dxtheta - k1) * s_dq[j] : s_w[jp] - (dxtheta + k1) * s_dq[jp];
+        double varq = dxrad * qs0 * s_rhos[j] * v0;
+        varq -= dxrad * qs1 * s_rhos[jp] * v1;
+        const double old = isrho ? s_rho[j] : row[j];
+        upd[cnt] = old + varq * invsurf;
+      }
+      __syncthreads();   // everyone finished reading s_rho / s_w before the density changes
+      cnt = 0;
+      for (int j = threadIdx.x; j < ns; j += blockDim.x, cnt++) {
+        if (isrho) s_rho[j] = upd[cnt];
+        else row[j] = upd[cnt];
+      }
+      __syncthreads();
+    }
+  }
+  if (fast) {
+    // AdvectSHIFT (TransportEuler.c:113-136) for every quantity
+    const int sh = sh_shift;
+    for (int q = 0; q < Q.n; q++) {
+      double *row = Q.q[q] + (size_t)i * ns;
+      const bool isrho = (q == Q.n - 1);
+      for (int j = threadIdx.x; j < ns; j += blockDim.x) s_w[j] = isrho ? s_rho[j] : row[j];
+      __syncthreads();
+      for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+        int ji = (j - sh) % ns;
+        if (ji < 0) ji += ns;
+        row[j] = s_w[ji];
+      }
+      __syncthreads();
+    }
+  } else {
+    for (int j = threadIdx.x; j < ns; j += blockDim.x) rho_g[j] = s_rho[j];
+  }
+}
+
+// ComputeVelocities (TransportEuler.c:350-381), followed for the gas by the
+// damping of v_r (DampingBoundary with DampTowards ZEROVRAD,
+// SideEuler.c:368-419) and the EOS refresh (ComputeTemperatureField,
+// ComputeSoundSpeed).
+__global__ void k_velocities(DevGrid g, const double *__restrict__ rho, const double *__restrict__ rmp,
+                             const double *__restrict__ rmm, const double *__restrict__ tmp_,
+                             const double *__restrict__ tmm, double *__restrict__ vr, double *__restrict__ vt,
+                             double omega_frame, int damp_vrad, double dt, double drin, double drout,
+                             const double *__restrict__ energy, double *__restrict__ temper, double *__restrict__ cs,
+                             double gm1, double gg1)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+  const double rm = g.r.Rmed[i];
+  double v;
+  if (i == 0) v = 0.0;
+  else v = (rmp[l - ns] + rmm[l]) / (rho[l] + rho[l - ns] + 1e-20);
+  if (damp_vrad && (rm < drin || rm > drout)) {
+    const double lambda = g.r.WaveKiller[i] * dt;
+    v = (v + lambda * 0.0) / (1.0 + lambda);
+  }
+  vr[l] = v;
+  vt[l] = (tmp_[ljm] + tmm[l]) / (rho[l] + rho[ljm] + 1e-15) / rm - rm * omega_frame;
+  if (temper) {
+    const double r = rho[l], e = energy[l];
+    double tmp2 = 1.0 / (r * 1.0);
+    double tmp1 = e * 1.0 * gm1;
+    temper[l] = tmp1 * tmp2;
+    cs[l] = sqrt(gg1 * fabs(e) / r);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launch wrappers
+void hydro_substep1(const DevGrid &g, const double *rho, const double *vrad, const double *vtheta,
+                    const double *energy, const double *agr, const double *agt, const double *dragr, const double *dragt,
+                    double *vradint, double *vthetaint, double *gaccr, double *gacct, double dt, double omega_frame,
+                    double gm1, int pebbles, int back_reaction, const double *supp_torque, const double *invdxtheta_r,
+                    cudaStream_t s)
+{
+  k_substep1<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, vrad, vtheta, energy, agr, agt, dragr, dragt, vradint,
+                                                   vthetaint, gaccr, gacct, dt, omega_frame, gm1, pebbles,
+                                                   back_reaction, supp_torque, invdxtheta_r);
+}
+
+void hydro_stress(const DevGrid &g, const double *vr, const double *vt, const double *rho, double *divv, double *trr,
+                  double *tpp, double *trp, double invdphi, cudaStream_t s)
+{
+  k_stress<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, vr, vt, rho, divv, trr, tpp, trp, invdphi);
+}
+
+void hydro_visc_update(const DevGrid &g, double *vr, double *vt, const double *rho, const double *trr, const double *tpp,
+                       const double *trp, double dt, double invdphi, int kepler, double vkin, double vkout,
+                       cudaStream_t s)
+{
+  k_visc_update<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, vr, vt, rho, trr, tpp, trp, dt, invdphi, kepler, vkin, vkout);
+}
+
+void hydro_substep2(const DevGrid &g, const double *rho, const double *vr, const double *vt, const double *energy,
+                    double *vrnew, double *vtnew, double *eint, double dt, int energy_eq, const double *invdxtheta_r,
+                    cudaStream_t s)
+{
+  k_substep2<<<grid2d(g.ns, g.nr + 1, BX), BX, 0, s>>>(g, rho, vr, vt, energy, vrnew, vtnew, eint, dt, energy_eq,
+                                                       invdxtheta_r);
+}
+
+void hydro_qplus(const DevGrid &g, const double *vr, const double *vt, const double *rho, double *divv, double *qplus,
+                 double invdphi, double lr01, double lr12, cudaStream_t s)
+{
+  k_qplus<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, vr, vt, rho, divv, qplus, invdphi);
+  k_qplus_row0<<<(g.ns + BX - 1) / BX, BX, 0, s>>>(g, qplus, lr01, lr12);
+}
+
+void hydro_eos(const DevGrid &g, const double *rho, const double *energy, double *temper, double *cs, double gm1,
+               double gg1, cudaStream_t s)
+{
+  k_eos<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, energy, temper, cs, gm1, gg1);
+}
+
+int hydro_diffcoef_blocks(const DevGrid &g) { return ((g.ns + BX - 1) / BX) * g.nr; }
+
+void hydro_diffcoef(const DevGrid &g, const double *rho, const double *T, const double *cs, double *opacity,
+                    double *qminus, double *dcen, double *dtmin_part, int law, double parametric_cu,
+                    double parametric_raw, double opacity_drop, double taueff_c, const double *invdxtheta_r,
+                    const double *deltar2_r, cudaStream_t s)
+{
+  k_diffcoef<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, T, cs, opacity, qminus, dcen, dtmin_part, law, parametric_cu,
+                                                   parametric_raw, opacity_drop, taueff_c, invdxtheta_r, deltar2_r);
+}
+
+void hydro_irradiation(const DevGrid &g, const double *rho, const double *cs, const double *opacity, double *flaring,
+                       double *qirr, double rstar, double tirr4fac, double opacity_drop, double taueff_c,
+                       const double *rinf15, const double *rsup15, cudaStream_t s)
+{
+  k_irradiation<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, cs, opacity, flaring, qirr, rstar, tirr4fac, opacity_drop,
+                                                      taueff_c, rinf15, rsup15);
+}
+
+void hydro_matrix(const DevGrid &g, const double *rho, const double *T, const double *cs, const double *dcen,
+                  const double *divv, const double *qminus, const double *qplus, const double *qirr, double *ml,
+                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs, double dt, double gm1,
+                  const double *invdxtheta2_r, int irradiation, int nheat, const int *heat_idx, const double *heat_val,
+                  cudaStream_t s)
+{
+  if (g.nr < 3) return;
+  k_matrix<<<grid2d(g.ns, g.nr - 2, BX), BX, 0, s>>>(g, rho, T, cs, dcen, divv, qminus, qplus, qirr, ml, mlip, mlim, mljp,
+                                                     mljm, rhs, dt, gm1, invdxtheta2_r, irradiation, nheat, heat_idx,
+                                                     heat_val);
+}
+
+static const int SOR_BX = 128;
+
+int sor_blocks(const DevGrid &g)
+{
+  const int half = g.ns / 2;
+  const int b1 = ((half + SOR_BX - 1) / SOR_BX) * (g.nr - 2);
+  const int b0 = ((g.ns + SOR_BX - 1) / SOR_BX) * (g.nr - 2);
+  return b1 > b0 ? b1 : b0;
+}
+
+void hydro_sor_resid0(const DevGrid &g, const double *T, const double *ml, const double *mlip, const double *mlim,
+                      const double *mljp, const double *mljm, const double *rhs, const SorCtl &c, cudaStream_t s)
+{
+  k_sor_resid0<<<grid2d(g.ns, g.nr - 2, SOR_BX), SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, c);
+}
+
+void hydro_sor_sweeps(const DevGrid &g, double *T, const double *ml, const double *mlip, const double *mlim,
+                      const double *mljp, const double *mljm, const double *rhs, const SorCtl &c, double omega,
+                      double eps, int first, int count, int maxiters, cudaStream_t s)
+{
+  dim3 grid = grid2d(g.ns / 2, g.nr - 2, SOR_BX);
+  for (int n = first; n < first + count && n <= maxiters; n++) {
+    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, c, omega, eps, 1, n, maxiters);
+    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, c, omega, eps, 2, n, maxiters);
+  }
+}
+
+void hydro_energy_from_t(const DevGrid &g, const double *rho, double *T, double *enew, cudaStream_t s)
+{
+  k_energy_from_t<<<grid2d(g.ns, g.nr + 1, BX), BX, 0, s>>>(g, rho, T, enew);
+}
+
+// Whole transport of one fluid.  q_in: rho, vr, vt, energy (NULL for
+// pebbles).  Scratch: 20 fields.  On return the caller's rho/energy pointers
+// are swapped with the updated buffers and vr/vt hold the new velocities.
+
+void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, double **energy, const TransportScratch &S,
+                     double dt, double omega_frame, int fast, int damp_vrad, double drin, double drout, double *temper,
+                     double *cs, double gm1, double gg1, cudaStream_t s)
+{
+  const int ns = g.ns, nr = g.nr;
+  const int nq = energy ? 6 : 5;
+  // quantity order for the radial step: rmp, rmm, tmp, tmm, [e], rho
+  k_rad_prep<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, nq, *rho, vr, vt, energy ? *energy : nullptr, S.mom[0], S.mom[1],
+                                               S.mom[2], S.mom[3], S.w[0], S.w[1], S.w[2], S.w[3], S.w[4], S.w[5],
+                                               omega_frame);
+  // slopes of the quotients (0..3, energy 4 if present, rho-quotient 5) and of rho (6)
+  PtrPack7 sl;
+  int n = 0;
+  for (int q = 0; q < 4; q++) { sl.src[n] = S.w[q]; sl.dst[n] = S.d[q]; n++; }
+  if (nq == 6) { sl.src[n] = S.w[4]; sl.dst[n] = S.d[4]; n++; }
+  sl.src[n] = S.w[5]; sl.dst[n] = S.d[5]; n++;
+  sl.src[n] = *rho; sl.dst[n] = S.d[6]; n++;
+  sl.n = n;
+  k_rad_slope<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, sl);
+  // faces: quotients and rho
+  PtrPack7 wf, dqf;
+  n = 0;
+  for (int q = 0; q < 4; q++) { wf.src[n] = S.w[q]; wf.dst[n] = S.f[q]; dqf.src[n] = S.d[q]; n++; }
+  if (nq == 6) { wf.src[n] = S.w[4]; wf.dst[n] = S.f[4]; dqf.src[n] = S.d[4]; n++; }
+  wf.src[n] = S.w[5]; wf.dst[n] = S.f[5]; dqf.src[n] = S.d[5]; n++;
+  wf.src[n] = *rho; wf.dst[n] = S.f[6]; dqf.src[n] = S.d[6]; n++;
+  wf.n = dqf.n = n;
+  k_rad_face<<<grid2d(ns, nr + 1, BX), BX, 0, s>>>(g, wf, dqf, vr, dt);
+  // flux divergence: in/out
+  PtrPack7 qf, io;
+  n = 0;
+  for (int q = 0; q < 4; q++) { qf.src[n] = S.f[q]; io.src[n] = S.mom[q]; io.dst[n] = S.mom[q]; n++; }
+  if (nq == 6) { qf.src[n] = S.f[4]; io.src[n] = *energy; io.dst[n] = S.e_new; n++; }
+  qf.src[n] = S.f[5]; io.src[n] = *rho; io.dst[n] = S.rho_new; n++;
+  qf.n = io.n = n;
+  k_rad_update<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, qf, S.f[6], vr, io, dt);
+  // azimuthal step on (rmp, rmm, tmp, tmm, [e], rho)
+  AziQ az;
+  n = 0;
+  for (int q = 0; q < 4; q++) az.q[n++] = S.mom[q];
+  if (nq == 6) az.q[n++] = S.e_new;
+  az.q[n++] = S.rho_new;
+  az.n = n;
+  const size_t smem = 4 * (size_t)ns * sizeof(double);
+  k_azimuthal<<<nr, 256, smem, s>>>(g, az, vt, dt, fast, S.nshift, S.vmed);
+  // velocities from the transported momenta
+  k_velocities<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, S.rho_new, S.mom[0], S.mom[1], S.mom[2], S.mom[3], vr, vt,
+                                                 omega_frame, damp_vrad, dt, drin, drout,
+                                                 energy ? S.e_new : nullptr, energy ? temper : nullptr, cs, gm1, gg1);
+}
+
+int hydro_azimuthal_smem(int ns) { return 4 * ns * (int)sizeof(double); }
+
+void hydro_set_smem_limits(int ns)
+{
+  const int need = hydro_azimuthal_smem(ns);
+  cudaFuncSetAttribute(k_azimuthal, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
+}

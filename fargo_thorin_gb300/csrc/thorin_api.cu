@@ -1,0 +1,1270 @@
+// thorin_api.cu -- the C ABI of include/thorin_gpu.h: device state of one
+// disk, host-side set-up that the reference performs once on the host
+// (grid, profiles, initial fields: SourceEuler.c:68-175, Theo.c,
+// Pframeforce.c:620-751, Pebbles.c:37-275), the substep driver of AlgoGas
+// (SourceEuler.c:210-317), the SOR control loop and omega schedule
+// (EnergySources.c:298-403), and the host N-body step standing in for
+// REBOUND (ReboundInterface.c:262-385, Psys.c:336).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "thorin_kernels.cuh"
+
+// Unit constants (src_main/fondam.h), evaluated with the host libm.
+#define H_PI 3.14159265358979323844
+#define H_MPI 3.14159265358979323846
+#define MSOL_SI 1.98855e30
+#define GM_SI 1.32712440018e20
+#define AU_SI 149597870700.0
+#define R_STANDARD 8.3144598
+#define MMW 2.4
+#define R_SI (R_STANDARD / (MMW * 0.001))
+#define OPA2CU (MSOL_SI * 1000.0 / pow(AU_SI * 100.0, 2.0))
+#define T2SI (GM_SI / R_SI / AU_SI)
+#define TIME2SI (sqrt(pow(AU_SI, 3.0) / GM_SI))
+#define RHO2CGS (MSOL_SI * 1000.0 / pow(AU_SI * 100.0, 3.0))
+#define STEFANBOLTZMANN (5.670367e-8 * (1.0 / MSOL_SI) * pow(1.0 / TIME2SI, -3.0) * pow(1.0 / T2SI, -4.0))
+#define FLUX2CU (0.000003 / (2.0 * H_PI))
+#define SQRT2PI_INV (1.0 / sqrt(2.0 * H_PI))
+
+static thread_local std::string g_last_error;
+
+#define CUCHK(call)                                                                     \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      g_last_error = std::string(#call) + ": " + cudaGetErrorString(e_);                \
+      return THORIN_ERR_CUDA;                                                           \
+    }                                                                                   \
+  } while (0)
+
+#define RCHK(expr)                     \
+  do {                                 \
+    int r_ = (expr);                   \
+    if (r_ != THORIN_OK) return r_;    \
+  } while (0)
+
+extern "C" const char *thorin_gpu_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" void thorin_params_default(thorin_params *p, int nrad, int nsec)
+{
+  // src_main/var.c:17-141 defaults and the derived switches of Interpret.c.
+  memset(p, 0, sizeof(*p));
+  p->nrad = nrad; p->nsec = nsec;
+  p->rmin = 1.0; p->rmax = 1.0;
+  p->sigma0 = 173.0; p->aspect_ratio = 0.05;
+  p->scaling_factor = 1.0;
+  p->cavity_ratio = 1.0; p->cavity_width = 1.0;
+  p->transition_ratio = 1.0; p->transition_width = 1.0;
+  p->tmri = 1000.0; p->twidth = 25.0;
+  p->adiabind = 1.4; p->cooling_time = -1.0;
+  p->opacity_drop = 0.6; p->effective_temperature = 5656.0; p->stellar_radius = 3.0; p->disc_albedo = 0.5;
+  p->hillcut = 0.8; p->indirect_term = 1; p->mass_taper = 0.0000001; p->vertical_damping = 0.1;
+  p->planetary_density = 1.0;
+  p->fast_transport = 1;
+  p->damp_vrad = 1;
+  p->damping_rmin_frac = 1.25; p->damping_rmax_frac = 0.84; p->damping_period_frac = 1.0;
+  p->dt = 1.0; p->first_step = -1.0; p->minimum_step = 1.0e-3; p->maximum_step = 1.0e6;
+  p->diffusive_particles = 1;
+  p->pebble_flux = 2.0e-4; p->pebble_alpha = 1.0e-4; p->pebble_coagulation = 0.5; p->pebble_bulk_dens = 1.0;
+  p->schmidt_number = 1.0; p->heating_delay = 100; p->pebble_to_gas_max = 0.01;
+  p->fragment_factor = 1.0; p->fragment_threshold = 1.0; p->fragment_alpha = 1.0e-3;
+  p->evaporation_temperature = 1000.0; p->evaporation_rate = 1.0e-3;
+  p->sor_eps = 1.0e-6; p->sor_maxiters = 100000;
+}
+
+// ---------------------------------------------------------------------------
+enum {  // ring arrays kept on the device
+  R_RINF, R_RSUP, R_RMED, R_SURF, R_INVRMED, R_INVSURF, R_INVDIFFRMED, R_INVDIFFRSUP, R_INVRINF, R_OMEGAINV, R_RMED2,
+  R_WAVEKILLER, R_RMED15, R_RINF15, R_RSUP15, R_COSTAB, R_SINTAB, R_SIGMAMED, R_ENERGYMED, R_VTHETAMED, R_PEBDENS0,
+  R_PEBVRAD0, R_PEBVTHETA0, R_CSMEAN, R_TEMPMEAN, R_NUMED, R_NUINF, R_INVDXTHETA, R_INVDXTHETA2, R_SUPPTORQUE,
+  R_DELTAR2, R_CFLDXRAD, R_CFLDXTHETA, R_CFLMINDX, R_CFLDEN5, R_VMOY, R_PVTMED, R_HAVR, R_SIGAVR, R_ISTAVR, R_PHAVR,
+  R_PISTAVR, R_VMED, R_COUNT
+};
+
+struct thorin_disk {
+  thorin_params p;
+  int nr, ns;
+  size_t fsize;                      // doubles per field allocation
+  cudaStream_t s;
+  DevGrid g;
+  std::vector<void *> allocs;
+  double *ring[R_COUNT];
+  // fields
+  double *rho, *vrad, *vtheta, *energy, *vrad_new, *vtheta_new, *energy_new, *vrad_int, *vtheta_int, *energy_int;
+  double *cs, *temper, *qplus, *qminus, *opacity, *divv, *trr, *trp, *tpp, *agr, *agt, *pagr, *pagt, *dcen;
+  double *ml, *mlip, *mlim, *mljp, *mljm, *rhs, *tbackup, *flaring, *qirr;
+  double *pdens, *pvrad, *pvtheta, *psize, *tau, *paccr, *pacct, *gaccr, *gacct, *dragr, *dragt, *macc;
+  double *t_rho_gas, *t_e_gas, *t_rho_peb;
+  TransportScratch ts;
+  double *partials, *scal;
+  int *iscal, *nshift, *heat_idx_d, *damp_rings_d;
+  double *heat_val_d;
+  unsigned int *ticket;
+  DevPlanet *planets_d;
+  SorCtl sor;
+  CflRings cfl;
+  ForceRings fr;
+  // pinned host mirrors
+  double *scal_h, *csmean_h;
+  int *iscal_h;
+  // host ring arrays
+  std::vector<double> Radii, GlobalRmed, Rinf, Rsup, Rmed, Surf, InvRmed, InvSurf, InvDiffRmed, InvDiffRsup, InvRinf,
+      OmegaInv, Rmed2, WaveKiller, SigmaMed, SigmaInf, EnergyMed, VthetaMed, PebDensInit, PebVradInit, PebVthetaInit;
+  std::vector<int> nshift_h;
+  int ndamp;
+  // scalars carried between substeps (static variables in the reference)
+  double PhysicalTime, PhysicalTimeInitial, OmegaFrame, MassTaper;
+  int cfl_first;
+  int sor_first, Niterlast, Niterbest;
+  double omega, domega, omegabest;
+  double heatsrc[THORIN_MAXPLANETS];
+  int heatsrc_index[THORIN_MAXPLANETS], heatsrc_max;
+  double gm1, gg1, drin, drout, invdphi, lr01, lr12, vkep_in, vkep_out, taueff_c, tirr4fac, rstar;
+  ViscParams vp;
+  thorin_stats st;
+};
+
+static int dalloc(thorin_disk *d, void **ptr, size_t bytes)
+{
+  CUCHK(cudaMalloc(ptr, bytes));
+  CUCHK(cudaMemsetAsync(*ptr, 0, bytes, d->s));
+  d->allocs.push_back(*ptr);
+  return THORIN_OK;
+}
+
+static int dfield(thorin_disk *d, double **ptr) { return dalloc(d, (void **)ptr, d->fsize * sizeof(double)); }
+
+static int upload_ring(thorin_disk *d, int id, const std::vector<double> &v)
+{
+  CUCHK(cudaMemcpyAsync(d->ring[id], v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  return THORIN_OK;
+}
+
+// FillPolar1DArrays (SourceEuler.c:68-131) and the per-ring constants of the
+// kernels, each with the expression the reference uses at that place.
+static void fill_rings(thorin_disk *d)
+{
+  const thorin_params &p = d->p;
+  const int nr = d->nr, ns = d->ns, n1 = nr + 2;
+  auto Z = [&](std::vector<double> &v) { v.assign(n1, 0.0); };
+  Z(d->Radii); Z(d->GlobalRmed); Z(d->Rinf); Z(d->Rsup); Z(d->Rmed); Z(d->Surf); Z(d->InvRmed); Z(d->InvSurf);
+  Z(d->InvDiffRmed); Z(d->InvDiffRsup); Z(d->InvRinf); Z(d->OmegaInv); Z(d->Rmed2); Z(d->WaveKiller);
+  Z(d->SigmaMed); Z(d->SigmaInf); Z(d->EnergyMed); Z(d->VthetaMed); Z(d->PebDensInit); Z(d->PebVradInit);
+  Z(d->PebVthetaInit);
+  const double drrsep = (p.rmax - p.rmin) / (double)nr;
+  for (int i = 0; i <= nr; i++)
+    d->Radii[i] = p.log_grid ? p.rmin * exp((double)i / (double)nr * log(p.rmax / p.rmin)) : p.rmin + drrsep * (double)i;
+  for (int i = 0; i < nr; i++) {
+    const double a = d->Radii[i], b = d->Radii[i + 1];
+    d->GlobalRmed[i] = 2.0 / 3.0 * (b * b * b - a * a * a);
+    d->GlobalRmed[i] = d->GlobalRmed[i] / (b * b - a * a);
+    d->Rinf[i] = a;
+    d->Rsup[i] = b;
+    d->Rmed[i] = 2.0 / 3.0 * (b * b * b - a * a * a);
+    d->Rmed[i] = d->Rmed[i] / (b * b - a * a);
+    d->Surf[i] = H_PI * (b * b - a * a) / (double)ns;
+    d->InvRmed[i] = 1.0 / d->Rmed[i];
+    d->InvSurf[i] = 1.0 / d->Surf[i];
+    d->InvDiffRsup[i] = 1.0 / (b - a);
+    d->InvRinf[i] = 1.0 / a;
+    d->OmegaInv[i] = pow(d->Rmed[i], 1.5);
+    d->Rmed2[i] = d->Rmed[i] * d->Rmed[i];
+  }
+  d->Rinf[nr] = d->Radii[nr];
+  for (int i = 1; i < nr; i++) d->InvDiffRmed[i] = 1.0 / (d->Rmed[i] - d->Rmed[i - 1]);
+  // SetWaveKillingZones (SideEuler.c:341-362)
+  d->drin = p.rmin * p.damping_rmin_frac;
+  d->drout = p.rmax * p.damping_rmax_frac;
+  const double tauin = p.damping_period_frac * 2.0 * H_PI * pow(p.rmin, 1.5);
+  const double tauout = p.damping_period_frac * 2.0 * H_PI * pow(d->drout, 1.5);
+  if (p.damping || p.pebbles)
+    for (int i = 0; i < nr; i++) {
+      double damp;
+      d->WaveKiller[i] = 0.0;
+      if (d->Rmed[i] < d->drin) { damp = (d->drin - d->Rmed[i]) / (d->drin - p.rmin); d->WaveKiller[i] = damp * damp / tauin; }
+      if (d->Rmed[i] > d->drout) { damp = (d->Rmed[i] - d->drout) / (p.rmax - d->drout); d->WaveKiller[i] = damp / tauout; }
+    }
+}
+
+static double fviscosity_host(const thorin_disk *d, int i_ring, double rad, const std::vector<double> &csm)
+{
+  // FViscosity (Viscosity.c:26-54) for the ring the reference's search finds.
+  const thorin_params &p = d->p;
+  double nu = p.viscosity;
+  if (p.viscosity_alpha) nu = p.alpha_viscosity * csm[i_ring] * csm[i_ring] * pow(rad, 1.5);
+  const double rmin = (p.cavity_radius - p.cavity_width * p.aspect_ratio);
+  const double rmax = (p.cavity_radius + p.cavity_width * p.aspect_ratio);
+  if (rad < rmin) nu *= p.cavity_ratio;
+  if ((rad >= rmin) && (rad <= rmax)) nu *= exp((rmax - rad) / (rmax - rmin) * log(p.cavity_ratio));
+  return nu;
+}
+
+static int upload_all_rings(thorin_disk *d)
+{
+  const int nr = d->nr, ns = d->ns, n1 = nr + 2;
+  const thorin_params &p = d->p;
+  std::vector<double> v(n1, 0.0);
+  RCHK(upload_ring(d, R_RINF, d->Rinf)); RCHK(upload_ring(d, R_RSUP, d->Rsup)); RCHK(upload_ring(d, R_RMED, d->Rmed));
+  RCHK(upload_ring(d, R_SURF, d->Surf)); RCHK(upload_ring(d, R_INVRMED, d->InvRmed));
+  RCHK(upload_ring(d, R_INVSURF, d->InvSurf)); RCHK(upload_ring(d, R_INVDIFFRMED, d->InvDiffRmed));
+  RCHK(upload_ring(d, R_INVDIFFRSUP, d->InvDiffRsup)); RCHK(upload_ring(d, R_INVRINF, d->InvRinf));
+  RCHK(upload_ring(d, R_OMEGAINV, d->OmegaInv)); RCHK(upload_ring(d, R_RMED2, d->Rmed2));
+  RCHK(upload_ring(d, R_WAVEKILLER, d->WaveKiller));
+  for (int i = 0; i < nr; i++) v[i] = pow(d->Rmed[i], 1.5);
+  RCHK(upload_ring(d, R_RMED15, v));
+  std::fill(v.begin(), v.end(), 0.0);
+  for (int i = 0; i <= nr; i++) v[i] = pow(d->Rinf[i], 1.5);
+  RCHK(upload_ring(d, R_RINF15, v));
+  std::fill(v.begin(), v.end(), 0.0);
+  for (int i = 0; i < nr; i++) v[i] = pow(d->Rsup[i], 1.5);
+  RCHK(upload_ring(d, R_RSUP15, v));
+  // trigonometric tables of InitComputeAccel (SideEuler.c:101-118):
+  // abscissa = Rmed[i] * cos(2 pi j / ns) is a single product.
+  std::vector<double> c(ns), sn(ns);
+  for (int j = 0; j < ns; j++) { c[j] = cos(2.0 * H_PI * (double)j / (double)ns); sn[j] = sin(2.0 * H_PI * (double)j / (double)ns); }
+  CUCHK(cudaMemcpyAsync(d->ring[R_COSTAB], c.data(), ns * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaMemcpyAsync(d->ring[R_SINTAB], sn.data(), ns * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  // per-ring expressions of SubStep1/2, ImplicitRadiativeDiffusion, DiffusionTimestep, ConditionCFL
+  std::vector<double> a(n1, 0.0), b(n1, 0.0), st(n1, 0.0), dr2(n1, 0.0), cdx(n1, 0.0), cdt(n1, 0.0), cmin(n1, 0.0),
+      cden(n1, 0.0);
+  for (int i = 0; i < nr; i++) {
+    const double dxtheta = 2.0 * H_PI / (double)ns * d->Rmed[i];
+    a[i] = 1.0 / dxtheta;
+    b[i] = 1.0 / dxtheta / dxtheta;
+    st[i] = p.imposed_disk_drift * .5 * pow(d->Rmed[i], -2.5 + p.sigma_slope);
+    double dr = d->Rsup[i] - d->Rinf[i];
+    dr2[i] = dr * dr / 2.0;
+    const double dxrad = d->Rsup[i] - d->Rinf[i];
+    const double dxth = d->Rmed[i] * 2.0 * H_PI / (double)ns;
+    cdx[i] = dxrad;
+    cdt[i] = dxth;
+    cmin[i] = (dxth < dxrad) ? dxth : dxrad;
+    cden[i] = pow(cmin[i], 2);
+  }
+  RCHK(upload_ring(d, R_INVDXTHETA, a)); RCHK(upload_ring(d, R_INVDXTHETA2, b));
+  RCHK(upload_ring(d, R_SUPPTORQUE, st)); RCHK(upload_ring(d, R_DELTAR2, dr2));
+  RCHK(upload_ring(d, R_CFLDXRAD, cdx)); RCHK(upload_ring(d, R_CFLDXTHETA, cdt));
+  RCHK(upload_ring(d, R_CFLMINDX, cmin)); RCHK(upload_ring(d, R_CFLDEN5, cden));
+  RCHK(upload_ring(d, R_SIGMAMED, d->SigmaMed)); RCHK(upload_ring(d, R_ENERGYMED, d->EnergyMed));
+  RCHK(upload_ring(d, R_VTHETAMED, d->VthetaMed)); RCHK(upload_ring(d, R_PEBDENS0, d->PebDensInit));
+  RCHK(upload_ring(d, R_PEBVRAD0, d->PebVradInit)); RCHK(upload_ring(d, R_PEBVTHETA0, d->PebVthetaInit));
+  return THORIN_OK;
+}
+
+static void build_grid(thorin_disk *d)
+{
+  DevGrid &g = d->g;
+  g.nr = d->nr; g.ns = d->ns;
+  DevRings &r = g.r;
+  double **R = d->ring;
+  r.Rinf = R[R_RINF]; r.Rsup = R[R_RSUP]; r.Rmed = R[R_RMED]; r.Surf = R[R_SURF]; r.InvRmed = R[R_INVRMED];
+  r.InvSurf = R[R_INVSURF]; r.InvDiffRmed = R[R_INVDIFFRMED]; r.InvDiffRsup = R[R_INVDIFFRSUP];
+  r.InvRinf = R[R_INVRINF]; r.OmegaInv = R[R_OMEGAINV]; r.Rmed2 = R[R_RMED2]; r.WaveKiller = R[R_WAVEKILLER];
+  r.Rmed15 = R[R_RMED15]; r.Rinf15 = R[R_RINF15]; r.costab = R[R_COSTAB]; r.sintab = R[R_SINTAB];
+  r.SigmaMed = R[R_SIGMAMED]; r.EnergyMed = R[R_ENERGYMED]; r.VthetaMed = R[R_VTHETAMED];
+  r.PebDensInit = R[R_PEBDENS0]; r.PebVradInit = R[R_PEBVRAD0]; r.PebVthetaInit = R[R_PEBVTHETA0];
+  r.csmean = R[R_CSMEAN]; r.tempmean = R[R_TEMPMEAN]; r.nu_med = R[R_NUMED]; r.nu_inf = R[R_NUINF];
+  DevConst &k = g.k;
+  const thorin_params &p = d->p;
+  k.opa2cu = OPA2CU; k.t2si = T2SI; k.rho2cgs = RHO2CGS; k.sigma_sb = STEFANBOLTZMANN; k.sqrt2pi_inv = SQRT2PI_INV;
+  k.pebbulkdens = p.pebble_bulk_dens / RHO2CGS;
+  k.cv = 1.0 / (1.0 * (p.adiabind - 1.0));
+  k.sqrt_adiabind_inv = 1.0 / sqrt(p.adiabind);
+  k.evaptemp = p.evaporation_temperature / T2SI;
+  k.sqrt3 = sqrt(3.0);
+  d->cfl.dxrad = R[R_CFLDXRAD]; d->cfl.dxtheta = R[R_CFLDXTHETA]; d->cfl.mindx = R[R_CFLMINDX];
+  d->cfl.den5 = R[R_CFLDEN5]; d->cfl.vmoy = R[R_VMOY]; d->cfl.pvtmed = R[R_PVTMED];
+  d->fr.H_avr = R[R_HAVR]; d->fr.sigma_avr = R[R_SIGAVR]; d->fr.integstar_avr = R[R_ISTAVR];
+  d->fr.p_H_avr = R[R_PHAVR]; d->fr.p_integstar_avr = R[R_PISTAVR];
+}
+
+static int check_supported(const thorin_params &p)
+{
+  const char *bad = nullptr;
+  if (p.nrad < 4 || p.nsec < 4 || (p.nsec & 1)) bad = "nrad, nsec >= 4 and nsec even (red-black SOR)";
+  else if (!p.energy_eq) bad = "isothermal runs (EnergyEquation NO)";
+  else if (p.open_inner || p.open_outer || p.non_reflecting || p.outer_source_mass) bad = "open/non-reflecting boundaries";
+  else if (p.damp_flux || p.damp_init) bad = "DampTowards INIT/GASFLUX";
+  else if (p.parametric_cooling) bad = "parametric cooling";
+  else if (p.accretion_rate > 1e-10) bad = "gas accretion onto planets";
+  else if (p.prescribed_accretion) bad = "ParametricAccretion";
+  else if (p.aerodynamic_drag) bad = "AerodynamicDrag";
+  else if (p.sloppy_cfl) bad = "SloppyCFL";
+  else if (p.omega_frame != 0.0) bad = "rotating frame";
+  if (bad) {
+    g_last_error = std::string("unsupported option: ") + bad;
+    return THORIN_ERR_ARG;
+  }
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
+{
+  if (!pin || !out) return THORIN_ERR_ARG;
+  RCHK(check_supported(*pin));
+  thorin_disk *d = new thorin_disk();
+  d->p = *pin;
+  d->nr = pin->nrad;
+  d->ns = pin->nsec;
+  d->fsize = (size_t)(d->nr + 3) * (size_t)(d->ns + 1) + 5;
+  CUCHK(cudaStreamCreateWithFlags(&d->s, cudaStreamNonBlocking));
+  const int n1 = d->nr + 2;
+  for (int q = 0; q < R_COUNT; q++) {
+    size_t n = (q == R_COSTAB || q == R_SINTAB) ? (size_t)d->ns : (size_t)n1;
+    RCHK(dalloc(d, (void **)&d->ring[q], n * sizeof(double)));
+  }
+  build_grid(d);
+  double **F[] = {&d->rho, &d->vrad, &d->vtheta, &d->energy, &d->vrad_new, &d->vtheta_new, &d->energy_new,
+                  &d->vrad_int, &d->vtheta_int, &d->energy_int, &d->cs, &d->temper, &d->qplus, &d->qminus,
+                  &d->opacity, &d->divv, &d->trr, &d->trp, &d->tpp, &d->agr, &d->agt, &d->dcen, &d->ml, &d->mlip,
+                  &d->mlim, &d->mljp, &d->mljm, &d->rhs, &d->tbackup, &d->t_rho_gas, &d->t_e_gas};
+  for (auto f : F) RCHK(dfield(d, f));
+  if (d->p.stellar_irradiation) { RCHK(dfield(d, &d->flaring)); RCHK(dfield(d, &d->qirr)); }
+  else { d->flaring = d->qirr = nullptr; }
+  if (d->p.pebbles) {
+    double **P[] = {&d->pagr, &d->pagt, &d->pdens, &d->pvrad, &d->pvtheta, &d->psize, &d->tau, &d->paccr, &d->pacct,
+                    &d->gaccr, &d->gacct, &d->dragr, &d->dragt, &d->macc, &d->t_rho_peb};
+    for (auto f : P) RCHK(dfield(d, f));
+  } else {
+    d->pagr = d->pagt = d->pdens = d->pvrad = d->pvtheta = d->psize = d->tau = nullptr;
+    d->paccr = d->pacct = d->gaccr = d->gacct = d->dragr = d->dragt = d->macc = d->t_rho_peb = nullptr;
+  }
+  for (int q = 0; q < 4; q++) RCHK(dfield(d, &d->ts.mom[q]));
+  for (int q = 0; q < 6; q++) RCHK(dfield(d, &d->ts.w[q]));
+  for (int q = 0; q < 7; q++) { RCHK(dfield(d, &d->ts.d[q])); RCHK(dfield(d, &d->ts.f[q])); }
+  RCHK(dalloc(d, (void **)&d->nshift, n1 * sizeof(int)));
+  d->ts.nshift = d->nshift;
+  d->ts.vmed = nullptr;
+  // reduction scratch: enough partials for every reduction kernel
+  const size_t nb = (size_t)((d->ns + 127) / 128 + 2) * (size_t)(d->nr + 2);
+  RCHK(dalloc(d, (void **)&d->partials, nb * (2 + 2 * MAXPL_DEV + 6) * sizeof(double)));
+  RCHK(dalloc(d, (void **)&d->scal, 256 * sizeof(double)));
+  RCHK(dalloc(d, (void **)&d->iscal, 64 * sizeof(int)));
+  RCHK(dalloc(d, (void **)&d->ticket, 16 * sizeof(unsigned int)));
+  RCHK(dalloc(d, (void **)&d->heat_idx_d, THORIN_MAXPLANETS * sizeof(int)));
+  RCHK(dalloc(d, (void **)&d->heat_val_d, THORIN_MAXPLANETS * sizeof(double)));
+  RCHK(dalloc(d, (void **)&d->damp_rings_d, n1 * sizeof(int)));
+  RCHK(dalloc(d, (void **)&d->planets_d, MAXPL_DEV * sizeof(DevPlanet)));
+  CUCHK(cudaMallocHost((void **)&d->scal_h, 256 * sizeof(double)));
+  CUCHK(cudaMallocHost((void **)&d->iscal_h, 64 * sizeof(int)));
+  CUCHK(cudaMallocHost((void **)&d->csmean_h, n1 * sizeof(double)));
+  // SOR control block
+  const int sb = sor_blocks(d->g);
+  double *sp;
+  int *ip;
+  RCHK(dalloc(d, (void **)&sp, (size_t)(2 * sb + 8) * sizeof(double)));
+  RCHK(dalloc(d, (void **)&ip, (size_t)(2 * sb + 8) * sizeof(int)));
+  d->sor.part = sp + 8;
+  d->sor.normres0 = sp;
+  d->sor.normres = sp + 1;
+  d->sor.ipart = ip + 8;
+  d->sor.done = ip;
+  d->sor.niter = ip + 1;
+  d->sor.changed = ip + 2;
+  d->sor.ticket = d->ticket;
+  fill_rings(d);
+  // damping rings (rows with Rmed outside [DRin, DRout])
+  std::vector<int> rings;
+  for (int i = 0; i < d->nr; i++)
+    if (d->Rmed[i] < d->drin || d->Rmed[i] > d->drout) rings.push_back(i);
+  d->ndamp = (int)rings.size();
+  if (d->ndamp) CUCHK(cudaMemcpyAsync(d->damp_rings_d, rings.data(), d->ndamp * sizeof(int), cudaMemcpyHostToDevice, d->s));
+  RCHK(upload_all_rings(d));
+  const thorin_params &p = d->p;
+  d->gm1 = p.adiabind - 1.0;
+  d->gg1 = p.adiabind * (p.adiabind - 1.0);
+  d->invdphi = 1.0 / (2.0 * H_MPI / (double)d->ns);
+  d->lr01 = log(d->Rmed[0] / d->Rmed[1]);
+  d->lr12 = log(d->Rmed[1] / d->Rmed[2]);
+  d->taueff_c = p.stellar_irradiation ? 0.5 : 0.25 * sqrt(3.0);
+  {
+    // ImposeKeplerianEdges (Viscosity.c:221-260) with AspectRatio (:56-71)
+    auto aspect = [&](double rad) {
+      double ar = p.aspect_ratio;
+      const double rmin = p.transition_radius - p.transition_width * p.aspect_ratio;
+      const double rmax = p.transition_radius + p.transition_width * p.aspect_ratio;
+      if (rad < rmin) ar *= p.transition_ratio;
+      if ((rad >= rmin) && (rad <= rmax)) ar *= exp((rmax - rad) / (rmax - rmin) * log(p.transition_ratio));
+      return ar;
+    };
+    const double r0 = d->Rmed[0], r1 = d->Rmed[d->nr - 1];
+    const double vin = sqrt(1.0 * 1.0 / r0) *
+                       sqrt(1.0 - pow(aspect(r0), 2.0) * pow(r0, 2.0 * p.flaring_index) *
+                                      (1. + p.sigma_slope - 2.0 * p.flaring_index));
+    const double vout = sqrt(1.0 * 1.0 / r1) *
+                        sqrt(1.0 - pow(aspect(r1), 2.0) * pow(r1, 2.0 * p.flaring_index) *
+                                       (1. + p.sigma_slope - 2.0 * p.flaring_index));
+    d->vkep_in = vin - r0 * p.omega_frame;
+    d->vkep_out = vout - r1 * p.omega_frame;
+  }
+  d->rstar = p.stellar_radius * 6.957e8 / AU_SI;
+  {
+    double Teff4 = pow(p.effective_temperature / T2SI, 4.0);
+    double Rstar2 = pow(p.stellar_radius * (6.957e8 / AU_SI), 2.0);
+    d->tirr4fac = (1.0 - p.disc_albedo) * Teff4 * Rstar2;
+  }
+  d->vp.viscosity = p.viscosity; d->vp.alpha = p.alpha_viscosity; d->vp.alpha_mri = p.alpha_mri;
+  d->vp.alpha_dead = p.alpha_dead; d->vp.tmri = p.tmri; d->vp.twidth = p.twidth; d->vp.t2si = T2SI;
+  d->vp.cav_rmin = p.cavity_radius - p.cavity_width * p.aspect_ratio;
+  d->vp.cav_rmax = p.cavity_radius + p.cavity_width * p.aspect_ratio;
+  d->vp.cav_ratio = p.cavity_ratio; d->vp.log_cav_ratio = log(p.cavity_ratio);
+  d->vp.viscosity_alpha = p.viscosity_alpha; d->vp.alpha_flock = p.alpha_flock;
+  if (p.lambda_doubling != 0.0) { g_last_error = "LambdaDoubling is not supported"; return THORIN_ERR_ARG; }
+  d->OmegaFrame = p.omega_frame;
+  d->MassTaper = 1.0;
+  d->cfl_first = 1;
+  d->sor_first = 1;
+  d->heatsrc_max = 0;
+  for (int k = 0; k < THORIN_MAXPLANETS; k++) { d->heatsrc[k] = 0.0; d->heatsrc_index[k] = -1; }
+  memset(&d->st, 0, sizeof(d->st));
+  d->scal_h[SC_DTSTELLAR] = 1.0e38;                   // global.h:47
+  CUCHK(cudaMemcpyAsync(d->scal + SC_DTSTELLAR, d->scal_h + SC_DTSTELLAR, sizeof(double), cudaMemcpyHostToDevice, d->s));
+  hydro_set_smem_limits(d->ns);
+  if (hydro_azimuthal_smem(d->ns) > 227 * 1024) { g_last_error = "nsec too large for the ring kernel"; return THORIN_ERR_ARG; }
+  CUCHK(cudaStreamSynchronize(d->s));
+  d->nshift_h.assign(d->nr, 0);
+  *out = d;
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_destroy(thorin_disk *d)
+{
+  if (!d) return THORIN_OK;
+  cudaStreamSynchronize(d->s);
+  for (void *a : d->allocs) cudaFree(a);
+  cudaFreeHost(d->scal_h);
+  cudaFreeHost(d->iscal_h);
+  cudaFreeHost(d->csmean_h);
+  cudaStreamDestroy(d->s);
+  delete d;
+  return THORIN_OK;
+}
+
+static double *field_ptr(thorin_disk *d, int id)
+{
+  switch (id) {
+  case THORIN_DENS: return d->rho;
+  case THORIN_VRAD: return d->vrad;
+  case THORIN_VTHETA: return d->vtheta;
+  case THORIN_ENERGY: return d->energy;
+  case THORIN_PEBDENS: return d->pdens;
+  case THORIN_PEBVRAD: return d->pvrad;
+  case THORIN_PEBVTHETA: return d->pvtheta;
+  case THORIN_PEBSIZE: return d->psize;
+  case THORIN_TEMPER: return d->temper;
+  case THORIN_SOUNDSPEED: return d->cs;
+  case THORIN_STOKES: return d->tau;
+  case THORIN_QPLUS: return d->qplus;
+  case THORIN_DIVV: return d->divv;
+  case THORIN_OPACITY: return d->opacity;
+  case THORIN_QMINUS: return d->qminus;
+  }
+  return nullptr;
+}
+
+extern "C" int thorin_gpu_upload(thorin_disk *d, int field, const double *host)
+{
+  if (!d || !host) return THORIN_ERR_ARG;
+  double *f = field_ptr(d, field);
+  if (!f || field == THORIN_PRESSURE) { g_last_error = "field not available"; return THORIN_ERR_ARG; }
+  CUCHK(cudaMemcpyAsync(f, host, (size_t)(d->nr + 1) * d->ns * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  return THORIN_OK;
+}
+
+// pressure (SourceEuler.c:740-762) is formed on the fly in the kernels; it
+// is rebuilt here from the energy when asked for.
+extern "C" int thorin_gpu_download(thorin_disk *d, int field, double *host)
+{
+  if (!d || !host) return THORIN_ERR_ARG;
+  const size_t n = (size_t)(d->nr + 1) * d->ns;
+  if (field == THORIN_PRESSURE) {
+    CUCHK(cudaMemcpyAsync(host, d->energy, n * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+    CUCHK(cudaStreamSynchronize(d->s));
+    for (size_t l = 0; l < (size_t)d->nr * d->ns; l++) host[l] = d->gm1 * host[l];
+    for (size_t l = (size_t)d->nr * d->ns; l < n; l++) host[l] = 0.0;
+    return THORIN_OK;
+  }
+  double *f = field_ptr(d, field);
+  if (!f) { g_last_error = "field not available"; return THORIN_ERR_ARG; }
+  CUCHK(cudaMemcpyAsync(host, f, n * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  return THORIN_OK;
+}
+
+static std::vector<double> *profile_vec(thorin_disk *d, int id, int *ring)
+{
+  switch (id) {
+  case THORIN_SIGMAMED: *ring = R_SIGMAMED; return &d->SigmaMed;
+  case THORIN_SIGMAINF: *ring = -1; return &d->SigmaInf;
+  case THORIN_ENERGYMED: *ring = R_ENERGYMED; return &d->EnergyMed;
+  case THORIN_VTHETAMED: *ring = R_VTHETAMED; return &d->VthetaMed;
+  case THORIN_PEBDENSINIT: *ring = R_PEBDENS0; return &d->PebDensInit;
+  case THORIN_PEBVRADINIT: *ring = R_PEBVRAD0; return &d->PebVradInit;
+  case THORIN_PEBVTHETAINIT: *ring = R_PEBVTHETA0; return &d->PebVthetaInit;
+  }
+  return nullptr;
+}
+
+extern "C" int thorin_gpu_set_profile(thorin_disk *d, int profile, const double *host)
+{
+  int ring;
+  std::vector<double> *v = profile_vec(d, profile, &ring);
+  if (!v || !host) return THORIN_ERR_ARG;
+  for (int i = 0; i < d->nr; i++) (*v)[i] = host[i];
+  if (ring >= 0) RCHK(upload_ring(d, ring, *v));
+  CUCHK(cudaStreamSynchronize(d->s));
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_get_profile(thorin_disk *d, int profile, double *host)
+{
+  int ring;
+  std::vector<double> *v = profile_vec(d, profile, &ring);
+  if (!v || !host) return THORIN_ERR_ARG;
+  for (int i = 0; i < d->nr; i++) host[i] = (*v)[i];
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_set_time(thorin_disk *d, double t)
+{
+  d->PhysicalTime = t;
+  d->PhysicalTimeInitial = t;
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_get_nshift(thorin_disk *d, int *host)
+{
+  for (int i = 0; i < d->nr; i++) host[i] = d->nshift_h[i];
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_get_stats(thorin_disk *d, thorin_stats *s)
+{
+  *s = d->st;
+  s->physical_time = d->PhysicalTime;
+  return THORIN_OK;
+}
+
+// EOS refresh of the state, ring-mean sound speed (and temperature), and the
+// viscosity per ring; the ring means are mirrored to the host.
+static int eos_refresh(thorin_disk *d)
+{
+  hydro_eos(d->g, d->rho, d->energy, d->temper, d->cs, d->gm1, d->gg1, d->s);
+  aux_ring_mean(d->g, d->cs, d->ring[R_CSMEAN], d->s);
+  if (d->p.alpha_flock) aux_ring_mean(d->g, d->temper, d->ring[R_TEMPMEAN], d->s);
+  aux_viscosity_rings(d->g, d->vp, d->s);
+  CUCHK(cudaMemcpyAsync(d->csmean_h, d->ring[R_CSMEAN], d->nr * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  return THORIN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Default initial state, built on the host like the reference does once
+// (InitEuler, SourceEuler.c:133-175; main.c:168-170).
+extern "C" int thorin_gpu_init_default(thorin_disk *d)
+{
+  const thorin_params &p = d->p;
+  const int nr = d->nr, ns = d->ns;
+  const size_t n = (size_t)(nr + 1) * ns;
+  std::vector<double> rho(n, 0.0), e(n, 0.0), vr(n, 0.0), vt(n, 0.0), cs(n, 0.0);
+  auto sigma = [&](double r) {            // Theo.c:15-23
+    double cavity = 1.0;
+    if (r < p.cavity_radius) cavity = 1.0 / p.cavity_ratio;
+    return cavity * p.scaling_factor * p.sigma0 * pow(r, -p.sigma_slope);
+  };
+  auto energy = [&](double r) {           // Theo.c:60-74
+    double fac = 1.0 / (1.0 * (p.adiabind - 1.0));
+    double power = -p.sigma_slope - 1.0 + 2.0 * p.flaring_index;
+    return 1.0 * p.sigma0 * pow(p.aspect_ratio, 2.0) * pow(r, power) * fac;
+  };
+  for (int i = 0; i < nr; i++) {
+    d->SigmaMed[i] = sigma(d->Rmed[i]);
+    d->SigmaInf[i] = sigma(d->Rinf[i]);
+    d->EnergyMed[i] = energy(d->Rmed[i]);
+  }
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < ns; j++) { rho[j + i * ns] = d->SigmaMed[i]; e[j + i * ns] = d->EnergyMed[i]; }
+  std::vector<double> csm(nr + 2, 0.0);
+  for (int i = 0; i < nr; i++) {
+    double sacc = 0.0;
+    for (int j = 0; j < ns; j++) {
+      const int l = j + i * ns;
+      cs[l] = sqrt(p.adiabind * (p.adiabind - 1.0) * fabs(e[l]) / rho[l]);
+      sacc += cs[l];
+    }
+    csm[i] = sacc / (double)ns;
+  }
+  // InitGasVelocity (Pframeforce.c:696-750)
+  for (int i = 0; i <= nr; i++) {
+    double r, ri;
+    int ir;
+    if (i == nr) { r = d->Rmed[nr - 1]; ri = d->Rinf[nr - 1]; ir = nr - 1; }
+    else { r = d->Rmed[i]; ri = d->Rinf[i]; ir = i; }
+    const double viscosity = fviscosity_host(d, ir, r, csm);
+    for (int j = 0; j < ns; j++) {
+      const int l = j + i * ns;
+      const double rg = r, omega = sqrt(1.0 * 1.0 / rg / rg / rg);
+      const double csl = (i == nr) ? 0.0 : cs[l];   // SoundSpeed row nrad is never set (zero)
+      vt[l] = omega * r * sqrt(1.0 - csl * csl * r / p.adiabind);
+      vt[l] -= d->OmegaFrame * r;
+      vr[l] = p.imposed_disk_drift * p.sigma0 / d->SigmaInf[i] / ri;
+      if (p.viscosity_alpha) vr[l] -= 3.0 * viscosity / r * (-p.sigma_slope + 2.0 * p.flaring_index + 1.0);
+      else vr[l] -= 3.0 * viscosity / r * (-p.sigma_slope + .5);
+    }
+  }
+  for (int j = 0; j < ns; j++) vr[j] = vr[j + ns * nr] = 0.0;
+  CUCHK(cudaMemcpyAsync(d->rho, rho.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaMemcpyAsync(d->energy, e.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaMemcpyAsync(d->vrad, vr.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaMemcpyAsync(d->vtheta, vt.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  if (p.pebbles) {
+    // EtaPressureSupport + InitPebblesViaFlux (Pebbles.c:80-275)
+    std::vector<double> etacc(n, 0.0), etafc(n, 0.0), pd(n, 0.0), pvr(n, 0.0), pvt(n, 0.0), ps(n, 0.0), tau(n, 0.0);
+    for (int i = 0; i < nr; i++) {
+      const double vtcorr = d->Rmed[i] * d->OmegaFrame, vkinv = sqrt(d->Rmed[i]);
+      for (int j = 0; j < ns; j++) {
+        const int l = j + i * ns, ljp = (j == ns - 1) ? i * ns : l + 1;
+        const double vtcc = 0.5 * (vt[l] + vt[ljp]);
+        etacc[l] = 1.0 - (vtcc + vtcorr) * vkinv;
+      }
+    }
+    for (int i = 1; i < nr; i++)
+      for (int j = 0; j < ns; j++) { const int l = j + i * ns; etafc[l] = 0.5 * (etacc[l] + etacc[l - ns]); }
+    for (int j = 0; j < ns; j++) etafc[j] = etafc[j + ns];
+    const double pebbleflux = p.pebble_flux * FLUX2CU, Ndf = 0.5, pb = p.pebble_bulk_dens / RHO2CGS;
+    for (int i = 0; i < nr; i++) {
+      double rho1 = 0, vr1 = 0, etafc1 = 0, etacc1 = 0, cs1 = 0;
+      for (int j = 0; j < ns; j++) {
+        const int l = j + i * ns;
+        rho1 += rho[l]; vr1 += vr[l]; etafc1 += etafc[l]; etacc1 += etacc[l]; cs1 += cs[l];
+      }
+      rho1 /= (double)ns; vr1 /= (double)ns; etafc1 /= (double)ns; etacc1 /= (double)ns; cs1 /= (double)ns;
+      double tau1 = sqrt(3.0) * p.pebble_coagulation * pebbleflux / (32.0 * H_PI * pow(d->Rmed[i], -1.5) * rho1);
+      tau1 = sqrt(tau1) / (d->Rmed[i] * etacc1);
+      double psize1 = fabs(tau1) * sqrt(p.adiabind) * rho1 / (2.0 * pb);
+      const double taudf = p.fragment_threshold * sqrt(d->Rmed[i]) / (2.0 * etacc1 * (1.0 - Ndf));
+      const double adf = fabs(taudf) * sqrt(p.adiabind) * rho1 / (2.0 * pb);
+      const double taufrag = p.fragment_factor / (3.0 * p.fragment_alpha) * pow(p.fragment_threshold / cs1, 2);
+      const double afrag = fabs(taufrag) * sqrt(p.adiabind) * rho1 / (2.0 * pb);
+      if ((psize1 < adf) && (psize1 < afrag)) {
+      } else if ((taudf > 0.0) && (adf < psize1) && (adf < afrag)) {
+        tau1 = taudf; psize1 = adf;
+      } else {
+        tau1 = taufrag; psize1 = afrag;
+      }
+      const double vtcorr = d->Rmed[i] * d->OmegaFrame, vkepl = pow(d->Rmed[i], -0.5);
+      const double fac = 1.0 / (tau1 * tau1 + 1.0);
+      double etaterm = etafc1 * vkepl;
+      const double pvr1 = -2.0 * tau1 * fac * (etaterm - 0.5 / tau1 * vr1);
+      etaterm = etacc1 * vkepl;
+      const double pvrtemp = -2.0 * tau1 * fac * (etaterm - 0.5 / tau1 * vr1);
+      double pvt1 = -fac * (etaterm - 0.5 * tau1 * vr1);
+      pvt1 += (vkepl - vtcorr);
+      double pdens1 = pebbleflux / (2.0 * H_PI * d->Rmed[i] * fabs(pvrtemp));
+      if (pdens1 / rho1 > p.pebble_to_gas_max) pdens1 = rho1 * p.pebble_to_gas_max;
+      for (int j = 0; j < ns; j++) {
+        const int l = j + i * ns;
+        ps[l] = psize1; tau[l] = tau1; pd[l] = pdens1; pvr[l] = pvr1; pvt[l] = pvt1;
+      }
+      d->PebDensInit[i] = pdens1;
+      d->PebVradInit[i] = pvr1;
+      d->PebVthetaInit[i] = pvt1 + d->Rmed[i] * d->OmegaFrame;
+    }
+    CUCHK(cudaMemcpyAsync(d->pdens, pd.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+    CUCHK(cudaMemcpyAsync(d->pvrad, pvr.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+    CUCHK(cudaMemcpyAsync(d->pvtheta, pvt.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+    CUCHK(cudaMemcpyAsync(d->psize, ps.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+    CUCHK(cudaMemcpyAsync(d->tau, tau.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+    CUCHK(cudaStreamSynchronize(d->s));
+  }
+  RCHK(upload_all_rings(d));
+  RCHK(eos_refresh(d));
+  CUCHK(cudaStreamSynchronize(d->s));
+  return THORIN_OK;
+}
+
+// Ring means of a device field, summed in order, to the host.
+static int ring_means_host(thorin_disk *d, const double *f, std::vector<double> &out)
+{
+  aux_ring_mean(d->g, f, d->ring[R_VMOY], d->s);
+  out.assign(d->nr + 2, 0.0);
+  CUCHK(cudaMemcpyAsync(out.data(), d->ring[R_VMOY], d->nr * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_refresh(thorin_disk *d, int flags)
+{
+  const thorin_params &p = d->p;
+  const int nr = d->nr;
+  if (flags & THORIN_REFILL_GAS) {
+    std::vector<double> m;
+    RCHK(ring_means_host(d, d->rho, m));                    // RefillSigma, Theo.c:33-57
+    for (int i = 0; i < nr; i++) d->SigmaMed[i] = m[i];
+    d->SigmaInf[0] = d->SigmaMed[0];
+    for (int i = 1; i < nr; i++)
+      d->SigmaInf[i] = (d->SigmaMed[i - 1] * (d->Rmed[i] - d->Rinf[i]) + d->SigmaMed[i] * (d->Rinf[i] - d->Rmed[i - 1])) /
+                       (d->Rmed[i] - d->Rmed[i - 1]);
+    RCHK(ring_means_host(d, d->energy, m));                 // RefillEnergy, Theo.c:82-100
+    for (int i = 0; i < nr; i++) d->EnergyMed[i] = m[i];
+  }
+  if ((flags & THORIN_REFILL_PEBBLES) && p.pebbles) {       // BckpFieldsForBC, Pebbles.c:208-232
+    std::vector<double> m;
+    RCHK(ring_means_host(d, d->pdens, m));
+    for (int i = 0; i < nr; i++) d->PebDensInit[i] = m[i];
+    RCHK(ring_means_host(d, d->pvrad, m));
+    for (int i = 0; i < nr; i++) d->PebVradInit[i] = m[i];
+    RCHK(ring_means_host(d, d->pvtheta, m));
+    for (int i = 0; i < nr; i++) d->PebVthetaInit[i] = m[i] + d->Rmed[i] * d->OmegaFrame;
+  }
+  RCHK(upload_all_rings(d));
+  RCHK(eos_refresh(d));
+  CUCHK(cudaStreamSynchronize(d->s));
+  return THORIN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host N-body step standing in for REBOUND's IAS15 (ReboundInterface.c:
+// 262-325): heliocentric -> barycentric, star + planets with mutual gravity
+// over dt (classical RK4 with 256 substeps), back to heliocentric.
+static void nbody_accel(int n, const double *m, const double *x, double *a)
+{
+  for (int i = 0; i < 3 * n; i++) a[i] = 0.0;
+  for (int i = 0; i < n; i++)
+    for (int j = i + 1; j < n; j++) {
+      double dx = x[3 * j] - x[3 * i], dy = x[3 * j + 1] - x[3 * i + 1], dz = x[3 * j + 2] - x[3 * i + 2];
+      double r2 = dx * dx + dy * dy + dz * dz, r = sqrt(r2), ir3 = 1.0 / (r2 * r);
+      a[3 * i] += 1.0 * m[j] * dx * ir3; a[3 * i + 1] += 1.0 * m[j] * dy * ir3; a[3 * i + 2] += 1.0 * m[j] * dz * ir3;
+      a[3 * j] -= 1.0 * m[i] * dx * ir3; a[3 * j + 1] -= 1.0 * m[i] * dy * ir3; a[3 * j + 2] -= 1.0 * m[i] * dz * ir3;
+    }
+}
+
+static void nbody_step(thorin_planets *sys, double dt)
+{
+  const int n = sys->nb + 1;
+  std::vector<double> m(n), x(3 * n), v(3 * n), k1x(3 * n), k1v(3 * n), xt(3 * n), ax(3 * n), sx(3 * n), sv(3 * n);
+  m[0] = 1.0;
+  for (int c = 0; c < 3; c++) { x[c] = 0.0; v[c] = 0.0; }
+  for (int k = 0; k < sys->nb; k++) {
+    m[k + 1] = sys->mass[k];
+    x[3 * k + 3] = sys->x[k]; x[3 * k + 4] = sys->y[k]; x[3 * k + 5] = sys->z[k];
+    v[3 * k + 3] = sys->vx[k]; v[3 * k + 4] = sys->vy[k]; v[3 * k + 5] = sys->vz[k];
+  }
+  double M = 0, cx[3] = {0, 0, 0}, cv[3] = {0, 0, 0};
+  for (int i = 0; i < n; i++) {
+    M += m[i];
+    for (int c = 0; c < 3; c++) { cx[c] += m[i] * x[3 * i + c]; cv[c] += m[i] * v[3 * i + c]; }
+  }
+  for (int i = 0; i < n; i++)
+    for (int c = 0; c < 3; c++) { x[3 * i + c] -= cx[c] / M; v[3 * i + c] -= cv[c] / M; }
+  const int nsteps = 256;
+  const double h = dt / nsteps;
+  static const double wts[4] = {1.0, 2.0, 2.0, 1.0}, cs[4] = {0.0, 0.5, 0.5, 1.0};
+  for (int s = 0; s < nsteps; s++) {
+    for (int q = 0; q < 3 * n; q++) { sx[q] = 0; sv[q] = 0; k1x[q] = 0; k1v[q] = 0; }
+    for (int stage = 0; stage < 4; stage++) {
+      for (int q = 0; q < 3 * n; q++) xt[q] = x[q] + cs[stage] * h * k1x[q];
+      nbody_accel(n, m.data(), xt.data(), ax.data());
+      for (int q = 0; q < 3 * n; q++) {
+        double vx = v[q] + cs[stage] * h * k1v[q];
+        k1x[q] = vx; k1v[q] = ax[q];
+        sx[q] += wts[stage] * k1x[q]; sv[q] += wts[stage] * k1v[q];
+      }
+    }
+    for (int q = 0; q < 3 * n; q++) { x[q] += h / 6.0 * sx[q]; v[q] += h / 6.0 * sv[q]; }
+  }
+  for (int k = 0; k < sys->nb; k++) {
+    sys->x[k] = x[3 * k + 3] - x[0]; sys->y[k] = x[3 * k + 4] - x[1]; sys->z[k] = x[3 * k + 5] - x[2];
+    sys->vx[k] = v[3 * k + 3] - v[0]; sys->vy[k] = v[3 * k + 4] - v[1]; sys->vz[k] = v[3 * k + 5] - v[2];
+  }
+}
+
+static double min_step_for_rebound(const thorin_planets *sys)   // ReboundInterface.c:360-385
+{
+  double dt = 1.e30;
+  for (int i = 0; i < sys->nb; i++)
+    for (int j = i + 1; j < sys->nb; j++) {
+      double dx = sys->x[i] - sys->x[j], dy = sys->y[i] - sys->y[j], dz = sys->z[i] - sys->z[j];
+      double dvx = sys->vx[i] - sys->vx[j], dvy = sys->vy[i] - sys->vy[j], dvz = sys->vz[i] - sys->vz[j];
+      double r2 = dx * dx + dy * dy + dz * dz, rv = dx * dvx + dy * dvy + dz * dvz;
+      double dtnew = fabs(r2 / rv);
+      if (dtnew < dt) dt = dtnew;
+    }
+  dt *= 0.25;
+  dt *= dt;
+  return 1.0 / dt;
+}
+
+static void rotate_psys(thorin_planets *sys, double angle)      // Psys.c:336-355
+{
+  double sint = sin(angle), cost = cos(angle);
+  for (int k = 0; k < sys->nb; k++) {
+    double xt = sys->x[k], yt = sys->y[k];
+    sys->x[k] = xt * cost + yt * sint; sys->y[k] = -xt * sint + yt * cost;
+    xt = sys->vx[k]; yt = sys->vy[k];
+    sys->vx[k] = xt * cost + yt * sint; sys->vy[k] = -xt * sint + yt * cost;
+  }
+}
+
+extern "C" int thorin_planet_from_elements(thorin_planets *sys, int k, float mass, float gas, float solid, float a,
+                                           float e, float inc, float Omega, float omega, float f)
+{
+  // SetupReboundSimulation (ReboundInterface.c:137-192) with
+  // reb_tools_orbit_to_particle (Murray & Dermott eqs. 2.122, 2.36).
+  if (!sys || k < 0 || k >= THORIN_MAXPLANETS) return THORIN_ERR_ARG;
+  const double rad = H_PI / 180.0;
+  const double m = mass, aa = a, ee = e, in = (double)inc * rad, Om = (double)Omega * rad, om = (double)omega * rad,
+               ff = (double)f * rad;
+  const double r = aa * (1 - ee * ee) / (1 + ee * cos(ff));
+  const double v0 = sqrt(1.0 * (m + 1.0) / aa / (1. - ee * ee));
+  const double cO = cos(Om), sO = sin(Om), co = cos(om), so = sin(om), cf = cos(ff), sf = sin(ff), ci = cos(in),
+               si = sin(in);
+  sys->mass[k] = m; sys->gas[k] = gas; sys->solid[k] = solid;
+  sys->x[k] = 0.0 + r * (cO * (co * cf - so * sf) - sO * (so * cf + co * sf) * ci);
+  sys->y[k] = 0.0 + r * (sO * (co * cf - so * sf) + cO * (so * cf + co * sf) * ci);
+  sys->z[k] = 0.0 + r * (so * cf + co * sf) * si;
+  sys->vx[k] = 0.0 + v0 * ((ee + cf) * (-ci * co * sO - cO * so) - sf * (co * cO - ci * so * sO));
+  sys->vy[k] = 0.0 + v0 * ((ee + cf) * (ci * co * cO - sO * so) - sf * (co * sO + ci * so * cO));
+  sys->vz[k] = 0.0 + v0 * ((ee + cf) * co * si - sf * si * so);
+  sys->ax[k] = sys->ay[k] = sys->az[k] = 0.0;
+  if (k >= sys->nb) sys->nb = k + 1;
+  return THORIN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Substep pieces
+extern "C" int thorin_gpu_cfl(thorin_disk *d, double dt_remaining, double invdtreb_sq, int *n_sub)
+{
+  const thorin_params &p = d->p;
+  if (p.pebbles) aux_stokes(d->g, d->rho, d->psize, d->tau, d->s);       // PebbleStokesNumbers
+  CflFinal f;
+  memset(&f, 0, sizeof(f));
+  f.pebbles = p.pebbles;
+  f.first_call = d->cfl_first;
+  f.deltaT = dt_remaining;
+  f.invdtreb_sq = invdtreb_sq;
+  f.minimum_step = p.minimum_step;
+  f.maximum_step = p.maximum_step;
+  f.first_step = p.first_step;
+  f.twopi_cfl_ns = 2.0 * H_PI * 0.5 / (double)d->ns;
+  aux_cfl(d->g, d->vrad, d->vtheta, d->cs, d->pvrad, d->pvtheta, d->cfl, p.pebbles, p.fast_transport,
+          (p.viscosity_alpha || p.viscosity != 0.0), d->partials, f, d->scal, d->iscal, d->s);
+  d->cfl_first = 0;
+  CUCHK(cudaMemcpyAsync(d->iscal_h, d->iscal, sizeof(int) * IS_COUNT, cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  *n_sub = d->iscal_h[IS_NSUB];
+  return THORIN_OK;
+}
+
+static int ring_of(const thorin_disk *d, double r)         // "while (Rsup[i] < r) i++"
+{
+  int i = 0;
+  while (i < d->nr - 1 && d->Rsup[i] < r) i++;
+  return i;
+}
+
+static double global_ifrac(const thorin_disk *d, double r)  // GetGlobalIFrac, LowTasks.c:21-31
+{
+  int i = 0;
+  if (r < d->GlobalRmed[0]) return 0.0;
+  if (r > d->GlobalRmed[d->nr - 1]) return (double)d->nr - 1.0;
+  while (d->GlobalRmed[i] <= r) i++;
+  return (double)i + (r - d->GlobalRmed[i - 1]) / (d->GlobalRmed[i] - d->GlobalRmed[i - 1]) - 1.0;
+}
+
+// Heating1 (Planet.c:222-247): accretion luminosity into the planet's cell.
+static void heating1(thorin_disk *d, double Mp, double dMp, double Xp, double Yp, double dt, int k)
+{
+  const thorin_params &p = d->p;
+  const int nr = d->nr, ns = d->ns;
+  const double Rperp = sqrt(Xp * Xp + Yp * Yp);
+  if (Rperp < d->Rinf[0] || Rperp > d->Rsup[nr - 1]) return;
+  const double tdelay = 4.0 * p.dt * (double)p.heating_delay;
+  double taper = d->PhysicalTime / tdelay;
+  if (taper > 1.0) taper = 1.0;
+  const double plrho = p.planetary_density / RHO2CGS;
+  const double plradius = pow(3.0 * Mp / (4.0 * H_PI * plrho), 1.0 / 3.0);
+  const double L = Mp * dMp / dt / plradius;
+  double ang = atan2(Yp, Xp);
+  if (ang < 0.0) ang += 2.0 * H_PI;
+  int i = 0;
+  while (d->Rsup[i] < Rperp) i++;
+  int j = (int)floor((double)ns / 2.0 / H_PI * ang + 0.5);
+  if (j == ns) j = 0;
+  d->heatsrc_index[k] = j + i * ns;
+  d->heatsrc[k] += L * taper / d->Surf[i];
+}
+
+extern "C" int thorin_gpu_accrete(thorin_disk *d, thorin_planets *sys, double dt)
+{
+  const thorin_params &p = d->p;
+  for (int k = 0; k < sys->nb; k++) { d->heatsrc[k] = 0.0; d->heatsrc_index[k] = -1; }   // InitHeating
+  if (!p.pebbles) return THORIN_OK;
+  if (p.accret_heating) d->heatsrc_max = sys->nb;
+  for (int k = 0; k < sys->nb; k++) {
+    AccArgs a;
+    a.pdens = d->pdens; a.macc = d->macc; a.pvr = d->pvrad; a.pvt = d->pvtheta; a.tau = d->tau; a.cs = d->cs;
+    a.vt = d->vtheta;
+    a.Xp = sys->x[k]; a.Yp = sys->y[k]; a.Zp = sys->z[k];
+    a.VXp = sys->vx[k]; a.VYp = sys->vy[k]; a.VZp = sys->vz[k];
+    a.Mp = sys->mass[k];
+    double Rp = a.Xp * a.Xp + a.Yp * a.Yp;
+    const double Rp3D = sqrt(Rp + a.Zp * a.Zp);
+    Rp = sqrt(Rp);
+    a.Rp = Rp;
+    a.Rhill = Rp3D * pow(1.0 / 3.0 * a.Mp, 1.0 / 3.0);
+    a.Omegap = pow(Rp, -1.5);
+    a.Rp15 = pow(Rp, 1.5);
+    const double ifrac = global_ifrac(d, Rp);
+    a.frac = ifrac - floor(ifrac);
+    a.iflow = (int)ifrac;
+    a.omega_frame = d->OmegaFrame;
+    a.dt = dt;
+    a.pebble_alpha = p.pebble_alpha;
+    int imax = d->nr - 1, imin = 0;
+    while (d->Rinf[imax] > (Rp + a.Rhill) && imax >= imin) imax--;
+    while (d->Rsup[imin] < (Rp - a.Rhill) && imin <= imax) imin++;
+    a.imin = imin; a.imax = imax;
+    double dMp = 0, dPx = 0, dPy = 0;
+    if (imin <= imax) {
+      aux_accrete(d->g, a, d->scal, d->s);
+      CUCHK(cudaMemcpyAsync(d->scal_h + SC_ACC_DM, d->scal + SC_ACC_DM, 3 * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+      CUCHK(cudaStreamSynchronize(d->s));
+      dMp = d->scal_h[SC_ACC_DM]; dPx = d->scal_h[SC_ACC_DPX]; dPy = d->scal_h[SC_ACC_DPY];
+    }
+    if (p.accret_heating) heating1(d, a.Mp, dMp, a.Xp, a.Yp, dt, k);
+    double PX = a.VXp * a.Mp + dPx, PY = a.VYp * a.Mp + dPy, M = a.Mp + dMp;
+    sys->mass[k] = M;
+    sys->solid[k] = sys->solid[k] + dMp;
+    sys->vx[k] = PX / M;
+    sys->vy[k] = PY / M;
+  }
+  if (p.evaporation_rate > 0.0) {                                  // EvaporatePebbles
+    double facc = p.evaporation_rate * dt;
+    if (facc > 1.0) facc = 1.0;
+    aux_evaporate(d->g, d->temper, d->pdens, facc, d->s);
+  }
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_forces(thorin_disk *d, thorin_planets *sys, double mass_taper, double indirect[2],
+                                 double *ring_rho, double *ring_cs)
+{
+  const thorin_params &p = d->p;
+  const int npl = sys->nb;
+  if (npl > MAXPL_DEV) { g_last_error = "more planets than the force kernel handles"; return THORIN_ERR_ARG; }
+  DevPlanet pl[MAXPL_DEV];
+  double axs = 0.0, ays = 0.0;
+  CUCHK(cudaStreamSynchronize(d->s));        // csmean_h is current
+  for (int k = 0; k < npl; k++) {
+    const double xpl = sys->x[k], ypl = sys->y[k], zpl = sys->z[k];
+    double mpl = sys->mass[k];
+    const double dpl = sqrt(xpl * xpl + ypl * ypl + zpl * zpl);
+    DevPlanet &P = pl[k];
+    P.x = xpl; P.y = ypl; P.z = zpl; P.m = mpl;
+    P.rhill = dpl * pow((1.0 / 3.0 * mpl), 1.0 / 3.0);
+    // ThicknessSmoothing (Force.c:75-102): ring-mean c_s at the planet's ring
+    double smoothing = 0.0;
+    const double r = sqrt(xpl * xpl + ypl * ypl);
+    if (r >= d->Rinf[0] && r <= d->Rsup[d->nr - 1]) {
+      const int i = ring_of(d, r);
+      smoothing = p.thickness_smoothing * (d->csmean_h[i] * d->OmegaInv[i] * (1.0 / sqrt(p.adiabind)));
+    }
+    P.Hpl = smoothing / p.thickness_smoothing;
+    P.smoothing2 = smoothing * smoothing;
+    const double rst = 0.5 * P.rhill;
+    P.rst2 = rst * rst; P.rst3 = P.rst2 * rst; P.rst4 = P.rst3 * rst;
+    const double rsm = 0.05 * P.rhill;
+    P.rsm2 = rsm * rsm;
+    P.rmorevert2 = 2.0 * P.rhill;
+    P.rmorevert2 *= P.rmorevert2;
+    if (p.indirect_term) {
+      const double invdpl3 = 1.0 / (dpl * dpl * dpl);
+      mpl *= mass_taper;
+      axs += mpl * invdpl3 * xpl;
+      ays += mpl * invdpl3 * ypl;
+    }
+  }
+  if (npl > 0) CUCHK(cudaMemcpyAsync(d->planets_d, pl, npl * sizeof(DevPlanet), cudaMemcpyHostToDevice, d->s));
+  ForceArgs a;
+  a.rho = d->rho; a.cs = d->cs; a.tau = d->tau; a.pdens = d->pdens;
+  a.agr = d->agr; a.agt = d->agt; a.pagr = d->pagr; a.pagt = d->pagt;
+  a.part = d->partials;
+  a.pl = d->planets_d;
+  a.npl = npl; a.pebbles = p.pebbles; a.exclude_hill = p.exclude_hill; a.pebble_gravity = p.pebble_gravity;
+  a.mass_taper = mass_taper; a.pebble_alpha = p.pebble_alpha; a.hillcut = p.hillcut;
+  const double indx_pl = p.indirect_term ? -axs : 0.0, indy_pl = p.indirect_term ? -ays : 0.0;
+  aux_forces(d->g, a, d->fr, indx_pl, indy_pl, d->scal, d->s);
+  // DampingTW04 needs the ring means of Sigma (and c_s) at each planet
+  for (int k = 0; k < npl; k++) {
+    const double r = sqrt(sys->x[k] * sys->x[k] + sys->y[k] * sys->y[k]);
+    if (ring_rho) ring_rho[k] = 0.0;
+    if (ring_cs) ring_cs[k] = 0.0;
+    if (r >= d->Rinf[0] && r <= d->Rsup[d->nr - 1]) {
+      const int i = ring_of(d, r);
+      aux_ring_mean_at(d->g, d->rho, i, d->scal + SC_PLANET_A + 2 * MAXPL_DEV + k, d->s);
+      if (ring_cs) ring_cs[k] = d->csmean_h[i];
+    }
+  }
+  CUCHK(cudaMemcpyAsync(d->scal_h, d->scal, 128 * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  for (int k = 0; k < npl; k++) {
+    sys->ax[k] = d->scal_h[SC_PLANET_A + 2 * k];
+    sys->ay[k] = d->scal_h[SC_PLANET_A + 2 * k + 1];
+    const double r = sqrt(sys->x[k] * sys->x[k] + sys->y[k] * sys->y[k]);
+    if (ring_rho && r >= d->Rinf[0] && r <= d->Rsup[d->nr - 1]) ring_rho[k] = d->scal_h[SC_PLANET_A + 2 * MAXPL_DEV + k];
+  }
+  // IndirectTerm of the disk (the planets' part is only added to the gas)
+  indirect[0] = d->scal_h[SC_INDX];
+  indirect[1] = d->scal_h[SC_INDY];
+  return THORIN_OK;
+}
+
+// SuccessiveOverrelaxation driver: residual, then sweeps launched in chunks;
+// converged sweeps turn later launches into no-ops.
+static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *capped)
+{
+  const thorin_params &p = d->p;
+  hydro_sor_resid0(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor, d->s);
+  int first = 1, chunk = hint > 0 ? hint : 4;
+  *capped = 0;
+  for (;;) {
+    hydro_sor_sweeps(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor, omega, p.sor_eps, first,
+                     chunk, p.sor_maxiters, d->s);
+    CUCHK(cudaMemcpyAsync(d->iscal_h + IS_SOR_DONE, d->sor.done, 2 * sizeof(int), cudaMemcpyDeviceToHost, d->s));
+    CUCHK(cudaStreamSynchronize(d->s));
+    const int done = d->iscal_h[IS_SOR_DONE];
+    if (done) {
+      *niter = d->iscal_h[IS_SOR_DONE + 1];
+      *capped = (done == 2);
+      return THORIN_OK;
+    }
+    first += chunk;
+    if (first > p.sor_maxiters) { *niter = p.sor_maxiters; *capped = 1; return THORIN_OK; }
+    chunk = chunk < 64 ? 2 * chunk : 64;
+  }
+}
+
+// IterateRelaxationParameter (EnergySources.c:340-403).
+static int iterate_relaxation(thorin_disk *d)
+{
+  const thorin_params &p = d->p;
+  const int nsplit = 9;
+  int count = 0, Niter, capped;
+  double omegamin = 1.0, omega = 1.0, omegamax = TH_OMEGAUPPER;
+  const size_t bytes = (size_t)d->nr * d->ns * sizeof(double);
+  CUCHK(cudaMemcpyAsync(d->tbackup, d->temper, bytes, cudaMemcpyDeviceToDevice, d->s));
+  d->domega = (omegamax - omegamin) / nsplit;
+  d->Niterbest = p.sor_maxiters;
+  d->omegabest = 1.0;
+  for (int outer = 0;; outer++) {
+    if (outer >= 1000) { g_last_error = "omega calibration did not settle"; return THORIN_ERR_OMEGA; }
+    for (int n = 0; n <= nsplit; n++) {
+      RCHK(sor_solve(d, omega, d->Niterbest < p.sor_maxiters ? d->Niterbest : 4, &Niter, &capped));
+      d->st.sor_sweeps += Niter;
+      if (Niter == d->Niterbest) count++;
+      if (Niter < d->Niterbest) { d->Niterbest = Niter; d->omegabest = omega; }
+      omega += d->domega;
+      CUCHK(cudaMemcpyAsync(d->temper, d->tbackup, bytes, cudaMemcpyDeviceToDevice, d->s));
+    }
+    if (d->Niterbest == p.sor_maxiters) { g_last_error = "SOR did not converge when estimating omega"; return THORIN_ERR_OMEGA; }
+    if (count == nsplit + 1) { d->domega = omegamax - omegamin; return THORIN_OK; }
+    count = 0;
+    omegamin = d->omegabest - d->domega;
+    omegamax = d->omegabest + d->domega;
+    if (omegamin < 1.0) omegamin = 1.0;
+    if (omegamax > TH_OMEGAUPPER) omegamax = TH_OMEGAUPPER;
+    d->domega = (omegamax - omegamin) / nsplit;
+    omega = omegamin;
+  }
+}
+
+// SubStep3 + ImplicitRadiativeDiffusion (SourceEuler.c:508-586,
+// EnergySources.c:201-335).  Leaves the new energy in d->energy.
+static int energy_step(thorin_disk *d, double dt)
+{
+  const thorin_params &p = d->p;
+  hydro_qplus(d->g, d->vrad, d->vtheta, d->rho, d->divv, d->qplus, d->invdphi, d->lr01, d->lr12, d->s);
+  hydro_eos(d->g, d->rho, d->energy_int, d->temper, d->cs, d->gm1, d->gg1, d->s);
+  hydro_diffcoef(d->g, d->rho, d->temper, d->cs, d->opacity, d->qminus, d->dcen, d->partials, p.opacity_law,
+                 p.parametric_opacity * OPA2CU, p.parametric_opacity, p.opacity_drop, d->taueff_c,
+                 d->ring[R_INVDXTHETA], d->ring[R_DELTAR2], d->s);
+  aux_min_final(d->partials, hydro_diffcoef_blocks(d->g), d->scal + SC_DTSTELLAR, d->s);
+  if (p.stellar_irradiation)
+    hydro_irradiation(d->g, d->rho, d->cs, d->opacity, d->flaring, d->qirr, d->rstar, d->tirr4fac, p.opacity_drop,
+                      d->taueff_c, d->ring[R_RINF15], d->ring[R_RSUP15], d->s);
+  int nheat = 0;
+  if (p.accret_heating || p.gas_accret_heating) {
+    nheat = d->heatsrc_max;
+    if (nheat > 0) {
+      CUCHK(cudaMemcpyAsync(d->heat_idx_d, d->heatsrc_index, nheat * sizeof(int), cudaMemcpyHostToDevice, d->s));
+      CUCHK(cudaMemcpyAsync(d->heat_val_d, d->heatsrc, nheat * sizeof(double), cudaMemcpyHostToDevice, d->s));
+    }
+  }
+  hydro_matrix(d->g, d->rho, d->temper, d->cs, d->dcen, d->divv, d->qminus, d->qplus, d->qirr, d->ml, d->mlip, d->mlim,
+               d->mljp, d->mljm, d->rhs, dt, d->gm1, d->ring[R_INVDXTHETA2], p.stellar_irradiation, nheat,
+               d->heat_idx_d, d->heat_val_d, d->s);
+  if (d->sor_first) {
+    d->sor_first = 0;
+    RCHK(iterate_relaxation(d));
+    d->omega = d->omegabest;
+    d->Niterlast = d->Niterbest;
+  }
+  d->omega += d->domega;
+  if (d->omega > TH_OMEGAUPPER) { d->omega = TH_OMEGAUPPER; d->domega = -d->domega; }
+  if (d->omega < 1.0) { d->omega = 1.0; d->domega = -d->domega; }
+  int Niter, capped;
+  RCHK(sor_solve(d, d->omega, d->Niterlast, &Niter, &capped));
+  d->st.sor_calls++;
+  d->st.sor_sweeps += Niter;
+  d->st.sor_last_niter = Niter;
+  d->st.sor_omega = d->omega;
+  if (Niter > d->Niterlast) d->domega = -d->domega;
+  d->Niterlast = Niter;
+  hydro_energy_from_t(d->g, d->rho, d->temper, d->energy_new, d->s);
+  std::swap(d->energy, d->energy_new);
+  return capped ? THORIN_ERR_SOR_MAXIT : THORIN_OK;
+}
+
+static void transport_fluid(thorin_disk *d, double **rho, double *vr, double *vt, double **energy, double **rho_scratch,
+                            double dt, int gas)
+{
+  TransportScratch S = d->ts;
+  S.rho_new = *rho_scratch;
+  S.e_new = energy ? d->t_e_gas : nullptr;
+  hydro_transport(d->g, rho, vr, vt, energy, S, dt, d->OmegaFrame, d->p.fast_transport,
+                  gas && d->p.damping && d->p.damp_vrad, d->drin, d->drout, gas ? d->temper : nullptr, d->cs, d->gm1,
+                  d->gg1, d->s);
+  std::swap(*rho, *rho_scratch);
+  if (energy) std::swap(*energy, d->t_e_gas);
+}
+
+extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
+{
+  const thorin_params &p = d->p;
+  const int damp = p.damping;
+  // ApplyBoundaryCondition, DetectCrash (SourceEuler.c:271-289)
+  if (damp) aux_damp_gas(d->g, d->vrad, d->rho, d->vtheta, d->energy, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, 0,
+                         p.energy_eq, d->s);
+  CUCHK(cudaMemsetAsync(d->iscal + IS_CRASH, 0, sizeof(int), d->s));
+  aux_crash(d->g, p.pebbles ? d->pdens : d->energy, d->iscal + IS_CRASH, d->s);
+  // SourceTermsPebbles (Pebbles.c:550-613)
+  if (p.pebbles) {
+    aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, d->s);
+    aux_pebble_sources(d->g, d->pdens, d->pvrad, d->pvtheta, d->tau, d->vrad, d->vtheta, d->pagr, d->pagt, d->paccr,
+                       d->pacct, d->dragr, d->dragt, d->OmegaFrame, p.back_reaction, d->s);
+  }
+  // SubStep1 with viscous terms (SourceEuler.c:319-415)
+  hydro_substep1(d->g, d->rho, d->vrad, d->vtheta, d->energy, d->agr, d->agt, d->dragr, d->dragt, d->vrad_int,
+                 d->vtheta_int, d->gaccr, d->gacct, dt, d->OmegaFrame, d->gm1, p.pebbles, p.back_reaction,
+                 d->ring[R_SUPPTORQUE], d->ring[R_INVDXTHETA], d->s);
+  hydro_stress(d->g, d->vrad_int, d->vtheta_int, d->rho, d->divv, d->trr, d->tpp, d->trp, d->invdphi, d->s);
+  const int kepler = (!p.damping) || (p.damping && p.damp_vrad);
+  hydro_visc_update(d->g, d->vrad_int, d->vtheta_int, d->rho, d->trr, d->tpp, d->trp, dt, d->invdphi, kepler,
+                    d->vkep_in, d->vkep_out, d->s);
+  if (p.pebbles)
+    aux_pebble_substep1(d->g, d->pvrad, d->pvtheta, d->tau, d->vrad, d->vtheta, d->paccr, d->pacct, d->gaccr, d->gacct,
+                        d->rho, d->pdens, dt, p.diffusive_particles, p.schmidt_number, d->ring[R_INVDXTHETA], d->s);
+  // SubStep2, ActualiseGas, ApplyBoundaryCondition
+  hydro_substep2(d->g, d->rho, d->vrad_int, d->vtheta_int, d->energy, d->vrad_new, d->vtheta_new, d->energy_int, dt,
+                 p.energy_eq, d->ring[R_INVDXTHETA], d->s);
+  std::swap(d->vrad, d->vrad_new);
+  std::swap(d->vtheta, d->vtheta_new);
+  if (damp) aux_damp_gas(d->g, d->vrad, d->rho, d->vtheta, d->energy, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, 0,
+                         p.energy_eq, d->s);
+  int status = THORIN_OK;
+  if (p.energy_eq) {
+    int s = energy_step(d, dt);
+    if (s != THORIN_OK && s != THORIN_ERR_SOR_MAXIT) return s;
+    status = s;
+  }
+  // Transport, ApplyBoundaryCondition, ComputeTemperatureField, ComputeSoundSpeed
+  transport_fluid(d, &d->rho, d->vrad, d->vtheta, p.energy_eq ? &d->energy : nullptr, &d->t_rho_gas, dt, 1);
+  CUCHK(cudaMemcpyAsync(d->nshift_h.data(), d->nshift, d->nr * sizeof(int), cudaMemcpyDeviceToHost, d->s));
+  aux_ring_mean(d->g, d->cs, d->ring[R_CSMEAN], d->s);
+  if (p.alpha_flock) aux_ring_mean(d->g, d->temper, d->ring[R_TEMPMEAN], d->s);
+  aux_viscosity_rings(d->g, d->vp, d->s);
+  CUCHK(cudaMemcpyAsync(d->csmean_h, d->ring[R_CSMEAN], d->nr * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  // EvolvePebbleDisk (Pebbles.c:702-708)
+  if (p.pebbles) {
+    aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, d->s);
+    transport_fluid(d, &d->pdens, d->pvrad, d->pvtheta, nullptr, &d->t_rho_peb, dt, 0);
+    aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, d->s);
+  }
+  CUCHK(cudaMemcpyAsync(d->iscal_h + IS_CRASH, d->iscal + IS_CRASH, sizeof(int), cudaMemcpyDeviceToHost, d->s));
+  d->PhysicalTime += dt;
+  d->st.last_dt = dt;
+  return status;
+}
+
+// AdvanceSystemFromDisk (Pframeforce.c:514-566) with DampingTW04 (:571-603).
+static void advance_from_disk(thorin_disk *d, thorin_planets *sys, double dt, const double ind[2], const double *rrho,
+                              const double *rcs)
+{
+  for (int k = 0; k < sys->nb; k++) {
+    if (!sys->feel_disk[k]) continue;
+    const double x = sys->x[k], y = sys->y[k], z = sys->z[k], vz = sys->vz[k], m = sys->mass[k];
+    double damp = 0.0;
+    const double r = sqrt(x * x + y * y);
+    if ((d->p.vertical_damping > 0.0) && (r >= d->Rinf[0] && r <= d->Rsup[d->nr - 1])) {
+      const double cs4inv = pow(rcs[k], -4.0), Omega = pow(r, -1.5);
+      damp = d->p.vertical_damping * m * rrho[k] * Omega * cs4inv * (-2.176 * vz - 0.871 * z * Omega);
+    }
+    sys->vx[k] += dt * sys->ax[k];
+    sys->vy[k] += dt * sys->ay[k];
+    sys->vz[k] += dt * (sys->az[k] + damp);
+    sys->vx[k] += dt * ind[0];
+    sys->vy[k] += dt * ind[1];
+  }
+}
+
+extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
+{
+  const thorin_params &p = d->p;
+  const double DT = p.dt;
+  double dtemp = 0.0, dt;
+  int nsub = 0, status = THORIN_OK;
+  if (!sys || sys->nb > MAXPL_DEV) { g_last_error = "planetary system missing or too large"; return THORIN_ERR_ARG; }
+  while (dtemp < 0.999999999 * DT) {
+    d->MassTaper = d->PhysicalTime / (p.mass_taper * 2.0 * H_MPI);
+    d->MassTaper = (d->MassTaper > 1.0 ? 1.0 : pow(sin(d->MassTaper * H_MPI / 2.0), 2.0));
+    const double invdtreb_sq = min_step_for_rebound(sys);
+    int n;
+    RCHK(thorin_gpu_cfl(d, DT - dtemp, invdtreb_sq, &n));
+    dt = (DT - dtemp) / (double)n;
+    RCHK(thorin_gpu_accrete(d, sys, dt));
+    dtemp += dt;
+    double ind[2], rrho[THORIN_MAXPLANETS], rcs[THORIN_MAXPLANETS];
+    RCHK(thorin_gpu_forces(d, sys, d->MassTaper, ind, rrho, rcs));
+    advance_from_disk(d, sys, dt, ind, rrho, rcs);
+    nbody_step(sys, dt);
+    rotate_psys(sys, d->OmegaFrame * dt);
+    int s = thorin_gpu_hydro(d, dt);
+    if (s != THORIN_OK && s != THORIN_ERR_SOR_MAXIT) return s;
+    if (s != THORIN_OK) status = s;
+    nsub++;
+  }
+  CUCHK(cudaStreamSynchronize(d->s));
+  d->st.substeps = nsub;
+  d->st.crashed = d->iscal_h[IS_CRASH];
+  return status;
+}
+
+extern "C" int thorin_gpu_integrals(thorin_disk *d, double *mass, double *momentum, double *energy, double *peb_mass,
+                                    double *peb_momentum)
+{
+  aux_integrals(d->g, d->rho, d->vrad, d->vtheta, d->energy, d->pdens, d->pvtheta, d->OmegaFrame, d->p.pebbles,
+                d->partials, d->scal, d->s);
+  CUCHK(cudaMemcpyAsync(d->scal_h + SC_MASS, d->scal + SC_MASS, 5 * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  if (mass) *mass = d->scal_h[SC_MASS];
+  if (momentum) *momentum = d->scal_h[SC_MOM];
+  if (energy) *energy = d->scal_h[SC_ENER];
+  if (peb_mass) *peb_mass = d->scal_h[SC_PMASS];
+  if (peb_momentum) *peb_momentum = d->scal_h[SC_PMOM];
+  return THORIN_OK;
+}

@@ -1,0 +1,113 @@
+// thorin_dev.cuh -- device-side layout and helpers shared by the kernels.
+//
+// One disk lives on one GPU.  Every 2D field uses the reference's PolarGrid
+// layout (src_main/LowTasks.c:73-103): (nrad+1) rows of nsec FP64 values,
+// azimuth contiguous, l = j + i*nsec; row nrad is the outer v_rad face.
+// Ring (1D) arrays hold nrad+2 values; entries the reference never sets stay
+// zero, like its zero-initialised MAX1D globals.
+//
+// All kernels are compiled with --fmad=false: the reference is built with
+// -std=c99, where gcc does not contract a*b+c, so keeping every multiply and
+// add separately rounded makes most per-cell results bit-identical.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../../include/thorin_gpu.h"
+
+#define TH_PI 3.14159265358979323844
+#define TH_MPI 3.14159265358979323846
+#define TH_CFLSECURITY 0.5
+#define TH_CVNR 1.41
+#define TH_SORMIN 1.0e-15
+#define TH_SORPRECISION 1.0e-15
+#define TH_OMEGAUPPER 1.9
+#define TH_KAPPAFLOOR 1.0e-12
+#define TH_FULL 0xffffffffu
+
+// Unit constants of src_main/fondam.h, evaluated once on the host with the
+// host libm (so they are the reference's bits) and passed in DevConst.
+struct DevConst {
+  double opa2cu, t2si, rho2cgs, sigma_sb, sqrt2pi_inv, pebbulkdens, cv, sqrt_adiabind_inv;
+  double evaptemp;           // EVAPORATIONTEMPERATURE / T2SI
+  double sqrt3;              // sqrt(3.0)
+};
+
+// Ring arrays (device pointers, nrad+2 entries each).
+struct DevRings {
+  const double *Rinf, *Rsup, *Rmed, *Surf, *InvRmed, *InvSurf, *InvDiffRmed, *InvDiffRsup, *InvRinf;
+  const double *OmegaInv, *Rmed2, *WaveKiller;
+  const double *Rmed15, *Rinf15;        // pow(Rmed,1.5), pow(Rinf,1.5) (FViscosity)
+  const double *costab, *sintab;         // cos/sin(2 pi j / nsec), nsec entries
+  const double *SigmaMed, *EnergyMed, *VthetaMed;
+  const double *PebDensInit, *PebVradInit, *PebVthetaInit;
+  double *csmean;                        // globcsvec   (ring mean of c_s)
+  double *tempmean;                      // globtempervec
+  double *nu_med, *nu_inf;               // FViscosity(Rmed[i]), FViscosity(Rinf[i])
+};
+
+struct DevGrid {
+  int nr, ns;
+  DevRings r;
+  DevConst k;
+};
+
+__device__ __forceinline__ int jp_of(int j, int ns) { return (j == ns - 1) ? 0 : j + 1; }
+__device__ __forceinline__ int jm_of(int j, int ns) { return (j == 0) ? ns - 1 : j - 1; }
+
+// Sum of row[0..n) in strictly left-to-right order (the reference's
+// sequential ring sums, e.g. mpi_make1Dprofile, mpiTasks.c:26-32), computed by
+// one warp: lanes load coalesced chunks, the running sum walks the chunk in
+// order through shuffles.  All lanes return the sum.
+__device__ __forceinline__ double warp_seq_sum(const double *row, int n)
+{
+  const int lane = threadIdx.x & 31;
+  double acc = 0.0;
+  for (int base = 0; base < n; base += 32) {
+    double v = (base + lane < n) ? row[base + lane] : 0.0;
+    int cnt = n - base < 32 ? n - base : 32;
+    for (int k = 0; k < cnt; k++) acc += __shfl_sync(TH_FULL, v, k);
+  }
+  return acc;
+}
+
+// Block-wide reductions (fixed order: warp shuffles then warp partials) -----
+template <typename T, typename Op>
+__device__ __forceinline__ T warp_reduce(T v, Op op)
+{
+  for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_down_sync(TH_FULL, v, o));
+  return v;
+}
+
+struct OpAdd { __device__ double operator()(double a, double b) const { return a + b; } };
+struct OpMin { __device__ double operator()(double a, double b) const { return b < a ? b : a; } };
+struct OpMax { __device__ double operator()(double a, double b) const { return b > a ? b : a; } };
+struct OpAddI { __device__ int operator()(int a, int b) const { return a + b; } };
+
+// Result valid in thread 0.  blockDim.x must be a multiple of 32 (<= 1024).
+template <typename T, typename Op>
+__device__ T block_reduce(T v, Op op, T identity)
+{
+  __shared__ T sh[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_reduce(v, op);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : identity;
+  if (wid == 0) v = warp_reduce(v, op);
+  return v;
+}
+
+// x^3 correctly rounded (Dekker two-product with fma): the reference uses
+// pow(T, 3.0) (EnergySources.c:95,590), which glibc returns correctly
+// rounded in all but vanishingly rare cases.
+__device__ __forceinline__ double cube_rn(double x)
+{
+  double h = x * x;
+  double l = __fma_rn(x, x, -h);          // x*x = h + l exactly
+  double p = h * x;
+  double e = __fma_rn(h, x, -p);          // h*x = p + e exactly
+  double t = __fma_rn(l, x, e);           // remaining terms
+  return __dadd_rn(p, t);
+}

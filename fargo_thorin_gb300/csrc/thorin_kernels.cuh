@@ -1,0 +1,150 @@
+// thorin_kernels.cuh -- argument structs and host launchers of the kernels.
+#pragma once
+#include "thorin_dev.cuh"
+
+#define MAXPL_DEV 8            // planets handled by the force kernel (per-thread arrays)
+
+// Planet data seen by the kernels (per-planet constants from the host).
+struct DevPlanet {
+  double x, y, z, m, rhill, Hpl, smoothing2, rst2, rst3, rst4, rsm2, rmorevert2;
+};
+
+// Indices into the small device scalar buffer.
+enum {
+  SC_NEWDT = 0, SC_INVDTPEB, SC_DTSTELLAR, SC_INDX, SC_INDY, SC_ACC_DM, SC_ACC_DPX, SC_ACC_DPY, SC_RINGRHO,
+  SC_MASS, SC_MOM, SC_ENER, SC_PMASS, SC_PMOM, SC_NORMRES0, SC_NORMRES,
+  SC_PLANET_A = 32            // 2 per planet: ax, ay
+};
+enum { IS_NSUB = 0, IS_SOR_DONE, IS_SOR_NITER, IS_SOR_CHANGED, IS_CRASH, IS_COUNT };
+
+// Red-black SOR control block (device pointers).
+struct SorCtl {
+  double *part;           // [2][nblocks] partial |resid| sums
+  int *ipart;             // [2][nblocks] partial changed counts
+  unsigned int *ticket;
+  int *done;              // 1 converged, 2 iteration cap; later sweeps are no-ops
+  int *niter;
+  double *normres0;
+  double *normres;
+  int *changed;
+};
+
+// Transport scratch (device fields).
+struct TransportScratch {
+  double *mom[4];          // RadMomP, RadMomM, ThetaMomP, ThetaMomM (updated in place)
+  double *rho_new, *e_new;
+  double *w[6], *d[7], *f[7];
+  int *nshift;
+  double *vmed;
+};
+
+struct PtrPack7 { const double *src[7]; double *dst[7]; int n; };
+struct AziQ { double *q[6]; int n; };   // q[n-1] is the density
+
+struct ViscParams {
+  double viscosity, alpha, alpha_mri, alpha_dead, tmri, twidth, t2si;
+  double cav_rmin, cav_rmax, cav_ratio, log_cav_ratio;
+  int viscosity_alpha, alpha_flock;
+};
+
+struct CflRings {
+  const double *dxrad, *dxtheta, *mindx, *den5;    // per ring, ConditionCFL's expressions
+  double *vmoy, *pvtmed;                           // ring means (scratch)
+};
+
+struct CflFinal {
+  int nb, pebbles, first_call;
+  double deltaT, invdtreb_sq, minimum_step, maximum_step, first_step, twopi_cfl_ns;
+};
+
+struct ForceRings { double *H_avr, *sigma_avr, *integstar_avr, *p_H_avr, *p_integstar_avr; };
+
+struct ForceArgs {
+  const double *rho, *cs, *tau, *pdens;
+  double *agr, *agt, *pagr, *pagt;
+  double *part;               // [nblocks][2 + 2*npl]
+  const DevPlanet *pl;
+  int npl, pebbles, exclude_hill, pebble_gravity;
+  double mass_taper, pebble_alpha, hillcut;
+};
+
+struct AccArgs {
+  double *pdens, *macc;
+  const double *pvr, *pvt, *tau, *cs, *vt;
+  double Xp, Yp, Zp, VXp, VYp, VZp, Mp, Rp, Rhill, Omegap, Rp15, omega_frame, dt, pebble_alpha, frac;
+  int imin, imax, iflow;
+};
+
+// kernels_hydro.cu
+void hydro_substep1(const DevGrid &g, const double *rho, const double *vrad, const double *vtheta,
+                    const double *energy, const double *agr, const double *agt, const double *dragr, const double *dragt,
+                    double *vradint, double *vthetaint, double *gaccr, double *gacct, double dt, double omega_frame,
+                    double gm1, int pebbles, int back_reaction, const double *supp_torque, const double *invdxtheta_r,
+                    cudaStream_t s);
+void hydro_stress(const DevGrid &g, const double *vr, const double *vt, const double *rho, double *divv, double *trr,
+                  double *tpp, double *trp, double invdphi, cudaStream_t s);
+void hydro_visc_update(const DevGrid &g, double *vr, double *vt, const double *rho, const double *trr, const double *tpp,
+                       const double *trp, double dt, double invdphi, int kepler, double vkin, double vkout,
+                       cudaStream_t s);
+void hydro_substep2(const DevGrid &g, const double *rho, const double *vr, const double *vt, const double *energy,
+                    double *vrnew, double *vtnew, double *eint, double dt, int energy_eq, const double *invdxtheta_r,
+                    cudaStream_t s);
+void hydro_qplus(const DevGrid &g, const double *vr, const double *vt, const double *rho, double *divv, double *qplus,
+                 double invdphi, double lr01, double lr12, cudaStream_t s);
+void hydro_eos(const DevGrid &g, const double *rho, const double *energy, double *temper, double *cs, double gm1,
+               double gg1, cudaStream_t s);
+int hydro_diffcoef_blocks(const DevGrid &g);
+void hydro_diffcoef(const DevGrid &g, const double *rho, const double *T, const double *cs, double *opacity,
+                    double *qminus, double *dcen, double *dtmin_part, int law, double parametric_cu,
+                    double parametric_raw, double opacity_drop, double taueff_c, const double *invdxtheta_r,
+                    const double *deltar2_r, cudaStream_t s);
+void hydro_irradiation(const DevGrid &g, const double *rho, const double *cs, const double *opacity, double *flaring,
+                       double *qirr, double rstar, double tirr4fac, double opacity_drop, double taueff_c,
+                       const double *rinf15, const double *rsup15, cudaStream_t s);
+void hydro_matrix(const DevGrid &g, const double *rho, const double *T, const double *cs, const double *dcen,
+                  const double *divv, const double *qminus, const double *qplus, const double *qirr, double *ml,
+                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs, double dt, double gm1,
+                  const double *invdxtheta2_r, int irradiation, int nheat, const int *heat_idx, const double *heat_val,
+                  cudaStream_t s);
+int sor_blocks(const DevGrid &g);
+void hydro_sor_resid0(const DevGrid &g, const double *T, const double *ml, const double *mlip, const double *mlim,
+                      const double *mljp, const double *mljm, const double *rhs, const SorCtl &c, cudaStream_t s);
+void hydro_sor_sweeps(const DevGrid &g, double *T, const double *ml, const double *mlip, const double *mlim,
+                      const double *mljp, const double *mljm, const double *rhs, const SorCtl &c, double omega,
+                      double eps, int first, int count, int maxiters, cudaStream_t s);
+void hydro_energy_from_t(const DevGrid &g, const double *rho, double *T, double *enew, cudaStream_t s);
+void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, double **energy, const TransportScratch &S,
+                     double dt, double omega_frame, int fast, int damp_vrad, double drin, double drout, double *temper,
+                     double *cs, double gm1, double gg1, cudaStream_t s);
+int hydro_azimuthal_smem(int ns);
+void hydro_set_smem_limits(int ns);
+
+// kernels_aux.cu
+void aux_ring_mean(const DevGrid &g, const double *f, double *out, cudaStream_t s);
+void aux_ring_mean_at(const DevGrid &g, const double *f, int ring, double *out, cudaStream_t s);
+void aux_viscosity_rings(const DevGrid &g, const ViscParams &v, cudaStream_t s);
+void aux_stokes(const DevGrid &g, const double *rho, const double *psize, double *tau, cudaStream_t s);
+void aux_cfl(const DevGrid &g, const double *vr, const double *vt, const double *cs, const double *pvr, const double *pvt,
+             const CflRings &cr, int pebbles, int fast, int viscous, double *part, const CflFinal &f0, double *scal,
+             int *iscal, cudaStream_t s);
+void aux_evaporate(const DevGrid &g, const double *T, double *pdens, double facc, cudaStream_t s);
+void aux_damp_gas(const DevGrid &g, double *vrad, double *rho, double *vtheta, double *energy, const int *rings,
+                  int nrings, double dt, double omega_frame, int damp_init, int energy_eq, cudaStream_t s);
+void aux_damp_peb(const DevGrid &g, double *pd, double *pvr, double *pvt, const int *rings, int nrings, double dt,
+                  double omega_frame, cudaStream_t s);
+void aux_crash(const DevGrid &g, const double *f, int *flag, cudaStream_t s);
+void aux_pebble_sources(const DevGrid &g, const double *pd, const double *pvr, const double *pvt, const double *tau,
+                        const double *vr, const double *vt, const double *pagr, const double *pagt, double *paccr,
+                        double *pacct, double *dragr, double *dragt, double omega_frame, int back_reaction,
+                        cudaStream_t s);
+void aux_pebble_substep1(const DevGrid &g, double *pvr, double *pvt, const double *tau, const double *vr, const double *vt,
+                         const double *paccr, const double *pacct, const double *gaccr, const double *gacct,
+                         const double *rho, const double *pd, double dt, int diffusion, double schmidt,
+                         const double *invdxtheta_r, cudaStream_t s);
+void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr, double indx_pl, double indy_pl,
+                double *scal, cudaStream_t s);
+void aux_accrete(const DevGrid &g, const AccArgs &a, double *scal, cudaStream_t s);
+void aux_integrals(const DevGrid &g, const double *rho, const double *vr, const double *vt, const double *e,
+                   const double *pd, const double *pvt, double omega_frame, int pebbles, double *part, double *scal,
+                   cudaStream_t s);
+void aux_min_final(const double *part, int nb, double *out, cudaStream_t s);

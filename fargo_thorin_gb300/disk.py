@@ -1,0 +1,80 @@
+"""Host-side handle of one disk resident on the GPU (C ABI wrapper)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .params import ThorinParams, ThorinPlanets, ThorinStats
+
+
+class GpuDisk:
+    """One FARGO_THORIN disk advanced by the sm_103a kernels.
+
+    The methods mirror the reference's hydro entry points: ``algogas``
+    advances one DT like AlgoGas (src_main/SourceEuler.c:210-317) with the
+    planets integrated on the host; ``init_default`` builds the initial state
+    of InitEuler; ``refresh`` recomputes derived fields after fields were
+    replaced (InitializeFromFile / restart paths of src_main/Init.c)."""
+
+    def __init__(self, params: ThorinParams):
+        self.L = _lib.load()
+        self.p = params
+        self.nr, self.ns = params.nrad, params.nsec
+        self.h = C.c_void_p()
+        _lib.check(self.L.thorin_gpu_create(C.byref(params), C.byref(self.h)), "thorin_gpu_create")
+
+    def close(self):
+        if self.h:
+            self.L.thorin_gpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init_default(self):
+        _lib.check(self.L.thorin_gpu_init_default(self.h), "thorin_gpu_init_default")
+
+    def refresh(self, flags: int):
+        _lib.check(self.L.thorin_gpu_refresh(self.h, flags), "thorin_gpu_refresh")
+
+    def get(self, fid: int) -> np.ndarray:
+        out = np.zeros((self.nr + 1) * self.ns)
+        _lib.check(self.L.thorin_gpu_download(self.h, fid, out.ctypes.data_as(C.POINTER(C.c_double))), "download")
+        return out
+
+    def set(self, fid: int, values: np.ndarray):
+        cur = self.get(fid)
+        v = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        cur[: v.size] = v
+        _lib.check(self.L.thorin_gpu_upload(self.h, fid, cur.ctypes.data_as(C.POINTER(C.c_double))), "upload")
+
+    def upload(self, fid: int, full: np.ndarray):
+        a = np.ascontiguousarray(full, dtype=np.float64)
+        assert a.size == (self.nr + 1) * self.ns
+        _lib.check(self.L.thorin_gpu_upload(self.h, fid, a.ctypes.data_as(C.POINTER(C.c_double))), "upload")
+
+    def set_time(self, t: float):
+        _lib.check(self.L.thorin_gpu_set_time(self.h, t), "set_time")
+
+    def algogas(self, sys_: ThorinPlanets) -> int:
+        return _lib.check(self.L.thorin_gpu_algogas(self.h, C.byref(sys_)), "thorin_gpu_algogas", ok=(0, 4))
+
+    def integrals(self):
+        vals = [C.c_double() for _ in range(5)]
+        _lib.check(self.L.thorin_gpu_integrals(self.h, *[C.byref(v) for v in vals]), "integrals")
+        return tuple(v.value for v in vals)
+
+    def nshift(self) -> np.ndarray:
+        out = np.zeros(self.nr, dtype=np.int32)
+        _lib.check(self.L.thorin_gpu_get_nshift(self.h, out.ctypes.data_as(C.POINTER(C.c_int))), "nshift")
+        return out
+
+    def stats(self) -> ThorinStats:
+        s = ThorinStats()
+        _lib.check(self.L.thorin_gpu_get_stats(self.h, C.byref(s)), "stats")
+        return s

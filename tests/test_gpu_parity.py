@@ -1,0 +1,83 @@
+"""GPU path (sm_103a kernels through the C ABI) against the oracle and the
+reference's golden outputs.
+
+Tolerance: FP64 fields within relative L2 1e-10 of the reference after the
+run (transcendental functions differ from glibc by an ulp or so); integer
+results exact: FARGO shifts, SOR iteration counts and substep counts.
+"""
+import numpy as np
+import pytest
+
+import harness as H
+import oracle as O
+from fargo_thorin_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40"]
+TOL = 1e-10
+
+
+def _gpu_disk(p):
+    from fargo_thorin_gb300.disk import GpuDisk
+    return GpuDisk(p)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_gpu_vs_reference_golden(name):
+    g = H.load(name)
+    p = H.case_params(g)
+    d = _gpu_disk(p)
+    d.init_default()
+    nr, ns = p.nrad, p.nsec
+    n = nr * ns
+    init_fields = H.GAS + (["pebbledens", "pebblevrad", "pebblevtheta", "pebblesize", "pebblestokes"] if p.pebbles else [])
+    for k in init_fields:
+        a, b = d.get(H.FIELD_IDS[k])[:n], g["init_" + k].ravel()
+        assert H.rel_l2(a, b) < 1e-14, f"init {k}"
+    H.start_state(d, p, {"dens": g["init_dens"].ravel(), "temper": g["init_temper"].ravel()})
+    sys_ = workloads.make_planets(p, [tuple(g["planet"])])
+    tq = g["tqwk"]
+    ntot, ninterm = int(g["ntot"]), int(g["ninterm"])
+    fields = H.GAS + (H.PEB if p.pebbles else [])
+    for step in range(1, ntot + 1):
+        sys_.x[0], sys_.y[0] = tq[step - 1][3], tq[step - 1][4]
+        d.algogas(sys_)
+        st = d.stats()
+        assert st.substeps == g["substeps"][step - 1]
+        assert st.sor_last_niter == g["sor_niter"][step - 1], f"SOR iterations at DT {step}"
+        m, mom, e, _, _ = d.integrals()
+        assert abs(m / g["mass"][step - 1] - 1) < 1e-12
+        assert abs(mom / g["momentum"][step - 1] - 1) < 1e-12
+        if step % ninterm == 0:
+            k = step // ninterm
+            for f in fields:
+                a = d.get(H.FIELD_IDS[f])[:n].reshape(nr, ns)
+                if f"out{k}_{f}" in g:
+                    assert H.rel_l2(a, g[f"out{k}_{f}"]) < TOL, f"{f} after {step} DT"
+                else:
+                    assert H.rel_l2(a[g["sample_rows"]], g[f"out{k}_{f}_rows"]) < TOL, f"{f} rows after {step} DT"
+                    assert H.rel_l2(a.mean(axis=1), g[f"out{k}_{f}_ringmean"]) < TOL, f"{f} ring means"
+
+
+@pytest.mark.parametrize("name", ["disk0_24x72", "disk1_32x96"])
+def test_gpu_vs_oracle_every_dt(name):
+    """GPU and oracle run the same host N-body code, so they share the planet
+    trajectory; compared after every DT, with the FARGO shifts exact."""
+    g = H.load(name)
+    p = H.case_params(g)
+    d = _gpu_disk(p)
+    o = O.OracleDisk(p)
+    for x in (d, o):
+        x.init_default()
+        H.start_state(x, p, {"dens": g["init_dens"].ravel(), "temper": g["init_temper"].ravel()})
+    sg = workloads.make_planets(p, [tuple(g["planet"])])
+    so = workloads.make_planets(p, [tuple(g["planet"])])
+    n = p.nrad * p.nsec
+    for step in range(1, 6):
+        d.algogas(sg)
+        o.algogas(so)
+        np.testing.assert_array_equal(d.nshift(), o.nshift())
+        assert d.stats().sor_last_niter == o.stats().sor_last_niter
+        for f in H.GAS + (H.PEB if p.pebbles else []) + ["energy"]:
+            assert H.rel_l2(d.get(H.FIELD_IDS[f])[:n], o.get(H.FIELD_IDS[f])[:n]) < 1e-12, f"{f} at DT {step}"
+        assert abs(sg.x[0] - so.x[0]) < 1e-14 and abs(sg.vx[0] - so.vx[0]) < 1e-14
