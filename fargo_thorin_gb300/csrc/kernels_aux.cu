@@ -152,7 +152,7 @@ __global__ void k_cfl_cells(DevGrid g, const double *__restrict__ vr, const doub
 }
 
 
-__global__ void k_cfl_final(DevGrid g, const double *__restrict__ part, CflRings cr, CflFinal f,
+__global__ void __launch_bounds__(1024) k_cfl_final(DevGrid g, const double *__restrict__ part, CflRings cr, CflFinal f,
                             double *__restrict__ scal, int *__restrict__ iscal)
 {
   double mg = 0.0, mp = -1.0e30, shear = 1e30;
@@ -592,7 +592,7 @@ __global__ void k_forces(DevGrid g, ForceArgs a, ForceRings fr)
   }
 }
 
-__global__ void k_forces_final(const double *__restrict__ part, int nb, int nq, double *__restrict__ scal)
+__global__ void __launch_bounds__(1024) k_forces_final(const double *__restrict__ part, int nb, int nq, double *__restrict__ scal)
 {
   // one block; quantity q summed over blocks in a fixed order
   for (int q = 0; q < nq; q++) {
@@ -669,7 +669,7 @@ __device__ double column_mass(double a, double b, double Hpeb)
   return __longlong_as_double(0x7ff8000000000000ULL);   // the reference aborts here
 }
 
-__global__ void k_accrete(DevGrid g, AccArgs a, double *__restrict__ scal)
+__global__ void __launch_bounds__(256) k_accrete(DevGrid g, AccArgs a, double *__restrict__ scal)
 {
   const int ns = g.ns;
   __shared__ double sh[8];
@@ -766,7 +766,7 @@ __global__ void k_accrete(DevGrid g, AccArgs a, double *__restrict__ scal)
 
 void aux_accrete(const DevGrid &g, const AccArgs &a, double *scal, cudaStream_t s)
 {
-  k_accrete<<<1, 1024, 0, s>>>(g, a, scal);
+  k_accrete<<<1, 256, 0, s>>>(g, a, scal);
 }
 
 // ---------------------------------------------------------------------------
@@ -807,7 +807,7 @@ __global__ void k_integrals(DevGrid g, const double *__restrict__ rho, const dou
   }
 }
 
-__global__ void k_integrals_final(const double *__restrict__ part, int nb, double *__restrict__ scal)
+__global__ void __launch_bounds__(1024) k_integrals_final(const double *__restrict__ part, int nb, double *__restrict__ scal)
 {
   for (int q = 0; q < 5; q++) {
     double s = 0.0;
@@ -831,7 +831,7 @@ void aux_integrals(const DevGrid &g, const double *rho, const double *vr, const 
 }
 
 // Final minimum of block partials (DiffusionTimestep's MPI_MIN).
-__global__ void k_min_final(const double *__restrict__ part, int nb, double *__restrict__ out)
+__global__ void __launch_bounds__(1024) k_min_final(const double *__restrict__ part, int nb, double *__restrict__ out)
 {
   double m = 1.0e38;
   for (int b = threadIdx.x; b < nb; b += blockDim.x) m = (part[b] < m) ? part[b] : m;

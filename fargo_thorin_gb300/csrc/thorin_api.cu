@@ -48,6 +48,17 @@ static thread_local std::string g_last_error;
 
 extern "C" const char *thorin_gpu_last_error(void) { return g_last_error.c_str(); }
 
+// Launch-time errors of the kernels enqueued so far (bad configuration,
+// resources) surface here; faults of running kernels at the next sync.
+#define KCHECK(where)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = cudaGetLastError();                                                \
+    if (e_ != cudaSuccess) {                                                            \
+      g_last_error = std::string(where) + ": " + cudaGetErrorString(e_);                \
+      return THORIN_ERR_CUDA;                                                           \
+    }                                                                                   \
+  } while (0)
+
 extern "C" void thorin_params_default(thorin_params *p, int nrad, int nsec)
 {
   // src_main/var.c:17-141 defaults and the derived switches of Interpret.c.
@@ -337,7 +348,7 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   for (int q = 0; q < 7; q++) { RCHK(dfield(d, &d->ts.d[q])); RCHK(dfield(d, &d->ts.f[q])); }
   RCHK(dalloc(d, (void **)&d->nshift, n1 * sizeof(int)));
   d->ts.nshift = d->nshift;
-  d->ts.vmed = nullptr;
+  d->ts.vmed = d->ring[R_VMED];
   // reduction scratch: enough partials for every reduction kernel
   const size_t nb = (size_t)((d->ns + 127) / 128 + 2) * (size_t)(d->nr + 2);
   RCHK(dalloc(d, (void **)&d->partials, nb * (2 + 2 * MAXPL_DEV + 6) * sizeof(double)));
@@ -683,6 +694,7 @@ extern "C" int thorin_gpu_init_default(thorin_disk *d)
   }
   RCHK(upload_all_rings(d));
   RCHK(eos_refresh(d));
+  KCHECK("initial EOS kernels");
   CUCHK(cudaStreamSynchronize(d->s));
   return THORIN_OK;
 }
@@ -854,6 +866,7 @@ extern "C" int thorin_gpu_cfl(thorin_disk *d, double dt_remaining, double invdtr
   aux_cfl(d->g, d->vrad, d->vtheta, d->cs, d->pvrad, d->pvtheta, d->cfl, p.pebbles, p.fast_transport,
           (p.viscosity_alpha || p.viscosity != 0.0), d->partials, f, d->scal, d->iscal, d->s);
   d->cfl_first = 0;
+  KCHECK("cfl kernels");
   CUCHK(cudaMemcpyAsync(d->iscal_h, d->iscal, sizeof(int) * IS_COUNT, cudaMemcpyDeviceToHost, d->s));
   CUCHK(cudaStreamSynchronize(d->s));
   *n_sub = d->iscal_h[IS_NSUB];
@@ -932,6 +945,7 @@ extern "C" int thorin_gpu_accrete(thorin_disk *d, thorin_planets *sys, double dt
     double dMp = 0, dPx = 0, dPy = 0;
     if (imin <= imax) {
       aux_accrete(d->g, a, d->scal, d->s);
+      KCHECK("accretion kernel");
       CUCHK(cudaMemcpyAsync(d->scal_h + SC_ACC_DM, d->scal + SC_ACC_DM, 3 * sizeof(double), cudaMemcpyDeviceToHost, d->s));
       CUCHK(cudaStreamSynchronize(d->s));
       dMp = d->scal_h[SC_ACC_DM]; dPx = d->scal_h[SC_ACC_DPX]; dPy = d->scal_h[SC_ACC_DPY];
@@ -999,6 +1013,7 @@ extern "C" int thorin_gpu_forces(thorin_disk *d, thorin_planets *sys, double mas
   a.mass_taper = mass_taper; a.pebble_alpha = p.pebble_alpha; a.hillcut = p.hillcut;
   const double indx_pl = p.indirect_term ? -axs : 0.0, indy_pl = p.indirect_term ? -ays : 0.0;
   aux_forces(d->g, a, d->fr, indx_pl, indy_pl, d->scal, d->s);
+  KCHECK("force kernels");
   // DampingTW04 needs the ring means of Sigma (and c_s) at each planet
   for (int k = 0; k < npl; k++) {
     const double r = sqrt(sys->x[k] * sys->x[k] + sys->y[k] * sys->y[k]);
@@ -1030,11 +1045,13 @@ static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *ca
 {
   const thorin_params &p = d->p;
   hydro_sor_resid0(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor, d->s);
+  KCHECK("SOR residual kernel");
   int first = 1, chunk = hint > 0 ? hint : 4;
   *capped = 0;
   for (;;) {
     hydro_sor_sweeps(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor, omega, p.sor_eps, first,
                      chunk, p.sor_maxiters, d->s);
+    KCHECK("SOR sweep kernels");
     CUCHK(cudaMemcpyAsync(d->iscal_h + IS_SOR_DONE, d->sor.done, 2 * sizeof(int), cudaMemcpyDeviceToHost, d->s));
     CUCHK(cudaStreamSynchronize(d->s));
     const int done = d->iscal_h[IS_SOR_DONE];
@@ -1108,6 +1125,7 @@ static int energy_step(thorin_disk *d, double dt)
   hydro_matrix(d->g, d->rho, d->temper, d->cs, d->dcen, d->divv, d->qminus, d->qplus, d->qirr, d->ml, d->mlip, d->mlim,
                d->mljp, d->mljm, d->rhs, dt, d->gm1, d->ring[R_INVDXTHETA2], p.stellar_irradiation, nheat,
                d->heat_idx_d, d->heat_val_d, d->s);
+  KCHECK("energy kernels");
   if (d->sor_first) {
     d->sor_first = 0;
     RCHK(iterate_relaxation(d));
@@ -1195,6 +1213,7 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
     transport_fluid(d, &d->pdens, d->pvrad, d->pvtheta, nullptr, &d->t_rho_peb, dt, 0);
     aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, d->s);
   }
+  KCHECK("hydro kernels");
   CUCHK(cudaMemcpyAsync(d->iscal_h + IS_CRASH, d->iscal + IS_CRASH, sizeof(int), cudaMemcpyDeviceToHost, d->s));
   d->PhysicalTime += dt;
   d->st.last_dt = dt;
@@ -1259,6 +1278,7 @@ extern "C" int thorin_gpu_integrals(thorin_disk *d, double *mass, double *moment
 {
   aux_integrals(d->g, d->rho, d->vrad, d->vtheta, d->energy, d->pdens, d->pvtheta, d->OmegaFrame, d->p.pebbles,
                 d->partials, d->scal, d->s);
+  KCHECK("integral kernels");
   CUCHK(cudaMemcpyAsync(d->scal_h + SC_MASS, d->scal + SC_MASS, 5 * sizeof(double), cudaMemcpyDeviceToHost, d->s));
   CUCHK(cudaStreamSynchronize(d->s));
   if (mass) *mass = d->scal_h[SC_MASS];

@@ -59,7 +59,7 @@ def test_gpu_vs_reference_golden(name):
                     assert H.rel_l2(a.mean(axis=1), g[f"out{k}_{f}_ringmean"]) < TOL, f"{f} ring means"
 
 
-@pytest.mark.parametrize("name", ["disk0_24x72", "disk1_32x96"])
+@pytest.mark.parametrize("name", ["disk0_24x72", "disk1_32x96", "disk1_64x192_40"])
 def test_gpu_vs_oracle_every_dt(name):
     """GPU and oracle run the same host N-body code, so they share the planet
     trajectory; compared after every DT, with the FARGO shifts exact."""
