@@ -1,0 +1,335 @@
+"""Benchmark: cell-updates/s of the FARGO_THORIN hydro loop on one GB300.
+
+Workload: the 1024 x 3072 pebble + embryo disk (log r in [0.4, 2.5], gas with
+Sigma = 5e-4 r^-0.5 perturbed by 1e-4 u, pebbles at 0.01 Sigma with Stokes
+number 0.1, a 3e-5 M* embryo at r = 1 that feels the disk, accretes pebbles
+and heats the gas, Bell & Lin opacity, SOR radiative diffusion at a relative
+residual of 1e-8), FP64, synthetic data built by the library's own set-up.
+
+A step is one DT of AlgoGas (all its CFL substeps, each one full hydro
+substep with SOR); cell-updates = nrad * nsec * substeps.  ``value`` is timed
+on the device with CUDA events on the library's stream with the state
+resident in HBM; ``e2e`` times the same steps through the C ABI with the
+state uploaded from pinned host buffers and downloaded back every step.
+
+--impl reference times the CPU restatement of the reference algorithm (the
+oracle, OpenMP over all host cores) on the same disk, one short DT per step.
+With torchrun (N > 1) every rank advances its own replica (the disk does not
+shard); rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NR, NS = 1024, 3072
+SOR_EPS = 1e-8
+METRIC = "cell-updates/s per full step (1024x3072 pebble+embryo disk, SOR 1e-8)"
+UNIT = "cell-updates/s"
+# Algorithmic bytes per cell of one full SOR sweep: T read + write, the five
+# matrix coefficients and the right-hand side (8 FP64 values).
+SOR_BYTES_PER_CELL_SWEEP = 64.0
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+STATE_FIELDS = [0, 1, 2, 3, 4, 5, 6, 7]      # dens, vrad, vtheta, energy, pebble dens/vrad/vtheta/size
+
+
+def make_disk(nr=NR, ns=NS):
+    from fargo_thorin_gb300 import workloads
+    from fargo_thorin_gb300.disk import GpuDisk
+    p = workloads.params_for("disk1", nr, ns, sor_eps=SOR_EPS)
+    d = GpuDisk(p)
+    d.init_default()
+    st = workloads.perturbed_state(p, {"dens": d.get(0), "temper": d.get(8)})
+    d.set(0, st["dens"]); d.set(1, st["vrad"]); d.set(3, st["energy"])
+    d.set(4, st["pebdens"]); d.set(7, st["pebsize"])
+    d.refresh(2)
+    sys_ = workloads.make_planets(p, [workloads.PLANET1])
+    return p, d, sys_
+
+
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from fargo_thorin_gb300 import _lib
+    _lib.load()
+    p, d, sys_ = make_disk()
+    for _ in range(args.warmup):
+        d.algogas(sys_)
+    stream = torch.cuda.ExternalStream(d.stream())
+    d.set_timing(True)
+    launches0 = d.stats().kernel_launches
+    clocks = ClockSampler(local)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # device-timed steps, state resident in HBM
+    barrier()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    subs, sweeps0 = 0, d.stats().sor_sweeps
+    for _ in range(args.steps):
+        d.algogas(sys_)
+        subs += d.stats().substeps
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    st = d.stats()
+    sweeps = st.sor_sweeps - sweeps0
+    launches = st.kernel_launches - launches0
+    sor_avg_ms = st.sor_time_ms / max(st.sor_passes, 1)
+    ms_t = torch.tensor([ms], device="cuda")
+    subs_t = torch.tensor([float(subs)], device="cuda")
+    if ws > 1:
+        import torch.distributed as dist
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(subs_t, op=dist.ReduceOp.SUM)
+    ms_max = float(ms_t.item())
+    total_updates = NR * NS * float(subs_t.item())
+    value = total_updates / (ms_max / 1e3)
+
+    # end to end through the C ABI with host buffers (pinned)
+    n = (NR + 1) * NS
+    host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True) for f in STATE_FIELDS}
+    for f in STATE_FIELDS:
+        host[f].numpy()[:] = d.get(f)
+    L, h = d.L, d.h
+    ptr = {f: C.cast(host[f].data_ptr(), C.POINTER(C.c_double)) for f in STATE_FIELDS}
+    barrier()
+    t0 = time.perf_counter()
+    esubs = 0
+    for _ in range(args.steps):
+        for f in STATE_FIELDS:
+            _lib.check(L.thorin_gpu_upload(h, f, ptr[f]), "upload")
+        d.algogas(sys_)
+        esubs += d.stats().substeps
+        for f in STATE_FIELDS[:7]:
+            _lib.check(L.thorin_gpu_download(h, f, ptr[f]), "download")
+    barrier()
+    e_s = time.perf_counter() - t0
+    e_t = torch.tensor([e_s], device="cuda")
+    es_t = torch.tensor([float(esubs)], device="cuda")
+    if ws > 1:
+        import torch.distributed as dist
+        dist.all_reduce(e_t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(es_t, op=dist.ReduceOp.SUM)
+    e2e_value = NR * NS * float(es_t.item()) / float(e_t.item())
+
+    if rank == 0:
+        peak, peak_kind = peaks()
+        cells_pass = (NR - 2) * NS / 2
+        bytes_pass = SOR_BYTES_PER_CELL_SWEEP * cells_pass
+        achieved = bytes_pass / (sor_avg_ms / 1e3) / 1e9
+        traffic = None
+        tf = os.path.join(ROOT, "profiles", "sor_pass_traffic.json")
+        if os.path.exists(tf):
+            try:
+                with open(tf) as f:
+                    traffic = json.load(f).get("bytes_per_launch")
+            except Exception:
+                traffic = None
+        cpu = None
+        if ws == 1 and not args.no_cpu_baseline:
+            cpu = cpu_baseline(d, sys_)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"disk1 {NR}x{NS} gas+pebbles+3e-5 embryo, BL94, SOR eps {SOR_EPS}",
+                       "nrad": NR, "nsec": NS, "substeps": subs, "sor_sweeps_per_substep": sweeps / max(subs, 1),
+                       "step": "one DT of AlgoGas (all CFL substeps)", "l2": "inputs larger than L2 (1.7 GB state)",
+                       "parallelism": "replicas" if ws > 1 else "single disk"},
+            "clocks": clk,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n * 8,
+                    "d2h_bytes_per_step": 7 * n * 8},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": "k_sor_pass", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": bytes_pass, "avg_launch_ms": sor_avg_ms},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    d.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def _oracle():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    return O
+
+
+def oracle_disk(O, omp=True, dt_div=8):
+    from fargo_thorin_gb300 import workloads
+    p = workloads.params_for("disk1", NR, NS, sor_eps=SOR_EPS)
+    p.dt = p.dt / dt_div          # one short DT per step keeps a step near one substep
+    o = O.OracleDisk(p, omp=omp)
+    o.init_default()
+    st = workloads.perturbed_state(p, {"dens": o.get(0), "temper": o.get(8)})
+    o.set(0, st["dens"]); o.set(1, st["vrad"]); o.set(3, st["energy"])
+    o.set(4, st["pebdens"]); o.set(7, st["pebsize"])
+    o.refresh(2)
+    return p, o, workloads.make_planets(p, [workloads.PLANET1])
+
+
+def cpu_baseline(d, sys_gpu):
+    """The oracle (OpenMP, all host cores) on the same disk: SOR omega schedule
+    taken from the GPU run so that the bounded sample times steady-state
+    substeps, a few short DTs."""
+    O = _oracle()
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    p, o, s = oracle_disk(O)
+    om, dom, nl, _ = d.sor_state()
+    o.set_sor_state(om, dom, nl)
+    t0 = time.perf_counter()
+    subs, steps = 0, 0
+    while time.perf_counter() - t0 < 15.0 and steps < 8:
+        o.algogas(s)
+        subs += o.stats().substeps
+        steps += 1
+    el = time.perf_counter() - t0
+    return {"value": NR * NS * subs / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{subs} substeps ({steps} DT/8 steps) of the {NR}x{NS} disk after the SOR omega calibration, "
+                      f"{el:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    O = _oracle()
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    p, o, s = oracle_disk(O)
+    for _ in range(args.warmup):
+        o.algogas(s)
+    t0 = time.perf_counter()
+    subs = 0
+    for _ in range(args.steps):
+        o.algogas(s)
+        subs += o.stats().substeps
+    el = time.perf_counter() - t0
+    value = NR * NS * subs / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"disk1 {NR}x{NS} gas+pebbles+3e-5 embryo, BL94, SOR eps {SOR_EPS}", "nrad": NR,
+                   "nsec": NS, "substeps": subs, "step": "one DT/8 of AlgoGas", "implementation":
+                   "CPU restatement of the reference algorithm (oracle), OpenMP"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{subs} substeps in {args.steps} DT/8 steps after {args.warmup} warm-up steps"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

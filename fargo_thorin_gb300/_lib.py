@@ -35,6 +35,10 @@ SIGNATURES = {
     "thorin_gpu_integrals": (C.c_int, [_P, _D, _D, _D, _D, _D]),
     "thorin_gpu_get_nshift": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "thorin_gpu_get_stats": (C.c_int, [_P, C.POINTER(ThorinStats)]),
+    "thorin_gpu_get_sor_state": (C.c_int, [_P, _D, _D, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "thorin_gpu_set_sor_state": (C.c_int, [_P, C.c_double, C.c_double, C.c_int]),
+    "thorin_gpu_set_timing": (C.c_int, [_P, C.c_int]),
+    "thorin_gpu_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "thorin_gpu_last_error": (C.c_char_p, []),
     "thorin_planet_from_elements": (C.c_int, [C.POINTER(ThorinPlanets), C.c_int] + [C.c_float] * 9),
 }

@@ -27,6 +27,7 @@ void aux_ring_mean(const DevGrid &g, const double *f, double *out, cudaStream_t 
 {
   const int threads = 256, warps = threads / 32;
   k_ring_mean<<<(g.nr + warps - 1) / warps, threads, 0, s>>>(g.nr, g.ns, f, out);
+  g_thorin_launches++;
 }
 
 // Ring mean of one ring (e.g. the ring holding a planet).
@@ -39,6 +40,7 @@ __global__ void k_ring_mean_at(int ns, const double *__restrict__ f, int ring, d
 void aux_ring_mean_at(const DevGrid &g, const double *f, int ring, double *out, cudaStream_t s)
 {
   k_ring_mean_at<<<1, 32, 0, s>>>(g.ns, f, ring, out);
+  g_thorin_launches++;
 }
 
 // FViscosity at Rmed[i] and Rinf[i] (Viscosity.c:26-54).  The ring index
@@ -70,6 +72,7 @@ __global__ void k_viscosity_rings(DevGrid g, ViscParams v)
 void aux_viscosity_rings(const DevGrid &g, const ViscParams &v, cudaStream_t s)
 {
   k_viscosity_rings<<<(g.nr + 127) / 128, 128, 0, s>>>(g, v);
+  g_thorin_launches++;
 }
 
 // ---------------------------------------------------------------------------
@@ -85,6 +88,7 @@ __global__ void k_stokes(DevGrid g, const double *__restrict__ rho, const double
 void aux_stokes(const DevGrid &g, const double *rho, const double *psize, double *tau, cudaStream_t s)
 {
   k_stokes<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, psize, tau);
+  g_thorin_launches++;
 }
 
 // ---------------------------------------------------------------------------
@@ -194,11 +198,14 @@ void aux_cfl(const DevGrid &g, const double *vr, const double *vt, const double 
 {
   const int threads = 256, warps = threads / 32;
   k_cfl_means<<<(g.nr + warps - 1) / warps, threads, 0, s>>>(g, vt, pvt, cr, pebbles && fast);
+  g_thorin_launches++;
   dim3 grid = grid2d(g.ns, g.nr - 1, 256);
   k_cfl_cells<<<grid, 256, 0, s>>>(g, vr, vt, cs, pvr, pvt, cr, pebbles, fast, viscous, part);
+  g_thorin_launches++;
   CflFinal f = f0;
   f.nb = grid.x * grid.y;
   k_cfl_final<<<1, 1024, 0, s>>>(g, part, cr, f, scal, iscal);
+  g_thorin_launches++;
 }
 
 // ---------------------------------------------------------------------------
@@ -217,6 +224,7 @@ __global__ void k_evaporate(DevGrid g, const double *__restrict__ T, double *__r
 void aux_evaporate(const DevGrid &g, const double *T, double *pdens, double facc, cudaStream_t s)
 {
   k_evaporate<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, T, pdens, facc);
+  g_thorin_launches++;
 }
 
 // ---------------------------------------------------------------------------
@@ -248,6 +256,7 @@ void aux_damp_gas(const DevGrid &g, double *vrad, double *rho, double *vtheta, d
   if (nrings <= 0) return;
   k_damp_gas<<<grid2d(g.ns, nrings, BX), BX, 0, s>>>(g, vrad, rho, vtheta, energy, rings, dt, omega_frame, damp_init,
                                                      energy_eq);
+  g_thorin_launches++;
 }
 
 __global__ void k_damp_peb(DevGrid g, double *__restrict__ pd, double *__restrict__ pvr, double *__restrict__ pvt,
@@ -271,6 +280,7 @@ void aux_damp_peb(const DevGrid &g, double *pd, double *pvr, double *pvt, const 
 {
   if (nrings <= 0) return;
   k_damp_peb<<<grid2d(g.ns, nrings, BX), BX, 0, s>>>(g, pd, pvr, pvt, rings, dt, omega_frame);
+  g_thorin_launches++;
 }
 
 // DetectCrash (SourceEuler.c:48-66): any negative value in rows 0..nr-1.
@@ -288,6 +298,7 @@ void aux_crash(const DevGrid &g, const double *f, int *flag, cudaStream_t s)
   int blocks = (n + 255) / 256;
   if (blocks > 1216) blocks = 1216;
   k_crash<<<blocks, 256, 0, s>>>(n, f, flag);
+  g_thorin_launches++;
 }
 
 // ---------------------------------------------------------------------------
@@ -329,6 +340,7 @@ void aux_pebble_sources(const DevGrid &g, const double *pd, const double *pvr, c
 {
   k_pebble_sources<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, pd, pvr, pvt, tau, vr, vt, pagr, pagt, paccr, pacct, dragr,
                                                          dragt, omega_frame, back_reaction);
+  g_thorin_launches++;
 }
 
 // SubStep1Pebbles (Pebbles.c:617-652) followed by ParticleDiffusion
@@ -374,6 +386,7 @@ void aux_pebble_substep1(const DevGrid &g, double *pvr, double *pvt, const doubl
 {
   k_pebble_substep1<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, pvr, pvt, tau, vr, vt, paccr, pacct, gaccr, gacct, rho, pd,
                                                           dt, diffusion, schmidt, invdxtheta_r);
+  g_thorin_launches++;
 }
 
 // ---------------------------------------------------------------------------
@@ -629,11 +642,15 @@ void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr, dou
 {
   const int threads = 256, warps = threads / 32;
   k_force_rings<<<(g.nr + warps - 1) / warps, threads, 0, s>>>(g, a0.cs, a0.tau, fr, a0.pebbles, a0.pebble_alpha);
+  g_thorin_launches++;
   dim3 grid = grid2d(g.ns, g.nr, 128);
   k_forces<<<grid, 128, 0, s>>>(g, a0, fr);
+  g_thorin_launches++;
   k_forces_final<<<1, 1024, 0, s>>>(a0.part, grid.x * grid.y, 2 + 2 * a0.npl, scal);
+  g_thorin_launches++;
   k_forces_indirect<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, a0.agr, a0.agt, a0.pagr, a0.pagt, scal, indx_pl, indy_pl,
                                                           a0.pebbles);
+  g_thorin_launches++;
 }
 
 // ---------------------------------------------------------------------------
@@ -767,6 +784,7 @@ __global__ void __launch_bounds__(256) k_accrete(DevGrid g, AccArgs a, double *_
 void aux_accrete(const DevGrid &g, const AccArgs &a, double *scal, cudaStream_t s)
 {
   k_accrete<<<1, 256, 0, s>>>(g, a, scal);
+  g_thorin_launches++;
 }
 
 // ---------------------------------------------------------------------------
@@ -827,7 +845,9 @@ void aux_integrals(const DevGrid &g, const double *rho, const double *vr, const 
 {
   dim3 grid = grid2d(g.ns, g.nr, 256);
   k_integrals<<<grid, 256, 0, s>>>(g, rho, vr, vt, e, pd, pvt, omega_frame, pebbles, part);
+  g_thorin_launches++;
   k_integrals_final<<<1, 1024, 0, s>>>(part, grid.x * grid.y, scal);
+  g_thorin_launches++;
 }
 
 // Final minimum of block partials (DiffusionTimestep's MPI_MIN).
@@ -842,4 +862,5 @@ __global__ void __launch_bounds__(1024) k_min_final(const double *__restrict__ p
 void aux_min_final(const double *part, int nb, double *out, cudaStream_t s)
 {
   k_min_final<<<1, 1024, 0, s>>>(part, nb, out);
+  g_thorin_launches++;
 }

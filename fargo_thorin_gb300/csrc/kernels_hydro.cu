@@ -842,12 +842,14 @@ void hydro_substep1(const DevGrid &g, const double *rho, const double *vrad, con
   k_substep1<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, vrad, vtheta, energy, agr, agt, dragr, dragt, vradint,
                                                    vthetaint, gaccr, gacct, dt, omega_frame, gm1, pebbles,
                                                    back_reaction, supp_torque, invdxtheta_r);
+  g_thorin_launches++;
 }
 
 void hydro_stress(const DevGrid &g, const double *vr, const double *vt, const double *rho, double *divv, double *trr,
                   double *tpp, double *trp, double invdphi, cudaStream_t s)
 {
   k_stress<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, vr, vt, rho, divv, trr, tpp, trp, invdphi);
+  g_thorin_launches++;
 }
 
 void hydro_visc_update(const DevGrid &g, double *vr, double *vt, const double *rho, const double *trr, const double *tpp,
@@ -855,6 +857,7 @@ void hydro_visc_update(const DevGrid &g, double *vr, double *vt, const double *r
                        cudaStream_t s)
 {
   k_visc_update<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, vr, vt, rho, trr, tpp, trp, dt, invdphi, kepler, vkin, vkout);
+  g_thorin_launches++;
 }
 
 void hydro_substep2(const DevGrid &g, const double *rho, const double *vr, const double *vt, const double *energy,
@@ -863,19 +866,23 @@ void hydro_substep2(const DevGrid &g, const double *rho, const double *vr, const
 {
   k_substep2<<<grid2d(g.ns, g.nr + 1, BX), BX, 0, s>>>(g, rho, vr, vt, energy, vrnew, vtnew, eint, dt, energy_eq,
                                                        invdxtheta_r);
+  g_thorin_launches++;
 }
 
 void hydro_qplus(const DevGrid &g, const double *vr, const double *vt, const double *rho, double *divv, double *qplus,
                  double invdphi, double lr01, double lr12, cudaStream_t s)
 {
   k_qplus<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, vr, vt, rho, divv, qplus, invdphi);
+  g_thorin_launches++;
   k_qplus_row0<<<(g.ns + BX - 1) / BX, BX, 0, s>>>(g, qplus, lr01, lr12);
+  g_thorin_launches++;
 }
 
 void hydro_eos(const DevGrid &g, const double *rho, const double *energy, double *temper, double *cs, double gm1,
                double gg1, cudaStream_t s)
 {
   k_eos<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, energy, temper, cs, gm1, gg1);
+  g_thorin_launches++;
 }
 
 int hydro_diffcoef_blocks(const DevGrid &g) { return ((g.ns + BX - 1) / BX) * g.nr; }
@@ -887,6 +894,7 @@ void hydro_diffcoef(const DevGrid &g, const double *rho, const double *T, const 
 {
   k_diffcoef<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, T, cs, opacity, qminus, dcen, dtmin_part, law, parametric_cu,
                                                    parametric_raw, opacity_drop, taueff_c, invdxtheta_r, deltar2_r);
+  g_thorin_launches++;
 }
 
 void hydro_irradiation(const DevGrid &g, const double *rho, const double *cs, const double *opacity, double *flaring,
@@ -895,6 +903,7 @@ void hydro_irradiation(const DevGrid &g, const double *rho, const double *cs, co
 {
   k_irradiation<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, cs, opacity, flaring, qirr, rstar, tirr4fac, opacity_drop,
                                                       taueff_c, rinf15, rsup15);
+  g_thorin_launches++;
 }
 
 void hydro_matrix(const DevGrid &g, const double *rho, const double *T, const double *cs, const double *dcen,
@@ -907,6 +916,7 @@ void hydro_matrix(const DevGrid &g, const double *rho, const double *T, const do
   k_matrix<<<grid2d(g.ns, g.nr - 2, BX), BX, 0, s>>>(g, rho, T, cs, dcen, divv, qminus, qplus, qirr, ml, mlip, mlim, mljp,
                                                      mljm, rhs, dt, gm1, invdxtheta2_r, irradiation, nheat, heat_idx,
                                                      heat_val);
+  g_thorin_launches++;
 }
 
 static const int SOR_BX = 128;
@@ -923,6 +933,7 @@ void hydro_sor_resid0(const DevGrid &g, const double *T, const double *ml, const
                       const double *mljp, const double *mljm, const double *rhs, const SorCtl &c, cudaStream_t s)
 {
   k_sor_resid0<<<grid2d(g.ns, g.nr - 2, SOR_BX), SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, c);
+  g_thorin_launches++;
 }
 
 void hydro_sor_sweeps(const DevGrid &g, double *T, const double *ml, const double *mlip, const double *mlim,
@@ -932,13 +943,16 @@ void hydro_sor_sweeps(const DevGrid &g, double *T, const double *ml, const doubl
   dim3 grid = grid2d(g.ns / 2, g.nr - 2, SOR_BX);
   for (int n = first; n < first + count && n <= maxiters; n++) {
     k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, c, omega, eps, 1, n, maxiters);
+    g_thorin_launches++;
     k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, c, omega, eps, 2, n, maxiters);
+    g_thorin_launches++;
   }
 }
 
 void hydro_energy_from_t(const DevGrid &g, const double *rho, double *T, double *enew, cudaStream_t s)
 {
   k_energy_from_t<<<grid2d(g.ns, g.nr + 1, BX), BX, 0, s>>>(g, rho, T, enew);
+  g_thorin_launches++;
 }
 
 // Whole transport of one fluid.  q_in: rho, vr, vt, energy (NULL for
@@ -955,6 +969,7 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
   k_rad_prep<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, nq, *rho, vr, vt, energy ? *energy : nullptr, S.mom[0], S.mom[1],
                                                S.mom[2], S.mom[3], S.w[0], S.w[1], S.w[2], S.w[3], S.w[4], S.w[5],
                                                omega_frame);
+  g_thorin_launches++;
   // slopes of the quotients (0..3, energy 4 if present, rho-quotient 5) and of rho (6)
   PtrPack7 sl;
   int n = 0;
@@ -964,6 +979,7 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
   sl.src[n] = *rho; sl.dst[n] = S.d[6]; n++;
   sl.n = n;
   k_rad_slope<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, sl);
+  g_thorin_launches++;
   // faces: quotients and rho
   PtrPack7 wf, dqf;
   n = 0;
@@ -973,6 +989,7 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
   wf.src[n] = *rho; wf.dst[n] = S.f[6]; dqf.src[n] = S.d[6]; n++;
   wf.n = dqf.n = n;
   k_rad_face<<<grid2d(ns, nr + 1, BX), BX, 0, s>>>(g, wf, dqf, vr, dt);
+  g_thorin_launches++;
   // flux divergence: in/out
   PtrPack7 qf, io;
   n = 0;
@@ -981,6 +998,7 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
   qf.src[n] = S.f[5]; io.src[n] = *rho; io.dst[n] = S.rho_new; n++;
   qf.n = io.n = n;
   k_rad_update<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, qf, S.f[6], vr, io, dt);
+  g_thorin_launches++;
   // azimuthal step on (rmp, rmm, tmp, tmm, [e], rho)
   AziQ az;
   n = 0;
@@ -990,10 +1008,12 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
   az.n = n;
   const size_t smem = 4 * (size_t)ns * sizeof(double);
   k_azimuthal<<<nr, 256, smem, s>>>(g, az, vt, dt, fast, S.nshift, S.vmed);
+  g_thorin_launches++;
   // velocities from the transported momenta
   k_velocities<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, S.rho_new, S.mom[0], S.mom[1], S.mom[2], S.mom[3], vr, vt,
                                                  omega_frame, damp_vrad, dt, drin, drout,
                                                  energy ? S.e_new : nullptr, energy ? temper : nullptr, cs, gm1, gg1);
+  g_thorin_launches++;
 }
 
 int hydro_azimuthal_smem(int ns) { return 4 * ns * (int)sizeof(double); }

@@ -30,6 +30,7 @@
 #define SQRT2PI_INV (1.0 / sqrt(2.0 * H_PI))
 
 static thread_local std::string g_last_error;
+long long g_thorin_launches = 0;
 
 #define CUCHK(call)                                                                     \
   do {                                                                                  \
@@ -136,6 +137,8 @@ struct thorin_disk {
   double gm1, gg1, drin, drout, invdphi, lr01, lr12, vkep_in, vkep_out, taueff_c, tirr4fac, rstar;
   ViscParams vp;
   thorin_stats st;
+  int timing;
+  cudaEvent_t ev[4];
 };
 
 static int dalloc(thorin_disk *d, void **ptr, size_t bytes)
@@ -433,6 +436,8 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   memset(&d->st, 0, sizeof(d->st));
   d->scal_h[SC_DTSTELLAR] = 1.0e38;                   // global.h:47
   CUCHK(cudaMemcpyAsync(d->scal + SC_DTSTELLAR, d->scal_h + SC_DTSTELLAR, sizeof(double), cudaMemcpyHostToDevice, d->s));
+  for (int q = 0; q < 4; q++) CUCHK(cudaEventCreate(&d->ev[q]));
+  d->timing = 0;
   hydro_set_smem_limits(d->ns);
   if (hydro_azimuthal_smem(d->ns) > 227 * 1024) { g_last_error = "nsec too large for the ring kernel"; return THORIN_ERR_ARG; }
   CUCHK(cudaStreamSynchronize(d->s));
@@ -449,6 +454,7 @@ extern "C" int thorin_gpu_destroy(thorin_disk *d)
   cudaFreeHost(d->scal_h);
   cudaFreeHost(d->iscal_h);
   cudaFreeHost(d->csmean_h);
+  for (int q = 0; q < 4; q++) cudaEventDestroy(d->ev[q]);
   cudaStreamDestroy(d->s);
   delete d;
   return THORIN_OK;
@@ -557,6 +563,7 @@ extern "C" int thorin_gpu_get_stats(thorin_disk *d, thorin_stats *s)
 {
   *s = d->st;
   s->physical_time = d->PhysicalTime;
+  s->kernel_launches = g_thorin_launches;
   return THORIN_OK;
 }
 
@@ -1049,12 +1056,21 @@ static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *ca
   int first = 1, chunk = hint > 0 ? hint : 4;
   *capped = 0;
   for (;;) {
+    if (d->timing) CUCHK(cudaEventRecord(d->ev[0], d->s));
     hydro_sor_sweeps(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor, omega, p.sor_eps, first,
                      chunk, p.sor_maxiters, d->s);
     KCHECK("SOR sweep kernels");
+    if (d->timing) CUCHK(cudaEventRecord(d->ev[1], d->s));
     CUCHK(cudaMemcpyAsync(d->iscal_h + IS_SOR_DONE, d->sor.done, 2 * sizeof(int), cudaMemcpyDeviceToHost, d->s));
     CUCHK(cudaStreamSynchronize(d->s));
     const int done = d->iscal_h[IS_SOR_DONE];
+    if (d->timing) {
+      float ms = 0.f;
+      CUCHK(cudaEventElapsedTime(&ms, d->ev[0], d->ev[1]));
+      d->st.sor_time_ms += ms;
+      const int did = done ? d->iscal_h[IS_SOR_DONE + 1] - first + 1 : chunk;
+      d->st.sor_passes += 2LL * (did > 0 ? did : 0);
+    }
     if (done) {
       *niter = d->iscal_h[IS_SOR_DONE + 1];
       *capped = (done == 2);
@@ -1248,6 +1264,7 @@ extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
   double dtemp = 0.0, dt;
   int nsub = 0, status = THORIN_OK;
   if (!sys || sys->nb > MAXPL_DEV) { g_last_error = "planetary system missing or too large"; return THORIN_ERR_ARG; }
+  if (d->timing) CUCHK(cudaEventRecord(d->ev[2], d->s));
   while (dtemp < 0.999999999 * DT) {
     d->MassTaper = d->PhysicalTime / (p.mass_taper * 2.0 * H_MPI);
     d->MassTaper = (d->MassTaper > 1.0 ? 1.0 : pow(sin(d->MassTaper * H_MPI / 2.0), 2.0));
@@ -1267,10 +1284,53 @@ extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
     if (s != THORIN_OK) status = s;
     nsub++;
   }
+  if (d->timing) CUCHK(cudaEventRecord(d->ev[3], d->s));
   CUCHK(cudaStreamSynchronize(d->s));
+  if (d->timing) {
+    float ms = 0.f;
+    CUCHK(cudaEventElapsedTime(&ms, d->ev[2], d->ev[3]));
+    d->st.step_time_ms = ms;
+  }
   d->st.substeps = nsub;
   d->st.crashed = d->iscal_h[IS_CRASH];
+  d->st.kernel_launches = g_thorin_launches;
   return status;
+}
+
+extern "C" int thorin_gpu_get_sor_state(thorin_disk *d, double *omega, double *domega, int *niterlast, int *calibrated)
+{
+  if (!d) return THORIN_ERR_ARG;
+  if (omega) *omega = d->omega;
+  if (domega) *domega = d->domega;
+  if (niterlast) *niterlast = d->Niterlast;
+  if (calibrated) *calibrated = !d->sor_first;
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_set_sor_state(thorin_disk *d, double omega, double domega, int niterlast)
+{
+  if (!d || !(omega >= 1.0 && omega <= TH_OMEGAUPPER)) return THORIN_ERR_ARG;
+  d->omega = omega;
+  d->domega = domega;
+  d->Niterlast = niterlast;
+  d->sor_first = 0;
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_set_timing(thorin_disk *d, int on)
+{
+  if (!d) return THORIN_ERR_ARG;
+  d->timing = on ? 1 : 0;
+  d->st.sor_time_ms = 0.0;
+  d->st.sor_passes = 0;
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_get_stream(thorin_disk *d, void **stream)
+{
+  if (!d || !stream) return THORIN_ERR_ARG;
+  *stream = (void *)d->s;
+  return THORIN_OK;
 }
 
 extern "C" int thorin_gpu_integrals(thorin_disk *d, double *mass, double *momentum, double *energy, double *peb_mass,

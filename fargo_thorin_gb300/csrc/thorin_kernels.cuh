@@ -75,6 +75,10 @@ struct AccArgs {
   int imin, imax, iflow;
 };
 
+// Number of kernels launched by this library (host-side bookkeeping; every
+// launcher below adds the launches it issues).
+extern long long g_thorin_launches;
+
 // kernels_hydro.cu
 void hydro_substep1(const DevGrid &g, const double *rho, const double *vrad, const double *vtheta,
                     const double *energy, const double *agr, const double *agt, const double *dragr, const double *dragt,

@@ -78,3 +78,20 @@ class GpuDisk:
         s = ThorinStats()
         _lib.check(self.L.thorin_gpu_get_stats(self.h, C.byref(s)), "stats")
         return s
+
+    def sor_state(self):
+        om, dom, nl, cal = C.c_double(), C.c_double(), C.c_int(), C.c_int()
+        _lib.check(self.L.thorin_gpu_get_sor_state(self.h, C.byref(om), C.byref(dom), C.byref(nl), C.byref(cal)),
+                   "get_sor_state")
+        return om.value, dom.value, nl.value, bool(cal.value)
+
+    def set_sor_state(self, omega: float, domega: float, niterlast: int):
+        _lib.check(self.L.thorin_gpu_set_sor_state(self.h, omega, domega, niterlast), "set_sor_state")
+
+    def set_timing(self, on: bool):
+        _lib.check(self.L.thorin_gpu_set_timing(self.h, 1 if on else 0), "set_timing")
+
+    def stream(self) -> int:
+        ptr = C.c_void_p()
+        _lib.check(self.L.thorin_gpu_get_stream(self.h, C.byref(ptr)), "get_stream")
+        return ptr.value or 0

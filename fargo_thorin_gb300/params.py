@@ -188,7 +188,8 @@ class ThorinPlanets(C.Structure):
 class ThorinStats(C.Structure):
     _fields_ = [("substeps", C.c_int), ("sor_calls", C.c_int), ("sor_sweeps", C.c_longlong),
                 ("sor_last_niter", C.c_int), ("sor_omega", C.c_double), ("crashed", C.c_int),
-                ("physical_time", C.c_double), ("last_dt", C.c_double)]
+                ("physical_time", C.c_double), ("last_dt", C.c_double), ("sor_time_ms", C.c_double),
+                ("sor_passes", C.c_longlong), ("step_time_ms", C.c_double), ("kernel_launches", C.c_longlong)]
 
 
 def _yes(s: str, ch: str) -> bool:

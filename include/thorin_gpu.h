@@ -166,6 +166,10 @@ typedef struct thorin_stats {
   int    crashed;                /* DetectCrash result of the last substep      */
   double physical_time;
   double last_dt;
+  double sor_time_ms;            /* device time of SOR sweeps (timing on)       */
+  long long sor_passes;          /* colour passes that did work (timing on)     */
+  double step_time_ms;           /* device time of the last thorin_gpu_algogas  */
+  long long kernel_launches;     /* kernels launched by the library so far      */
 } thorin_stats;
 
 /* Fill p with the reference defaults of src_main/var.c and nrad x nsec. */
@@ -251,6 +255,20 @@ int thorin_gpu_integrals(thorin_disk *d, double *mass, double *momentum,
 int thorin_gpu_get_nshift(thorin_disk *d, int *host);
 
 int thorin_gpu_get_stats(thorin_disk *d, thorin_stats *s);
+
+/* SOR over-relaxation schedule (EnergySources.c:298-317).  The reference
+ * calibrates omega on its first solve (IterateRelaxationParameter,
+ * :340-403) and then nudges it by +-domega each call; get/set lets a
+ * restarted run continue the schedule instead of recalibrating. */
+int thorin_gpu_get_sor_state(thorin_disk *d, double *omega, double *domega, int *niterlast, int *calibrated);
+int thorin_gpu_set_sor_state(thorin_disk *d, double omega, double domega, int niterlast);
+
+/* Device timing of the SOR sweeps and of whole DTs with CUDA events on the
+ * library's stream (counters in thorin_stats). */
+int thorin_gpu_set_timing(thorin_disk *d, int on);
+
+/* The CUDA stream all work of this disk is issued on (cudaStream_t). */
+int thorin_gpu_get_stream(thorin_disk *d, void **stream);
 
 /* Last CUDA error string (thread-local, for diagnostics). */
 const char *thorin_gpu_last_error(void);

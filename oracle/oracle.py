@@ -29,7 +29,8 @@ def build(force: bool = False) -> None:
     for out, extra in ((LIB_SEQ, []), (LIB_OMP, ["-fopenmp", "-DORACLE_OMP"])):
         if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(SRC):
             continue
-        cmd = ["gcc", "-O2", "-std=c99", "-fPIC", "-shared", *extra, SRC, "-o", out + ".tmp", "-lm"]
+        cmd = ["gcc", "-O2", "-std=c99", "-Wno-unknown-pragmas", "-fPIC", "-shared", *extra, SRC, "-o", out + ".tmp",
+               "-lm"]
         subprocess.run(cmd, check=True)
         os.replace(out + ".tmp", out)
 
@@ -60,6 +61,7 @@ def lib(omp: bool = False):
         L.ora_algogas.restype = C.c_int
         L.ora_algogas.argtypes = [C.c_void_p, C.POINTER(ThorinPlanets)]
         L.ora_integrals.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 5
+        L.ora_set_sor_state.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int]
         _libs[path] = L
     return _libs[path]
 
@@ -115,3 +117,6 @@ class OracleDisk:
         vals = [C.c_double() for _ in range(5)]
         self.L.ora_integrals(self.h, *[C.byref(v) for v in vals])
         return tuple(v.value for v in vals)
+
+    def set_sor_state(self, omega: float, domega: float, niterlast: int):
+        self.L.ora_set_sor_state(self.h, omega, domega, niterlast)

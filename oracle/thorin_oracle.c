@@ -52,6 +52,14 @@
 #define EVAPOREDSIGMA 1.0e-8                            /* Pebbles.c:832 */
 #define KAPPAFLOOR 1.0e-12                              /* Opacity.c:29 */
 
+/* The OpenMP build (the CPU baseline) parallelises the same loops as the
+ * reference's OpenMP build; the sequential build ignores the pragmas. */
+#ifdef _OPENMP
+#define OMP_FOR _Pragma("omp parallel for schedule(static)")
+#else
+#define OMP_FOR
+#endif
+
 typedef struct ora_disk {
   thorin_params p;
   int nr, ns;
@@ -134,6 +142,7 @@ static double AspectRatio(const ora_disk *d, double rad)
 /* mpi_make1Dprofile, sequential build: mpiTasks.c:12-36 */
 static void make1Dprofile(const ora_disk *d, const double *f, double *axi)
 {
+  OMP_FOR
   for (int i = 0; i < d->nr; i++) {
     double s = 0.0;
     for (int j = 0; j < d->ns; j++) s += f[i * d->ns + j];
@@ -224,6 +233,7 @@ static void ComputeSoundSpeed(ora_disk *d, const double *rho, const double *ener
 {
   const thorin_params *p = &d->p;
   int nr = d->nr, ns = d->ns;
+  OMP_FOR
   for (int i = 0; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns;
@@ -238,6 +248,7 @@ static void ComputeSoundSpeed(ora_disk *d, const double *rho, const double *ener
 static void ComputePressureField(ora_disk *d, const double *rho, const double *energy)
 {
   int nr = d->nr, ns = d->ns;
+  OMP_FOR
   for (int i = 0; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns;
@@ -249,6 +260,7 @@ static void ComputePressureField(ora_disk *d, const double *rho, const double *e
 static void ComputeTemperatureField(ora_disk *d, const double *rho, const double *energy)
 {
   int nr = d->nr, ns = d->ns;
+  OMP_FOR
   for (int i = 0; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns;
@@ -618,6 +630,7 @@ static void DampingBoundary(ora_disk *d, double step)       /* SideEuler.c:368-4
 {
   const thorin_params *p = &d->p;
   double DRin = p->rmin * p->damping_rmin_frac, DRout = p->rmax * p->damping_rmax_frac;
+  OMP_FOR
   for (int i = 0; i < d->nr; i++) {
     if (d->Rmed[i] < DRin || d->Rmed[i] > DRout) {
       double vrad0 = 0.0, vtheta0 = 0.0, rho0 = 0.0, energy0 = 0.0, lambda;
@@ -647,6 +660,7 @@ static void DampPebbles(ora_disk *d, double dt)             /* SideEuler.c:423-4
 {
   const thorin_params *p = &d->p;
   double DRin = p->rmin * p->damping_rmin_frac, DRout = p->rmax * p->damping_rmax_frac;
+  OMP_FOR
   for (int i = 0; i < d->nr; i++) {
     if (d->Rmed[i] < DRin || d->Rmed[i] > DRout) {
       double lambda = d->WaveKiller[i] * dt;
@@ -673,7 +687,10 @@ static int DetectCrash(const ora_disk *d, const double *f)  /* SourceEuler.c:48-
 static void CriticalCharTime(ora_disk *d)
 {
   int ns = d->ns;
-  d->invdtpeb_sq = -1.e30;
+  double mx = -1.e30;
+#ifdef _OPENMP
+#pragma omp parallel for reduction(max : mx)
+#endif
   for (int i = 1; i < d->nr; i++) {
     double dxrad = d->Rsup[i] - d->Rinf[i], dxtheta = d->Rmed[i] * 2.0 * PI / (double)ns, pvtmed = 0.0;
     if (d->p.fast_transport) {
@@ -688,33 +705,34 @@ static void CriticalCharTime(ora_disk *d)
       double invdt3 = fabs(d->pvrad[l] - d->vrad[l]) / dxrad;
       double invdt4 = fabs(d->pvtheta[l] - d->vtheta[l]) / dxtheta;
       double temp = invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4;
-      if (temp > d->invdtpeb_sq) d->invdtpeb_sq = temp;   /* max2 */
+      if (temp > mx) mx = temp;   /* max2 */
     }
   }
+  d->invdtpeb_sq = mx;
 }
 
 static int ConditionCFL(ora_disk *d, double deltaT)
 {
   const thorin_params *p = &d->p;
   int nr = d->nr, ns = d->ns;
-  double newdt = 1e30, invdt5 = 1e-30, *Vres = vec(ns + 1);
+  double newdt = 1e30;
+  OMP_FOR
   for (int i = 0; i < nr; i++) {
     double s = 0.0;
     for (int j = 0; j < ns; j++) s += d->vtheta[j + i * ns];
     d->Vmoy[i] = s / (double)ns;
   }
+#ifdef _OPENMP
+#pragma omp parallel for reduction(min : newdt)
+#endif
   for (int i = 1; i < nr; i++) {
-    double dxrad = d->Rsup[i] - d->Rinf[i], dxtheta = d->Rmed[i] * 2.0 * PI / (double)ns;
-    for (int j = 0; j < ns; j++) {
-      int l = j + i * ns;
-      Vres[j] = p->fast_transport ? d->vtheta[l] - d->Vmoy[i] : d->vtheta[l];
-    }
+    double dxrad = d->Rsup[i] - d->Rinf[i], dxtheta = d->Rmed[i] * 2.0 * PI / (double)ns, invdt5 = 1e-30;
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lip = l + ns, ljp = (j == ns - 1) ? i * ns : l + 1;
       double cs = d->cs[l], mindx = (dxtheta < dxrad) ? dxtheta : dxrad;   /* min2(dxrad,dxtheta) */
       double invdt1 = cs / mindx;
       double invdt2 = fabs(d->vrad[l]) / dxrad;
-      double invdt3 = fabs(Vres[j]) / dxtheta;
+      double invdt3 = fabs(p->fast_transport ? d->vtheta[l] - d->Vmoy[i] : d->vtheta[l]) / dxtheta;
       double dvr = d->vrad[lip] - d->vrad[l], dvt = d->vtheta[ljp] - d->vtheta[l], invdt4, dt;
       if (dvr >= 0.0) dvr = 1e-10; else dvr = -dvr;
       if (dvt >= 0.0) dvt = 1e-10; else dvt = -dvt;
@@ -739,7 +757,6 @@ static int ConditionCFL(ora_disk *d, double deltaT)
   newdt = (newdt < p->maximum_step) ? newdt : p->maximum_step;
   if (d->cfl_count == 0) { if (p->first_step > 0.0) newdt = p->first_step; d->cfl_count = 1; }
   if (deltaT < newdt) newdt = deltaT;
-  free(Vres);
   return (int)(ceil(deltaT / newdt));
 }
 
@@ -749,6 +766,7 @@ static void UpdateDivVelocAndStressTensor(ora_disk *d, const double *vr, const d
 {
   int nr = d->nr, ns = d->ns;
   double dphi = 2.0 * M_PI / (double)ns, invdphi = 1.0 / dphi, onethird = 1.0 / 3.0;
+  OMP_FOR
   for (int i = 0; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lip = l + ns, ljp = (j == ns - 1) ? i * ns : l + 1;
@@ -757,12 +775,14 @@ static void UpdateDivVelocAndStressTensor(ora_disk *d, const double *vr, const d
       d->divv[l] = (vr[lip] * d->Rsup[i] - vr[l] * d->Rinf[i]) * d->InvDiffRsup[i] * d->InvRmed[i];
       d->divv[l] += (vt[ljp] - vt[l]) * invdphi * d->InvRmed[i];
     }
+  OMP_FOR
   for (int i = 1; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, ljm = (j == 0) ? i * ns + ns - 1 : l - 1, lim = l - ns;
       d->Drp[l] = 0.5 * (d->Rinf[i] * (vt[l] * d->InvRmed[i] - vt[lim] * d->InvRmed[i - 1]) * d->InvDiffRmed[i] +
                          (vr[l] - vr[ljm]) * invdphi * d->InvRinf[i]);
     }
+  OMP_FOR
   for (int i = 0; i < nr; i++) {
     double viscosity = FViscosity(d, d->Rmed[i]);
     for (int j = 0; j < ns; j++) {
@@ -771,6 +791,7 @@ static void UpdateDivVelocAndStressTensor(ora_disk *d, const double *vr, const d
       d->Tpp[l] = 2.0 * rho[l] * viscosity * (d->Dpp[l] - onethird * d->divv[l]);
     }
   }
+  OMP_FOR
   for (int i = 1; i < nr; i++) {
     double viscosity = FViscosity(d, d->Rinf[i]);
     for (int j = 0; j < ns; j++) {
@@ -784,6 +805,7 @@ static void UpdateVelocityWithViscousTerms(ora_disk *d, double *vr, double *vt, 
 {
   int nr = d->nr, ns = d->ns;
   double invdphi = 1.0 / (2.0 * M_PI / (double)ns);
+  OMP_FOR
   for (int i = 1; i < nr - 1; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lip = l + ns, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
@@ -791,6 +813,7 @@ static void UpdateVelocityWithViscousTerms(ora_disk *d, double *vr, double *vt, 
                                          (d->Tpp[l] - d->Tpp[ljm]) * invdphi + 0.5 * (d->Trp[l] + d->Trp[lip])) /
                (0.5 * (rho[l] + rho[ljm]));
     }
+  OMP_FOR
   for (int i = 1; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lim = l - ns, ljp = (j == ns - 1) ? i * ns : l + 1;
@@ -817,6 +840,7 @@ static void SubStep1(ora_disk *d, double dt)
   const thorin_params *p = &d->p;
   int nr = d->nr, ns = d->ns;
   const double *rho = d->rho, *vrad = d->vrad, *vtheta = d->vtheta, *press = d->press;
+  OMP_FOR
   for (int i = 1; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lim = l - ns, ljp = (j == ns - 1) ? i * ns : l + 1;
@@ -835,6 +859,7 @@ static void SubStep1(ora_disk *d, double dt)
         }
       }
     }
+  OMP_FOR
   for (int i = 0; i < nr; i++) {
     double supp_torque = p->imposed_disk_drift * .5 * pow(d->Rmed[i], -2.5 + p->sigma_slope);
     double dxtheta = 2.0 * PI / (double)ns * d->Rmed[i], invdxtheta = 1.0 / dxtheta;
@@ -865,6 +890,7 @@ static void SubStep2(ora_disk *d, double dt)
   int nr = d->nr, ns = d->ns;
   const double *rho = d->rho, *vrad = d->VradInt, *vtheta = d->VthetaInt;
   double *qr = d->RhoInt, *qt = d->TemperInt;
+  OMP_FOR
   for (int i = 0; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lip = l + ns, ljp = (j == ns - 1) ? i * ns : l + 1;
@@ -873,11 +899,13 @@ static void SubStep2(ora_disk *d, double dt)
       dv = vtheta[ljp] - vtheta[l];
       qt[l] = (dv < 0.0) ? CVNR * CVNR * rho[l] * dv * dv : 0.0;
     }
+  OMP_FOR
   for (int i = 1; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lim = l - ns;
       d->VradNew[l] = vrad[l] - dt * 2.0 / (rho[l] + rho[lim]) * (qr[l] - qr[lim]) * d->InvDiffRmed[i];
     }
+  OMP_FOR
   for (int i = 0; i < nr; i++) {
     double dxtheta = 2.0 * PI / (double)ns * d->Rmed[i], invdxtheta = 1.0 / dxtheta;
     for (int j = 0; j < ns; j++) {
@@ -917,6 +945,7 @@ static double EffectiveOpticalDepth(const ora_disk *d, double tau)   /* EnergySo
 
 static void MidplaneVolumeDensity(ora_disk *d)              /* EnergySources.c:658-680 */
 {
+  OMP_FOR
   for (int i = 0; i < d->nr; i++)
     for (int j = 0; j < d->ns; j++) {
       int l = j + i * d->ns;
@@ -932,12 +961,14 @@ static void OpacityProfile(ora_disk *d)                     /* Opacity.c:231-266
     for (int l = 0; l < d->nr * d->ns; l++) d->opacity[l] = tmp;
     return;
   }
+  OMP_FOR
   for (int l = 0; l < d->nr * d->ns; l++)
     d->opacity[l] = opacity_func(d, d->voldens[l] * RHO2CGS, d->temper[l] * T2SI) * OPA2CU;
 }
 
 static void CalculateQminus(ora_disk *d)                    /* EnergySources.c:75-99 */
 {
+  OMP_FOR
   for (int l = 0; l < d->nr * d->ns; l++) {
     double tau = d->p.opacity_drop * 0.5 * d->opacity[l] * d->rho[l];
     double taueff = EffectiveOpticalDepth(d, tau);
@@ -949,6 +980,7 @@ static void CalculateFlaring(ora_disk *d)                   /* EnergySources.c:1
 {
   int nr = d->nr, ns = d->ns;
   double *cs = d->cs, *fl = d->flaring, Rstar = d->Rstar;
+  OMP_FOR
   for (int i = 1; i < nr - 1; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lip = l + ns, lim = l - ns;
@@ -980,6 +1012,7 @@ static void CalculateQirr(ora_disk *d)                      /* EnergySources.c:1
     double Rstar2 = pow(p->stellar_radius * (6.957e8 / AU_SI), 2.0);
     d->Tirr4fac = (1.0 - p->disc_albedo) * Teff4 * Rstar2;
   }
+  OMP_FOR
   for (int i = 0; i < d->nr; i++) {
     double r2inv = 1.0 / d->Rmed2[i];
     for (int j = 0; j < d->ns; j++) {
@@ -997,6 +1030,7 @@ static void TemperatureGradient(ora_disk *d)                /* EnergySources.c:6
 {
   int nr = d->nr, ns = d->ns;
   const double *T = d->temper;
+  OMP_FOR
   for (int i = 1; i < nr; i++) {
     double dxtheta = 2.0 * PI / (double)ns * d->Rmed[i], invdxtheta = 1.0 / dxtheta;
     for (int j = 0; j < ns; j++) {
@@ -1005,6 +1039,7 @@ static void TemperatureGradient(ora_disk *d)                /* EnergySources.c:6
       d->GradTt[l] = (T[l] - T[ljm]) * invdxtheta;
     }
   }
+  OMP_FOR
   for (int i = 1; i < nr - 1; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lip = l + ns, ljp = (j == ns - 1) ? i * ns : l + 1;
@@ -1017,6 +1052,7 @@ static void DiffusionCoefs(ora_disk *d)                     /* EnergySources.c:5
 {
   int nr = d->nr, ns = d->ns;
   TemperatureGradient(d);
+  OMP_FOR
   for (int i = 0; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns;
@@ -1025,6 +1061,7 @@ static void DiffusionCoefs(ora_disk *d)                     /* EnergySources.c:5
       double s = 4.0 * gradt * fac / d->temper[l];
       d->Dcen[l] = FluxLimiterValue(s) * 16.0 * STEFANBOLTZMANN * pow(d->temper[l], 3.0) * fac;
     }
+  OMP_FOR
   for (int i = 1; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lim = l - ns, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
@@ -1036,6 +1073,9 @@ static void DiffusionCoefs(ora_disk *d)                     /* EnergySources.c:5
 static void DiffusionTimestep(ora_disk *d)                  /* EnergySources.c:833-856 */
 {
   double dtmin = 1.0e38;
+#ifdef _OPENMP
+#pragma omp parallel for reduction(min : dtmin)
+#endif
   for (int i = 0; i < d->nr; i++) {
     double dr2 = d->Rsup[i] - d->Rinf[i];
     dr2 = dr2 * dr2 / 2.0;
@@ -1054,6 +1094,9 @@ static int SuccessiveOverrelaxation(ora_disk *d, double omega, int *maxed)
   double *T = d->temper, normres0 = 0.0, normres = 0.0;
   const double *Ml = d->Ml, *Mlip = d->Mlip, *Mlim = d->Mlim, *Mljp = d->Mljp, *Mljm = d->Mljm, *RHS = d->RHS;
   *maxed = 0;
+#ifdef _OPENMP
+#pragma omp parallel for reduction(+ : normres0)
+#endif
   for (int i = 1; i < nr - 1; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lip = l + ns, lim = l - ns, ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
@@ -1064,8 +1107,12 @@ static int SuccessiveOverrelaxation(ora_disk *d, double omega, int *maxed)
     int changed = 0;
     normres = 0.0;
     for (int ipass = 1; ipass <= 2; ipass++) {
-      int jchess = (ipass == 1) ? d->jchess1st : d->jchess2nd;
+      const int jstart = (ipass == 1) ? d->jchess1st : d->jchess2nd;
+#ifdef _OPENMP
+#pragma omp parallel for reduction(+ : normres, changed)
+#endif
       for (int i = 1; i < nr - 1; i++) {
+        const int jchess = jstart ^ ((i - 1) & 1);   /* flips every ring */
         for (int j = jchess; j < ns; j += 2) {
           int l = j + i * ns, lip = l + ns, lim = l - ns, ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
           double resid = T[l] * Ml[l] + T[lip] * Mlip[l] + T[lim] * Mlim[l] + T[ljp] * Mljp[l] + T[ljm] * Mljm[l] - RHS[l];
@@ -1074,7 +1121,6 @@ static int SuccessiveOverrelaxation(ora_disk *d, double omega, int *maxed)
           T[l] -= delta;
           if (delta > T[l] * SORPRECISION) changed++;
         }
-        jchess = 1 - jchess;
       }
     }
     if (normres < d->p.sor_eps * normres0) return n;
@@ -1130,6 +1176,7 @@ static int ImplicitRadiativeDiffusion(ora_disk *d, double dt)   /* EnergySources
   if (p->stellar_irradiation) { CalculateFlaring(d); CalculateQirr(d); }
   DiffusionCoefs(d);
   DiffusionTimestep(d);
+  OMP_FOR
   for (int i = 1; i < nr; i++) {
     double dxtheta = 2.0 * PI / (double)ns * d->Rmed[i], invdxtheta2 = 1.0 / dxtheta / dxtheta;
     for (int j = 0; j < ns; j++) {
@@ -1139,6 +1186,7 @@ static int ImplicitRadiativeDiffusion(ora_disk *d, double dt)   /* EnergySources
       d->B[l] = d->Dt[l] * invdxtheta2 * 2.0 * H;
     }
   }
+  OMP_FOR
   for (int i = 1; i < nr - 1; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lip = l + ns, ljp = (j == ns - 1) ? i * ns : l + 1;
@@ -1170,8 +1218,11 @@ static int ImplicitRadiativeDiffusion(ora_disk *d, double dt)   /* EnergySources
   d->st.sor_calls++; d->st.sor_sweeps += Niter; d->st.sor_last_niter = Niter; d->st.sor_omega = d->omega;
   if (Niter > d->Niterlast) d->domega = -d->domega;
   d->Niterlast = Niter;
+  OMP_FOR
   for (int j = 0; j < ns; j++) d->temper[j] = d->temper[j + ns];
+  OMP_FOR
   for (int j = 0; j < ns; j++) d->temper[j + (nr - 1) * ns] = d->temper[j + (nr - 2) * ns];
+  OMP_FOR
   for (int l = 0; l < nr * ns; l++) d->EnergyNew[l] = d->rho[l] * d->temper[l] * d->CV;
   return status;
 }
@@ -1181,8 +1232,9 @@ static int SubStep3(ora_disk *d, double dt)                 /* SourceEuler.c:508
   int nr = d->nr, ns = d->ns;
   const double *rho = d->rho;
   double r0 = d->Rmed[0], r1 = d->Rmed[1], r2 = d->Rmed[2], viscosity;
+  OMP_FOR
   for (int i = 1; i < nr; i++) {
-    viscosity = FViscosity(d, d->Rmed[i]);
+    const double viscosity = FViscosity(d, d->Rmed[i]);
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns;
       if (viscosity != 0.0) {
@@ -1192,6 +1244,7 @@ static int SubStep3(ora_disk *d, double dt)                 /* SourceEuler.c:508
     }
   }
   viscosity = FViscosity(d, d->Rmed[0]);
+  OMP_FOR
   for (int j = 0; j < ns; j++) {
     double q1 = d->qplus[j + ns], q2 = d->qplus[j + 2 * ns];
     if (viscosity != 0.0) d->qplus[j] = q1 * exp(log(q1 / q2) * log(r0 / r1) / log(r1 / r2));
@@ -1205,6 +1258,7 @@ static int SubStep3(ora_disk *d, double dt)                 /* SourceEuler.c:508
 static void ComputeLRMomenta(ora_disk *d, const double *rho, const double *vr, const double *vt)   /* :318-347 */
 {
   int nr = d->nr, ns = d->ns;
+  OMP_FOR
   for (int i = 0; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lip = l + ns, ljp = (j == ns - 1) ? i * ns : l + 1;
@@ -1218,6 +1272,7 @@ static void ComputeLRMomenta(ora_disk *d, const double *rho, const double *vr, c
 static void ComputeVelocities(ora_disk *d, const double *rho, double *vr, double *vt)   /* :350-381 */
 {
   int nr = d->nr, ns = d->ns;
+  OMP_FOR
   for (int i = 0; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lim = l - ns, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
@@ -1232,6 +1287,7 @@ static void DivisePolarGrid(const ora_disk *d, const double *num, const double *
   /* The reference swaps Nrad/Nsec in the bounds; the covered index range is
    * l < (nsec+1)*nrad.  Only rows 0..nrad-1 are read afterwards. */
   int cnt = (d->ns + 1) * d->nr;
+  OMP_FOR
   for (int l = 0; l < cnt; l++) res[l] = num[l] / (den[l] + 1e-20);
 }
 
@@ -1239,6 +1295,7 @@ static void ComputeStarRad(ora_disk *d, const double *qb, const double *vr, doub
 {
   int nr = d->nr, ns = d->ns;
   double *dq = d->dq;
+  OMP_FOR
   for (int j = 0; j < ns; j++) {
     for (int i = 0; i < nr; i++) {
       int l = j + i * ns, lq = i + j * nr, lip = l + ns, lim = l - ns;
@@ -1262,6 +1319,7 @@ static void ComputeStarTheta(ora_disk *d, const double *qb, const double *vt, do
 {
   int nr = d->nr, ns = d->ns;
   double *dq = d->dq;
+  OMP_FOR
   for (int i = 0; i < nr; i++) {
     double dxtheta = 2.0 * PI / (double)ns * d->Rmed[i], invdxtheta = 1.0 / dxtheta;
     for (int j = 0; j < ns; j++) {
@@ -1284,6 +1342,7 @@ static void VanLeerRadial(ora_disk *d, const double *vr, double *qb, double dt) 
   double dtheta = 2.0 * PI / (double)ns;
   DivisePolarGrid(d, qb, d->RhoInt, d->Work);
   ComputeStarRad(d, d->Work, vr, d->QRStar, dt);
+  OMP_FOR
   for (int i = 0; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lip = l + ns;
@@ -1298,6 +1357,7 @@ static void VanLeerTheta(ora_disk *d, const double *vt, double *qb, double dt)  
   int nr = d->nr, ns = d->ns;
   DivisePolarGrid(d, qb, d->RhoInt, d->Work);
   ComputeStarTheta(d, d->Work, vt, d->QRStar, dt);
+  OMP_FOR
   for (int i = 0; i < nr; i++) {
     double dxrad = (d->Rsup[i] - d->Rinf[i]) * dt, invsurf = 1.0 / d->Surf[i];
     for (int j = 0; j < ns; j++) {
@@ -1313,6 +1373,7 @@ static void ComputeResiduals(ora_disk *d, double *vt, double dt)   /* :70-111 */
 {
   int nr = d->nr, ns = d->ns;
   double invdt = 1.0 / dt, dpinvns = 2.0 * PI / (double)ns;
+  OMP_FOR
   for (int i = 0; i < nr; i++) {
     double moy = 0.0;
     for (int j = 0; j < ns; j++) moy += vt[j + i * ns];
@@ -1333,6 +1394,7 @@ static void ComputeResiduals(ora_disk *d, double *vt, double dt)   /* :70-111 */
 static void AdvectSHIFT(ora_disk *d, double *val)           /* :113-136 */
 {
   int nr = d->nr, ns = d->ns;
+  OMP_FOR
   for (int i = 0; i < nr; i++) {
     for (int j = 0; j < ns; j++) {
       int ji = j - d->Nshift[i];
@@ -1386,6 +1448,7 @@ static void TransportFluid(ora_disk *d, double *rho, double *vr, double *vt, dou
 /* Pebbles: Pebbles.c                                                    */
 static void PebbleStokesNumbers(ora_disk *d)                /* :280-300 */
 {
+  OMP_FOR
   for (int l = 0; l < d->nr * d->ns; l++)
     d->tau[l] = 2.0 * d->pebbulkdens * d->psize[l] / d->rho[l] * d->SQRT_ADIABIND_INV;
 }
@@ -1542,6 +1605,7 @@ static void EvaporatePebbles(ora_disk *d, double dt)        /* :834-864 */
   double facc = p->evaporation_rate * dt;
   if (facc > 1.0) facc = 1.0;
   double evaptemp = p->evaporation_temperature / T2SI;
+  OMP_FOR
   for (int l = 0; l < d->nr * d->ns; l++)
     if (d->temper[l] > evaptemp) {
       d->pdens[l] *= (1.0 - facc);
@@ -1554,6 +1618,7 @@ static void SourceTermsPebbles(ora_disk *d, double dt)      /* :550-613 */
   const thorin_params *p = &d->p;
   int nr = d->nr, ns = d->ns;
   DampPebbles(d, dt);
+  OMP_FOR
   for (int i = 1; i < nr; i++) {
     double Omega = 1.0 / d->OmegaInv[i];
     for (int j = 0; j < ns; j++) {
@@ -1568,6 +1633,7 @@ static void SourceTermsPebbles(ora_disk *d, double dt)      /* :550-613 */
       }
     }
   }
+  OMP_FOR
   for (int i = 0; i < nr; i++) {
     double Omega = 1.0 / d->OmegaInv[i];
     for (int j = 0; j < ns; j++) {
@@ -1584,6 +1650,7 @@ static void SourceTermsPebbles(ora_disk *d, double dt)      /* :550-613 */
 static void SubStep1Pebbles(ora_disk *d, double dt)         /* :617-652 */
 {
   int nr = d->nr, ns = d->ns;
+  OMP_FOR
   for (int i = 0; i < nr; i++) {
     double Omega = 1.0 / d->OmegaInv[i];
     for (int j = 0; j < ns; j++) {
@@ -1600,6 +1667,7 @@ static void ParticleDiffusion(ora_disk *d)                  /* :656-698 */
 {
   int nr = d->nr, ns = d->ns;
   const double *rho = d->rho, *pd = d->pdens;
+  OMP_FOR
   for (int i = 1; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns, lim = l - ns;
@@ -1608,6 +1676,7 @@ static void ParticleDiffusion(ora_disk *d)                  /* :656-698 */
       corr *= (pd[l] / rho[l] - pd[lim] / rho[lim]) * d->InvDiffRmed[i];
       d->pvrad[l] += corr;
     }
+  OMP_FOR
   for (int i = 0; i < nr; i++) {
     double dxtheta = 2.0 * PI / (double)ns * d->Rmed[i], invdxtheta = 1.0 / dxtheta;
     for (int j = 0; j < ns; j++) {
@@ -1646,6 +1715,7 @@ static void FillForcesArrays(ora_disk *d, thorin_planets *sys)
   double axpl[THORIN_MAXPLANETS], aypl[THORIN_MAXPLANETS];
   int IntegrateWithPlanet[THORIN_MAXPLANETS];
   double axstar = 0.0, aystar = 0.0, MassTaper = d->MassTaper;
+  for (int k = 0; k < THORIN_MAXPLANETS; k++) axpl[k] = aypl[k] = 0.0;
   size_t bytes = sizeof(double) * (size_t)(nr + 1) * (size_t)ns;
   memset(d->agr, 0, bytes); memset(d->agt, 0, bytes);
   if (peb) { memset(d->pagr, 0, bytes); memset(d->pagt, 0, bytes); }
@@ -1673,6 +1743,10 @@ static void FillForcesArrays(ora_disk *d, thorin_planets *sys)
   }
   double indpl_x = -axstar, indpl_y = -aystar;
   axstar = aystar = 0.0;
+#ifdef _OPENMP
+#pragma omp parallel for firstprivate(hillcut) private(s2, integpl, p_integpl, IntegrateWithPlanet) \
+    reduction(+ : axstar, aystar, axpl[:THORIN_MAXPLANETS], aypl[:THORIN_MAXPLANETS])
+#endif
   for (int i = 0; i < nr; i++) {
     double omegainv = d->OmegaInv[i], r2 = d->Rmed2[i], Rsup_Rinf2 = d->Rsup[i] - d->Rinf[i];
     Rsup_Rinf2 *= Rsup_Rinf2;
@@ -1832,6 +1906,7 @@ static void FillForcesArrays(ora_disk *d, thorin_planets *sys)
   for (int k = 0; k < npl; k++) { sys->ax[k] = axpl[k]; sys->ay[k] = aypl[k]; }
   double axindir = d->indirect_x, ayindir = d->indirect_y;
   if (p->indirect_term) { axindir += indpl_x; ayindir += indpl_y; }
+  OMP_FOR
   for (int i = 0; i < nr; i++)
     for (int j = 0; j < ns; j++) {
       int l = j + i * ns;
@@ -2044,4 +2119,14 @@ void ora_integrals(ora_disk *d, double *mass, double *mom, double *energy, doubl
     }
   }
   *mass = m; *mom = 0.5 * am; *energy = e; *pmass = pm; *pmom = 0.5 * pam;
+}
+
+/* Continue an SOR omega schedule instead of calibrating it (used to time
+ * steady-state substeps). */
+void ora_set_sor_state(ora_disk *d, double omega, double domega, int niterlast)
+{
+  d->omega = omega;
+  d->domega = domega;
+  d->Niterlast = niterlast;
+  d->sor_first = 0;
 }
