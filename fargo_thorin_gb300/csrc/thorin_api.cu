@@ -29,7 +29,7 @@
 #define FLUX2CU (0.000003 / (2.0 * H_PI))
 #define SQRT2PI_INV (1.0 / sqrt(2.0 * H_PI))
 
-static thread_local std::string g_last_error;
+thread_local std::string g_last_error;
 long long g_thorin_launches = 0;
 
 #define CUCHK(call)                                                                     \

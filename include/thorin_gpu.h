@@ -270,6 +270,26 @@ int thorin_gpu_set_timing(thorin_disk *d, int on);
 /* The CUDA stream all work of this disk is issued on (cudaStream_t). */
 int thorin_gpu_get_stream(thorin_disk *d, void **stream);
 
+/* Gas mass, angular momentum and total energy (the sums of GasTotalMass,
+ * GasMomentum and GasTotalEnergy) of fields the caller already holds in
+ * device memory, computed without allocating any device memory.  No
+ * counterpart in the reference: it is for callers that cannot allocate, such
+ * as a host program whose pool allocator already owns all free GPU memory, or
+ * a hook inside a latency-critical loop where a cudaMalloc (which can
+ * synchronise the device) is not acceptable.
+ * Inputs: rho, vrad, vtheta, energy in the PolarGrid layout ((nrad+1)*nsec
+ * doubles; vrad row nrad is read), and per-ring surf, rinf, rsup, rmed (nrad
+ * doubles) -- all device pointers.  Output: out[0..2] = mass, momentum,
+ * energy, a device pointer.  Work is issued on stream (a cudaStream_t, or
+ * NULL for the default stream); the call returns without waiting.
+ * Limit: 1 <= nrad <= 16384 (the reference's MAX1D); larger grids are
+ * rejected with THORIN_ERR_ARG.  The partial sums use one fixed device array
+ * per GPU, found on the first call made while that GPU is current (make that
+ * call before any stream capture); concurrent calls on one GPU race on it. */
+int thorin_integrals_static(const double *rho, const double *vrad, const double *vtheta, const double *energy,
+                            const double *surf, const double *rinf, const double *rsup, const double *rmed,
+                            int nrad, int nsec, double omega_frame, double *out, void *stream);
+
 /* Last CUDA error string (thread-local, for diagnostics). */
 const char *thorin_gpu_last_error(void);
 
