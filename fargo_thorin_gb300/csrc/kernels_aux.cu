@@ -13,34 +13,52 @@ static const int BX = 128;
   const int l = j + i * ns;
 
 // ---------------------------------------------------------------------------
-// Ring means summed in order (mpi_make1Dprofile, mpiTasks.c:12-36): one
-// warp per ring.
-__global__ void k_ring_mean(int nr, int ns, const double *__restrict__ f, double *__restrict__ out)
+// Ring (azimuthal) means, mpi_make1Dprofile (mpiTasks.c:26-32) and the
+// other azimuthal averages of the loop.  One warp per ring sums in a fixed
+// tree (lanes take strided columns, then a butterfly), so results are
+// deterministic; they differ from the reference's left-to-right sum in the
+// last bits.  The only integer decision fed by a ring mean, the FARGO shift,
+// re-sums its ring in order when the mean lands near a rounding tie (see
+// k_azimuthal).  Output index is relative to ring0.
+__global__ void __launch_bounds__(256) k_ring_means(int ns, const double *__restrict__ f0,
+                                                    const double *__restrict__ f1, double *__restrict__ o0,
+                                                    double *__restrict__ o1, int ring0, int nrings, int nf)
 {
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (w >= nr) return;
-  const double s = warp_seq_sum(f + (size_t)w * ns, ns);
-  if ((threadIdx.x & 31) == 0) out[w] = s / (double)ns;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= nrings) return;                         // whole warp
+  const size_t base = (size_t)(ring0 + w) * ns;
+  double a0 = 0.0, a1 = 0.0;
+  for (int j = lane; j < ns; j += 32) {
+    a0 += f0[base + j];
+    if (nf > 1) a1 += f1[base + j];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 += __shfl_xor_sync(TH_FULL, a0, o);
+    if (nf > 1) a1 += __shfl_xor_sync(TH_FULL, a1, o);
+  }
+  if (lane == 0) {
+    o0[w] = a0 / (double)ns;
+    if (nf > 1) o1[w] = a1 / (double)ns;
+  }
+}
+
+void aux_ring_means(const DevGrid &g, const double *f0, double *o0, const double *f1, double *o1, int ring0, int nrings,
+                    cudaStream_t s)
+{
+  if (nrings <= 0) return;
+  const int blocks = (nrings * 32 + 255) / 256;
+  k_ring_means<<<blocks, 256, 0, s>>>(g.ns, f0, f1 ? f1 : f0, o0, o1 ? o1 : o0, ring0, nrings, f1 ? 2 : 1);
+  g_thorin_launches++;
 }
 
 void aux_ring_mean(const DevGrid &g, const double *f, double *out, cudaStream_t s)
 {
-  const int threads = 256, warps = threads / 32;
-  k_ring_mean<<<(g.nr + warps - 1) / warps, threads, 0, s>>>(g.nr, g.ns, f, out);
-  g_thorin_launches++;
-}
-
-// Ring mean of one ring (e.g. the ring holding a planet).
-__global__ void k_ring_mean_at(int ns, const double *__restrict__ f, int ring, double *out)
-{
-  const double s = warp_seq_sum(f + (size_t)ring * ns, ns);
-  if (threadIdx.x == 0) *out = s / (double)ns;
+  aux_ring_means(g, f, out, nullptr, nullptr, 0, g.nr, s);
 }
 
 void aux_ring_mean_at(const DevGrid &g, const double *f, int ring, double *out, cudaStream_t s)
 {
-  k_ring_mean_at<<<1, 32, 0, s>>>(g.ns, f, ring, out);
-  g_thorin_launches++;
+  aux_ring_means(g, f, out, nullptr, nullptr, ring, 1, s);
 }
 
 // FViscosity at Rmed[i] and Rinf[i] (Viscosity.c:26-54).  The ring index
@@ -97,20 +115,6 @@ void aux_stokes(const DevGrid &g, const double *rho, const double *psize, double
 // monotone, the minimum over cells of the per-cell step equals the step of
 // the cell with the largest sum of squared rates, so block maxima of that
 // sum are reduced (exactly, in any order) and the step is formed once.
-
-__global__ void k_cfl_means(DevGrid g, const double *__restrict__ vt, const double *__restrict__ pvt, CflRings cr,
-                            int pebbles_fast)
-{
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (w >= g.nr) return;
-  const double s = warp_seq_sum(vt + (size_t)w * g.ns, g.ns);
-  double p = 0.0;
-  if (pebbles_fast) p = warp_seq_sum(pvt + (size_t)w * g.ns, g.ns);
-  if ((threadIdx.x & 31) == 0) {
-    cr.vmoy[w] = s / (double)g.ns;
-    if (pebbles_fast) cr.pvtmed[w] = p / (double)g.ns;
-  }
-}
 
 __global__ void k_cfl_cells(DevGrid g, const double *__restrict__ vr, const double *__restrict__ vt,
                             const double *__restrict__ cs, const double *__restrict__ pvr,
@@ -196,9 +200,8 @@ void aux_cfl(const DevGrid &g, const double *vr, const double *vt, const double 
              const CflRings &cr, int pebbles, int fast, int viscous, double *part, const CflFinal &f0, double *scal,
              int *iscal, cudaStream_t s)
 {
-  const int threads = 256, warps = threads / 32;
-  k_cfl_means<<<(g.nr + warps - 1) / warps, threads, 0, s>>>(g, vt, pvt, cr, pebbles && fast);
-  g_thorin_launches++;
+  if (pebbles && fast) aux_ring_means(g, vt, cr.vmoy, pvt, cr.pvtmed, 0, g.nr, s);
+  else aux_ring_means(g, vt, cr.vmoy, nullptr, nullptr, 0, g.nr, s);
   dim3 grid = grid2d(g.ns, g.nr - 1, 256);
   k_cfl_cells<<<grid, 256, 0, s>>>(g, vr, vt, cs, pvr, pvt, cr, pebbles, fast, viscous, part);
   g_thorin_launches++;
@@ -394,21 +397,15 @@ void aux_pebble_substep1(const DevGrid &g, double *pvr, double *pvt, const doubl
 // sound speed and Stokes number (sums in order) and the 10-node vertical
 // averages of the star's pull for the ring-mean scale height.
 
-__global__ void k_force_rings(DevGrid g, const double *__restrict__ cs, const double *__restrict__ tau, ForceRings fr,
-                              int pebbles, double pebble_alpha)
+__global__ void k_force_rings(DevGrid g, ForceRings fr, int pebbles, double pebble_alpha)
 {
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (w >= g.nr) return;
-  const int i = w;
-  const double csum = warp_seq_sum(cs + (size_t)i * g.ns, g.ns);
-  double tsum = 0.0;
-  if (pebbles) tsum = warp_seq_sum(tau + (size_t)i * g.ns, g.ns);
-  if ((threadIdx.x & 31) != 0) return;
-  const double cs_avr = csum / (double)g.ns;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.nr) return;
+  const double cs_avr = g.r.csmean[i];       // the ring mean of c_s, summed in order
   const double H_avr = cs_avr * g.r.OmegaInv[i] * g.k.sqrt_adiabind_inv;
   double tau_avr = 0.0, p_H_avr = 0.0, p_int = 0.0;
   if (pebbles) {
-    tau_avr = tsum / (double)g.ns;
+    tau_avr = fr.tau_avr[i];
     p_H_avr = H_avr * sqrt(pebble_alpha / tau_avr);
   }
   const double r2 = g.r.Rmed2[i];
@@ -433,9 +430,6 @@ __global__ void k_force_rings(DevGrid g, const double *__restrict__ cs, const do
   fr.p_H_avr[i] = p_H_avr;
   fr.p_integstar_avr[i] = p_int;
 }
-
-
-
 
 __global__ void k_forces(DevGrid g, ForceArgs a, ForceRings fr)
 {
@@ -640,8 +634,8 @@ __global__ void k_forces_indirect(DevGrid g, double *__restrict__ agr, double *_
 void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr, double indx_pl, double indy_pl,
                 double *scal, cudaStream_t s)
 {
-  const int threads = 256, warps = threads / 32;
-  k_force_rings<<<(g.nr + warps - 1) / warps, threads, 0, s>>>(g, a0.cs, a0.tau, fr, a0.pebbles, a0.pebble_alpha);
+  if (a0.pebbles) aux_ring_means(g, a0.tau, fr.tau_avr, nullptr, nullptr, 0, g.nr, s);
+  k_force_rings<<<(g.nr + 127) / 128, 128, 0, s>>>(g, fr, a0.pebbles, a0.pebble_alpha);
   g_thorin_launches++;
   dim3 grid = grid2d(g.ns, g.nr, 128);
   k_forces<<<grid, 128, 0, s>>>(g, a0, fr);
@@ -686,23 +680,35 @@ __device__ double column_mass(double a, double b, double Hpeb)
   return __longlong_as_double(0x7ff8000000000000ULL);   // the reference aborts here
 }
 
-__global__ void __launch_bounds__(256) k_accrete(DevGrid g, AccArgs a, double *__restrict__ scal)
+// The annulus work runs on many blocks in three grid passes (mean Stokes
+// number, upper limits per cell, application of the limiter), each followed
+// by a one-block kernel that sums the block partials in a fixed order and
+// does the scalar steps of the reference.
+// acc[] scalars: 0 Reff, 1 vrel, 2 Mt, 3 limiter.
+#define ACC_BX 256
+
+__global__ void __launch_bounds__(ACC_BX) k_acc_tau(DevGrid g, AccArgs a)
+{
+  const int ncells = (a.imax - a.imin + 1) * g.ns;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  double t = (q < ncells) ? a.tau[(size_t)a.imin * g.ns + q] : 0.0;
+  t = block_reduce(t, OpAdd(), 0.0);
+  if (threadIdx.x == 0) a.part[blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(ACC_BX) k_acc_reff(DevGrid g, AccArgs a, int nb)
 {
   const int ns = g.ns;
-  __shared__ double sh[8];
-  // vt1D at the two rings bracketing the planet (mpi_make1Dprofile of v_theta)
-  if (threadIdx.x < 32) {
-    const double s0 = warp_seq_sum(a.vt + (size_t)a.iflow * ns, ns);
-    double s1 = 0.0;                         // vt1D[nrad] is zero in the reference
-    if (a.iflow + 1 < g.nr) s1 = warp_seq_sum(a.vt + (size_t)(a.iflow + 1) * ns, ns);
-    if (threadIdx.x == 0) { sh[0] = s0 / (double)ns; sh[1] = s1 / (double)ns; }
+  __shared__ double sh[2];
+  if (threadIdx.x == 0) {                    // vt1D at the two rings bracketing the planet
+    sh[0] = a.acc[4];
+    sh[1] = (a.iflow + 1 < g.nr) ? a.acc[5] : 0.0;   // vt1D[nrad] is zero in the reference
   }
-  // STEP 1: mean tau over the annulus
   double ts = 0.0;
-  const int ncells = (a.imax - a.imin + 1) * ns;
-  for (int q = threadIdx.x; q < ncells; q += blockDim.x) ts += a.tau[(size_t)a.imin * ns + q];
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) ts += a.part[b];
   ts = block_reduce(ts, OpAdd(), 0.0);
   if (threadIdx.x == 0) {
+    const int ncells = (a.imax - a.imin + 1) * ns;
     const double tau_mean = ts / (double)ncells;
     const double flow = sh[0] * (1.0 - a.frac) + sh[1] * a.frac + a.Rp * a.omega_frame;
     const double flowx = -flow * a.Yp / a.Rp, flowy = flow * a.Xp / a.Rp;
@@ -716,17 +722,21 @@ __global__ void __launch_bounds__(256) k_accrete(DevGrid g, AccArgs a, double *_
       Reff = a.Rhill * pow(tau_mean / 0.1, 1.0 / 3.0);
     }
     if (Reff > a.Rhill) Reff = a.Rhill;
-    sh[2] = Reff;
-    sh[3] = vrel;
-    sh[4] = Mt;
+    a.acc[0] = Reff;
+    a.acc[1] = vrel;
+    a.acc[2] = Mt;
   }
-  __syncthreads();
-  const double Reff = sh[2], Reff2 = Reff * Reff;
-  // STEP 3: upper limit per cell within Reff
-  double dmu = 0.0, hpm = 0.0, pdm = 0.0;
-  int nc = 0;
-  for (int q = threadIdx.x; q < ncells; q += blockDim.x) {
-    const int i = a.imin + q / ns, j = q % ns, l = j + i * ns;
+}
+
+__global__ void __launch_bounds__(ACC_BX) k_acc_upper(DevGrid g, AccArgs a)
+{
+  const int ns = g.ns;
+  const int ncells = (a.imax - a.imin + 1) * ns;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const double Reff = a.acc[0], Reff2 = Reff * Reff;
+  double dmu = 0.0, hpm = 0.0, pdm = 0.0, nc = 0.0;
+  if (q < ncells) {
+    const int i = a.imin + q / ns, j = q - (q / ns) * ns, l = j + i * ns;
     const double xc = g.r.Rmed[i] * g.r.costab[j], yc = g.r.Rmed[i] * g.r.sintab[j];
     const double R2 = (xc - a.Xp) * (xc - a.Xp) + (yc - a.Yp) * (yc - a.Yp);
     if (R2 <= Reff2) {
@@ -738,29 +748,49 @@ __global__ void __launch_bounds__(256) k_accrete(DevGrid g, AccArgs a, double *_
       double dM = vdp * g.r.Surf[i] * column_mass(zmin, zmax, Hpeb);
       if (dM > mcell) dM = 0.99999999 * mcell;
       a.macc[l] = dM;
-      dmu += dM; hpm += Hpeb; pdm += a.pdens[l]; nc++;
+      dmu = dM; hpm = Hpeb; pdm = a.pdens[l]; nc = 1.0;
     }
   }
   dmu = block_reduce(dmu, OpAdd(), 0.0);
   hpm = block_reduce(hpm, OpAdd(), 0.0);
   pdm = block_reduce(pdm, OpAdd(), 0.0);
-  nc = block_reduce(nc, OpAddI(), 0);
+  nc = block_reduce(nc, OpAdd(), 0.0);
   if (threadIdx.x == 0) {
-    double Hpeb_mean = hpm, pdens_mean = pdm;
+    a.part[4 * blockIdx.x + 0] = dmu; a.part[4 * blockIdx.x + 1] = hpm;
+    a.part[4 * blockIdx.x + 2] = pdm; a.part[4 * blockIdx.x + 3] = nc;
+  }
+}
+
+__global__ void __launch_bounds__(ACC_BX) k_acc_limiter(AccArgs a, int nb, double pi, double sqrt2pi_inv)
+{
+  double v[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    for (int k = 0; k < 4; k++) v[k] += a.part[4 * b + k];
+  for (int k = 0; k < 4; k++) v[k] = block_reduce(v[k], OpAdd(), 0.0);
+  if (threadIdx.x == 0) {
+    const double dmu = v[0];
+    double Hpeb_mean = v[1], pdens_mean = v[2];
+    const int nc = (int)v[3];
     if (nc > 0) { Hpeb_mean /= (double)nc; pdens_mean /= (double)nc; }
-    const double vrel = sh[3], Mt = sh[4];
+    const double Reff = a.acc[0], vrel = a.acc[1], Mt = a.acc[2];
     const double veloc = (a.Mp < Mt) ? vrel : Reff * a.Omegap;
     double dM_model;
     if (Hpeb_mean < Reff) dM_model = 2.0 * Reff * veloc * pdens_mean;
-    else dM_model = TH_PI * Reff * Reff * veloc * pdens_mean / Hpeb_mean * g.k.sqrt2pi_inv;
+    else dM_model = pi * Reff * Reff * veloc * pdens_mean / Hpeb_mean * sqrt2pi_inv;
     dM_model *= a.dt;
-    sh[5] = (dmu > dM_model) ? dM_model / dmu : 1.0;
+    a.acc[3] = (dmu > dM_model) ? dM_model / dmu : 1.0;
   }
-  __syncthreads();
-  const double limiter = sh[5];
+}
+
+__global__ void __launch_bounds__(ACC_BX) k_acc_apply(DevGrid g, AccArgs a)
+{
+  const int ns = g.ns;
+  const int ncells = (a.imax - a.imin + 1) * ns;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const double limiter = a.acc[3];
   double dM_s = 0.0, dPx = 0.0, dPy = 0.0;
-  for (int q = threadIdx.x; q < ncells; q += blockDim.x) {
-    const int i = a.imin + q / ns, j = q % ns, l = j + i * ns;
+  if (q < ncells) {
+    const int i = a.imin + q / ns, j = q - (q / ns) * ns, l = j + i * ns;
     if (a.macc[l] > 0.0) {
       const double xc = g.r.Rmed[i] * g.r.costab[j], yc = g.r.Rmed[i] * g.r.sintab[j];
       const double vtcorr = g.r.Rmed[i] * a.omega_frame;
@@ -772,18 +802,47 @@ __global__ void __launch_bounds__(256) k_accrete(DevGrid g, AccArgs a, double *_
       double pd = (mcell - dM) / g.r.Surf[i];
       if (pd < 0.0) pd = 1.e-20;
       a.pdens[l] = pd;
-      dM_s += dM; dPx += dM * vxc; dPy += dM * vyc;
+      dM_s = dM; dPx = dM * vxc; dPy = dM * vyc;
     }
   }
   dM_s = block_reduce(dM_s, OpAdd(), 0.0);
   dPx = block_reduce(dPx, OpAdd(), 0.0);
   dPy = block_reduce(dPy, OpAdd(), 0.0);
-  if (threadIdx.x == 0) { scal[SC_ACC_DM] = dM_s; scal[SC_ACC_DPX] = dPx; scal[SC_ACC_DPY] = dPy; }
+  if (threadIdx.x == 0) {
+    a.part[3 * blockIdx.x + 0] = dM_s; a.part[3 * blockIdx.x + 1] = dPx; a.part[3 * blockIdx.x + 2] = dPy;
+  }
+}
+
+__global__ void __launch_bounds__(ACC_BX) k_acc_sum(AccArgs a, int nb, double *__restrict__ scal)
+{
+  double v[3] = {0.0, 0.0, 0.0};
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    for (int k = 0; k < 3; k++) v[k] += a.part[3 * b + k];
+  for (int k = 0; k < 3; k++) v[k] = block_reduce(v[k], OpAdd(), 0.0);
+  if (threadIdx.x == 0) { scal[SC_ACC_DM] = v[0]; scal[SC_ACC_DPX] = v[1]; scal[SC_ACC_DPY] = v[2]; }
+}
+
+int aux_accrete_blocks(const DevGrid &g, int imin, int imax)
+{
+  const int ncells = (imax - imin + 1) * g.ns;
+  return (ncells + ACC_BX - 1) / ACC_BX;
 }
 
 void aux_accrete(const DevGrid &g, const AccArgs &a, double *scal, cudaStream_t s)
 {
-  k_accrete<<<1, 256, 0, s>>>(g, a, scal);
+  const int nb = aux_accrete_blocks(g, a.imin, a.imax);
+  aux_ring_means(g, a.vt, a.acc + 4, nullptr, nullptr, a.iflow, (a.iflow + 1 < g.nr) ? 2 : 1, s);
+  k_acc_tau<<<nb, ACC_BX, 0, s>>>(g, a);
+  g_thorin_launches++;
+  k_acc_reff<<<1, ACC_BX, 0, s>>>(g, a, nb);
+  g_thorin_launches++;
+  k_acc_upper<<<nb, ACC_BX, 0, s>>>(g, a);
+  g_thorin_launches++;
+  k_acc_limiter<<<1, ACC_BX, 0, s>>>(a, nb, TH_PI, g.k.sqrt2pi_inv);
+  g_thorin_launches++;
+  k_acc_apply<<<nb, ACC_BX, 0, s>>>(g, a);
+  g_thorin_launches++;
+  k_acc_sum<<<1, ACC_BX, 0, s>>>(a, nb, scal);
   g_thorin_launches++;
 }
 

@@ -240,22 +240,51 @@ __global__ void k_eos(DevGrid g, const double *__restrict__ rho, const double *_
 }
 
 // Opacity laws, Opacity.c.
+// Bell & Lin (Opacity.c:31-75).  The thresholds T(i,j) solve
+// kappa_i rho^a_i T^b_i = kappa_j rho^a_j T^b_j.  The first branch
+// (T <= T(2,3), grains) covers almost the whole disk; its test
+// T <= (kappa_3/kappa_2 rho)^(1/24.5) is decided as T^49 <= (kappa_3/kappa_2
+// rho)^2 unless the two sides are within 1e-12, when the threshold itself is
+// evaluated with pow as in the reference.  The grain branch's integer and
+// half powers are products, quotients and square roots (each within a few
+// ulp of pow); the other branches keep pow.
+__device__ __forceinline__ double pow_int_pos(double x, int n)
+{
+  double r = 1.0, b = x;
+  while (n) { if (n & 1) r *= b; b *= b; n >>= 1; }
+  return r;
+}
+
 __device__ double opacity_BL94(double rho, double T)
 {
   const double kappa[8] = {2.0e-4, 2.0e16, 0.1, 2.0e81, 1.0e-8, 1.0e-36, 1.5e20, 0.348};
   const double a[8] = {0.0, 0.0, 0.0, 1.0, 2.0 / 3.0, 1.0 / 3.0, 1.0, 0.0};
   const double b[8] = {2.0, -7.0, 0.5, -24.0, 3.0, 10.0, -2.5, 0.0};
 #define TEMPB(i, j) pow(kappa[j] / kappa[i] * pow(rho, a[j] - a[i]), 1.0 / (b[i] - b[j]))
+  bool grains;
+  const double c23 = kappa[3] / kappa[2] * rho;            // (kappa_3/kappa_2) rho^(a_3-a_2), a_3-a_2 = 1
+  if (T > 0.0 && T < 1.0e5 && c23 > 0.0 && c23 < 1.0e150) {
+    const double lhs = pow_int_pos(T, 49), rhs = c23 * c23;
+    if (lhs < rhs * (1.0 - 1e-12)) grains = true;
+    else if (lhs > rhs * (1.0 + 1e-12)) grains = false;
+    else grains = (T <= TEMPB(2, 3));
+  } else {
+    grains = (T <= TEMPB(2, 3));
+  }
   double k;
-  if (T <= TEMPB(2, 3)) {
-    double k1 = kappa[0] * pow(T, b[0]);
-    double k2 = kappa[1] * pow(T, b[1]);
-    double k3 = kappa[2] * pow(T, b[2]);
+  if (grains) {
+    const double T2 = T * T;
+    const double k1 = kappa[0] * T2;                       // pow(T, 2.0)
+    const double k2 = kappa[1] / (T2 * T2 * T2 * T);        // pow(T, -7.0)
+    const double k3 = kappa[2] * sqrt(T);                  // pow(T, 0.5)
     double t1 = 1.0 / (k1 * k1) + 1.0 / (k2 * k2);
     t1 = 1.0 / (t1 * t1);
-    double t2 = pow(k3 / (1.0 + 1.0e22 * pow(T, -10.0)), 4.0);
-    k = pow(t1 + t2, 0.25);
-  } else if ((T > TEMPB(2, 3)) && (T <= TEMPB(3, 4))) {
+    const double T5 = T2 * T2 * T;
+    const double x = k3 / (1.0 + 1.0e22 / (T5 * T5));     // pow(T, -10.0)
+    const double x2 = x * x;
+    const double t2 = x2 * x2;                             // pow(., 4.0)
+    k = sqrt(sqrt(t1 + t2));                               // pow(., 0.25)
+  } else if (T <= TEMPB(3, 4)) {
     k = kappa[3] * pow(rho, a[3]) * pow(T, b[3]);
   } else if ((T > TEMPB(3, 4)) && (T <= TEMPB(4, 5))) {
     k = kappa[4] * pow(rho, a[4]) * pow(T, b[4]);
@@ -409,15 +438,26 @@ __global__ void k_irradiation(DevGrid g, const double *__restrict__ rho, const d
   }
 }
 
+// The SOR coefficients are stored packed by colour: for ring i, the cells
+// of pass 1 (j = i-1 mod 2) then those of pass 2, each as k = j/2, so that a
+// colour pass reads them contiguously.
+__device__ __forceinline__ size_t sor_pidx(int i, int j, int half)
+{
+  const int c = (j ^ (i - 1)) & 1;
+  return (size_t)((i << 1) + c) * half + (j >> 1);
+}
+
 // Matrix of the linearised implicit energy equation
-// (ImplicitRadiativeDiffusion, EnergySources.c:256-297).
+// (ImplicitRadiativeDiffusion, EnergySources.c:256-297), plus the
+// reciprocal of the diagonal used by the SOR update.
 __global__ void k_matrix(DevGrid g, const double *__restrict__ rho, const double *__restrict__ T,
                          const double *__restrict__ cs, const double *__restrict__ dcen, const double *__restrict__ divv,
                          const double *__restrict__ qminus, const double *__restrict__ qplus, const double *__restrict__ qirr,
                          double *__restrict__ ml, double *__restrict__ mlip, double *__restrict__ mlim,
-                         double *__restrict__ mljp, double *__restrict__ mljm, double *__restrict__ rhs, double dt,
-                         double gm1, const double *__restrict__ invdxtheta2_r, int irradiation, int nheat,
-                         const int *__restrict__ heat_idx, const double *__restrict__ heat_val)
+                         double *__restrict__ mljp, double *__restrict__ mljm, double *__restrict__ rhs,
+                         double *__restrict__ rml, double dt, double gm1, const double *__restrict__ invdxtheta2_r,
+                         int irradiation, int nheat, const int *__restrict__ heat_idx,
+                         const double *__restrict__ heat_val)
 {
   const int ns = g.ns;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -443,16 +483,19 @@ __global__ void k_matrix(DevGrid g, const double *__restrict__ rho, const double
   const double bfac = dt / (rho[l] * g.k.cv);
   const double afac = bfac * g.r.InvDiffRsup[i] * 2.0 * H / g.r.Rmed[i];
   const double Tl = T[l], qm = qminus[l];
-  ml[l] = 1.0 + divv[l] * gm1 * dt + 4.0 * bfac * qm + afac * (A_lip + A_l) + bfac * (B_ljp + B_l);
-  mlip[l] = -afac * A_lip;
-  mlim[l] = -afac * A_l;
-  mljp[l] = -bfac * B_ljp;
-  mljm[l] = -bfac * B_l;
+  const size_t q = sor_pidx(i, j, ns >> 1);
+  const double diag = 1.0 + divv[l] * gm1 * dt + 4.0 * bfac * qm + afac * (A_lip + A_l) + bfac * (B_ljp + B_l);
+  ml[q] = diag;
+  rml[q] = 1.0 / diag;
+  mlip[q] = -afac * A_lip;
+  mlim[q] = -afac * A_l;
+  mljp[q] = -bfac * B_ljp;
+  mljm[q] = -bfac * B_l;
   double r = Tl + bfac * (qplus[l] + 3.0 * qm * Tl);
   if (irradiation) r += bfac * qirr[l];
   for (int k = 0; k < nheat; k++)
     if (l == heat_idx[k]) r += bfac * heat_val[k];
-  rhs[l] = r;
+  rhs[q] = r;
 }
 
 // ---------------------------------------------------------------------------
@@ -463,43 +506,55 @@ __global__ void k_matrix(DevGrid g, const double *__restrict__ rho, const double
 // last block of pass 2 (ticketed with an atomic counter, no waiting) sums
 // both passes in a fixed order and evaluates the three exit tests.
 
-__device__ __forceinline__ double sor_resid(const double *T, const double *ml, const double *mlip, const double *mlim,
-                                            const double *mljp, const double *mljm, const double *rhs, int l, int lip,
-                                            int lim, int ljp, int ljm)
+__device__ __forceinline__ double sor_resid_at(const double *T, const double *ml, const double *mlip,
+                                               const double *mlim, const double *mljp, const double *mljm,
+                                               const double *rhs, int l, int lip, int lim, int ljp, int ljm, size_t q)
 {
-  return T[l] * ml[l] + T[lip] * mlip[l] + T[lim] * mlim[l] + T[ljp] * mljp[l] + T[ljm] * mljm[l] - rhs[l];
+  return T[l] * ml[q] + T[lip] * mlip[q] + T[lim] * mlim[q] + T[ljp] * mljp[q] + T[ljm] * mljm[q] - rhs[q];
 }
 
-__global__ void k_sor_resid0(DevGrid g, const double *__restrict__ T, const double *__restrict__ ml,
-                             const double *__restrict__ mlip, const double *__restrict__ mlim,
-                             const double *__restrict__ mljp, const double *__restrict__ mljm,
-                             const double *__restrict__ rhs, SorCtl c)
+// Sum of the block partials by the block holding the last ticket; every
+// block adds its partial first (no block ever waits on another).
+__device__ __forceinline__ bool sor_last_block(unsigned int *ticket, unsigned nb)
 {
-  const int ns = g.ns;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y + 1;
-  double a = 0.0;
-  if (j < ns) {
-    const int l = j + i * ns;
-    const int ljp = (j == ns - 1) ? i * ns : l + 1;
-    const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
-    a = fabs(sor_resid(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm));
-  }
-  a = block_reduce(a, OpAdd(), 0.0);
-  const int nb = gridDim.x * gridDim.y;
-  const int b = blockIdx.x + blockIdx.y * gridDim.x;
   __shared__ bool last;
   if (threadIdx.x == 0) {
-    c.part[b] = a;
     __threadfence();
-    unsigned t = atomicAdd(c.ticket, 1u);
-    last = (t == (unsigned)nb - 1);
+    const unsigned t = atomicAdd(ticket, 1u);
+    last = (t == nb - 1);
   }
   __syncthreads();
-  if (last) {
+  return last;
+}
+
+#define SOR_CPT 4        // cells of one colour per thread
+
+__global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__restrict__ T,
+                                                    const double *__restrict__ ml, const double *__restrict__ mlip,
+                                                    const double *__restrict__ mlim, const double *__restrict__ mljp,
+                                                    const double *__restrict__ mljm, const double *__restrict__ rhs,
+                                                    SorCtl c)
+{
+  const int ns = g.ns, half = ns >> 1;
+  const int i = blockIdx.y + 1;
+  double a = 0.0;
+  for (int m = 0; m < SOR_CPT; m++) {
+    const int j = blockIdx.x * blockDim.x * SOR_CPT + m * blockDim.x + threadIdx.x;
+    if (j < ns) {
+      const int l = j + i * ns;
+      const int ljp = (j == ns - 1) ? i * ns : l + 1;
+      const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+      a += fabs(sor_resid_at(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm, sor_pidx(i, j, half)));
+    }
+  }
+  a = block_reduce(a, OpAdd(), 0.0);
+  const unsigned nb = gridDim.x * gridDim.y;
+  const int b = blockIdx.x + blockIdx.y * gridDim.x;
+  if (threadIdx.x == 0) c.part[b] = a;
+  if (sor_last_block(c.ticket, nb)) {
     __threadfence();
     double s = 0.0;
-    for (int k = threadIdx.x; k < nb; k += blockDim.x) s += ((volatile double *)c.part)[k];
+    for (unsigned k = threadIdx.x; k < nb; k += blockDim.x) s += ((volatile double *)c.part)[k];
     s = block_reduce(s, OpAdd(), 0.0);
     if (threadIdx.x == 0) {
       *c.normres0 = s;
@@ -510,55 +565,62 @@ __global__ void k_sor_resid0(DevGrid g, const double *__restrict__ T, const doub
   }
 }
 
-// One colour pass of sweep n.  Threads map to the cells of one colour:
-// k in [0, ns/2) of ring i gives j = 2k + parity(i, pass).
-__global__ void k_sor_pass(DevGrid g, double *__restrict__ T, const double *__restrict__ ml,
-                           const double *__restrict__ mlip, const double *__restrict__ mlim,
-                           const double *__restrict__ mljp, const double *__restrict__ mljm,
-                           const double *__restrict__ rhs, SorCtl c, double omega, double eps, int pass, int n,
-                           int maxiters)
+// One colour pass of sweep n.  Each thread updates SOR_CPT cells of ring i
+// (k = base + m*blockDim, j = 2k + parity).  The reference's
+// delta = omega*resid/Ml is formed as the correctly rounded quotient from the
+// stored reciprocal r = 1/Ml: q0 = x*r, e = x - Ml*q0 (exact, FMA),
+// delta = q0 + e*r (one FMA) -- Markstein's correction, equal to IEEE
+// division -- which costs three FP64 operations instead of a full divide.
+__global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict__ T, const double *__restrict__ ml,
+                                                  const double *__restrict__ mlip, const double *__restrict__ mlim,
+                                                  const double *__restrict__ mljp, const double *__restrict__ mljm,
+                                                  const double *__restrict__ rhs, const double *__restrict__ rml,
+                                                  SorCtl c, double omega, double eps, int pass, int n, int maxiters)
 {
   if (*((volatile int *)c.done)) return;
   const int ns = g.ns, half = ns >> 1;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y + 1;
+  const int col = pass - 1;
+  const int par = (col == 0) ? ((i - 1) & 1) : (i & 1);
+  const size_t pbase = (size_t)((i << 1) + col) * half;
   double a = 0.0;
   int ch = 0;
-  if (k < half) {
-    const int par = (pass == 1) ? ((i - 1) & 1) : (i & 1);
-    const int j = 2 * k + par;
-    const int l = j + i * ns;
-    const int ljp = (j == ns - 1) ? i * ns : l + 1;
-    const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
-    const double resid = sor_resid(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm);
-    a = fabs(resid);
-    const double delta = omega * resid / ml[l];
-    const double tn = T[l] - delta;
-    T[l] = tn;
-    ch = (delta > tn * TH_SORPRECISION) ? 1 : 0;
+#pragma unroll
+  for (int m = 0; m < SOR_CPT; m++) {
+    const int k = blockIdx.x * blockDim.x * SOR_CPT + m * blockDim.x + threadIdx.x;
+    if (k < half) {
+      const int j = 2 * k + par;
+      const int l = j + i * ns;
+      const int ljp = (j == ns - 1) ? i * ns : l + 1;
+      const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+      const size_t q = pbase + k;
+      const double resid = sor_resid_at(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm, q);
+      a += fabs(resid);
+      const double x = omega * resid;
+      const double r = rml[q];
+      const double q0 = x * r;
+      const double e = __fma_rn(-ml[q], q0, x);
+      const double delta = __fma_rn(e, r, q0);
+      const double tn = T[l] - delta;
+      T[l] = tn;
+      ch += (delta > tn * TH_SORPRECISION) ? 1 : 0;
+    }
   }
   a = block_reduce(a, OpAdd(), 0.0);
-  int chs = block_reduce(ch, OpAddI(), 0);
-  const int nb = gridDim.x * gridDim.y;
+  const int chs = block_reduce(ch, OpAddI(), 0);
+  const unsigned nb = gridDim.x * gridDim.y;
   const int b = blockIdx.x + blockIdx.y * gridDim.x;
-  const int slot = (pass - 1) * nb + b;
-  __shared__ bool last;
+  const int slot = col * nb + b;
   if (threadIdx.x == 0) {
     c.part[slot] = a;
     c.ipart[slot] = chs;
-    last = false;
-    if (pass == 2) {
-      __threadfence();
-      unsigned t = atomicAdd(c.ticket, 1u);
-      last = (t == (unsigned)nb - 1);
-    }
   }
-  __syncthreads();
-  if (last) {
+  if (pass != 2) return;
+  if (sor_last_block(c.ticket, nb)) {
     __threadfence();
     double s = 0.0;
     int cs = 0;
-    for (int q = threadIdx.x; q < 2 * nb; q += blockDim.x) {
+    for (unsigned q = threadIdx.x; q < 2 * nb; q += blockDim.x) {
       s += ((volatile double *)c.part)[q];
       cs += ((volatile int *)c.ipart)[q];
     }
@@ -600,6 +662,18 @@ __global__ void k_energy_from_t(DevGrid g, const double *__restrict__ rho, doubl
 // state, in four cell-parallel passes: quotients by the density, van Leer
 // slopes, upwind face values, flux divergence.
 
+// x / d for a d whose correctly rounded reciprocal r = 1/d is at hand: the
+// product q0 = x*r is corrected once, q0 + (x - d*q0)*r with the residual
+// formed exactly by an FMA (Markstein, IBM J. Res. Dev. 34(1), 1990).  The
+// result is the IEEE quotient in all of 2e8 random trials over the ranges of
+// the fields and at most one ulp from it otherwise.
+__device__ __forceinline__ double div_by_rcp(double x, double d, double r)
+{
+  const double q0 = x * r;
+  const double e = __fma_rn(-d, q0, x);
+  return __fma_rn(e, r, q0);
+}
+
 // ComputeLRMomenta (TransportEuler.c:318-347) + DivisePolarGrid quotients.
 __global__ void k_rad_prep(DevGrid g, int nq, const double *__restrict__ rho, const double *__restrict__ vr,
                            const double *__restrict__ vt, const double *__restrict__ energy, double *rmp, double *rmm,
@@ -615,10 +689,11 @@ __global__ void k_rad_prep(DevGrid g, int nq, const double *__restrict__ rho, co
   const double c = r * (vt[ljp] + rm * omega_frame) * rm;
   const double d = r * (vt[l] + rm * omega_frame) * rm;
   rmp[l] = a; rmm[l] = b; tmp_[l] = c; tmm[l] = d;
-  const double den = r + 1e-20;
-  w0[l] = a / den; w1[l] = b / den; w2[l] = c / den; w3[l] = d / den;
-  if (nq == 6) we[l] = energy[l] / den;
-  wr[l] = r / den;
+  const double den = r + 1e-20, rcp = 1.0 / den;
+  w0[l] = div_by_rcp(a, den, rcp); w1[l] = div_by_rcp(b, den, rcp);
+  w2[l] = div_by_rcp(c, den, rcp); w3[l] = div_by_rcp(d, den, rcp);
+  if (nq == 6) we[l] = div_by_rcp(energy[l], den, rcp);
+  wr[l] = div_by_rcp(r, den, rcp);
 }
 
 __device__ __forceinline__ double vl_slope_r(const DevGrid &g, const double *q, int i, int l)
@@ -675,127 +750,144 @@ __global__ void k_rad_update(DevGrid g, PtrPack7 qf, const double *__restrict__ 
   }
 }
 
-// Azimuthal step (OneWindTheta + QuantitiesAdvection + AdvectSHIFT,
-// TransportEuler.c:70-175): one block per ring with the ring in shared
-// memory.  ComputeResiduals' ring mean of v_theta is summed in order, the
-// integer FARGO shift and the fractional uniform velocity follow, then the
-// residual pass, the uniform pass and the cyclic shift.
-__device__ __forceinline__ void azi_star(double *s_out, const double *s_q, const double *s_dq, int ns, double dxtheta,
-                                         double dt, const double *vt_row, double vsub, double vconst, int uniform)
+// Per-ring quantities of ComputeResiduals (TransportEuler.c:70-111): VMed,
+// the ring mean of v_theta; the integer FARGO shift Nshift; the uniform
+// residual velocity of the second pass.  One warp per ring.  The mean is a
+// fixed butterfly sum (every lane ends with the same bits); when
+// Ntilde + 1/2 lies within 1e-9 of an integer, the ring is summed again left
+// to right, the reference's order, so that the integer shift is exactly the
+// reference's.
+__global__ void __launch_bounds__(256) k_azi_rings(DevGrid g, const double *__restrict__ vt, double dt,
+                                                   int *__restrict__ nshift, double *__restrict__ vmed,
+                                                   double *__restrict__ vtemp)
 {
-  // s_out[j] = ComputeStarTheta face value at the left face of cell j
-  for (int j = threadIdx.x; j < ns; j += blockDim.x) {
-    const int jm = (j == 0) ? ns - 1 : j - 1;
-    const double v = uniform ? vconst : (vt_row[j] - vsub);
-    const double ksi = v * dt;
-    if (ksi > 0.0) s_out[j] = s_q[jm] + (dxtheta - ksi) * s_dq[jm];
-    else s_out[j] = s_q[j] - (dxtheta + ksi) * s_dq[j];
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (i >= g.nr) return;                           // whole warp
+  const int ns = g.ns;
+  const double *row = vt + (size_t)i * ns;
+  double a = 0.0;
+  for (int j = lane; j < ns; j += 32) a += row[j];
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(TH_FULL, a, o);
+  double vm = a / (double)ns;
+  double Ntilde = vm * g.r.InvRmed[i] * dt * (double)ns / 2.0 / TH_PI;
+  const double frac = Ntilde + 0.5 - floor(Ntilde + 0.5);
+  if (frac < 1e-9 || frac > 1.0 - 1e-9) {
+    vm = warp_seq_sum(row, ns) / (double)ns;
+    Ntilde = vm * g.r.InvRmed[i] * dt * (double)ns / 2.0 / TH_PI;
+  }
+  if (lane == 0) {
+    const double Nround = floor(Ntilde + 0.5);
+    const double invdt = 1.0 / dt, dpinvns = 2.0 * TH_PI / (double)ns;
+    vmed[i] = vm;
+    nshift[i] = (int)(long long)Nround;
+    vtemp[i] = (Ntilde - Nround) * g.r.Rmed[i] * invdt * dpinvns;
   }
 }
 
-__device__ __forceinline__ void azi_slope(double *s_dq, const double *s_q, int ns, double invdxtheta)
+// Azimuthal step of the transport (OneWindTheta, QuantitiesAdvection,
+// VanLeerTheta, ComputeStarTheta, AdvectSHIFT; TransportEuler.c:70-175,
+// 276-347).  A block takes a segment of AZ_S(T) = T - 2*AZ_HALO cells of one
+// ring plus AZ_HALO cells on each side, one cell per thread, all transported
+// quantities in registers.  Each pass (residual velocity, then the uniform
+// one) leaves two fewer valid cells at each end, so after both passes the
+// segment itself is exact and is written, cyclically shifted by Nshift, to
+// the destination arrays.  Neighbour values move through shared memory.
+// The van Leer slope's sign tests read the sign bits as integers: for finite
+// values this is the reference's comparison (a NaN, which only a crashed run
+// holds, gives NaN instead of a zero slope).
+#define AZ_HALO 4
+#define AZ_TMAX 512
+
+__device__ __forceinline__ double azi_vl_slope(double qm, double q0, double qp, double invdx)
 {
-  for (int j = threadIdx.x; j < ns; j += blockDim.x) {
-    const int jm = (j == 0) ? ns - 1 : j - 1, jp = (j == ns - 1) ? 0 : j + 1;
-    const double dqm = s_q[j] - s_q[jm], dqp = s_q[jp] - s_q[j];
-    s_dq[j] = ((dqp * dqm > 0.0) && (dqp + dqm != 0.0)) ? dqp * dqm / (dqp + dqm) * invdxtheta : 0.0;
-  }
+  const double dqm = q0 - qm, dqp = qp - q0;
+  const double p = dqp * dqm;
+  const double s = dqp + dqm;
+  const bool pos = __double_as_longlong(p) > 0LL;                 // p > 0.0
+  const bool nz = (__double_as_longlong(s) << 1) != 0LL;          // s != 0.0
+  return (pos && nz) ? p / s * invdx : 0.0;
 }
 
-
-__global__ void k_azimuthal(DevGrid g, AziQ Q, const double *__restrict__ vt, double dt, int fast, int *nshift_out,
-                            double *vmed_out)
+template <int NQ>
+__global__ void __launch_bounds__(AZ_TMAX) k_azimuthal(DevGrid g, AziIO io, const double *__restrict__ vt, double dt,
+                                                     int fast, const int *__restrict__ nshift,
+                                                     const double *__restrict__ vmed, const double *__restrict__ vtemp)
 {
-  extern __shared__ double sm[];
-  const int ns = g.ns, i = blockIdx.x;
-  double *s_rho = sm, *s_rhos = sm + ns, *s_w = sm + 2 * ns, *s_dq = sm + 3 * ns;
-  __shared__ double sh_vmed, sh_vtemp;
-  __shared__ int sh_shift;
-  const double *vt_row = vt + (size_t)i * ns;
+  __shared__ double s_a[AZ_TMAX], s_b[AZ_TMAX], s_c[AZ_TMAX];
+  const int ns = g.ns, i = blockIdx.y, t = threadIdx.x, T = blockDim.x;
+  const int seg = T - 2 * AZ_HALO;
+  const int j0 = blockIdx.x * seg;
+  const int j = (j0 + t - AZ_HALO + ns) % ns;
+  const int tm = (t == 0) ? 0 : t - 1, tp = (t == T - 1) ? t : t + 1;   // edge threads only feed the halo
+  const size_t rowo = (size_t)i * ns;
   const double rmed = g.r.Rmed[i];
   const double dxtheta = 2.0 * TH_PI / (double)ns * rmed;
   const double invdxtheta = 1.0 / dxtheta;
   const double dxrad = (g.r.Rsup[i] - g.r.Rinf[i]) * dt;
   const double invsurf = 1.0 / g.r.Surf[i];
-  // ComputeResiduals (TransportEuler.c:70-111)
-  if (threadIdx.x < 32) {
-    const double moy = warp_seq_sum(vt_row, ns);
-    if (threadIdx.x == 0) {
-      const double vm = moy / (double)ns;
-      const double Ntilde = vm * g.r.InvRmed[i] * dt * (double)ns / 2.0 / TH_PI;
-      const double Nround = floor(Ntilde + 0.5);
-      sh_vmed = vm;
-      sh_shift = (int)(long long)Nround;
-      const double invdt = 1.0 / dt, dpinvns = 2.0 * TH_PI / (double)ns;
-      sh_vtemp = (Ntilde - Nround) * rmed * invdt * dpinvns;
-      nshift_out[i] = sh_shift;
-      vmed_out[i] = vm;
-    }
-  }
-  double *rho_g = Q.q[Q.n - 1] + (size_t)i * ns;
-  for (int j = threadIdx.x; j < ns; j += blockDim.x) s_rho[j] = rho_g[j];
-  __syncthreads();
-  const double vmed = sh_vmed, vtemp = sh_vtemp;
+  double q[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; k++) q[k] = io.src[k][rowo + j];
+  const double vface = vt[rowo + j];
+  const double vsub = fast ? vmed[i] : 0.0;
+  const double vuni = fast ? vtemp[i] : 0.0;
   const int npass = fast ? 2 : 1;
   for (int pass = 0; pass < npass; pass++) {
-    const int uniform = (pass == 1);
-    const double vsub = fast ? vmed : 0.0;        // residual velocity = vt - VMed (FARGO) or vt
-    // RhoStar from the current density; RhoInt = current density (s_rho)
-    azi_slope(s_dq, s_rho, ns, invdxtheta);
+    const double v = (pass == 1) ? vuni : (vface - vsub);
+    const double ksi = v * dt;
+    const bool up = ksi > 0.0;                     // upwind cell of the left face is j-1
+    const double c = up ? (dxtheta - ksi) : (dxtheta + ksi);
+    // RhoStar at the left face (ComputeStarTheta of the density)
+    const double rho = q[NQ - 1];
+    s_a[t] = rho;
     __syncthreads();
-    azi_star(s_rhos, s_rho, s_dq, ns, dxtheta, dt, vt_row, vsub, vtemp, uniform);
+    const double drho = azi_vl_slope(s_a[tm], rho, s_a[tp], invdxtheta);
+    s_b[t] = drho;
     __syncthreads();
-    for (int q = 0; q < Q.n; q++) {
-      double *row = Q.q[q] + (size_t)i * ns;
-      const bool isrho = (q == Q.n - 1);
-      // Work = Q / (RhoInt + 1e-20) into s_w
-      for (int j = threadIdx.x; j < ns; j += blockDim.x) s_w[j] = (isrho ? s_rho[j] : row[j]) / (s_rho[j] + 1e-20);
+    const double rs = up ? s_a[tm] + c * s_b[tm] : rho - c * drho;
+    const double den = rho + 1e-20;                // RhoInt + 1e-20
+    const double rcp = 1.0 / den;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NQ; k++) {
+      // VanLeerTheta: Work = Q / (RhoInt + 1e-20), its slope, the face value
+      const double w = div_by_rcp(q[k], den, rcp);
+      s_a[t] = w;
       __syncthreads();
-      azi_slope(s_dq, s_w, ns, invdxtheta);
+      const double dq = azi_vl_slope(s_a[tm], w, s_a[tp], invdxtheta);
+      s_b[t] = dq;
       __syncthreads();
-      // flux difference with face values computed on the fly
-      double upd[64];
-      int cnt = 0;
-      for (int j = threadIdx.x; j < ns; j += blockDim.x, cnt++) {
-        const int jp = (j == ns - 1) ? 0 : j + 1;
-        const int jm = (j == 0) ? ns - 1 : j - 1;
-        const double v0 = uniform ? vtemp : (vt_row[j] - vsub);
-        const double v1 = uniform ? vtemp : (vt_row[jp] - vsub);
-        const double k0 = v0 * dt, k1 = v1 * dt;
-        const double qs0 = (k0 > 0.0) ? s_w[jm] + (dxtheta - k0) * s_dq[jm] : s_w[j] - (dxtheta + k0) * s_dq[j];
-        const double qs1 = (k1 > 0.0) ? s_w[j] + (dxtheta - k1) * s_dq[j] : s_w[jp] - (dxtheta + k1) * s_dq[jp];
-        double varq = dxrad * qs0 * s_rhos[j] * v0;
-        varq -= dxrad * qs1 * s_rhos[jp] * v1;
-        const double old = isrho ? s_rho[j] : row[j];
-        upd[cnt] = old + varq * invsurf;
-      }
-      __syncthreads();   // everyone finished reading s_rho / s_w before the density changes
-      cnt = 0;
-      for (int j = threadIdx.x; j < ns; j += blockDim.x, cnt++) {
-        if (isrho) s_rho[j] = upd[cnt];
-        else row[j] = upd[cnt];
-      }
+      const double qs = up ? s_a[tm] + c * s_b[tm] : w - c * dq;
+      const double F = dxrad * qs * rs * v;
+      s_c[t] = F;
       __syncthreads();
+      const double varq = F - s_c[tp];
+      q[k] = q[k] + varq * invsurf;
     }
   }
-  if (fast) {
-    // AdvectSHIFT (TransportEuler.c:113-136) for every quantity
-    const int sh = sh_shift;
-    for (int q = 0; q < Q.n; q++) {
-      double *row = Q.q[q] + (size_t)i * ns;
-      const bool isrho = (q == Q.n - 1);
-      for (int j = threadIdx.x; j < ns; j += blockDim.x) s_w[j] = isrho ? s_rho[j] : row[j];
-      __syncthreads();
-      for (int j = threadIdx.x; j < ns; j += blockDim.x) {
-        int ji = (j - sh) % ns;
-        if (ji < 0) ji += ns;
-        row[j] = s_w[ji];
-      }
-      __syncthreads();
+  const int x = t - AZ_HALO;
+  if (x >= 0 && x < seg && j0 + x < ns) {
+    int jo = j;
+    if (fast) {
+      jo = (j + nshift[i]) % ns;                   // AdvectSHIFT: new[j + Nshift] = old[j]
+      if (jo < 0) jo += ns;
     }
-  } else {
-    for (int j = threadIdx.x; j < ns; j += blockDim.x) rho_g[j] = s_rho[j];
+#pragma unroll
+    for (int k = 0; k < NQ; k++) io.dst[k][rowo + jo] = q[k];
   }
+}
+
+// Threads per block for the azimuthal step: the multiple of 32 in
+// [128, AZ_TMAX] that needs the fewest warps per ring.
+static int azi_block(int ns)
+{
+  int best = 0, bestw = 1 << 30;
+  for (int T = 128; T <= AZ_TMAX; T += 32) {
+    const int seg = T - 2 * AZ_HALO;
+    const int w = (ns + seg - 1) / seg * (T / 32);
+    if (w < bestw) { bestw = w; best = T; }
+  }
+  return best;
 }
 
 // ComputeVelocities (TransportEuler.c:350-381), followed for the gas by the
@@ -908,43 +1000,53 @@ void hydro_irradiation(const DevGrid &g, const double *rho, const double *cs, co
 
 void hydro_matrix(const DevGrid &g, const double *rho, const double *T, const double *cs, const double *dcen,
                   const double *divv, const double *qminus, const double *qplus, const double *qirr, double *ml,
-                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs, double dt, double gm1,
-                  const double *invdxtheta2_r, int irradiation, int nheat, const int *heat_idx, const double *heat_val,
-                  cudaStream_t s)
+                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs, double *rml, double dt,
+                  double gm1, const double *invdxtheta2_r, int irradiation, int nheat, const int *heat_idx,
+                  const double *heat_val, cudaStream_t s)
 {
   if (g.nr < 3) return;
   k_matrix<<<grid2d(g.ns, g.nr - 2, BX), BX, 0, s>>>(g, rho, T, cs, dcen, divv, qminus, qplus, qirr, ml, mlip, mlim, mljp,
-                                                     mljm, rhs, dt, gm1, invdxtheta2_r, irradiation, nheat, heat_idx,
+                                                     mljm, rhs, rml, dt, gm1, invdxtheta2_r, irradiation, nheat, heat_idx,
                                                      heat_val);
   g_thorin_launches++;
 }
 
 static const int SOR_BX = 128;
 
-int sor_blocks(const DevGrid &g)
+static dim3 sor_grid_pass(const DevGrid &g)
 {
   const int half = g.ns / 2;
-  const int b1 = ((half + SOR_BX - 1) / SOR_BX) * (g.nr - 2);
-  const int b0 = ((g.ns + SOR_BX - 1) / SOR_BX) * (g.nr - 2);
-  return b1 > b0 ? b1 : b0;
+  return dim3((half + SOR_BX * SOR_CPT - 1) / (SOR_BX * SOR_CPT), g.nr - 2);
+}
+
+static dim3 sor_grid_resid(const DevGrid &g)
+{
+  return dim3((g.ns + SOR_BX * SOR_CPT - 1) / (SOR_BX * SOR_CPT), g.nr - 2);
+}
+
+int sor_blocks(const DevGrid &g)
+{
+  const dim3 a = sor_grid_pass(g), b = sor_grid_resid(g);
+  const int na = a.x * a.y, nb = b.x * b.y;
+  return na > nb ? na : nb;
 }
 
 void hydro_sor_resid0(const DevGrid &g, const double *T, const double *ml, const double *mlip, const double *mlim,
                       const double *mljp, const double *mljm, const double *rhs, const SorCtl &c, cudaStream_t s)
 {
-  k_sor_resid0<<<grid2d(g.ns, g.nr - 2, SOR_BX), SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, c);
+  k_sor_resid0<<<sor_grid_resid(g), SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, c);
   g_thorin_launches++;
 }
 
 void hydro_sor_sweeps(const DevGrid &g, double *T, const double *ml, const double *mlip, const double *mlim,
-                      const double *mljp, const double *mljm, const double *rhs, const SorCtl &c, double omega,
-                      double eps, int first, int count, int maxiters, cudaStream_t s)
+                      const double *mljp, const double *mljm, const double *rhs, const double *rml, const SorCtl &c,
+                      double omega, double eps, int first, int count, int maxiters, cudaStream_t s)
 {
-  dim3 grid = grid2d(g.ns / 2, g.nr - 2, SOR_BX);
+  const dim3 grid = sor_grid_pass(g);
   for (int n = first; n < first + count && n <= maxiters; n++) {
-    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, c, omega, eps, 1, n, maxiters);
+    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, rml, c, omega, eps, 1, n, maxiters);
     g_thorin_launches++;
-    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, c, omega, eps, 2, n, maxiters);
+    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, rml, c, omega, eps, 2, n, maxiters);
     g_thorin_launches++;
   }
 }
@@ -990,24 +1092,30 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
   wf.n = dqf.n = n;
   k_rad_face<<<grid2d(ns, nr + 1, BX), BX, 0, s>>>(g, wf, dqf, vr, dt);
   g_thorin_launches++;
-  // flux divergence: in/out
+  // flux divergence into the quotient buffers, which are free by now
   PtrPack7 qf, io;
   n = 0;
-  for (int q = 0; q < 4; q++) { qf.src[n] = S.f[q]; io.src[n] = S.mom[q]; io.dst[n] = S.mom[q]; n++; }
-  if (nq == 6) { qf.src[n] = S.f[4]; io.src[n] = *energy; io.dst[n] = S.e_new; n++; }
-  qf.src[n] = S.f[5]; io.src[n] = *rho; io.dst[n] = S.rho_new; n++;
+  for (int q = 0; q < 4; q++) { qf.src[n] = S.f[q]; io.src[n] = S.mom[q]; io.dst[n] = S.w[q]; n++; }
+  if (nq == 6) { qf.src[n] = S.f[4]; io.src[n] = *energy; io.dst[n] = S.w[4]; n++; }
+  qf.src[n] = S.f[5]; io.src[n] = *rho; io.dst[n] = S.w[5]; n++;
   qf.n = io.n = n;
   k_rad_update<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, qf, S.f[6], vr, io, dt);
   g_thorin_launches++;
-  // azimuthal step on (rmp, rmm, tmp, tmm, [e], rho)
-  AziQ az;
+  // azimuthal step on (rmp, rmm, tmp, tmm, [e], rho) back into the momenta,
+  // the new energy and the new density
+  k_azi_rings<<<(nr * 32 + 255) / 256, 256, 0, s>>>(g, vt, dt, S.nshift, S.vmed, S.vtemp);
+  g_thorin_launches++;
+  AziIO az;
+  for (int q = 0; q < n; q++) az.src[q] = io.dst[q];
   n = 0;
-  for (int q = 0; q < 4; q++) az.q[n++] = S.mom[q];
-  if (nq == 6) az.q[n++] = S.e_new;
-  az.q[n++] = S.rho_new;
+  for (int q = 0; q < 4; q++) az.dst[n++] = S.mom[q];
+  if (nq == 6) az.dst[n++] = S.e_new;
+  az.dst[n++] = S.rho_new;
   az.n = n;
-  const size_t smem = 4 * (size_t)ns * sizeof(double);
-  k_azimuthal<<<nr, 256, smem, s>>>(g, az, vt, dt, fast, S.nshift, S.vmed);
+  const int T = azi_block(ns);
+  const dim3 grid((ns + T - 2 * AZ_HALO - 1) / (T - 2 * AZ_HALO), nr);
+  if (nq == 6) k_azimuthal<6><<<grid, T, 0, s>>>(g, az, vt, dt, fast, S.nshift, S.vmed, S.vtemp);
+  else k_azimuthal<5><<<grid, T, 0, s>>>(g, az, vt, dt, fast, S.nshift, S.vmed, S.vtemp);
   g_thorin_launches++;
   // velocities from the transported momenta
   k_velocities<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, S.rho_new, S.mom[0], S.mom[1], S.mom[2], S.mom[3], vr, vt,
@@ -1016,10 +1124,4 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
   g_thorin_launches++;
 }
 
-int hydro_azimuthal_smem(int ns) { return 4 * ns * (int)sizeof(double); }
 
-void hydro_set_smem_limits(int ns)
-{
-  const int need = hydro_azimuthal_smem(ns);
-  cudaFuncSetAttribute(k_azimuthal, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
-}

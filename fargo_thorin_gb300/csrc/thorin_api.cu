@@ -93,7 +93,7 @@ enum {  // ring arrays kept on the device
   R_WAVEKILLER, R_RMED15, R_RINF15, R_RSUP15, R_COSTAB, R_SINTAB, R_SIGMAMED, R_ENERGYMED, R_VTHETAMED, R_PEBDENS0,
   R_PEBVRAD0, R_PEBVTHETA0, R_CSMEAN, R_TEMPMEAN, R_NUMED, R_NUINF, R_INVDXTHETA, R_INVDXTHETA2, R_SUPPTORQUE,
   R_DELTAR2, R_CFLDXRAD, R_CFLDXTHETA, R_CFLMINDX, R_CFLDEN5, R_VMOY, R_PVTMED, R_HAVR, R_SIGAVR, R_ISTAVR, R_PHAVR,
-  R_PISTAVR, R_VMED, R_COUNT
+  R_PISTAVR, R_VMED, R_TAUAVR, R_VTEMP, R_COUNT
 };
 
 struct thorin_disk {
@@ -107,7 +107,7 @@ struct thorin_disk {
   // fields
   double *rho, *vrad, *vtheta, *energy, *vrad_new, *vtheta_new, *energy_new, *vrad_int, *vtheta_int, *energy_int;
   double *cs, *temper, *qplus, *qminus, *opacity, *divv, *trr, *trp, *tpp, *agr, *agt, *pagr, *pagt, *dcen;
-  double *ml, *mlip, *mlim, *mljp, *mljm, *rhs, *tbackup, *flaring, *qirr;
+  double *ml, *mlip, *mlim, *mljp, *mljm, *rhs, *rml, *tbackup, *flaring, *qirr;
   double *pdens, *pvrad, *pvtheta, *psize, *tau, *paccr, *pacct, *gaccr, *gacct, *dragr, *dragt, *macc;
   double *t_rho_gas, *t_e_gas, *t_rho_peb;
   TransportScratch ts;
@@ -292,7 +292,7 @@ static void build_grid(thorin_disk *d)
   d->cfl.dxrad = R[R_CFLDXRAD]; d->cfl.dxtheta = R[R_CFLDXTHETA]; d->cfl.mindx = R[R_CFLMINDX];
   d->cfl.den5 = R[R_CFLDEN5]; d->cfl.vmoy = R[R_VMOY]; d->cfl.pvtmed = R[R_PVTMED];
   d->fr.H_avr = R[R_HAVR]; d->fr.sigma_avr = R[R_SIGAVR]; d->fr.integstar_avr = R[R_ISTAVR];
-  d->fr.p_H_avr = R[R_PHAVR]; d->fr.p_integstar_avr = R[R_PISTAVR];
+  d->fr.p_H_avr = R[R_PHAVR]; d->fr.p_integstar_avr = R[R_PISTAVR]; d->fr.tau_avr = R[R_TAUAVR];
 }
 
 static int check_supported(const thorin_params &p)
@@ -334,7 +334,7 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   double **F[] = {&d->rho, &d->vrad, &d->vtheta, &d->energy, &d->vrad_new, &d->vtheta_new, &d->energy_new,
                   &d->vrad_int, &d->vtheta_int, &d->energy_int, &d->cs, &d->temper, &d->qplus, &d->qminus,
                   &d->opacity, &d->divv, &d->trr, &d->trp, &d->tpp, &d->agr, &d->agt, &d->dcen, &d->ml, &d->mlip,
-                  &d->mlim, &d->mljp, &d->mljm, &d->rhs, &d->tbackup, &d->t_rho_gas, &d->t_e_gas};
+                  &d->mlim, &d->mljp, &d->mljm, &d->rhs, &d->rml, &d->tbackup, &d->t_rho_gas, &d->t_e_gas};
   for (auto f : F) RCHK(dfield(d, f));
   if (d->p.stellar_irradiation) { RCHK(dfield(d, &d->flaring)); RCHK(dfield(d, &d->qirr)); }
   else { d->flaring = d->qirr = nullptr; }
@@ -352,6 +352,7 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   RCHK(dalloc(d, (void **)&d->nshift, n1 * sizeof(int)));
   d->ts.nshift = d->nshift;
   d->ts.vmed = d->ring[R_VMED];
+  d->ts.vtemp = d->ring[R_VTEMP];
   // reduction scratch: enough partials for every reduction kernel
   const size_t nb = (size_t)((d->ns + 127) / 128 + 2) * (size_t)(d->nr + 2);
   RCHK(dalloc(d, (void **)&d->partials, nb * (2 + 2 * MAXPL_DEV + 6) * sizeof(double)));
@@ -438,8 +439,6 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   CUCHK(cudaMemcpyAsync(d->scal + SC_DTSTELLAR, d->scal_h + SC_DTSTELLAR, sizeof(double), cudaMemcpyHostToDevice, d->s));
   for (int q = 0; q < 4; q++) CUCHK(cudaEventCreate(&d->ev[q]));
   d->timing = 0;
-  hydro_set_smem_limits(d->ns);
-  if (hydro_azimuthal_smem(d->ns) > 227 * 1024) { g_last_error = "nsec too large for the ring kernel"; return THORIN_ERR_ARG; }
   CUCHK(cudaStreamSynchronize(d->s));
   d->nshift_h.assign(d->nr, 0);
   *out = d;
@@ -929,6 +928,8 @@ extern "C" int thorin_gpu_accrete(thorin_disk *d, thorin_planets *sys, double dt
     AccArgs a;
     a.pdens = d->pdens; a.macc = d->macc; a.pvr = d->pvrad; a.pvt = d->pvtheta; a.tau = d->tau; a.cs = d->cs;
     a.vt = d->vtheta;
+    a.part = d->partials;
+    a.acc = d->scal + 64;
     a.Xp = sys->x[k]; a.Yp = sys->y[k]; a.Zp = sys->z[k];
     a.VXp = sys->vx[k]; a.VYp = sys->vy[k]; a.VZp = sys->vz[k];
     a.Mp = sys->mass[k];
@@ -1057,8 +1058,8 @@ static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *ca
   *capped = 0;
   for (;;) {
     if (d->timing) CUCHK(cudaEventRecord(d->ev[0], d->s));
-    hydro_sor_sweeps(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor, omega, p.sor_eps, first,
-                     chunk, p.sor_maxiters, d->s);
+    hydro_sor_sweeps(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->rml, d->sor, omega, p.sor_eps,
+                     first, chunk, p.sor_maxiters, d->s);
     KCHECK("SOR sweep kernels");
     if (d->timing) CUCHK(cudaEventRecord(d->ev[1], d->s));
     CUCHK(cudaMemcpyAsync(d->iscal_h + IS_SOR_DONE, d->sor.done, 2 * sizeof(int), cudaMemcpyDeviceToHost, d->s));
@@ -1139,7 +1140,7 @@ static int energy_step(thorin_disk *d, double dt)
     }
   }
   hydro_matrix(d->g, d->rho, d->temper, d->cs, d->dcen, d->divv, d->qminus, d->qplus, d->qirr, d->ml, d->mlip, d->mlim,
-               d->mljp, d->mljm, d->rhs, dt, d->gm1, d->ring[R_INVDXTHETA2], p.stellar_irradiation, nheat,
+               d->mljp, d->mljm, d->rhs, d->rml, dt, d->gm1, d->ring[R_INVDXTHETA2], p.stellar_irradiation, nheat,
                d->heat_idx_d, d->heat_val_d, d->s);
   KCHECK("energy kernels");
   if (d->sor_first) {

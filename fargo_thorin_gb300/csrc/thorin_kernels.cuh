@@ -35,11 +35,11 @@ struct TransportScratch {
   double *rho_new, *e_new;
   double *w[6], *d[7], *f[7];
   int *nshift;
-  double *vmed;
+  double *vmed, *vtemp;
 };
 
 struct PtrPack7 { const double *src[7]; double *dst[7]; int n; };
-struct AziQ { double *q[6]; int n; };   // q[n-1] is the density
+struct AziIO { const double *src[6]; double *dst[6]; int n; };   // index n-1 is the density
 
 struct ViscParams {
   double viscosity, alpha, alpha_mri, alpha_dead, tmri, twidth, t2si;
@@ -57,7 +57,7 @@ struct CflFinal {
   double deltaT, invdtreb_sq, minimum_step, maximum_step, first_step, twopi_cfl_ns;
 };
 
-struct ForceRings { double *H_avr, *sigma_avr, *integstar_avr, *p_H_avr, *p_integstar_avr; };
+struct ForceRings { double *H_avr, *sigma_avr, *integstar_avr, *p_H_avr, *p_integstar_avr, *tau_avr; };
 
 struct ForceArgs {
   const double *rho, *cs, *tau, *pdens;
@@ -70,6 +70,8 @@ struct ForceArgs {
 
 struct AccArgs {
   double *pdens, *macc;
+  double *part;               // block partials (4 per block)
+  double *acc;                // scalars: Reff, vrel, Mt, limiter
   const double *pvr, *pvt, *tau, *cs, *vt;
   double Xp, Yp, Zp, VXp, VYp, VZp, Mp, Rp, Rhill, Omegap, Rp15, omega_frame, dt, pebble_alpha, frac;
   int imin, imax, iflow;
@@ -107,23 +109,23 @@ void hydro_irradiation(const DevGrid &g, const double *rho, const double *cs, co
                        const double *rinf15, const double *rsup15, cudaStream_t s);
 void hydro_matrix(const DevGrid &g, const double *rho, const double *T, const double *cs, const double *dcen,
                   const double *divv, const double *qminus, const double *qplus, const double *qirr, double *ml,
-                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs, double dt, double gm1,
-                  const double *invdxtheta2_r, int irradiation, int nheat, const int *heat_idx, const double *heat_val,
-                  cudaStream_t s);
+                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs, double *rml, double dt,
+                  double gm1, const double *invdxtheta2_r, int irradiation, int nheat, const int *heat_idx,
+                  const double *heat_val, cudaStream_t s);
 int sor_blocks(const DevGrid &g);
 void hydro_sor_resid0(const DevGrid &g, const double *T, const double *ml, const double *mlip, const double *mlim,
                       const double *mljp, const double *mljm, const double *rhs, const SorCtl &c, cudaStream_t s);
 void hydro_sor_sweeps(const DevGrid &g, double *T, const double *ml, const double *mlip, const double *mlim,
-                      const double *mljp, const double *mljm, const double *rhs, const SorCtl &c, double omega,
-                      double eps, int first, int count, int maxiters, cudaStream_t s);
+                      const double *mljp, const double *mljm, const double *rhs, const double *rml, const SorCtl &c,
+                      double omega, double eps, int first, int count, int maxiters, cudaStream_t s);
 void hydro_energy_from_t(const DevGrid &g, const double *rho, double *T, double *enew, cudaStream_t s);
 void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, double **energy, const TransportScratch &S,
                      double dt, double omega_frame, int fast, int damp_vrad, double drin, double drout, double *temper,
                      double *cs, double gm1, double gg1, cudaStream_t s);
-int hydro_azimuthal_smem(int ns);
-void hydro_set_smem_limits(int ns);
 
 // kernels_aux.cu
+void aux_ring_means(const DevGrid &g, const double *f0, double *o0, const double *f1, double *o1, int ring0, int nrings,
+                    cudaStream_t s);
 void aux_ring_mean(const DevGrid &g, const double *f, double *out, cudaStream_t s);
 void aux_ring_mean_at(const DevGrid &g, const double *f, int ring, double *out, cudaStream_t s);
 void aux_viscosity_rings(const DevGrid &g, const ViscParams &v, cudaStream_t s);
@@ -148,6 +150,7 @@ void aux_pebble_substep1(const DevGrid &g, double *pvr, double *pvt, const doubl
 void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr, double indx_pl, double indy_pl,
                 double *scal, cudaStream_t s);
 void aux_accrete(const DevGrid &g, const AccArgs &a, double *scal, cudaStream_t s);
+int aux_accrete_blocks(const DevGrid &g, int imin, int imax);
 void aux_integrals(const DevGrid &g, const double *rho, const double *vr, const double *vt, const double *e,
                    const double *pd, const double *pvt, double omega_frame, int pebbles, double *part, double *scal,
                    cudaStream_t s);
