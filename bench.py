@@ -122,6 +122,22 @@ def make_disk(nr=NR, ns=NS):
     return p, d, sys_
 
 
+def reduce_over_ranks(values, ops, device):
+    """All-reduce each value over the ranks of the initialised process group
+    ("max" or "sum"); with one rank (or no group) the values come back as
+    they are.  Used for the max-over-ranks step time and summed updates."""
+    import torch
+    import torch.distributed as dist
+    multi = dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1
+    out = []
+    for v, op in zip(values, ops):
+        t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+        if multi:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+        out.append(float(t.item()))
+    return out
+
+
 def run_gpu(args):
     import torch
     ws, rank, local = dist_env()
@@ -165,14 +181,8 @@ def run_gpu(args):
     sweeps = st.sor_sweeps - sweeps0
     launches = st.kernel_launches - launches0
     sor_avg_ms = st.sor_time_ms / max(st.sor_passes, 1)
-    ms_t = torch.tensor([ms], device="cuda")
-    subs_t = torch.tensor([float(subs)], device="cuda")
-    if ws > 1:
-        import torch.distributed as dist
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-        dist.all_reduce(subs_t, op=dist.ReduceOp.SUM)
-    ms_max = float(ms_t.item())
-    total_updates = NR * NS * float(subs_t.item())
+    ms_max, subs_all = reduce_over_ranks([ms, subs], ["max", "sum"], "cuda")
+    total_updates = NR * NS * subs_all
     value = total_updates / (ms_max / 1e3)
 
     # end to end through the C ABI with host buffers (pinned)
@@ -194,13 +204,8 @@ def run_gpu(args):
             _lib.check(L.thorin_gpu_download(h, f, ptr[f]), "download")
     barrier()
     e_s = time.perf_counter() - t0
-    e_t = torch.tensor([e_s], device="cuda")
-    es_t = torch.tensor([float(esubs)], device="cuda")
-    if ws > 1:
-        import torch.distributed as dist
-        dist.all_reduce(e_t, op=dist.ReduceOp.MAX)
-        dist.all_reduce(es_t, op=dist.ReduceOp.SUM)
-    e2e_value = NR * NS * float(es_t.item()) / float(e_t.item())
+    e_max, esubs_all = reduce_over_ranks([e_s, esubs], ["max", "sum"], "cuda")
+    e2e_value = NR * NS * esubs_all / e_max
 
     if rank == 0:
         peak, peak_kind = peaks()
@@ -315,6 +320,24 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile(args, nr=NR, ns=NS):
+    """One warm-up DT, then ``--steps`` DTs bracketed by cuProfilerStart/Stop,
+    for ``ncu --profile-from-start off``.  Prints one line; no bench value."""
+    import ctypes
+    from fargo_thorin_gb300 import _lib
+    _lib.load()
+    p, d, sys_ = make_disk(nr, ns)
+    d.algogas(sys_)
+    cu = ctypes.CDLL("libcuda.so.1")
+    cu.cuProfilerStart()
+    for _ in range(args.steps):
+        d.algogas(sys_)
+    cu.cuProfilerStop()
+    st = d.stats()
+    print(json.dumps({"profiled_dts": args.steps, "nrad": nr, "nsec": ns, "substeps_last_dt": st.substeps,
+                      "sor_last_niter": st.sor_last_niter}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -322,7 +345,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="run --steps DTs inside cuProfilerStart/Stop for ncu; prints no bench line")
+    ap.add_argument("--grid", type=int, nargs=2, metavar=("NRAD", "NSEC"), default=(NR, NS),
+                    help="grid of the --profile run")
     args = ap.parse_args()
+    if args.profile:
+        run_profile(args, *args.grid)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -100,7 +100,7 @@ __global__ void k_stokes(DevGrid g, const double *__restrict__ rho, const double
 {
   const int ns = g.ns;
   CELL_LOOP_2D
-  tau[l] = 2.0 * g.k.pebbulkdens * psize[l] / rho[l] * g.k.sqrt_adiabind_inv;
+  tau[l] = div_fast(2.0 * g.k.pebbulkdens * psize[l], rho[l]) * g.k.sqrt_adiabind_inv;
 }
 
 void aux_stokes(const DevGrid &g, const double *rho, const double *psize, double *tau, cudaStream_t s)
@@ -130,23 +130,23 @@ __global__ void k_cfl_cells(DevGrid g, const double *__restrict__ vr, const doub
     const int ljp = (j == ns - 1) ? i * ns : l + 1;
     const double dxrad = cr.dxrad[i], dxtheta = cr.dxtheta[i];
     const double vres = fast ? vt[l] - cr.vmoy[i] : vt[l];
-    const double invdt1 = cs[l] / cr.mindx[i];
-    const double invdt2 = fabs(vr[l]) / dxrad;
-    const double invdt3 = fabs(vres) / dxtheta;
+    const double invdt1 = div_fast(cs[l], cr.mindx[i]);
+    const double invdt2 = div_fast(fabs(vr[l]), dxrad);
+    const double invdt3 = div_fast(fabs(vres), dxtheta);
     double dvr = vr[lip] - vr[l], dvt = vt[ljp] - vt[l];
     dvr = (dvr >= 0.0) ? 1e-10 : -dvr;
     dvt = (dvt >= 0.0) ? 1e-10 : -dvt;
-    const double a = dvr / dxrad, b = dvt / dxtheta;
+    const double a = div_fast(dvr, dxrad), b = div_fast(dvt, dxtheta);
     double invdt4 = (b > a) ? b : a;
     invdt4 *= 4.0 * TH_CVNR * TH_CVNR;
-    const double invdt5 = viscous ? g.r.nu_med[i] * 4. / cr.den5[i] : 1e-30;
+    const double invdt5 = viscous ? div_fast(g.r.nu_med[i] * 4., cr.den5[i]) : 1e-30;
     gas = invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4 + invdt5 * invdt5;
     if (pebbles) {
-      const double p1 = fabs(pvr[l]) / dxrad;
+      const double p1 = div_fast(fabs(pvr[l]), dxrad);
       const double vrp = fast ? pvt[l] - cr.pvtmed[i] : pvt[l];
-      const double p2 = fabs(vrp) / dxtheta;
-      const double p3 = fabs(pvr[l] - vr[l]) / dxrad;
-      const double p4 = fabs(pvt[l] - vt[l]) / dxtheta;
+      const double p2 = div_fast(fabs(vrp), dxtheta);
+      const double p3 = div_fast(fabs(pvr[l] - vr[l]), dxrad);
+      const double p4 = div_fast(fabs(pvt[l] - vt[l]), dxtheta);
       peb = p1 * p1 + p2 * p2 + p3 * p3 + p4 * p4;
     }
   }
@@ -315,7 +315,7 @@ __global__ void k_pebble_sources(DevGrid g, const double *__restrict__ pd, const
 {
   const int ns = g.ns;
   CELL_LOOP_2D
-  const double Omega = 1.0 / g.r.OmegaInv[i];
+  const double Omega = div_fast(1.0, g.r.OmegaInv[i]);
   const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
   if (i >= 1) {
     const int lim = l - ns;
@@ -325,13 +325,13 @@ __global__ void k_pebble_sources(DevGrid g, const double *__restrict__ pd, const
     vt2 = vt2 * vt2;
     paccr[l] = vt2 * g.r.InvRinf[i] + 0.5 * (pagr[l] + pagr[lim]);
     if (back_reaction) {
-      const double drag = Omega * (pvr[l] - vr[l]) / tau[l];
+      const double drag = div_fast(Omega * (pvr[l] - vr[l]), tau[l]);
       dragr[l] = 0.5 * (pd[l] + pd[lim]) * drag;
     }
   }
   pacct[l] = 0.5 * (pagt[l] + pagt[ljm]);
   if (back_reaction) {
-    const double drag = Omega * (pvt[l] - vt[l]) / tau[l];
+    const double drag = div_fast(Omega * (pvt[l] - vt[l]), tau[l]);
     dragt[l] = 0.5 * (pd[l] + pd[ljm]) * drag;
   }
 }
@@ -358,24 +358,24 @@ __global__ void k_pebble_substep1(DevGrid g, double *__restrict__ pvr, double *_
 {
   const int ns = g.ns;
   CELL_LOOP_2D
-  const double Omega = 1.0 / g.r.OmegaInv[i];
+  const double Omega = div_fast(1.0, g.r.OmegaInv[i]);
   const double t = tau[l];
-  const double efac = exp(-dt * Omega / t);
+  const double efac = exp(div_fast(-dt * Omega, t));
   double a = pvr[l], b = pvt[l];
-  if (i > 0) a = a * efac + gaccr[l] * dt + (vr[l] + (paccr[l] - gaccr[l]) * t / Omega) * (1.0 - efac);
-  b = b * efac + gacct[l] * dt + (vt[l] + (pacct[l] - gacct[l]) * t / Omega) * (1.0 - efac);
+  if (i > 0) a = a * efac + gaccr[l] * dt + (vr[l] + div_fast((paccr[l] - gaccr[l]) * t, Omega)) * (1.0 - efac);
+  b = b * efac + gacct[l] * dt + (vt[l] + div_fast((pacct[l] - gacct[l]) * t, Omega)) * (1.0 - efac);
   if (diffusion) {
     if (i >= 1) {
       const int lim = l - ns;
       double corr = -g.r.nu_inf[i] / schmidt;
-      corr *= (rho[l] + rho[lim]) / (pd[l] + pd[lim]);
-      corr *= (pd[l] / rho[l] - pd[lim] / rho[lim]) * g.r.InvDiffRmed[i];
+      corr *= div_fast(rho[l] + rho[lim], pd[l] + pd[lim]);
+      corr *= (div_fast(pd[l], rho[l]) - div_fast(pd[lim], rho[lim])) * g.r.InvDiffRmed[i];
       a += corr;
     }
     const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
     double corr = -g.r.nu_med[i] / schmidt;
-    corr *= (rho[l] + rho[ljm]) / (pd[l] + pd[ljm]);
-    corr *= (pd[l] / rho[l] - pd[ljm] / rho[ljm]) * invdxtheta_r[i];
+    corr *= div_fast(rho[l] + rho[ljm], pd[l] + pd[ljm]);
+    corr *= (div_fast(pd[l], rho[l]) - div_fast(pd[ljm], rho[ljm])) * invdxtheta_r[i];
     b += corr;
   }
   pvr[l] = a;
@@ -431,6 +431,58 @@ __global__ void k_force_rings(DevGrid g, ForceRings fr, int pebbles, double pebb
   fr.p_integstar_avr[i] = p_int;
 }
 
+// One quadrature node of a planet's potential (FillForcesArrays,
+// Pframeforce.c:300-372): cubic-spline taper inside rst, softened 1/d^3.
+__device__ __forceinline__ double planet_node(double s2, double dz, double mx, const DevPlanet &P)
+{
+  double d2 = s2 + dz * dz, taper = 1.0;
+  if (d2 < P.rst2) {
+    const double dd = sqrt(d2);
+    taper = div_fast(-3.0 * d2 * d2, P.rst4) + div_fast(4.0 * dd * d2, P.rst3);
+  }
+  const double iv = rsqrt(d2 + mx);
+  return iv * iv * iv * taper;
+}
+
+// Vertical quadrature of one cell (FillForcesArrays, Pframeforce.c:260-372)
+// over NV nodes z_m = (m - 1/2) 3H/NV.  The Gaussian weights depend only on
+// m and NV and come precomputed; 1/d^3 comes from one reciprocal square root.
+template <int NV>
+__device__ __forceinline__ void vert_quad(const double (&wq)[NV], double H, double r2, double Hcorr, double pH, int peb,
+                                          int npl, const int *with, const double *s2, double Rsup_Rinf2,
+                                          const DevPlanet *pl, double &integstar, double &p_integstar,
+                                          double *integpl, double *p_integpl)
+{
+  const double deltaz = 3.0 * H / (double)NV;
+  const double hc2 = Hcorr * Hcorr;
+  double is = 0.0, pis = 0.0;
+#pragma unroll
+  for (int m = 1; m <= NV; m++) {
+    const double znode = ((double)m - 0.5) * deltaz, znode2 = znode * znode;
+    const double sum = wq[m - 1];
+    double iv = rsqrt(r2 + znode2);
+    is += sum * iv * iv * iv;
+    if (peb) {
+      iv = rsqrt(r2 + znode2 * hc2);
+      pis += sum * iv * iv * iv;
+    }
+    for (int k = 0; k < npl; k++) {
+      if (!with[k]) continue;
+      const DevPlanet P = pl[k];
+      const double mx = (P.rsm2 > Rsup_Rinf2) ? P.rsm2 : Rsup_Rinf2;
+      integpl[k] += sum * planet_node(s2[k], znode - P.z, mx, P);
+      if (P.z < -0.05 * H || P.z > 0.05 * H) integpl[k] += sum * planet_node(s2[k], -znode - P.z, mx, P);
+      if (peb) {
+        const double zp = znode * Hcorr;
+        p_integpl[k] += sum * planet_node(s2[k], zp - P.z, mx, P);
+        if (P.z < -0.05 * pH || P.z > 0.05 * pH) p_integpl[k] += sum * planet_node(s2[k], -zp - P.z, mx, P);
+      }
+    }
+  }
+  integstar = is;
+  p_integstar = pis;
+}
+
 __global__ void k_forces(DevGrid g, ForceArgs a, ForceRings fr)
 {
   const int ns = g.ns;
@@ -448,16 +500,15 @@ __global__ void k_forces(DevGrid g, ForceArgs a, ForceRings fr)
     const double y = g.r.Rmed[i] * g.r.sintab[j];
     const double mcell = a.rho[l] * g.r.Surf[i];
     const double H = a.cs[l] * omegainv * g.k.sqrt_adiabind_inv;
-    const double H2 = H * H;
     const double H_avr = fr.H_avr[i];
-    int local = (fabs(H - H_avr) / H_avr > 0.05) ? 1 : 0;
+    int local = (div_fast(fabs(H - H_avr), H_avr) > 0.05) ? 1 : 0;
     double Hcorr = 0.0, pH = 0.0, pmcell = 0.0;
     if (peb) {
       pmcell = a.pdens[l] * g.r.Surf[i];
-      Hcorr = sqrt(a.pebble_alpha / a.tau[l]);
+      Hcorr = sqrt(div_fast(a.pebble_alpha, a.tau[l]));
       pH = H * Hcorr;
       const double p_H_avr = fr.p_H_avr[i];
-      if (fabs(pH - p_H_avr) / p_H_avr > 0.05) local = 1;
+      if (div_fast(fabs(pH - p_H_avr), p_H_avr) > 0.05) local = 1;
     }
     double s2[MAXPL_DEV], integpl[MAXPL_DEV], p_integpl[MAXPL_DEV], hillcut[MAXPL_DEV];
     int with[MAXPL_DEV];
@@ -484,100 +535,68 @@ __global__ void k_forces(DevGrid g, ForceArgs a, ForceRings fr)
     }
     double sigma, integstar, p_integstar = 0.0;
     if (local) {
-      const double zmax = 3.0 * H, deltaz = zmax / (double)Nvert;
-      sigma = 0.0;
-      integstar = 0.0;
-      for (int m = 1; m <= Nvert; m++) {
-        const double znode = ((double)m - 0.5) * deltaz, znode2 = znode * znode;
-        const double sum = exp(-(0.5 * znode2 / H2));
-        sigma += sum;
-        double d2 = r2 + znode2, d = sqrt(d2), denom = d * d2;
-        integstar += sum / denom;
-        if (peb) {
-          d2 = r2 + znode2 * Hcorr * Hcorr; d = sqrt(d2); denom = d * d2;
-          p_integstar += sum / denom;
-        }
-        for (int k = 0; k < npl; k++) {
-          if (!with[k]) continue;
-          const DevPlanet P = a.pl[k];
-          const double mx = (P.rsm2 > Rsup_Rinf2) ? P.rsm2 : Rsup_Rinf2;
-          double taper, dd;
-          d2 = s2[k] + (znode - P.z) * (znode - P.z);
-          if (d2 < P.rst2) { dd = sqrt(d2); taper = -3.0 * d2 * d2 / P.rst4 + 4.0 * dd * d2 / P.rst3; } else taper = 1.0;
-          d2 += mx; dd = sqrt(d2); denom = dd * d2;
-          integpl[k] += sum / denom * taper;
-          if (P.z < -0.05 * H || P.z > 0.05 * H) {
-            d2 = s2[k] + (-znode - P.z) * (-znode - P.z);
-            if (d2 < P.rst2) { dd = sqrt(d2); taper = -3.0 * d2 * d2 / P.rst4 + 4.0 * dd * d2 / P.rst3; } else taper = 1.0;
-            d2 += mx; dd = sqrt(d2); denom = dd * d2;
-            integpl[k] += sum / denom * taper;
-          }
-          if (peb) {
-            d2 = s2[k] + (znode * Hcorr - P.z) * (znode * Hcorr - P.z);
-            if (d2 < P.rst2) { dd = sqrt(d2); taper = -3.0 * d2 * d2 / P.rst4 + 4.0 * dd * d2 / P.rst3; } else taper = 1.0;
-            d2 += mx; dd = sqrt(d2); denom = dd * d2;
-            p_integpl[k] += sum / denom * taper;
-            if (P.z < -0.05 * pH || P.z > 0.05 * pH) {
-              d2 = s2[k] + (-znode * Hcorr - P.z) * (-znode * Hcorr - P.z);
-              if (d2 < P.rst2) { dd = sqrt(d2); taper = -3.0 * d2 * d2 / P.rst4 + 4.0 * dd * d2 / P.rst3; } else taper = 1.0;
-              d2 += mx; dd = sqrt(d2); denom = dd * d2;
-              p_integpl[k] += sum / denom * taper;
-            }
-          }
-        }
+      if (Nvert == 10) {
+        sigma = a.sig10;
+        vert_quad<10>(a.wq10, H, r2, Hcorr, pH, peb, npl, with, s2, Rsup_Rinf2, a.pl, integstar, p_integstar,
+                      integpl, p_integpl);
+      } else {
+        sigma = a.sig30;
+        vert_quad<30>(a.wq30, H, r2, Hcorr, pH, peb, npl, with, s2, Rsup_Rinf2, a.pl, integstar, p_integstar,
+                      integpl, p_integpl);
       }
     } else {
       sigma = fr.sigma_avr[i];
       integstar = fr.integstar_avr[i];
       if (peb) p_integstar = fr.p_integstar_avr[i];
     }
-    double tmp = integstar / sigma;
+    const double isig = div_fast(1.0, sigma);
+    double tmp = integstar * isig;
     double agr = -g.r.Rmed[i] * tmp;            // 0.0 + ar
     acc[0] = mcell * tmp * x;
     acc[1] = mcell * tmp * y;
     double pagr = 0.0;
-    if (peb) { const double pt = p_integstar / sigma; pagr = -g.r.Rmed[i] * pt; }
+    if (peb) { const double pt = p_integstar * isig; pagr = -g.r.Rmed[i] * pt; }
     double ax = 0.0, ay = 0.0, pax = 0.0, pay = 0.0;
     for (int k = 0; k < npl; k++) {
       const DevPlanet P = a.pl[k];
       double mpl = P.m;
       if (with[k]) {
         const bool off = (P.z < -0.05 * H || P.z > 0.05 * H);
-        tmp = off ? (x - P.x) * integpl[k] / (2.0 * sigma) : (x - P.x) * integpl[k] / sigma;
+        tmp = (x - P.x) * integpl[k] * (off ? 0.5 * isig : isig);
         ax += -mpl * tmp;
         if (a.exclude_hill) tmp *= hillcut[k];
         acc[2 + 2 * k] += mcell * tmp;
-        tmp = off ? (y - P.y) * integpl[k] / (2.0 * sigma) : (y - P.y) * integpl[k] / sigma;
+        tmp = (y - P.y) * integpl[k] * (off ? 0.5 * isig : isig);
         ay += -mpl * tmp;
         if (a.exclude_hill) tmp *= hillcut[k];
         acc[3 + 2 * k] += mcell * tmp;
         if (peb) {
           const bool poff = (P.z < -0.05 * pH || P.z > 0.05 * pH);
-          tmp = poff ? (x - P.x) * p_integpl[k] / (2.0 * sigma) : (x - P.x) * p_integpl[k] / sigma;
+          tmp = (x - P.x) * p_integpl[k] * (poff ? 0.5 * isig : isig);
           pax += -mpl * tmp;
           if (a.pebble_gravity) { if (a.exclude_hill) tmp *= hillcut[k]; acc[2 + 2 * k] += pmcell * tmp; }
-          tmp = poff ? (y - P.y) * p_integpl[k] / (2.0 * sigma) : (y - P.y) * p_integpl[k] / sigma;
+          tmp = (y - P.y) * p_integpl[k] * (poff ? 0.5 * isig : isig);
           pay += -mpl * tmp;
           if (a.pebble_gravity) { if (a.exclude_hill) tmp *= hillcut[k]; acc[3 + 2 * k] += pmcell * tmp; }
         }
       } else {
         mpl *= a.mass_taper;
-        double d2 = s2[k] + P.z * P.z + P.smoothing2, d = sqrt(d2), denom = d * d2;
-        tmp = (x - P.x) / denom;
+        double d2 = s2[k] + P.z * P.z + P.smoothing2, iv = rsqrt(d2), id3 = iv * iv * iv;
+        tmp = (x - P.x) * id3;
         ax += -mpl * tmp;
         if (a.exclude_hill) tmp *= hillcut[k];
         acc[2 + 2 * k] += mcell * tmp;
-        tmp = (y - P.y) / denom;
+        tmp = (y - P.y) * id3;
         ay += -mpl * tmp;
         if (a.exclude_hill) tmp *= hillcut[k];
         acc[3 + 2 * k] += mcell * tmp;
         if (peb) {
           d2 += -P.smoothing2 + P.smoothing2 * Hcorr * Hcorr;
-          d = sqrt(d2); denom = d * d2;
-          tmp = (x - P.x) / denom;
+          iv = rsqrt(d2); id3 = iv * iv * iv;
+          tmp = (x - P.x) * id3;
           pax += -mpl * tmp;
           if (a.pebble_gravity) { if (a.exclude_hill) tmp *= hillcut[k]; acc[2 + 2 * k] += pmcell * tmp; }
-          tmp = (y - P.y) / denom;
+          tmp = (y - P.y) * id3;
           pay += -mpl * tmp;
           if (a.pebble_gravity) { if (a.exclude_hill) tmp *= hillcut[k]; acc[3 + 2 * k] += pmcell * tmp; }
         }
@@ -637,8 +656,20 @@ void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr, dou
   if (a0.pebbles) aux_ring_means(g, a0.tau, fr.tau_avr, nullptr, nullptr, 0, g.nr, s);
   k_force_rings<<<(g.nr + 127) / 128, 128, 0, s>>>(g, fr, a0.pebbles, a0.pebble_alpha);
   g_thorin_launches++;
+  ForceArgs a = a0;
+  for (int pass = 0; pass < 2; pass++) {
+    const int nv = pass ? 30 : 10;
+    double *w = pass ? a.wq30 : a.wq10, sig = 0.0;
+    const double deltaz = 3.0 / (double)nv;          // H = 1
+    for (int m = 1; m <= nv; m++) {
+      const double z = ((double)m - 0.5) * deltaz;
+      w[m - 1] = exp(-(0.5 * (z * z)));
+      sig += w[m - 1];
+    }
+    if (pass) a.sig30 = sig; else a.sig10 = sig;
+  }
   dim3 grid = grid2d(g.ns, g.nr, 128);
-  k_forces<<<grid, 128, 0, s>>>(g, a0, fr);
+  k_forces<<<grid, 128, 0, s>>>(g, a, fr);
   g_thorin_launches++;
   k_forces_final<<<1, 1024, 0, s>>>(a0.part, grid.x * grid.y, 2 + 2 * a0.npl, scal);
   g_thorin_launches++;

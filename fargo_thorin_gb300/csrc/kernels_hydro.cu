@@ -37,7 +37,7 @@ __global__ void k_substep1(DevGrid g, const double *__restrict__ rho, const doub
   if (i >= 1) {
     const int lim = l - ns;
     const double plim = gm1 * energy[lim];
-    double gradp = (pl - plim) * 2.0 / (rho[l] + rho[lim]) * g.r.InvDiffRmed[i];
+    double gradp = div_fast((pl - plim) * 2.0, rho[l] + rho[lim]) * g.r.InvDiffRmed[i];
     double vt2 = vtheta[l] + vtheta[ljp] + vtheta[lim] + vtheta[ljp - ns];
     vt2 = vt2 / 4.0 + g.r.Rinf[i] * omega_frame;
     vt2 = vt2 * vt2;
@@ -46,7 +46,7 @@ __global__ void k_substep1(DevGrid g, const double *__restrict__ rho, const doub
     if (pebbles) {
       double acc = tmp;
       if (back_reaction) {
-        tmp = dragr[l] * 2.0 / (rho[l] + rho[lim]);
+        tmp = div_fast(dragr[l] * 2.0, rho[l] + rho[lim]);
         v += dt * tmp;
         acc += tmp;
       }
@@ -57,14 +57,14 @@ __global__ void k_substep1(DevGrid g, const double *__restrict__ rho, const doub
   {
     const double invdxtheta = invdxtheta_r[i];
     const double pljm = gm1 * energy[ljm];
-    double gradp = (pl - pljm) * 2.0 / (rho[l] + rho[ljm]) * invdxtheta;
+    double gradp = div_fast((pl - pljm) * 2.0, rho[l] + rho[ljm]) * invdxtheta;
     double tmp = -gradp + 0.5 * (agt[l] + agt[ljm]);
     double v = vtheta[l] + dt * tmp;
     v += dt * supp_torque[i];
     if (pebbles) {
       double acc = tmp + supp_torque[i];
       if (back_reaction) {
-        tmp = dragt[l] * 2.0 / (rho[l] + rho[ljm]);
+        tmp = div_fast(dragt[l] * 2.0, rho[l] + rho[ljm]);
         v += dt * tmp;
         acc += tmp;
       }
@@ -179,13 +179,13 @@ __global__ void k_substep2(DevGrid g, const double *__restrict__ rho, const doub
   if (i >= 1) {
     const int lim = l - ns;
     const double qrm = avisc(vr[l] - vr[lim], rho[lim]);
-    vrnew[l] = vr[l] - dt * 2.0 / (rho[l] + rho[lim]) * (qr - qrm) * g.r.InvDiffRmed[i];
+    vrnew[l] = vr[l] - div_fast(dt * 2.0, rho[l] + rho[lim]) * (qr - qrm) * g.r.InvDiffRmed[i];
   } else {
     vrnew[l] = 0.0;
   }
   const double invdxtheta = invdxtheta_r[i];
   const double qtm = avisc(vt[l] - vt[ljm], rho[ljm]);
-  vtnew[l] = vt[l] - dt * 2.0 / (rho[l] + rho[ljm]) * (qt - qtm) * invdxtheta;
+  vtnew[l] = vt[l] - div_fast(dt * 2.0, rho[l] + rho[ljm]) * (qt - qtm) * invdxtheta;
   if (energy_eq)
     eint[l] = energy[l] - dt * qr * (vr[lip] - vr[l]) * g.r.InvDiffRsup[i] - dt * qt * (vt[ljp] - vt[l]) * invdxtheta;
 }
@@ -205,7 +205,7 @@ __global__ void k_qplus(DevGrid g, const double *__restrict__ vr, const double *
     const double nu = g.r.nu_med[i];
     double q;
     if (nu != 0.0) {
-      q = 0.5 / nu / rho[l] * (s.trr * s.trr + 2.0 * s.trp * s.trp + s.tpp * s.tpp);
+      q = div_fast(div_fast(0.5, nu), rho[l]) * (s.trr * s.trr + 2.0 * s.trp * s.trp + s.tpp * s.tpp);
       q += (2.0 / 9.0) * nu * rho[l] * s.divv * s.divv;
     } else {
       q = 0.0;
@@ -233,10 +233,10 @@ __global__ void k_eos(DevGrid g, const double *__restrict__ rho, const double *_
   const int ns = g.ns;
   CELL_LOOP_2D
   const double r = rho[l], e = energy[l];
-  double tmp2 = 1.0 / (r * 1.0);
+  double tmp2 = div_fast(1.0, r * 1.0);
   double tmp1 = e * 1.0 * gm1;
   temper[l] = tmp1 * tmp2;
-  cs[l] = sqrt(gg1 * fabs(e) / r);
+  cs[l] = sqrt(div_fast(gg1 * fabs(e), r));
 }
 
 // Opacity laws, Opacity.c.
@@ -275,12 +275,12 @@ __device__ double opacity_BL94(double rho, double T)
   if (grains) {
     const double T2 = T * T;
     const double k1 = kappa[0] * T2;                       // pow(T, 2.0)
-    const double k2 = kappa[1] / (T2 * T2 * T2 * T);        // pow(T, -7.0)
+    const double k2 = div_fast(kappa[1], T2 * T2 * T2 * T);        // pow(T, -7.0)
     const double k3 = kappa[2] * sqrt(T);                  // pow(T, 0.5)
-    double t1 = 1.0 / (k1 * k1) + 1.0 / (k2 * k2);
-    t1 = 1.0 / (t1 * t1);
+    double t1 = div_fast(1.0, k1 * k1) + div_fast(1.0, k2 * k2);
+    t1 = div_fast(1.0, t1 * t1);
     const double T5 = T2 * T2 * T;
-    const double x = k3 / (1.0 + 1.0e22 / (T5 * T5));     // pow(T, -10.0)
+    const double x = div_fast(k3, 1.0 + div_fast(1.0e22, T5 * T5));     // pow(T, -10.0)
     const double x2 = x * x;
     const double t2 = x2 * x2;                             // pow(., 4.0)
     k = sqrt(sqrt(t1 + t2));                               // pow(., 0.25)
@@ -358,8 +358,8 @@ __device__ __forceinline__ double gradt_mag(const DevGrid &g, const double *T, i
 
 __device__ __forceinline__ double flux_limiter(double s)
 {
-  if (s <= 2.0) return 2.0 / (3.0 + sqrt(9.0 + 10.0 * s * s));
-  return 10.0 / (10.0 * s + 9.0 + sqrt(81.0 + 180.0 * s));
+  if (s <= 2.0) return div_fast(2.0, 3.0 + sqrt(9.0 + 10.0 * s * s));
+  return div_fast(10.0, 10.0 * s + 9.0 + sqrt(81.0 + 180.0 * s));
 }
 
 // MidplaneVolumeDensity, OpacityProfile, CalculateQminus and the centred
@@ -379,23 +379,23 @@ __global__ void k_diffcoef(DevGrid g, const double *__restrict__ rho, const doub
   if (j < ns) {
     const int l = j + i * ns;
     const double H = cs[l] * g.r.OmegaInv[i] * g.k.sqrt_adiabind_inv;
-    const double vd = rho[l] / H * g.k.sqrt2pi_inv;
+    const double vd = div_fast(rho[l], H) * g.k.sqrt2pi_inv;
     const double Tl = T[l];
     double kap;
     if (parametric_raw > 0.0) kap = parametric_cu;
     else kap = opacity_law(law, vd * g.k.rho2cgs, Tl * g.k.t2si, parametric_raw) * g.k.opa2cu;
     opacity[l] = kap;
     const double tau = opacity_drop * 0.5 * kap * rho[l];
-    const double taueff = 0.375 * tau + taueff_c + 0.25 / tau;
+    const double taueff = 0.375 * tau + taueff_c + div_fast(0.25, tau);
     const double T3 = cube_rn(Tl);
-    qminus[l] = 2.0 * g.k.sigma_sb * T3 / taueff;
+    qminus[l] = div_fast(2.0 * g.k.sigma_sb * T3, taueff);
     const int ig = (i == 0) ? 1 : (i == nr - 1 ? nr - 2 : i);
     const double gradt = gradt_mag(g, T, ig, j, invdxtheta_r);
-    const double fac = 1.0 / (vd * kap);
-    const double s = 4.0 * gradt * fac / Tl;
+    const double fac = div_fast(1.0, vd * kap);
+    const double s = div_fast(4.0 * gradt * fac, Tl);
     const double D = flux_limiter(s) * 16.0 * g.k.sigma_sb * T3 * fac;
     dcen[l] = D;
-    dtl = deltar2_r[i] / D;
+    dtl = div_fast(deltar2_r[i], D);
   }
   const double m = block_reduce(dtl, OpMin(), 1.0e38);
   if (threadIdx.x == 0) dtmin_part[blockIdx.x + blockIdx.y * gridDim.x] = m;
@@ -480,13 +480,13 @@ __global__ void k_matrix(DevGrid g, const double *__restrict__ rho, const double
   const double Hjp = cs[ljp] * oi * sqi;
   const double Dt_ljp = 0.5 * (dcen[ljp] + dcen[l]);
   const double B_ljp = Dt_ljp * idx2 * 2.0 * Hjp;
-  const double bfac = dt / (rho[l] * g.k.cv);
-  const double afac = bfac * g.r.InvDiffRsup[i] * 2.0 * H / g.r.Rmed[i];
+  const double bfac = div_fast(dt, rho[l] * g.k.cv);
+  const double afac = div_fast(bfac * g.r.InvDiffRsup[i] * 2.0 * H, g.r.Rmed[i]);
   const double Tl = T[l], qm = qminus[l];
   const size_t q = sor_pidx(i, j, ns >> 1);
   const double diag = 1.0 + divv[l] * gm1 * dt + 4.0 * bfac * qm + afac * (A_lip + A_l) + bfac * (B_ljp + B_l);
   ml[q] = diag;
-  rml[q] = 1.0 / diag;
+  rml[q] = div_fast(1.0, diag);
   mlip[q] = -afac * A_lip;
   mlim[q] = -afac * A_l;
   mljp[q] = -bfac * B_ljp;
@@ -662,17 +662,6 @@ __global__ void k_energy_from_t(DevGrid g, const double *__restrict__ rho, doubl
 // state, in four cell-parallel passes: quotients by the density, van Leer
 // slopes, upwind face values, flux divergence.
 
-// x / d for a d whose correctly rounded reciprocal r = 1/d is at hand: the
-// product q0 = x*r is corrected once, q0 + (x - d*q0)*r with the residual
-// formed exactly by an FMA (Markstein, IBM J. Res. Dev. 34(1), 1990).  The
-// result is the IEEE quotient in all of 2e8 random trials over the ranges of
-// the fields and at most one ulp from it otherwise.
-__device__ __forceinline__ double div_by_rcp(double x, double d, double r)
-{
-  const double q0 = x * r;
-  const double e = __fma_rn(-d, q0, x);
-  return __fma_rn(e, r, q0);
-}
 
 // ComputeLRMomenta (TransportEuler.c:318-347) + DivisePolarGrid quotients.
 __global__ void k_rad_prep(DevGrid g, int nq, const double *__restrict__ rho, const double *__restrict__ vr,
@@ -689,7 +678,7 @@ __global__ void k_rad_prep(DevGrid g, int nq, const double *__restrict__ rho, co
   const double c = r * (vt[ljp] + rm * omega_frame) * rm;
   const double d = r * (vt[l] + rm * omega_frame) * rm;
   rmp[l] = a; rmm[l] = b; tmp_[l] = c; tmm[l] = d;
-  const double den = r + 1e-20, rcp = 1.0 / den;
+  const double den = r + 1e-20, rcp = div_fast(1.0, den);
   w0[l] = div_by_rcp(a, den, rcp); w1[l] = div_by_rcp(b, den, rcp);
   w2[l] = div_by_rcp(c, den, rcp); w3[l] = div_by_rcp(d, den, rcp);
   if (nq == 6) we[l] = div_by_rcp(energy[l], den, rcp);
@@ -702,7 +691,7 @@ __device__ __forceinline__ double vl_slope_r(const DevGrid &g, const double *q, 
   if (i == 0 || i == nr - 1) return 0.0;
   const double dqm = (q[l] - q[l - ns]) * g.r.InvDiffRmed[i];
   const double dqp = (q[l + ns] - q[l]) * g.r.InvDiffRmed[i + 1];
-  return (dqp * dqm > 0.0) ? 2.0 * dqp * dqm / (dqp + dqm) : 0.0;
+  return (dqp * dqm > 0.0) ? div_fast(2.0 * dqp * dqm, dqp + dqm) : 0.0;
 }
 
 
@@ -805,7 +794,7 @@ __device__ __forceinline__ double azi_vl_slope(double qm, double q0, double qp, 
   const double s = dqp + dqm;
   const bool pos = __double_as_longlong(p) > 0LL;                 // p > 0.0
   const bool nz = (__double_as_longlong(s) << 1) != 0LL;          // s != 0.0
-  return (pos && nz) ? p / s * invdx : 0.0;
+  return (pos && nz) ? div_fast(p, s) * invdx : 0.0;
 }
 
 template <int NQ>
@@ -846,7 +835,7 @@ __global__ void __launch_bounds__(AZ_TMAX) k_azimuthal(DevGrid g, AziIO io, cons
     __syncthreads();
     const double rs = up ? s_a[tm] + c * s_b[tm] : rho - c * drho;
     const double den = rho + 1e-20;                // RhoInt + 1e-20
-    const double rcp = 1.0 / den;
+    const double rcp = div_fast(1.0, den);
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < NQ; k++) {
@@ -907,19 +896,19 @@ __global__ void k_velocities(DevGrid g, const double *__restrict__ rho, const do
   const double rm = g.r.Rmed[i];
   double v;
   if (i == 0) v = 0.0;
-  else v = (rmp[l - ns] + rmm[l]) / (rho[l] + rho[l - ns] + 1e-20);
+  else v = div_fast(rmp[l - ns] + rmm[l], rho[l] + rho[l - ns] + 1e-20);
   if (damp_vrad && (rm < drin || rm > drout)) {
     const double lambda = g.r.WaveKiller[i] * dt;
     v = (v + lambda * 0.0) / (1.0 + lambda);
   }
   vr[l] = v;
-  vt[l] = (tmp_[ljm] + tmm[l]) / (rho[l] + rho[ljm] + 1e-15) / rm - rm * omega_frame;
+  vt[l] = div_fast(div_fast(tmp_[ljm] + tmm[l], rho[l] + rho[ljm] + 1e-15), rm) - rm * omega_frame;
   if (temper) {
     const double r = rho[l], e = energy[l];
-    double tmp2 = 1.0 / (r * 1.0);
+    double tmp2 = div_fast(1.0, r * 1.0);
     double tmp1 = e * 1.0 * gm1;
     temper[l] = tmp1 * tmp2;
-    cs[l] = sqrt(gg1 * fabs(e) / r);
+    cs[l] = sqrt(div_fast(gg1 * fabs(e), r));
   }
 }
 

@@ -1,0 +1,65 @@
+// thorin_selftest.cu -- on-device check of the kernels' division routine
+// (div_fast) against IEEE division.
+#include <string>
+#include "thorin_kernels.cuh"
+
+extern thread_local std::string g_last_error;
+
+// splitmix64 finaliser as a counter-based random source
+__device__ __forceinline__ unsigned long long st_mix(unsigned long long z)
+{
+  z += 0x9e3779b97f4a7c15ULL;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+
+// random double with uniform mantissa, exponent uniform in [-emax, emax], random sign
+__device__ __forceinline__ double st_value(unsigned long long key, double emax)
+{
+  const unsigned long long a = st_mix(key), b = st_mix(key ^ 0x5bd1e995ULL);
+  const double u = (double)(a >> 11) * (1.0 / 9007199254740992.0);
+  const double m = 1.0 + (double)(b >> 11) * (1.0 / 9007199254740992.0);
+  const double v = m * exp2(-emax + 2.0 * emax * u);
+  return (b & 1ULL) ? -v : v;
+}
+
+__global__ void k_selftest_division(long long n, unsigned long long seed, double emax,
+                                    unsigned long long *__restrict__ out)
+{
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const double x = st_value(seed + 2ULL * (unsigned long long)t, emax);
+  const double d = st_value(seed + 2ULL * (unsigned long long)t + 1ULL, emax);
+  const long long a = __double_as_longlong(x / d), b = __double_as_longlong(div_fast(x, d));
+  const unsigned long long u = (unsigned long long)(a > b ? a - b : b - a);
+  if (u) {
+    atomicAdd(out, 1ULL);
+    atomicMax(out + 1, u);
+  }
+}
+
+extern "C" int thorin_selftest_division(long long n, unsigned long long seed, double max_exponent,
+                                        unsigned long long *mismatches, unsigned long long *max_ulp)
+{
+  if (n < 1 || !mismatches || !max_ulp || !(max_exponent >= 0.0 && max_exponent <= 1000.0)) {
+    g_last_error = "selftest_division: n >= 1, 0 <= max_exponent <= 1000 and output pointers required";
+    return THORIN_ERR_ARG;
+  }
+  unsigned long long *dev = nullptr, host[2] = {0ULL, 0ULL};
+  cudaError_t e = cudaMalloc((void **)&dev, sizeof(host));
+  if (e == cudaSuccess) e = cudaMemset(dev, 0, sizeof(host));
+  if (e == cudaSuccess) {
+    k_selftest_division<<<(unsigned)((n + 255) / 256), 256>>>(n, seed, max_exponent, dev);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(host, dev, sizeof(host), cudaMemcpyDeviceToHost);
+  if (dev) cudaFree(dev);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("selftest_division: ") + cudaGetErrorString(e);
+    return THORIN_ERR_CUDA;
+  }
+  *mismatches = host[0];
+  *max_ulp = host[1];
+  return THORIN_OK;
+}

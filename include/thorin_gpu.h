@@ -290,6 +290,15 @@ int thorin_integrals_static(const double *rho, const double *vrad, const double 
                             const double *surf, const double *rinf, const double *rsup, const double *rmed,
                             int nrad, int nsec, double omega_frame, double *out, void *stream);
 
+/* Self-test of the kernels' division routine (reciprocal estimate, one
+ * Newton-Raphson step, Markstein correction) against IEEE division on the
+ * current GPU: n random quotients of values with exponents uniform in
+ * [-max_exponent, max_exponent]; returns how many differ and the largest
+ * difference in ulps.  No counterpart in the reference (its divisions are
+ * the C operator). */
+int thorin_selftest_division(long long n, unsigned long long seed, double max_exponent,
+                             unsigned long long *mismatches, unsigned long long *max_ulp);
+
 /* Last CUDA error string (thread-local, for diagnostics). */
 const char *thorin_gpu_last_error(void);
 

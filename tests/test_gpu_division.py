@@ -1,0 +1,20 @@
+"""The kernels divide with a reciprocal estimate, one Newton-Raphson step and
+Markstein's correction instead of the IEEE divide sequence.  This checks the
+routine against CUDA's IEEE division on the GPU over random operands: at
+most one ulp apart, and in practice identical."""
+import ctypes as C
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("max_exponent,seed", [(40.0, 1), (300.0, 2), (1000.0, 3)])
+def test_division_matches_ieee(max_exponent, seed):
+    from fargo_thorin_gb300 import _lib
+    lib = _lib.load()
+    n = 1 << 26
+    mis, ulp = C.c_ulonglong(), C.c_ulonglong()
+    _lib.check(lib.thorin_selftest_division(n, seed, max_exponent, C.byref(mis), C.byref(ulp)), "selftest_division")
+    assert ulp.value <= 1
+    assert mis.value <= n // 1000000

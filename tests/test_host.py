@@ -1,0 +1,141 @@
+"""Host-side logic and the C-ABI boundary, without a GPU: the library loads
+and exports every function include/thorin_gpu.h declares, parameter handling
+matches the reference's variable table, unsupported options are rejected
+before any device work, and the multi-replica bench aggregation (max time,
+summed updates) works across two gloo ranks."""
+import ctypes as C
+import os
+import re
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "thorin_gpu.h")
+sys.path.insert(0, ROOT)
+
+from fargo_thorin_gb300 import params as P  # noqa: E402
+from fargo_thorin_gb300 import workloads  # noqa: E402
+
+
+def _declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\**\s*(thorin_\w+)\s*\(", text, flags=re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from fargo_thorin_gb300 import _lib
+    from fargo_thorin_gb300 import build as B
+    if not os.path.exists(_lib.LIB_PATH):
+        B.build()
+    return _lib.load()
+
+
+def test_header_functions_exported(lib):
+    from fargo_thorin_gb300 import _lib
+    names = _declared_functions()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in the header but not exported"
+        assert n in _lib.SIGNATURES, f"{n} has no ctypes signature"
+
+
+def test_params_default_matches_struct(lib):
+    """thorin_params_default fills the grid size and the SOR controls the same
+    way the Python in.par path does for an empty file plus mandatory keys."""
+    p = P.ThorinParams()
+    lib.thorin_params_default(C.byref(p), 128, 384)
+    assert (p.nrad, p.nsec) == (128, 384)
+    q = workloads.params_for("disk0", 128, 384)
+    assert p.sor_maxiters == q.sor_maxiters
+    assert p.adiabind == q.adiabind
+
+
+def test_read_inpar_case_insensitive_and_defaults():
+    text = workloads.inpar_text("disk1", 64, 192).replace("Nrad", "nRaD")
+    v = P.read_inpar(text)
+    assert v["NRAD"] == 64 and v["NSEC"] == 192
+    assert v["INNERBOUNDARY"].upper() == "DAMPING"
+    p = P.derive(v)
+    assert p.pebbles == 1 and p.back_reaction == 1 and p.feel_disk == 1
+    assert p.diffusive_particles == 1          # Interpret.c assigns instead of comparing
+    with pytest.warns(UserWarning):
+        P.read_inpar(text + "\nNoSuchKey 3\n")
+
+
+@pytest.mark.parametrize("key,val,msg", [("EnergyEquation", "NO", "isothermal"),
+                                         ("InnerBoundary", "OPEN", "open"),
+                                         ("AerodynamicDrag", "YES", "AerodynamicDrag")])
+def test_unsupported_rejected(lib, key, val, msg):
+    text = workloads.inpar_text("disk1", 32, 96) + f"\n{key} {val}\n"
+    p = P.derive(P.read_inpar(text))
+    with pytest.raises(NotImplementedError, match=msg):
+        P.check_supported(p)
+    h = C.c_void_p()
+    rc = lib.thorin_gpu_create(C.byref(p), C.byref(h))
+    assert rc == 1                                  # THORIN_ERR_ARG, before any CUDA call
+    assert not h.value
+    assert msg in lib.thorin_gpu_last_error().decode()
+
+
+def test_bad_grid_rejected(lib):
+    p = workloads.params_for("disk0", 24, 71)      # odd nsec
+    h = C.c_void_p()
+    assert lib.thorin_gpu_create(C.byref(p), C.byref(h)) != 0
+
+
+def test_planet_from_elements_circular(lib):
+    s = P.ThorinPlanets()
+    rc = lib.thorin_planet_from_elements(C.byref(s), 0, *[C.c_float(v) for v in (3e-5, 0, 0, 1.0, 0, 0, 0, 0, 0)])
+    assert rc == 0
+    py = workloads.planet_from_elements(3e-5, 0, 0, 1.0, 0, 0, 0, 0, 0)
+    assert abs(s.x[0] - py["x"]) == 0.0 and abs(s.vy[0] - py["vy"]) < 1e-15
+    assert abs(s.vy[0] - (1.0 + float(__import__("numpy").float32(3e-5))) ** 0.5) < 1e-15
+
+
+def test_create_without_gpu_fails_loudly():
+    """No CPU fallback: without a GPU the product path reports a CUDA error."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from fargo_thorin_gb300.disk import GpuDisk
+    from fargo_thorin_gb300._lib import ThorinError
+    with pytest.raises(ThorinError):
+        GpuDisk(workloads.params_for("disk0", 24, 72))
+
+
+def _gloo_rank(rank, ws, port, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    sys.path.insert(0, ROOT)
+    import bench
+    out = bench.reduce_over_ranks([10.0 + rank, 3 + rank], ["max", "sum"], "cpu")
+    dist.destroy_process_group()
+    q.put((rank, out))
+
+
+def test_replica_aggregation_gloo():
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29500 + os.getpid() % 1000
+    procs = [ctx.Process(target=_gloo_rank, args=(r, 2, port, q)) for r in range(2)]
+    for pr in procs:
+        pr.start()
+    res = dict(q.get(timeout=120) for _ in procs)
+    for pr in procs:
+        pr.join(60)
+        assert pr.exitcode == 0
+    assert res[0] == res[1] == [11.0, 7.0]
+
+
+def test_reference_arm_nonzero_rank_exits():
+    """Under torchrun only rank 0 runs the CPU reference arm."""
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference"], env=env,
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == ""
