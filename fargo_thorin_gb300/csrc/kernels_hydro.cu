@@ -455,7 +455,7 @@ __global__ void k_matrix(DevGrid g, const double *__restrict__ rho, const double
                          const double *__restrict__ qminus, const double *__restrict__ qplus, const double *__restrict__ qirr,
                          double *__restrict__ ml, double *__restrict__ mlip, double *__restrict__ mlim,
                          double *__restrict__ mljp, double *__restrict__ mljm, double *__restrict__ rhs,
-                         double *__restrict__ rml, double dt, double gm1, const double *__restrict__ invdxtheta2_r,
+                         double dt, double gm1, const double *__restrict__ invdxtheta2_r,
                          int irradiation, int nheat, const int *__restrict__ heat_idx,
                          const double *__restrict__ heat_val)
 {
@@ -486,7 +486,6 @@ __global__ void k_matrix(DevGrid g, const double *__restrict__ rho, const double
   const size_t q = sor_pidx(i, j, ns >> 1);
   const double diag = 1.0 + divv[l] * gm1 * dt + 4.0 * bfac * qm + afac * (A_lip + A_l) + bfac * (B_ljp + B_l);
   ml[q] = diag;
-  rml[q] = div_fast(1.0, diag);
   mlip[q] = -afac * A_lip;
   mlim[q] = -afac * A_l;
   mljp[q] = -bfac * B_ljp;
@@ -510,7 +509,12 @@ __device__ __forceinline__ double sor_resid_at(const double *T, const double *ml
                                                const double *mlim, const double *mljp, const double *mljm,
                                                const double *rhs, int l, int lip, int lim, int ljp, int ljm, size_t q)
 {
-  return T[l] * ml[q] + T[lip] * mlip[q] + T[lim] * mlim[q] + T[ljp] * mljp[q] + T[ljm] * mljm[q] - rhs[q];
+  // the reference's sum T ml + T_ip mlip + T_im mlim + T_jp mljp + T_jm mljm - rhs as a chain of five FMAs
+  double r = __fma_rn(T[l], ml[q], -rhs[q]);
+  r = __fma_rn(T[lip], mlip[q], r);
+  r = __fma_rn(T[lim], mlim[q], r);
+  r = __fma_rn(T[ljp], mljp[q], r);
+  return __fma_rn(T[ljm], mljm[q], r);
 }
 
 // Sum of the block partials by the block holding the last ticket; every
@@ -533,7 +537,7 @@ __global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__r
                                                     const double *__restrict__ ml, const double *__restrict__ mlip,
                                                     const double *__restrict__ mlim, const double *__restrict__ mljp,
                                                     const double *__restrict__ mljm, const double *__restrict__ rhs,
-                                                    SorCtl c)
+                                                    double *__restrict__ cw, double omega, SorCtl c)
 {
   const int ns = g.ns, half = ns >> 1;
   const int i = blockIdx.y + 1;
@@ -544,7 +548,9 @@ __global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__r
       const int l = j + i * ns;
       const int ljp = (j == ns - 1) ? i * ns : l + 1;
       const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
-      a += fabs(sor_resid_at(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm, sor_pidx(i, j, half)));
+      const size_t q = sor_pidx(i, j, half);
+      a += fabs(sor_resid_at(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm, q));
+      cw[q] = div_fast(omega, ml[q]);              // the sweeps' update is resid * omega / ml
     }
   }
   a = block_reduce(a, OpAdd(), 0.0);
@@ -566,16 +572,16 @@ __global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__r
 }
 
 // One colour pass of sweep n.  Each thread updates SOR_CPT cells of ring i
-// (k = base + m*blockDim, j = 2k + parity).  The reference's
-// delta = omega*resid/Ml is formed as the correctly rounded quotient from the
-// stored reciprocal r = 1/Ml: q0 = x*r, e = x - Ml*q0 (exact, FMA),
-// delta = q0 + e*r (one FMA) -- Markstein's correction, equal to IEEE
-// division -- which costs three FP64 operations instead of a full divide.
+// (k = base + m*blockDim, j = 2k + parity).  The pass is bound by the FP64
+// pipe, so each cell costs nine FP64 instructions: the residual as five FMAs,
+// its absolute value added to the L1 norm, delta = resid * (omega/Ml) with
+// omega/Ml prepared once per solve by k_sor_resid0, the update, and the
+// change test delta > T*SORPRECISION taken from the sign of one FMA.
 __global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict__ T, const double *__restrict__ ml,
                                                   const double *__restrict__ mlip, const double *__restrict__ mlim,
                                                   const double *__restrict__ mljp, const double *__restrict__ mljm,
-                                                  const double *__restrict__ rhs, const double *__restrict__ rml,
-                                                  SorCtl c, double omega, double eps, int pass, int n, int maxiters)
+                                                  const double *__restrict__ rhs, const double *__restrict__ cw,
+                                                  SorCtl c, double eps, int pass, int n, int maxiters)
 {
   if (*((volatile int *)c.done)) return;
   const int ns = g.ns, half = ns >> 1;
@@ -596,14 +602,11 @@ __global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict_
       const size_t q = pbase + k;
       const double resid = sor_resid_at(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm, q);
       a += fabs(resid);
-      const double x = omega * resid;
-      const double r = rml[q];
-      const double q0 = x * r;
-      const double e = __fma_rn(-ml[q], q0, x);
-      const double delta = __fma_rn(e, r, q0);
+      const double delta = resid * cw[q];
       const double tn = T[l] - delta;
       T[l] = tn;
-      ch += (delta > tn * TH_SORPRECISION) ? 1 : 0;
+      // delta > tn * SORPRECISION, from the sign of the exact difference
+      ch += (__double_as_longlong(__fma_rn(-tn, TH_SORPRECISION, delta)) > 0LL) ? 1 : 0;
     }
   }
   a = block_reduce(a, OpAdd(), 0.0);
@@ -989,13 +992,13 @@ void hydro_irradiation(const DevGrid &g, const double *rho, const double *cs, co
 
 void hydro_matrix(const DevGrid &g, const double *rho, const double *T, const double *cs, const double *dcen,
                   const double *divv, const double *qminus, const double *qplus, const double *qirr, double *ml,
-                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs, double *rml, double dt,
+                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs, double dt,
                   double gm1, const double *invdxtheta2_r, int irradiation, int nheat, const int *heat_idx,
                   const double *heat_val, cudaStream_t s)
 {
   if (g.nr < 3) return;
   k_matrix<<<grid2d(g.ns, g.nr - 2, BX), BX, 0, s>>>(g, rho, T, cs, dcen, divv, qminus, qplus, qirr, ml, mlip, mlim, mljp,
-                                                     mljm, rhs, rml, dt, gm1, invdxtheta2_r, irradiation, nheat, heat_idx,
+                                                     mljm, rhs, dt, gm1, invdxtheta2_r, irradiation, nheat, heat_idx,
                                                      heat_val);
   g_thorin_launches++;
 }
@@ -1021,21 +1024,22 @@ int sor_blocks(const DevGrid &g)
 }
 
 void hydro_sor_resid0(const DevGrid &g, const double *T, const double *ml, const double *mlip, const double *mlim,
-                      const double *mljp, const double *mljm, const double *rhs, const SorCtl &c, cudaStream_t s)
+                      const double *mljp, const double *mljm, const double *rhs, double *cw, double omega,
+                      const SorCtl &c, cudaStream_t s)
 {
-  k_sor_resid0<<<sor_grid_resid(g), SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, c);
+  k_sor_resid0<<<sor_grid_resid(g), SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, cw, omega, c);
   g_thorin_launches++;
 }
 
 void hydro_sor_sweeps(const DevGrid &g, double *T, const double *ml, const double *mlip, const double *mlim,
-                      const double *mljp, const double *mljm, const double *rhs, const double *rml, const SorCtl &c,
-                      double omega, double eps, int first, int count, int maxiters, cudaStream_t s)
+                      const double *mljp, const double *mljm, const double *rhs, const double *cw, const SorCtl &c,
+                      double eps, int first, int count, int maxiters, cudaStream_t s)
 {
   const dim3 grid = sor_grid_pass(g);
   for (int n = first; n < first + count && n <= maxiters; n++) {
-    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, rml, c, omega, eps, 1, n, maxiters);
+    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, cw, c, eps, 1, n, maxiters);
     g_thorin_launches++;
-    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, rml, c, omega, eps, 2, n, maxiters);
+    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, cw, c, eps, 2, n, maxiters);
     g_thorin_launches++;
   }
 }

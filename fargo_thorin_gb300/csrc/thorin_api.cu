@@ -107,7 +107,7 @@ struct thorin_disk {
   // fields
   double *rho, *vrad, *vtheta, *energy, *vrad_new, *vtheta_new, *energy_new, *vrad_int, *vtheta_int, *energy_int;
   double *cs, *temper, *qplus, *qminus, *opacity, *divv, *trr, *trp, *tpp, *agr, *agt, *pagr, *pagt, *dcen;
-  double *ml, *mlip, *mlim, *mljp, *mljm, *rhs, *rml, *tbackup, *flaring, *qirr;
+  double *ml, *mlip, *mlim, *mljp, *mljm, *rhs, *sor_cw, *tbackup, *flaring, *qirr;   // sor_cw = omega / ml
   double *pdens, *pvrad, *pvtheta, *psize, *tau, *paccr, *pacct, *gaccr, *gacct, *dragr, *dragt, *macc;
   double *t_rho_gas, *t_e_gas, *t_rho_peb;
   TransportScratch ts;
@@ -334,7 +334,7 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   double **F[] = {&d->rho, &d->vrad, &d->vtheta, &d->energy, &d->vrad_new, &d->vtheta_new, &d->energy_new,
                   &d->vrad_int, &d->vtheta_int, &d->energy_int, &d->cs, &d->temper, &d->qplus, &d->qminus,
                   &d->opacity, &d->divv, &d->trr, &d->trp, &d->tpp, &d->agr, &d->agt, &d->dcen, &d->ml, &d->mlip,
-                  &d->mlim, &d->mljp, &d->mljm, &d->rhs, &d->rml, &d->tbackup, &d->t_rho_gas, &d->t_e_gas};
+                  &d->mlim, &d->mljp, &d->mljm, &d->rhs, &d->sor_cw, &d->tbackup, &d->t_rho_gas, &d->t_e_gas};
   for (auto f : F) RCHK(dfield(d, f));
   if (d->p.stellar_irradiation) { RCHK(dfield(d, &d->flaring)); RCHK(dfield(d, &d->qirr)); }
   else { d->flaring = d->qirr = nullptr; }
@@ -1052,13 +1052,13 @@ extern "C" int thorin_gpu_forces(thorin_disk *d, thorin_planets *sys, double mas
 static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *capped)
 {
   const thorin_params &p = d->p;
-  hydro_sor_resid0(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor, d->s);
+  hydro_sor_resid0(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, omega, d->sor, d->s);
   KCHECK("SOR residual kernel");
   int first = 1, chunk = hint > 0 ? hint : 4;
   *capped = 0;
   for (;;) {
     if (d->timing) CUCHK(cudaEventRecord(d->ev[0], d->s));
-    hydro_sor_sweeps(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->rml, d->sor, omega, p.sor_eps,
+    hydro_sor_sweeps(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, d->sor, p.sor_eps,
                      first, chunk, p.sor_maxiters, d->s);
     KCHECK("SOR sweep kernels");
     if (d->timing) CUCHK(cudaEventRecord(d->ev[1], d->s));
@@ -1140,7 +1140,7 @@ static int energy_step(thorin_disk *d, double dt)
     }
   }
   hydro_matrix(d->g, d->rho, d->temper, d->cs, d->dcen, d->divv, d->qminus, d->qplus, d->qirr, d->ml, d->mlip, d->mlim,
-               d->mljp, d->mljm, d->rhs, d->rml, dt, d->gm1, d->ring[R_INVDXTHETA2], p.stellar_irradiation, nheat,
+               d->mljp, d->mljm, d->rhs, dt, d->gm1, d->ring[R_INVDXTHETA2], p.stellar_irradiation, nheat,
                d->heat_idx_d, d->heat_val_d, d->s);
   KCHECK("energy kernels");
   if (d->sor_first) {

@@ -112,15 +112,16 @@ void hydro_irradiation(const DevGrid &g, const double *rho, const double *cs, co
                        const double *rinf15, const double *rsup15, cudaStream_t s);
 void hydro_matrix(const DevGrid &g, const double *rho, const double *T, const double *cs, const double *dcen,
                   const double *divv, const double *qminus, const double *qplus, const double *qirr, double *ml,
-                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs, double *rml, double dt,
+                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs, double dt,
                   double gm1, const double *invdxtheta2_r, int irradiation, int nheat, const int *heat_idx,
                   const double *heat_val, cudaStream_t s);
 int sor_blocks(const DevGrid &g);
 void hydro_sor_resid0(const DevGrid &g, const double *T, const double *ml, const double *mlip, const double *mlim,
-                      const double *mljp, const double *mljm, const double *rhs, const SorCtl &c, cudaStream_t s);
+                      const double *mljp, const double *mljm, const double *rhs, double *cw, double omega,
+                      const SorCtl &c, cudaStream_t s);
 void hydro_sor_sweeps(const DevGrid &g, double *T, const double *ml, const double *mlip, const double *mlim,
-                      const double *mljp, const double *mljm, const double *rhs, const double *rml, const SorCtl &c,
-                      double omega, double eps, int first, int count, int maxiters, cudaStream_t s);
+                      const double *mljp, const double *mljm, const double *rhs, const double *cw, const SorCtl &c,
+                      double eps, int first, int count, int maxiters, cudaStream_t s);
 void hydro_energy_from_t(const DevGrid &g, const double *rho, double *T, double *enew, cudaStream_t s);
 void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, double **energy, const TransportScratch &S,
                      double dt, double omega_frame, int fast, int damp_vrad, double drin, double drout, double *temper,
