@@ -116,21 +116,30 @@ void aux_stokes(const DevGrid &g, const double *rho, const double *psize, double
 // the cell with the largest sum of squared rates, so block maxima of that
 // sum are reduced (exactly, in any order) and the step is formed once.
 
-__global__ void k_cfl_cells(DevGrid g, const double *__restrict__ vr, const double *__restrict__ vt,
-                            const double *__restrict__ cs, const double *__restrict__ pvr,
-                            const double *__restrict__ pvt, CflRings cr, int pebbles, int fast, int viscous,
-                            double *__restrict__ part)
+#define CFL_CPT 4       // cells per thread
+
+// The sums of squared rates are >= 0, so their maxima are taken on the bit
+// patterns as 64-bit integers (same order, integer pipe).
+struct OpMaxI64 { __device__ long long operator()(long long a, long long b) const { return b > a ? b : a; } };
+
+__global__ void __launch_bounds__(256) k_cfl_cells(DevGrid g, const double *__restrict__ vr,
+                                                   const double *__restrict__ vt, const double *__restrict__ cs,
+                                                   const double *__restrict__ pvr, const double *__restrict__ pvt,
+                                                   CflRings cr, int pebbles, int fast, int viscous,
+                                                   double *__restrict__ part)
 {
   const int ns = g.ns;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y + 1;                    // rings One_or_active .. Max_or_active-1
-  double gas = 0.0, peb = -1.0e30;
-  if (j < ns) {
+  const double dxrad = cr.dxrad[i], dxtheta = cr.dxtheta[i], mindx = cr.mindx[i];
+  const double invdt5 = viscous ? div_fast(g.r.nu_med[i] * 4., cr.den5[i]) : 1e-30;
+  long long gas = 0, peb = 0;
+  for (int m = 0; m < CFL_CPT; m++) {
+    const int j = (blockIdx.x * CFL_CPT + m) * blockDim.x + threadIdx.x;
+    if (j >= ns) break;
     const int l = j + i * ns, lip = l + ns;
     const int ljp = (j == ns - 1) ? i * ns : l + 1;
-    const double dxrad = cr.dxrad[i], dxtheta = cr.dxtheta[i];
     const double vres = fast ? vt[l] - cr.vmoy[i] : vt[l];
-    const double invdt1 = div_fast(cs[l], cr.mindx[i]);
+    const double invdt1 = div_fast(cs[l], mindx);
     const double invdt2 = div_fast(fabs(vr[l]), dxrad);
     const double invdt3 = div_fast(fabs(vres), dxtheta);
     double dvr = vr[lip] - vr[l], dvt = vt[ljp] - vt[l];
@@ -139,26 +148,27 @@ __global__ void k_cfl_cells(DevGrid g, const double *__restrict__ vr, const doub
     const double a = div_fast(dvr, dxrad), b = div_fast(dvt, dxtheta);
     double invdt4 = (b > a) ? b : a;
     invdt4 *= 4.0 * TH_CVNR * TH_CVNR;
-    const double invdt5 = viscous ? div_fast(g.r.nu_med[i] * 4., cr.den5[i]) : 1e-30;
-    gas = invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4 + invdt5 * invdt5;
+    const double sg = invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4 + invdt5 * invdt5;
+    const long long bg = __double_as_longlong(sg);
+    gas = bg > gas ? bg : gas;
     if (pebbles) {
       const double p1 = div_fast(fabs(pvr[l]), dxrad);
       const double vrp = fast ? pvt[l] - cr.pvtmed[i] : pvt[l];
       const double p2 = div_fast(fabs(vrp), dxtheta);
       const double p3 = div_fast(fabs(pvr[l] - vr[l]), dxrad);
       const double p4 = div_fast(fabs(pvt[l] - vt[l]), dxtheta);
-      peb = p1 * p1 + p2 * p2 + p3 * p3 + p4 * p4;
+      const long long bp = __double_as_longlong(p1 * p1 + p2 * p2 + p3 * p3 + p4 * p4);
+      peb = bp > peb ? bp : peb;
     }
   }
-  const double mg = block_reduce(gas, OpMax(), 0.0);
-  const double mp = block_reduce(peb, OpMax(), -1.0e30);
+  const long long mg = block_reduce(gas, OpMaxI64(), 0LL);
+  const long long mp = pebbles ? block_reduce(peb, OpMaxI64(), 0LL) : 0LL;
   if (threadIdx.x == 0) {
     const int b = blockIdx.x + blockIdx.y * gridDim.x;
-    part[2 * b] = mg;
-    part[2 * b + 1] = mp;
+    part[2 * b] = __longlong_as_double(mg);
+    part[2 * b + 1] = pebbles ? __longlong_as_double(mp) : -1.0e30;
   }
 }
-
 
 __global__ void __launch_bounds__(1024) k_cfl_final(DevGrid g, const double *__restrict__ part, CflRings cr, CflFinal f,
                             double *__restrict__ scal, int *__restrict__ iscal)
@@ -202,7 +212,7 @@ void aux_cfl(const DevGrid &g, const double *vr, const double *vt, const double 
 {
   if (pebbles && fast) aux_ring_means(g, vt, cr.vmoy, pvt, cr.pvtmed, 0, g.nr, s);
   else aux_ring_means(g, vt, cr.vmoy, nullptr, nullptr, 0, g.nr, s);
-  dim3 grid = grid2d(g.ns, g.nr - 1, 256);
+  dim3 grid = grid2d(g.ns, g.nr - 1, 256 * CFL_CPT);
   k_cfl_cells<<<grid, 256, 0, s>>>(g, vr, vt, cs, pvr, pvt, cr, pebbles, fast, viscous, part);
   g_thorin_launches++;
   CflFinal f = f0;
@@ -483,15 +493,18 @@ __device__ __forceinline__ void vert_quad(const double (&wq)[NV], double H, doub
   p_integstar = pis;
 }
 
-__global__ void k_forces(DevGrid g, ForceArgs a, ForceRings fr)
+#define FORCE_CPT 4     // cells per thread: one block reduction per 4*128 cells
+
+__global__ void __launch_bounds__(128) k_forces(DevGrid g, ForceArgs a, ForceRings fr)
 {
   const int ns = g.ns;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y;
   const int npl = a.npl, peb = a.pebbles;
   double acc[2 + 2 * MAXPL_DEV];
   for (int q = 0; q < 2 + 2 * npl; q++) acc[q] = 0.0;
-  if (j < ns) {
+  for (int mc = 0; mc < FORCE_CPT; mc++) {
+    const int j = (blockIdx.x * FORCE_CPT + mc) * blockDim.x + threadIdx.x;
+    if (j >= ns) break;
     const int l = j + i * ns;
     const double omegainv = g.r.OmegaInv[i], r2 = g.r.Rmed2[i];
     double Rsup_Rinf2 = g.r.Rsup[i] - g.r.Rinf[i];
@@ -552,8 +565,8 @@ __global__ void k_forces(DevGrid g, ForceArgs a, ForceRings fr)
     const double isig = div_fast(1.0, sigma);
     double tmp = integstar * isig;
     double agr = -g.r.Rmed[i] * tmp;            // 0.0 + ar
-    acc[0] = mcell * tmp * x;
-    acc[1] = mcell * tmp * y;
+    acc[0] += mcell * tmp * x;
+    acc[1] += mcell * tmp * y;
     double pagr = 0.0;
     if (peb) { const double pt = p_integstar * isig; pagr = -g.r.Rmed[i] * pt; }
     double ax = 0.0, ay = 0.0, pax = 0.0, pay = 0.0;
@@ -668,7 +681,7 @@ void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr, dou
     }
     if (pass) a.sig30 = sig; else a.sig10 = sig;
   }
-  dim3 grid = grid2d(g.ns, g.nr, 128);
+  dim3 grid = grid2d(g.ns, g.nr, 128 * FORCE_CPT);
   k_forces<<<grid, 128, 0, s>>>(g, a, fr);
   g_thorin_launches++;
   k_forces_final<<<1, 1024, 0, s>>>(a0.part, grid.x * grid.y, 2 + 2 * a0.npl, scal);

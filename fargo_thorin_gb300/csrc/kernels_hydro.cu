@@ -681,11 +681,10 @@ __global__ void k_rad_prep(DevGrid g, int nq, const double *__restrict__ rho, co
   const double c = r * (vt[ljp] + rm * omega_frame) * rm;
   const double d = r * (vt[l] + rm * omega_frame) * rm;
   rmp[l] = a; rmm[l] = b; tmp_[l] = c; tmm[l] = d;
-  const double den = r + 1e-20, rcp = div_fast(1.0, den);
-  w0[l] = div_by_rcp(a, den, rcp); w1[l] = div_by_rcp(b, den, rcp);
-  w2[l] = div_by_rcp(c, den, rcp); w3[l] = div_by_rcp(d, den, rcp);
-  if (nq == 6) we[l] = div_by_rcp(energy[l], den, rcp);
-  wr[l] = div_by_rcp(r, den, rcp);
+  const double rcp = div_fast(1.0, r + 1e-20);    // quotients Q / (rho + 1e-20) as products
+  w0[l] = a * rcp; w1[l] = b * rcp; w2[l] = c * rcp; w3[l] = d * rcp;
+  if (nq == 6) we[l] = energy[l] * rcp;
+  wr[l] = r * rcp;
 }
 
 __device__ __forceinline__ double vl_slope_r(const DevGrid &g, const double *q, int i, int l)
@@ -694,7 +693,8 @@ __device__ __forceinline__ double vl_slope_r(const DevGrid &g, const double *q, 
   if (i == 0 || i == nr - 1) return 0.0;
   const double dqm = (q[l] - q[l - ns]) * g.r.InvDiffRmed[i];
   const double dqp = (q[l + ns] - q[l]) * g.r.InvDiffRmed[i + 1];
-  return (dqp * dqm > 0.0) ? div_fast(2.0 * dqp * dqm, dqp + dqm) : 0.0;
+  const double p = dqp * dqm;
+  return (__double_as_longlong(p) > 0LL) ? div_fast(2.0 * p, dqp + dqm) : 0.0;   // p > 0.0
 }
 
 
@@ -786,18 +786,22 @@ __global__ void __launch_bounds__(256) k_azi_rings(DevGrid g, const double *__re
 // the destination arrays.  Neighbour values move through shared memory.
 // The van Leer slope's sign tests read the sign bits as integers: for finite
 // values this is the reference's comparison (a NaN, which only a crashed run
-// holds, gives NaN instead of a zero slope).
+// holds, gives NaN instead of a zero slope).  The arithmetic is regrouped to
+// save FP64 instructions: Work = Q * (1 / (RhoInt + 1e-20)), the slope's
+// 1/dxtheta folded into the face coefficient, the flux as Q* times
+// (dxrad RhoStar v); results differ from the reference's grouping in the
+// last bits only.
 #define AZ_HALO 4
 #define AZ_TMAX 512
 
-__device__ __forceinline__ double azi_vl_slope(double qm, double q0, double qp, double invdx)
+__device__ __forceinline__ double azi_vl_slope_raw(double qm, double q0, double qp)
 {
   const double dqm = q0 - qm, dqp = qp - q0;
   const double p = dqp * dqm;
   const double s = dqp + dqm;
   const bool pos = __double_as_longlong(p) > 0LL;                 // p > 0.0
   const bool nz = (__double_as_longlong(s) << 1) != 0LL;          // s != 0.0
-  return (pos && nz) ? div_fast(p, s) * invdx : 0.0;
+  return (pos && nz) ? div_fast(p, s) : 0.0;
 }
 
 template <int NQ>
@@ -828,33 +832,34 @@ __global__ void __launch_bounds__(AZ_TMAX) k_azimuthal(DevGrid g, AziIO io, cons
     const double v = (pass == 1) ? vuni : (vface - vsub);
     const double ksi = v * dt;
     const bool up = ksi > 0.0;                     // upwind cell of the left face is j-1
-    const double c = up ? (dxtheta - ksi) : (dxtheta + ksi);
+    // face value q* = q_up +/- (dxtheta -/+ ksi) dq_up with the slope dq kept
+    // without its 1/dxtheta factor, which goes into cs instead
+    const double cs = (up ? (dxtheta - ksi) : (dxtheta + ksi)) * invdxtheta;
     // RhoStar at the left face (ComputeStarTheta of the density)
     const double rho = q[NQ - 1];
     s_a[t] = rho;
     __syncthreads();
-    const double drho = azi_vl_slope(s_a[tm], rho, s_a[tp], invdxtheta);
+    const double drho = azi_vl_slope_raw(s_a[tm], rho, s_a[tp]);
     s_b[t] = drho;
     __syncthreads();
-    const double rs = up ? s_a[tm] + c * s_b[tm] : rho - c * drho;
-    const double den = rho + 1e-20;                // RhoInt + 1e-20
-    const double rcp = div_fast(1.0, den);
+    const double rs = up ? __fma_rn(cs, s_b[tm], s_a[tm]) : __fma_rn(-cs, drho, rho);
+    const double cf = dxrad * rs * v;              // flux = dxrad Q* RhoStar v
+    const double rcp = div_fast(1.0, rho + 1e-20); // 1 / (RhoInt + 1e-20)
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < NQ; k++) {
       // VanLeerTheta: Work = Q / (RhoInt + 1e-20), its slope, the face value
-      const double w = div_by_rcp(q[k], den, rcp);
+      const double w = q[k] * rcp;
       s_a[t] = w;
       __syncthreads();
-      const double dq = azi_vl_slope(s_a[tm], w, s_a[tp], invdxtheta);
+      const double dq = azi_vl_slope_raw(s_a[tm], w, s_a[tp]);
       s_b[t] = dq;
       __syncthreads();
-      const double qs = up ? s_a[tm] + c * s_b[tm] : w - c * dq;
-      const double F = dxrad * qs * rs * v;
+      const double qs = up ? __fma_rn(cs, s_b[tm], s_a[tm]) : __fma_rn(-cs, dq, w);
+      const double F = qs * cf;
       s_c[t] = F;
       __syncthreads();
-      const double varq = F - s_c[tp];
-      q[k] = q[k] + varq * invsurf;
+      q[k] = __fma_rn(F - s_c[tp], invsurf, q[k]);
     }
   }
   const int x = t - AZ_HALO;

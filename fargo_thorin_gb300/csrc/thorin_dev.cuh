@@ -138,10 +138,3 @@ __device__ __forceinline__ double div_fast(double x, double d)
   return x / d;
 }
 
-// x / d given r = 1/d: the product x r with Markstein's correction, as above.
-__device__ __forceinline__ double div_by_rcp(double x, double d, double r)
-{
-  const double q0 = x * r;
-  const double e = __fma_rn(-d, q0, x);
-  return __fma_rn(e, r, q0);
-}

@@ -83,3 +83,31 @@ def test_gpu_vs_oracle_every_dt(name):
         for f in H.GAS + (H.PEB if p.pebbles else []) + ["energy"]:
             assert H.rel_l2(d.get(H.FIELD_IDS[f])[:n], o.get(H.FIELD_IDS[f])[:n]) < 1e-11, f"{f} at DT {step}"
         assert abs(sg.x[0] - so.x[0]) < 1e-14 and abs(sg.vx[0] - so.vx[0]) < 1e-14
+
+
+@pytest.mark.parametrize("kind,nr,ns", [("disk0", 20, 1536), ("disk1", 24, 1152)])
+def test_gpu_vs_oracle_wide_rings(kind, nr, ns):
+    """Rings wider than one thread block of every kernel (several blocks per
+    ring in the force, CFL, SOR and accretion reductions; several segments
+    per ring in the azimuthal transport), against the oracle after each DT."""
+    p = workloads.params_for(kind, nr, ns)
+    d = _gpu_disk(p)
+    o = O.OracleDisk(p)
+    o.init_default()
+    init = {"dens": o.get(H.FIELD_IDS["dens"]).copy(), "temper": o.get(H.FIELD_IDS["temper"]).copy()}
+    d.init_default()
+    for x in (d, o):
+        H.start_state(x, p, init)
+    row = workloads.PLANET1 if kind == "disk1" else workloads.PLANET0
+    sg = workloads.make_planets(p, [row])
+    so = workloads.make_planets(p, [row])
+    n = nr * ns
+    for step in range(1, 3):
+        d.algogas(sg)
+        o.algogas(so)
+        assert d.stats().substeps == o.stats().substeps
+        np.testing.assert_array_equal(d.nshift(), o.nshift())
+        assert d.stats().sor_last_niter == o.stats().sor_last_niter
+        for f in H.GAS + (H.PEB if p.pebbles else []) + ["energy"]:
+            assert H.rel_l2(d.get(H.FIELD_IDS[f])[:n], o.get(H.FIELD_IDS[f])[:n]) < 1e-11, f"{f} at DT {step}"
+        assert abs(sg.x[0] - so.x[0]) < 1e-14 and abs(sg.vx[0] - so.vx[0]) < 1e-14
