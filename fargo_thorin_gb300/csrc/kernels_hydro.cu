@@ -532,6 +532,7 @@ __device__ __forceinline__ bool sor_last_block(unsigned int *ticket, unsigned nb
 }
 
 #define SOR_CPT 4        // cells of one colour per thread
+#define SOR_BX 128       // threads per SOR block
 
 __global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__restrict__ T,
                                                     const double *__restrict__ ml, const double *__restrict__ mlip,
@@ -585,34 +586,40 @@ __global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict_
 {
   if (*((volatile int *)c.done)) return;
   const int ns = g.ns, half = ns >> 1;
-  const int i = blockIdx.y + 1;
   const int col = pass - 1;
-  const int par = (col == 0) ? ((i - 1) & 1) : (i & 1);
-  const size_t pbase = (size_t)((i << 1) + col) * half;
+  const int cpt = SOR_BX * SOR_CPT;                // cells of one colour per tile
+  const int tpr = (half + cpt - 1) / cpt;          // tiles per ring
+  const int ntiles = tpr * (g.nr - 2);
   double a = 0.0;
   int ch = 0;
+  // grid-stride over (ring, tile): the grid is one wave of resident blocks
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int i = tile / tpr + 1, kx = tile - (i - 1) * tpr;
+    const int par = (col == 0) ? ((i - 1) & 1) : (i & 1);
+    const size_t pbase = (size_t)((i << 1) + col) * half;
 #pragma unroll
-  for (int m = 0; m < SOR_CPT; m++) {
-    const int k = blockIdx.x * blockDim.x * SOR_CPT + m * blockDim.x + threadIdx.x;
-    if (k < half) {
-      const int j = 2 * k + par;
-      const int l = j + i * ns;
-      const int ljp = (j == ns - 1) ? i * ns : l + 1;
-      const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
-      const size_t q = pbase + k;
-      const double resid = sor_resid_at(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm, q);
-      a += fabs(resid);
-      const double delta = resid * cw[q];
-      const double tn = T[l] - delta;
-      T[l] = tn;
-      // delta > tn * SORPRECISION, from the sign of the exact difference
-      ch += (__double_as_longlong(__fma_rn(-tn, TH_SORPRECISION, delta)) > 0LL) ? 1 : 0;
+    for (int m = 0; m < SOR_CPT; m++) {
+      const int k = kx * cpt + m * blockDim.x + threadIdx.x;
+      if (k < half) {
+        const int j = 2 * k + par;
+        const int l = j + i * ns;
+        const int ljp = (j == ns - 1) ? i * ns : l + 1;
+        const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+        const size_t q = pbase + k;
+        const double resid = sor_resid_at(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm, q);
+        a += fabs(resid);
+        const double delta = resid * cw[q];
+        const double tn = T[l] - delta;
+        T[l] = tn;
+        // delta > tn * SORPRECISION, from the sign of the exact difference
+        ch += (__double_as_longlong(__fma_rn(-tn, TH_SORPRECISION, delta)) > 0LL) ? 1 : 0;
+      }
     }
   }
   a = block_reduce(a, OpAdd(), 0.0);
   const int chs = block_reduce(ch, OpAddI(), 0);
-  const unsigned nb = gridDim.x * gridDim.y;
-  const int b = blockIdx.x + blockIdx.y * gridDim.x;
+  const unsigned nb = gridDim.x;
+  const int b = blockIdx.x;
   const int slot = col * nb + b;
   if (threadIdx.x == 0) {
     c.part[slot] = a;
@@ -1008,12 +1015,17 @@ void hydro_matrix(const DevGrid &g, const double *rho, const double *T, const do
   g_thorin_launches++;
 }
 
-static const int SOR_BX = 128;
 
 static dim3 sor_grid_pass(const DevGrid &g)
 {
+  static int occ = 0;                              // resident k_sor_pass blocks per multiprocessor
+  if (occ == 0) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sor_pass, SOR_BX, 0) != cudaSuccess || occ < 1) occ = 1;
+  }
   const int half = g.ns / 2;
-  return dim3((half + SOR_BX * SOR_CPT - 1) / (SOR_BX * SOR_CPT), g.nr - 2);
+  const long long ntiles = (long long)((half + SOR_BX * SOR_CPT - 1) / (SOR_BX * SOR_CPT)) * (g.nr - 2);
+  const long long wave = (long long)g.nsm * occ;
+  return dim3((unsigned)(ntiles < wave ? ntiles : wave));
 }
 
 static dim3 sor_grid_resid(const DevGrid &g)

@@ -272,6 +272,9 @@ static void build_grid(thorin_disk *d)
 {
   DevGrid &g = d->g;
   g.nr = d->nr; g.ns = d->ns;
+  int dev = 0;
+  g.nsm = 1;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&g.nsm, cudaDevAttrMultiProcessorCount, dev);
   DevRings &r = g.r;
   double **R = d->ring;
   r.Rinf = R[R_RINF]; r.Rsup = R[R_RSUP]; r.Rmed = R[R_RMED]; r.Surf = R[R_SURF]; r.InvRmed = R[R_INVRMED];

@@ -49,6 +49,7 @@ struct DevRings {
 
 struct DevGrid {
   int nr, ns;
+  int nsm;                               // multiprocessors of the disk's GPU
   DevRings r;
   DevConst k;
 };
