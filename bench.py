@@ -212,14 +212,26 @@ def run_gpu(args):
         cells_pass = (NR - 2) * NS / 2
         bytes_pass = SOR_BYTES_PER_CELL_SWEEP * cells_pass
         achieved = bytes_pass / (sor_avg_ms / 1e3) / 1e9
-        traffic = None
-        tf = os.path.join(ROOT, "profiles", "sor_pass_traffic.json")
+        prof = {}
+        tf = os.path.join(ROOT, "profiles", "k_sor_pass_disk1_1024x3072.json")
         if os.path.exists(tf):
             try:
                 with open(tf) as f:
-                    traffic = json.load(f).get("bytes_per_launch")
+                    prof = json.load(f)
             except Exception:
-                traffic = None
+                prof = {}
+        traffic = prof.get("bytes_per_launch")
+        # The pass is bound by the FP64 pipe: its FP64 instructions per launch
+        # (ncu count) over the live launch time, against this GPU's FMA rate.
+        fp64 = None
+        gf = C.c_double()
+        if _lib.load().thorin_selftest_fp64_peak(C.byref(gf)) == 0 and prof.get("fp64_inst_per_launch"):
+            inst = float(prof["fp64_inst_per_launch"])
+            ach = inst / (sor_avg_ms / 1e3) / 1e9
+            fp64 = {"bound": "fp64 pipe", "kernel": "k_sor_pass", "achieved": ach, "peak": gf.value / 2.0,
+                    "unit": "G FP64 inst/s", "frac": ach / (gf.value / 2.0), "inst_per_launch": inst,
+                    "peak_source": "FMA loop on this GPU at run time (thorin_selftest_fp64_peak), one FMA per "
+                                   "instruction"}
         cpu = None
         if ws == 1 and not args.no_cpu_baseline:
             cpu = cpu_baseline(d, sys_)
@@ -238,6 +250,7 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "kernel": "k_sor_pass", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": bytes_pass, "avg_launch_ms": sor_avg_ms},
+            "fp64_roofline": fp64,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

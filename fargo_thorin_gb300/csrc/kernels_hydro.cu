@@ -561,7 +561,7 @@ __global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__r
   if (sor_last_block(c.ticket, nb)) {
     __threadfence();
     double s = 0.0;
-    for (unsigned k = threadIdx.x; k < nb; k += blockDim.x) s += ((volatile double *)c.part)[k];
+    for (unsigned k = threadIdx.x; k < nb; k += blockDim.x) s += __ldcg(c.part + k);   // L2, past L1
     s = block_reduce(s, OpAdd(), 0.0);
     if (threadIdx.x == 0) {
       *c.normres0 = s;
@@ -626,25 +626,48 @@ __global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict_
     c.ipart[slot] = chs;
   }
   if (pass != 2) return;
-  if (sor_last_block(c.ticket, nb)) {
-    __threadfence();
-    double s = 0.0;
-    int cs = 0;
-    for (unsigned q = threadIdx.x; q < 2 * nb; q += blockDim.x) {
-      s += ((volatile double *)c.part)[q];
-      cs += ((volatile int *)c.ipart)[q];
-    }
-    s = block_reduce(s, OpAdd(), 0.0);
-    cs = block_reduce(cs, OpAddI(), 0);
-    if (threadIdx.x == 0) {
-      const double r0 = *c.normres0;
-      *c.normres = s;
-      *c.changed = cs;
-      *c.niter = n;
-      if (s < eps * r0 || s < TH_SORMIN || cs == 0) *c.done = 1;
-      else if (n >= maxiters) *c.done = 2;
-      *c.ticket = 0u;
-    }
+  // Completion in two levels so that no block sums thousands of partials
+  // while the GPU idles: the last block of each group of SOR_GROUP blocks
+  // sums the group's partials of both colours, the last group to finish sums
+  // the group sums and applies the exit tests.  The order of every sum is
+  // fixed, so the result does not depend on timing.
+  const unsigned grp = b / SOR_GROUP, g0 = grp * SOR_GROUP;
+  const unsigned gsize = (nb - g0 < SOR_GROUP) ? nb - g0 : SOR_GROUP;
+  if (!sor_last_block(c.gticket + grp * SOR_TSTRIDE, gsize)) return;
+  __threadfence();
+  double s = 0.0;
+  int cs = 0;
+  for (unsigned q = threadIdx.x; q < 2 * gsize; q += blockDim.x) {
+    const unsigned cc = q / gsize, bb = g0 + (q - cc * gsize);
+    s += __ldcg(c.part + cc * nb + bb);
+    cs += __ldcg(c.ipart + cc * nb + bb);
+  }
+  s = block_reduce(s, OpAdd(), 0.0);
+  cs = block_reduce(cs, OpAddI(), 0);
+  if (threadIdx.x == 0) {
+    c.gpart[grp] = s;
+    c.gipart[grp] = cs;
+    c.gticket[grp * SOR_TSTRIDE] = 0u;
+  }
+  const unsigned ng = (nb + SOR_GROUP - 1) / SOR_GROUP;
+  if (!sor_last_block(c.ticket, ng)) return;
+  __threadfence();
+  s = 0.0;
+  cs = 0;
+  for (unsigned q = threadIdx.x; q < ng; q += blockDim.x) {
+    s += __ldcg(c.gpart + q);
+    cs += __ldcg(c.gipart + q);
+  }
+  s = block_reduce(s, OpAdd(), 0.0);
+  cs = block_reduce(cs, OpAddI(), 0);
+  if (threadIdx.x == 0) {
+    const double r0 = *c.normres0;
+    *c.normres = s;
+    *c.changed = cs;
+    *c.niter = n;
+    if (s < eps * r0 || s < TH_SORMIN || cs == 0) *c.done = 1;
+    else if (n >= maxiters) *c.done = 2;
+    *c.ticket = 0u;
   }
 }
 

@@ -383,6 +383,10 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   d->sor.niter = ip + 1;
   d->sor.changed = ip + 2;
   d->sor.ticket = d->ticket;
+  const int ng = (sb + SOR_GROUP - 1) / SOR_GROUP;
+  RCHK(dalloc(d, (void **)&d->sor.gpart, (size_t)ng * sizeof(double)));
+  RCHK(dalloc(d, (void **)&d->sor.gipart, (size_t)ng * sizeof(int)));
+  RCHK(dalloc(d, (void **)&d->sor.gticket, (size_t)ng * SOR_TSTRIDE * sizeof(unsigned int)));
   fill_rings(d);
   // damping rings (rows with Rmed outside [DRin, DRout])
   std::vector<int> rings;

@@ -18,9 +18,15 @@ enum {
 enum { IS_NSUB = 0, IS_SOR_DONE, IS_SOR_NITER, IS_SOR_CHANGED, IS_CRASH, IS_COUNT };
 
 // Red-black SOR control block (device pointers).
+#define SOR_GROUP 64      // blocks per completion group of a SOR pass
+#define SOR_TSTRIDE 32    // group tickets 128 bytes apart
+
 struct SorCtl {
   double *part;           // [2][nblocks] partial |resid| sums
   int *ipart;             // [2][nblocks] partial changed counts
+  double *gpart;          // [ngroups] group sums of both colours
+  int *gipart;            // [ngroups]
+  unsigned int *gticket;  // [ngroups * SOR_TSTRIDE] group tickets
   unsigned int *ticket;
   int *done;              // 1 converged, 2 iteration cap; later sweeps are no-ops
   int *niter;

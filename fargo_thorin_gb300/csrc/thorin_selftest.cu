@@ -63,3 +63,52 @@ extern "C" int thorin_selftest_division(long long n, unsigned long long seed, do
   *max_ulp = host[1];
   return THORIN_OK;
 }
+
+// FP64 fused multiply-add throughput of the current GPU: eight independent
+// FMA chains per thread, one wave of blocks per multiprocessor times eight.
+__global__ void __launch_bounds__(256) k_selftest_dfma(double *__restrict__ out, int iters, double a, double b)
+{
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1.0, x2 = x0 + 2.0, x3 = x0 + 3.0;
+  double x4 = x0 + 4.0, x5 = x0 + 5.0, x6 = x0 + 6.0, x7 = x0 + 7.0;
+  for (int k = 0; k < iters; k++) {
+    x0 = __fma_rn(x0, a, b); x1 = __fma_rn(x1, a, b); x2 = __fma_rn(x2, a, b); x3 = __fma_rn(x3, a, b);
+    x4 = __fma_rn(x4, a, b); x5 = __fma_rn(x5, a, b); x6 = __fma_rn(x6, a, b); x7 = __fma_rn(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+extern "C" int thorin_selftest_fp64_peak(double *gflops)
+{
+  if (!gflops) {
+    g_last_error = "selftest_fp64_peak: output pointer required";
+    return THORIN_ERR_ARG;
+  }
+  int dev = 0, nsm = 1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int nb = nsm * 8, nt = 256, iters = 4096;
+  double *out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaMalloc((void **)&out, sizeof(double) * nb * nt);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) {
+    k_selftest_dfma<<<nb, nt>>>(out, 64, 1.0000001, 1e-9);          // warm-up
+    cudaEventRecord(e0);
+    k_selftest_dfma<<<nb, nt>>>(out, iters, 1.0000001, 1e-9);
+    cudaEventRecord(e1);
+    e = cudaEventSynchronize(e1);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (out) cudaFree(out);
+  if (e != cudaSuccess || ms <= 0.f) {
+    g_last_error = std::string("selftest_fp64_peak: ") + cudaGetErrorString(e);
+    return THORIN_ERR_CUDA;
+  }
+  *gflops = 2.0 * 8.0 * iters * (double)nb * nt / (ms * 1e6);
+  return THORIN_OK;
+}

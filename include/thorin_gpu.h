@@ -299,6 +299,12 @@ int thorin_integrals_static(const double *rho, const double *vrad, const double 
 int thorin_selftest_division(long long n, unsigned long long seed, double max_exponent,
                              unsigned long long *mismatches, unsigned long long *max_ulp);
 
+/* FP64 fused multiply-add throughput of the current GPU in GFLOP/s (two
+ * flops per FMA), measured with a short kernel of independent FMA chains:
+ * the FP64-pipe ceiling for the roofline of the kernels.  No counterpart in
+ * the reference. */
+int thorin_selftest_fp64_peak(double *gflops);
+
 /* Last CUDA error string (thread-local, for diagnostics). */
 const char *thorin_gpu_last_error(void);
 
