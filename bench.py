@@ -9,8 +9,10 @@ residual of 1e-8), FP64, synthetic data built by the library's own set-up.
 A step is one DT of AlgoGas (all its CFL substeps, each one full hydro
 substep with SOR); cell-updates = nrad * nsec * substeps.  ``value`` is timed
 on the device with CUDA events on the library's stream with the state
-resident in HBM; ``e2e`` times the same steps through the C ABI with the
-state uploaded from pinned host buffers and downloaded back every step.
+resident in HBM; ``e2e`` restores the state from before those steps and
+replays the same DTs (same substeps and SOR sweeps, checked) through the C
+ABI with the state uploaded from pinned host buffers and downloaded back
+every step.
 
 --impl reference times the CPU restatement of the reference algorithm (the
 oracle, OpenMP over all host cores) on the same disk, one short DT per step.
@@ -106,6 +108,7 @@ class ClockSampler:
 
 
 STATE_FIELDS = [0, 1, 2, 3, 4, 5, 6, 7]      # dens, vrad, vtheta, energy, pebble dens/vrad/vtheta/size
+SNAPSHOT_FIELDS = STATE_FIELDS + [8, 9, 11]   # + temperature, sound speed, Stokes number
 
 
 def make_disk(nr=NR, ns=NS):
@@ -153,6 +156,12 @@ def run_gpu(args):
     for _ in range(args.warmup):
         d.algogas(sys_)
     stream = torch.cuda.ExternalStream(d.stream())
+    # snapshot of the whole disk state, so that the end-to-end phase below
+    # repeats exactly the DTs of the device-timed phase
+    snap = {f: d.get(f) for f in SNAPSHOT_FIELDS}
+    snap_sor = d.sor_state()
+    snap_time = d.stats().physical_time
+    snap_sys = sys_.copy()
     d.set_timing(True)
     launches0 = d.stats().kernel_launches
     clocks = ClockSampler(local)
@@ -185,11 +194,18 @@ def run_gpu(args):
     total_updates = NR * NS * subs_all
     value = total_updates / (ms_max / 1e3)
 
-    # end to end through the C ABI with host buffers (pinned)
+    # end to end through the C ABI with host buffers (pinned), from the same
+    # starting state: the same DTs, substeps and SOR sweeps as above
+    for f, v in snap.items():
+        d.upload(f, v)
+    d.set_sor_state(*snap_sor[:3])
+    d.set_time(snap_time)
+    sys_ = snap_sys
+    sweeps_e0 = d.stats().sor_sweeps
     n = (NR + 1) * NS
     host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True) for f in STATE_FIELDS}
     for f in STATE_FIELDS:
-        host[f].numpy()[:] = d.get(f)
+        host[f].numpy()[:] = snap[f]
     L, h = d.L, d.h
     ptr = {f: C.cast(host[f].data_ptr(), C.POINTER(C.c_double)) for f in STATE_FIELDS}
     barrier()
@@ -200,10 +216,11 @@ def run_gpu(args):
             _lib.check(L.thorin_gpu_upload(h, f, ptr[f]), "upload")
         d.algogas(sys_)
         esubs += d.stats().substeps
-        for f in STATE_FIELDS[:7]:
+        for f in STATE_FIELDS:
             _lib.check(L.thorin_gpu_download(h, f, ptr[f]), "download")
     barrier()
     e_s = time.perf_counter() - t0
+    esweeps = d.stats().sor_sweeps - sweeps_e0
     e_max, esubs_all = reduce_over_ranks([e_s, esubs], ["max", "sum"], "cuda")
     e2e_value = NR * NS * esubs_all / e_max
 
@@ -245,7 +262,8 @@ def run_gpu(args):
                        "parallelism": "replicas" if ws > 1 else "single disk"},
             "clocks": clk,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n * 8,
-                    "d2h_bytes_per_step": 7 * n * 8},
+                    "d2h_bytes_per_step": 8 * n * 8, "substeps": esubs, "sor_sweeps": esweeps,
+                    "same_work_as_value": bool(esubs == subs and esweeps == sweeps)},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": "k_sor_pass", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
