@@ -8,7 +8,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-from .params import ThorinParams, ThorinPlanets, ThorinStats
+from .params import ThorinParams, ThorinPlanets, ThorinStats, ThorinTorque
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libthorin_gpu.so")
@@ -43,6 +43,9 @@ SIGNATURES = {
     "thorin_selftest_division": (C.c_int, [C.c_longlong, C.c_ulonglong, C.c_double, C.POINTER(C.c_ulonglong),
                                            C.POINTER(C.c_ulonglong)]),
     "thorin_selftest_fp64_peak": (C.c_int, [_D]),
+    "thorin_gpu_request_torques": (C.c_int, [_P]),
+    "thorin_gpu_init_pebbles": (C.c_int, [_P]),
+    "thorin_gpu_get_torques": (C.c_int, [_P, C.POINTER(ThorinTorque), C.c_int, C.POINTER(C.c_int)]),
     "thorin_gpu_last_error": (C.c_char_p, []),
     "thorin_planet_from_elements": (C.c_int, [C.POINTER(ThorinPlanets), C.c_int] + [C.c_float] * 9),
 }

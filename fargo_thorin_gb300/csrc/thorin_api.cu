@@ -131,6 +131,8 @@ struct thorin_disk {
   double PhysicalTime, PhysicalTimeInitial, OmegaFrame, MassTaper;
   int cfl_first;
   int sor_first, Niterlast, Niterbest;
+  int torque_pending = 0, ntorque = 0;
+  thorin_torque torques[THORIN_MAXPLANETS];
   double omega, domega, omegabest;
   double heatsrc[THORIN_MAXPLANETS];
   int heatsrc_index[THORIN_MAXPLANETS], heatsrc_max;
@@ -588,6 +590,75 @@ static int eos_refresh(thorin_disk *d)
 // ---------------------------------------------------------------------------
 // Default initial state, built on the host like the reference does once
 // (InitEuler, SourceEuler.c:133-175; main.c:168-170).
+// EtaPressureSupport + InitPebblesViaFlux (Pebbles.c:80-275): the pebble disk
+// in a coagulation-drift equilibrium with the given gas state (host copies
+// of Sigma, v_r, v_theta and c_s in the PolarGrid layout).
+static int init_pebbles_host(thorin_disk *d, const std::vector<double> &rho, const std::vector<double> &vr,
+                             const std::vector<double> &vt, const std::vector<double> &cs)
+{
+  const thorin_params &p = d->p;
+  const int nr = d->nr, ns = d->ns;
+  const size_t n = (size_t)(nr + 1) * ns;
+  std::vector<double> etacc(n, 0.0), etafc(n, 0.0), pd(n, 0.0), pvr(n, 0.0), pvt(n, 0.0), ps(n, 0.0), tau(n, 0.0);
+  for (int i = 0; i < nr; i++) {
+    const double vtcorr = d->Rmed[i] * d->OmegaFrame, vkinv = sqrt(d->Rmed[i]);
+    for (int j = 0; j < ns; j++) {
+      const int l = j + i * ns, ljp = (j == ns - 1) ? i * ns : l + 1;
+      const double vtcc = 0.5 * (vt[l] + vt[ljp]);
+      etacc[l] = 1.0 - (vtcc + vtcorr) * vkinv;
+    }
+  }
+  for (int i = 1; i < nr; i++)
+    for (int j = 0; j < ns; j++) { const int l = j + i * ns; etafc[l] = 0.5 * (etacc[l] + etacc[l - ns]); }
+  for (int j = 0; j < ns; j++) etafc[j] = etafc[j + ns];
+  const double pebbleflux = p.pebble_flux * FLUX2CU, Ndf = 0.5, pb = p.pebble_bulk_dens / RHO2CGS;
+  for (int i = 0; i < nr; i++) {
+    double rho1 = 0, vr1 = 0, etafc1 = 0, etacc1 = 0, cs1 = 0;
+    for (int j = 0; j < ns; j++) {
+      const int l = j + i * ns;
+      rho1 += rho[l]; vr1 += vr[l]; etafc1 += etafc[l]; etacc1 += etacc[l]; cs1 += cs[l];
+    }
+    rho1 /= (double)ns; vr1 /= (double)ns; etafc1 /= (double)ns; etacc1 /= (double)ns; cs1 /= (double)ns;
+    double tau1 = sqrt(3.0) * p.pebble_coagulation * pebbleflux / (32.0 * H_PI * pow(d->Rmed[i], -1.5) * rho1);
+    tau1 = sqrt(tau1) / (d->Rmed[i] * etacc1);
+    double psize1 = fabs(tau1) * sqrt(p.adiabind) * rho1 / (2.0 * pb);
+    const double taudf = p.fragment_threshold * sqrt(d->Rmed[i]) / (2.0 * etacc1 * (1.0 - Ndf));
+    const double adf = fabs(taudf) * sqrt(p.adiabind) * rho1 / (2.0 * pb);
+    const double taufrag = p.fragment_factor / (3.0 * p.fragment_alpha) * pow(p.fragment_threshold / cs1, 2);
+    const double afrag = fabs(taufrag) * sqrt(p.adiabind) * rho1 / (2.0 * pb);
+    if ((psize1 < adf) && (psize1 < afrag)) {
+    } else if ((taudf > 0.0) && (adf < psize1) && (adf < afrag)) {
+      tau1 = taudf; psize1 = adf;
+    } else {
+      tau1 = taufrag; psize1 = afrag;
+    }
+    const double vtcorr = d->Rmed[i] * d->OmegaFrame, vkepl = pow(d->Rmed[i], -0.5);
+    const double fac = 1.0 / (tau1 * tau1 + 1.0);
+    double etaterm = etafc1 * vkepl;
+    const double pvr1 = -2.0 * tau1 * fac * (etaterm - 0.5 / tau1 * vr1);
+    etaterm = etacc1 * vkepl;
+    const double pvrtemp = -2.0 * tau1 * fac * (etaterm - 0.5 / tau1 * vr1);
+    double pvt1 = -fac * (etaterm - 0.5 * tau1 * vr1);
+    pvt1 += (vkepl - vtcorr);
+    double pdens1 = pebbleflux / (2.0 * H_PI * d->Rmed[i] * fabs(pvrtemp));
+    if (pdens1 / rho1 > p.pebble_to_gas_max) pdens1 = rho1 * p.pebble_to_gas_max;
+    for (int j = 0; j < ns; j++) {
+      const int l = j + i * ns;
+      ps[l] = psize1; tau[l] = tau1; pd[l] = pdens1; pvr[l] = pvr1; pvt[l] = pvt1;
+    }
+    d->PebDensInit[i] = pdens1;
+    d->PebVradInit[i] = pvr1;
+    d->PebVthetaInit[i] = pvt1 + d->Rmed[i] * d->OmegaFrame;
+  }
+  CUCHK(cudaMemcpyAsync(d->pdens, pd.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaMemcpyAsync(d->pvrad, pvr.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaMemcpyAsync(d->pvtheta, pvt.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaMemcpyAsync(d->psize, ps.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaMemcpyAsync(d->tau, tau.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  return THORIN_OK;
+}
+
 extern "C" int thorin_gpu_init_default(thorin_disk *d)
 {
   const thorin_params &p = d->p;
@@ -645,66 +716,7 @@ extern "C" int thorin_gpu_init_default(thorin_disk *d)
   CUCHK(cudaMemcpyAsync(d->vrad, vr.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
   CUCHK(cudaMemcpyAsync(d->vtheta, vt.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
   CUCHK(cudaStreamSynchronize(d->s));
-  if (p.pebbles) {
-    // EtaPressureSupport + InitPebblesViaFlux (Pebbles.c:80-275)
-    std::vector<double> etacc(n, 0.0), etafc(n, 0.0), pd(n, 0.0), pvr(n, 0.0), pvt(n, 0.0), ps(n, 0.0), tau(n, 0.0);
-    for (int i = 0; i < nr; i++) {
-      const double vtcorr = d->Rmed[i] * d->OmegaFrame, vkinv = sqrt(d->Rmed[i]);
-      for (int j = 0; j < ns; j++) {
-        const int l = j + i * ns, ljp = (j == ns - 1) ? i * ns : l + 1;
-        const double vtcc = 0.5 * (vt[l] + vt[ljp]);
-        etacc[l] = 1.0 - (vtcc + vtcorr) * vkinv;
-      }
-    }
-    for (int i = 1; i < nr; i++)
-      for (int j = 0; j < ns; j++) { const int l = j + i * ns; etafc[l] = 0.5 * (etacc[l] + etacc[l - ns]); }
-    for (int j = 0; j < ns; j++) etafc[j] = etafc[j + ns];
-    const double pebbleflux = p.pebble_flux * FLUX2CU, Ndf = 0.5, pb = p.pebble_bulk_dens / RHO2CGS;
-    for (int i = 0; i < nr; i++) {
-      double rho1 = 0, vr1 = 0, etafc1 = 0, etacc1 = 0, cs1 = 0;
-      for (int j = 0; j < ns; j++) {
-        const int l = j + i * ns;
-        rho1 += rho[l]; vr1 += vr[l]; etafc1 += etafc[l]; etacc1 += etacc[l]; cs1 += cs[l];
-      }
-      rho1 /= (double)ns; vr1 /= (double)ns; etafc1 /= (double)ns; etacc1 /= (double)ns; cs1 /= (double)ns;
-      double tau1 = sqrt(3.0) * p.pebble_coagulation * pebbleflux / (32.0 * H_PI * pow(d->Rmed[i], -1.5) * rho1);
-      tau1 = sqrt(tau1) / (d->Rmed[i] * etacc1);
-      double psize1 = fabs(tau1) * sqrt(p.adiabind) * rho1 / (2.0 * pb);
-      const double taudf = p.fragment_threshold * sqrt(d->Rmed[i]) / (2.0 * etacc1 * (1.0 - Ndf));
-      const double adf = fabs(taudf) * sqrt(p.adiabind) * rho1 / (2.0 * pb);
-      const double taufrag = p.fragment_factor / (3.0 * p.fragment_alpha) * pow(p.fragment_threshold / cs1, 2);
-      const double afrag = fabs(taufrag) * sqrt(p.adiabind) * rho1 / (2.0 * pb);
-      if ((psize1 < adf) && (psize1 < afrag)) {
-      } else if ((taudf > 0.0) && (adf < psize1) && (adf < afrag)) {
-        tau1 = taudf; psize1 = adf;
-      } else {
-        tau1 = taufrag; psize1 = afrag;
-      }
-      const double vtcorr = d->Rmed[i] * d->OmegaFrame, vkepl = pow(d->Rmed[i], -0.5);
-      const double fac = 1.0 / (tau1 * tau1 + 1.0);
-      double etaterm = etafc1 * vkepl;
-      const double pvr1 = -2.0 * tau1 * fac * (etaterm - 0.5 / tau1 * vr1);
-      etaterm = etacc1 * vkepl;
-      const double pvrtemp = -2.0 * tau1 * fac * (etaterm - 0.5 / tau1 * vr1);
-      double pvt1 = -fac * (etaterm - 0.5 * tau1 * vr1);
-      pvt1 += (vkepl - vtcorr);
-      double pdens1 = pebbleflux / (2.0 * H_PI * d->Rmed[i] * fabs(pvrtemp));
-      if (pdens1 / rho1 > p.pebble_to_gas_max) pdens1 = rho1 * p.pebble_to_gas_max;
-      for (int j = 0; j < ns; j++) {
-        const int l = j + i * ns;
-        ps[l] = psize1; tau[l] = tau1; pd[l] = pdens1; pvr[l] = pvr1; pvt[l] = pvt1;
-      }
-      d->PebDensInit[i] = pdens1;
-      d->PebVradInit[i] = pvr1;
-      d->PebVthetaInit[i] = pvt1 + d->Rmed[i] * d->OmegaFrame;
-    }
-    CUCHK(cudaMemcpyAsync(d->pdens, pd.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
-    CUCHK(cudaMemcpyAsync(d->pvrad, pvr.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
-    CUCHK(cudaMemcpyAsync(d->pvtheta, pvt.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
-    CUCHK(cudaMemcpyAsync(d->psize, ps.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
-    CUCHK(cudaMemcpyAsync(d->tau, tau.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
-    CUCHK(cudaStreamSynchronize(d->s));
-  }
+  if (p.pebbles) RCHK(init_pebbles_host(d, rho, vr, vt, cs));
   RCHK(upload_all_rings(d));
   RCHK(eos_refresh(d));
   KCHECK("initial EOS kernels");
@@ -712,7 +724,7 @@ extern "C" int thorin_gpu_init_default(thorin_disk *d)
   return THORIN_OK;
 }
 
-// Ring means of a device field, summed in order, to the host.
+// Ring means of a device field (warp tree sums) to the host.
 static int ring_means_host(thorin_disk *d, const double *f, std::vector<double> &out)
 {
   aux_ring_mean(d->g, f, d->ring[R_VMOY], d->s);
@@ -746,6 +758,27 @@ extern "C" int thorin_gpu_refresh(thorin_disk *d, int flags)
     RCHK(ring_means_host(d, d->pvtheta, m));
     for (int i = 0; i < nr; i++) d->PebVthetaInit[i] = m[i] + d->Rmed[i] * d->OmegaFrame;
   }
+  RCHK(upload_all_rings(d));
+  RCHK(eos_refresh(d));
+  CUCHK(cudaStreamSynchronize(d->s));
+  return THORIN_OK;
+}
+
+// EquilPebbleDisk on the current gas state, for runs that load the gas from
+// files (Init.c:144-148): after the gas fields are uploaded.
+extern "C" int thorin_gpu_init_pebbles(thorin_disk *d)
+{
+  if (!d) return THORIN_ERR_ARG;
+  if (!d->p.pebbles) return THORIN_OK;
+  const size_t n = (size_t)(d->nr + 1) * d->ns;
+  RCHK(eos_refresh(d));
+  std::vector<double> rho(n), vr(n), vt(n), cs(n);
+  CUCHK(cudaMemcpyAsync(rho.data(), d->rho, n * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaMemcpyAsync(vr.data(), d->vrad, n * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaMemcpyAsync(vt.data(), d->vtheta, n * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaMemcpyAsync(cs.data(), d->cs, n * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  RCHK(init_pebbles_host(d, rho, vr, vt, cs));
   RCHK(upload_all_rings(d));
   RCHK(eos_refresh(d));
   CUCHK(cudaStreamSynchronize(d->s));
@@ -1040,6 +1073,17 @@ extern "C" int thorin_gpu_forces(thorin_disk *d, thorin_planets *sys, double mas
       if (ring_cs) ring_cs[k] = d->csmean_h[i];
     }
   }
+  // UpdateLog (Force.c:27-70) needs Sigma's ring means either side of each planet
+  int tq_ring[MAXPL_DEV];
+  const int torques = d->torque_pending;
+  if (torques) {
+    for (int k = 0; k < npl; k++) {
+      const double r = sqrt(sys->x[k] * sys->x[k] + sys->y[k] * sys->y[k]);
+      tq_ring[k] = (int)global_ifrac(d, r);
+      aux_ring_mean_at(d->g, d->rho, tq_ring[k], d->scal + SC_TORQUE + 2 * k, d->s);
+      if (tq_ring[k] + 1 <= d->nr) aux_ring_mean_at(d->g, d->rho, tq_ring[k] + 1, d->scal + SC_TORQUE + 2 * k + 1, d->s);
+    }
+  }
   CUCHK(cudaMemcpyAsync(d->scal_h, d->scal, 128 * sizeof(double), cudaMemcpyDeviceToHost, d->s));
   CUCHK(cudaStreamSynchronize(d->s));
   for (int k = 0; k < npl; k++) {
@@ -1048,9 +1092,50 @@ extern "C" int thorin_gpu_forces(thorin_disk *d, thorin_planets *sys, double mas
     const double r = sqrt(sys->x[k] * sys->x[k] + sys->y[k] * sys->y[k]);
     if (ring_rho && r >= d->Rinf[0] && r <= d->Rsup[d->nr - 1]) ring_rho[k] = d->scal_h[SC_PLANET_A + 2 * MAXPL_DEV + k];
   }
+  if (torques) {
+    for (int k = 0; k < npl; k++) {
+      const double x = sys->x[k], y = sys->y[k], ax = sys->ax[k], ay = sys->ay[k], m = sys->mass[k];
+      const double r2 = x * x + y * y, r = sqrt(r2);
+      const double ifrac = global_ifrac(d, r), frac = ifrac - floor(ifrac);
+      const int ii = tq_ring[k];
+      const double rho_hi = (ii + 1 <= d->nr) ? d->scal_h[SC_TORQUE + 2 * k + 1] : 0.0;
+      const double cs_hi = (ii + 1 <= d->nr) ? d->csmean_h[ii + 1] : 0.0;
+      const double rhopl = d->scal_h[SC_TORQUE + 2 * k] * (1.0 - frac) + rho_hi * frac;
+      const double cspl = d->csmean_h[ii] * (1.0 - frac) + cs_hi * frac;
+      const double omega = pow(r, -1.5);
+      const double h = cspl / (omega * r) * (1.0 / sqrt(p.adiabind));
+      double norm = m * omega * r2 / h;
+      norm *= norm;
+      norm *= rhopl;
+      const double tq = x * ay - y * ax;
+      thorin_torque &t = d->torques[k];
+      t.time = d->PhysicalTime;
+      t.torque = tq;
+      t.torque_norm = tq * m * p.adiabind / norm;
+      t.x = x; t.y = y; t.ax = ax; t.ay = ay;
+    }
+    d->ntorque = npl;
+    d->torque_pending = 0;
+  }
   // IndirectTerm of the disk (the planets' part is only added to the gas)
   indirect[0] = d->scal_h[SC_INDX];
   indirect[1] = d->scal_h[SC_INDY];
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_request_torques(thorin_disk *d)
+{
+  if (!d) return THORIN_ERR_ARG;
+  d->torque_pending = 1;
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_get_torques(thorin_disk *d, thorin_torque *out, int max, int *n)
+{
+  if (!d || !n || (max > 0 && !out)) return THORIN_ERR_ARG;
+  const int m = d->ntorque < max ? d->ntorque : max;
+  for (int k = 0; k < m; k++) out[k] = d->torques[k];
+  *n = d->ntorque;
   return THORIN_OK;
 }
 
@@ -1273,6 +1358,7 @@ extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
   int nsub = 0, status = THORIN_OK;
   if (!sys || sys->nb > MAXPL_DEV) { g_last_error = "planetary system missing or too large"; return THORIN_ERR_ARG; }
   if (d->timing) CUCHK(cudaEventRecord(d->ev[2], d->s));
+  d->torque_pending = 1;                       // DumpTorqueNow: log the first substep's torques
   while (dtemp < 0.999999999 * DT) {
     d->MassTaper = d->PhysicalTime / (p.mass_taper * 2.0 * H_MPI);
     d->MassTaper = (d->MassTaper > 1.0 ? 1.0 : pow(sin(d->MassTaper * H_MPI / 2.0), 2.0));

@@ -13,7 +13,8 @@ struct DevPlanet {
 enum {
   SC_NEWDT = 0, SC_INVDTPEB, SC_DTSTELLAR, SC_INDX, SC_INDY, SC_ACC_DM, SC_ACC_DPX, SC_ACC_DPY, SC_RINGRHO,
   SC_MASS, SC_MOM, SC_ENER, SC_PMASS, SC_PMOM, SC_NORMRES0, SC_NORMRES,
-  SC_PLANET_A = 32            // 2 per planet: ax, ay
+  SC_PLANET_A = 32,           // 2 per planet: ax, ay (then the ring means of Sigma for DampingTW04)
+  SC_TORQUE = 56              // 2 per planet: ring means of Sigma either side of the planet (UpdateLog)
 };
 enum { IS_NSUB = 0, IS_SOR_DONE, IS_SOR_NITER, IS_SOR_CHANGED, IS_CRASH, IS_COUNT };
 

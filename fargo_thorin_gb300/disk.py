@@ -79,6 +79,18 @@ class GpuDisk:
         _lib.check(self.L.thorin_gpu_get_stats(self.h, C.byref(s)), "stats")
         return s
 
+    def init_pebbles(self):
+        """EquilPebbleDisk on the gas state now on the device."""
+        _lib.check(self.L.thorin_gpu_init_pebbles(self.h), "init_pebbles")
+
+    def torques(self):
+        """Torque-log records (one per planet) of the last algogas call."""
+        from .params import ThorinTorque
+        out = (ThorinTorque * 120)()
+        n = C.c_int()
+        _lib.check(self.L.thorin_gpu_get_torques(self.h, out, 120, C.byref(n)), "get_torques")
+        return [out[k] for k in range(min(n.value, 120))]
+
     def sor_state(self):
         om, dom, nl, cal = C.c_double(), C.c_double(), C.c_int(), C.c_int()
         _lib.check(self.L.thorin_gpu_get_sor_state(self.h, C.byref(om), C.byref(dom), C.byref(nl), C.byref(cal)),

@@ -185,6 +185,15 @@ class ThorinPlanets(C.Structure):
         return {k: list(getattr(self, k)[:n]) for k in ("mass", "x", "y", "z", "vx", "vy", "vz")}
 
 
+class ThorinTorque(C.Structure):
+    """One line of tqwk<k>.dat (UpdateLog, src_main/Force.c:27-70)."""
+    _fields_ = [("time", C.c_double), ("torque", C.c_double), ("torque_norm", C.c_double), ("x", C.c_double),
+                ("y", C.c_double), ("ax", C.c_double), ("ay", C.c_double)]
+
+    def row(self):
+        return (self.time, self.torque, self.torque_norm, self.x, self.y, self.ax, self.ay)
+
+
 class ThorinStats(C.Structure):
     _fields_ = [("substeps", C.c_int), ("sor_calls", C.c_int), ("sor_sweeps", C.c_longlong),
                 ("sor_last_niter", C.c_int), ("sor_omega", C.c_double), ("crashed", C.c_int),

@@ -156,6 +156,15 @@ typedef struct thorin_planets {
   int    feel_disk[THORIN_MAXPLANETS];
 } thorin_planets;
 
+/* One line of the torque log tqwk<k>.dat (UpdateLog, src_main/Force.c:27-70):
+ * the disk's torque on planet k at the first substep of a DT. */
+typedef struct thorin_torque {
+  double time;                   /* PhysicalTime at the start of the DT          */
+  double torque;                 /* x a_y - y a_x                                */
+  double torque_norm;            /* torque * m * gamma / (m Omega r^2 / h)^2 / Sigma */
+  double x, y, ax, ay;           /* planet position and disk acceleration        */
+} thorin_torque;
+
 /* Run statistics of the last call. */
 typedef struct thorin_stats {
   int    substeps;               /* hydro substeps done in the last DT          */
@@ -289,6 +298,19 @@ int thorin_gpu_get_stream(thorin_disk *d, void **stream);
 int thorin_integrals_static(const double *rho, const double *vrad, const double *vtheta, const double *energy,
                             const double *surf, const double *rinf, const double *rsup, const double *rmed,
                             int nrad, int nsec, double omega_frame, double *out, void *stream);
+
+/* EquilPebbleDisk (Pebbles.c:54-60) on the gas state now on the device:
+ * for runs that upload their gas from files before the pebbles are set up
+ * (Init.c:144-148).  No-op without pebbles. */
+int thorin_gpu_init_pebbles(thorin_disk *d);
+
+/* Torque log of the last thorin_gpu_algogas call (one record per planet,
+ * taken at its first substep like UpdateLog, which AdvanceSystemFromDisk
+ * calls once per DT, Pframeforce.c:523-526).  Phase-API drivers call
+ * thorin_gpu_request_torques before the thorin_gpu_forces call whose
+ * accelerations should be logged.  *n receives the number of records. */
+int thorin_gpu_request_torques(thorin_disk *d);
+int thorin_gpu_get_torques(thorin_disk *d, thorin_torque *out, int max, int *n);
 
 /* Self-test of the kernels' division routine (reciprocal estimate, one
  * Newton-Raphson step, Markstein correction) against IEEE division on the

@@ -45,6 +45,16 @@ def test_gpu_vs_reference_golden(name):
         st = d.stats()
         assert st.substeps == g["substeps"][step - 1]
         assert st.sor_last_niter == g["sor_niter"][step - 1], f"SOR iterations at DT {step}"
+        # torque log (tqwk0.dat) of the DT's first substep: disk acceleration on the planet
+        t, ref = d.torques()[0], tq[step - 1]
+        amag = np.hypot(ref[5], ref[6])
+        assert abs(t.time - ref[0]) <= 1e-12 * max(1.0, abs(ref[0]))
+        assert np.hypot(t.ax - ref[5], t.ay - ref[6]) < 1e-9 * amag, f"planet acceleration at DT {step}"
+        assert abs(t.torque - ref[1]) < 1e-9 * amag * np.hypot(ref[3], ref[4])
+        if np.isnan(ref[2]):
+            assert np.isnan(t.torque_norm)
+        elif ref[1] != 0.0:
+            assert abs(t.torque_norm / t.torque / (ref[2] / ref[1]) - 1) < 1e-10
         m, mom, e, _, _ = d.integrals()
         assert abs(m / g["mass"][step - 1] - 1) < 1e-12
         assert abs(mom / g["momentum"][step - 1] - 1) < 1e-12
