@@ -244,8 +244,8 @@ void aux_evaporate(const DevGrid &g, const double *T, double *pdens, double facc
 // Damping boundaries (DampingBoundary, SideEuler.c:368-419, and DampPebbles,
 // SideEuler.c:423-456).  Only rings inside the damping zones are launched.
 __global__ void k_damp_gas(DevGrid g, double *__restrict__ vrad, double *__restrict__ rho, double *__restrict__ vtheta,
-                           double *__restrict__ energy, const int *__restrict__ rings, double dt, double omega_frame,
-                           int damp_init, int energy_eq)
+                           double *__restrict__ energy, const int *__restrict__ rings, const double *__restrict__ vr0r,
+                           double dt, double omega_frame, int damp_init, int damp_flux, int energy_eq)
 {
   const int ns = g.ns;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -253,7 +253,8 @@ __global__ void k_damp_gas(DevGrid g, double *__restrict__ vrad, double *__restr
   const int i = rings[blockIdx.y];
   const int l = j + i * ns;
   const double lambda = g.r.WaveKiller[i] * dt;
-  vrad[l] = (vrad[l] + lambda * 0.0) / (1.0 + lambda);
+  const double vrad0 = damp_flux ? vr0r[i] : 0.0;
+  vrad[l] = (vrad[l] + lambda * vrad0) / (1.0 + lambda);
   if (damp_init) {
     const double rho0 = g.r.SigmaMed[i], e0 = g.r.EnergyMed[i];
     const double vt0 = g.r.VthetaMed[i] - g.r.Rmed[i] * omega_frame;
@@ -261,14 +262,40 @@ __global__ void k_damp_gas(DevGrid g, double *__restrict__ vrad, double *__restr
     vtheta[l] = (vtheta[l] + lambda * vt0) / (1.0 + lambda);
     if (energy_eq) energy[l] = (energy[l] + lambda * e0) / (1.0 + lambda);
   }
+  if (damp_flux) rho[l] = (rho[l] + lambda * g.r.SigmaMed[i]) / (1.0 + lambda);
 }
 
 void aux_damp_gas(const DevGrid &g, double *vrad, double *rho, double *vtheta, double *energy, const int *rings,
-                  int nrings, double dt, double omega_frame, int damp_init, int energy_eq, cudaStream_t s)
+                  int nrings, const double *vr0r, double dt, double omega_frame, int damp_init, int damp_flux,
+                  int energy_eq, cudaStream_t s)
 {
   if (nrings <= 0) return;
-  k_damp_gas<<<grid2d(g.ns, nrings, BX), BX, 0, s>>>(g, vrad, rho, vtheta, energy, rings, dt, omega_frame, damp_init,
-                                                     energy_eq);
+  k_damp_gas<<<grid2d(g.ns, nrings, BX), BX, 0, s>>>(g, vrad, rho, vtheta, energy, rings, vr0r, dt, omega_frame,
+                                                     damp_init, damp_flux, energy_eq);
+  g_thorin_launches++;
+}
+
+// Isothermal equation of state (ComputeSoundSpeed, ComputePressureField,
+// ComputeTemperatureField without the energy equation, SourceEuler.c:
+// 715-792): c_s is the ring profile AspectRatio(r) sqrt(G/r) r^f, P = Sigma
+// c_s^2, T = mu P / (Sigma R).  Each part is done only when asked for: the
+// reference forms P at the start of a substep and T from that P and the
+// transported Sigma at its end.
+__global__ void k_iso_eos(DevGrid g, const double *__restrict__ rho, const double *__restrict__ csr,
+                          double *__restrict__ cs, double *__restrict__ press, double *__restrict__ temper, int set_cs,
+                          int set_press, int set_temper)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  if (set_cs) cs[l] = csr[i];
+  if (set_press) press[l] = rho[l] * cs[l] * cs[l];
+  if (set_temper) temper[l] = (1.0 * press[l]) * div_fast(1.0, rho[l] * 1.0);
+}
+
+void aux_iso_eos(const DevGrid &g, const double *rho, const double *csr, double *cs, double *press, double *temper,
+                 int set_cs, int set_press, int set_temper, cudaStream_t s)
+{
+  k_iso_eos<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, csr, cs, press, temper, set_cs, set_press, set_temper);
   g_thorin_launches++;
 }
 

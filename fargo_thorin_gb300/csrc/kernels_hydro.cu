@@ -19,9 +19,11 @@ static const int BX = 128;
 
 // ---------------------------------------------------------------------------
 // SubStep1 velocity predictor (SourceEuler.c:319-407), pressure from the
-// energy (ComputePressureField, SourceEuler.c:740-762).
+// energy (ComputePressureField, SourceEuler.c:740-762) or, in isothermal
+// runs, the pressure field formed at the start of the substep.
 __global__ void k_substep1(DevGrid g, const double *__restrict__ rho, const double *__restrict__ vrad,
                            const double *__restrict__ vtheta, const double *__restrict__ energy,
+                           const double *__restrict__ press,
                            const double *__restrict__ agr, const double *__restrict__ agt,
                            const double *__restrict__ dragr, const double *__restrict__ dragt,
                            double *__restrict__ vradint, double *__restrict__ vthetaint,
@@ -33,10 +35,10 @@ __global__ void k_substep1(DevGrid g, const double *__restrict__ rho, const doub
   CELL_LOOP_2D
   const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
   const int ljp = (j == ns - 1) ? i * ns : l + 1;
-  const double pl = gm1 * energy[l];
+  const double pl = press ? press[l] : gm1 * energy[l];
   if (i >= 1) {
     const int lim = l - ns;
-    const double plim = gm1 * energy[lim];
+    const double plim = press ? press[lim] : gm1 * energy[lim];
     double gradp = div_fast((pl - plim) * 2.0, rho[l] + rho[lim]) * g.r.InvDiffRmed[i];
     double vt2 = vtheta[l] + vtheta[ljp] + vtheta[lim] + vtheta[ljp - ns];
     vt2 = vt2 / 4.0 + g.r.Rinf[i] * omega_frame;
@@ -56,7 +58,7 @@ __global__ void k_substep1(DevGrid g, const double *__restrict__ rho, const doub
   }
   {
     const double invdxtheta = invdxtheta_r[i];
-    const double pljm = gm1 * energy[ljm];
+    const double pljm = press ? press[ljm] : gm1 * energy[ljm];
     double gradp = div_fast((pl - pljm) * 2.0, rho[l] + rho[ljm]) * invdxtheta;
     double tmp = -gradp + 0.5 * (agt[l] + agt[ljm]);
     double v = vtheta[l] + dt * tmp;
@@ -953,12 +955,12 @@ __global__ void k_velocities(DevGrid g, const double *__restrict__ rho, const do
 // ---------------------------------------------------------------------------
 // Launch wrappers
 void hydro_substep1(const DevGrid &g, const double *rho, const double *vrad, const double *vtheta,
-                    const double *energy, const double *agr, const double *agt, const double *dragr, const double *dragt,
-                    double *vradint, double *vthetaint, double *gaccr, double *gacct, double dt, double omega_frame,
-                    double gm1, int pebbles, int back_reaction, const double *supp_torque, const double *invdxtheta_r,
-                    cudaStream_t s)
+                    const double *energy, const double *press, const double *agr, const double *agt,
+                    const double *dragr, const double *dragt, double *vradint, double *vthetaint, double *gaccr,
+                    double *gacct, double dt, double omega_frame, double gm1, int pebbles, int back_reaction,
+                    const double *supp_torque, const double *invdxtheta_r, cudaStream_t s)
 {
-  k_substep1<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, vrad, vtheta, energy, agr, agt, dragr, dragt, vradint,
+  k_substep1<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, vrad, vtheta, energy, press, agr, agt, dragr, dragt, vradint,
                                                    vthetaint, gaccr, gacct, dt, omega_frame, gm1, pebbles,
                                                    back_reaction, supp_torque, invdxtheta_r);
   g_thorin_launches++;

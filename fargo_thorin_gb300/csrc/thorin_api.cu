@@ -93,7 +93,7 @@ enum {  // ring arrays kept on the device
   R_WAVEKILLER, R_RMED15, R_RINF15, R_RSUP15, R_COSTAB, R_SINTAB, R_SIGMAMED, R_ENERGYMED, R_VTHETAMED, R_PEBDENS0,
   R_PEBVRAD0, R_PEBVTHETA0, R_CSMEAN, R_TEMPMEAN, R_NUMED, R_NUINF, R_INVDXTHETA, R_INVDXTHETA2, R_SUPPTORQUE,
   R_DELTAR2, R_CFLDXRAD, R_CFLDXTHETA, R_CFLMINDX, R_CFLDEN5, R_VMOY, R_PVTMED, R_HAVR, R_SIGAVR, R_ISTAVR, R_PHAVR,
-  R_PISTAVR, R_VMED, R_TAUAVR, R_VTEMP, R_COUNT
+  R_PISTAVR, R_VMED, R_TAUAVR, R_VTEMP, R_DAMPVR0, R_CSISO, R_COUNT
 };
 
 struct thorin_disk {
@@ -108,6 +108,7 @@ struct thorin_disk {
   double *rho, *vrad, *vtheta, *energy, *vrad_new, *vtheta_new, *energy_new, *vrad_int, *vtheta_int, *energy_int;
   double *cs, *temper, *qplus, *qminus, *opacity, *divv, *trr, *trp, *tpp, *agr, *agt, *pagr, *pagt, *dcen;
   double *ml, *mlip, *mlim, *mljp, *mljm, *rhs, *sor_cw, *tbackup, *flaring, *qirr;   // sor_cw = omega / ml
+  double *press = nullptr;   // pressure field of isothermal runs (formed at the start of each substep)
   double *pdens, *pvrad, *pvtheta, *psize, *tau, *paccr, *pacct, *gaccr, *gacct, *dragr, *dragt, *macc;
   double *t_rho_gas, *t_e_gas, *t_rho_peb;
   TransportScratch ts;
@@ -267,6 +268,11 @@ static int upload_all_rings(thorin_disk *d)
   RCHK(upload_ring(d, R_SIGMAMED, d->SigmaMed)); RCHK(upload_ring(d, R_ENERGYMED, d->EnergyMed));
   RCHK(upload_ring(d, R_VTHETAMED, d->VthetaMed)); RCHK(upload_ring(d, R_PEBDENS0, d->PebDensInit));
   RCHK(upload_ring(d, R_PEBVRAD0, d->PebVradInit)); RCHK(upload_ring(d, R_PEBVTHETA0, d->PebVthetaInit));
+  // DampingBoundary's v_r target with DampTowards GASFLUX (SideEuler.c:395-398)
+  std::vector<double> vr0(n1, 0.0);
+  if (p.damp_flux)
+    for (int i = 0; i < nr; i++) vr0[i] = -p.gasflux / (2.0 * H_PI * d->Rinf[i] * d->SigmaInf[i]);
+  RCHK(upload_ring(d, R_DAMPVR0, vr0));
   return THORIN_OK;
 }
 
@@ -304,15 +310,12 @@ static int check_supported(const thorin_params &p)
 {
   const char *bad = nullptr;
   if (p.nrad < 4 || p.nsec < 4 || (p.nsec & 1)) bad = "nrad, nsec >= 4 and nsec even (red-black SOR)";
-  else if (!p.energy_eq) bad = "isothermal runs (EnergyEquation NO)";
   else if (p.open_inner || p.open_outer || p.non_reflecting || p.outer_source_mass) bad = "open/non-reflecting boundaries";
-  else if (p.damp_flux || p.damp_init) bad = "DampTowards INIT/GASFLUX";
   else if (p.parametric_cooling) bad = "parametric cooling";
   else if (p.accretion_rate > 1e-10) bad = "gas accretion onto planets";
   else if (p.prescribed_accretion) bad = "ParametricAccretion";
   else if (p.aerodynamic_drag) bad = "AerodynamicDrag";
   else if (p.sloppy_cfl) bad = "SloppyCFL";
-  else if (p.omega_frame != 0.0) bad = "rotating frame";
   if (bad) {
     g_last_error = std::string("unsupported option: ") + bad;
     return THORIN_ERR_ARG;
@@ -341,6 +344,7 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
                   &d->opacity, &d->divv, &d->trr, &d->trp, &d->tpp, &d->agr, &d->agt, &d->dcen, &d->ml, &d->mlip,
                   &d->mlim, &d->mljp, &d->mljm, &d->rhs, &d->sor_cw, &d->tbackup, &d->t_rho_gas, &d->t_e_gas};
   for (auto f : F) RCHK(dfield(d, f));
+  if (!d->p.energy_eq) RCHK(dfield(d, &d->press));
   if (d->p.stellar_irradiation) { RCHK(dfield(d, &d->flaring)); RCHK(dfield(d, &d->qirr)); }
   else { d->flaring = d->qirr = nullptr; }
   if (d->p.pebbles) {
@@ -577,9 +581,40 @@ extern "C" int thorin_gpu_get_stats(thorin_disk *d, thorin_stats *s)
 
 // EOS refresh of the state, ring-mean sound speed (and temperature), and the
 // viscosity per ring; the ring means are mirrored to the host.
+// AspectRatio (Viscosity.c:56-71) at the current time.
+static double aspect_ratio_host(const thorin_disk *d, double rad)
+{
+  const thorin_params &p = d->p;
+  double ar = p.aspect_ratio;
+  double rmin = p.transition_radius - p.transition_width * p.aspect_ratio;
+  double rmax = p.transition_radius + p.transition_width * p.aspect_ratio;
+  const double scale = 1.0 + (d->PhysicalTime - d->PhysicalTimeInitial) * p.lambda_doubling;
+  rmin *= scale;
+  rmax *= scale;
+  if (rad < rmin) ar *= p.transition_ratio;
+  if ((rad >= rmin) && (rad <= rmax)) ar *= exp((rmax - rad) / (rmax - rmin) * log(p.transition_ratio));
+  return ar;
+}
+
+// Isothermal sound speed of ring i (ComputeSoundSpeed, SourceEuler.c:729-731).
+static double cs_iso_host(const thorin_disk *d, int i)
+{
+  const double r = d->Rmed[i];
+  return aspect_ratio_host(d, r) * sqrt(1.0 * 1.0 / r) * pow(r, d->p.flaring_index);
+}
+
+// ComputeSoundSpeed, ComputePressureField, ComputeTemperatureField and the
+// ring means that depend on them (Init.c:131-133).
 static int eos_refresh(thorin_disk *d)
 {
-  hydro_eos(d->g, d->rho, d->energy, d->temper, d->cs, d->gm1, d->gg1, d->s);
+  if (d->p.energy_eq) {
+    hydro_eos(d->g, d->rho, d->energy, d->temper, d->cs, d->gm1, d->gg1, d->s);
+  } else {
+    std::vector<double> c(d->nr + 2, 0.0);
+    for (int i = 0; i < d->nr; i++) c[i] = cs_iso_host(d, i);
+    RCHK(upload_ring(d, R_CSISO, c));
+    aux_iso_eos(d->g, d->rho, d->ring[R_CSISO], d->cs, d->press, d->temper, 1, 1, 1, d->s);
+  }
   aux_ring_mean(d->g, d->cs, d->ring[R_CSMEAN], d->s);
   if (d->p.alpha_flock) aux_ring_mean(d->g, d->temper, d->ring[R_TEMPMEAN], d->s);
   aux_viscosity_rings(d->g, d->vp, d->s);
@@ -685,9 +720,10 @@ extern "C" int thorin_gpu_init_default(thorin_disk *d)
   std::vector<double> csm(nr + 2, 0.0);
   for (int i = 0; i < nr; i++) {
     double sacc = 0.0;
+    const double csi = p.energy_eq ? 0.0 : cs_iso_host(d, i);
     for (int j = 0; j < ns; j++) {
       const int l = j + i * ns;
-      cs[l] = sqrt(p.adiabind * (p.adiabind - 1.0) * fabs(e[l]) / rho[l]);
+      cs[l] = p.energy_eq ? sqrt(p.adiabind * (p.adiabind - 1.0) * fabs(e[l]) / rho[l]) : csi;
       sacc += cs[l];
     }
     csm[i] = sacc / (double)ns;
@@ -706,11 +742,26 @@ extern "C" int thorin_gpu_init_default(thorin_disk *d)
       vt[l] = omega * r * sqrt(1.0 - csl * csl * r / p.adiabind);
       vt[l] -= d->OmegaFrame * r;
       vr[l] = p.imposed_disk_drift * p.sigma0 / d->SigmaInf[i] / ri;
-      if (p.viscosity_alpha) vr[l] -= 3.0 * viscosity / r * (-p.sigma_slope + 2.0 * p.flaring_index + 1.0);
-      else vr[l] -= 3.0 * viscosity / r * (-p.sigma_slope + .5);
+      if (p.damp_flux) {                   // steady inflow of GASFLUX (Pframeforce.c:735-740)
+        const double rhoinf = (i == 0) ? d->SigmaMed[i] - 0.5 * (d->SigmaMed[i + 1] - d->SigmaMed[i])
+                                       : 0.5 * (d->SigmaMed[i - 1] + d->SigmaMed[i]);
+        vr[l] -= p.gasflux / (2.0 * H_PI * ri * rhoinf);
+      } else if (p.viscosity_alpha) {
+        vr[l] -= 3.0 * viscosity / r * (-p.sigma_slope + 2.0 * p.flaring_index + 1.0);
+      } else {
+        vr[l] -= 3.0 * viscosity / r * (-p.sigma_slope + .5);
+      }
     }
   }
-  for (int j = 0; j < ns; j++) vr[j] = vr[j + ns * nr] = 0.0;
+  if (!p.damp_flux)
+    for (int j = 0; j < ns; j++) vr[j] = vr[j + ns * nr] = 0.0;
+  if (p.damp_init)                         // FillVtheta (Theo.c:132-151)
+    for (int i = 0; i < nr; i++) {
+      double moy = 0.0;
+      const double vtcorr = d->Rmed[i] * d->OmegaFrame;
+      for (int j = 0; j < ns; j++) moy += vt[j + i * ns] + vtcorr;
+      d->VthetaMed[i] = moy / (double)ns;
+    }
   CUCHK(cudaMemcpyAsync(d->rho, rho.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
   CUCHK(cudaMemcpyAsync(d->energy, e.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
   CUCHK(cudaMemcpyAsync(d->vrad, vr.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
@@ -746,8 +797,14 @@ extern "C" int thorin_gpu_refresh(thorin_disk *d, int flags)
     for (int i = 1; i < nr; i++)
       d->SigmaInf[i] = (d->SigmaMed[i - 1] * (d->Rmed[i] - d->Rinf[i]) + d->SigmaMed[i] * (d->Rinf[i] - d->Rmed[i - 1])) /
                        (d->Rmed[i] - d->Rmed[i - 1]);
-    RCHK(ring_means_host(d, d->energy, m));                 // RefillEnergy, Theo.c:82-100
-    for (int i = 0; i < nr; i++) d->EnergyMed[i] = m[i];
+    if (p.energy_eq) {
+      RCHK(ring_means_host(d, d->energy, m));               // RefillEnergy, Theo.c:82-100
+      for (int i = 0; i < nr; i++) d->EnergyMed[i] = m[i];
+    }
+    if (p.damp_init) {
+      RCHK(ring_means_host(d, d->vtheta, m));               // FillVtheta, Theo.c:132-151
+      for (int i = 0; i < nr; i++) d->VthetaMed[i] = m[i] + d->Rmed[i] * d->OmegaFrame;
+    }
   }
   if ((flags & THORIN_REFILL_PEBBLES) && p.pebbles) {       // BckpFieldsForBC, Pebbles.c:208-232
     std::vector<double> m;
@@ -1274,11 +1331,15 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
 {
   const thorin_params &p = d->p;
   const int damp = p.damping;
-  // ApplyBoundaryCondition, DetectCrash (SourceEuler.c:271-289)
-  if (damp) aux_damp_gas(d->g, d->vrad, d->rho, d->vtheta, d->energy, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, 0,
-                         p.energy_eq, d->s);
+  auto boundary = [&]() {                // ApplyBoundaryCondition -> DampingBoundary (SideEuler.c:368-419)
+    if (damp) aux_damp_gas(d->g, d->vrad, d->rho, d->vtheta, d->energy, d->damp_rings_d, d->ndamp, d->ring[R_DAMPVR0],
+                           dt, d->OmegaFrame, p.damp_init, p.damp_flux, p.energy_eq, d->s);
+  };
+  // ApplyBoundaryCondition, DetectCrash, ComputePressureField (SourceEuler.c:271-292)
+  boundary();
   CUCHK(cudaMemsetAsync(d->iscal + IS_CRASH, 0, sizeof(int), d->s));
   aux_crash(d->g, p.pebbles ? d->pdens : d->energy, d->iscal + IS_CRASH, d->s);
+  if (!p.energy_eq) aux_iso_eos(d->g, d->rho, nullptr, d->cs, d->press, d->temper, 0, 1, 0, d->s);
   // SourceTermsPebbles (Pebbles.c:550-613)
   if (p.pebbles) {
     aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, d->s);
@@ -1286,7 +1347,7 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
                        d->pacct, d->dragr, d->dragt, d->OmegaFrame, p.back_reaction, d->s);
   }
   // SubStep1 with viscous terms (SourceEuler.c:319-415)
-  hydro_substep1(d->g, d->rho, d->vrad, d->vtheta, d->energy, d->agr, d->agt, d->dragr, d->dragt, d->vrad_int,
+  hydro_substep1(d->g, d->rho, d->vrad, d->vtheta, d->energy, p.energy_eq ? nullptr : d->press, d->agr, d->agt, d->dragr, d->dragt, d->vrad_int,
                  d->vtheta_int, d->gaccr, d->gacct, dt, d->OmegaFrame, d->gm1, p.pebbles, p.back_reaction,
                  d->ring[R_SUPPTORQUE], d->ring[R_INVDXTHETA], d->s);
   hydro_stress(d->g, d->vrad_int, d->vtheta_int, d->rho, d->divv, d->trr, d->tpp, d->trp, d->invdphi, d->s);
@@ -1301,8 +1362,7 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
                  p.energy_eq, d->ring[R_INVDXTHETA], d->s);
   std::swap(d->vrad, d->vrad_new);
   std::swap(d->vtheta, d->vtheta_new);
-  if (damp) aux_damp_gas(d->g, d->vrad, d->rho, d->vtheta, d->energy, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, 0,
-                         p.energy_eq, d->s);
+  boundary();
   int status = THORIN_OK;
   if (p.energy_eq) {
     int s = energy_step(d, dt);
@@ -1312,6 +1372,13 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
   // Transport, ApplyBoundaryCondition, ComputeTemperatureField, ComputeSoundSpeed
   transport_fluid(d, &d->rho, d->vrad, d->vtheta, p.energy_eq ? &d->energy : nullptr, &d->t_rho_gas, dt, 1);
   CUCHK(cudaMemcpyAsync(d->nshift_h.data(), d->nshift, d->nr * sizeof(int), cudaMemcpyDeviceToHost, d->s));
+  if (damp && !p.damp_vrad) {
+    // damping towards INIT / GASFLUX changes Sigma (and e): the boundary
+    // call, then ComputeTemperatureField and ComputeSoundSpeed
+    boundary();
+    if (p.energy_eq) hydro_eos(d->g, d->rho, d->energy, d->temper, d->cs, d->gm1, d->gg1, d->s);
+  }
+  if (!p.energy_eq) aux_iso_eos(d->g, d->rho, nullptr, d->cs, d->press, d->temper, 0, 0, 1, d->s);
   aux_ring_mean(d->g, d->cs, d->ring[R_CSMEAN], d->s);
   if (p.alpha_flock) aux_ring_mean(d->g, d->temper, d->ring[R_TEMPMEAN], d->s);
   aux_viscosity_rings(d->g, d->vp, d->s);

@@ -93,7 +93,7 @@ extern long long g_thorin_launches;
 
 // kernels_hydro.cu
 void hydro_substep1(const DevGrid &g, const double *rho, const double *vrad, const double *vtheta,
-                    const double *energy, const double *agr, const double *agt, const double *dragr, const double *dragt,
+                    const double *energy, const double *press, const double *agr, const double *agt, const double *dragr, const double *dragt,
                     double *vradint, double *vthetaint, double *gaccr, double *gacct, double dt, double omega_frame,
                     double gm1, int pebbles, int back_reaction, const double *supp_torque, const double *invdxtheta_r,
                     cudaStream_t s);
@@ -146,7 +146,10 @@ void aux_cfl(const DevGrid &g, const double *vr, const double *vt, const double 
              int *iscal, cudaStream_t s);
 void aux_evaporate(const DevGrid &g, const double *T, double *pdens, double facc, cudaStream_t s);
 void aux_damp_gas(const DevGrid &g, double *vrad, double *rho, double *vtheta, double *energy, const int *rings,
-                  int nrings, double dt, double omega_frame, int damp_init, int energy_eq, cudaStream_t s);
+                  int nrings, const double *vr0r, double dt, double omega_frame, int damp_init, int damp_flux,
+                  int energy_eq, cudaStream_t s);
+void aux_iso_eos(const DevGrid &g, const double *rho, const double *csr, double *cs, double *press, double *temper,
+                 int set_cs, int set_press, int set_temper, cudaStream_t s);
 void aux_damp_peb(const DevGrid &g, double *pd, double *pvr, double *pvt, const int *rings, int nrings, double dt,
                   double omega_frame, cudaStream_t s);
 void aux_crash(const DevGrid &g, const double *f, int *flag, cudaStream_t s);

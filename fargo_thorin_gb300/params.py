@@ -303,8 +303,6 @@ def check_supported(p: ThorinParams) -> None:
     bad = []
     if p.open_inner or p.open_outer or p.non_reflecting or p.outer_source_mass:
         bad.append("open/non-reflecting/outer-source boundaries")
-    if p.damp_flux:
-        bad.append("DampTowards GASFLUX")
     if p.parametric_cooling:
         bad.append("parametric cooling (CoolingTime > 0)")
     if p.accretion_rate > 1e-10:
@@ -315,8 +313,6 @@ def check_supported(p: ThorinParams) -> None:
         bad.append("AerodynamicDrag")
     if p.sloppy_cfl:
         bad.append("SloppyCFL (-c)")
-    if not p.energy_eq:
-        bad.append("isothermal runs (EnergyEquation NO)")
     if bad:
         raise NotImplementedError("unsupported options: " + ", ".join(bad))
 

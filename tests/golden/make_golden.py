@@ -42,6 +42,12 @@ CASES = {
     "disk1_32x96": ("disk1", 32, 96, 3, 1, "", True),
     "disk0_128x384_200": ("disk0", 128, 384, 200, 100, "", False),
     "disk1_64x192_40": ("disk1", 64, 192, 40, 20, "", False),
+    # in.par options beyond the two measured set-ups
+    "iso_24x72": ("disk0", 24, 72, 6, 2, "EnergyEquation NO\nWriteTemperature YES\n", True),
+    "iso_peb_32x96": ("disk1", 32, 96, 6, 2, "EnergyEquation NO\nWriteTemperature YES\n", True),
+    "dampinit_24x72": ("disk0", 24, 72, 6, 2, "DampTowards INIT\n", True),
+    "gasflux_24x72": ("disk0", 24, 72, 6, 2, "DampTowards GASFLUX\nGasFlux 1e-8\n", True),
+    "frame_24x72": ("disk0", 24, 72, 6, 2, "OmegaFrame 1.0\n", True),
 }
 GAS = ["dens", "vrad", "vtheta", "temper"]
 PEB = ["pebbledens", "pebblevrad", "pebblevtheta"]

@@ -33,7 +33,8 @@ def start_state(disk, params, init_fields, seed=0):
     st = workloads.perturbed_state(params, init_fields, seed=seed)
     disk.set(FIELD_IDS["dens"], st["dens"])
     disk.set(FIELD_IDS["vrad"], st["vrad"])
-    disk.set(FIELD_IDS["energy"], st["energy"])
+    if params.energy_eq:                            # isothermal runs do not read TemperInfile (Init.c:96)
+        disk.set(FIELD_IDS["energy"], st["energy"])
     if params.pebbles:
         disk.set(FIELD_IDS["pebbledens"], st["pebdens"])
         disk.set(FIELD_IDS["pebblesize"], st["pebsize"])

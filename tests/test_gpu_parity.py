@@ -13,7 +13,8 @@ import oracle as O
 from fargo_thorin_gb300 import workloads
 
 pytestmark = pytest.mark.gpu
-CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40"]
+CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "iso_24x72", "iso_peb_32x96",
+         "dampinit_24x72", "gasflux_24x72", "frame_24x72"]
 TOL = 1e-10
 
 
@@ -44,7 +45,8 @@ def test_gpu_vs_reference_golden(name):
         d.algogas(sys_)
         st = d.stats()
         assert st.substeps == g["substeps"][step - 1]
-        assert st.sor_last_niter == g["sor_niter"][step - 1], f"SOR iterations at DT {step}"
+        if len(g["sor_niter"]):                     # no SOR in isothermal runs
+            assert st.sor_last_niter == g["sor_niter"][step - 1], f"SOR iterations at DT {step}"
         # torque log (tqwk0.dat) of the DT's first substep: disk acceleration on the planet
         t, ref = d.torques()[0], tq[step - 1]
         amag = np.hypot(ref[5], ref[6])
@@ -69,7 +71,8 @@ def test_gpu_vs_reference_golden(name):
                     assert H.rel_l2(a.mean(axis=1), g[f"out{k}_{f}_ringmean"]) < TOL, f"{f} ring means"
 
 
-@pytest.mark.parametrize("name", ["disk0_24x72", "disk1_32x96", "disk1_64x192_40"])
+@pytest.mark.parametrize("name", ["disk0_24x72", "disk1_32x96", "disk1_64x192_40", "iso_peb_32x96", "dampinit_24x72",
+                                  "gasflux_24x72", "frame_24x72"])
 def test_gpu_vs_oracle_every_dt(name):
     """GPU and oracle run the same host N-body code, so they share the planet
     trajectory; compared after every DT, with the FARGO shifts and SOR counts

@@ -66,7 +66,7 @@ def test_read_inpar_case_insensitive_and_defaults():
         P.read_inpar(text + "\nNoSuchKey 3\n")
 
 
-@pytest.mark.parametrize("key,val,msg", [("EnergyEquation", "NO", "isothermal"),
+@pytest.mark.parametrize("key,val,msg", [("CoolingTime", "10.0", "parametric cooling"),
                                          ("InnerBoundary", "OPEN", "open"),
                                          ("AerodynamicDrag", "YES", "AerodynamicDrag")])
 def test_unsupported_rejected(lib, key, val, msg):

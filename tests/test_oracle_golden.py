@@ -13,7 +13,8 @@ import harness as H
 import oracle as O
 from fargo_thorin_gb300 import workloads
 
-CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40"]
+CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "iso_24x72", "iso_peb_32x96",
+         "dampinit_24x72", "gasflux_24x72", "frame_24x72"]
 
 
 def _run(name, force_planet=True):
@@ -42,7 +43,8 @@ def test_oracle_bit_exact_vs_reference(name):
         assert d.algogas(sys_) == 0
         st = d.stats()
         assert st.substeps == g["substeps"][step - 1]
-        assert st.sor_last_niter == g["sor_niter"][step - 1]
+        if len(g["sor_niter"]):                     # no SOR in isothermal runs
+            assert st.sor_last_niter == g["sor_niter"][step - 1]
         m, mom, e, _, _ = d.integrals()
         assert m == g["mass"][step - 1] and mom == g["momentum"][step - 1] and e == g["energy"][step - 1]
         if step % ninterm == 0:
