@@ -994,3 +994,180 @@ void aux_min_final(const double *part, int nb, double *out, cudaStream_t s)
   k_min_final<<<1, 1024, 0, s>>>(part, nb, out);
   g_thorin_launches++;
 }
+
+// ---------------------------------------------------------------------------
+// Open, non-reflecting and source-mass boundaries (ApplyBoundaryCondition,
+// SideEuler.c:133-337, 458-486).  The reference's floors of the open inner
+// ghost ring (SideEuler.c:15-16):
+#define TH_DENSITYFLOOR 1.0e-16
+#define TH_ENERGYFLOOR 1.0e-16
+
+// OpenInnerBoundary (SideEuler.c:133-178): ring 0 is the ghost ring.
+__global__ void k_open_inner(DevGrid g, double *__restrict__ rho, double *__restrict__ vr,
+                             double *__restrict__ energy, int energy_eq, int damp_flux, double gasflux)
+{
+  const int ns = g.ns, i = 1;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ns) return;
+  const int l = j + i * ns;
+  const double a = rho[l] + (rho[l] - rho[l + ns]);
+  rho[l - ns] = (a > TH_DENSITYFLOOR) ? a : TH_DENSITYFLOOR;
+  if (energy_eq) {
+    const double b = energy[l] + (energy[l] - energy[l + ns]);
+    energy[l - ns] = (b > TH_ENERGYFLOOR) ? b : TH_ENERGYFLOOR;
+  }
+  if (vr[l + ns] > 0.0) { vr[l] = 0.0; vr[l - ns] = 0.0; }
+  else { vr[l] = vr[l + ns]; vr[l - ns] = vr[l]; }
+  if (damp_flux) {
+    double rhoinf = 0.5 * (rho[l] + rho[l - ns]);
+    vr[l] = div_fast(-gasflux, 2.0 * TH_PI * g.r.Rinf[i] * rhoinf);
+    rhoinf = rho[l - ns] - 0.5 * (rho[l] - rho[l - ns]);
+    vr[l - ns] = div_fast(-gasflux, 2.0 * TH_PI * g.r.Rinf[i - 1] * rhoinf);
+  }
+}
+
+// OpenOuterBoundary (SideEuler.c:193-232): ring nrad is the ghost ring.
+__global__ void k_open_outer(DevGrid g, double *__restrict__ rho, double *__restrict__ vr,
+                             double *__restrict__ energy, int energy_eq, int damp_flux, double gasflux)
+{
+  const int ns = g.ns, i = g.nr - 1;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ns) return;
+  const int l = j + i * ns;
+  rho[l + ns] = rho[l] + (rho[l] - rho[l - ns]);
+  if (energy_eq) energy[l + ns] = energy[l] + (energy[l] - energy[l - ns]);
+  if (vr[l] > 0.0) { vr[l] = 0.0; vr[l + ns] = 0.0; }
+  else { vr[l] = vr[l - ns]; vr[l + ns] = vr[l]; }
+  if (damp_flux) {
+    double rhoinf = 0.5 * (rho[l] + rho[l + ns]);
+    vr[l + ns] = div_fast(-gasflux, 2.0 * TH_PI * g.r.Rinf[i + 1] * rhoinf);
+    rhoinf = rho[l + ns] + 0.5 * (rho[l + ns] - rho[l]);
+    vr[l + 2 * ns] = div_fast(-gasflux, 2.0 * TH_PI * g.r.Rsup[i + 1] * rhoinf);
+  }
+}
+
+// Block-wide sum of a ring, valid in every thread (fixed tree order).
+__device__ double ring_sum_block(const double *__restrict__ row, int ns)
+{
+  __shared__ double sh;
+  double a = 0.0;
+  for (int j = threadIdx.x; j < ns; j += blockDim.x) a += row[j];
+  a = block_reduce(a, OpAdd(), 0.0);
+  if (threadIdx.x == 0) sh = a;
+  __syncthreads();
+  a = sh;
+  __syncthreads();
+  return a;
+}
+
+// NonReflectingBoundary (SideEuler.c:234-337): block 0 the inner edge,
+// block 1 the outer edge.  Each block copies the ring next to the edge into
+// the edge ring rotated by the Keplerian shear over one cell, sets v_r from
+// the outgoing characteristic, and restores the edge ring's mean density and
+// energy to the initial profile.
+__global__ void __launch_bounds__(1024) k_nonreflecting(DevGrid g, double *__restrict__ rho,
+                                                        double *__restrict__ vr, double *__restrict__ energy,
+                                                        const double *__restrict__ cs)
+{
+  const int ns = g.ns, nr = g.nr;
+  const bool inner = (blockIdx.x == 0);
+  const int ia = inner ? 0 : nr - 2, ib = inner ? 1 : nr - 1;     // rings whose c_s are averaged
+  const double csin = ring_sum_block(cs + (size_t)ia * ns, ns) / (double)ns;
+  const double csout = ring_sum_block(cs + (size_t)ib * ns, ns) / (double)ns;
+  double dangle;
+  if (inner) dangle = (pow(g.r.Rinf[1], -1.5) - 1.0) / (.5 * (csin + csout)) * (g.r.Rmed[1] - g.r.Rmed[0]);
+  else dangle = (pow(g.r.Rinf[nr - 2], -1.5) - 1.0) / (.5 * (csin + csout)) * (g.r.Rmed[nr - 1] - g.r.Rmed[nr - 2]);
+  const int i_angle = (int)(dangle / 2.0 / TH_PI * (double)ns + .5);
+  const int i = inner ? 1 : nr - 1;
+  const int edge = inner ? 0 : nr - 1;
+  const double sig = inner ? g.r.SigmaMed[1] : g.r.SigmaMed[nr - 2];
+  for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+    const int l = j + i * ns;
+    int jp = inner ? j + i_angle : j - i_angle;
+    if (jp >= ns) jp -= ns;
+    if (jp < 0) jp += ns;
+    if (inner) {
+      const int lp = jp;
+      rho[lp] = rho[l];
+      energy[lp] = energy[l];
+      const double vr_med = div_fast(-cs[l] * (rho[l] - sig), sig);
+      vr[l] = 2. * vr_med - vr[l + ns];
+    } else {
+      const int lp = jp + (i - 1) * ns;
+      rho[l] = rho[lp];
+      energy[l] = energy[lp];
+      const double vr_med = div_fast(cs[l] * (rho[l - ns] - sig), sig);
+      vr[l] = 2. * vr_med - vr[l - ns];
+    }
+  }
+  __syncthreads();
+  double *re = rho + (size_t)edge * ns, *ee = energy + (size_t)edge * ns;
+  const double mr = ring_sum_block(re, ns) / (double)ns;
+  for (int j = threadIdx.x; j < ns; j += blockDim.x) re[j] += g.r.SigmaMed[edge] - mr;
+  __syncthreads();
+  const double me = ring_sum_block(ee, ns) / (double)ns;
+  for (int j = threadIdx.x; j < ns; j += blockDim.x) ee[j] += g.r.EnergyMed[edge] - me;
+}
+
+// ApplyOuterSourceMass (SideEuler.c:458-486), one block.
+__global__ void __launch_bounds__(1024) k_outer_source_mass(DevGrid g, double *__restrict__ rho,
+                                                            double *__restrict__ vr, double penul_vr)
+{
+  const int ns = g.ns, i = g.nr - 1;
+  double *row = rho + (size_t)i * ns;
+  const double avg = g.r.SigmaMed[i] - ring_sum_block(row, ns) / (double)ns;
+  for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+    row[j] += avg;
+    vr[j + i * ns] = penul_vr;
+  }
+}
+
+void aux_open_inner(const DevGrid &g, double *rho, double *vr, double *energy, int energy_eq, int damp_flux,
+                    double gasflux, cudaStream_t s)
+{
+  k_open_inner<<<(g.ns + BX - 1) / BX, BX, 0, s>>>(g, rho, vr, energy, energy_eq, damp_flux, gasflux);
+  g_thorin_launches++;
+}
+
+void aux_open_outer(const DevGrid &g, double *rho, double *vr, double *energy, int energy_eq, int damp_flux,
+                    double gasflux, cudaStream_t s)
+{
+  k_open_outer<<<(g.ns + BX - 1) / BX, BX, 0, s>>>(g, rho, vr, energy, energy_eq, damp_flux, gasflux);
+  g_thorin_launches++;
+}
+
+void aux_nonreflecting(const DevGrid &g, double *rho, double *vr, double *energy, const double *cs, cudaStream_t s)
+{
+  k_nonreflecting<<<2, 1024, 0, s>>>(g, rho, vr, energy, cs);
+  g_thorin_launches++;
+}
+
+void aux_outer_source_mass(const DevGrid &g, double *rho, double *vr, double penul_vr, cudaStream_t s)
+{
+  k_outer_source_mass<<<1, 1024, 0, s>>>(g, rho, vr, penul_vr);
+  g_thorin_launches++;
+}
+
+// Parametric cooling of SubStep3 (SourceEuler.c:569-582): the energy relaxes
+// towards the initial profile on the cooling time, heated by Q+.
+__global__ void k_parametric_cooling(DevGrid g, const double *__restrict__ rho, const double *__restrict__ eint,
+                                     const double *__restrict__ qplus, const double *__restrict__ divv,
+                                     const double *__restrict__ coolt, const double *__restrict__ qplusmed,
+                                     double *__restrict__ enew, double dt, double gm1)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  const double tc = coolt[i], sm = g.r.SigmaMed[i];
+  const double tmp1 = div_fast(g.r.EnergyMed[i] * dt * rho[l], sm) + tc * eint[l] +
+                      dt * tc * (qplus[l] - div_fast(qplusmed[i] * rho[l], sm));
+  const double tmp2 = dt + tc + gm1 * dt * tc * divv[l];
+  enew[l] = div_fast(tmp1, tmp2);
+}
+
+void aux_parametric_cooling(const DevGrid &g, const double *rho, const double *eint, const double *qplus,
+                            const double *divv, const double *coolt, const double *qplusmed, double *enew, double dt,
+                            double gm1, cudaStream_t s)
+{
+  k_parametric_cooling<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, eint, qplus, divv, coolt, qplusmed, enew, dt, gm1);
+  g_thorin_launches++;
+}

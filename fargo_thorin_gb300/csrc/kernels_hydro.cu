@@ -235,9 +235,11 @@ __global__ void k_eos(DevGrid g, const double *__restrict__ rho, const double *_
   const int ns = g.ns;
   CELL_LOOP_2D
   const double r = rho[l], e = energy[l];
-  double tmp2 = div_fast(1.0, r * 1.0);
-  double tmp1 = e * 1.0 * gm1;
-  temper[l] = tmp1 * tmp2;
+  if (temper) {                             // NULL: ComputeSoundSpeed alone
+    double tmp2 = div_fast(1.0, r * 1.0);
+    double tmp1 = e * 1.0 * gm1;
+    temper[l] = tmp1 * tmp2;
+  }
   cs[l] = sqrt(div_fast(gg1 * fabs(e), r));
 }
 

@@ -93,7 +93,7 @@ enum {  // ring arrays kept on the device
   R_WAVEKILLER, R_RMED15, R_RINF15, R_RSUP15, R_COSTAB, R_SINTAB, R_SIGMAMED, R_ENERGYMED, R_VTHETAMED, R_PEBDENS0,
   R_PEBVRAD0, R_PEBVTHETA0, R_CSMEAN, R_TEMPMEAN, R_NUMED, R_NUINF, R_INVDXTHETA, R_INVDXTHETA2, R_SUPPTORQUE,
   R_DELTAR2, R_CFLDXRAD, R_CFLDXTHETA, R_CFLMINDX, R_CFLDEN5, R_VMOY, R_PVTMED, R_HAVR, R_SIGAVR, R_ISTAVR, R_PHAVR,
-  R_PISTAVR, R_VMED, R_TAUAVR, R_VTEMP, R_DAMPVR0, R_CSISO, R_COUNT
+  R_PISTAVR, R_VMED, R_TAUAVR, R_VTEMP, R_DAMPVR0, R_CSISO, R_COOLT, R_QPLUSMED, R_COUNT
 };
 
 struct thorin_disk {
@@ -310,8 +310,6 @@ static int check_supported(const thorin_params &p)
 {
   const char *bad = nullptr;
   if (p.nrad < 4 || p.nsec < 4 || (p.nsec & 1)) bad = "nrad, nsec >= 4 and nsec even (red-black SOR)";
-  else if (p.open_inner || p.open_outer || p.non_reflecting || p.outer_source_mass) bad = "open/non-reflecting boundaries";
-  else if (p.parametric_cooling) bad = "parametric cooling";
   else if (p.accretion_rate > 1e-10) bad = "gas accretion onto planets";
   else if (p.prescribed_accretion) bad = "ParametricAccretion";
   else if (p.aerodynamic_drag) bad = "AerodynamicDrag";
@@ -727,6 +725,15 @@ extern "C" int thorin_gpu_init_default(thorin_disk *d)
       sacc += cs[l];
     }
     csm[i] = sacc / (double)ns;
+  }
+  if (p.parametric_cooling) {             // FillCoolingTime, FillQplus (Theo.c:103-129)
+    std::vector<double> ct(nr + 2, 0.0), qm(nr + 2, 0.0);
+    for (int i = 0; i < nr; i++) {
+      ct[i] = p.cooling_time * pow(d->Rmed[i], 2.0 + 2.0 * p.flaring_index);
+      qm[i] = 2.25 * fviscosity_host(d, i, d->Rmed[i], csm) * p.sigma0 * pow(d->Rmed[i], -p.sigma_slope - 3.0);
+    }
+    RCHK(upload_ring(d, R_COOLT, ct));
+    RCHK(upload_ring(d, R_QPLUSMED, qm));
   }
   // InitGasVelocity (Pframeforce.c:696-750)
   for (int i = 0; i <= nr; i++) {
@@ -1272,6 +1279,13 @@ static int energy_step(thorin_disk *d, double dt)
 {
   const thorin_params &p = d->p;
   hydro_qplus(d->g, d->vrad, d->vtheta, d->rho, d->divv, d->qplus, d->invdphi, d->lr01, d->lr12, d->s);
+  if (p.parametric_cooling) {
+    aux_parametric_cooling(d->g, d->rho, d->energy_int, d->qplus, d->divv, d->ring[R_COOLT], d->ring[R_QPLUSMED],
+                           d->energy_new, dt, d->gm1, d->s);
+    KCHECK("cooling kernel");
+    std::swap(d->energy, d->energy_new);
+    return THORIN_OK;
+  }
   hydro_eos(d->g, d->rho, d->energy_int, d->temper, d->cs, d->gm1, d->gg1, d->s);
   hydro_diffcoef(d->g, d->rho, d->temper, d->cs, d->opacity, d->qminus, d->dcen, d->partials, p.opacity_law,
                  p.parametric_opacity * OPA2CU, p.parametric_opacity, p.opacity_drop, d->taueff_c,
@@ -1320,9 +1334,12 @@ static void transport_fluid(thorin_disk *d, double **rho, double *vr, double *vt
   TransportScratch S = d->ts;
   S.rho_new = *rho_scratch;
   S.e_new = energy ? d->t_e_gas : nullptr;
-  hydro_transport(d->g, rho, vr, vt, energy, S, dt, d->OmegaFrame, d->p.fast_transport,
-                  gas && d->p.damping && d->p.damp_vrad, d->drin, d->drout, gas ? d->temper : nullptr, d->cs, d->gm1,
-                  d->gg1, d->s);
+  // the v_r damping of the boundary call after the transport is fused into
+  // the velocity kernel when it is the only boundary condition
+  const thorin_params &p = d->p;
+  const int fused = p.damping && p.damp_vrad && !(p.open_inner || p.open_outer || p.non_reflecting || p.outer_source_mass);
+  hydro_transport(d->g, rho, vr, vt, energy, S, dt, d->OmegaFrame, p.fast_transport, gas && fused, d->drin, d->drout,
+                  gas ? d->temper : nullptr, d->cs, d->gm1, d->gg1, d->s);
   std::swap(*rho, *rho_scratch);
   if (energy) std::swap(*energy, d->t_e_gas);
 }
@@ -1331,7 +1348,20 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
 {
   const thorin_params &p = d->p;
   const int damp = p.damping;
-  auto boundary = [&]() {                // ApplyBoundaryCondition -> DampingBoundary (SideEuler.c:368-419)
+  auto boundary = [&]() {                // ApplyBoundaryCondition (SideEuler.c:490-503)
+    if (p.open_inner) aux_open_inner(d->g, d->rho, d->vrad, d->energy, p.energy_eq, p.damp_flux, p.gasflux, d->s);
+    if (p.open_outer) aux_open_outer(d->g, d->rho, d->vrad, d->energy, p.energy_eq, p.damp_flux, p.gasflux, d->s);
+    if (p.non_reflecting) {
+      if (p.energy_eq) {                   // ComputeSoundSpeed: c_s, its ring means and the viscosity
+        hydro_eos(d->g, d->rho, d->energy, nullptr, d->cs, d->gm1, d->gg1, d->s);
+        aux_ring_mean(d->g, d->cs, d->ring[R_CSMEAN], d->s);
+        aux_viscosity_rings(d->g, d->vp, d->s);
+      }
+      aux_nonreflecting(d->g, d->rho, d->vrad, d->energy, d->cs, d->s);
+    }
+    if (p.outer_source_mass)
+      aux_outer_source_mass(d->g, d->rho, d->vrad, p.imposed_disk_drift * pow((d->Rinf[d->nr - 1] / 1.0), -p.sigma_slope),
+                            d->s);
     if (damp) aux_damp_gas(d->g, d->vrad, d->rho, d->vtheta, d->energy, d->damp_rings_d, d->ndamp, d->ring[R_DAMPVR0],
                            dt, d->OmegaFrame, p.damp_init, p.damp_flux, p.energy_eq, d->s);
   };
@@ -1372,7 +1402,7 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
   // Transport, ApplyBoundaryCondition, ComputeTemperatureField, ComputeSoundSpeed
   transport_fluid(d, &d->rho, d->vrad, d->vtheta, p.energy_eq ? &d->energy : nullptr, &d->t_rho_gas, dt, 1);
   CUCHK(cudaMemcpyAsync(d->nshift_h.data(), d->nshift, d->nr * sizeof(int), cudaMemcpyDeviceToHost, d->s));
-  if (damp && !p.damp_vrad) {
+  if ((damp && !p.damp_vrad) || p.open_inner || p.open_outer || p.non_reflecting || p.outer_source_mass) {
     // damping towards INIT / GASFLUX changes Sigma (and e): the boundary
     // call, then ComputeTemperatureField and ComputeSoundSpeed
     boundary();

@@ -148,6 +148,15 @@ void aux_evaporate(const DevGrid &g, const double *T, double *pdens, double facc
 void aux_damp_gas(const DevGrid &g, double *vrad, double *rho, double *vtheta, double *energy, const int *rings,
                   int nrings, const double *vr0r, double dt, double omega_frame, int damp_init, int damp_flux,
                   int energy_eq, cudaStream_t s);
+void aux_open_inner(const DevGrid &g, double *rho, double *vr, double *energy, int energy_eq, int damp_flux,
+                    double gasflux, cudaStream_t s);
+void aux_open_outer(const DevGrid &g, double *rho, double *vr, double *energy, int energy_eq, int damp_flux,
+                    double gasflux, cudaStream_t s);
+void aux_nonreflecting(const DevGrid &g, double *rho, double *vr, double *energy, const double *cs, cudaStream_t s);
+void aux_outer_source_mass(const DevGrid &g, double *rho, double *vr, double penul_vr, cudaStream_t s);
+void aux_parametric_cooling(const DevGrid &g, const double *rho, const double *eint, const double *qplus,
+                            const double *divv, const double *coolt, const double *qplusmed, double *enew, double dt,
+                            double gm1, cudaStream_t s);
 void aux_iso_eos(const DevGrid &g, const double *rho, const double *csr, double *cs, double *press, double *temper,
                  int set_cs, int set_press, int set_temper, cudaStream_t s);
 void aux_damp_peb(const DevGrid &g, double *pd, double *pvr, double *pvt, const int *rings, int nrings, double dt,

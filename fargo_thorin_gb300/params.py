@@ -301,10 +301,6 @@ def derive(v: dict, *, sor_eps: float = SOREPS, sor_maxiters: int = SORMAXITERS,
 def check_supported(p: ThorinParams) -> None:
     """Raise for options outside the implemented hot path (fail loudly)."""
     bad = []
-    if p.open_inner or p.open_outer or p.non_reflecting or p.outer_source_mass:
-        bad.append("open/non-reflecting/outer-source boundaries")
-    if p.parametric_cooling:
-        bad.append("parametric cooling (CoolingTime > 0)")
     if p.accretion_rate > 1e-10:
         bad.append("gas accretion onto planets (AccretionRate > 0)")
     if p.prescribed_accretion:

@@ -67,6 +67,7 @@ typedef struct ora_disk {
   double *Radii, *GlobalRmed, *Rinf, *Rsup, *Rmed, *Surf, *InvRmed, *InvSurf;
   double *InvDiffRmed, *InvDiffRsup, *InvRinf, *OmegaInv, *Rmed2;
   double *SigmaMed, *SigmaInf, *EnergyMed, *VthetaMed, *WaveKiller;
+  double *CoolingTimeMed, *QplusMed;
   double *globcsvec, *globtempervec, *globpressvec, *vt1D;
   double *PebDensInit, *PebVradInit, *PebVthetaInit;
   double *VMed, *Vmoy; int *Nshift, *NshiftGas;
@@ -351,6 +352,11 @@ static void InitGasVelocity(ora_disk *d)                   /* Pframeforce.c:644-
     ConstructSequence(vt_cent, vt_int, nr);
     vt_cent[nr] = vt_cent[nr - 1];
   }
+  if (p->parametric_cooling)                                 /* FillCoolingTime, FillQplus (Theo.c:103-129) */
+    for (int i = 0; i < nr; i++) {
+      d->CoolingTimeMed[i] = p->cooling_time * pow(d->Rmed[i], 2.0 + 2.0 * p->flaring_index);
+      d->QplusMed[i] = 2.25 * FViscosity(d, d->Rmed[i]) * p->sigma0 * pow(d->Rmed[i], -p->sigma_slope - 3.0);
+    }
   for (int i = 0; i <= nr; i++) {
     double r, ri, viscosity;
     if (i == nr) { r = d->Rmed[nr - 1]; ri = d->Rinf[nr - 1]; }
@@ -496,7 +502,8 @@ ora_disk *ora_create(const thorin_params *p)
   double **v1[] = {&d->Radii, &d->GlobalRmed, &d->Rinf, &d->Rsup, &d->Rmed, &d->Surf, &d->InvRmed, &d->InvSurf,
                    &d->InvDiffRmed, &d->InvDiffRsup, &d->InvRinf, &d->OmegaInv, &d->Rmed2, &d->SigmaMed, &d->SigmaInf,
                    &d->EnergyMed, &d->VthetaMed, &d->WaveKiller, &d->globcsvec, &d->globtempervec, &d->globpressvec,
-                   &d->vt1D, &d->PebDensInit, &d->PebVradInit, &d->PebVthetaInit, &d->VMed, &d->Vmoy};
+                   &d->vt1D, &d->PebDensInit, &d->PebVradInit, &d->PebVthetaInit, &d->VMed, &d->Vmoy,
+                   &d->CoolingTimeMed, &d->QplusMed};
   for (size_t k = 0; k < sizeof(v1) / sizeof(v1[0]); k++) *v1[k] = vec(n1);
   d->Nshift = (int *)calloc((size_t)n1, sizeof(int));
   d->NshiftGas = (int *)calloc((size_t)n1, sizeof(int));
@@ -651,9 +658,137 @@ static void DampingBoundary(ora_disk *d, double step)       /* SideEuler.c:368-4
   }
 }
 
+#define DENSITYFLOOR 1.0e-16                                /* SideEuler.c:15-16 */
+#define ENERGYFLOOR 1.0e-16
+
+static void OpenInnerBoundary(ora_disk *d)                 /* SideEuler.c:133-178 */
+{
+  const thorin_params *p = &d->p;
+  int ns = d->ns, i = 1;
+  double *rho = d->rho, *vr = d->vrad, *energy = d->energy;
+  for (int j = 0; j < ns; j++) {
+    int l = j + i * ns;
+    double a = rho[l] + (rho[l] - rho[l + ns]);
+    rho[l - ns] = (a > DENSITYFLOOR) ? a : DENSITYFLOOR;
+    if (p->energy_eq) {
+      double b = energy[l] + (energy[l] - energy[l + ns]);
+      energy[l - ns] = (b > ENERGYFLOOR) ? b : ENERGYFLOOR;
+    }
+    if (vr[l + ns] > 0.0) { vr[l] = 0.0; vr[l - ns] = 0.0; }
+    else { vr[l] = vr[l + ns]; vr[l - ns] = vr[l]; }
+    if (p->damp_flux) {
+      double rhoinf = 0.5 * (rho[l] + rho[l - ns]);
+      vr[l] = -p->gasflux / (2.0 * PI * d->Rinf[i] * rhoinf);
+      rhoinf = rho[l - ns] - 0.5 * (rho[l] - rho[l - ns]);
+      vr[l - ns] = -p->gasflux / (2.0 * PI * d->Rinf[i - 1] * rhoinf);
+    }
+  }
+}
+
+static void OpenOuterBoundary(ora_disk *d)                 /* SideEuler.c:193-232 */
+{
+  const thorin_params *p = &d->p;
+  int ns = d->ns, i = d->nr - 1;
+  double *rho = d->rho, *vr = d->vrad, *energy = d->energy;
+  for (int j = 0; j < ns; j++) {
+    int l = j + i * ns;
+    rho[l + ns] = rho[l] + (rho[l] - rho[l - ns]);
+    if (p->energy_eq) energy[l + ns] = energy[l] + (energy[l] - energy[l - ns]);
+    if (vr[l] > 0.0) { vr[l] = 0.0; vr[l + ns] = 0.0; }
+    else { vr[l] = vr[l - ns]; vr[l + ns] = vr[l]; }
+    if (p->damp_flux) {
+      double rhoinf = 0.5 * (rho[l] + rho[l + ns]);
+      vr[l + ns] = -p->gasflux / (2.0 * PI * d->Rinf[i + 1] * rhoinf);
+      rhoinf = rho[l + ns] + 0.5 * (rho[l + ns] - rho[l]);
+      vr[l + 2 * ns] = -p->gasflux / (2.0 * PI * d->Rsup[i + 1] * rhoinf);
+    }
+  }
+}
+
+static void NonReflectingBoundary(ora_disk *d)             /* SideEuler.c:234-337 */
+{
+  int ns = d->ns, nr = d->nr;
+  double *rho = d->rho, *vr = d->vrad, *energy = d->energy, *cs = d->cs;
+  double csin = 0.0, csout = 0.0, dangle, mean;
+  int i, i_angle;
+  for (int j = 0; j < ns; j++) { csin += cs[j]; csout += cs[ns + j]; }
+  csin /= (double)ns;
+  csout /= (double)ns;
+  i = 1;
+  dangle = (pow(d->Rinf[1], -1.5) - 1.0) / (.5 * (csin + csout));
+  dangle *= (d->Rmed[1] - d->Rmed[0]);
+  i_angle = (int)(dangle / 2.0 / PI * (double)ns + .5);
+  for (int j = 0; j < ns; j++) {
+    int l = j + i * ns, jp = j + i_angle;
+    if (jp >= ns) jp -= ns;
+    if (jp < 0) jp += ns;
+    int lp = jp;
+    rho[lp] = rho[l];
+    energy[lp] = energy[l];
+    double vr_med = -cs[l] * (rho[l] - d->SigmaMed[1]) / d->SigmaMed[1];
+    vr[l] = 2. * vr_med - vr[l + ns];
+  }
+  mean = 0.0;
+  for (int j = 0; j < ns; j++) mean += rho[j];
+  mean /= (double)ns;
+  for (int j = 0; j < ns; j++) rho[j] += d->SigmaMed[0] - mean;
+  mean = 0.0;
+  for (int j = 0; j < ns; j++) mean += energy[j];
+  mean /= (double)ns;
+  for (int j = 0; j < ns; j++) energy[j] += d->EnergyMed[0] - mean;
+  csin = 0.0;
+  csout = 0.0;
+  for (int j = 0; j < ns; j++) { csin += cs[(nr - 2) * ns + j]; csout += cs[(nr - 1) * ns + j]; }
+  csin /= (double)ns;
+  csout /= (double)ns;
+  i = nr - 1;
+  dangle = (pow(d->Rinf[nr - 2], -1.5) - 1.0) / (.5 * (csin + csout));
+  dangle *= (d->Rmed[nr - 1] - d->Rmed[nr - 2]);
+  i_angle = (int)(dangle / 2.0 / PI * (double)ns + .5);
+  for (int j = 0; j < ns; j++) {
+    int l = j + i * ns, jp = j - i_angle;
+    if (jp >= ns) jp -= ns;
+    if (jp < 0) jp += ns;
+    int lp = jp + (i - 1) * ns;
+    rho[l] = rho[lp];
+    energy[l] = energy[lp];
+    double vr_med = cs[l] * (rho[l - ns] - d->SigmaMed[nr - 2]) / d->SigmaMed[nr - 2];
+    vr[l] = 2. * vr_med - vr[l - ns];
+  }
+  mean = 0.0;
+  for (int j = 0; j < ns; j++) mean += rho[j + ns * (nr - 1)];
+  mean /= (double)ns;
+  for (int j = 0; j < ns; j++) rho[j + (nr - 1) * ns] += d->SigmaMed[nr - 1] - mean;
+  mean = 0.0;
+  for (int j = 0; j < ns; j++) mean += energy[j + ns * (nr - 1)];
+  mean /= (double)ns;
+  for (int j = 0; j < ns; j++) energy[j + (nr - 1) * ns] += d->EnergyMed[nr - 1] - mean;
+}
+
+static void ApplyOuterSourceMass(ora_disk *d)              /* SideEuler.c:458-486 */
+{
+  const thorin_params *p = &d->p;
+  int ns = d->ns, nr = d->nr, i = nr - 1;
+  double average_rho = 0.0, penul_vr;
+  for (int j = 0; j < ns; j++) average_rho += d->rho[j + i * ns];
+  average_rho /= (double)ns;
+  average_rho = d->SigmaMed[nr - 1] - average_rho;
+  for (int j = 0; j < ns; j++) d->rho[j + i * ns] += average_rho;
+  penul_vr = p->imposed_disk_drift * pow((d->Rinf[nr - 1] / 1.0), -p->sigma_slope);
+  for (int j = 0; j < ns; j++) d->vrad[j + i * ns] = penul_vr;
+}
+
 static void ApplyBoundaryCondition(ora_disk *d, double dt)  /* SideEuler.c:490-503 */
 {
-  if (d->p.damping) DampingBoundary(d, dt);
+  const thorin_params *p = &d->p;
+  if (p->open_inner) OpenInnerBoundary(d);
+  if (p->open_outer) OpenOuterBoundary(d);
+  if (p->non_reflecting) {
+    if (p->energy_eq) ComputeSoundSpeed(d, d->rho, d->energy);
+    NonReflectingBoundary(d);
+  }
+  if (p->outer_source_mass) ApplyOuterSourceMass(d);
+  if (p->damping) DampingBoundary(d, dt);
 }
 
 static void DampPebbles(ora_disk *d, double dt)             /* SideEuler.c:423-456 */
@@ -1249,6 +1384,19 @@ static int SubStep3(ora_disk *d, double dt)                 /* SourceEuler.c:508
     double q1 = d->qplus[j + ns], q2 = d->qplus[j + 2 * ns];
     if (viscosity != 0.0) d->qplus[j] = q1 * exp(log(q1 / q2) * log(r0 / r1) / log(r1 / r2));
     else d->qplus[j] = 0.0;
+  }
+  if (d->p.parametric_cooling) {                             /* SourceEuler.c:569-582 */
+    const double *energy = d->EnergyInt;
+    OMP_FOR
+    for (int i = 0; i < nr; i++)
+      for (int j = 0; j < ns; j++) {
+        int l = j + i * ns;
+        double tmp1 = d->EnergyMed[i] * dt * rho[l] / d->SigmaMed[i] + d->CoolingTimeMed[i] * energy[l] +
+                      dt * d->CoolingTimeMed[i] * (d->qplus[l] - d->QplusMed[i] * rho[l] / d->SigmaMed[i]);
+        double tmp2 = dt + d->CoolingTimeMed[i] + (d->p.adiabind - 1.0) * dt * d->CoolingTimeMed[i] * d->divv[l];
+        d->EnergyNew[l] = tmp1 / tmp2;
+      }
+    return THORIN_OK;
   }
   return ImplicitRadiativeDiffusion(d, dt);
 }

@@ -48,6 +48,10 @@ CASES = {
     "dampinit_24x72": ("disk0", 24, 72, 6, 2, "DampTowards INIT\n", True),
     "gasflux_24x72": ("disk0", 24, 72, 6, 2, "DampTowards GASFLUX\nGasFlux 1e-8\n", True),
     "frame_24x72": ("disk0", 24, 72, 6, 2, "OmegaFrame 1.0\n", True),
+    "open_24x72": ("disk0", 24, 72, 6, 2, "InnerBoundary OPEN\nOuterBoundary OPEN\n", True),
+    "nonrefl_24x72": ("disk0", 24, 72, 6, 2, "InnerBoundary NONREFLECTING\n", True),
+    "srcmass_24x72": ("disk0", 24, 72, 6, 2, "OuterSourceMass YES\n", True),
+    "cooling_24x72": ("disk0", 24, 72, 6, 2, "CoolingTime 10.0\n", True),
 }
 GAS = ["dens", "vrad", "vtheta", "temper"]
 PEB = ["pebbledens", "pebblevrad", "pebblevtheta"]

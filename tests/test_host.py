@@ -66,8 +66,8 @@ def test_read_inpar_case_insensitive_and_defaults():
         P.read_inpar(text + "\nNoSuchKey 3\n")
 
 
-@pytest.mark.parametrize("key,val,msg", [("CoolingTime", "10.0", "parametric cooling"),
-                                         ("InnerBoundary", "OPEN", "open"),
+@pytest.mark.parametrize("key,val,msg", [("ParametricAccretion", "1e-5", "ParametricAccretion"),
+                                         ("AccretionRate", "1.0", "gas accretion"),
                                          ("AerodynamicDrag", "YES", "AerodynamicDrag")])
 def test_unsupported_rejected(lib, key, val, msg):
     text = workloads.inpar_text("disk1", 32, 96) + f"\n{key} {val}\n"
