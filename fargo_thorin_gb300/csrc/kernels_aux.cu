@@ -1171,3 +1171,111 @@ void aux_parametric_cooling(const DevGrid &g, const double *rho, const double *e
   k_parametric_cooling<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, eint, qplus, divv, coolt, qplusmed, enew, dt, gm1);
   g_thorin_launches++;
 }
+
+// ---------------------------------------------------------------------------
+// Gas accretion onto a planet, Kley's prescription (AccreteOntoPlanets,
+// Planet.c:34-166): within frac1 = 0.75 and frac2 = 0.45 Roche radii a cell
+// loses facc1 times the Gaussian column between the planet's height +/- the
+// chord (trapezoid rule refined to 1e-4, at most 16 levels: qtrap,
+// Planet.c:172-211) and then the fraction facc2.  One block per planet over
+// the window [i_min, i_max] x [j_min, j_max] (narrower than a ring, so no cell
+// is visited twice); the mass and momentum taken are block sums written to
+// out[0..2].
+__device__ double qtrap_gauss(double a, double b)
+{
+  double s = 0.0, olds = 0.0;
+  for (int n = 1; n <= 16; n++) {
+    if (n == 1) {
+      s = 0.5 * (b - a) * (exp(-a * a) + exp(-b * b));
+    } else {
+      int it = 1;
+      for (int j = 1; j < n - 1; j++) it <<= 1;
+      const double tnm = it, del = div_fast(b - a, tnm);
+      double x = a + 0.5 * del, sum = 0.0;
+      for (int j = 1; j <= it; j++, x += del) sum += exp(-x * x);
+      s = 0.5 * (s + div_fast((b - a) * sum, tnm));
+    }
+    if (n > 5)
+      if (fabs(s - olds) < 1.e-4 * fabs(olds) || (s == 0.0 && olds == 0.0)) return s;
+    olds = s;
+  }
+  return s;
+}
+
+__global__ void __launch_bounds__(256) k_gas_accrete(DevGrid g, double *__restrict__ dens,
+                                                     const double *__restrict__ vrad,
+                                                     const double *__restrict__ vtheta,
+                                                     const double *__restrict__ cs, GasAccArgs a,
+                                                     double *__restrict__ out)
+{
+  const int ns = g.ns;
+  const int nj = a.j_max - a.j_min + 1;
+  const int ncell = (a.i_max - a.i_min + 1) * nj;
+  double dM = 0.0, dPx = 0.0, dPy = 0.0;
+  for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+    const int i = a.i_min + c / nj;
+    const int j = a.j_min + c % nj;
+    int jf = j;
+    while (jf < 0) jf += ns;
+    while (jf >= ns) jf -= ns;
+    const int l = jf + i * ns, lip = l + ns;
+    const int ljp = (jf == ns - 1) ? i * ns : l + 1;
+    const double rm = g.r.Rmed[i];
+    const double xc = rm * g.r.costab[jf], yc = rm * g.r.sintab[jf];
+    const double dx = a.Xp - xc, dy = a.Yp - yc;
+    const double distance = sqrt(dx * dx + dy * dy);
+    const double vtcell = 0.5 * (vtheta[l] + vtheta[ljp]) + rm * a.omega_frame;
+    const double vrcell = 0.5 * (vrad[l] + vrad[lip]);
+    const double vxcell = div_fast(vrcell * xc - vtcell * yc, rm);
+    const double vycell = div_fast(vrcell * yc + vtcell * xc, rm);
+    const double H = cs[l] * g.r.OmegaInv[i] * g.k.sqrt_adiabind_inv;
+    const double sq2H = sqrt(2.0) * H;
+    for (int pass = 0; pass < 2; pass++) {
+      const double fr = pass ? 0.45 : 0.75;
+      if (distance < fr * a.RRoche) {
+        const double dz = sqrt((fr * a.RRoche) * (fr * a.RRoche) - distance * distance);
+        double factor = qtrap_gauss(div_fast(a.Zp - dz, sq2H), div_fast(a.Zp + dz, sq2H));
+        factor *= div_fast(1.0, sqrt(2.0 * TH_PI) * H);
+        const double fa = pass ? a.facc2 : a.facc1;
+        const double deltaM = fa * factor * dens[l] * g.r.Surf[i];
+        dens[l] *= pass ? (1.0 - fa) : (1.0 - fa * factor);
+        dPx += deltaM * vxcell;
+        dPy += deltaM * vycell;
+        dM += deltaM;
+      }
+    }
+  }
+  dM = block_reduce(dM, OpAdd(), 0.0);
+  dPx = block_reduce(dPx, OpAdd(), 0.0);
+  dPy = block_reduce(dPy, OpAdd(), 0.0);
+  if (threadIdx.x == 0) { out[0] = dM; out[1] = dPx; out[2] = dPy; }
+}
+
+void aux_gas_accrete(const DevGrid &g, double *dens, const double *vrad, const double *vtheta, const double *cs,
+                     const GasAccArgs &a, double *out, cudaStream_t s)
+{
+  k_gas_accrete<<<1, 256, 0, s>>>(g, dens, vrad, vtheta, cs, a, out);
+  g_thorin_launches++;
+}
+
+// The gas state of one cell for the planet's aerodynamic drag (StokesDrag,
+// Drag.c:17-95): Sigma, c_s, v_r at l and l+nsec, v_theta at l and l+1.
+__global__ void k_drag_cell(const double *__restrict__ rho, const double *__restrict__ cs,
+                            const double *__restrict__ vrad, const double *__restrict__ vtheta, int l, int ns,
+                            double *__restrict__ out)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  out[0] = rho[l];
+  out[1] = cs[l];
+  out[2] = vrad[l];
+  out[3] = vrad[l + ns];
+  out[4] = vtheta[l];
+  out[5] = vtheta[l + 1];
+}
+
+void aux_drag_cell(const double *rho, const double *cs, const double *vrad, const double *vtheta, int l, int ns,
+                   double *out, cudaStream_t s)
+{
+  k_drag_cell<<<1, 32, 0, s>>>(rho, cs, vrad, vtheta, l, ns, out);
+  g_thorin_launches++;
+}

@@ -133,6 +133,7 @@ struct thorin_disk {
   int cfl_first;
   int sor_first, Niterlast, Niterbest;
   int torque_pending = 0, ntorque = 0;
+  double doubling = 0.0;         // ParametricAccretion's doubling time, fixed at its first call
   thorin_torque torques[THORIN_MAXPLANETS];
   double omega, domega, omegabest;
   double heatsrc[THORIN_MAXPLANETS];
@@ -310,9 +311,6 @@ static int check_supported(const thorin_params &p)
 {
   const char *bad = nullptr;
   if (p.nrad < 4 || p.nsec < 4 || (p.nsec & 1)) bad = "nrad, nsec >= 4 and nsec even (red-black SOR)";
-  else if (p.accretion_rate > 1e-10) bad = "gas accretion onto planets";
-  else if (p.prescribed_accretion) bad = "ParametricAccretion";
-  else if (p.aerodynamic_drag) bad = "AerodynamicDrag";
   else if (p.sloppy_cfl) bad = "SloppyCFL";
   if (bad) {
     g_last_error = std::string("unsupported option: ") + bad;
@@ -1026,6 +1024,55 @@ extern "C" int thorin_gpu_accrete(thorin_disk *d, thorin_planets *sys, double dt
 {
   const thorin_params &p = d->p;
   for (int k = 0; k < sys->nb; k++) { d->heatsrc[k] = 0.0; d->heatsrc_index[k] = -1; }   // InitHeating
+  // AccreteOntoPlanets (Planet.c:34-166)
+  for (int k = 0; k < sys->nb; k++) {
+    if (!(sys->acc[k] > 1e-10)) continue;
+    const double facc = fabs(dt) * sys->acc[k];
+    GasAccArgs a;
+    a.facc1 = 1.0 / 3.0 * facc; a.facc2 = 2.0 / 3.0 * facc;
+    if (a.facc1 > 1.0) a.facc1 = 1.0;
+    if (a.facc2 > 1.0) a.facc2 = 1.0;
+    a.Xp = sys->x[k]; a.Yp = sys->y[k]; a.Zp = sys->z[k];
+    const double VX = sys->vx[k], VY = sys->vy[k];
+    double M = sys->mass[k];
+    const double Rperp = sqrt(a.Xp * a.Xp + a.Yp * a.Yp);
+    const double Rplanet = sqrt(a.Xp * a.Xp + a.Yp * a.Yp + a.Zp * a.Zp);
+    a.RRoche = pow((1.0 / 3.0 * M * d->MassTaper), (1.0 / 3.0)) * Rplanet;
+    a.i_min = 0; a.i_max = d->nr - 1;
+    while ((a.i_min < d->nr) && (d->Rsup[a.i_min] < Rperp - a.RRoche)) a.i_min++;
+    while ((d->Rinf[a.i_max] > Rperp + a.RRoche) && (a.i_max > 0)) a.i_max--;
+    const double angle = atan2(a.Yp, a.Xp);
+    a.j_min = (int)((double)d->ns / 2.0 / H_PI * (angle - 2.0 * a.RRoche / Rperp));
+    a.j_max = (int)((double)d->ns / 2.0 / H_PI * (angle + 2.0 * a.RRoche / Rperp));
+    a.omega_frame = d->OmegaFrame;
+    if (a.j_max - a.j_min + 1 > d->ns) {
+      g_last_error = "gas accretion: the planet's Roche window is wider than a ring";
+      return THORIN_ERR_ARG;
+    }
+    double dM = 0.0, dPx = 0.0, dPy = 0.0;
+    if (a.i_min <= a.i_max) {
+      aux_gas_accrete(d->g, d->rho, d->vrad, d->vtheta, d->cs, a, d->scal + SC_GASACC, d->s);
+      KCHECK("gas accretion kernel");
+      CUCHK(cudaMemcpyAsync(d->scal_h + SC_GASACC, d->scal + SC_GASACC, 3 * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+      CUCHK(cudaStreamSynchronize(d->s));
+      dM = d->scal_h[SC_GASACC]; dPx = d->scal_h[SC_GASACC + 1]; dPy = d->scal_h[SC_GASACC + 2];
+    }
+    if (p.gas_accret_heating) heating1(d, M, dM, a.Xp, a.Yp, dt, k);
+    const double PX = M * VX + dPx, PY = M * VY + dPy;
+    M += dM;
+    if (sys->feel_disk[k]) { sys->vx[k] = PX / M; sys->vy[k] = PY / M; }
+    sys->mass[k] = M;
+  }
+  // ParametricAccretion (Pebbles.c:806-828)
+  if (p.prescribed_accretion) {
+    if (d->doubling == 0.0) d->doubling = p.parametric_accretion * 1000.0 * 2.0 * H_PI;
+    if (p.accret_heating) d->heatsrc_max = sys->nb;
+    for (int k = 0; k < sys->nb; k++) {
+      const double M = sys->mass[k], dM = M * dt / d->doubling;
+      if (p.accret_heating) heating1(d, M, dM, sys->x[k], sys->y[k], dt, k);
+      sys->mass[k] = M + dM;
+    }
+  }
   if (!p.pebbles) return THORIN_OK;
   if (p.accret_heating) d->heatsrc_max = sys->nb;
   for (int k = 0; k < sys->nb; k++) {
@@ -1447,6 +1494,56 @@ static void advance_from_disk(thorin_disk *d, thorin_planets *sys, double dt, co
   }
 }
 
+// StokesDrag + AdvanceSystemFromDrag (Drag.c:17-119): the drag of the gas in
+// the planet's own cell (its v_theta neighbour is l+1 without wrapping, as in
+// the reference).
+extern "C" int thorin_gpu_drag(thorin_disk *d, thorin_planets *sys, double dt)
+{
+  if (!d || !sys) return THORIN_ERR_ARG;
+  const thorin_params &p = d->p;
+  const int nr = d->nr, ns = d->ns;
+  for (int k = 0; k < sys->nb; k++) {
+    if (!sys->feel_disk[k]) continue;
+    const double m = sys->mass[k], x = sys->x[k], y = sys->y[k], z = sys->z[k];
+    const double vx = sys->vx[k], vy = sys->vy[k], vz = sys->vz[k];
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    const double Rperp = sqrt(x * x + y * y);
+    if (Rperp >= d->Rinf[0] && Rperp <= d->Rsup[nr - 1]) {
+      int i = 0;
+      while (d->Rsup[i] < Rperp) i++;
+      double ang = atan2(y, x);
+      if (ang < 0.0) ang += 2.0 * H_PI;
+      int j = (int)floor((double)ns / 2.0 / H_PI * ang + 0.5);
+      if (j == ns) j = 0;
+      const int l = j + i * ns;
+      aux_drag_cell(d->rho, d->cs, d->vrad, d->vtheta, l, ns, d->scal + SC_DRAGCELL, d->s);
+      CUCHK(cudaMemcpyAsync(d->scal_h + SC_DRAGCELL, d->scal + SC_DRAGCELL, 6 * sizeof(double), cudaMemcpyDeviceToHost,
+                            d->s));
+      CUCHK(cudaStreamSynchronize(d->s));
+      const double *c = d->scal_h + SC_DRAGCELL;
+      const double xc = d->Rmed[i] * cos(2.0 * H_PI * (double)j / (double)ns);
+      const double yc = d->Rmed[i] * sin(2.0 * H_PI * (double)j / (double)ns);
+      const double vtcell = 0.5 * (c[4] + c[5]) + d->Rmed[i] * d->OmegaFrame;
+      const double vrcell = 0.5 * (c[2] + c[3]);
+      const double vxcell = (vrcell * xc - vtcell * yc) / d->Rmed[i];
+      const double vycell = (vrcell * yc + vtcell * xc) / d->Rmed[i];
+      const double H = c[1] * d->OmegaInv[i] * (1.0 / sqrt(p.adiabind));
+      double factor = exp(-(z / (sqrt(2.0) * H)) * (z / (sqrt(2.0) * H)));
+      factor *= 1.0 / (sqrt(2.0 * H_PI) * H);
+      const double plrho = p.planetary_density / RHO2CGS;
+      const double plradius = pow(3.0 * m / (4.0 * H_PI * plrho), 1.0 / 3.0);
+      const double dvx = vx - vxcell, dvy = vy - vycell, dvz = vz - 0.0;
+      const double dvsq = dvx * dvx + dvy * dvy + dvz * dvz;
+      const double tmp = -0.5 * 0.48 * H_PI * plradius * plradius / m * factor * c[0] * dvsq * 1.0 / sqrt(dvsq);
+      ax = tmp * dvx; ay = tmp * dvy; az = tmp * dvz;
+    }
+    sys->vx[k] += dt * ax;
+    sys->vy[k] += dt * ay;
+    sys->vz[k] += dt * az;
+  }
+  return THORIN_OK;
+}
+
 extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
 {
   const thorin_params &p = d->p;
@@ -1468,6 +1565,7 @@ extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
     double ind[2], rrho[THORIN_MAXPLANETS], rcs[THORIN_MAXPLANETS];
     RCHK(thorin_gpu_forces(d, sys, d->MassTaper, ind, rrho, rcs));
     advance_from_disk(d, sys, dt, ind, rrho, rcs);
+    if (p.aerodynamic_drag) RCHK(thorin_gpu_drag(d, sys, dt));
     nbody_step(sys, dt);
     rotate_psys(sys, d->OmegaFrame * dt);
     int s = thorin_gpu_hydro(d, dt);

@@ -14,7 +14,9 @@ enum {
   SC_NEWDT = 0, SC_INVDTPEB, SC_DTSTELLAR, SC_INDX, SC_INDY, SC_ACC_DM, SC_ACC_DPX, SC_ACC_DPY, SC_RINGRHO,
   SC_MASS, SC_MOM, SC_ENER, SC_PMASS, SC_PMOM, SC_NORMRES0, SC_NORMRES,
   SC_PLANET_A = 32,           // 2 per planet: ax, ay (then the ring means of Sigma for DampingTW04)
-  SC_TORQUE = 56              // 2 per planet: ring means of Sigma either side of the planet (UpdateLog)
+  SC_TORQUE = 56,             // 2 per planet: ring means of Sigma either side of the planet (UpdateLog)
+  SC_GASACC = 80,             // dM, dPx, dPy of the gas accretion onto one planet
+  SC_DRAGCELL = 84            // 6 values of the planet's cell for the aerodynamic drag
 };
 enum { IS_NSUB = 0, IS_SOR_DONE, IS_SOR_NITER, IS_SOR_CHANGED, IS_CRASH, IS_COUNT };
 
@@ -76,6 +78,11 @@ struct ForceArgs {
   // vertical quadrature weights exp(-z_m^2 / 2H^2) at z_m = (m - 1/2) 3H/N,
   // which do not depend on H, and their sums (filled by aux_forces)
   double wq10[10], wq30[30], sig10, sig30;
+};
+
+struct GasAccArgs {           // one planet of AccreteOntoPlanets (Planet.c:34-166)
+  double Xp, Yp, Zp, RRoche, facc1, facc2, omega_frame;
+  int i_min, i_max, j_min, j_max;
 };
 
 struct AccArgs {
@@ -157,6 +164,10 @@ void aux_outer_source_mass(const DevGrid &g, double *rho, double *vr, double pen
 void aux_parametric_cooling(const DevGrid &g, const double *rho, const double *eint, const double *qplus,
                             const double *divv, const double *coolt, const double *qplusmed, double *enew, double dt,
                             double gm1, cudaStream_t s);
+void aux_gas_accrete(const DevGrid &g, double *dens, const double *vrad, const double *vtheta, const double *cs,
+                     const GasAccArgs &a, double *out, cudaStream_t s);
+void aux_drag_cell(const double *rho, const double *cs, const double *vrad, const double *vtheta, int l, int ns,
+                   double *out, cudaStream_t s);
 void aux_iso_eos(const DevGrid &g, const double *rho, const double *csr, double *cs, double *press, double *temper,
                  int set_cs, int set_press, int set_temper, cudaStream_t s);
 void aux_damp_peb(const DevGrid &g, double *pd, double *pvr, double *pvt, const int *rings, int nrings, double dt,

@@ -301,12 +301,6 @@ def derive(v: dict, *, sor_eps: float = SOREPS, sor_maxiters: int = SORMAXITERS,
 def check_supported(p: ThorinParams) -> None:
     """Raise for options outside the implemented hot path (fail loudly)."""
     bad = []
-    if p.accretion_rate > 1e-10:
-        bad.append("gas accretion onto planets (AccretionRate > 0)")
-    if p.prescribed_accretion:
-        bad.append("ParametricAccretion")
-    if p.aerodynamic_drag:
-        bad.append("AerodynamicDrag")
     if p.sloppy_cfl:
         bad.append("SloppyCFL (-c)")
     if bad:

@@ -299,6 +299,12 @@ int thorin_integrals_static(const double *rho, const double *vrad, const double 
                             const double *surf, const double *rinf, const double *rsup, const double *rmed,
                             int nrad, int nsec, double omega_frame, double *out, void *stream);
 
+/* AdvanceSystemFromDrag (Drag.c:97-119): velocity kicks of the planets that
+ * feel the disk from the Stokes drag of the gas in their own cell, for
+ * AerodynamicDrag YES.  thorin_gpu_algogas calls it after the disk's pull;
+ * a phase-API driver calls it after AdvanceSystemFromDisk. */
+int thorin_gpu_drag(thorin_disk *d, thorin_planets *sys, double dt);
+
 /* EquilPebbleDisk (Pebbles.c:54-60) on the gas state now on the device:
  * for runs that upload their gas from files before the pebbles are set up
  * (Init.c:144-148).  No-op without pebbles. */

@@ -89,6 +89,7 @@ typedef struct ora_disk {
   /* scalars carried between calls (file-static in the reference) */
   double PhysicalTime, PhysicalTimeInitial, MassTaper, OmegaFrame;
   double dt_stellar, invdtpeb_sq, invdtreb_sq, pebbulkdens, CV, SQRT_ADIABIND_INV;
+  double doubling;               /* ParametricAccretion's static doubling time */
   double indirect_x, indirect_y;
   double heatsrc[THORIN_MAXPLANETS]; int heatsrc_index[THORIN_MAXPLANETS]; int heatsrc_max;
   int cfl_count;                 /* ConditionCFL's static count  */
@@ -1658,6 +1659,172 @@ static void Heating1(ora_disk *d, double Mplanet, double dMplanet, double Xp, do
   d->heatsrc[k] += L * taper / d->Surf[i];
 }
 
+/* Kley's gas accretion (Planet.c:34-210): within 0.75 and 0.45 Roche radii
+ * the density loses the fractions dt*acc/3 and 2 dt*acc/3 of the column
+ * between the planet's height +/- the chord, integrated by the trapezoid
+ * rule refined to a relative precision of 1e-4 (qtrap, at most 16 levels). */
+#define QTRAPEPS 1.e-4
+#define QTRAPMAX 16
+static double rho_func(double z) { return exp(-z * z); }
+
+static double trapzd_g(double a, double b, int n, double *s)
+{
+  if (n == 1) return (*s = 0.5 * (b - a) * (rho_func(a) + rho_func(b)));
+  int it = 1;
+  for (int j = 1; j < n - 1; j++) it <<= 1;
+  double tnm = it, del = (b - a) / tnm, x = a + 0.5 * del, sum = 0.0;
+  for (int j = 1; j <= it; j++, x += del) sum += rho_func(x);
+  *s = 0.5 * (*s + (b - a) * sum / tnm);
+  return *s;
+}
+
+static double qtrap_g(double a, double b, double eps)
+{
+  double s = 0.0, olds = 0.0, st = 0.0;
+  for (int j = 1; j <= QTRAPMAX; j++) {
+    s = trapzd_g(a, b, j, &st);
+    if (j > 5)
+      if (fabs(s - olds) < eps * fabs(olds) || (s == 0.0 && olds == 0.0)) return s;
+    olds = s;
+  }
+  return s;
+}
+
+static void AccreteOntoPlanets(ora_disk *d, thorin_planets *sys, double dt)
+{
+  const thorin_params *p = &d->p;
+  int nr = d->nr, ns = d->ns;
+  double *dens = d->rho, *vrad = d->vrad, *vtheta = d->vtheta;
+  for (int k = 0; k < sys->nb; k++) {
+    if (!(sys->acc[k] > 1e-10)) continue;
+    double dMplanet = 0.0, dPxPlanet = 0.0, dPyPlanet = 0.0;
+    double facc = fabs(dt) * (sys->acc[k]);
+    double facc1 = 1.0 / 3.0 * facc, facc2 = 2.0 / 3.0 * facc, frac1 = 0.75, frac2 = 0.45;
+    facc1 = (facc1 < 1.0) ? facc1 : 1.0;
+    facc2 = (facc2 < 1.0) ? facc2 : 1.0;
+    double Xplanet = sys->x[k], Yplanet = sys->y[k], Zplanet = sys->z[k];
+    double VXplanet = sys->vx[k], VYplanet = sys->vy[k], Mplanet = sys->mass[k];
+    double Rperp = sqrt(Xplanet * Xplanet + Yplanet * Yplanet);
+    double Rplanet = sqrt(Xplanet * Xplanet + Yplanet * Yplanet + Zplanet * Zplanet);
+    double RRoche = pow((1.0 / 3.0 * Mplanet * d->MassTaper), (1.0 / 3.0)) * Rplanet;
+    int i_min = 0, i_max = nr - 1;
+    while ((d->Rsup[i_min] < Rperp - RRoche) && (i_min < nr)) i_min++;
+    while ((d->Rinf[i_max] > Rperp + RRoche) && (i_max > 0)) i_max--;
+    double angle = atan2(Yplanet, Xplanet);
+    int j_min = (int)((double)ns / 2.0 / PI * (angle - 2.0 * RRoche / Rperp));
+    int j_max = (int)((double)ns / 2.0 / PI * (angle + 2.0 * RRoche / Rperp));
+    double PxPlanet = Mplanet * VXplanet, PyPlanet = Mplanet * VYplanet;
+    for (int i = i_min; i <= i_max; i++)
+      for (int j = j_min; j <= j_max; j++) {
+        int jf = j;
+        while (jf < 0) jf += ns;
+        while (jf >= ns) jf -= ns;
+        int l = jf + i * ns, lip = l + ns, ljp = l + 1;
+        if (jf == ns - 1) ljp = i * ns;
+        double xc = d->abscissa[l], yc = d->ordinate[l];
+        double dx = Xplanet - xc, dy = Yplanet - yc, distance = sqrt(dx * dx + dy * dy);
+        double vtcell = 0.5 * (vtheta[l] + vtheta[ljp]) + d->Rmed[i] * d->OmegaFrame;
+        double vrcell = 0.5 * (vrad[l] + vrad[lip]);
+        double vxcell = (vrcell * xc - vtcell * yc) / d->Rmed[i];
+        double vycell = (vrcell * yc + vtcell * xc) / d->Rmed[i];
+        double H = d->cs[l] * d->OmegaInv[i] * d->SQRT_ADIABIND_INV;
+        if (distance < frac1 * RRoche) {
+          double dz = sqrt(pow(frac1 * RRoche, 2) - pow(distance, 2));
+          double z1 = Zplanet - dz, z2 = Zplanet + dz;
+          double factor = qtrap_g(z1 / (sqrt(2.0) * H), z2 / (sqrt(2.0) * H), QTRAPEPS);
+          factor *= 1.0 / (sqrt(2.0 * PI) * H);
+          double deltaM = facc1 * factor * dens[l] * d->Surf[i];
+          if (i < 0) deltaM = 0.0;                              /* Zero_or_active = 0 */
+          if (i >= nr) deltaM = 0.0;                            /* Max_or_active = nr */
+          dens[l] *= (1.0 - facc1 * factor);
+          dPxPlanet += deltaM * vxcell;
+          dPyPlanet += deltaM * vycell;
+          dMplanet += deltaM;
+        }
+        if (distance < frac2 * RRoche) {
+          double dz = sqrt(pow(frac2 * RRoche, 2) - pow(distance, 2));
+          double z1 = Zplanet - dz, z2 = Zplanet + dz;
+          double factor = qtrap_g(z1 / (sqrt(2.0) * H), z2 / (sqrt(2.0) * H), QTRAPEPS);
+          factor *= 1.0 / (sqrt(2.0 * PI) * H);
+          double deltaM = facc2 * factor * dens[l] * d->Surf[i];
+          if (i < 0) deltaM = 0.0;
+          if (i >= nr) deltaM = 0.0;
+          dens[l] *= (1.0 - facc2);
+          dPxPlanet += deltaM * vxcell;
+          dPyPlanet += deltaM * vycell;
+          dMplanet += deltaM;
+        }
+      }
+    if (p->gas_accret_heating) Heating1(d, Mplanet, dMplanet, Xplanet, Yplanet, dt, k);
+    PxPlanet += dPxPlanet;
+    PyPlanet += dPyPlanet;
+    Mplanet += dMplanet;
+    if (sys->feel_disk[k]) {
+      sys->vx[k] = PxPlanet / Mplanet;
+      sys->vy[k] = PyPlanet / Mplanet;
+    }
+    sys->mass[k] = Mplanet;
+  }
+}
+
+/* ParametricAccretion (Pebbles.c:806-828): mass doubling every
+ * PARAMETRICACCRETION kyr; the doubling time is fixed at the first call. */
+static void ParametricAccretion(ora_disk *d, thorin_planets *sys, double dt)
+{
+  const thorin_params *p = &d->p;
+  if (d->doubling == 0.0) d->doubling = p->parametric_accretion * 1000.0 * 2.0 * PI;
+  if (p->accret_heating) d->heatsrc_max = sys->nb;
+  for (int k = 0; k < sys->nb; k++) {
+    double Mplanet = sys->mass[k];
+    double dMplanet = Mplanet * dt / d->doubling;
+    if (p->accret_heating) Heating1(d, Mplanet, dMplanet, sys->x[k], sys->y[k], dt, k);
+    sys->mass[k] = Mplanet + dMplanet;
+  }
+}
+
+/* StokesDrag + AdvanceSystemFromDrag (Drag.c:17-119): drag of the gas in
+ * the planet's cell (the cell's v_theta neighbour is l+1 without wrapping,
+ * as in the reference). */
+#define DRAGCOEFF 0.48
+static void AdvanceSystemFromDrag(ora_disk *d, thorin_planets *sys, double dt)
+{
+  const thorin_params *p = &d->p;
+  int nr = d->nr, ns = d->ns;
+  for (int k = 0; k < sys->nb; k++) {
+    if (!sys->feel_disk[k]) continue;
+    double m = sys->mass[k], x = sys->x[k], y = sys->y[k], z = sys->z[k];
+    double vx = sys->vx[k], vy = sys->vy[k], vz = sys->vz[k], ax = 0.0, ay = 0.0, az = 0.0;
+    double Rperp = sqrt(x * x + y * y);
+    if (Rperp >= d->Rinf[0] && Rperp <= d->Rsup[nr - 1]) {
+      int i = 0;
+      while (d->Rsup[i] < Rperp) i++;
+      double ang = atan2(y, x);
+      if (ang < 0.0) ang += 2.0 * PI;
+      int j = (int)floor((double)ns / 2.0 / PI * ang + 0.5);
+      if (j == ns) j = 0;
+      int l = j + i * ns, lip = l + ns, ljp = l + 1;
+      double xc = d->abscissa[l], yc = d->ordinate[l];
+      double vtcell = 0.5 * (d->vtheta[l] + d->vtheta[ljp]) + d->Rmed[i] * d->OmegaFrame;
+      double vrcell = 0.5 * (d->vrad[l] + d->vrad[lip]);
+      double vxcell = (vrcell * xc - vtcell * yc) / d->Rmed[i];
+      double vycell = (vrcell * yc + vtcell * xc) / d->Rmed[i];
+      double vzcell = 0.0;
+      double H = d->cs[l] * d->OmegaInv[i] * d->SQRT_ADIABIND_INV;
+      double factor = rho_func(z / (sqrt(2.0) * H));
+      factor *= 1.0 / (sqrt(2.0 * PI) * H);
+      double plrho = p->planetary_density / RHO2CGS;
+      double plradius = pow(3.0 * m / (4.0 * PI * plrho), 1.0 / 3.0);
+      double dvx = vx - vxcell, dvy = vy - vycell, dvz = vz - vzcell;
+      double dvsq = dvx * dvx + dvy * dvy + dvz * dvz;
+      double tmp = -0.5 * DRAGCOEFF * PI * plradius * plradius / m * factor * d->rho[l] * dvsq * 1.0 / sqrt(dvsq);
+      ax = tmp * dvx; ay = tmp * dvy; az = tmp * dvz;
+    }
+    sys->vx[k] += dt * ax;
+    sys->vy[k] += dt * ay;
+    sys->vz[k] += dt * az;
+  }
+}
+
 static void AccretePebblesOntoPlanets(ora_disk *d, thorin_planets *sys, double dt)   /* :353-539 */
 {
   const thorin_params *p = &d->p;
@@ -2195,10 +2362,13 @@ int ora_algogas(ora_disk *d, thorin_planets *sys)
     int n = ConditionCFL(d, DT - dtemp);
     dt = (DT - dtemp) / (double)n;
     for (int k = 0; k < sys->nb; k++) { d->heatsrc[k] = 0.0; d->heatsrc_index[k] = -1; }   /* InitHeating */
+    AccreteOntoPlanets(d, sys, dt);
+    if (p->prescribed_accretion) ParametricAccretion(d, sys, dt);
     if (p->pebbles) { AccretePebblesOntoPlanets(d, sys, dt); EvaporatePebbles(d, dt); }
     dtemp += dt;
     FillForcesArrays(d, sys);
     AdvanceSystemFromDisk(d, sys, dt);
+    if (p->aerodynamic_drag) AdvanceSystemFromDrag(d, sys, dt);
     AdvanceSystemNbody(sys, dt);
     RotatePsys(sys, d->OmegaFrame * dt);
     ApplyBoundaryCondition(d, dt);

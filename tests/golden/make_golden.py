@@ -52,6 +52,13 @@ CASES = {
     "nonrefl_24x72": ("disk0", 24, 72, 6, 2, "InnerBoundary NONREFLECTING\n", True),
     "srcmass_24x72": ("disk0", 24, 72, 6, 2, "OuterSourceMass YES\n", True),
     "cooling_24x72": ("disk0", 24, 72, 6, 2, "CoolingTime 10.0\n", True),
+    # planets: a Jupiter-mass planet accreting gas (Kley), a pebble-disk embryo
+    # growing at a prescribed rate, and a small body braked by gas drag
+    "gasacc_24x72": ("disk0", 24, 72, 6, 2, "AccretionRate 1.0\nPlanetsFeelDisk YES\n", True,
+                     (1.0e-3, 0.0, 0.0, 1.05, 0.0, 0.0, 0.0, 0.0, 0.0)),
+    "paracc_32x96": ("disk1", 32, 96, 6, 2, "ParametricAccretion 10.0\n", True, None),
+    "drag_24x72": ("disk0", 24, 72, 6, 2, "AerodynamicDrag YES\nPlanetsFeelDisk YES\n", True,
+                   (1.0e-7, 0.0, 0.0, 1.05, 0.05, 0.0, 0.0, 0.0, 0.0)),
 }
 GAS = ["dens", "vrad", "vtheta", "temper"]
 PEB = ["pebbledens", "pebblevrad", "pebblevtheta"]
@@ -96,7 +103,8 @@ def parse_log(text):
 
 
 def make_case(name):
-    kind, nr, ns, ntot, ninterm, extra, full = CASES[name]
+    kind, nr, ns, ntot, ninterm, extra, full = CASES[name][:7]
+    planet_override = CASES[name][7] if len(CASES[name]) > 7 else None
     work = tempfile.mkdtemp(prefix="thorin_golden_")
     try:
         out = os.path.join(work, "out")
@@ -105,6 +113,8 @@ def make_case(name):
         par = re.sub(r"Ninterm \d+", f"Ninterm {ninterm}", par)
         par = par.replace("OutputDir out", f"OutputDir {out}")
         planet = workloads.PLANET1 if kind == "disk1" else workloads.PLANET0
+        if planet_override is not None:
+            planet = planet_override
         with open(os.path.join(work, "planet.cfg"), "w") as f:
             f.write("Embryo1 " + " ".join(repr(v) for v in planet) + "\n")
         par += f"PlanetConfig {os.path.join(work, 'planet.cfg')}\n"

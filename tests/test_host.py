@@ -66,19 +66,23 @@ def test_read_inpar_case_insensitive_and_defaults():
         P.read_inpar(text + "\nNoSuchKey 3\n")
 
 
-@pytest.mark.parametrize("key,val,msg", [("ParametricAccretion", "1e-5", "ParametricAccretion"),
-                                         ("AccretionRate", "1.0", "gas accretion"),
-                                         ("AerodynamicDrag", "YES", "AerodynamicDrag")])
-def test_unsupported_rejected(lib, key, val, msg):
-    text = workloads.inpar_text("disk1", 32, 96) + f"\n{key} {val}\n"
-    p = P.derive(P.read_inpar(text))
-    with pytest.raises(NotImplementedError, match=msg):
+def test_unsupported_rejected(lib):
+    """SloppyCFL (-c) is outside the GPU path: refused by the host checks and
+    by thorin_gpu_create before any CUDA call."""
+    p = P.derive(P.read_inpar(workloads.inpar_text("disk1", 32, 96)), sloppy_cfl=True)
+    with pytest.raises(NotImplementedError, match="SloppyCFL"):
         P.check_supported(p)
     h = C.c_void_p()
     rc = lib.thorin_gpu_create(C.byref(p), C.byref(h))
     assert rc == 1                                  # THORIN_ERR_ARG, before any CUDA call
     assert not h.value
-    assert msg in lib.thorin_gpu_last_error().decode()
+    assert "SloppyCFL" in lib.thorin_gpu_last_error().decode()
+
+
+def test_corotating_frame_refused():
+    text = workloads.inpar_text("disk0", 24, 72) + "\nFrame COROTATING\n"
+    with pytest.raises(ValueError, match="Corotating"):
+        P.derive(P.read_inpar(text))
 
 
 def test_bad_grid_rejected(lib):

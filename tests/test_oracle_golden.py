@@ -15,7 +15,7 @@ from fargo_thorin_gb300 import workloads
 
 CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "iso_24x72", "iso_peb_32x96",
          "dampinit_24x72", "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
-         "cooling_24x72"]
+         "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72"]
 
 
 def _run(name, force_planet=True):
