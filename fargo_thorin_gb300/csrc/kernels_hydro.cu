@@ -704,7 +704,7 @@ __global__ void k_energy_from_t(DevGrid g, const double *__restrict__ rho, doubl
 __global__ void k_rad_prep(DevGrid g, int nq, const double *__restrict__ rho, const double *__restrict__ vr,
                            const double *__restrict__ vt, const double *__restrict__ energy, double *rmp, double *rmm,
                            double *tmp_, double *tmm, double *w0, double *w1, double *w2, double *w3, double *we,
-                           double *wr, double omega_frame)
+                           double *wr, double omega_frame, const double *__restrict__ label, double *ext, double *wx)
 {
   const int ns = g.ns;
   CELL_LOOP_2D
@@ -717,8 +717,22 @@ __global__ void k_rad_prep(DevGrid g, int nq, const double *__restrict__ rho, co
   rmp[l] = a; rmm[l] = b; tmp_[l] = c; tmm[l] = d;
   const double rcp = div_fast(1.0, r + 1e-20);    // quotients Q / (rho + 1e-20) as products
   w0[l] = a * rcp; w1[l] = b * rcp; w2[l] = c * rcp; w3[l] = d * rcp;
-  if (nq == 6) we[l] = energy[l] * rcp;
+  if (energy) we[l] = energy[l] * rcp;
+  if (label) {                              // ComputeExtQty (TransportEuler.c:177-195)
+    const double x = r * label[l];
+    ext[l] = x;
+    wx[l] = x * rcp;
+  }
   wr[l] = r * rcp;
+}
+
+// ComputeSpeQty (TransportEuler.c:197-215): the tracer back from rho*label.
+__global__ void k_label_from_ext(DevGrid g, const double *__restrict__ rho, const double *__restrict__ ext,
+                                 double *__restrict__ label)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  label[l] = div_fast(ext[l], rho[l]);
 }
 
 __device__ __forceinline__ double vl_slope_r(const DevGrid &g, const double *q, int i, int l)
@@ -732,7 +746,7 @@ __device__ __forceinline__ double vl_slope_r(const DevGrid &g, const double *q, 
 }
 
 
-__global__ void k_rad_slope(DevGrid g, PtrPack7 pk)
+__global__ void k_rad_slope(DevGrid g, PtrPack8 pk)
 {
   const int ns = g.ns;
   CELL_LOOP_2D
@@ -741,7 +755,7 @@ __global__ void k_rad_slope(DevGrid g, PtrPack7 pk)
 
 // ComputeStarRad (TransportEuler.c:232-273): upwind face values at the inner
 // face of ring i (faces 0 and nr are zero).
-__global__ void k_rad_face(DevGrid g, PtrPack7 w, PtrPack7 dq, const double *__restrict__ vr, double dt)
+__global__ void k_rad_face(DevGrid g, PtrPack8 w, PtrPack8 dq, const double *__restrict__ vr, double dt)
 {
   const int ns = g.ns, nr = g.nr;
   CELL_LOOP_2D
@@ -760,8 +774,8 @@ __global__ void k_rad_face(DevGrid g, PtrPack7 w, PtrPack7 dq, const double *__r
 }
 
 // VanLeerRadial update (TransportEuler.c:384-415).
-__global__ void k_rad_update(DevGrid g, PtrPack7 qf, const double *__restrict__ rhos, const double *__restrict__ vr,
-                             PtrPack7 io, double dt)
+__global__ void k_rad_update(DevGrid g, PtrPack8 qf, const double *__restrict__ rhos, const double *__restrict__ vr,
+                             PtrPack8 io, double dt)
 {
   const int ns = g.ns;
   CELL_LOOP_2D
@@ -1098,60 +1112,67 @@ void hydro_energy_from_t(const DevGrid &g, const double *rho, double *T, double 
 // pebbles).  Scratch: 20 fields.  On return the caller's rho/energy pointers
 // are swapped with the updated buffers and vr/vt hold the new velocities.
 
-void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, double **energy, const TransportScratch &S,
-                     double dt, double omega_frame, int fast, int damp_vrad, double drin, double drout, double *temper,
-                     double *cs, double gm1, double gg1, cudaStream_t s)
+void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, double **energy, double *label,
+                     const TransportScratch &S, double dt, double omega_frame, int fast, int damp_vrad, double drin,
+                     double drout, double *temper, double *cs, double gm1, double gg1, cudaStream_t s)
 {
   const int ns = g.ns, nr = g.nr;
-  const int nq = energy ? 6 : 5;
-  // quantity order for the radial step: rmp, rmm, tmp, tmm, [e], rho
+  // transported quantities in the reference's order: rmp, rmm, tmp, tmm,
+  // [e], [rho*label], rho.  Quotient buffers: w[0..3] momenta, w[4] energy,
+  // w[6] tracer, w[5] rho.
+  int qi[7], nq = 0;
+  for (int q = 0; q < 4; q++) qi[nq++] = q;
+  if (energy) qi[nq++] = 4;
+  if (label) qi[nq++] = 6;
+  qi[nq++] = 5;
   k_rad_prep<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, nq, *rho, vr, vt, energy ? *energy : nullptr, S.mom[0], S.mom[1],
                                                S.mom[2], S.mom[3], S.w[0], S.w[1], S.w[2], S.w[3], S.w[4], S.w[5],
-                                               omega_frame);
+                                               omega_frame, label, S.ext, S.w[6]);
   g_thorin_launches++;
-  // slopes of the quotients (0..3, energy 4 if present, rho-quotient 5) and of rho (6)
-  PtrPack7 sl;
+  // slopes of the quotients and of rho (slot 7)
+  PtrPack8 sl;
   int n = 0;
-  for (int q = 0; q < 4; q++) { sl.src[n] = S.w[q]; sl.dst[n] = S.d[q]; n++; }
-  if (nq == 6) { sl.src[n] = S.w[4]; sl.dst[n] = S.d[4]; n++; }
-  sl.src[n] = S.w[5]; sl.dst[n] = S.d[5]; n++;
-  sl.src[n] = *rho; sl.dst[n] = S.d[6]; n++;
+  for (int k = 0; k < nq; k++) { sl.src[n] = S.w[qi[k]]; sl.dst[n] = S.d[qi[k]]; n++; }
+  sl.src[n] = *rho; sl.dst[n] = S.d[7]; n++;
   sl.n = n;
   k_rad_slope<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, sl);
   g_thorin_launches++;
   // faces: quotients and rho
-  PtrPack7 wf, dqf;
+  PtrPack8 wf, dqf;
   n = 0;
-  for (int q = 0; q < 4; q++) { wf.src[n] = S.w[q]; wf.dst[n] = S.f[q]; dqf.src[n] = S.d[q]; n++; }
-  if (nq == 6) { wf.src[n] = S.w[4]; wf.dst[n] = S.f[4]; dqf.src[n] = S.d[4]; n++; }
-  wf.src[n] = S.w[5]; wf.dst[n] = S.f[5]; dqf.src[n] = S.d[5]; n++;
-  wf.src[n] = *rho; wf.dst[n] = S.f[6]; dqf.src[n] = S.d[6]; n++;
+  for (int k = 0; k < nq; k++) { wf.src[n] = S.w[qi[k]]; wf.dst[n] = S.f[qi[k]]; dqf.src[n] = S.d[qi[k]]; n++; }
+  wf.src[n] = *rho; wf.dst[n] = S.f[7]; dqf.src[n] = S.d[7]; n++;
   wf.n = dqf.n = n;
   k_rad_face<<<grid2d(ns, nr + 1, BX), BX, 0, s>>>(g, wf, dqf, vr, dt);
   g_thorin_launches++;
   // flux divergence into the quotient buffers, which are free by now
-  PtrPack7 qf, io;
+  PtrPack8 qf, io;
   n = 0;
-  for (int q = 0; q < 4; q++) { qf.src[n] = S.f[q]; io.src[n] = S.mom[q]; io.dst[n] = S.w[q]; n++; }
-  if (nq == 6) { qf.src[n] = S.f[4]; io.src[n] = *energy; io.dst[n] = S.w[4]; n++; }
-  qf.src[n] = S.f[5]; io.src[n] = *rho; io.dst[n] = S.w[5]; n++;
+  for (int k = 0; k < nq; k++) {
+    const int q = qi[k];
+    qf.src[n] = S.f[q];
+    io.src[n] = (q < 4) ? S.mom[q] : (q == 4) ? *energy : (q == 6) ? S.ext : *rho;
+    io.dst[n] = S.w[q];
+    n++;
+  }
   qf.n = io.n = n;
-  k_rad_update<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, qf, S.f[6], vr, io, dt);
+  k_rad_update<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, qf, S.f[7], vr, io, dt);
   g_thorin_launches++;
-  // azimuthal step on (rmp, rmm, tmp, tmm, [e], rho) back into the momenta,
-  // the new energy and the new density
+  // azimuthal step back into the momenta, the new energy, the tracer and
+  // the new density
   k_azi_rings<<<(nr * 32 + 255) / 256, 256, 0, s>>>(g, vt, dt, S.nshift, S.vmed, S.vtemp);
   g_thorin_launches++;
   AziIO az;
-  for (int q = 0; q < n; q++) az.src[q] = io.dst[q];
-  n = 0;
-  for (int q = 0; q < 4; q++) az.dst[n++] = S.mom[q];
-  if (nq == 6) az.dst[n++] = S.e_new;
-  az.dst[n++] = S.rho_new;
-  az.n = n;
+  for (int k = 0; k < nq; k++) {
+    const int q = qi[k];
+    az.src[k] = io.dst[k];
+    az.dst[k] = (q < 4) ? S.mom[q] : (q == 4) ? S.e_new : (q == 6) ? S.ext_new : S.rho_new;
+  }
+  az.n = nq;
   const int T = azi_block(ns);
   const dim3 grid((ns + T - 2 * AZ_HALO - 1) / (T - 2 * AZ_HALO), nr);
-  if (nq == 6) k_azimuthal<6><<<grid, T, 0, s>>>(g, az, vt, dt, fast, S.nshift, S.vmed, S.vtemp);
+  if (nq == 7) k_azimuthal<7><<<grid, T, 0, s>>>(g, az, vt, dt, fast, S.nshift, S.vmed, S.vtemp);
+  else if (nq == 6) k_azimuthal<6><<<grid, T, 0, s>>>(g, az, vt, dt, fast, S.nshift, S.vmed, S.vtemp);
   else k_azimuthal<5><<<grid, T, 0, s>>>(g, az, vt, dt, fast, S.nshift, S.vmed, S.vtemp);
   g_thorin_launches++;
   // velocities from the transported momenta
@@ -1159,6 +1180,10 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
                                                  omega_frame, damp_vrad, dt, drin, drout,
                                                  energy ? S.e_new : nullptr, energy ? temper : nullptr, cs, gm1, gg1);
   g_thorin_launches++;
+  if (label) {
+    k_label_from_ext<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, S.rho_new, S.ext_new, label);
+    g_thorin_launches++;
+  }
 }
 
 

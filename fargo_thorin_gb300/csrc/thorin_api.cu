@@ -109,6 +109,7 @@ struct thorin_disk {
   double *cs, *temper, *qplus, *qminus, *opacity, *divv, *trr, *trp, *tpp, *agr, *agt, *pagr, *pagt, *dcen;
   double *ml, *mlip, *mlim, *mljp, *mljm, *rhs, *sor_cw, *tbackup, *flaring, *qirr;   // sor_cw = omega / ml
   double *press = nullptr;   // pressure field of isothermal runs (formed at the start of each substep)
+  double *label = nullptr;   // passive tracer (LabelAdvection)
   double *pdens, *pvrad, *pvtheta, *psize, *tau, *paccr, *pacct, *gaccr, *gacct, *dragr, *dragt, *macc;
   double *t_rho_gas, *t_e_gas, *t_rho_peb;
   TransportScratch ts;
@@ -353,7 +354,18 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   }
   for (int q = 0; q < 4; q++) RCHK(dfield(d, &d->ts.mom[q]));
   for (int q = 0; q < 6; q++) RCHK(dfield(d, &d->ts.w[q]));
-  for (int q = 0; q < 7; q++) { RCHK(dfield(d, &d->ts.d[q])); RCHK(dfield(d, &d->ts.f[q])); }
+  for (int q = 0; q < 8; q++) {
+    if (q == 6 && !d->p.label_advection) { d->ts.d[q] = d->ts.f[q] = nullptr; continue; }
+    RCHK(dfield(d, &d->ts.d[q]));
+    RCHK(dfield(d, &d->ts.f[q]));
+  }
+  d->ts.w[6] = d->ts.ext = d->ts.ext_new = nullptr;
+  if (d->p.label_advection) {
+    RCHK(dfield(d, &d->ts.w[6]));
+    RCHK(dfield(d, &d->ts.ext));
+    RCHK(dfield(d, &d->ts.ext_new));
+    RCHK(dfield(d, &d->label));
+  }
   RCHK(dalloc(d, (void **)&d->nshift, n1 * sizeof(int)));
   d->ts.nshift = d->nshift;
   d->ts.vmed = d->ring[R_VMED];
@@ -486,6 +498,7 @@ static double *field_ptr(thorin_disk *d, int id)
   case THORIN_DIVV: return d->divv;
   case THORIN_OPACITY: return d->opacity;
   case THORIN_QMINUS: return d->qminus;
+  case THORIN_LABEL: return d->label;
   }
   return nullptr;
 }
@@ -733,6 +746,41 @@ extern "C" int thorin_gpu_init_default(thorin_disk *d)
     RCHK(upload_ring(d, R_COOLT, ct));
     RCHK(upload_ring(d, R_QPLUSMED, qm));
   }
+  // -b: v_theta from the radial balance of pressure, gravity and rotation
+  // (InitGasVelocity, Pframeforce.c:666-688, with ConstructSequence :605-617)
+  std::vector<double> vt_cent(nr + 2, 0.0);
+  if (p.centrifugal_balance) {
+    std::vector<double> gp(nr + 2, 0.0), vt_int(nr + 2, 0.0);
+    for (int i = 0; i < nr; i++) {
+      double acc = 0.0;
+      for (int j = 0; j < ns; j++) {
+        const int l = j + i * ns;
+        acc += p.energy_eq ? (p.adiabind - 1.0) * e[l] : rho[l] * cs[l] * cs[l];
+      }
+      gp[i] = acc / (double)ns;
+    }
+    const std::vector<double> &GR = d->GlobalRmed;
+    for (int i = 1; i < nr; i++) {
+      vt_int[i] = (gp[i] - gp[i - 1]) / (.5 * (sigma(GR[i]) + sigma(GR[i - 1]))) / (GR[i] - GR[i - 1]) +
+                  1.0 * (1.0 / GR[i - 1] - 1.0 / GR[i]) / (GR[i] - GR[i - 1]);
+      vt_int[i] = sqrt(vt_int[i] * d->Radii[i]) - d->Radii[i] * d->OmegaFrame;
+    }
+    auto construct = [&](void) {
+      for (int i = 1; i < nr; i++) vt_cent[i] = 2.0 * vt_int[i] - vt_cent[i - 1];
+      double lapl = 0.0;
+      for (int i = 1; i < nr - 1; i++) lapl += fabs(vt_cent[i + 1] + vt_cent[i - 1] - 2.0 * vt_cent[i]);
+      return lapl;
+    };
+    double t1 = vt_cent[0] = vt_int[1] + .75 * (vt_int[1] - vt_int[2]);
+    const double r1 = construct();
+    vt_cent[0] += .25 * (vt_int[1] - vt_int[2]);
+    const double t2 = vt_cent[0];
+    const double r2 = construct();
+    t1 = t1 - r1 / (r2 - r1) * (t2 - t1);
+    vt_cent[0] = t1;
+    construct();
+    vt_cent[nr] = vt_cent[nr - 1];
+  }
   // InitGasVelocity (Pframeforce.c:696-750)
   for (int i = 0; i <= nr; i++) {
     double r, ri;
@@ -746,6 +794,7 @@ extern "C" int thorin_gpu_init_default(thorin_disk *d)
       const double csl = (i == nr) ? 0.0 : cs[l];   // SoundSpeed row nrad is never set (zero)
       vt[l] = omega * r * sqrt(1.0 - csl * csl * r / p.adiabind);
       vt[l] -= d->OmegaFrame * r;
+      if (p.centrifugal_balance) vt[l] = vt_cent[i];
       vr[l] = p.imposed_disk_drift * p.sigma0 / d->SigmaInf[i] / ri;
       if (p.damp_flux) {                   // steady inflow of GASFLUX (Pframeforce.c:735-740)
         const double rhoinf = (i == 0) ? d->SigmaMed[i] - 0.5 * (d->SigmaMed[i + 1] - d->SigmaMed[i])
@@ -771,6 +820,13 @@ extern "C" int thorin_gpu_init_default(thorin_disk *d)
   CUCHK(cudaMemcpyAsync(d->energy, e.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
   CUCHK(cudaMemcpyAsync(d->vrad, vr.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
   CUCHK(cudaMemcpyAsync(d->vtheta, vt.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  std::vector<double> lab;
+  if (p.label_advection) {                 // InitLabel (Init.c:59-72), rows 0..nrad
+    lab.assign(n, 0.0);
+    for (int i = 0; i <= nr; i++)
+      for (int j = 0; j < ns; j++) lab[j + i * ns] = (d->Rmed[i] - p.rmin) / (p.rmax - p.rmin);
+    CUCHK(cudaMemcpyAsync(d->label, lab.data(), n * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  }
   CUCHK(cudaStreamSynchronize(d->s));
   if (p.pebbles) RCHK(init_pebbles_host(d, rho, vr, vt, cs));
   RCHK(upload_all_rings(d));
@@ -1385,8 +1441,9 @@ static void transport_fluid(thorin_disk *d, double **rho, double *vr, double *vt
   // the velocity kernel when it is the only boundary condition
   const thorin_params &p = d->p;
   const int fused = p.damping && p.damp_vrad && !(p.open_inner || p.open_outer || p.non_reflecting || p.outer_source_mass);
-  hydro_transport(d->g, rho, vr, vt, energy, S, dt, d->OmegaFrame, p.fast_transport, gas && fused, d->drin, d->drout,
-                  gas ? d->temper : nullptr, d->cs, d->gm1, d->gg1, d->s);
+  hydro_transport(d->g, rho, vr, vt, energy, (gas && p.label_advection) ? d->label : nullptr, S, dt, d->OmegaFrame,
+                  p.fast_transport, gas && fused, d->drin, d->drout, gas ? d->temper : nullptr, d->cs, d->gm1, d->gg1,
+                  d->s);
   std::swap(*rho, *rho_scratch);
   if (energy) std::swap(*energy, d->t_e_gas);
 }

@@ -42,13 +42,14 @@ struct SorCtl {
 struct TransportScratch {
   double *mom[4];          // RadMomP, RadMomM, ThetaMomP, ThetaMomM (updated in place)
   double *rho_new, *e_new;
-  double *w[6], *d[7], *f[7];
+  double *ext, *ext_new;   // rho * label before and after the transport (LabelAdvection)
+  double *w[7], *d[8], *f[8];
   int *nshift;
   double *vmed, *vtemp;
 };
 
-struct PtrPack7 { const double *src[7]; double *dst[7]; int n; };
-struct AziIO { const double *src[6]; double *dst[6]; int n; };   // index n-1 is the density
+struct PtrPack8 { const double *src[8]; double *dst[8]; int n; };
+struct AziIO { const double *src[7]; double *dst[7]; int n; };   // index n-1 is the density
 
 struct ViscParams {
   double viscosity, alpha, alpha_mri, alpha_dead, tmri, twidth, t2si;
@@ -137,9 +138,9 @@ void hydro_sor_sweeps(const DevGrid &g, double *T, const double *ml, const doubl
                       const double *mljp, const double *mljm, const double *rhs, const double *cw, const SorCtl &c,
                       double eps, int first, int count, int maxiters, cudaStream_t s);
 void hydro_energy_from_t(const DevGrid &g, const double *rho, double *T, double *enew, cudaStream_t s);
-void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, double **energy, const TransportScratch &S,
-                     double dt, double omega_frame, int fast, int damp_vrad, double drin, double drout, double *temper,
-                     double *cs, double gm1, double gg1, cudaStream_t s);
+void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, double **energy, double *label,
+                     const TransportScratch &S, double dt, double omega_frame, int fast, int damp_vrad, double drin,
+                     double drout, double *temper, double *cs, double gm1, double gg1, cudaStream_t s);
 
 // kernels_aux.cu
 void aux_ring_means(const DevGrid &g, const double *f0, double *o0, const double *f1, double *o1, int ring0, int nrings,

@@ -160,7 +160,8 @@ class ThorinParams(C.Structure):
         ("fragment_factor", C.c_double), ("fragment_threshold", C.c_double), ("fragment_alpha", C.c_double),
         ("evaporation_rate", C.c_double), ("evaporation_temperature", C.c_double), ("heating_delay", C.c_int),
         ("parametric_accretion", C.c_double), ("prescribed_accretion", C.c_int),
-        ("sor_eps", C.c_double), ("sor_maxiters", C.c_int),
+        ("sor_eps", C.c_double), ("sor_maxiters", C.c_int), ("centrifugal_balance", C.c_int),
+        ("label_advection", C.c_int),
     ]
 
     def as_dict(self):
@@ -206,7 +207,7 @@ def _yes(s: str, ch: str) -> bool:
 
 
 def derive(v: dict, *, sor_eps: float = SOREPS, sor_maxiters: int = SORMAXITERS,
-           scaling_factor: float = 1.0, sloppy_cfl: bool = False) -> ThorinParams:
+           scaling_factor: float = 1.0, sloppy_cfl: bool = False, centrifugal_balance: bool = False) -> ThorinParams:
     """Build thorin_params from parsed variables with the switch logic of
     src_main/Interpret.c:149-265."""
     p = ThorinParams()
@@ -295,6 +296,8 @@ def derive(v: dict, *, sor_eps: float = SOREPS, sor_maxiters: int = SORMAXITERS,
     p.parametric_accretion = v["PARAMETRICACCRETION"]
     p.prescribed_accretion = int(p.parametric_accretion > 0.0)
     p.sor_eps, p.sor_maxiters = sor_eps, sor_maxiters
+    p.centrifugal_balance = int(centrifugal_balance)
+    p.label_advection = int(_yes(v["LABELADVECTION"], "Y"))
     return p
 
 

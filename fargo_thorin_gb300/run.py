@@ -28,8 +28,7 @@ in for REBOUND; their state at each output goes to nbody.state<N>.dat
 (PhysicalTime, then one line per planet: mass gas solid x y z vx vy vz),
 which ``-s N`` reads back where the reference reads its REBOUND binary
 nbody.simulation<N>.dat (ReboundInterface.c:211-259).  Options outside the
-GPU path (label advection, Qbalance, torque maps, custom radii.dat) are
-refused.
+GPU path (Qbalance, torque maps, custom radii.dat) are refused.
 """
 from __future__ import annotations
 
@@ -44,7 +43,8 @@ from . import params as P
 from . import workloads
 
 FIELD = {"dens": 0, "vrad": 1, "vtheta": 2, "energy": 3, "pebbledens": 4, "pebblevrad": 5, "pebblevtheta": 6,
-         "pebblesize": 7, "temper": 8, "soundspeed": 9, "pebblestokes": 11, "qplus": 12, "divv": 13, "opacity": 14}
+         "pebblesize": 7, "temper": 8, "soundspeed": 9, "pebblestokes": 11, "qplus": 12, "divv": 13, "opacity": 14,
+         "label": 16}
 
 
 def _yes(s) -> bool:
@@ -71,8 +71,6 @@ class Run:
         os.makedirs(self.out, exist_ok=True)
         if os.path.exists(self.out + "radii.dat"):
             raise NotImplementedError("a custom radii.dat grid is not supported by the GPU path")
-        if _yes(self.v["LABELADVECTION"]):
-            raise NotImplementedError("label advection is not supported by the GPU path")
         self.ntot, self.ninterm = int(self.v["NTOT"]), int(self.v["NINTERM"])
         self.nr, self.ns = self.p.nrad, self.p.nsec
         if disk_factory is None:
@@ -132,6 +130,8 @@ class Run:
         vi = self.write_velocity and index or 0
         self.write_polar("vrad", FIELD["vrad"], vi)
         self.write_polar("vtheta", FIELD["vtheta"], vi)
+        if self.p.label_advection:
+            self.write_polar("label", FIELD["label"], index)
         for name in ("energy", "temper", "divv", "qplus", "opacity"):
             if self.write[name]:
                 self.write_polar(name, FIELD[name], index)
@@ -186,6 +186,10 @@ class Run:
                     if t is not None:
                         rho = d.get(FIELD["dens"])[: t.size]
                         self._upload_rows("energy", t * rho / (p.adiabind - 1.0))
+                if p.label_advection:
+                    lab = self.read_polar("label", restart)
+                    if lab is not None:
+                        self._upload_rows("label", lab)
                 d.refresh(0)
                 self._restart_planets(restart)
         if self.scaling != 1.0:                       # main.c:160

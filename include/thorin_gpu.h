@@ -61,6 +61,7 @@ enum thorin_field {
   THORIN_DIVV,            /* velocity divergence (output only)         */
   THORIN_OPACITY,         /* opacity in code units (output only)       */
   THORIN_QMINUS,          /* radiative cooling term (output only)      */
+  THORIN_LABEL,           /* passive tracer (LabelAdvection YES)       */
   THORIN_NFIELDS
 };
 
@@ -143,6 +144,9 @@ typedef struct thorin_params {
    * there and a parameter here) */
   double sor_eps;                /* SOREPS                              */
   int    sor_maxiters;           /* SORMAXITERS                         */
+  /* command-line switches of main.c:56-100 */
+  int    centrifugal_balance;    /* -b: v_theta from the radial force balance */
+  int    label_advection;        /* LabelAdvection YES: a passive tracer    */
 } thorin_params;
 
 /* The planetary system as seen by the hydro loop (src_main/types.h:96-115). */

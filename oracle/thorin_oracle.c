@@ -72,7 +72,7 @@ typedef struct ora_disk {
   double *PebDensInit, *PebVradInit, *PebVthetaInit;
   double *VMed, *Vmoy; int *Nshift, *NshiftGas;
   /* hydro fields, (nr+3)*(ns+1)+5 doubles each (LowTasks.c:85) */
-  double *rho, *vrad, *vtheta, *energy;
+  double *rho, *vrad, *vtheta, *energy, *label, *ExtLabel;
   double *RhoStar, *RhoInt, *VradNew, *VradInt, *VthetaNew, *VthetaInt, *TemperInt;
   double *agr, *agt, *pagr, *pagt, *EnergyInt, *EnergyNew;
   double *cs, *press, *temper, *qplus, *qminus, *opacity;
@@ -368,6 +368,7 @@ static void InitGasVelocity(ora_disk *d)                   /* Pframeforce.c:644-
       double rg = r, omega = sqrt(G * 1.0 / rg / rg / rg), rhoinf;
       d->vtheta[l] = omega * r * sqrt(1.0 - d->cs[l] * d->cs[l] * r / p->adiabind);
       d->vtheta[l] -= d->OmegaFrame * r;
+      if (p->centrifugal_balance) d->vtheta[l] = vt_cent[i];      /* -b, IMIN = 0 */
       d->vrad[l] = p->imposed_disk_drift * p->sigma0 / d->SigmaInf[i] / ri;
       if (p->damp_flux) {
         if (i == 0) rhoinf = d->SigmaMed[i] - 0.5 * (d->SigmaMed[i + 1] - d->SigmaMed[i]);
@@ -508,7 +509,7 @@ ora_disk *ora_create(const thorin_params *p)
   for (size_t k = 0; k < sizeof(v1) / sizeof(v1[0]); k++) *v1[k] = vec(n1);
   d->Nshift = (int *)calloc((size_t)n1, sizeof(int));
   d->NshiftGas = (int *)calloc((size_t)n1, sizeof(int));
-  double **v2[] = {&d->rho, &d->vrad, &d->vtheta, &d->energy, &d->RhoStar, &d->RhoInt, &d->VradNew, &d->VradInt,
+  double **v2[] = {&d->rho, &d->vrad, &d->vtheta, &d->energy, &d->label, &d->ExtLabel, &d->RhoStar, &d->RhoInt, &d->VradNew, &d->VradInt,
                    &d->VthetaNew, &d->VthetaInt, &d->TemperInt, &d->agr, &d->agt, &d->pagr, &d->pagt, &d->EnergyInt,
                    &d->EnergyNew, &d->cs, &d->press, &d->temper, &d->qplus, &d->qminus, &d->opacity, &d->divv,
                    &d->Drr, &d->Drp, &d->Dpp, &d->Trr, &d->Trp, &d->Tpp, &d->RadMomP, &d->RadMomM, &d->ThetaMomP,
@@ -552,6 +553,8 @@ void ora_init_default(ora_disk *d)
   ComputePressureField(d, d->rho, d->energy);
   ComputeTemperatureField(d, d->rho, d->energy);
   InitGasVelocity(d);
+  for (int i = 0; i <= nr; i++)                               /* InitLabel, Init.c:59-72 */
+    for (int j = 0; j < ns; j++) d->label[j + i * ns] = (d->Rmed[i] - p->rmin) / (p->rmax - p->rmin);
   if (p->damp_init) FillVtheta(d);
   if (p->damping || p->pebbles) SetWaveKillingZones(d);
   if (p->pebbles) { EtaPressureSupport(d); InitPebblesViaFlux(d); }
@@ -609,6 +612,7 @@ double *ora_field(ora_disk *d, int id)
   case THORIN_DIVV: return d->divv;
   case THORIN_OPACITY: return d->opacity;
   case THORIN_QMINUS: return d->qminus;
+  case THORIN_LABEL: return d->label;
   }
   return NULL;
 }
@@ -1557,9 +1561,16 @@ static void AdvectSHIFT(ora_disk *d, double *val)           /* :113-136 */
 
 /* Transport (TransportEuler.c:34-47) and TransportPebbles (:449-505):
  * with_energy selects the gas (energy transported) variant. */
+/* Transport (TransportEuler.c:34-47): the gas with its energy and, with
+ * LabelAdvection, the tracer as rho*label (ComputeExtQty, :177-195); the
+ * pebbles without either. */
 static void TransportFluid(ora_disk *d, double *rho, double *vr, double *vt, double *energy, double dt)
 {
+  double *ext = (rho == d->rho && d->p.label_advection) ? d->ExtLabel : NULL;
   ComputeLRMomenta(d, rho, vr, vt);
+  if (ext)
+    for (int i = 0; i < d->nr; i++)
+      for (int j = 0; j < d->ns; j++) { int l = j + i * d->ns; ext[l] = rho[l] * d->label[l]; }
   /* OneWindRad */
   ComputeStarRad(d, rho, vr, d->RhoStar, dt);
   ActualiseGas(d, d->RhoInt, rho);
@@ -1568,6 +1579,7 @@ static void TransportFluid(ora_disk *d, double *rho, double *vr, double *vt, dou
   VanLeerRadial(d, vr, d->ThetaMomP, dt);
   VanLeerRadial(d, vr, d->ThetaMomM, dt);
   if (energy) VanLeerRadial(d, vr, energy, dt);
+  if (ext) VanLeerRadial(d, vr, ext, dt);
   VanLeerRadial(d, vr, rho, dt);
   /* OneWindTheta */
   ComputeResiduals(d, vt, dt);
@@ -1580,6 +1592,7 @@ static void TransportFluid(ora_disk *d, double *rho, double *vr, double *vt, dou
     VanLeerTheta(d, v, d->ThetaMomP, dt);
     VanLeerTheta(d, v, d->ThetaMomM, dt);
     if (energy) VanLeerTheta(d, v, energy, dt);
+    if (ext) VanLeerTheta(d, v, ext, dt);
     VanLeerTheta(d, v, rho, dt);
   }
   if (d->p.fast_transport) {
@@ -1588,9 +1601,13 @@ static void TransportFluid(ora_disk *d, double *rho, double *vr, double *vt, dou
     AdvectSHIFT(d, d->ThetaMomP);
     AdvectSHIFT(d, d->ThetaMomM);
     if (energy) AdvectSHIFT(d, energy);
+    if (ext) AdvectSHIFT(d, ext);
     AdvectSHIFT(d, rho);
   }
   ComputeVelocities(d, rho, vr, vt);
+  if (ext)                                                    /* ComputeSpeQty, TransportEuler.c:197-215 */
+    for (int i = 0; i < d->nr; i++)
+      for (int j = 0; j < d->ns; j++) { int l = j + i * d->ns; d->label[l] = ext[l] / rho[l]; }
 }
 
 /* ------------------------------------------------------------------ */

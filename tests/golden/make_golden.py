@@ -59,6 +59,9 @@ CASES = {
     "paracc_32x96": ("disk1", 32, 96, 6, 2, "ParametricAccretion 10.0\n", True, None),
     "drag_24x72": ("disk0", 24, 72, 6, 2, "AerodynamicDrag YES\nPlanetsFeelDisk YES\n", True,
                    (1.0e-7, 0.0, 0.0, 1.05, 0.05, 0.0, 0.0, 0.0, 0.0)),
+    # command-line switch -b: v_theta from the centrifugal balance
+    "cbal_24x72": ("disk0", 24, 72, 6, 2, "", True, None, "b"),
+    "label_24x72": ("disk0", 24, 72, 6, 2, "LabelAdvection YES\n", True),
 }
 GAS = ["dens", "vrad", "vtheta", "temper"]
 PEB = ["pebbledens", "pebblevrad", "pebblevtheta"]
@@ -105,6 +108,7 @@ def parse_log(text):
 def make_case(name):
     kind, nr, ns, ntot, ninterm, extra, full = CASES[name][:7]
     planet_override = CASES[name][7] if len(CASES[name]) > 7 else None
+    flags = CASES[name][8] if len(CASES[name]) > 8 else ""
     work = tempfile.mkdtemp(prefix="thorin_golden_")
     try:
         out = os.path.join(work, "out")
@@ -120,7 +124,7 @@ def make_case(name):
         par += f"PlanetConfig {os.path.join(work, 'planet.cfg')}\n"
         with open(os.path.join(work, "in.par"), "w") as f:
             f.write(par)
-        run([THORIN, "-0", "in.par"], work)
+        run([THORIN, "-0" + flags, "in.par"], work)
         init = {k: read_dump(out, k, 0, nr, ns) for k in GAS}
         if kind == "disk1":
             for k in PEB + ["pebblesize", "pebblestokes"]:
@@ -137,19 +141,19 @@ def make_case(name):
             par += "InitializeFromFile YES\n"
             with open(os.path.join(work, "in.par"), "w") as f:
                 f.write(par)
-            log = run([THORIN, "-ad", "in.par"], work)
+            log = run([THORIN, "-ad" + flags, "in.par"], work)
         else:
             st["dens"].astype("<f8").tofile(os.path.join(out, "gasdens0.dat"))
             st["vrad"].astype("<f8").tofile(os.path.join(out, "gasvrad0.dat"))
             st["pebdens"].astype("<f8").tofile(os.path.join(out, "gaspebbledens0.dat"))
             st["pebsize"].astype("<f8").tofile(os.path.join(out, "gaspebblesize0.dat"))
-            log = run([THORIN, "-ad", "-s", "0", "in.par"], work)
-        res = {"inpar": np.array(par), "planet": np.array(planet), "nrad": nr, "nsec": ns,
+            log = run([THORIN, "-ad" + flags, "-s", "0", "in.par"], work)
+        res = {"inpar": np.array(par), "planet": np.array(planet), "flags": np.array(flags), "nrad": nr, "nsec": ns,
                "ntot": ntot, "ninterm": ninterm, "kind": np.array(kind)}
         for k, v in init.items():
             res["init_" + k] = v
         res.update(parse_log(log))
-        names = GAS + (PEB if kind == "disk1" else [])
+        names = GAS + (PEB if kind == "disk1" else []) + (["label"] if "LabelAdvection YES" in extra else [])
         rows = sorted({min(nr - 1, int(round(f * (nr - 1)))) for f in SAMPLE_ROWS_FRAC})
         res["sample_rows"] = np.array(rows)
         for k in range(1, ntot // ninterm + 1):

@@ -12,7 +12,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 FIELD_IDS = {"dens": 0, "vrad": 1, "vtheta": 2, "energy": 3, "pebbledens": 4, "pebblevrad": 5,
              "pebblevtheta": 6, "pebblesize": 7, "temper": 8, "soundspeed": 9, "pressure": 10,
-             "pebblestokes": 11, "qplus": 12, "divv": 13, "opacity": 14, "qminus": 15}
+             "pebblestokes": 11, "qplus": 12, "divv": 13, "opacity": 14, "qminus": 15, "label": 16}
 GAS = ["dens", "vrad", "vtheta", "temper"]
 PEB = ["pebbledens", "pebblevrad", "pebblevtheta"]
 
@@ -22,7 +22,8 @@ def load(name):
 
 
 def case_params(g, **kw):
-    return derive(read_inpar(str(g["inpar"])), **kw)
+    flags = str(g["flags"]) if "flags" in g.files else ""
+    return derive(read_inpar(str(g["inpar"])), centrifugal_balance="b" in flags, **kw)
 
 
 def start_state(disk, params, init_fields, seed=0):

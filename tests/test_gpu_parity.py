@@ -15,7 +15,7 @@ from fargo_thorin_gb300 import workloads
 pytestmark = pytest.mark.gpu
 CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "iso_24x72", "iso_peb_32x96",
          "dampinit_24x72", "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
-         "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72"]
+         "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72", "label_24x72"]
 TOL = 1e-10
 
 
@@ -40,7 +40,7 @@ def test_gpu_vs_reference_golden(name):
     sys_ = workloads.make_planets(p, [tuple(g["planet"])])
     tq = g["tqwk"]
     ntot, ninterm = int(g["ntot"]), int(g["ninterm"])
-    fields = H.GAS + (H.PEB if p.pebbles else [])
+    fields = H.GAS + (H.PEB if p.pebbles else []) + (["label"] if p.label_advection else [])
     for step in range(1, ntot + 1):
         sys_.x[0], sys_.y[0] = tq[step - 1][3], tq[step - 1][4]
         d.algogas(sys_)
@@ -74,7 +74,8 @@ def test_gpu_vs_reference_golden(name):
 
 @pytest.mark.parametrize("name", ["disk0_24x72", "disk1_32x96", "disk1_64x192_40", "iso_peb_32x96", "dampinit_24x72",
                                   "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
-                                  "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72"])
+                                  "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72",
+                                  "label_24x72"])
 def test_gpu_vs_oracle_every_dt(name):
     """GPU and oracle run the same host N-body code, so they share the planet
     trajectory; compared after every DT, with the FARGO shifts and SOR counts
@@ -95,7 +96,7 @@ def test_gpu_vs_oracle_every_dt(name):
         o.algogas(so)
         np.testing.assert_array_equal(d.nshift(), o.nshift())
         assert d.stats().sor_last_niter == o.stats().sor_last_niter
-        for f in H.GAS + (H.PEB if p.pebbles else []) + ["energy"]:
+        for f in H.GAS + (H.PEB if p.pebbles else []) + ["energy"] + (["label"] if p.label_advection else []):
             assert H.rel_l2(d.get(H.FIELD_IDS[f])[:n], o.get(H.FIELD_IDS[f])[:n]) < 1e-11, f"{f} at DT {step}"
         assert abs(sg.x[0] - so.x[0]) < 1e-14 and abs(sg.vx[0] - so.vx[0]) < 1e-14
 
@@ -123,6 +124,6 @@ def test_gpu_vs_oracle_wide_rings(kind, nr, ns):
         assert d.stats().substeps == o.stats().substeps
         np.testing.assert_array_equal(d.nshift(), o.nshift())
         assert d.stats().sor_last_niter == o.stats().sor_last_niter
-        for f in H.GAS + (H.PEB if p.pebbles else []) + ["energy"]:
+        for f in H.GAS + (H.PEB if p.pebbles else []) + ["energy"] + (["label"] if p.label_advection else []):
             assert H.rel_l2(d.get(H.FIELD_IDS[f])[:n], o.get(H.FIELD_IDS[f])[:n]) < 1e-11, f"{f} at DT {step}"
         assert abs(sg.x[0] - so.x[0]) < 1e-14 and abs(sg.vx[0] - so.vx[0]) < 1e-14

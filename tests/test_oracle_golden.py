@@ -15,7 +15,7 @@ from fargo_thorin_gb300 import workloads
 
 CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "iso_24x72", "iso_peb_32x96",
          "dampinit_24x72", "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
-         "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72"]
+         "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72", "label_24x72"]
 
 
 def _run(name, force_planet=True):
@@ -38,7 +38,7 @@ def _run(name, force_planet=True):
 def test_oracle_bit_exact_vs_reference(name):
     g, p, d, sys_, tq, ntot, ninterm, n = _run(name)
     nr, ns = p.nrad, p.nsec
-    fields = H.GAS + (H.PEB if p.pebbles else [])
+    fields = H.GAS + (H.PEB if p.pebbles else []) + (["label"] if p.label_advection else [])
     for step in range(1, ntot + 1):
         sys_.x[0], sys_.y[0] = tq[step - 1][3], tq[step - 1][4]
         assert d.algogas(sys_) == 0
