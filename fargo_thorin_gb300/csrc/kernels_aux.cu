@@ -1279,3 +1279,18 @@ void aux_drag_cell(const double *rho, const double *cs, const double *vrad, cons
   k_drag_cell<<<1, 32, 0, s>>>(rho, cs, vrad, vtheta, l, ns, out);
   g_thorin_launches++;
 }
+
+// CorrectVtheta (SideEuler.c:505-519): v_theta -= domega * Rmed when the
+// frame's rotation rate changes by domega.
+__global__ void k_correct_vtheta(DevGrid g, double *__restrict__ vt, double domega)
+{
+  const int ns = g.ns;
+  CELL_LOOP_2D
+  vt[l] -= domega * g.r.Rmed[i];
+}
+
+void aux_correct_vtheta(const DevGrid &g, double *vt, double domega, cudaStream_t s)
+{
+  k_correct_vtheta<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, vt, domega);
+  g_thorin_launches++;
+}

@@ -139,7 +139,8 @@ struct thorin_disk {
   double omega, domega, omegabest;
   double heatsrc[THORIN_MAXPLANETS];
   int heatsrc_index[THORIN_MAXPLANETS], heatsrc_max;
-  double gm1, gg1, drin, drout, invdphi, lr01, lr12, vkep_in, vkep_out, taueff_c, tirr4fac, rstar;
+  double gm1, gg1, drin, drout, invdphi, lr01, lr12, taueff_c, tirr4fac, rstar;
+  double vkep_in, vkep_out;      // Keplerian edge velocities (ImposeKeplerianEdges) in the inertial frame
   ViscParams vp;
   thorin_stats st;
   int timing;
@@ -433,8 +434,8 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
     const double vout = sqrt(1.0 * 1.0 / r1) *
                         sqrt(1.0 - pow(aspect(r1), 2.0) * pow(r1, 2.0 * p.flaring_index) *
                                        (1. + p.sigma_slope - 2.0 * p.flaring_index));
-    d->vkep_in = vin - r0 * p.omega_frame;
-    d->vkep_out = vout - r1 * p.omega_frame;
+    d->vkep_in = vin;                      // inertial; the frame's rotation is taken off per substep
+    d->vkep_out = vout;
   }
   d->rstar = p.stellar_radius * 6.957e8 / AU_SI;
   {
@@ -580,10 +581,18 @@ extern "C" int thorin_gpu_get_nshift(thorin_disk *d, int *host)
   return THORIN_OK;
 }
 
+extern "C" int thorin_gpu_set_frame(thorin_disk *d, double omega_frame)
+{
+  if (!d) return THORIN_ERR_ARG;
+  d->OmegaFrame = omega_frame;
+  return THORIN_OK;
+}
+
 extern "C" int thorin_gpu_get_stats(thorin_disk *d, thorin_stats *s)
 {
   *s = d->st;
   s->physical_time = d->PhysicalTime;
+  s->omega_frame = d->OmegaFrame;
   s->kernel_launches = g_thorin_launches;
   return THORIN_OK;
 }
@@ -1487,7 +1496,7 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
   hydro_stress(d->g, d->vrad_int, d->vtheta_int, d->rho, d->divv, d->trr, d->tpp, d->trp, d->invdphi, d->s);
   const int kepler = (!p.damping) || (p.damping && p.damp_vrad);
   hydro_visc_update(d->g, d->vrad_int, d->vtheta_int, d->rho, d->trr, d->tpp, d->trp, dt, d->invdphi, kepler,
-                    d->vkep_in, d->vkep_out, d->s);
+                    d->vkep_in - d->Rmed[0] * d->OmegaFrame, d->vkep_out - d->Rmed[d->nr - 1] * d->OmegaFrame, d->s);
   if (p.pebbles)
     aux_pebble_substep1(d->g, d->pvrad, d->pvtheta, d->tau, d->vrad, d->vtheta, d->paccr, d->pacct, d->gaccr, d->gacct,
                         d->rho, d->pdens, dt, p.diffusive_particles, p.schmidt_number, d->ring[R_INVDXTHETA], d->s);
@@ -1608,6 +1617,7 @@ extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
   double dtemp = 0.0, dt;
   int nsub = 0, status = THORIN_OK;
   if (!sys || sys->nb > MAXPL_DEV) { g_last_error = "planetary system missing or too large"; return THORIN_ERR_ARG; }
+  if (p.corotating && sys->nb < 1) { g_last_error = "Frame COROTATING needs a planet"; return THORIN_ERR_ARG; }
   if (d->timing) CUCHK(cudaEventRecord(d->ev[2], d->s));
   d->torque_pending = 1;                       // DumpTorqueNow: log the first substep's torques
   while (dtemp < 0.999999999 * DT) {
@@ -1620,10 +1630,24 @@ extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
     RCHK(thorin_gpu_accrete(d, sys, dt));
     dtemp += dt;
     double ind[2], rrho[THORIN_MAXPLANETS], rcs[THORIN_MAXPLANETS];
+    const double xmark = sys->x[0], ymark = sys->y[0];      // GetPsysInfo (MARK)
     RCHK(thorin_gpu_forces(d, sys, d->MassTaper, ind, rrho, rcs));
     advance_from_disk(d, sys, dt, ind, rrho, rcs);
     if (p.aerodynamic_drag) RCHK(thorin_gpu_drag(d, sys, dt));
     nbody_step(sys, dt);
+    if (p.corotating) {
+      // GetPsysInfo (GET): the angle planet 0 moved through; the frame
+      // follows it and the azimuthal velocities are corrected
+      // (SourceEuler.c:261-267, CorrectVtheta SideEuler.c:505-519)
+      const double x = sys->x[0], y = sys->y[0];
+      const double d2 = sqrt(x * x + y * y), d1 = sqrt(xmark * xmark + ymark * ymark);
+      const double cross = xmark * y - x * ymark;
+      const double OmegaNew = asin(cross / (d1 * d2)) / dt;
+      const double domega = OmegaNew - d->OmegaFrame;
+      aux_correct_vtheta(d->g, d->vtheta, domega, d->s);
+      if (p.pebbles) aux_correct_vtheta(d->g, d->pvtheta, domega, d->s);
+      d->OmegaFrame = OmegaNew;
+    }
     rotate_psys(sys, d->OmegaFrame * dt);
     int s = thorin_gpu_hydro(d, dt);
     if (s != THORIN_OK && s != THORIN_ERR_SOR_MAXIT) return s;

@@ -169,6 +169,7 @@ void aux_gas_accrete(const DevGrid &g, double *dens, const double *vrad, const d
                      const GasAccArgs &a, double *out, cudaStream_t s);
 void aux_drag_cell(const double *rho, const double *cs, const double *vrad, const double *vtheta, int l, int ns,
                    double *out, cudaStream_t s);
+void aux_correct_vtheta(const DevGrid &g, double *vt, double domega, cudaStream_t s);
 void aux_iso_eos(const DevGrid &g, const double *rho, const double *csr, double *cs, double *press, double *temper,
                  int set_cs, int set_press, int set_temper, cudaStream_t s);
 void aux_damp_peb(const DevGrid &g, double *pd, double *pvr, double *pvt, const int *rings, int nrings, double dt,

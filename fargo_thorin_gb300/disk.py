@@ -58,6 +58,10 @@ class GpuDisk:
         assert a.size == (self.nr + 1) * self.ns
         _lib.check(self.L.thorin_gpu_upload(self.h, fid, a.ctypes.data_as(C.POINTER(C.c_double))), "upload")
 
+    def set_frame(self, omega_frame: float):
+        """Rotation rate of the frame (OmegaFrame)."""
+        _lib.check(self.L.thorin_gpu_set_frame(self.h, omega_frame), "set_frame")
+
     def set_time(self, t: float):
         _lib.check(self.L.thorin_gpu_set_time(self.h, t), "set_time")
 

@@ -161,7 +161,7 @@ class ThorinParams(C.Structure):
         ("evaporation_rate", C.c_double), ("evaporation_temperature", C.c_double), ("heating_delay", C.c_int),
         ("parametric_accretion", C.c_double), ("prescribed_accretion", C.c_int),
         ("sor_eps", C.c_double), ("sor_maxiters", C.c_int), ("centrifugal_balance", C.c_int),
-        ("label_advection", C.c_int),
+        ("label_advection", C.c_int), ("corotating", C.c_int),
     ]
 
     def as_dict(self):
@@ -199,7 +199,8 @@ class ThorinStats(C.Structure):
     _fields_ = [("substeps", C.c_int), ("sor_calls", C.c_int), ("sor_sweeps", C.c_longlong),
                 ("sor_last_niter", C.c_int), ("sor_omega", C.c_double), ("crashed", C.c_int),
                 ("physical_time", C.c_double), ("last_dt", C.c_double), ("sor_time_ms", C.c_double),
-                ("sor_passes", C.c_longlong), ("step_time_ms", C.c_double), ("kernel_launches", C.c_longlong)]
+                ("sor_passes", C.c_longlong), ("step_time_ms", C.c_double), ("kernel_launches", C.c_longlong),
+                ("omega_frame", C.c_double)]
 
 
 def _yes(s: str, ch: str) -> bool:
@@ -263,8 +264,9 @@ def derive(v: dict, *, sor_eps: float = SOREPS, sor_maxiters: int = SORMAXITERS,
     p.planetary_density = v["PLANETARYDENSITY"]
     p.aerodynamic_drag = int(_yes(v["AERODYNAMICDRAG"], "Y"))
     p.omega_frame = v["OMEGAFRAME"]
-    if _yes(v["FRAME"], "C") or _yes(v["FRAME"], "G"):
-        raise ValueError("Frame Corotating/GuidingCenter is not supported (fixed frame only)")
+    if _yes(v["FRAME"], "G"):
+        raise ValueError("Frame GuidingCenter is not supported (fixed or corotating frames only)")
+    p.corotating = int(_yes(v["FRAME"], "C"))
     p.fast_transport = int(not _yes(v["TRANSPORT"], "S"))
     ib, ob = v["INNERBOUNDARY"], v["OUTERBOUNDARY"]
     p.open_inner = int(_yes(ib, "O"))
@@ -324,3 +326,14 @@ def read_planet_config(text: str):
             raise ValueError(f"Error reading planet line {line!r}")
         out.append(vals)
     return out
+
+
+def corotating_frame(p: ThorinParams, planets) -> None:
+    """Frame COROTATING: the run starts in the frame of planet 0, rotating at
+    its angular speed (x vy - y vx) / (x^2 + y^2) (GetPsysInfo FREQUENCY,
+    Psys.c:195-262; main.c:161)."""
+    if p.corotating:
+        if planets.nb < 1:
+            raise ValueError("Frame COROTATING needs a planet")
+        x, y, vx, vy = planets.x[0], planets.y[0], planets.vx[0], planets.vy[0]
+        p.omega_frame = (x * vy - y * vx) / (x * x + y * y)

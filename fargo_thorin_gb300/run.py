@@ -145,7 +145,7 @@ class Run:
                 f.write("\t".join("%.18g" % v for v in (s.mass[k], s.gas[k], s.solid[k], s.x[k], s.y[k], s.z[k],
                                                          s.vx[k], s.vy[k], s.vz[k])) + "\n")
         with open(self._path("omegaframe.dat"), "a") as f:
-            f.write("%d\t%#.18g\n" % (index, self.p.omega_frame))
+            f.write("%d\t%#.18g\n" % (index, self.disk.stats().omega_frame))
 
     def write_torques(self):
         """One tqwk<k>.dat line per planet (UpdateLog, Force.c:65-67)."""
@@ -158,13 +158,18 @@ class Run:
         """Initialization (Init.c:59-148) and the planets (SetupReboundSimulation
         / RestartReboundSimulation)."""
         d, p = self.disk, self.p
-        d.init_default()                              # InitEuler (+ pebble equilibrium)
         if restart is None:
             with open(self.v["PLANETCONFIG"]) as f:
                 rows = P.read_planet_config(f.read())
             self.sys = workloads.make_planets(p, rows)
             for name in ("tqwk%d.dat" % k for k in range(self.sys.nb)):
                 open(self._path(name), "w").close()
+        else:
+            self._restart_planets(restart)            # also sets PhysicalTime
+        if p.corotating:                              # OmegaFrame = GetPsysInfo (sys, FREQUENCY), main.c:161
+            P.corotating_frame(p, self.sys)
+            d.set_frame(p.omega_frame)
+        d.init_default()                              # InitEuler (+ pebble equilibrium)
         init_file = _yes(self.v["INITIALIZEFROMFILE"])
         if init_file or restart is not None:
             rho_full = d.get(FIELD["dens"])
@@ -191,7 +196,8 @@ class Run:
                     if lab is not None:
                         self._upload_rows("label", lab)
                 d.refresh(0)
-                self._restart_planets(restart)
+                if p.corotating:                      # GetOmegaFrame (Output.c:280-310)
+                    d.set_frame(self._omega_frame_at(restart))
         if self.scaling != 1.0:                       # main.c:160
             self._upload_rows("dens", d.get(FIELD["dens"])[: self.nr * self.ns] * self.scaling)
             d.refresh(0)
@@ -227,6 +233,14 @@ class Run:
             raise ValueError(f"Number of values in the initialization file {path} is larger than the size of "
                              "hydrodynamic arrays")
         return a
+
+    def _omega_frame_at(self, n: int) -> float:
+        with open(self._path("omegaframe.dat")) as f:
+            for line in f:
+                tok = line.split()
+                if tok and int(tok[0]) == n:
+                    return float(tok[1])
+        raise ValueError(f"Can't read entry {n} in 'omegaframe.dat' file. Aborting restart.")
 
     def _restart_planets(self, n: int):
         with open(self._path(f"nbody.state{n}.dat")) as f:

@@ -147,6 +147,8 @@ typedef struct thorin_params {
   /* command-line switches of main.c:56-100 */
   int    centrifugal_balance;    /* -b: v_theta from the radial force balance */
   int    label_advection;        /* LabelAdvection YES: a passive tracer    */
+  int    corotating;             /* Frame COROTATING: the frame follows planet 0
+                                    (omega_frame starts at its angular speed) */
 } thorin_params;
 
 /* The planetary system as seen by the hydro loop (src_main/types.h:96-115). */
@@ -183,6 +185,7 @@ typedef struct thorin_stats {
   long long sor_passes;          /* colour passes that did work (timing on)     */
   double step_time_ms;           /* device time of the last thorin_gpu_algogas  */
   long long kernel_launches;     /* kernels launched by the library so far      */
+  double omega_frame;            /* OmegaFrame now (changes in corotating runs) */
 } thorin_stats;
 
 /* Fill p with the reference defaults of src_main/var.c and nrad x nsec. */
@@ -220,6 +223,10 @@ int thorin_gpu_refresh(thorin_disk *d, int flags);
 /* Ring profiles (nrad doubles each). */
 int thorin_gpu_set_profile(thorin_disk *d, int profile, const double *host);
 int thorin_gpu_get_profile(thorin_disk *d, int profile, double *host);
+
+/* Rotation rate of the frame, e.g. OmegaFrame of omegaframe.dat at a
+ * restart (GetOmegaFrame, Output.c:280-310). */
+int thorin_gpu_set_frame(thorin_disk *d, double omega_frame);
 
 /* Simulation clock (PhysicalTime / PhysicalTimeInitial, main.c:166). */
 int thorin_gpu_set_time(thorin_disk *d, double physical_time);

@@ -634,7 +634,12 @@ double *ora_profile(ora_disk *d, int id)
 double *ora_radii(ora_disk *d) { return d->Radii; }
 int *ora_nshift(ora_disk *d) { return d->NshiftGas; }
 void ora_set_time(ora_disk *d, double t) { d->PhysicalTime = t; d->PhysicalTimeInitial = t; }
-void ora_get_stats(ora_disk *d, thorin_stats *s) { *s = d->st; s->physical_time = d->PhysicalTime; }
+void ora_get_stats(ora_disk *d, thorin_stats *s)
+{
+  *s = d->st;
+  s->physical_time = d->PhysicalTime;
+  s->omega_frame = d->OmegaFrame;
+}
 
 /* ------------------------------------------------------------------ */
 /* Boundaries: SideEuler.c                                              */
@@ -2383,10 +2388,25 @@ int ora_algogas(ora_disk *d, thorin_planets *sys)
     if (p->prescribed_accretion) ParametricAccretion(d, sys, dt);
     if (p->pebbles) { AccretePebblesOntoPlanets(d, sys, dt); EvaporatePebbles(d, dt); }
     dtemp += dt;
+    double xmark = sys->x[0], ymark = sys->y[0];              /* GetPsysInfo (MARK), Psys.c:240-244 */
     FillForcesArrays(d, sys);
     AdvanceSystemFromDisk(d, sys, dt);
     if (p->aerodynamic_drag) AdvanceSystemFromDrag(d, sys, dt);
     AdvanceSystemNbody(sys, dt);
+    if (p->corotating) {                                       /* SourceEuler.c:261-267 */
+      double x = sys->x[0], y = sys->y[0];
+      double d2 = sqrt(x * x + y * y), d1 = sqrt(xmark * xmark + ymark * ymark);
+      double cross = xmark * y - x * ymark;
+      double OmegaNew = asin(cross / (d1 * d2)) / dt;         /* GetPsysInfo (GET), Psys.c:245-254 */
+      double domega = OmegaNew - d->OmegaFrame;
+      for (int i = 0; i < d->nr; i++)                          /* CorrectVtheta, SideEuler.c:505-519 */
+        for (int j = 0; j < d->ns; j++) {
+          int l = j + i * d->ns;
+          d->vtheta[l] -= domega * d->Rmed[i];
+          if (p->pebbles) d->pvtheta[l] -= domega * d->Rmed[i];
+        }
+      d->OmegaFrame = OmegaNew;
+    }
     RotatePsys(sys, d->OmegaFrame * dt);
     ApplyBoundaryCondition(d, dt);
     int crashed = DetectCrash(d, d->rho);

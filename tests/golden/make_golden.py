@@ -62,6 +62,8 @@ CASES = {
     # command-line switch -b: v_theta from the centrifugal balance
     "cbal_24x72": ("disk0", 24, 72, 6, 2, "", True, None, "b"),
     "label_24x72": ("disk0", 24, 72, 6, 2, "LabelAdvection YES\n", True),
+    "corot_24x72": ("disk0", 24, 72, 6, 2, "Frame COROTATING\n", True),
+    "corot_peb_32x96": ("disk1", 32, 96, 6, 2, "Frame COROTATING\n", True),
 }
 GAS = ["dens", "vrad", "vtheta", "temper"]
 PEB = ["pebbledens", "pebblevrad", "pebblevtheta"]

@@ -6,7 +6,7 @@ import os
 import numpy as np
 
 from fargo_thorin_gb300 import workloads
-from fargo_thorin_gb300.params import derive, read_inpar
+from fargo_thorin_gb300.params import corotating_frame, derive, read_inpar
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -23,7 +23,10 @@ def load(name):
 
 def case_params(g, **kw):
     flags = str(g["flags"]) if "flags" in g.files else ""
-    return derive(read_inpar(str(g["inpar"])), centrifugal_balance="b" in flags, **kw)
+    p = derive(read_inpar(str(g["inpar"])), centrifugal_balance="b" in flags, **kw)
+    if p.corotating:                                  # the frame of planet 0 (main.c:161)
+        corotating_frame(p, workloads.make_planets(p, [tuple(g["planet"])]))
+    return p
 
 
 def start_state(disk, params, init_fields, seed=0):

@@ -79,10 +79,20 @@ def test_unsupported_rejected(lib):
     assert "SloppyCFL" in lib.thorin_gpu_last_error().decode()
 
 
-def test_corotating_frame_refused():
-    text = workloads.inpar_text("disk0", 24, 72) + "\nFrame COROTATING\n"
-    with pytest.raises(ValueError, match="Corotating"):
+def test_guiding_centre_frame_refused():
+    text = workloads.inpar_text("disk0", 24, 72) + "\nFrame GUIDINGCENTER\n"
+    with pytest.raises(ValueError, match="GuidingCenter"):
         P.derive(P.read_inpar(text))
+
+
+def test_corotating_frame_rate():
+    """Frame COROTATING starts at planet 0's angular speed (GetPsysInfo)."""
+    p = P.derive(P.read_inpar(workloads.inpar_text("disk0", 24, 72) + "\nFrame COROTATING\n"))
+    assert p.corotating == 1
+    sys_ = workloads.make_planets(p, [workloads.PLANET1])
+    P.corotating_frame(p, sys_)
+    x, y, vx, vy = sys_.x[0], sys_.y[0], sys_.vx[0], sys_.vy[0]
+    assert p.omega_frame == (x * vy - y * vx) / (x * x + y * y)
 
 
 def test_bad_grid_rejected(lib):

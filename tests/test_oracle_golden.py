@@ -15,7 +15,8 @@ from fargo_thorin_gb300 import workloads
 
 CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "iso_24x72", "iso_peb_32x96",
          "dampinit_24x72", "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
-         "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72", "label_24x72"]
+         "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72", "label_24x72",
+         "corot_24x72", "corot_peb_32x96"]
 
 
 def _run(name, force_planet=True):
@@ -34,9 +35,25 @@ def _run(name, force_planet=True):
     return g, p, d, sys_, tq, ntot, ninterm, n
 
 
+# In a corotating frame the frame's rotation rate comes from the planet's
+# N-body step each substep, which the reference takes from REBOUND (IAS15)
+# and the oracle from the library's RK4: the rate differs in the last bit,
+# and so do the fields (relative 1e-16 per DT).  These cases are compared
+# within 1e-12 instead of bit for bit.
+NBODY_FRAME = {"corot_24x72", "corot_peb_32x96"}
+
+
+def _same(a, b, err_msg, exact=True):
+    if exact:
+        np.testing.assert_array_equal(a, b, err_msg=err_msg)
+    else:
+        assert H.rel_l2(a, b) < 1e-12, err_msg
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_oracle_bit_exact_vs_reference(name):
     g, p, d, sys_, tq, ntot, ninterm, n = _run(name)
+    exact = name not in NBODY_FRAME
     nr, ns = p.nrad, p.nsec
     fields = H.GAS + (H.PEB if p.pebbles else []) + (["label"] if p.label_advection else [])
     for step in range(1, ntot + 1):
@@ -47,16 +64,17 @@ def test_oracle_bit_exact_vs_reference(name):
         if len(g["sor_niter"]):                     # no SOR in isothermal runs
             assert st.sor_last_niter == g["sor_niter"][step - 1]
         m, mom, e, _, _ = d.integrals()
-        assert m == g["mass"][step - 1] and mom == g["momentum"][step - 1] and e == g["energy"][step - 1]
+        _same(np.array([m, mom, e]), np.array([g["mass"][step - 1], g["momentum"][step - 1], g["energy"][step - 1]]),
+              f"integrals after {step} DT", exact)
         if step % ninterm == 0:
             k = step // ninterm
             for f in fields:
                 a = d.get(H.FIELD_IDS[f])[:n].reshape(nr, ns)
                 if f"out{k}_{f}" in g:
-                    np.testing.assert_array_equal(a, g[f"out{k}_{f}"], err_msg=f"{f} after {step} DT")
+                    _same(a, g[f"out{k}_{f}"], f"{f} after {step} DT", exact)
                 else:
-                    np.testing.assert_array_equal(a[g["sample_rows"]], g[f"out{k}_{f}_rows"])
-                    np.testing.assert_array_equal(a.mean(axis=1), g[f"out{k}_{f}_ringmean"])
+                    _same(a[g["sample_rows"]], g[f"out{k}_{f}_rows"], f"{f} rows", exact)
+                    _same(a.mean(axis=1), g[f"out{k}_{f}_ringmean"], f"{f} ring means", exact)
 
 
 @pytest.mark.parametrize("name", ["disk1_32x96", "disk1_64x192_40"])
