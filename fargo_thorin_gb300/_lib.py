@@ -47,6 +47,7 @@ SIGNATURES = {
     "thorin_gpu_init_pebbles": (C.c_int, [_P]),
     "thorin_gpu_drag": (C.c_int, [_P, C.POINTER(ThorinPlanets), C.c_double]),
     "thorin_gpu_set_frame": (C.c_int, [_P, C.c_double]),
+    "thorin_gpu_set_opacity_table": (C.c_int, [_P, C.c_int, C.c_int, _D, _D, _D, _D]),
     "thorin_gpu_get_torques": (C.c_int, [_P, C.POINTER(ThorinTorque), C.c_int, C.POINTER(C.c_int)]),
     "thorin_gpu_last_error": (C.c_char_p, []),
     "thorin_planet_from_elements": (C.c_int, [C.POINTER(ThorinPlanets), C.c_int] + [C.c_float] * 9),

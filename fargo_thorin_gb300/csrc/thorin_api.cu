@@ -581,6 +581,27 @@ extern "C" int thorin_gpu_get_nshift(thorin_disk *d, int *host)
   return THORIN_OK;
 }
 
+extern "C" int thorin_gpu_set_opacity_table(thorin_disk *d, int rows, int cols, const double *pgrid, const double *tgrid,
+                                            const double *planck, const double *rosseland)
+{
+  if (!d || rows < 2 || cols < 3 || !pgrid || !tgrid || !rosseland) {
+    g_last_error = "opacity table: rows >= 2, cols >= 3 and the grids and the Rosseland table are required";
+    return THORIN_ERR_ARG;
+  }
+  (void)planck;                                   // the hydro uses Rosseland means only (opacity_SM03)
+  double *pg, *tg, *ro;
+  RCHK(dalloc(d, (void **)&pg, rows * sizeof(double)));
+  RCHK(dalloc(d, (void **)&tg, cols * sizeof(double)));
+  RCHK(dalloc(d, (void **)&ro, (size_t)rows * cols * sizeof(double)));
+  CUCHK(cudaMemcpyAsync(pg, pgrid, rows * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaMemcpyAsync(tg, tgrid, cols * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaMemcpyAsync(ro, rosseland, (size_t)rows * cols * sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  d->g.k.sm_pgrid = pg; d->g.k.sm_tgrid = tg; d->g.k.sm_ross = ro;
+  d->g.k.sm_rows = rows; d->g.k.sm_cols = cols;
+  return THORIN_OK;
+}
+
 extern "C" int thorin_gpu_set_frame(thorin_disk *d, double omega_frame)
 {
   if (!d) return THORIN_ERR_ARG;
@@ -1397,6 +1418,10 @@ static int energy_step(thorin_disk *d, double dt)
     KCHECK("cooling kernel");
     std::swap(d->energy, d->energy_new);
     return THORIN_OK;
+  }
+  if (p.opacity_law == THORIN_OPA_SM03 && !d->g.k.sm_ross) {
+    g_last_error = "OpacityTable SM03 needs the gas opacity table (thorin_gpu_set_opacity_table)";
+    return THORIN_ERR_STATE;
   }
   hydro_eos(d->g, d->rho, d->energy_int, d->temper, d->cs, d->gm1, d->gg1, d->s);
   hydro_diffcoef(d->g, d->rho, d->temper, d->cs, d->opacity, d->qminus, d->dcen, d->partials, p.opacity_law,

@@ -32,6 +32,9 @@ struct DevConst {
   double opa2cu, t2si, rho2cgs, sigma_sb, sqrt2pi_inv, pebbulkdens, cv, sqrt_adiabind_inv;
   double evaptemp;           // EVAPORATIONTEMPERATURE / T2SI
   double sqrt3;              // sqrt(3.0)
+  // OpacityTable SM03: the Malygin gas table (device copies)
+  const double *sm_pgrid, *sm_tgrid, *sm_ross;
+  int sm_rows, sm_cols;
 };
 
 // Ring arrays (device pointers, nrad+2 entries each).

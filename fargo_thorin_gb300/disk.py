@@ -58,6 +58,13 @@ class GpuDisk:
         assert a.size == (self.nr + 1) * self.ns
         _lib.check(self.L.thorin_gpu_upload(self.h, fid, a.ctypes.data_as(C.POINTER(C.c_double))), "upload")
 
+    def set_opacity_table(self, rows, cols, pgrid, tgrid, planck, rosseland):
+        """OpacityTable SM03 gas table (InitOpacities, Opacity2.c:247-297)."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (pgrid, tgrid, planck, rosseland)]
+        _lib.check(self.L.thorin_gpu_set_opacity_table(self.h, int(rows), int(cols),
+                                                       *[a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs]),
+                   "set_opacity_table")
+
     def set_frame(self, omega_frame: float):
         """Rotation rate of the frame (OmegaFrame)."""
         _lib.check(self.L.thorin_gpu_set_frame(self.h, omega_frame), "set_frame")

@@ -244,7 +244,7 @@ def derive(v: dict, *, sor_eps: float = SOREPS, sor_maxiters: int = SORMAXITERS,
     elif tab[:1] == "L":
         p.opacity_law = 2
     elif tab[:1] == "S":
-        raise ValueError("OpacityTable SM03 (tabulated Semenov/Malygin) is not supported")
+        p.opacity_law = 4
     else:
         p.opacity_law = 0
     ts, rs = v["THICKNESSSMOOTHING"], v["ROCHESMOOTHING"]
@@ -337,3 +337,17 @@ def corotating_frame(p: ThorinParams, planets) -> None:
             raise ValueError("Frame COROTATING needs a planet")
         x, y, vx, vy = planets.x[0], planets.y[0], planets.vx[0], planets.vy[0]
         p.omega_frame = (x * vy - y * vx) / (x * x + y * y)
+
+
+def read_opacity_table(path: str):
+    """InitOpacities (Opacity2.c:247-297): rows, cols, pressure grid,
+    temperature grid, Planck table, Rosseland table (whitespace-separated)."""
+    import numpy as np
+    with open(path) as f:
+        tok = f.read().split()
+    rows, cols = int(tok[0]), int(tok[1])
+    v = np.array([float(t) for t in tok[2:2 + rows + cols + 2 * rows * cols]], dtype=np.float64)
+    pgrid, tgrid = v[:rows], v[rows:rows + cols]
+    planck = v[rows + cols:rows + cols + rows * cols]
+    rosseland = v[rows + cols + rows * cols:]
+    return rows, cols, pgrid, tgrid, planck, rosseland

@@ -166,6 +166,12 @@ class Run:
                 open(self._path(name), "w").close()
         else:
             self._restart_planets(restart)            # also sets PhysicalTime
+        if p.opacity_law == 4:                        # InitOpacities (Opacity2.c:247-297)
+            indir = self.v["INPUTDIR"]
+            path = os.path.join(indir if indir.endswith("/") else indir + "/", "data_gasopacity_malygin.txt")
+            if not os.path.exists(path):
+                raise FileNotFoundError(f"Opacity file '{path}' not found. Stopping.")
+            d.set_opacity_table(*P.read_opacity_table(path))
         if p.corotating:                              # OmegaFrame = GetPsysInfo (sys, FREQUENCY), main.c:161
             P.corotating_frame(p, self.sys)
             d.set_frame(p.omega_frame)

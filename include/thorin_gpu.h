@@ -41,6 +41,7 @@ extern "C" {
 #define THORIN_OPA_ZHU12  1
 #define THORIN_OPA_LP85   2
 #define THORIN_OPA_CONST  3
+#define THORIN_OPA_SM03   4   /* Semenov et al. (2003) dust + Malygin et al. (2014) gas table */
 
 /* Field identifiers for upload/download.  Sizes are (nrad+1)*nsec doubles
  * (the reference allocates nrad+1 rows; row nrad is the outer v_rad face). */
@@ -309,6 +310,14 @@ int thorin_gpu_get_stream(thorin_disk *d, void **stream);
 int thorin_integrals_static(const double *rho, const double *vrad, const double *vtheta, const double *energy,
                             const double *surf, const double *rinf, const double *rsup, const double *rmed,
                             int nrad, int nsec, double omega_frame, double *out, void *stream);
+
+/* Gas opacity table of OpacityTable SM03 (InitOpacities, Opacity2.c:247-297:
+ * the file data_gasopacity_malygin.txt holds rows, cols, the pressure grid
+ * (rows values), the temperature grid (cols values), then the Planck and the
+ * Rosseland tables, rows*cols values each, pressure-major).  Copied to the
+ * device; required before the first step of an SM03 run. */
+int thorin_gpu_set_opacity_table(thorin_disk *d, int rows, int cols, const double *pgrid, const double *tgrid,
+                                 const double *planck, const double *rosseland);
 
 /* AdvanceSystemFromDrag (Drag.c:97-119): velocity kicks of the planets that
  * feel the disk from the Stokes drag of the gas in their own cell, for

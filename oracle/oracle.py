@@ -62,6 +62,8 @@ def lib(omp: bool = False):
         L.ora_algogas.argtypes = [C.c_void_p, C.POINTER(ThorinPlanets)]
         L.ora_integrals.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 5
         L.ora_set_sor_state.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int]
+        _D = C.POINTER(C.c_double)
+        L.ora_set_opacity_table.argtypes = [C.c_int, C.c_int, _D, _D, _D, _D]
         _libs[path] = L
     return _libs[path]
 
@@ -120,3 +122,8 @@ class OracleDisk:
 
     def set_sor_state(self, omega: float, domega: float, niterlast: int):
         self.L.ora_set_sor_state(self.h, omega, domega, niterlast)
+
+    def set_opacity_table(self, rows, cols, pgrid, tgrid, planck, rosseland):
+        """OpacityTable SM03 gas table (shared by all oracle disks)."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (pgrid, tgrid, planck, rosseland)]
+        self.L.ora_set_opacity_table(int(rows), int(cols), *[a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs])

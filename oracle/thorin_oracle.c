@@ -219,9 +219,136 @@ static double opacity_LP85(double rho, double T)          /* Opacity.c:201-227 *
   return kappa;
 }
 
+/* Semenov et al. (2003) dust and Malygin et al. (2014) gas opacities
+ * (Opacity2.c:25-245), Rosseland means.  The dust part is a fifth-order
+ * polynomial in T per temperature regime with the evaporation temperatures
+ * interpolated in log rho and sine smoothing across each transition; the
+ * gas part interpolates the tabulated Rosseland opacity bilinearly in
+ * pressure and temperature.  The reference's integer abs() of the
+ * temperature difference in the smoothing test is kept. */
+static int sm_rows, sm_cols;
+static double *sm_pgrid, *sm_tgrid, *sm_planck, *sm_rosseland;
+
+void ora_set_opacity_table(int rows, int cols, const double *pgrid, const double *tgrid, const double *planck,
+                           const double *rosseland)
+{
+  sm_rows = rows; sm_cols = cols;
+  sm_pgrid = (double *)malloc(sizeof(double) * rows);
+  sm_tgrid = (double *)malloc(sizeof(double) * cols);
+  sm_planck = (double *)malloc(sizeof(double) * rows * cols);
+  sm_rosseland = (double *)malloc(sizeof(double) * rows * cols);
+  memcpy(sm_pgrid, pgrid, sizeof(double) * rows);
+  memcpy(sm_tgrid, tgrid, sizeof(double) * cols);
+  memcpy(sm_planck, planck, sizeof(double) * rows * cols);
+  memcpy(sm_rosseland, rosseland, sizeof(double) * rows * cols);
+}
+
+static double sm_interp(const double *x, const double *y, int n, double x0)   /* Opacity2.c:28-41 */
+{
+  if (n <= 1) return y[0];
+  if (x0 < x[0]) return y[0];
+  if (x0 > x[n - 1]) return y[n - 1];
+  int i = 1;
+  while ((x[i] < x0) && (i < n - 1)) i++;
+  return y[i - 1] + (y[i] - y[i - 1]) * (x0 - x[i - 1]) / (x[i] - x[i - 1]);
+}
+
+static double opacity_malygin(double rho, double T_gas)     /* Opacity2.c:45-92, Rosseland */
+{
+  const int rows = sm_rows, cols = sm_cols;
+  const double *array = sm_rosseland;
+  double tP = 8.3144598 * 1.0e7 / 2.4 * rho * T_gas, tT = T_gas;
+  int Tlow = 0, Thigh = 1, Plow, Phigh;
+  if (tT < sm_tgrid[0]) return 0.0;
+  else if (tT > sm_tgrid[cols - 1]) tT = sm_tgrid[cols - 1];
+  if (tP < sm_pgrid[0]) tP = sm_pgrid[0];
+  else if (tP > sm_pgrid[rows - 1]) tP = sm_pgrid[rows - 1];
+  for (int i = 0; i < cols - 2; i++)
+    if (tT >= sm_tgrid[i]) { Tlow = i; Thigh = i + 1; }
+  double fac = ((double)rows) / log10(sm_pgrid[rows - 1] / sm_pgrid[0]);
+  Plow = (int)(fac * log10(tP / sm_pgrid[0]));
+  Plow = (Plow > 0) ? Plow : 0;
+  Plow = (Plow < rows - 2) ? Plow : rows - 2;
+  Phigh = Plow + 1;
+  double denom = 1.0 / ((sm_tgrid[Thigh] - sm_tgrid[Tlow]) * (sm_pgrid[Phigh] - sm_pgrid[Plow]));
+  double mul1 = (sm_tgrid[Thigh] - tT) * (sm_pgrid[Phigh] - tP);
+  double mul2 = (tT - sm_tgrid[Tlow]) * (sm_pgrid[Phigh] - tP);
+  double mul3 = (sm_tgrid[Thigh] - tT) * (tP - sm_pgrid[Plow]);
+  double mul4 = (tT - sm_tgrid[Tlow]) * (tP - sm_pgrid[Plow]);
+  return denom * (mul1 * array[Tlow + Plow * cols] + mul2 * array[Thigh + Plow * cols] +
+                  mul3 * array[Tlow + Phigh * cols] + mul4 * array[Thigh + Phigh * cols]);
+}
+
+/* Semenov et al. (2003) Rosseland dust coefficients (5 regimes x 6) and the
+ * evaporation temperatures log T_ev(log rho) of water ice, iron,
+ * orthopyroxene and olivine at 8 densities (published tables). */
+static const double SM_DUST_ROSS[6][6] = {
+  {0.244153190819473e-03, -0.191588103585833e-03, 0.229132294521843e-03, 0.454088516995579e-06, -0.389280273285906e-08,
+   0.319006401785413e-11},
+  {0.292517586013911e+01, -0.801305197566973e-01, 0.923001367150898e-03, -0.349287851393541e-05, 0.587151269508960e-08,
+   -0.371333580736933e-11},
+  {-0.125893536782728e+02, 0.160197849829283e+00, -0.582601311634824e-03, 0.110792133181219e-05, -0.105506373600323e-08,
+   0.404997080931974e-12},
+  {-0.192550086994197e+01, 0.354301116460647e-01, -0.127355043519226e-03, 0.233773506650911e-06, -0.207587683535083e-09,
+   0.728005983960845e-13},
+  {0.165244978116957e+01, -0.260479348963077e-02, 0.590717655258634e-05, -0.300202906476749e-08, 0.803836688553263e-12,
+   -0.916709776405312e-16},
+  {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}};
+static const double SM_LOGTT[8][4] = {
+  {2.03742650, 2.92168648, 2.95520654, 2.96801571}, {2.07188201, 2.95808585, 2.99122608, 2.99869516},
+  {2.11058971, 2.99738638, 3.02077549, 3.03181227}, {2.15533604, 3.04139269, 3.05269394, 3.06744284},
+  {2.20139712, 3.08990511, 3.08707121, 3.10619090}, {2.25527251, 3.14457421, 3.12417806, 3.14860265},
+  {2.31597035, 3.20736504, 3.16494737, 3.19589965}, {2.38738983, 3.28057837, 3.20978301, 3.24895362}};
+static const double SM_LOGRR[8] = {-18.0, -16.0, -14.0, -12.0, -10.0, -8.0, -6.0, -4.0};
+
+static double opacity_SM03(double rho, double T_dust)       /* Opacity2.c:96-245, Rosseland */
+{
+  const double *eD = &SM_DUST_ROSS[0][0];
+  double T_ev[4], temp[8], dT[5], T[5], aKext = 0.0;
+  if (T_dust <= 0.9) return 0.9;
+  double logrho = log10(rho);
+  for (int i = 0; i < 4; i++) {
+    for (int j = 0; j < 8; j++) temp[j] = SM_LOGTT[j][i];
+    T_ev[i] = pow(10.0, sm_interp(SM_LOGRR, temp, 8, logrho));
+  }
+  T[0] = T_ev[0]; T[1] = 275.0; T[2] = 425.0; T[3] = 680.0;
+  double tmax1 = (T_ev[1] > T_ev[2]) ? T_ev[1] : T_ev[2];
+  double tmax2 = (T_ev[2] > T_ev[3]) ? T_ev[2] : T_ev[3];
+  T[4] = (tmax1 < tmax2) ? tmax1 : tmax2;
+  dT[0] = 5.0; dT[1] = 5.0; dT[2] = 15.0; dT[3] = 5.0; dT[4] = 100.0;
+  int KK = 5;
+  if (T_dust <= (T[0] + dT[0])) KK = 0;
+  for (int i = 1; i < 5; i++)
+    if ((T_dust > (T[i - 1] + dT[i - 1])) && (T_dust <= (T[i] + dT[i]))) KK = i;
+  if (KK != 5) {
+    int smooth = 0;
+    for (int i = 0; i < 5; i++)
+      if (abs((int)(T_dust - T[i])) < dT[i]) smooth = 1;
+    if (smooth == 1) {
+      double T1 = T[KK] - dT[KK], T2 = T[KK] + dT[KK], TD = T_dust - T[KK], aKrL, aKrR;
+      int j = (KK + 1) * 6;
+      aKrL = ((((eD[j - 1] * T1 + eD[j - 2]) * T1 + eD[j - 3]) * T1 + eD[j - 4]) * T1 + eD[j - 5]) * T1 + eD[j - 6];
+      if (KK == 4) aKrR = 0.0;
+      else {
+        j = (KK + 2) * 6;
+        aKrR = ((((eD[j - 1] * T2 + eD[j - 2]) * T2 + eD[j - 3]) * T2 + eD[j - 4]) * T2 + eD[j - 5]) * T2 + eD[j - 6];
+      }
+      double AA = 0.5e0 * (aKrL - aKrR), BB = 0.5e0 * (aKrL + aKrR), FF = PI / 2.0 / dT[KK];
+      aKext = BB - AA * sin(FF * TD);
+    } else {
+      int j = (KK + 1) * 6;
+      aKext = ((((eD[j - 1] * T_dust + eD[j - 2]) * T_dust + eD[j - 3]) * T_dust + eD[j - 4]) * T_dust + eD[j - 5]) *
+                  T_dust + eD[j - 6];
+    }
+  }
+  double kappa_dust = aKext, kappa_gas = opacity_malygin(rho, T_dust);
+  return (kappa_dust > kappa_gas) ? kappa_dust : kappa_gas;
+}
+
 static double opacity_func(const ora_disk *d, double rho, double T)
 {
   switch (d->p.opacity_law) {
+  case THORIN_OPA_SM03: return opacity_SM03(rho, T);
   case THORIN_OPA_ZHU12: return opacity_ZHU12(rho, T);
   case THORIN_OPA_LP85: return opacity_LP85(rho, T);
   case THORIN_OPA_CONST: return d->p.parametric_opacity;

@@ -64,7 +64,28 @@ CASES = {
     "label_24x72": ("disk0", 24, 72, 6, 2, "LabelAdvection YES\n", True),
     "corot_24x72": ("disk0", 24, 72, 6, 2, "Frame COROTATING\n", True),
     "corot_peb_32x96": ("disk1", 32, 96, 6, 2, "Frame COROTATING\n", True),
+    # OpacityTable SM03 with a synthetic gas table (the run reads it from in/)
+    "sm03_24x72": ("disk0", 24, 72, 6, 2, "OpacityTable SM03\n", True),
 }
+
+
+def synthetic_gas_table(rows=40, cols=30):
+    """A smooth made-up gas-opacity table in the layout of
+    data_gasopacity_malygin.txt: log-spaced pressures and temperatures,
+    Rosseland kappa = 1e-3 (T/100)^1.5 (P/1)^0.2, Planck twice that."""
+    pgrid = np.logspace(-6.0, 8.0, rows)
+    tgrid = np.logspace(np.log10(50.0), 4.0, cols)
+    P, T = np.meshgrid(pgrid, tgrid, indexing="ij")
+    ross = 1e-3 * (T / 100.0) ** 1.5 * P ** 0.2
+    return rows, cols, pgrid, tgrid, 2.0 * ross.ravel(), ross.ravel()
+
+
+def write_gas_table(path, table):
+    rows, cols, pgrid, tgrid, planck, ross = table
+    with open(path, "w") as f:
+        f.write(f"{rows} {cols}\n")
+        for arr in (pgrid, tgrid, planck, ross):
+            f.write("\n".join("%.17g" % v for v in arr) + "\n")
 GAS = ["dens", "vrad", "vtheta", "temper"]
 PEB = ["pebbledens", "pebblevrad", "pebblevtheta"]
 SAMPLE_ROWS_FRAC = [0.0, 0.3, 0.5, 0.75, 1.0]
@@ -126,6 +147,11 @@ def make_case(name):
         par += f"PlanetConfig {os.path.join(work, 'planet.cfg')}\n"
         with open(os.path.join(work, "in.par"), "w") as f:
             f.write(par)
+        table = None
+        if "OpacityTable SM03" in extra:
+            table = synthetic_gas_table()
+            os.makedirs(os.path.join(work, "in"), exist_ok=True)
+            write_gas_table(os.path.join(work, "in", "data_gasopacity_malygin.txt"), table)
         run([THORIN, "-0" + flags, "in.par"], work)
         init = {k: read_dump(out, k, 0, nr, ns) for k in GAS}
         if kind == "disk1":
@@ -154,6 +180,9 @@ def make_case(name):
                "ntot": ntot, "ninterm": ninterm, "kind": np.array(kind)}
         for k, v in init.items():
             res["init_" + k] = v
+        if table is not None:
+            for key, v in zip(("sm_rows", "sm_cols", "sm_pgrid", "sm_tgrid", "sm_planck", "sm_rosseland"), table):
+                res[key] = v
         res.update(parse_log(log))
         names = GAS + (PEB if kind == "disk1" else []) + (["label"] if "LabelAdvection YES" in extra else [])
         rows = sorted({min(nr - 1, int(round(f * (nr - 1)))) for f in SAMPLE_ROWS_FRAC})

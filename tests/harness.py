@@ -29,6 +29,13 @@ def case_params(g, **kw):
     return p
 
 
+def opacity_table(disk, g):
+    """Give the disk the golden run's SM03 gas-opacity table, if it has one."""
+    if "sm_rows" in g.files:
+        disk.set_opacity_table(int(g["sm_rows"]), int(g["sm_cols"]), g["sm_pgrid"], g["sm_tgrid"], g["sm_planck"],
+                               g["sm_rosseland"])
+
+
 def start_state(disk, params, init_fields, seed=0):
     """Apply the measured initial state (perturbed Sigma, v_r = 0, pebble
     overrides) on top of a disk that holds the default initial fields, then

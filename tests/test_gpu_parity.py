@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "iso_24x72", "iso_peb_32x96",
          "dampinit_24x72", "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
          "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72", "label_24x72",
-         "corot_24x72", "corot_peb_32x96"]
+         "corot_24x72", "corot_peb_32x96", "sm03_24x72"]
 TOL = 1e-10
 
 
@@ -37,6 +37,7 @@ def test_gpu_vs_reference_golden(name):
     for k in init_fields:
         a, b = d.get(H.FIELD_IDS[k])[:n], g["init_" + k].ravel()
         assert H.rel_l2(a, b) < 1e-14, f"init {k}"
+    H.opacity_table(d, g)
     H.start_state(d, p, {"dens": g["init_dens"].ravel(), "temper": g["init_temper"].ravel()})
     sys_ = workloads.make_planets(p, [tuple(g["planet"])])
     tq = g["tqwk"]
@@ -76,7 +77,7 @@ def test_gpu_vs_reference_golden(name):
 @pytest.mark.parametrize("name", ["disk0_24x72", "disk1_32x96", "disk1_64x192_40", "iso_peb_32x96", "dampinit_24x72",
                                   "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
                                   "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72",
-                                  "label_24x72", "corot_24x72", "corot_peb_32x96"])
+                                  "label_24x72", "corot_24x72", "corot_peb_32x96", "sm03_24x72"])
 def test_gpu_vs_oracle_every_dt(name):
     """GPU and oracle run the same host N-body code, so they share the planet
     trajectory; compared after every DT, with the FARGO shifts and SOR counts
@@ -88,6 +89,7 @@ def test_gpu_vs_oracle_every_dt(name):
     o = O.OracleDisk(p)
     for x in (d, o):
         x.init_default()
+        H.opacity_table(x, g)
         H.start_state(x, p, {"dens": g["init_dens"].ravel(), "temper": g["init_temper"].ravel()})
     sg = workloads.make_planets(p, [tuple(g["planet"])])
     so = workloads.make_planets(p, [tuple(g["planet"])])

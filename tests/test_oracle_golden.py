@@ -16,7 +16,7 @@ from fargo_thorin_gb300 import workloads
 CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "iso_24x72", "iso_peb_32x96",
          "dampinit_24x72", "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
          "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72", "label_24x72",
-         "corot_24x72", "corot_peb_32x96"]
+         "corot_24x72", "corot_peb_32x96", "sm03_24x72"]
 
 
 def _run(name, force_planet=True):
@@ -28,6 +28,7 @@ def _run(name, force_planet=True):
     n = nr * ns
     for k in H.GAS + (["pebbledens", "pebblevrad", "pebblevtheta", "pebblesize", "pebblestokes"] if p.pebbles else []):
         np.testing.assert_array_equal(d.get(H.FIELD_IDS[k])[:n], g["init_" + k].ravel(), err_msg=f"init {k}")
+    H.opacity_table(d, g)
     H.start_state(d, p, {"dens": g["init_dens"].ravel(), "temper": g["init_temper"].ravel()})
     sys_ = workloads.make_planets(p, [tuple(g["planet"])])
     tq = g["tqwk"]
