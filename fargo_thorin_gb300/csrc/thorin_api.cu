@@ -134,6 +134,7 @@ struct thorin_disk {
   int cfl_first;
   int sor_first, Niterlast, Niterbest;
   int torque_pending = 0, ntorque = 0;
+  int sloppy_pass = 0;           // the once-per-DT CFL of SloppyCFL runs
   double doubling = 0.0;         // ParametricAccretion's doubling time, fixed at its first call
   thorin_torque torques[THORIN_MAXPLANETS];
   double omega, domega, omegabest;
@@ -313,7 +314,6 @@ static int check_supported(const thorin_params &p)
 {
   const char *bad = nullptr;
   if (p.nrad < 4 || p.nsec < 4 || (p.nsec & 1)) bad = "nrad, nsec >= 4 and nsec even (red-black SOR)";
-  else if (p.sloppy_cfl) bad = "SloppyCFL";
   if (bad) {
     g_last_error = std::string("unsupported option: ") + bad;
     return THORIN_ERR_ARG;
@@ -1049,7 +1049,7 @@ extern "C" int thorin_gpu_cfl(thorin_disk *d, double dt_remaining, double invdtr
   if (p.pebbles) aux_stokes(d->g, d->rho, d->psize, d->tau, d->s);       // PebbleStokesNumbers
   CflFinal f;
   memset(&f, 0, sizeof(f));
-  f.pebbles = p.pebbles;
+  f.pebbles = p.pebbles && !d->sloppy_pass;   // SloppyCFL: CriticalCharTime is never called (rate 0)
   f.first_call = d->cfl_first;
   f.deltaT = dt_remaining;
   f.invdtreb_sq = invdtreb_sq;
@@ -1645,13 +1645,28 @@ extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
   if (p.corotating && sys->nb < 1) { g_last_error = "Frame COROTATING needs a planet"; return THORIN_ERR_ARG; }
   if (d->timing) CUCHK(cudaEventRecord(d->ev[2], d->s));
   d->torque_pending = 1;                       // DumpTorqueNow: log the first substep's torques
+  if (p.sloppy_cfl) {
+    // SloppyCFL (-c): one CFL per DT, with the rebound and pebble rates of
+    // MinStepForRebound/CriticalCharTime, which are then never called (0),
+    // SourceEuler.c:221-226
+    int n;
+    d->sloppy_pass = 1;
+    const int rc = thorin_gpu_cfl(d, DT - dtemp, 0.0, &n);
+    d->sloppy_pass = 0;
+    RCHK(rc);
+    dt = DT / (double)n;
+  }
   while (dtemp < 0.999999999 * DT) {
     d->MassTaper = d->PhysicalTime / (p.mass_taper * 2.0 * H_MPI);
     d->MassTaper = (d->MassTaper > 1.0 ? 1.0 : pow(sin(d->MassTaper * H_MPI / 2.0), 2.0));
-    const double invdtreb_sq = min_step_for_rebound(sys);
-    int n;
-    RCHK(thorin_gpu_cfl(d, DT - dtemp, invdtreb_sq, &n));
-    dt = (DT - dtemp) / (double)n;
+    if (!p.sloppy_cfl) {
+      const double invdtreb_sq = min_step_for_rebound(sys);
+      int n;
+      RCHK(thorin_gpu_cfl(d, DT - dtemp, invdtreb_sq, &n));
+      dt = (DT - dtemp) / (double)n;
+    } else if (p.pebbles) {
+      aux_stokes(d->g, d->rho, d->psize, d->tau, d->s);       // PebbleStokesNumbers, every substep
+    }
     RCHK(thorin_gpu_accrete(d, sys, dt));
     dtemp += dt;
     double ind[2], rrho[THORIN_MAXPLANETS], rcs[THORIN_MAXPLANETS];

@@ -306,8 +306,6 @@ def derive(v: dict, *, sor_eps: float = SOREPS, sor_maxiters: int = SORMAXITERS,
 def check_supported(p: ThorinParams) -> None:
     """Raise for options outside the implemented hot path (fail loudly)."""
     bad = []
-    if p.sloppy_cfl:
-        bad.append("SloppyCFL (-c)")
     if bad:
         raise NotImplementedError("unsupported options: " + ", ".join(bad))
 

@@ -2502,14 +2502,17 @@ int ora_algogas(ora_disk *d, thorin_planets *sys)
   const thorin_params *p = &d->p;
   double dt, dtemp = 0.0, DT = p->dt;
   int status = THORIN_OK, nsub = 0;
+  if (p->sloppy_cfl) dt = DT / (double)ConditionCFL(d, DT - dtemp);   /* SourceEuler.c:221-227 */
   while (dtemp < 0.999999999 * DT) {
     d->MassTaper = d->PhysicalTime / (p->mass_taper * 2.0 * M_PI);
     d->MassTaper = (d->MassTaper > 1.0 ? 1.0 : pow(sin(d->MassTaper * M_PI / 2.0), 2.0));
     if (p->pebbles) PebbleStokesNumbers(d);
-    MinStepForRebound(d, sys);
-    if (p->pebbles) CriticalCharTime(d);
-    int n = ConditionCFL(d, DT - dtemp);
-    dt = (DT - dtemp) / (double)n;
+    if (!p->sloppy_cfl) {
+      MinStepForRebound(d, sys);
+      if (p->pebbles) CriticalCharTime(d);
+      int n = ConditionCFL(d, DT - dtemp);
+      dt = (DT - dtemp) / (double)n;
+    }
     for (int k = 0; k < sys->nb; k++) { d->heatsrc[k] = 0.0; d->heatsrc_index[k] = -1; }   /* InitHeating */
     AccreteOntoPlanets(d, sys, dt);
     if (p->prescribed_accretion) ParametricAccretion(d, sys, dt);

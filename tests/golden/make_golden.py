@@ -66,6 +66,8 @@ CASES = {
     "corot_peb_32x96": ("disk1", 32, 96, 6, 2, "Frame COROTATING\n", True),
     # OpacityTable SM03 with a synthetic gas table (the run reads it from in/)
     "sm03_24x72": ("disk0", 24, 72, 6, 2, "OpacityTable SM03\n", True),
+    # command-line switch -c: one CFL per DT (and a DT long enough to need substeps)
+    "sloppy_peb_32x96": ("disk1", 32, 96, 6, 2, "DT 0.4\n", True, None, "c"),
 }
 
 

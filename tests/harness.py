@@ -23,7 +23,7 @@ def load(name):
 
 def case_params(g, **kw):
     flags = str(g["flags"]) if "flags" in g.files else ""
-    p = derive(read_inpar(str(g["inpar"])), centrifugal_balance="b" in flags, **kw)
+    p = derive(read_inpar(str(g["inpar"])), centrifugal_balance="b" in flags, sloppy_cfl="c" in flags, **kw)
     if p.corotating:                                  # the frame of planet 0 (main.c:161)
         corotating_frame(p, workloads.make_planets(p, [tuple(g["planet"])]))
     return p

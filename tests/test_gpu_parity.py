@@ -16,7 +16,8 @@ pytestmark = pytest.mark.gpu
 CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "iso_24x72", "iso_peb_32x96",
          "dampinit_24x72", "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
          "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72", "label_24x72",
-         "corot_24x72", "corot_peb_32x96", "sm03_24x72"]
+         "corot_24x72", "corot_peb_32x96", "sm03_24x72",
+         "sloppy_peb_32x96"]
 TOL = 1e-10
 
 
@@ -47,8 +48,12 @@ def test_gpu_vs_reference_golden(name):
         sys_.x[0], sys_.y[0] = tq[step - 1][3], tq[step - 1][4]
         d.algogas(sys_)
         st = d.stats()
-        assert st.substeps == g["substeps"][step - 1]
-        if len(g["sor_niter"]):                     # no SOR in isothermal runs
+        # the reference's log gives one CFL line per DT under -c and SOR counts
+        # per solve, so the counts are compared per DT only without -c
+        counts = "c" not in (str(g["flags"]) if "flags" in g.files else "")
+        if counts:
+            assert st.substeps == g["substeps"][step - 1]
+        if counts and len(g["sor_niter"]):          # no SOR in isothermal runs
             assert st.sor_last_niter == g["sor_niter"][step - 1], f"SOR iterations at DT {step}"
         # torque log (tqwk0.dat) of the DT's first substep: disk acceleration on the planet
         t, ref = d.torques()[0], tq[step - 1]
@@ -77,7 +82,8 @@ def test_gpu_vs_reference_golden(name):
 @pytest.mark.parametrize("name", ["disk0_24x72", "disk1_32x96", "disk1_64x192_40", "iso_peb_32x96", "dampinit_24x72",
                                   "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
                                   "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72",
-                                  "label_24x72", "corot_24x72", "corot_peb_32x96", "sm03_24x72"])
+                                  "label_24x72", "corot_24x72", "corot_peb_32x96", "sm03_24x72",
+         "sloppy_peb_32x96"])
 def test_gpu_vs_oracle_every_dt(name):
     """GPU and oracle run the same host N-body code, so they share the planet
     trajectory; compared after every DT, with the FARGO shifts and SOR counts

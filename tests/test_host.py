@@ -66,17 +66,15 @@ def test_read_inpar_case_insensitive_and_defaults():
         P.read_inpar(text + "\nNoSuchKey 3\n")
 
 
-def test_unsupported_rejected(lib):
-    """SloppyCFL (-c) is outside the GPU path: refused by the host checks and
-    by thorin_gpu_create before any CUDA call."""
-    p = P.derive(P.read_inpar(workloads.inpar_text("disk1", 32, 96)), sloppy_cfl=True)
-    with pytest.raises(NotImplementedError, match="SloppyCFL"):
-        P.check_supported(p)
+def test_bad_options_rejected_before_cuda(lib):
+    """Grids the red-black SOR cannot colour are refused by thorin_gpu_create
+    before any CUDA call, with the reason in thorin_gpu_last_error."""
+    p = P.derive(P.read_inpar(workloads.inpar_text("disk1", 32, 95)))
     h = C.c_void_p()
     rc = lib.thorin_gpu_create(C.byref(p), C.byref(h))
-    assert rc == 1                                  # THORIN_ERR_ARG, before any CUDA call
+    assert rc == 1                                  # THORIN_ERR_ARG
     assert not h.value
-    assert "SloppyCFL" in lib.thorin_gpu_last_error().decode()
+    assert "nsec even" in lib.thorin_gpu_last_error().decode()
 
 
 def test_guiding_centre_frame_refused():

@@ -16,7 +16,8 @@ from fargo_thorin_gb300 import workloads
 CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "iso_24x72", "iso_peb_32x96",
          "dampinit_24x72", "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
          "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72", "label_24x72",
-         "corot_24x72", "corot_peb_32x96", "sm03_24x72"]
+         "corot_24x72", "corot_peb_32x96", "sm03_24x72",
+         "sloppy_peb_32x96"]
 
 
 def _run(name, force_planet=True):
@@ -36,12 +37,14 @@ def _run(name, force_planet=True):
     return g, p, d, sys_, tq, ntot, ninterm, n
 
 
-# In a corotating frame the frame's rotation rate comes from the planet's
-# N-body step each substep, which the reference takes from REBOUND (IAS15)
-# and the oracle from the library's RK4: the rate differs in the last bit,
-# and so do the fields (relative 1e-16 per DT).  These cases are compared
-# within 1e-12 instead of bit for bit.
-NBODY_FRAME = {"corot_24x72", "corot_peb_32x96"}
+# The planet is integrated outside the hydro path (REBOUND's IAS15 in the
+# reference, the library's RK4 here) and only its position at the start of
+# each DT is taken from the reference's torque log.  Where the hydro depends
+# on the planet within a DT -- the frame's rotation rate in a corotating
+# frame, the planet's position in the later substeps of a multi-substep DT
+# -- the fields differ in the last bit (relative 1e-16 per DT), so these
+# cases are compared within 1e-12 instead of bit for bit.
+NBODY_FRAME = {"corot_24x72", "corot_peb_32x96", "sloppy_peb_32x96"}
 
 
 def _same(a, b, err_msg, exact=True):
@@ -61,8 +64,12 @@ def test_oracle_bit_exact_vs_reference(name):
         sys_.x[0], sys_.y[0] = tq[step - 1][3], tq[step - 1][4]
         assert d.algogas(sys_) == 0
         st = d.stats()
-        assert st.substeps == g["substeps"][step - 1]
-        if len(g["sor_niter"]):                     # no SOR in isothermal runs
+        # the reference's log gives one CFL line per DT under -c and SOR counts
+        # per solve, so the counts are compared per DT only without -c
+        counts = "c" not in (str(g["flags"]) if "flags" in g.files else "")
+        if counts:
+            assert st.substeps == g["substeps"][step - 1]
+        if counts and len(g["sor_niter"]):          # no SOR in isothermal runs
             assert st.sor_last_niter == g["sor_niter"][step - 1]
         m, mom, e, _, _ = d.integrals()
         _same(np.array([m, mom, e]), np.array([g["mass"][step - 1], g["momentum"][step - 1], g["energy"][step - 1]]),
