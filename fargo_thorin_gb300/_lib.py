@@ -50,6 +50,18 @@ SIGNATURES = {
     "thorin_gpu_set_opacity_table": (C.c_int, [_P, C.c_int, C.c_int, _D, _D, _D, _D]),
     "thorin_gpu_get_torques": (C.c_int, [_P, C.POINTER(ThorinTorque), C.c_int, C.POINTER(C.c_int)]),
     "thorin_gpu_last_error": (C.c_char_p, []),
+    # learned SOR warm start (include/thorin_warmnet.h)
+    "thorin_warmnet_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(_P)]),
+    "thorin_warmnet_destroy": (C.c_int, [_P]),
+    "thorin_warmnet_set_params": (C.c_int, [_P, C.POINTER(C.c_float), C.c_int]),
+    "thorin_warmnet_get_params": (C.c_int, [_P, C.POINTER(C.c_float), C.c_int]),
+    "thorin_warmnet_forward": (C.c_int, [_P, C.c_int, C.POINTER(C.c_uint16), C.POINTER(C.c_float)]),
+    "thorin_warmnet_gradient": (C.c_int, [_P, C.c_int, C.POINTER(C.c_uint16), C.POINTER(C.c_float),
+                                          C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "thorin_warmnet_adam": (C.c_int, [_P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float]),
+    "thorin_gpu_warmstart": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_float]),
+    "thorin_gpu_warmstart_stats": (C.c_int, [_P, _P]),
+    "thorin_selftest_umma": (C.c_int, [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.POINTER(C.c_float)]),
     "thorin_planet_from_elements": (C.c_int, [C.POINTER(ThorinPlanets), C.c_int] + [C.c_float] * 9),
 }
 

@@ -11,6 +11,16 @@
 #include <string>
 #include <vector>
 #include "thorin_kernels.cuh"
+#include "../../include/thorin_warmnet.h"
+
+// learned SOR warm start (warmnet.cu)
+int wn_sor_predict(thorin_warmnet *n, int nr, int ns, double *T, const double *ml, const double *mlip,
+                   const double *mlim, const double *mljp, const double *mljm, const double *rhs, cudaStream_t s);
+int wn_sor_train(thorin_warmnet *n, int nr, int ns, const double *tk, const double *tconv, const double *ml,
+                 const double *mlip, const double *mlim, const double *mljp, const double *mljm, const double *rhs,
+                 float lr, cudaStream_t s);
+int wn_last_loss(thorin_warmnet *n, double *loss);
+int wn_dims(const thorin_warmnet *n, int *nr, int *ns);
 
 // Unit constants (src_main/fondam.h), evaluated with the host libm.
 #define H_PI 3.14159265358979323844
@@ -138,6 +148,11 @@ struct thorin_disk {
   double doubling = 0.0;         // ParametricAccretion's doubling time, fixed at its first call
   thorin_torque torques[THORIN_MAXPLANETS];
   double omega, domega, omegabest;
+  // learned warm start of the SOR solve (off unless attached)
+  thorin_warmnet *ws_net = nullptr;
+  int ws_mode = THORIN_WS_OFF, ws_restart = 0;
+  float ws_lr = 0.f;
+  thorin_ws_stats ws_st = {0, 0, 0.0};
   double heatsrc[THORIN_MAXPLANETS];
   int heatsrc_index[THORIN_MAXPLANETS], heatsrc_max;
   double gm1, gg1, drin, drout, invdphi, lr01, lr12, taueff_c, tirr4fac, rstar;
@@ -464,6 +479,37 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   CUCHK(cudaStreamSynchronize(d->s));
   d->nshift_h.assign(d->nr, 0);
   *out = d;
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode, int restart_every, float lr)
+{
+  if (!d || mode < THORIN_WS_OFF || mode > THORIN_WS_TRAIN || restart_every < 0 ||
+      (mode != THORIN_WS_OFF && !n) || (mode == THORIN_WS_TRAIN && !(lr > 0.f))) {
+    g_last_error = "warmstart: mode OFF/PREDICT/TRAIN, a network unless OFF, restart_every >= 0, lr > 0 to train";
+    return THORIN_ERR_ARG;
+  }
+  if (n) {
+    int nr = 0, ns = 0;
+    wn_dims(n, &nr, &ns);
+    if (nr != d->nr || ns != d->ns) {
+      g_last_error = "warmstart: the network's grid differs from the disk's";
+      return THORIN_ERR_ARG;
+    }
+  }
+  d->ws_net = mode == THORIN_WS_OFF ? nullptr : n;
+  d->ws_mode = mode;
+  d->ws_restart = restart_every;
+  d->ws_lr = lr;
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_warmstart_stats(thorin_disk *d, thorin_ws_stats *out)
+{
+  if (!d || !out) return THORIN_ERR_ARG;
+  CUCHK(cudaStreamSynchronize(d->s));
+  if (d->ws_net && d->ws_st.train_steps > 0) RCHK(wn_last_loss(d->ws_net, &d->ws_st.last_loss));
+  *out = d->ws_st;
   return THORIN_OK;
 }
 
@@ -1338,12 +1384,22 @@ extern "C" int thorin_gpu_get_torques(thorin_disk *d, thorin_torque *out, int ma
 
 // SuccessiveOverrelaxation driver: residual, then sweeps launched in chunks;
 // converged sweeps turn later launches into no-ops.
-static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *capped)
+static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *capped, bool learned = false)
 {
   const thorin_params &p = d->p;
+  // normres0 and the threshold always come from the start temperature as
+  // the reference has it; a learned start only moves T before the sweeps
   hydro_sor_resid0(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, omega, d->sor, d->s);
   KCHECK("SOR residual kernel");
+  const bool predict = learned && d->ws_net && d->ws_mode == THORIN_WS_PREDICT;
+  auto apply_net = [&]() -> int {
+    RCHK(wn_sor_predict(d->ws_net, d->nr, d->ns, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->s));
+    d->ws_st.predictions++;
+    return THORIN_OK;
+  };
+  if (predict) RCHK(apply_net());
   int first = 1, chunk = hint > 0 ? hint : 4;
+  if (predict && d->ws_restart > 0) chunk = d->ws_restart;
   *capped = 0;
   for (;;) {
     if (d->timing) CUCHK(cudaEventRecord(d->ev[0], d->s));
@@ -1368,6 +1424,10 @@ static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *ca
     }
     first += chunk;
     if (first > p.sor_maxiters) { *niter = p.sor_maxiters; *capped = 1; return THORIN_OK; }
+    if (predict && d->ws_restart > 0) {
+      RCHK(apply_net());      // re-apply the network to the current residual
+      continue;
+    }
     chunk = chunk < 64 ? 2 * chunk : 64;
   }
 }
@@ -1453,7 +1513,15 @@ static int energy_step(thorin_disk *d, double dt)
   if (d->omega > TH_OMEGAUPPER) { d->omega = TH_OMEGAUPPER; d->domega = -d->domega; }
   if (d->omega < 1.0) { d->omega = 1.0; d->domega = -d->domega; }
   int Niter, capped;
-  RCHK(sor_solve(d, d->omega, d->Niterlast, &Niter, &capped));
+  const bool train = d->ws_net && d->ws_mode == THORIN_WS_TRAIN;
+  const size_t tbytes = (size_t)d->nr * d->ns * sizeof(double);
+  if (train) CUCHK(cudaMemcpyAsync(d->tbackup, d->temper, tbytes, cudaMemcpyDeviceToDevice, d->s));
+  RCHK(sor_solve(d, d->omega, d->Niterlast, &Niter, &capped, true));
+  if (train) {
+    RCHK(wn_sor_train(d->ws_net, d->nr, d->ns, d->tbackup, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm,
+                      d->rhs, d->ws_lr, d->s));
+    d->ws_st.train_steps++;
+  }
   d->st.sor_calls++;
   d->st.sor_sweeps += Niter;
   d->st.sor_last_niter = Niter;

@@ -112,3 +112,95 @@ extern "C" int thorin_selftest_fp64_peak(double *gflops)
   *gflops = 2.0 * 8.0 * iters * (double)nb * nt / (ms * 1e6);
   return THORIN_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Tensor-core layout check: one CTA computes D[128][32] = A[128][64] *
+// B[32][64]^T with bf16 operands in the K-major, no-swizzle shared-memory
+// layout the network kernels use ([k/8][row][16 bytes]) and FP32
+// accumulation in TMEM.  The operands sit at the start of a 200 KB shared
+// buffer, so any reading of the descriptors stays inside the allocation.
+#include "tc_umma.cuh"
+
+__global__ void __launch_bounds__(128) k_selftest_umma(const uint16_t *__restrict__ A, const uint16_t *__restrict__ B,
+                                                        float *__restrict__ D, int *__restrict__ status)
+{
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *s = (unsigned char *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+  unsigned char *sA = s, *sB = s + 8 * 128 * 16;
+  uint64_t *bar = (uint64_t *)(sB + 8 * 32 * 16);
+  uint32_t *tslot = (uint32_t *)(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int c = tid; c < 128 * 8; c += 128) {       // row m, k-group kg
+    const int m = c >> 3, kg = c & 7;
+    *(uint4 *)(sA + kg * 2048 + m * 16) = *(const uint4 *)(A + m * 64 + kg * 8);
+  }
+  for (int c = tid; c < 32 * 8; c += 128) {
+    const int n = c >> 3, kg = c & 7;
+    *(uint4 *)(sB + kg * 512 + n * 16) = *(const uint4 *)(B + n * 64 + kg * 8);
+  }
+  if (tid == 0) umma::mbar_init(bar, 1);
+  if (warp == 0) umma::tmem_alloc(tslot, 32);
+  umma::fence_smem_async();
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  if (tid == 0) {
+    const uint32_t a0 = umma::smem_addr(sA), b0 = umma::smem_addr(sB);
+    for (int ks = 0; ks < 4; ks++)
+      umma::mma_bf16(tmem, umma::desc(a0 + ks * 4096, 2048, 128), umma::desc(b0 + ks * 1024, 512, 128),
+                     umma::idesc_bf16(128, 32), ks > 0);
+    umma::mma_commit(bar);
+  }
+  __syncwarp();
+  bool ok = umma::mbar_wait(bar, 0, 1LL << 26);
+  ok = __syncthreads_and(ok);
+  if (ok) {
+    umma::fence_after_sync();
+    float v[32];
+    umma::tmem_ld<32>(tmem + ((uint32_t)(warp * 32) << 16), v);
+    for (int n = 0; n < 32; n++) D[tid * 32 + n] = v[n];
+  } else if (tid == 0) {
+    *status = 1;
+    umma::mbar_wait(bar, 0, 1LL << 26);
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_dealloc(tmem, 32);
+}
+
+extern "C" int thorin_selftest_umma(const uint16_t *a, const uint16_t *b, float *d)
+{
+  if (!a || !b || !d) {
+    g_last_error = "selftest_umma: buffers required";
+    return THORIN_ERR_ARG;
+  }
+  uint16_t *dA = nullptr, *dB = nullptr;
+  float *dD = nullptr;
+  int *dS = nullptr, st = 0;
+  const int smem = 200 * 1024;
+  cudaError_t e = cudaMalloc((void **)&dA, 128 * 64 * 2);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&dB, 32 * 64 * 2);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&dD, 128 * 32 * 4);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&dS, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(dS, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(dA, a, 128 * 64 * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dB, b, 32 * 64 * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_selftest_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) {
+    k_selftest_umma<<<1, 128, smem>>>(dA, dB, dD, dS);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(d, dD, 128 * 32 * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&st, dS, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(dS);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("selftest_umma: ") + cudaGetErrorString(e);
+    return THORIN_ERR_CUDA;
+  }
+  if (st) {
+    g_last_error = "selftest_umma: the MMA completion wait timed out";
+    return THORIN_ERR_TIMEOUT;
+  }
+  return THORIN_OK;
+}

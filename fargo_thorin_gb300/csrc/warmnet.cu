@@ -1,0 +1,1001 @@
+// warmnet.cu -- the learned SOR warm start (include/thorin_warmnet.h).
+//
+// A polar-periodic convolutional encoder-decoder in BF16 with FP32
+// accumulation.  Every 3x3 convolution of the forward pass, of the input
+// gradient and of the weight gradient is an implicit GEMM on the tcgen05
+// tensor cores: 128 cells per tile, operands staged from global memory into
+// shared memory (im2col with the azimuthal wrap and the radial zero pad),
+// one thread issues the MMAs into a TMEM accumulator, the warpgroup reads it
+// back with tcgen05.ld for the epilogue.  Pooling, upsampling, ReLU masks,
+// the loss, gradient reductions and Adam are plain kernels.  All reductions
+// run in a fixed order, so results repeat bit for bit.
+#include <cuda_bf16.h>
+#include <cmath>
+#include <string>
+#include "thorin_kernels.cuh"
+#include "tc_umma.cuh"
+#include "../../include/thorin_warmnet.h"
+
+extern thread_local std::string g_last_error;
+
+typedef __nv_bfloat16 bf16;
+
+namespace {
+
+constexpr int WN_C = 32;          // feature channels
+constexpr int WN_NL = 8;          // layers: e0 e1 e2 e3 d2 d1 d0 out
+constexpr int WN_NIN = 6;         // input channels used
+constexpr float WN_YSCALE = 32.f; // output unit, in residual scales
+constexpr long long WN_WAIT = 1LL << 26;  // mbarrier polls before giving up
+
+struct LayerDef {
+  int cin, cout, cinp, coutp;
+};
+__host__ __device__ constexpr LayerDef layer_def(int l)
+{
+  return l == 0 ? LayerDef{WN_NIN, WN_C, THORIN_WN_INPUTS, WN_C}
+                : (l == WN_NL - 1 ? LayerDef{WN_C, 1, WN_C, 16} : LayerDef{WN_C, WN_C, WN_C, WN_C});
+}
+__host__ __device__ constexpr int layer_size(int l) { return layer_def(l).cout * 9 * layer_def(l).cin + layer_def(l).cout; }
+__host__ __device__ constexpr int layer_off(int l) { return l == 0 ? 0 : layer_off(l - 1) + layer_size(l - 1); }
+static_assert(layer_off(WN_NL) == THORIN_WN_NPARAMS, "parameter count");
+
+__device__ __forceinline__ unsigned char *align128(unsigned char *p)
+{
+  return (unsigned char *)(((uintptr_t)p + 127) & ~(uintptr_t)127);
+}
+
+// ---------------------------------------------------------------------------
+// Convolution, forward and input-gradient form.  out[p] = sum over taps and
+// input channels of in[p + tap] * W, with in = 0 outside rings 0..H-1 and the
+// azimuth periodic.  MODE 0: bf16 [P][N] = relu(acc + bias); MODE 1: float
+// [P] = acc[0] + bias[0]; MODE 2: float [P][N] = acc.
+// A tile: [kg][128 cells][16 B] (LBO 2048, SBO 128); B: [kg][N][16 B]
+// (LBO N*16, SBO 128); wk is [N][9*CIN] (K index = tap*CIN + c).
+struct ConvArgs {
+  const bf16 *in;
+  const bf16 *wk;
+  const float *bias;
+  int coutr;
+  void *out;
+  int B, H, W;
+  int *err;
+};
+
+template <int CIN, int N>
+constexpr int conv_smem() { return 9 * CIN * 128 * 2 + 9 * CIN * N * 2 + 128 + 128; }
+
+template <int CIN, int N, int MODE>
+__global__ void __launch_bounds__(128) k_wn_conv(ConvArgs a)
+{
+  constexpr int K = 9 * CIN, KG = K / 8, A_BYTES = KG * 128 * 16, B_BYTES = KG * N * 16;
+  constexpr uint32_t IDESC = umma::idesc_bf16(128, N);
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *sA = align128(smem_raw), *sB = sA + A_BYTES;
+  uint64_t *bar = (uint64_t *)(sB + B_BYTES);
+  uint32_t *tslot = (uint32_t *)(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  for (int c = tid; c < N * KG; c += 128) {
+    const int n = c / KG, kg = c - n * KG;
+    *(uint4 *)(sB + kg * N * 16 + n * 16) = *(const uint4 *)(a.wk + (size_t)n * K + kg * 8);
+  }
+  if (tid == 0) umma::mbar_init(bar, 1);
+  if (warp == 0) umma::tmem_alloc(tslot, 32);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tslot;
+
+  float bias[N];
+#pragma unroll
+  for (int n = 0; n < N; n++) bias[n] = (MODE != 2 && n < a.coutr) ? a.bias[n] : 0.f;
+
+  const long long HW = (long long)a.H * a.W, P = (long long)a.B * HW;
+  const long long ntiles = (P + 127) / 128;
+  uint32_t phase = 0;
+  bool ok = true;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long p = tile * 128 + tid;
+    const bool live = p < P;
+    int b = 0, i = 0, j = 0;
+    if (live) {
+      b = (int)(p / HW);
+      const long long rem = p - (long long)b * HW;
+      i = (int)(rem / a.W);
+      j = (int)(rem - (long long)i * a.W);
+    }
+#pragma unroll
+    for (int t = 0; t < 9; t++) {
+      const int ii = i + t / 3 - 1;
+      int jj = j + t % 3 - 1;
+      jj = jj < 0 ? jj + a.W : (jj >= a.W ? jj - a.W : jj);
+      const bool v = live && ii >= 0 && ii < a.H;
+      const uint4 *src = (const uint4 *)(a.in + (((long long)b * a.H + (v ? ii : 0)) * a.W + jj) * CIN);
+#pragma unroll
+      for (int c8 = 0; c8 < CIN / 8; c8++) {
+        const uint4 val = v ? src[c8] : make_uint4(0u, 0u, 0u, 0u);
+        *(uint4 *)(sA + (t * (CIN / 8) + c8) * 2048 + tid * 16) = val;
+      }
+    }
+    umma::fence_smem_async();
+    __syncthreads();
+    if (tid == 0) {
+      umma::fence_after_sync();
+      const uint32_t a0 = umma::smem_addr(sA), b0 = umma::smem_addr(sB);
+#pragma unroll
+      for (int ks = 0; ks < K / 16; ks++)
+        umma::mma_bf16(tmem, umma::desc(a0 + ks * 4096, 2048, 128), umma::desc(b0 + ks * 2 * N * 16, N * 16, 128), IDESC,
+                       ks > 0);
+      umma::mma_commit(bar);
+    }
+    __syncwarp();
+    ok = umma::mbar_wait(bar, phase, WN_WAIT);
+    ok = __syncthreads_and(ok);
+    phase ^= 1u;
+    if (!ok) break;
+    umma::fence_after_sync();
+    float v[N];
+    umma::tmem_ld<N>(tmem + ((uint32_t)(warp * 32) << 16), v);
+    if (live) {
+      if (MODE == 0) {
+        uint4 *dst = (uint4 *)((bf16 *)a.out + p * N);
+#pragma unroll
+        for (int q = 0; q < N / 8; q++) {
+          __nv_bfloat162 h[4];
+#pragma unroll
+          for (int e = 0; e < 4; e++)
+            h[e] = __floats2bfloat162_rn(fmaxf(v[8 * q + 2 * e] + bias[8 * q + 2 * e], 0.f),
+                                         fmaxf(v[8 * q + 2 * e + 1] + bias[8 * q + 2 * e + 1], 0.f));
+          dst[q] = *(uint4 *)h;
+        }
+      } else if (MODE == 1) {
+        ((float *)a.out)[p] = v[0] + bias[0];
+      } else {
+        float4 *dst = (float4 *)((float *)a.out + p * N);
+#pragma unroll
+        for (int q = 0; q < N / 4; q++) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+  }
+  if (!ok) {
+    if (tid == 0) atomicExch(a.err, 1);
+    umma::mbar_wait(bar, phase ^ 1u, WN_WAIT);   // let an MMA still in flight finish before freeing TMEM
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_dealloc(tmem, 32);
+}
+
+// ---------------------------------------------------------------------------
+// Weight gradient: D[(tap, ci)][co] = sum over cells p of in[p + tap][ci] *
+// gout[p][co], K = cells (128 per chunk).  Rows 9*CIN are cut into M tiles of
+// 128; each tile is [kg = cell/8][row][16 B] (LBO 2048, SBO 128), gout is
+// [kg][co][16 B] (LBO N*16, SBO 128).  Each block accumulates its chunks in
+// TMEM and writes its partial D and the partial bias gradient.
+struct WgradArgs {
+  const bf16 *in;
+  const bf16 *gout;
+  float *part;       // [grid][9*CIN][N], then [grid][N]
+  int B, H, W;
+  int *err;
+};
+
+template <int CIN, int N>
+struct WgradShape {
+  static constexpr int R = 9 * CIN, MT = (R + 127) / 128, A_TILE = 16 * 128 * 16, A_BYTES = MT * A_TILE,
+                       B_BYTES = 16 * N * 16, COLS = MT * N <= 32 ? 32 : (MT * N <= 64 ? 64 : 128),
+                       SMEM = A_BYTES + B_BYTES + 4 * N * 4 + 128 + 128;
+};
+
+template <int CIN, int N>
+__global__ void __launch_bounds__(128) k_wn_wgrad(WgradArgs a)
+{
+  using S = WgradShape<CIN, N>;
+  constexpr uint32_t IDESC = umma::idesc_bf16(128, N);
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *sA = align128(smem_raw), *sB = sA + S::A_BYTES;
+  float *sred = (float *)(sB + S::B_BYTES);
+  uint64_t *bar = (uint64_t *)(sred + 4 * N);
+  uint32_t *tslot = (uint32_t *)(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  for (int o = tid * 16; o < S::A_BYTES; o += 128 * 16) *(uint4 *)(sA + o) = make_uint4(0u, 0u, 0u, 0u);
+  if (tid == 0) umma::mbar_init(bar, 1);
+  if (warp == 0) umma::tmem_alloc(tslot, S::COLS);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tslot;
+
+  float db[N];
+#pragma unroll
+  for (int n = 0; n < N; n++) db[n] = 0.f;
+  const long long HW = (long long)a.H * a.W, P = (long long)a.B * HW;
+  const long long nchunks = (P + 127) / 128;
+  uint32_t phase = 0;
+  bool ok = true;
+  int started = 0;
+  for (long long ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+    const long long p = ch * 128 + tid;
+    const bool live = p < P;
+    int b = 0, i = 0, j = 0;
+    if (live) {
+      b = (int)(p / HW);
+      const long long rem = p - (long long)b * HW;
+      i = (int)(rem / a.W);
+      j = (int)(rem - (long long)i * a.W);
+    }
+    const int kg = tid >> 3, kk = (tid & 7) * 2;
+    {
+      const uint4 *src = (const uint4 *)(a.gout + (live ? p : 0) * N);
+#pragma unroll
+      for (int q = 0; q < N / 8; q++) {
+        uint4 val = live ? src[q] : make_uint4(0u, 0u, 0u, 0u);
+        const bf16 *h = (const bf16 *)&val;
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+          const int n = 8 * q + e;
+          *(bf16 *)(sB + kg * N * 16 + n * 16 + kk) = h[e];
+          db[n] += __bfloat162float(h[e]);
+        }
+      }
+    }
+#pragma unroll 1
+    for (int t = 0; t < 9; t++) {
+      const int ii = i + t / 3 - 1;
+      int jj = j + t % 3 - 1;
+      jj = jj < 0 ? jj + a.W : (jj >= a.W ? jj - a.W : jj);
+      const bool v = live && ii >= 0 && ii < a.H;
+      const uint4 *src = (const uint4 *)(a.in + (((long long)b * a.H + (v ? ii : 0)) * a.W + jj) * CIN);
+#pragma unroll
+      for (int q = 0; q < CIN / 8; q++) {
+        uint4 val = v ? src[q] : make_uint4(0u, 0u, 0u, 0u);
+        const bf16 *h = (const bf16 *)&val;
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+          const int r = t * CIN + 8 * q + e;
+          *(bf16 *)(sA + (r >> 7) * S::A_TILE + kg * 2048 + (r & 127) * 16 + kk) = h[e];
+        }
+      }
+    }
+    umma::fence_smem_async();
+    __syncthreads();
+    if (tid == 0) {
+      umma::fence_after_sync();
+      const uint32_t a0 = umma::smem_addr(sA), b0 = umma::smem_addr(sB);
+#pragma unroll
+      for (int q = 0; q < S::MT; q++)
+#pragma unroll
+        for (int ks = 0; ks < 8; ks++)
+          umma::mma_bf16(tmem + q * N, umma::desc(a0 + q * S::A_TILE + ks * 4096, 2048, 128),
+                         umma::desc(b0 + ks * 2 * N * 16, N * 16, 128), IDESC, started || ks > 0);
+      umma::mma_commit(bar);
+    }
+    __syncwarp();
+    ok = umma::mbar_wait(bar, phase, WN_WAIT);
+    ok = __syncthreads_and(ok);
+    phase ^= 1u;
+    started = 1;
+    if (!ok) break;
+  }
+  if (!ok) {
+    if (tid == 0) atomicExch(a.err, 1);
+    umma::mbar_wait(bar, phase ^ 1u, WN_WAIT);
+  } else {
+    umma::fence_after_sync();
+    float *pd = a.part + (size_t)blockIdx.x * S::R * N;
+#pragma unroll 1
+    for (int q = 0; q < S::MT; q++) {
+      float v[N];
+      umma::tmem_ld<N>(tmem + q * N + ((uint32_t)(warp * 32) << 16), v);
+      const int r = q * 128 + warp * 32 + lane;
+      if (r < S::R) {
+#pragma unroll
+        for (int n = 0; n < N; n++) pd[(size_t)r * N + n] = started ? v[n] : 0.f;
+      }
+    }
+  }
+  // bias gradient: fixed-order reduction over the block
+#pragma unroll
+  for (int n = 0; n < N; n++) {
+    float s = db[n];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) sred[warp * N + n] = s;
+  }
+  __syncthreads();
+  if (tid < N)
+    a.part[(size_t)gridDim.x * S::R * N + (size_t)blockIdx.x * N + tid] =
+        ((sred[tid] + sred[N + tid]) + sred[2 * N + tid]) + sred[3 * N + tid];
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_dealloc(tmem, S::COLS);
+}
+
+// Sum the block partials in block order and scatter into the FP32 gradient
+// layout W[cout][tap][cin], bias[cout].
+__global__ void k_wn_wgrad_reduce(const float *__restrict__ part, int nblk, int cin, int cinp, int cout, int n,
+                                  float *__restrict__ gw)
+{
+  const int R = 9 * cinp;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < R * n) {
+    const int r = idx / n, co = idx - r * n, t = r / cinp, ci = r - t * cinp;
+    if (ci >= cin || co >= cout) return;
+    float s = 0.f;
+    for (int k = 0; k < nblk; k++) s += part[(size_t)k * R * n + idx];
+    gw[(co * 9 + t) * cin + ci] = s;
+  } else if (idx < R * n + cout) {
+    const int co = idx - R * n;
+    float s = 0.f;
+    const float *pb = part + (size_t)nblk * R * n;
+    for (int k = 0; k < nblk; k++) s += pb[(size_t)k * n + co];
+    gw[cout * 9 * cin + co] = s;
+  }
+}
+
+// FP32 master W[cout][tap][cin] -> wk [coutp][9*cinp] and the flipped,
+// transposed wt [cinp][9*coutp] (input-gradient convolution).
+__global__ void k_wn_pack(const float *__restrict__ w, int cin, int cout, int cinp, int coutp, bf16 *__restrict__ wk,
+                          bf16 *__restrict__ wt)
+{
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nk = coutp * 9 * cinp;
+  if (idx < nk) {
+    const int n = idx / (9 * cinp), k = idx - n * 9 * cinp, t = k / cinp, ci = k - t * cinp;
+    wk[idx] = __float2bfloat16_rn((n < cout && ci < cin) ? w[(n * 9 + t) * cin + ci] : 0.f);
+  } else if (idx < 2 * nk) {
+    const int o = idx - nk;
+    const int ci = o / (9 * coutp), k = o - ci * 9 * coutp, t = k / coutp, co = k - t * coutp;
+    wt[o] = __float2bfloat16_rn((co < cout && ci < cin) ? w[(co * 9 + (8 - t)) * cin + ci] : 0.f);
+  }
+}
+
+// 2x2 average pooling, bf16 [B][H][W][32] -> [B][H/2][W/2][32]
+__global__ void k_wn_pool(const bf16 *__restrict__ a, bf16 *__restrict__ p, int B, int H, int W)
+{
+  const long long n = (long long)B * (H / 2) * (W / 2) * WN_C;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const int c = (int)(idx % WN_C);
+  long long q = idx / WN_C;
+  const int j = (int)(q % (W / 2));
+  q /= W / 2;
+  const int i = (int)(q % (H / 2));
+  const int b = (int)(q / (H / 2));
+  const bf16 *s = a + (((long long)b * H + 2 * i) * W + 2 * j) * WN_C + c;
+  const float v = (__bfloat162float(s[0]) + __bfloat162float(s[WN_C])) +
+                  (__bfloat162float(s[(long long)W * WN_C]) + __bfloat162float(s[(long long)W * WN_C + WN_C]));
+  p[idx] = __float2bfloat16_rn(0.25f * v);
+}
+
+// u = up2(low) + skip, bf16 at the finer level [B][H][W][32]
+__global__ void k_wn_upadd(const bf16 *__restrict__ low, const bf16 *__restrict__ skip, bf16 *__restrict__ u, int B,
+                           int H, int W)
+{
+  const long long n = (long long)B * H * W * WN_C;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const int c = (int)(idx % WN_C);
+  long long q = idx / WN_C;
+  const int j = (int)(q % W);
+  q /= W;
+  const int i = (int)(q % H);
+  const int b = (int)(q / H);
+  const float v = __bfloat162float(low[(((long long)b * (H / 2) + i / 2) * (W / 2) + j / 2) * WN_C + c]) +
+                  __bfloat162float(skip[idx]);
+  u[idx] = __float2bfloat16_rn(v);
+}
+
+// bf16 gradient = g * (act > 0)
+__global__ void k_wn_relu_mask(const float *__restrict__ g, const bf16 *__restrict__ act, bf16 *__restrict__ out,
+                               long long n)
+{
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  out[idx] = __float2bfloat16_rn(__bfloat162float(act[idx]) > 0.f ? g[idx] : 0.f);
+}
+
+// coarse gradient of up2: sum of the 4 fine children, then the ReLU mask of
+// the coarse activation; bf16 out at the coarse level [B][H/2][W/2][32]
+__global__ void k_wn_downsum_mask(const float *__restrict__ gu, const bf16 *__restrict__ act, bf16 *__restrict__ out,
+                                  int B, int H, int W)
+{
+  const long long n = (long long)B * (H / 2) * (W / 2) * WN_C;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const int c = (int)(idx % WN_C);
+  long long q = idx / WN_C;
+  const int j = (int)(q % (W / 2));
+  q /= W / 2;
+  const int i = (int)(q % (H / 2));
+  const int b = (int)(q / (H / 2));
+  const float *s = gu + (((long long)b * H + 2 * i) * W + 2 * j) * WN_C + c;
+  const float v = (s[0] + s[WN_C]) + (s[(long long)W * WN_C] + s[(long long)W * WN_C + WN_C]);
+  out[idx] = __float2bfloat16_rn(__bfloat162float(act[idx]) > 0.f ? v : 0.f);
+}
+
+// fine gradient of the pooling: ga += 0.25 * gp(coarse); the result then
+// gets the ReLU mask of the fine activation, bf16 out
+__global__ void k_wn_unpool_mask(const float *__restrict__ ga, const float *__restrict__ gp, const bf16 *__restrict__ act,
+                                 bf16 *__restrict__ out, int B, int H, int W)
+{
+  const long long n = (long long)B * H * W * WN_C;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const int c = (int)(idx % WN_C);
+  long long q = idx / WN_C;
+  const int j = (int)(q % W);
+  q /= W;
+  const int i = (int)(q % H);
+  const int b = (int)(q / H);
+  const float v = ga[idx] + 0.25f * gp[(((long long)b * (H / 2) + i / 2) * (W / 2) + j / 2) * WN_C + c];
+  out[idx] = __float2bfloat16_rn(__bfloat162float(act[idx]) > 0.f ? v : 0.f);
+}
+
+// loss = sum over rings 1..H-2 of (y - t)^2 * inv_n; gy16[p][0] = dloss/dy
+__global__ void k_wn_loss(const float *__restrict__ y, const float *__restrict__ t, int B, int H, int W, float inv_n,
+                          bf16 *__restrict__ gy16, double *__restrict__ lpart)
+{
+  const long long P = (long long)B * H * W;
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double l = 0.0;
+  if (p < P) {
+    const int i = (int)((p / W) % H);
+    float g = 0.f;
+    if (i >= 1 && i <= H - 2) {
+      const float d = y[p] - t[p];
+      l = (double)d * (double)d;
+      g = 2.f * d * inv_n;
+    }
+    uint4 z[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+    ((bf16 *)z)[0] = __float2bfloat16_rn(g);
+    uint4 *dst = (uint4 *)(gy16 + p * 16);
+    dst[0] = z[0];
+    dst[1] = z[1];
+  }
+  l = block_reduce(l, OpAdd(), 0.0);
+  if (threadIdx.x == 0) lpart[blockIdx.x] = l;
+}
+
+// ordered sum of n partials times scale -> *out (one warp)
+__global__ void k_wn_sum(const double *__restrict__ part, int n, double scale, double *__restrict__ out)
+{
+  double s = 0.0;
+  for (int k = threadIdx.x; k < n; k += 32) s += part[k];
+  s = warp_reduce(s, OpAdd());
+  if (threadIdx.x == 0) *out = s * scale;
+}
+
+__global__ void k_wn_sqnorm(const float *__restrict__ g, int n, double *__restrict__ part)
+{
+  double s = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) s += (double)g[k] * g[k];
+  s = block_reduce(s, OpAdd(), 0.0);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void k_wn_adam(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m,
+                          float *__restrict__ v, int n, float lr, float b1, float b2, float eps, float bc1, float bc2,
+                          const double *__restrict__ sqnorm, float max_norm)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double nrm = sqrt(*sqnorm);
+  const float clip = (max_norm > 0.f && nrm > (double)max_norm) ? (float)((double)max_norm / nrm) : 1.f;
+  const float gk = g[k] * clip;
+  const float mk = b1 * m[k] + (1.f - b1) * gk, vk = b2 * v[k] + (1.f - b2) * gk * gk;
+  m[k] = mk;
+  v[k] = vk;
+  w[k] -= lr * (mk / bc1) / (sqrtf(vk / bc2) + eps);
+}
+
+// ---------------------------------------------------------------------------
+// Coupling to the SOR system (rows 1..nr-2 are the unknowns).
+__device__ __forceinline__ double sor_resid(const double *T, const double *ml, const double *mlip, const double *mlim,
+                                            const double *mljp, const double *mljm, const double *rhs, int l, int lip,
+                                            int lim, int ljp, int ljm)
+{
+  return T[l] * ml[l] + T[lip] * mlip[l] + T[lim] * mlim[l] + T[ljp] * mljp[l] + T[ljm] * mljm[l] - rhs[l];
+}
+
+struct SorSys {
+  const double *ml, *mlip, *mlim, *mljp, *mljm, *rhs;
+};
+
+// partial sums of |r / Ml| over the unknowns (grid-stride, block order)
+__global__ void k_wn_scale(int nr, int ns, const double *__restrict__ T, SorSys m, double *__restrict__ part)
+{
+  double s = 0.0;
+  const long long n = (long long)(nr - 2) * ns;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(q / ns), j = (int)(q % ns), l = j + i * ns;
+    const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+    s += fabs(sor_resid(T, m.ml, m.mlip, m.mlim, m.mljp, m.mljm, m.rhs, l, l + ns, l - ns, ljp, ljm) / m.ml[l]);
+  }
+  s = block_reduce(s, OpAdd(), 0.0);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// network input x[l][16] and the Jacobi step jac = -r / Ml
+__global__ void k_wn_features(int nr, int ns, const double *__restrict__ T, SorSys m, const double *__restrict__ scale,
+                              bf16 *__restrict__ x, double *__restrict__ jac)
+{
+  const long long n = (long long)nr * ns;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int i = (int)(q / ns), j = (int)(q % ns), l = (int)q;
+  float f[WN_NIN] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  double jl = 0.0;
+  if (i >= 1 && i <= nr - 2) {
+    const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+    const double ml = m.ml[l];
+    const double rj = sor_resid(T, m.ml, m.mlip, m.mlim, m.mljp, m.mljm, m.rhs, l, l + ns, l - ns, ljp, ljm) / ml;
+    jl = -rj;
+    const double s = *scale;
+    const double rs = s > 0.0 ? rj / s : 0.0;
+    f[0] = (float)fmin(fmax(rs, -16.0), 16.0);
+    const double w1 = -m.mlip[l] / ml, w2 = -m.mlim[l] / ml, w3 = -m.mljp[l] / ml, w4 = -m.mljm[l] / ml;
+    f[1] = (float)w1; f[2] = (float)w2; f[3] = (float)w3; f[4] = (float)w4;
+    f[5] = (float)(-log(fmax(1.0 - (((w1 + w2) + w3) + w4), 1e-6)) * 0.25);
+  }
+  jac[l] = jl;
+  uint4 z[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+  bf16 *h = (bf16 *)z;
+#pragma unroll
+  for (int c = 0; c < WN_NIN; c++) h[c] = __float2bfloat16_rn(f[c]);
+  uint4 *dst = (uint4 *)(x + q * THORIN_WN_INPUTS);
+  dst[0] = z[0];
+  dst[1] = z[1];
+}
+
+// T += jac + scale * YSCALE * y on the unknowns; a non-positive result keeps T
+__global__ void k_wn_apply(int nr, int ns, double *__restrict__ T, const double *__restrict__ jac,
+                           const float *__restrict__ y, const double *__restrict__ scale)
+{
+  const long long n = (long long)(nr - 2) * ns;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const long long l = q + ns;
+  const double t = T[l] + jac[l] + (*scale) * (double)WN_YSCALE * (double)y[l];
+  if (t > 0.0) T[l] = t;
+}
+
+// training target (T_conv - T_k - jac) / (scale * YSCALE); zero off the unknowns
+__global__ void k_wn_target(int nr, int ns, const double *__restrict__ tconv, const double *__restrict__ tk,
+                            const double *__restrict__ jac, const double *__restrict__ scale, float *__restrict__ tgt)
+{
+  const long long n = (long long)nr * ns;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int i = (int)(q / ns);
+  const double s = *scale;
+  tgt[q] = (i >= 1 && i <= nr - 2 && s > 0.0) ? (float)((tconv[q] - tk[q] - jac[q]) / (s * (double)WN_YSCALE)) : 0.f;
+}
+
+inline unsigned nblk(long long n, int bs = 256) { return (unsigned)((n + bs - 1) / bs); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct thorin_warmnet {
+  int nr, ns, maxb, nsm;
+  cudaStream_t own;
+  float *w, *g, *m, *v;                  // FP32 parameters, gradient, Adam moments
+  bf16 *wk[WN_NL], *wt[WN_NL];
+  bf16 *x;                               // [B][H][W][16]
+  bf16 *act[14];                         // a0 p1 a1 p2 a2 p3 a3 u2 b2 u1 b1 u0 b0, gy16
+  float *y, *tgt;
+  float *gf[4], *ga[4];                  // FP32 gradient scratch per level
+  bf16 *gb[4];                           // bf16 masked gradient per level
+  float *part;                           // weight-gradient partials
+  int part_blocks;
+  double *dscal;                         // [0] loss, [1] grad sq-norm, [2] residual scale, partials from 8
+  double *jac;                           // Jacobi step of the coupled disk
+  int *err;
+  int adam_t;
+  int B;                                 // batch of the last forward
+};
+
+enum { A0, P1, A1, P2, A2, P3, A3, U2, B2, U1, B1, U0, B0, GY16 };
+
+static int wn_fail(const char *what, cudaError_t e)
+{
+  g_last_error = std::string("warmnet: ") + what + ": " + cudaGetErrorString(e);
+  return THORIN_ERR_CUDA;
+}
+#define RCHK_WN(...)              \
+  do {                            \
+    const int r_ = (__VA_ARGS__); \
+    if (r_) return r_;            \
+  } while (0)
+#define WNCHK(call)                                    \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return wn_fail(#call, e_);  \
+  } while (0)
+
+template <int CIN, int N, int MODE>
+static int conv_launch(thorin_warmnet *n, const bf16 *in, const bf16 *wk, const float *bias, int coutr, void *out,
+                       int B, int H, int W, cudaStream_t s)
+{
+  constexpr int SM = conv_smem<CIN, N>();
+  static bool attr = false;
+  if (!attr) {
+    WNCHK(cudaFuncSetAttribute(k_wn_conv<CIN, N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
+    attr = true;
+  }
+  const long long tiles = ((long long)B * H * W + 127) / 128;
+  const int grid = (int)(tiles < 2LL * n->nsm ? tiles : 2LL * n->nsm);
+  ConvArgs a{in, wk, bias, coutr, out, B, H, W, n->err};
+  k_wn_conv<CIN, N, MODE><<<grid, 128, SM, s>>>(a);
+  g_thorin_launches++;
+  return THORIN_OK;
+}
+
+template <int CIN, int N>
+static int wgrad_launch(thorin_warmnet *n, int layer, const bf16 *in, const bf16 *gout, int B, int H, int W,
+                        cudaStream_t s)
+{
+  using S = WgradShape<CIN, N>;
+  static bool attr = false;
+  if (!attr) {
+    WNCHK(cudaFuncSetAttribute(k_wn_wgrad<CIN, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM));
+    attr = true;
+  }
+  const long long chunks = ((long long)B * H * W + 127) / 128;
+  const int grid = (int)(chunks < n->part_blocks ? chunks : n->part_blocks);
+  WgradArgs a{in, gout, n->part, B, H, W, n->err};
+  k_wn_wgrad<CIN, N><<<grid, 128, S::SMEM, s>>>(a);
+  g_thorin_launches++;
+  const LayerDef L = layer_def(layer);
+  const int tot = 9 * L.cinp * N + L.cout;
+  k_wn_wgrad_reduce<<<nblk(tot), 256, 0, s>>>(n->part, grid, L.cin, L.cinp, L.cout, N, n->g + layer_off(layer));
+  g_thorin_launches++;
+  return THORIN_OK;
+}
+
+static void pack_all(thorin_warmnet *n, cudaStream_t s)
+{
+  for (int l = 0; l < WN_NL; l++) {
+    const LayerDef L = layer_def(l);
+    k_wn_pack<<<nblk(2LL * L.coutp * 9 * L.cinp), 256, 0, s>>>(n->w + layer_off(l), L.cin, L.cout, L.cinp, L.coutp,
+                                                              n->wk[l], n->wt[l]);
+    g_thorin_launches++;
+  }
+}
+
+static inline const float *bias_of(const thorin_warmnet *n, int l)
+{
+  const LayerDef L = layer_def(l);
+  return n->w + layer_off(l) + L.cout * 9 * L.cin;
+}
+
+// forward pass of the batch in n->x -> n->y
+static int wn_forward(thorin_warmnet *n, int B, cudaStream_t s)
+{
+  const int H = n->nr, W = n->ns;
+  int h[4] = {H, H / 2, H / 4, H / 8}, w[4] = {W, W / 2, W / 4, W / 8};
+  bf16 **A = n->act;
+  auto pool = [&](const bf16 *a, bf16 *p, int lv) {
+    k_wn_pool<<<nblk((long long)B * h[lv + 1] * w[lv + 1] * WN_C), 256, 0, s>>>(a, p, B, h[lv], w[lv]);
+    g_thorin_launches++;
+  };
+  auto upadd = [&](const bf16 *low, const bf16 *skip, bf16 *u, int lv) {
+    k_wn_upadd<<<nblk((long long)B * h[lv] * w[lv] * WN_C), 256, 0, s>>>(low, skip, u, B, h[lv], w[lv]);
+    g_thorin_launches++;
+  };
+  RCHK_WN(conv_launch<16, 32, 0>(n, n->x, n->wk[0], bias_of(n, 0), 32, A[A0], B, h[0], w[0], s));
+  pool(A[A0], A[P1], 0);
+  RCHK_WN(conv_launch<32, 32, 0>(n, A[P1], n->wk[1], bias_of(n, 1), 32, A[A1], B, h[1], w[1], s));
+  pool(A[A1], A[P2], 1);
+  RCHK_WN(conv_launch<32, 32, 0>(n, A[P2], n->wk[2], bias_of(n, 2), 32, A[A2], B, h[2], w[2], s));
+  pool(A[A2], A[P3], 2);
+  RCHK_WN(conv_launch<32, 32, 0>(n, A[P3], n->wk[3], bias_of(n, 3), 32, A[A3], B, h[3], w[3], s));
+  upadd(A[A3], A[A2], A[U2], 2);
+  RCHK_WN(conv_launch<32, 32, 0>(n, A[U2], n->wk[4], bias_of(n, 4), 32, A[B2], B, h[2], w[2], s));
+  upadd(A[B2], A[A1], A[U1], 1);
+  RCHK_WN(conv_launch<32, 32, 0>(n, A[U1], n->wk[5], bias_of(n, 5), 32, A[B1], B, h[1], w[1], s));
+  upadd(A[B1], A[A0], A[U0], 0);
+  RCHK_WN(conv_launch<32, 32, 0>(n, A[U0], n->wk[6], bias_of(n, 6), 32, A[B0], B, h[0], w[0], s));
+  RCHK_WN(conv_launch<32, 16, 1>(n, A[B0], n->wk[7], bias_of(n, 7), 1, n->y, B, h[0], w[0], s));
+  n->B = B;
+  return THORIN_OK;
+}
+
+// loss of n->y against n->tgt and the gradient into n->g (after wn_forward)
+static int wn_backward(thorin_warmnet *n, int B, cudaStream_t s)
+{
+  const int H = n->nr, W = n->ns;
+  int h[4] = {H, H / 2, H / 4, H / 8}, w[4] = {W, W / 2, W / 4, W / 8};
+  bf16 **A = n->act;
+  const long long P0 = (long long)B * H * W;
+  const float inv_n = (float)(1.0 / ((double)B * (H - 2) * W));
+  const unsigned lb = nblk(P0);
+  double *lpart = n->dscal + 8;
+  k_wn_loss<<<lb, 256, 0, s>>>(n->y, n->tgt, B, H, W, inv_n, A[GY16], lpart);
+  g_thorin_launches++;
+  k_wn_sum<<<1, 32, 0, s>>>(lpart, (int)lb, (double)inv_n, n->dscal);
+  g_thorin_launches++;
+  auto cnt = [&](int lv) { return (long long)B * h[lv] * w[lv] * WN_C; };
+  // out layer
+  RCHK_WN(wgrad_launch<32, 16>(n, 7, A[B0], A[GY16], B, h[0], w[0], s));
+  RCHK_WN(conv_launch<16, 32, 2>(n, A[GY16], n->wt[7], nullptr, 0, n->gf[0], B, h[0], w[0], s));
+  k_wn_relu_mask<<<nblk(cnt(0)), 256, 0, s>>>(n->gf[0], A[B0], n->gb[0], cnt(0));
+  g_thorin_launches++;
+  // d0 (input u0 = up(b1) + a0)
+  RCHK_WN(wgrad_launch<32, 32>(n, 6, A[U0], n->gb[0], B, h[0], w[0], s));
+  RCHK_WN(conv_launch<32, 32, 2>(n, n->gb[0], n->wt[6], nullptr, 0, n->ga[0], B, h[0], w[0], s));
+  k_wn_downsum_mask<<<nblk(cnt(1)), 256, 0, s>>>(n->ga[0], A[B1], n->gb[1], B, h[0], w[0]);
+  g_thorin_launches++;
+  // d1
+  RCHK_WN(wgrad_launch<32, 32>(n, 5, A[U1], n->gb[1], B, h[1], w[1], s));
+  RCHK_WN(conv_launch<32, 32, 2>(n, n->gb[1], n->wt[5], nullptr, 0, n->ga[1], B, h[1], w[1], s));
+  k_wn_downsum_mask<<<nblk(cnt(2)), 256, 0, s>>>(n->ga[1], A[B2], n->gb[2], B, h[1], w[1]);
+  g_thorin_launches++;
+  // d2
+  RCHK_WN(wgrad_launch<32, 32>(n, 4, A[U2], n->gb[2], B, h[2], w[2], s));
+  RCHK_WN(conv_launch<32, 32, 2>(n, n->gb[2], n->wt[4], nullptr, 0, n->ga[2], B, h[2], w[2], s));
+  k_wn_downsum_mask<<<nblk(cnt(3)), 256, 0, s>>>(n->ga[2], A[A3], n->gb[3], B, h[2], w[2]);
+  g_thorin_launches++;
+  // e3 (input p3 = pool(a2))
+  RCHK_WN(wgrad_launch<32, 32>(n, 3, A[P3], n->gb[3], B, h[3], w[3], s));
+  RCHK_WN(conv_launch<32, 32, 2>(n, n->gb[3], n->wt[3], nullptr, 0, n->gf[3], B, h[3], w[3], s));
+  k_wn_unpool_mask<<<nblk(cnt(2)), 256, 0, s>>>(n->ga[2], n->gf[3], A[A2], n->gb[2], B, h[2], w[2]);
+  g_thorin_launches++;
+  // e2
+  RCHK_WN(wgrad_launch<32, 32>(n, 2, A[P2], n->gb[2], B, h[2], w[2], s));
+  RCHK_WN(conv_launch<32, 32, 2>(n, n->gb[2], n->wt[2], nullptr, 0, n->gf[2], B, h[2], w[2], s));
+  k_wn_unpool_mask<<<nblk(cnt(1)), 256, 0, s>>>(n->ga[1], n->gf[2], A[A1], n->gb[1], B, h[1], w[1]);
+  g_thorin_launches++;
+  // e1
+  RCHK_WN(wgrad_launch<32, 32>(n, 1, A[P1], n->gb[1], B, h[1], w[1], s));
+  RCHK_WN(conv_launch<32, 32, 2>(n, n->gb[1], n->wt[1], nullptr, 0, n->gf[1], B, h[1], w[1], s));
+  k_wn_unpool_mask<<<nblk(cnt(0)), 256, 0, s>>>(n->ga[0], n->gf[1], A[A0], n->gb[0], B, h[0], w[0]);
+  g_thorin_launches++;
+  // e0
+  RCHK_WN(wgrad_launch<16, 32>(n, 0, n->x, n->gb[0], B, h[0], w[0], s));
+  return THORIN_OK;
+}
+
+static int wn_adam(thorin_warmnet *n, float lr, float b1, float b2, float eps, float max_norm, cudaStream_t s)
+{
+  const int np = THORIN_WN_NPARAMS;
+  double *part = n->dscal + 8;
+  k_wn_sqnorm<<<64, 256, 0, s>>>(n->g, np, part);
+  g_thorin_launches++;
+  k_wn_sum<<<1, 32, 0, s>>>(part, 64, 1.0, n->dscal + 1);
+  g_thorin_launches++;
+  n->adam_t++;
+  const float bc1 = 1.f - powf(b1, (float)n->adam_t), bc2 = 1.f - powf(b2, (float)n->adam_t);
+  k_wn_adam<<<nblk(np), 256, 0, s>>>(n->w, n->g, n->m, n->v, np, lr, b1, b2, eps, bc1, bc2, n->dscal + 1, max_norm);
+  g_thorin_launches++;
+  pack_all(n, s);
+  return THORIN_OK;
+}
+
+static int wn_check_err(thorin_warmnet *n)
+{
+  int e = 0;
+  WNCHK(cudaMemcpy(&e, n->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    g_last_error = "warmnet: a tensor-core wait timed out";
+    return THORIN_ERR_TIMEOUT;
+  }
+  return THORIN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Disk coupling, called from the SOR driver on the disk's stream.
+
+// T (start of the solve, or the current iterate) -> T + jac + network
+int wn_sor_predict(thorin_warmnet *n, int nr, int ns, double *T, const double *ml, const double *mlip,
+                   const double *mlim, const double *mljp, const double *mljm, const double *rhs, cudaStream_t s)
+{
+  SorSys m{ml, mlip, mlim, mljp, mljm, rhs};
+  double *part = n->dscal + 8;
+  const int sb = 2 * n->nsm;
+  k_wn_scale<<<sb, 256, 0, s>>>(nr, ns, T, m, part);
+  k_wn_sum<<<1, 32, 0, s>>>(part, sb, 1.0 / ((double)(nr - 2) * ns), n->dscal + 2);
+  k_wn_features<<<nblk((long long)nr * ns), 256, 0, s>>>(nr, ns, T, m, n->dscal + 2, n->x, n->jac);
+  g_thorin_launches += 3;
+  RCHK_WN(wn_forward(n, 1, s));
+  k_wn_apply<<<nblk((long long)(nr - 2) * ns), 256, 0, s>>>(nr, ns, T, n->jac, n->y, n->dscal + 2);
+  g_thorin_launches++;
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? THORIN_OK : wn_fail("predict kernels", e);
+}
+
+// one training step on the solve that went from tk to tconv
+int wn_sor_train(thorin_warmnet *n, int nr, int ns, const double *tk, const double *tconv, const double *ml,
+                 const double *mlip, const double *mlim, const double *mljp, const double *mljm, const double *rhs,
+                 float lr, cudaStream_t s)
+{
+  SorSys m{ml, mlip, mlim, mljp, mljm, rhs};
+  double *part = n->dscal + 8;
+  const int sb = 2 * n->nsm;
+  k_wn_scale<<<sb, 256, 0, s>>>(nr, ns, tk, m, part);
+  k_wn_sum<<<1, 32, 0, s>>>(part, sb, 1.0 / ((double)(nr - 2) * ns), n->dscal + 2);
+  k_wn_features<<<nblk((long long)nr * ns), 256, 0, s>>>(nr, ns, tk, m, n->dscal + 2, n->x, n->jac);
+  k_wn_target<<<nblk((long long)nr * ns), 256, 0, s>>>(nr, ns, tconv, tk, n->jac, n->dscal + 2, n->tgt);
+  g_thorin_launches += 4;
+  RCHK_WN(wn_forward(n, 1, s));
+  RCHK_WN(wn_backward(n, 1, s));
+  RCHK_WN(wn_adam(n, lr, 0.9f, 0.999f, 1e-8f, 1.0f, s));
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? THORIN_OK : wn_fail("training kernels", e);
+}
+
+int wn_last_loss(thorin_warmnet *n, double *loss)
+{
+  WNCHK(cudaMemcpy(loss, n->dscal, sizeof(double), cudaMemcpyDeviceToHost));
+  return wn_check_err(n);
+}
+
+int wn_dims(const thorin_warmnet *n, int *nr, int *ns)
+{
+  *nr = n->nr;
+  *ns = n->ns;
+  return THORIN_OK;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" int thorin_warmnet_create(int nrad, int nsec, int max_batch, thorin_warmnet **out)
+{
+  if (!out || nrad < 16 || nsec < 16 || nrad % 8 || nsec % 8 || max_batch < 1) {
+    g_last_error = "warmnet_create: nrad, nsec multiples of 8 and >= 16, max_batch >= 1";
+    return THORIN_ERR_ARG;
+  }
+  *out = nullptr;
+  thorin_warmnet *n = new thorin_warmnet();
+  n->nr = nrad;
+  n->ns = nsec;
+  n->maxb = max_batch;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n->nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (n->nsm < 1) n->nsm = 1;
+  n->part_blocks = 2 * n->nsm;
+  const long long P0 = (long long)max_batch * nrad * nsec;
+  long long lv[4];
+  for (int k = 0; k < 4; k++) lv[k] = P0 >> (2 * k);
+  auto fail = [&](cudaError_t e) {
+    thorin_warmnet_destroy(n);
+    return wn_fail("allocation", e);
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&n->own, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return fail(e);
+  const int np = THORIN_WN_NPARAMS;
+  float **fp[] = {&n->w, &n->g, &n->m, &n->v};
+  for (float **p : fp) {
+    if ((e = cudaMalloc((void **)p, np * sizeof(float))) != cudaSuccess) return fail(e);
+    cudaMemset(*p, 0, np * sizeof(float));
+  }
+  for (int l = 0; l < WN_NL; l++) {
+    const LayerDef L = layer_def(l);
+    const size_t nk = (size_t)L.coutp * 9 * L.cinp;
+    if ((e = cudaMalloc((void **)&n->wk[l], nk * sizeof(bf16))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void **)&n->wt[l], nk * sizeof(bf16))) != cudaSuccess) return fail(e);
+  }
+  if ((e = cudaMalloc((void **)&n->x, P0 * THORIN_WN_INPUTS * sizeof(bf16))) != cudaSuccess) return fail(e);
+  const int lvl[14] = {0, 1, 1, 2, 2, 3, 3, 2, 2, 1, 1, 0, 0, 0};
+  for (int k = 0; k < 14; k++) {
+    const size_t cnt = (size_t)lv[lvl[k]] * (k == GY16 ? 16 : WN_C);
+    if ((e = cudaMalloc((void **)&n->act[k], cnt * sizeof(bf16))) != cudaSuccess) return fail(e);
+  }
+  if ((e = cudaMalloc((void **)&n->y, P0 * sizeof(float))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc((void **)&n->tgt, P0 * sizeof(float))) != cudaSuccess) return fail(e);
+  for (int k = 0; k < 4; k++) {
+    if ((e = cudaMalloc((void **)&n->gf[k], lv[k] * WN_C * sizeof(float))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void **)&n->ga[k], lv[k] * WN_C * sizeof(float))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void **)&n->gb[k], lv[k] * WN_C * sizeof(bf16))) != cudaSuccess) return fail(e);
+  }
+  const size_t part = (size_t)n->part_blocks * (9 * WN_C * WN_C + WN_C);
+  if ((e = cudaMalloc((void **)&n->part, part * sizeof(float))) != cudaSuccess) return fail(e);
+  const size_t nd = 8 + (size_t)(nblk(P0) > 4096 ? nblk(P0) : 4096);
+  if ((e = cudaMalloc((void **)&n->dscal, nd * sizeof(double))) != cudaSuccess) return fail(e);
+  cudaMemset(n->dscal, 0, nd * sizeof(double));
+  if ((e = cudaMalloc((void **)&n->jac, (size_t)nrad * nsec * sizeof(double))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc((void **)&n->err, sizeof(int))) != cudaSuccess) return fail(e);
+  cudaMemset(n->err, 0, sizeof(int));
+  pack_all(n, n->own);
+  if ((e = cudaStreamSynchronize(n->own)) != cudaSuccess) return fail(e);
+  *out = n;
+  return THORIN_OK;
+}
+
+extern "C" int thorin_warmnet_destroy(thorin_warmnet *n)
+{
+  if (!n) return THORIN_OK;
+  if (n->own) cudaStreamSynchronize(n->own);
+  void *ptrs[] = {n->w, n->g, n->m, n->v, n->x, n->y, n->tgt, n->part, n->dscal, n->jac, n->err};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  for (int l = 0; l < WN_NL; l++) {
+    if (n->wk[l]) cudaFree(n->wk[l]);
+    if (n->wt[l]) cudaFree(n->wt[l]);
+  }
+  for (bf16 *p : n->act)
+    if (p) cudaFree(p);
+  for (int k = 0; k < 4; k++) {
+    if (n->gf[k]) cudaFree(n->gf[k]);
+    if (n->ga[k]) cudaFree(n->ga[k]);
+    if (n->gb[k]) cudaFree(n->gb[k]);
+  }
+  if (n->own) cudaStreamDestroy(n->own);
+  delete n;
+  return THORIN_OK;
+}
+
+extern "C" int thorin_warmnet_set_params(thorin_warmnet *n, const float *host, int count)
+{
+  if (!n || !host || count != THORIN_WN_NPARAMS) {
+    g_last_error = "warmnet_set_params: count must be THORIN_WN_NPARAMS";
+    return THORIN_ERR_ARG;
+  }
+  WNCHK(cudaMemcpyAsync(n->w, host, count * sizeof(float), cudaMemcpyHostToDevice, n->own));
+  WNCHK(cudaMemsetAsync(n->m, 0, count * sizeof(float), n->own));
+  WNCHK(cudaMemsetAsync(n->v, 0, count * sizeof(float), n->own));
+  n->adam_t = 0;
+  pack_all(n, n->own);
+  WNCHK(cudaStreamSynchronize(n->own));
+  return THORIN_OK;
+}
+
+extern "C" int thorin_warmnet_get_params(thorin_warmnet *n, float *host, int count)
+{
+  if (!n || !host || count != THORIN_WN_NPARAMS) {
+    g_last_error = "warmnet_get_params: count must be THORIN_WN_NPARAMS";
+    return THORIN_ERR_ARG;
+  }
+  WNCHK(cudaDeviceSynchronize());
+  WNCHK(cudaMemcpy(host, n->w, count * sizeof(float), cudaMemcpyDeviceToHost));
+  return THORIN_OK;
+}
+
+extern "C" int thorin_warmnet_forward(thorin_warmnet *n, int batch, const uint16_t *x, float *y)
+{
+  if (!n || !x || !y || batch < 1 || batch > n->maxb) {
+    g_last_error = "warmnet_forward: 1 <= batch <= max_batch and buffers required";
+    return THORIN_ERR_ARG;
+  }
+  const size_t P = (size_t)batch * n->nr * n->ns;
+  WNCHK(cudaMemcpyAsync(n->x, x, P * THORIN_WN_INPUTS * sizeof(bf16), cudaMemcpyHostToDevice, n->own));
+  RCHK_WN(wn_forward(n, batch, n->own));
+  WNCHK(cudaMemcpyAsync(y, n->y, P * sizeof(float), cudaMemcpyDeviceToHost, n->own));
+  WNCHK(cudaStreamSynchronize(n->own));
+  return wn_check_err(n);
+}
+
+extern "C" int thorin_warmnet_gradient(thorin_warmnet *n, int batch, const uint16_t *x, const float *target,
+                                       float *loss, float *grad)
+{
+  if (!n || !x || !target || batch < 1 || batch > n->maxb) {
+    g_last_error = "warmnet_gradient: 1 <= batch <= max_batch and buffers required";
+    return THORIN_ERR_ARG;
+  }
+  const size_t P = (size_t)batch * n->nr * n->ns;
+  WNCHK(cudaMemcpyAsync(n->x, x, P * THORIN_WN_INPUTS * sizeof(bf16), cudaMemcpyHostToDevice, n->own));
+  WNCHK(cudaMemcpyAsync(n->tgt, target, P * sizeof(float), cudaMemcpyHostToDevice, n->own));
+  RCHK_WN(wn_forward(n, batch, n->own));
+  RCHK_WN(wn_backward(n, batch, n->own));
+  double l = 0.0;
+  WNCHK(cudaMemcpyAsync(&l, n->dscal, sizeof(double), cudaMemcpyDeviceToHost, n->own));
+  if (grad) WNCHK(cudaMemcpyAsync(grad, n->g, THORIN_WN_NPARAMS * sizeof(float), cudaMemcpyDeviceToHost, n->own));
+  WNCHK(cudaStreamSynchronize(n->own));
+  if (loss) *loss = (float)l;
+  return wn_check_err(n);
+}
+
+extern "C" int thorin_warmnet_adam(thorin_warmnet *n, float lr, float beta1, float beta2, float eps, float max_norm)
+{
+  if (!n || !(lr > 0.f) || !(beta1 >= 0.f && beta1 < 1.f) || !(beta2 >= 0.f && beta2 < 1.f) || !(eps > 0.f)) {
+    g_last_error = "warmnet_adam: lr > 0, 0 <= beta < 1, eps > 0";
+    return THORIN_ERR_ARG;
+  }
+  RCHK_WN(wn_adam(n, lr, beta1, beta2, eps, max_norm, n->own));
+  WNCHK(cudaStreamSynchronize(n->own));
+  return THORIN_OK;
+}

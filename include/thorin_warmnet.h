@@ -1,0 +1,94 @@
+/* thorin_warmnet.h -- learned warm start of the radiative-diffusion SOR solve.
+ *
+ * The reference solves the implicit energy equation of
+ * ImplicitRadiativeDiffusion (src_main/EnergySources.c:201-335) with
+ * SuccessiveOverrelaxation (EnergySources.c:406-511), starting every solve
+ * from the previous temperature.  This interface adds, beside that plain
+ * method, a small polar-periodic convolutional encoder-decoder that predicts
+ * the temperature update of a solve from the local fields; SOR then iterates
+ * from the prediction to the same residual threshold as the plain solve
+ * (eps times the L1 residual of the previous-temperature start), so the
+ * converged temperature is the method's own.  It has no counterpart in the
+ * reference.
+ *
+ * Network (fixed): 4 levels, 3x3 convolutions periodic in azimuth and
+ * zero-padded in radius, 32 channels, ReLU, 2x2 average pooling down and
+ * nearest-neighbour upsampling with additive skips up, one output channel;
+ * 57,537 FP32 master parameters, BF16 weights and activations, FP32
+ * accumulation on the tensor cores.  Inputs per cell (6 of 16 channels):
+ * the Jacobi-scaled SOR residual of the start temperature (divided by its
+ * grid mean and clipped to +-16), the four neighbour weights -M/Ml of the
+ * SOR matrix and the local stiffness -log(1 - sum of the weights) / 4.
+ * These carry Sigma, T_old, the heating, the opacity and the dt-scaled
+ * diffusion coefficients through the matrix and right-hand side that they
+ * build.  Output: the update beyond one Jacobi step, in units of 32 times
+ * the residual scale.
+ */
+#ifndef THORIN_WARMNET_H
+#define THORIN_WARMNET_H
+
+#include <stdint.h>
+#include "thorin_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define THORIN_WN_INPUTS   16    /* input channels per cell (6 used, rest zero) */
+#define THORIN_WN_NPARAMS  57537 /* FP32 parameters */
+
+#define THORIN_WS_OFF      0     /* plain SOR (the reference's method)          */
+#define THORIN_WS_PREDICT  1     /* warm-start every SOR solve from the network */
+#define THORIN_WS_TRAIN    2     /* plain SOR; each solve then trains the net   */
+
+typedef struct thorin_warmnet thorin_warmnet;
+
+/* A network with activations for batch images of nrad x nsec cells
+ * (nrad and nsec multiples of 8) on the current CUDA device.  Parameters
+ * start at zero: set them with thorin_warmnet_set_params. */
+int thorin_warmnet_create(int nrad, int nsec, int max_batch, thorin_warmnet **out);
+int thorin_warmnet_destroy(thorin_warmnet *n);
+
+/* FP32 parameters, per layer (e0, e1, e2, e3, d2, d1, d0, out) the weights
+ * W[cout][3x3 tap (dr, dphi) row-major][cin] followed by the bias[cout]. */
+int thorin_warmnet_set_params(thorin_warmnet *n, const float *host, int count);
+int thorin_warmnet_get_params(thorin_warmnet *n, float *host, int count);
+
+/* Raw network I/O (host buffers).  x: bf16 bit patterns
+ * [batch][nrad][nsec][THORIN_WN_INPUTS]; y, target: [batch][nrad][nsec].
+ * thorin_warmnet_gradient evaluates the loss
+ *   mean over rings 1..nrad-2 of (y - target)^2
+ * and its gradient with respect to the parameters (grad may be NULL; the
+ * gradient also stays on the device for thorin_warmnet_adam). */
+int thorin_warmnet_forward(thorin_warmnet *n, int batch, const uint16_t *x, float *y);
+int thorin_warmnet_gradient(thorin_warmnet *n, int batch, const uint16_t *x, const float *target, float *loss,
+                            float *grad);
+
+/* One Adam step with the last gradient, clipped to global norm max_norm. */
+int thorin_warmnet_adam(thorin_warmnet *n, float lr, float beta1, float beta2, float eps, float max_norm);
+
+/* Attach a network to a disk (same nrad x nsec, batch >= 1) or detach it
+ * (mode THORIN_WS_OFF, n may be NULL).  PREDICT: every SOR solve of the
+ * disk starts from T_old + Jacobi step + network prediction and, when
+ * restart_every > 0, re-applies the network to the current residual every
+ * restart_every sweeps while the solve has not converged.  TRAIN: the solve
+ * is plain; afterwards one Adam step (learning rate lr, moments 0.9/0.999,
+ * norm clip 1) fits the network to that solve's converged update. */
+int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode, int restart_every, float lr);
+
+/* Layout check of the tensor-core path: D[128][32] = A[128][64] * B[32][64]^T
+ * with bf16 bit patterns a, b (row-major) and FP32 d, on one CTA. */
+int thorin_selftest_umma(const uint16_t *a, const uint16_t *b, float *d);
+
+/* Counters of the attached network's use on this disk. */
+typedef struct thorin_ws_stats {
+  long long predictions;   /* network applications inside SOR solves   */
+  long long train_steps;   /* training steps taken                     */
+  double last_loss;        /* loss of the last training step           */
+} thorin_ws_stats;
+int thorin_gpu_warmstart_stats(thorin_disk *d, thorin_ws_stats *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -61,6 +61,10 @@ def lib(omp: bool = False):
         L.ora_algogas.restype = C.c_int
         L.ora_algogas.argtypes = [C.c_void_p, C.POINTER(ThorinPlanets)]
         L.ora_integrals.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 5
+        L.ora_sor_array.restype = C.POINTER(C.c_double)
+        L.ora_sor_array.argtypes = [C.c_void_p, C.c_int]
+        L.ora_sor_omega.restype = C.c_double
+        L.ora_sor_omega.argtypes = [C.c_void_p]
         L.ora_set_sor_state.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int]
         _D = C.POINTER(C.c_double)
         L.ora_set_opacity_table.argtypes = [C.c_int, C.c_int, _D, _D, _D, _D]
@@ -122,6 +126,16 @@ class OracleDisk:
 
     def set_sor_state(self, omega: float, domega: float, niterlast: int):
         self.L.ora_set_sor_state(self.h, omega, domega, niterlast)
+
+    def sor_system(self) -> dict:
+        """The last SOR solve: its five coefficient arrays, RHS, start
+        temperature and omega (copies)."""
+        n = self.nr * self.ns
+        names = ("ml", "mlip", "mlim", "mljp", "mljm", "rhs", "tstart")
+        out = {k: np.ctypeslib.as_array(self.L.ora_sor_array(self.h, i), shape=(n,)).copy()
+               for i, k in enumerate(names)}
+        out["omega"] = self.L.ora_sor_omega(self.h)
+        return out
 
     def set_opacity_table(self, rows, cols, pgrid, tgrid, planck, rosseland):
         """OpacityTable SM03 gas table (shared by all oracle disks)."""

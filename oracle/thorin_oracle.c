@@ -83,6 +83,7 @@ typedef struct ora_disk {
   /* energy sources */
   double *GradTr, *GradTt, *GradTm, *Dcen, *Dr, *Dt, *voldens, *flaring, *qirr;
   double *A, *B, *Ml, *Mlip, *Mlim, *Mljp, *Mljm, *RHS;
+  double *TsorStart;             /* T handed to the last SOR solve (its start) */
   /* pebbles */
   double *pdens, *pvrad, *pvtheta, *psize, *tau, *paccr, *pacct, *gaccr, *gacct;
   double *etafc, *etacc, *macc, *dragr, *dragt;
@@ -642,7 +643,7 @@ ora_disk *ora_create(const thorin_params *p)
                    &d->Drr, &d->Drp, &d->Dpp, &d->Trr, &d->Trp, &d->Tpp, &d->RadMomP, &d->RadMomM, &d->ThetaMomP,
                    &d->ThetaMomM, &d->Work, &d->QRStar, &d->VthetaRes, &d->TempShift, &d->dq, &d->abscissa,
                    &d->ordinate, &d->GradTr, &d->GradTt, &d->GradTm, &d->Dcen, &d->Dr, &d->Dt, &d->voldens,
-                   &d->flaring, &d->qirr, &d->A, &d->B, &d->Ml, &d->Mlip, &d->Mlim, &d->Mljp, &d->Mljm, &d->RHS,
+                   &d->flaring, &d->qirr, &d->A, &d->B, &d->Ml, &d->Mlip, &d->Mlim, &d->Mljp, &d->Mljm, &d->RHS, &d->TsorStart,
                    &d->pdens, &d->pvrad, &d->pvtheta, &d->psize, &d->tau, &d->paccr, &d->pacct, &d->gaccr,
                    &d->gacct, &d->etafc, &d->etacc, &d->macc, &d->dragr, &d->dragt};
   for (size_t k = 0; k < sizeof(v2) / sizeof(v2[0]); k++) *v2[k] = grid(d);
@@ -760,6 +761,15 @@ double *ora_profile(ora_disk *d, int id)
 
 double *ora_radii(ora_disk *d) { return d->Radii; }
 int *ora_nshift(ora_disk *d) { return d->NshiftGas; }
+
+/* The last SOR system: 0..5 = Ml, Mlip, Mlim, Mljp, Mljm, RHS; 6 = the
+ * temperature the solve started from.  Rows 1..nr-2 are the unknowns. */
+double *ora_sor_array(ora_disk *d, int k)
+{
+  double *a[] = {d->Ml, d->Mlip, d->Mlim, d->Mljp, d->Mljm, d->RHS, d->TsorStart};
+  return (k >= 0 && k < 7) ? a[k] : NULL;
+}
+double ora_sor_omega(ora_disk *d) { return d->omega; }
 void ora_set_time(ora_disk *d, double t) { d->PhysicalTime = t; d->PhysicalTimeInitial = t; }
 void ora_get_stats(ora_disk *d, thorin_stats *s)
 {
@@ -1485,6 +1495,7 @@ static int ImplicitRadiativeDiffusion(ora_disk *d, double dt)   /* EnergySources
   d->omega += d->domega;
   if (d->omega > OMEGAUPPER) { d->omega = OMEGAUPPER; d->domega = -d->domega; }
   if (d->omega < 1.0) { d->omega = 1.0; d->domega = -d->domega; }
+  memcpy(d->TsorStart, d->temper, sizeof(double) * (size_t)nr * (size_t)ns);
   Niter = SuccessiveOverrelaxation(d, d->omega, &maxed);
   if (maxed) status = THORIN_ERR_SOR_MAXIT;       /* reference only warns */
   d->st.sor_calls++; d->st.sor_sweeps += Niter; d->st.sor_last_niter = Niter; d->st.sor_omega = d->omega;

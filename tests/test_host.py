@@ -1,5 +1,5 @@
 """Host-side logic and the C-ABI boundary, without a GPU: the library loads
-and exports every function include/thorin_gpu.h declares, parameter handling
+and exports every function include/*.h declares, parameter handling
 matches the reference's variable table, unsupported options are rejected
 before any device work, and the multi-replica bench aggregation (max time,
 summed updates) works across two gloo ranks."""
@@ -12,7 +12,8 @@ import sys
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-HEADER = os.path.join(ROOT, "include", "thorin_gpu.h")
+HEADERS = [os.path.join(ROOT, "include", h) for h in sorted(os.listdir(os.path.join(ROOT, "include")))
+           if h.endswith(".h")]
 sys.path.insert(0, ROOT)
 
 from fargo_thorin_gb300 import params as P  # noqa: E402
@@ -20,7 +21,7 @@ from fargo_thorin_gb300 import workloads  # noqa: E402
 
 
 def _declared_functions():
-    text = open(HEADER).read()
+    text = "".join(open(h).read() for h in HEADERS)
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\**\s*(thorin_\w+)\s*\(", text, flags=re.M)))
 

@@ -1,0 +1,146 @@
+"""The learned SOR warm start (include/thorin_warmnet.h).
+
+CPU: the numpy restatement of the network (oracle/warmnet_oracle.py) has a
+backward pass that matches finite differences of its float64 forward pass,
+and its bfloat16 rounding is round-to-nearest-even.
+GPU: the tcgen05 layout self-test GEMM is exact; the CUDA forward pass, loss
+and parameter gradient match the oracle's bf16 emulation; gradients repeat
+bit for bit; Adam steps on a fixed batch lower the loss.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import warmnet_oracle as WO  # noqa: E402
+from fargo_thorin_gb300 import warmstart as WS  # noqa: E402
+
+
+def _params(seed, out_std=0.05):
+    p = WS.init_params(seed).astype(np.float64)
+    o = WO.OFFSETS[7]
+    rng = np.random.default_rng(seed + 1)
+    p[o:] = rng.standard_normal(p.size - o) * out_std
+    for k, (cin, cout) in enumerate(WO.LAYERS):      # small nonzero biases
+        b0 = WO.OFFSETS[k] + cout * 9 * cin
+        p[b0:b0 + cout] = rng.uniform(-0.05, 0.05, cout)
+    return p
+
+
+def _inputs(seed, B, H, W):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((B, H, W, WO.INPUTS), np.float32)
+    x[..., :WO.NIN] = rng.uniform(-1.0, 1.0, (B, H, W, WO.NIN))
+    t = rng.standard_normal((B, H, W)).astype(np.float32) * 0.1
+    return WO.bf16(x), t
+
+
+def test_param_count_and_init():
+    assert WO.NPARAMS == WS.NPARAMS == 57537
+    p = WS.init_params(3)
+    assert p.dtype == np.float32 and p.size == WS.NPARAMS
+    assert np.all(p[WO.OFFSETS[7]:] == 0.0)            # output layer starts at zero
+
+
+def test_bf16_rounding_ties_to_even():
+    vals = np.array([1.0, 1.0 + 2.0 ** -8, 1.0 + 3 * 2.0 ** -8, 1.0 + 2.0 ** -9, -2.5, 3.0e-39], np.float32)
+    got = WO.bf16(vals)
+    assert got[0] == 1.0
+    assert got[1] == 1.0                                # tie -> even mantissa
+    assert got[2] == np.float32(1.0 + 4 * 2.0 ** -8)    # tie -> even (rounds up)
+    assert got[3] == 1.0
+    assert got[4] == -2.5
+    assert np.all(WO.from_bits(WO.bf16_bits(vals)) == got)
+
+
+def test_oracle_backward_matches_finite_differences():
+    B, H, W = 1, 16, 16
+    p = _params(5, out_std=0.2)
+    x, t = _inputs(6, B, H, W)
+    loss, g, _ = WO.loss_and_grad(p, x.astype(np.float64), t.astype(np.float64), bf=False)
+    rng = np.random.default_rng(7)
+    idx = np.concatenate([rng.integers(WO.OFFSETS[k], WO.OFFSETS[k + 1] if k < 7 else WO.NPARAMS, 3)
+                          for k in range(8)])
+    h = 1e-6
+    for i in idx:
+        pp, pm = p.copy(), p.copy()
+        pp[i] += h
+        pm[i] -= h
+        lp = WO.loss_and_grad(pp, x.astype(np.float64), t.astype(np.float64), bf=False)[0]
+        lm = WO.loss_and_grad(pm, x.astype(np.float64), t.astype(np.float64), bf=False)[0]
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-5 * max(abs(fd), 1e-6), (i, fd, g[i])
+
+
+# --------------------------------------------------------------------- GPU
+@pytest.fixture(scope="module")
+def lib():
+    from fargo_thorin_gb300 import _lib
+    return _lib.load()
+
+
+@pytest.mark.gpu
+def test_umma_selftest_exact(lib):
+    import ctypes as C
+    rng = np.random.default_rng(0)
+    a = WO.bf16(rng.uniform(-1, 1, (128, 64)).astype(np.float32))
+    b = WO.bf16(rng.uniform(-1, 1, (32, 64)).astype(np.float32))
+    ab, bb = WO.bf16_bits(a), WO.bf16_bits(b)
+    d = np.zeros((128, 32), np.float32)
+    from fargo_thorin_gb300 import _lib
+    _lib.check(lib.thorin_selftest_umma(ab.ctypes.data_as(C.POINTER(C.c_uint16)),
+                                        bb.ctypes.data_as(C.POINTER(C.c_uint16)),
+                                        d.ctypes.data_as(C.POINTER(C.c_float))), "selftest_umma")
+    ref = a.astype(np.float64) @ b.astype(np.float64).T
+    np.save(os.path.join(ROOT, "gpurun_out", "umma_selftest.npy"), d) if os.path.isdir(
+        os.path.join(ROOT, "gpurun_out")) else None
+    assert np.max(np.abs(d - ref)) <= 1e-5 * np.max(np.abs(ref)), np.max(np.abs(d - ref))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("B,H,W", [(1, 16, 32), (2, 24, 40)])
+def test_forward_matches_oracle(B, H, W):
+    p = _params(11)
+    x, _ = _inputs(12, B, H, W)
+    net = WS.WarmNet(H, W, max_batch=B, params=p.astype(np.float32))
+    y = net.forward(WO.bf16_bits(x))
+    yo, _ = WO.forward(p.astype(np.float32), x, bf=True)
+    err = np.linalg.norm(y - yo) / np.linalg.norm(yo)
+    assert err < 1e-2, err
+
+
+@pytest.mark.gpu
+def test_gradient_matches_oracle_and_repeats():
+    B, H, W = 2, 16, 32
+    p = _params(21)
+    x, t = _inputs(22, B, H, W)
+    net = WS.WarmNet(H, W, max_batch=B, params=p.astype(np.float32))
+    loss, g = net.gradient(WO.bf16_bits(x), t)
+    lo, go, _ = WO.loss_and_grad(p.astype(np.float32), x, t, bf=True)
+    assert abs(loss - lo) <= 1e-3 * lo, (loss, lo)
+    for k in range(8):
+        a, b = WO.OFFSETS[k], (WO.OFFSETS[k + 1] if k < 7 else WO.NPARAMS)
+        err = np.linalg.norm(g[a:b] - go[a:b]) / np.linalg.norm(go[a:b])
+        assert err < 3e-2, (k, err)
+    loss2, g2 = net.gradient(WO.bf16_bits(x), t)
+    assert loss2 == loss and np.array_equal(g2, g)
+
+
+@pytest.mark.gpu
+def test_adam_lowers_loss_on_fixed_batch():
+    B, H, W = 2, 16, 32
+    p = _params(31)
+    x, t = _inputs(32, B, H, W)
+    net = WS.WarmNet(H, W, max_batch=B, params=p.astype(np.float32))
+    xb = WO.bf16_bits(x)
+    l0, _ = net.gradient(xb, t)
+    for _ in range(40):
+        net.gradient(xb, t)
+        net.adam(3e-3)
+    l1, _ = net.gradient(xb, t)
+    assert l1 < 0.5 * l0, (l0, l1)
