@@ -141,6 +141,49 @@ def reduce_over_ranks(values, ops, device):
     return out
 
 
+WARMNET = os.path.join(ROOT, "fargo_thorin_gb300", "warmnet_disk1_1024x3072.npy")
+
+
+def warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, steps, stream, barrier, t_plain, plain_per_solve):
+    """Replay the timed DTs with the trained network attached in PREDICT
+    mode: SOR sweeps per solve against the plain run, the throughput, and the
+    temperature difference after the DTs (both meet the same threshold)."""
+    import torch
+    from fargo_thorin_gb300 import warmstart as WS
+    if not os.path.exists(WARMNET):
+        return {"unavailable": "no trained network file"}
+    net = WS.WarmNet(NR, NS, params=WS.WarmNet.load_params(WARMNET))
+    for f, v in snap.items():
+        d.upload(f, v)
+    d.set_sor_state(*snap_sor[:3])
+    d.set_time(snap_time)
+    sys_ = snap_sys.copy()
+    WS.attach(d, net, WS.PREDICT)
+    st0 = d.stats()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    subs = 0
+    for _ in range(steps):
+        d.algogas(sys_)
+        subs += d.stats().substeps
+    e1.record(stream)
+    barrier()
+    ms = e0.elapsed_time(e1)
+    st1 = d.stats()
+    pred = WS.stats(d).predictions
+    WS.attach(d, None, WS.OFF)
+    t = d.get(8)
+    net.close()
+    per_solve = (st1.sor_sweeps - st0.sor_sweeps) / max(st1.sor_calls - st0.sor_calls, 1)
+    return {"plain_sweeps_per_solve": plain_per_solve, "learned_sweeps_per_solve": per_solve,
+            "sweeps_ratio_plain_over_learned": plain_per_solve / per_solve if per_solve else None,
+            "learned_value": NR * NS * subs / (ms / 1e3), "learned_ms_per_step": ms / steps, "substeps": subs,
+            "network_applications": pred, "network": os.path.relpath(WARMNET, ROOT),
+            "t_rel_l2_vs_plain": float(np.linalg.norm(t - t_plain) / np.linalg.norm(t_plain)),
+            "threshold": "eps * L1 residual of the previous-temperature start, as the plain solve"}
+
+
 def run_gpu(args):
     import torch
     ws, rank, local = dist_env()
@@ -178,7 +221,7 @@ def run_gpu(args):
     clocks.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    subs, sweeps0 = 0, d.stats().sor_sweeps
+    subs, sweeps0, calls0 = 0, d.stats().sor_sweeps, d.stats().sor_calls
     for _ in range(args.steps):
         d.algogas(sys_)
         subs += d.stats().substeps
@@ -188,6 +231,8 @@ def run_gpu(args):
     ms = e0.elapsed_time(e1)
     st = d.stats()
     sweeps = st.sor_sweeps - sweeps0
+    solves = st.sor_calls - calls0
+    t_plain = d.get(8)
     launches = st.kernel_launches - launches0
     sor_avg_ms = st.sor_time_ms / max(st.sor_passes, 1)
     ms_max, subs_all = reduce_over_ranks([ms, subs], ["max", "sum"], "cuda")
@@ -200,7 +245,7 @@ def run_gpu(args):
         d.upload(f, v)
     d.set_sor_state(*snap_sor[:3])
     d.set_time(snap_time)
-    sys_ = snap_sys
+    sys_ = snap_sys.copy()
     sweeps_e0 = d.stats().sor_sweeps
     n = (NR + 1) * NS
     host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True) for f in STATE_FIELDS}
@@ -223,6 +268,10 @@ def run_gpu(args):
     esweeps = d.stats().sor_sweeps - sweeps_e0
     e_max, esubs_all = reduce_over_ranks([e_s, esubs], ["max", "sum"], "cuda")
     e2e_value = NR * NS * esubs_all / e_max
+
+    # the same DTs again with the learned SOR warm start (device-timed)
+    learned = warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, args.steps, stream, barrier, t_plain,
+                               sweeps / max(solves, 1))
 
     if rank == 0:
         peak, peak_kind = peaks()
@@ -269,6 +318,7 @@ def run_gpu(args):
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": bytes_pass, "avg_launch_ms": sor_avg_ms},
             "fp64_roofline": fp64,
+            "sor_warm_start": learned,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

@@ -59,7 +59,7 @@ SIGNATURES = {
     "thorin_warmnet_gradient": (C.c_int, [_P, C.c_int, C.POINTER(C.c_uint16), C.POINTER(C.c_float),
                                           C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "thorin_warmnet_adam": (C.c_int, [_P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float]),
-    "thorin_gpu_warmstart": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_float]),
+    "thorin_gpu_warmstart": (C.c_int, [_P, _P, C.c_int, C.c_float]),
     "thorin_gpu_warmstart_stats": (C.c_int, [_P, _P]),
     "thorin_selftest_umma": (C.c_int, [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.POINTER(C.c_float)]),
     "thorin_planet_from_elements": (C.c_int, [C.POINTER(ThorinPlanets), C.c_int] + [C.c_float] * 9),

@@ -18,7 +18,7 @@ int wn_sor_predict(thorin_warmnet *n, int nr, int ns, double *T, const double *m
                    const double *mlim, const double *mljp, const double *mljm, const double *rhs, cudaStream_t s);
 int wn_sor_train(thorin_warmnet *n, int nr, int ns, const double *tk, const double *tconv, const double *ml,
                  const double *mlip, const double *mlim, const double *mljp, const double *mljm, const double *rhs,
-                 float lr, cudaStream_t s);
+                 float lr, double *scratch, cudaStream_t s);
 int wn_last_loss(thorin_warmnet *n, double *loss);
 int wn_dims(const thorin_warmnet *n, int *nr, int *ns);
 
@@ -150,9 +150,9 @@ struct thorin_disk {
   double omega, domega, omegabest;
   // learned warm start of the SOR solve (off unless attached)
   thorin_warmnet *ws_net = nullptr;
-  int ws_mode = THORIN_WS_OFF, ws_restart = 0;
+  int ws_mode = THORIN_WS_OFF;
   float ws_lr = 0.f;
-  thorin_ws_stats ws_st = {0, 0, 0.0};
+  thorin_ws_stats ws_st = {0, 0, 0.0, 0.0, 0.0};
   double heatsrc[THORIN_MAXPLANETS];
   int heatsrc_index[THORIN_MAXPLANETS], heatsrc_max;
   double gm1, gg1, drin, drout, invdphi, lr01, lr12, taueff_c, tirr4fac, rstar;
@@ -482,11 +482,11 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   return THORIN_OK;
 }
 
-extern "C" int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode, int restart_every, float lr)
+extern "C" int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode, float lr)
 {
-  if (!d || mode < THORIN_WS_OFF || mode > THORIN_WS_TRAIN || restart_every < 0 ||
-      (mode != THORIN_WS_OFF && !n) || (mode == THORIN_WS_TRAIN && !(lr > 0.f))) {
-    g_last_error = "warmstart: mode OFF/PREDICT/TRAIN, a network unless OFF, restart_every >= 0, lr > 0 to train";
+  if (!d || mode < THORIN_WS_OFF || mode > THORIN_WS_TRAIN || (mode != THORIN_WS_OFF && !n) ||
+      (mode == THORIN_WS_TRAIN && !(lr > 0.f))) {
+    g_last_error = "warmstart: mode OFF/PREDICT/TRAIN, a network unless OFF, lr > 0 to train";
     return THORIN_ERR_ARG;
   }
   if (n) {
@@ -499,7 +499,6 @@ extern "C" int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode,
   }
   d->ws_net = mode == THORIN_WS_OFF ? nullptr : n;
   d->ws_mode = mode;
-  d->ws_restart = restart_every;
   d->ws_lr = lr;
   return THORIN_OK;
 }
@@ -508,7 +507,13 @@ extern "C" int thorin_gpu_warmstart_stats(thorin_disk *d, thorin_ws_stats *out)
 {
   if (!d || !out) return THORIN_ERR_ARG;
   CUCHK(cudaStreamSynchronize(d->s));
-  if (d->ws_net && d->ws_st.train_steps > 0) RCHK(wn_last_loss(d->ws_net, &d->ws_st.last_loss));
+  if (d->ws_net && d->ws_st.train_steps > 0) {
+    double l[3];
+    RCHK(wn_last_loss(d->ws_net, l));
+    d->ws_st.last_loss = l[0];
+    d->ws_st.last_res_loss = l[1];
+    d->ws_st.last_sup_loss = l[2];
+  }
   *out = d->ws_st;
   return THORIN_OK;
 }
@@ -1391,15 +1396,11 @@ static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *ca
   // the reference has it; a learned start only moves T before the sweeps
   hydro_sor_resid0(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, omega, d->sor, d->s);
   KCHECK("SOR residual kernel");
-  const bool predict = learned && d->ws_net && d->ws_mode == THORIN_WS_PREDICT;
-  auto apply_net = [&]() -> int {
+  if (learned && d->ws_net && d->ws_mode == THORIN_WS_PREDICT) {
     RCHK(wn_sor_predict(d->ws_net, d->nr, d->ns, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->s));
     d->ws_st.predictions++;
-    return THORIN_OK;
-  };
-  if (predict) RCHK(apply_net());
+  }
   int first = 1, chunk = hint > 0 ? hint : 4;
-  if (predict && d->ws_restart > 0) chunk = d->ws_restart;
   *capped = 0;
   for (;;) {
     if (d->timing) CUCHK(cudaEventRecord(d->ev[0], d->s));
@@ -1424,10 +1425,6 @@ static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *ca
     }
     first += chunk;
     if (first > p.sor_maxiters) { *niter = p.sor_maxiters; *capped = 1; return THORIN_OK; }
-    if (predict && d->ws_restart > 0) {
-      RCHK(apply_net());      // re-apply the network to the current residual
-      continue;
-    }
     chunk = chunk < 64 ? 2 * chunk : 64;
   }
 }
@@ -1518,8 +1515,9 @@ static int energy_step(thorin_disk *d, double dt)
   if (train) CUCHK(cudaMemcpyAsync(d->tbackup, d->temper, tbytes, cudaMemcpyDeviceToDevice, d->s));
   RCHK(sor_solve(d, d->omega, d->Niterlast, &Niter, &capped, true));
   if (train) {
+    // fit the network to this solve; energy_new is free until the energy is formed below
     RCHK(wn_sor_train(d->ws_net, d->nr, d->ns, d->tbackup, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm,
-                      d->rhs, d->ws_lr, d->s));
+                      d->rhs, d->ws_lr, d->energy_new, d->s));
     d->ws_st.train_steps++;
   }
   d->st.sor_calls++;

@@ -505,18 +505,23 @@ struct SorSys {
   const double *ml, *mlip, *mlim, *mljp, *mljm, *rhs;
 };
 
-// partial sums of |r / Ml| over the unknowns (grid-stride, block order)
+// partial sums over the unknowns of |r / Ml| (part[block]) and |r|
+// (part[grid + block]), grid-stride, block order
 __global__ void k_wn_scale(int nr, int ns, const double *__restrict__ T, SorSys m, double *__restrict__ part)
 {
-  double s = 0.0;
+  double s = 0.0, sr = 0.0;
   const long long n = (long long)(nr - 2) * ns;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
     const int i = 1 + (int)(q / ns), j = (int)(q % ns), l = j + i * ns;
     const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
-    s += fabs(sor_resid(T, m.ml, m.mlip, m.mlim, m.mljp, m.mljm, m.rhs, l, l + ns, l - ns, ljp, ljm) / m.ml[l]);
+    const double r = sor_resid(T, m.ml, m.mlip, m.mlim, m.mljp, m.mljm, m.rhs, l, l + ns, l - ns, ljp, ljm);
+    s += fabs(r / m.ml[l]);
+    sr += fabs(r);
   }
   s = block_reduce(s, OpAdd(), 0.0);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
+  sr = block_reduce(sr, OpAdd(), 0.0);
+  if (threadIdx.x == 0) part[gridDim.x + blockIdx.x] = sr;
 }
 
 // network input x[l][16] and the Jacobi step jac = -r / Ml
@@ -573,6 +578,78 @@ __global__ void k_wn_target(int nr, int ns, const double *__restrict__ tconv, co
   const int i = (int)(q / ns);
   const double s = *scale;
   tgt[q] = (i >= 1 && i <= nr - 2 && s > 0.0) ? (float)((tconv[q] - tk[q] - jac[q]) / (s * (double)WN_YSCALE)) : 0.f;
+}
+
+// predicted start temperature: tp = T_k + jac + scale * YSCALE * y on the
+// unknowns, T_k on the boundary rings
+__global__ void k_wn_tpred(int nr, int ns, const double *__restrict__ tk, const double *__restrict__ jac,
+                           const float *__restrict__ y, const double *__restrict__ scale, double *__restrict__ tp)
+{
+  const long long n = (long long)nr * ns;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int i = (int)(q / ns);
+  tp[q] = (i >= 1 && i <= nr - 2) ? tk[q] + jac[q] + (*scale) * (double)WN_YSCALE * (double)y[q] : tk[q];
+}
+
+// rs = (A tp - rhs) / sr on the unknowns (zero elsewhere); partial sums of rs^2
+__global__ void k_wn_res(int nr, int ns, const double *__restrict__ tp, SorSys m, const double *__restrict__ sr,
+                         float *__restrict__ rs, double *__restrict__ part)
+{
+  const long long n = (long long)nr * ns;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (q < n) {
+    const int i = (int)(q / ns), j = (int)(q % ns), l = (int)q;
+    float v = 0.f;
+    if (i >= 1 && i <= nr - 2 && *sr > 0.0) {
+      const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+      const double r = sor_resid(tp, m.ml, m.mlip, m.mlim, m.mljp, m.mljm, m.rhs, l, l + ns, l - ns, ljp, ljm) / *sr;
+      v = (float)r;
+      acc = r * r;
+    }
+    rs[l] = v;
+  }
+  acc = block_reduce(acc, OpAdd(), 0.0);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// output gradient of  wres * mean(rs^2) + wsup * mean((y - tgt)^2)  over the
+// unknowns: wres * 2/N * (scale * YSCALE / sr) * (A^T rs) + wsup * 2/N * (y - tgt),
+// as channel 0 of gy16; partial sums of (y - tgt)^2
+__global__ void k_wn_res_grad(int nr, int ns, const float *__restrict__ rs, SorSys m, const double *__restrict__ scale,
+                              const double *__restrict__ sr, const float *__restrict__ y, const float *__restrict__ tgt,
+                              float wres, float wsup, double inv_n, bf16 *__restrict__ gy16, double *__restrict__ part)
+{
+  const long long n = (long long)nr * ns;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (q < n) {
+    const int i = (int)(q / ns), j = (int)(q % ns), l = (int)q;
+    float g = 0.f;
+    if (i >= 1 && i <= nr - 2 && *sr > 0.0) {
+      const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+      double at = m.ml[l] * rs[l] + m.mljm[ljp] * rs[ljp] + m.mljp[ljm] * rs[ljm];
+      if (i + 1 <= nr - 2) at += m.mlim[l + ns] * rs[l + ns];
+      if (i - 1 >= 1) at += m.mlip[l - ns] * rs[l - ns];
+      const double d = (double)y[l] - (double)tgt[l];
+      acc = d * d;
+      g = (float)(2.0 * inv_n * ((double)wres * (*scale) * (double)WN_YSCALE / (*sr) * at + (double)wsup * d));
+    }
+    uint4 z[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+    ((bf16 *)z)[0] = __float2bfloat16_rn(g);
+    uint4 *dst = (uint4 *)(gy16 + q * 16);
+    dst[0] = z[0];
+    dst[1] = z[1];
+  }
+  acc = block_reduce(acc, OpAdd(), 0.0);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// dscal[0] = wres * dscal[4] + wsup * dscal[5]
+__global__ void k_wn_total(double *dscal, float wres, float wsup)
+{
+  dscal[0] = (double)wres * dscal[4] + (double)wsup * dscal[5];
 }
 
 inline unsigned nblk(long long n, int bs = 256) { return (unsigned)((n + bs - 1) / bs); }
@@ -706,7 +783,7 @@ static int wn_forward(thorin_warmnet *n, int B, cudaStream_t s)
 }
 
 // loss of n->y against n->tgt and the gradient into n->g (after wn_forward)
-static int wn_backward(thorin_warmnet *n, int B, cudaStream_t s)
+static int wn_backward(thorin_warmnet *n, int B, cudaStream_t s, bool mse_loss = true)
 {
   const int H = n->nr, W = n->ns;
   int h[4] = {H, H / 2, H / 4, H / 8}, w[4] = {W, W / 2, W / 4, W / 8};
@@ -715,10 +792,12 @@ static int wn_backward(thorin_warmnet *n, int B, cudaStream_t s)
   const float inv_n = (float)(1.0 / ((double)B * (H - 2) * W));
   const unsigned lb = nblk(P0);
   double *lpart = n->dscal + 8;
-  k_wn_loss<<<lb, 256, 0, s>>>(n->y, n->tgt, B, H, W, inv_n, A[GY16], lpart);
-  g_thorin_launches++;
-  k_wn_sum<<<1, 32, 0, s>>>(lpart, (int)lb, (double)inv_n, n->dscal);
-  g_thorin_launches++;
+  if (mse_loss) {       // otherwise the caller filled gy16 and the loss
+    k_wn_loss<<<lb, 256, 0, s>>>(n->y, n->tgt, B, H, W, inv_n, A[GY16], lpart);
+    g_thorin_launches++;
+    k_wn_sum<<<1, 32, 0, s>>>(lpart, (int)lb, (double)inv_n, n->dscal);
+    g_thorin_launches++;
+  }
   auto cnt = [&](int lv) { return (long long)B * h[lv] * w[lv] * WN_C; };
   // out layer
   RCHK_WN(wgrad_launch<32, 16>(n, 7, A[B0], A[GY16], B, h[0], w[0], s));
@@ -794,6 +873,8 @@ static int wn_check_err(thorin_warmnet *n)
 int wn_sor_predict(thorin_warmnet *n, int nr, int ns, double *T, const double *ml, const double *mlip,
                    const double *mlim, const double *mljp, const double *mljm, const double *rhs, cudaStream_t s)
 {
+  // dscal: [2] mean |r/Ml| of the start, [3] mean |r|, [4] residual loss,
+  // [5] supervised loss, [0] total loss; partials from dscal + 8
   SorSys m{ml, mlip, mlim, mljp, mljm, rhs};
   double *part = n->dscal + 8;
   const int sb = 2 * n->nsm;
@@ -808,29 +889,50 @@ int wn_sor_predict(thorin_warmnet *n, int nr, int ns, double *T, const double *m
   return e == cudaSuccess ? THORIN_OK : wn_fail("predict kernels", e);
 }
 
-// one training step on the solve that went from tk to tconv
+// one training step on the solve that went from tk to tconv: loss = WRES *
+// mean((A T_pred - rhs)^2) / mean|r_k|^2 + WSUP * mean((y - target)^2) over the
+// unknowns, T_pred = tk + jac + scale * YSCALE * y, target the converged update
+// beyond the Jacobi step in the same units
 int wn_sor_train(thorin_warmnet *n, int nr, int ns, const double *tk, const double *tconv, const double *ml,
                  const double *mlip, const double *mlim, const double *mljp, const double *mljm, const double *rhs,
-                 float lr, cudaStream_t s)
+                 float lr, double *scratch, cudaStream_t s)
 {
+  constexpr float WRES = 1.0f, WSUP = 0.1f;
   SorSys m{ml, mlip, mlim, mljp, mljm, rhs};
   double *part = n->dscal + 8;
   const int sb = 2 * n->nsm;
+  const long long cells = (long long)nr * ns;
+  const double inv_n = 1.0 / ((double)(nr - 2) * ns);
   k_wn_scale<<<sb, 256, 0, s>>>(nr, ns, tk, m, part);
-  k_wn_sum<<<1, 32, 0, s>>>(part, sb, 1.0 / ((double)(nr - 2) * ns), n->dscal + 2);
-  k_wn_features<<<nblk((long long)nr * ns), 256, 0, s>>>(nr, ns, tk, m, n->dscal + 2, n->x, n->jac);
-  k_wn_target<<<nblk((long long)nr * ns), 256, 0, s>>>(nr, ns, tconv, tk, n->jac, n->dscal + 2, n->tgt);
-  g_thorin_launches += 4;
+  k_wn_sum<<<1, 32, 0, s>>>(part, sb, inv_n, n->dscal + 2);
+  k_wn_sum<<<1, 32, 0, s>>>(part + sb, sb, inv_n, n->dscal + 3);
+  k_wn_features<<<nblk(cells), 256, 0, s>>>(nr, ns, tk, m, n->dscal + 2, n->x, n->jac);
+  k_wn_target<<<nblk(cells), 256, 0, s>>>(nr, ns, tconv, tk, n->jac, n->dscal + 2, n->tgt);
+  g_thorin_launches += 5;
   RCHK_WN(wn_forward(n, 1, s));
-  RCHK_WN(wn_backward(n, 1, s));
+  float *rs = n->gf[0];                       // free until the backward pass
+  k_wn_tpred<<<nblk(cells), 256, 0, s>>>(nr, ns, tk, n->jac, n->y, n->dscal + 2, scratch);
+  k_wn_res<<<nblk(cells), 256, 0, s>>>(nr, ns, scratch, m, n->dscal + 3, rs, part);
+  k_wn_sum<<<1, 32, 0, s>>>(part, (int)nblk(cells), inv_n, n->dscal + 4);
+  k_wn_res_grad<<<nblk(cells), 256, 0, s>>>(nr, ns, rs, m, n->dscal + 2, n->dscal + 3, n->y, n->tgt, WRES, WSUP, inv_n,
+                                            n->act[GY16], part);
+  k_wn_sum<<<1, 32, 0, s>>>(part, (int)nblk(cells), inv_n, n->dscal + 5);
+  k_wn_total<<<1, 1, 0, s>>>(n->dscal, WRES, WSUP);
+  g_thorin_launches += 6;
+  RCHK_WN(wn_backward(n, 1, s, false));
   RCHK_WN(wn_adam(n, lr, 0.9f, 0.999f, 1e-8f, 1.0f, s));
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? THORIN_OK : wn_fail("training kernels", e);
 }
 
+// total, residual and supervised loss of the last training step
 int wn_last_loss(thorin_warmnet *n, double *loss)
 {
-  WNCHK(cudaMemcpy(loss, n->dscal, sizeof(double), cudaMemcpyDeviceToHost));
+  double v[6];
+  WNCHK(cudaMemcpy(v, n->dscal, sizeof(v), cudaMemcpyDeviceToHost));
+  loss[0] = v[0];
+  loss[1] = v[4];
+  loss[2] = v[5];
   return wn_check_err(n);
 }
 

@@ -118,14 +118,15 @@ class WarmNet:
         return p
 
 
-def attach(disk, net: WarmNet | None, mode: int, restart_every: int = 0, lr: float = 0.0):
+def attach(disk, net: WarmNet | None, mode: int, lr: float = 0.0):
     """Attach net to disk (PREDICT or TRAIN) or detach (OFF)."""
     h = net.h if net is not None else C.c_void_p()
-    _lib.check(disk.L.thorin_gpu_warmstart(disk.h, h, mode, restart_every, lr), "thorin_gpu_warmstart")
+    _lib.check(disk.L.thorin_gpu_warmstart(disk.h, h, mode, lr), "thorin_gpu_warmstart")
 
 
 class WsStats(C.Structure):
-    _fields_ = [("predictions", C.c_longlong), ("train_steps", C.c_longlong), ("last_loss", C.c_double)]
+    _fields_ = [("predictions", C.c_longlong), ("train_steps", C.c_longlong), ("last_loss", C.c_double),
+                ("last_res_loss", C.c_double), ("last_sup_loss", C.c_double)]
 
 
 def stats(disk) -> WsStats:
@@ -172,21 +173,21 @@ def train(net: WarmNet, ndisks: int, steps_per_disk: int, lr: float = 1e-3, seed
         rate = lr if lr_final is None or ndisks == 1 else lr * (lr_final / lr) ** (k / (ndisks - 1))
         draw = draw_disk(rng)
         p, d, sys_ = make_training_disk(net.nr, net.ns, draw, seed=1000 * seed + k, dt_div=dt_div)
-        attach(d, net, TRAIN, 0, rate)
+        attach(d, net, TRAIN, rate)
         for _ in range(steps_per_disk):
             d.algogas(sys_)
         s = stats(d)
         losses.append(s.last_loss)
         if log:
             log(f"disk {k}: alpha {draw['alpha']:.2e} h {draw['aspect']:.3f} m {draw['mplanet']:.1e} "
-                f"lr {rate:.1e} solves {s.train_steps} loss {s.last_loss:.3e}")
+                f"lr {rate:.1e} steps {s.train_steps} loss {s.last_loss:.3e} (residual {s.last_res_loss:.3e}, "
+                f"supervised {s.last_sup_loss:.3e})", flush=True)
         attach(d, None, OFF)
         d.close()
     return losses
 
 
-def compare_sweeps(net: WarmNet, draw: dict, ndt: int, seed: int = 12345, restart_every: int = 0,
-                   dt_div: float = 1.0, warm: int = 1) -> dict:
+def compare_sweeps(net: WarmNet, draw: dict, ndt: int, seed: int = 12345, dt_div: float = 1.0, warm: int = 1) -> dict:
     """SOR sweeps per solve of the same disk run plain and with the network
     (PREDICT), after `warm` DTs that include the omega calibration.  Also
     returns the relative L2 difference of the temperatures after the first
@@ -197,7 +198,7 @@ def compare_sweeps(net: WarmNet, draw: dict, ndt: int, seed: int = 12345, restar
         p, d, sys_ = make_training_disk(net.nr, net.ns, draw, seed=seed, dt_div=dt_div)
         for _ in range(warm):
             d.algogas(sys_)
-        attach(d, net if mode == PREDICT else None, mode, restart_every if mode == PREDICT else 0)
+        attach(d, net if mode == PREDICT else None, mode)
         s0 = d.stats()
         sweeps0, calls0 = s0.sor_sweeps, s0.sor_calls
         for k in range(ndt):
@@ -230,7 +231,6 @@ if __name__ == "__main__":
     ap.add_argument("--init", default=None, help="start from this parameter file")
     ap.add_argument("--out", default=None, help="write the trained parameters here (.npy)")
     ap.add_argument("--eval-dts", type=int, default=2)
-    ap.add_argument("--restart", type=int, default=0)
     a = ap.parse_args()
     t0 = time.time()
     net = WarmNet(a.nrad, a.nsec, params=WarmNet.load_params(a.init) if a.init else None)
@@ -242,4 +242,4 @@ if __name__ == "__main__":
     if a.eval_dts > 0:
         from . import workloads
         draw = {"alpha": 1.0e-3, "aspect": 0.05, "mplanet": workloads.PLANET1[0]}
-        print("disk1 workload:", compare_sweeps(net, draw, a.eval_dts, restart_every=a.restart), flush=True)
+        print("disk1 workload:", compare_sweeps(net, draw, a.eval_dts), flush=True)

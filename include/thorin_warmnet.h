@@ -67,14 +67,17 @@ int thorin_warmnet_gradient(thorin_warmnet *n, int batch, const uint16_t *x, con
 /* One Adam step with the last gradient, clipped to global norm max_norm. */
 int thorin_warmnet_adam(thorin_warmnet *n, float lr, float beta1, float beta2, float eps, float max_norm);
 
-/* Attach a network to a disk (same nrad x nsec, batch >= 1) or detach it
- * (mode THORIN_WS_OFF, n may be NULL).  PREDICT: every SOR solve of the
- * disk starts from T_old + Jacobi step + network prediction and, when
- * restart_every > 0, re-applies the network to the current residual every
- * restart_every sweeps while the solve has not converged.  TRAIN: the solve
- * is plain; afterwards one Adam step (learning rate lr, moments 0.9/0.999,
- * norm clip 1) fits the network to that solve's converged update. */
-int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode, int restart_every, float lr);
+/* Attach a network to a disk (same nrad x nsec) or detach it (mode
+ * THORIN_WS_OFF, n may be NULL).  PREDICT: every SOR solve of the disk
+ * starts from T_old + Jacobi step + network prediction (a cell whose
+ * predicted temperature is not positive keeps T_old).  TRAIN: the solve is
+ * plain; afterwards one Adam step (learning rate lr, moments 0.9/0.999,
+ * norm clip 1) fits the network to that solve.  The loss of a step from
+ * start temperature T_k is
+ *   mean((A T_pred - rhs)^2) / mean|A T_k - rhs|^2 + 0.1 mean((y - target)^2)
+ * over the unknowns, T_pred = T_k + Jacobi step + the prediction and target
+ * the converged update beyond the Jacobi step in the network's units. */
+int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode, float lr);
 
 /* Layout check of the tensor-core path: D[128][32] = A[128][64] * B[32][64]^T
  * with bf16 bit patterns a, b (row-major) and FP32 d, on one CTA. */
@@ -85,6 +88,8 @@ typedef struct thorin_ws_stats {
   long long predictions;   /* network applications inside SOR solves   */
   long long train_steps;   /* training steps taken                     */
   double last_loss;        /* loss of the last training step           */
+  double last_res_loss;    /* its residual term                        */
+  double last_sup_loss;    /* its supervised term                      */
 } thorin_ws_stats;
 int thorin_gpu_warmstart_stats(thorin_disk *d, thorin_ws_stats *out);
 

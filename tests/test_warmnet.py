@@ -144,3 +144,68 @@ def test_adam_lowers_loss_on_fixed_batch():
         net.adam(3e-3)
     l1, _ = net.gradient(xb, t)
     assert l1 < 0.5 * l0, (l0, l1)
+
+
+def _small_disk():
+    return WS.make_training_disk(64, 192, {"alpha": 1e-3, "aspect": 0.05, "mplanet": 3e-5}, seed=3)
+
+
+@pytest.mark.gpu
+def test_training_leaves_the_plain_solve_unchanged():
+    """TRAIN mode fits the network after each solve; the disk's own fields
+    stay bit-identical to a run without a network."""
+    out = []
+    for mode in (WS.OFF, WS.TRAIN):
+        p, d, sys_ = _small_disk()
+        net = WS.WarmNet(64, 192)
+        if mode == WS.TRAIN:
+            WS.attach(d, net, WS.TRAIN, 1e-3)
+        for _ in range(2):
+            d.algogas(sys_)
+        out.append([d.get(f) for f in (0, 1, 2, 3, 4, 8)])
+        if mode == WS.TRAIN:
+            s = WS.stats(d)
+            assert s.train_steps == d.stats().sor_calls and np.isfinite(s.last_loss)
+        d.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_predicted_start_meets_the_same_threshold():
+    """From an untrained network (prediction = one Jacobi step) the solve
+    still converges to the plain solve's threshold: temperatures agree to the
+    SOR tolerance."""
+    temps, per = [], []
+    for mode in (WS.OFF, WS.PREDICT):
+        p, d, sys_ = _small_disk()
+        d.algogas(sys_)
+        net = WS.WarmNet(64, 192)
+        WS.attach(d, net, mode)
+        s0 = d.stats()
+        d.algogas(sys_)
+        s1 = d.stats()
+        temps.append(d.get(8))
+        per.append((s1.sor_sweeps - s0.sor_sweeps) / (s1.sor_calls - s0.sor_calls))
+        if mode == WS.PREDICT:
+            assert WS.stats(d).predictions == s1.sor_calls - s0.sor_calls
+        d.close()
+    assert np.linalg.norm(temps[1] - temps[0]) / np.linalg.norm(temps[0]) < 1e-9
+    assert per[1] <= per[0] + 1
+
+
+WEIGHTS = os.path.join(ROOT, "fargo_thorin_gb300", "warmnet_disk1_1024x3072.npy")
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not os.path.exists(WEIGHTS), reason="no trained network file")
+def test_trained_network_saves_sweeps_on_the_disk1_workload():
+    """The committed network, trained on the plain solver's solves of drawn
+    1024 x 3072 disks, against plain SOR on the measured disk1 workload: fewer
+    sweeps per solve at the same threshold, the same temperatures to 1e-9."""
+    from fargo_thorin_gb300 import workloads
+    net = WS.WarmNet(1024, 3072, params=WS.WarmNet.load_params(WEIGHTS))
+    r = WS.compare_sweeps(net, {"alpha": 1.0e-3, "aspect": 0.05, "mplanet": workloads.PLANET1[0]}, ndt=1)
+    print(r)
+    assert r["learned"] < r["plain"]
+    assert r["t_rel_l2"] < 1e-9
