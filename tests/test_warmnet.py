@@ -97,8 +97,6 @@ def test_umma_selftest_exact(lib):
                                         bb.ctypes.data_as(C.POINTER(C.c_uint16)),
                                         d.ctypes.data_as(C.POINTER(C.c_float))), "selftest_umma")
     ref = a.astype(np.float64) @ b.astype(np.float64).T
-    np.save(os.path.join(ROOT, "gpurun_out", "umma_selftest.npy"), d) if os.path.isdir(
-        os.path.join(ROOT, "gpurun_out")) else None
     assert np.max(np.abs(d - ref)) <= 1e-5 * np.max(np.abs(ref)), np.max(np.abs(d - ref))
 
 
