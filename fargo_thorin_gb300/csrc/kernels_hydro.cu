@@ -277,17 +277,16 @@ __device__ double opacity_BL94(double rho, double T)
   }
   double k;
   if (grains) {
-    const double T2 = T * T;
-    const double k1 = kappa[0] * T2;                       // pow(T, 2.0)
-    const double k2 = div_fast(kappa[1], T2 * T2 * T2 * T);        // pow(T, -7.0)
-    const double k3 = kappa[2] * sqrt(T);                  // pow(T, 0.5)
-    double t1 = div_fast(1.0, k1 * k1) + div_fast(1.0, k2 * k2);
-    t1 = div_fast(1.0, t1 * t1);
-    const double T5 = T2 * T2 * T;
-    const double x = div_fast(k3, 1.0 + div_fast(1.0e22, T5 * T5));     // pow(T, -10.0)
+    // k1 = kappa0 T^2, k2 = kappa1 T^-7, k3 = kappa2 T^0.5;
+    // t1 = (k1^-2 + k2^-2)^-2, x = k3 / (1 + 1e22 T^-10), k = (t1 + x^4)^(1/4),
+    // rearranged to three divisions
+    const double T2 = T * T, T4 = T2 * T2, T5 = T4 * T, T7 = T5 * T2, T10 = T5 * T5;
+    const double k3 = kappa[2] * sqrt(T);
+    const double ik = div_fast(1.0, 2.5e7 * div_fast(1.0, T4) + 2.5e-33 * (T7 * T7));   // 1 / (k1^-2 + k2^-2)
+    const double t1 = ik * ik;
+    const double x = div_fast(k3 * T10, T10 + 1.0e22);
     const double x2 = x * x;
-    const double t2 = x2 * x2;                             // pow(., 4.0)
-    k = sqrt(sqrt(t1 + t2));                               // pow(., 0.25)
+    k = sqrt(sqrt(t1 + x2 * x2));
   } else if (T <= TEMPB(3, 4)) {
     k = kappa[3] * pow(rho, a[3]) * pow(T, b[3]);
   } else if ((T > TEMPB(3, 4)) && (T <= TEMPB(4, 5))) {
@@ -487,13 +486,15 @@ __global__ void k_diffcoef(DevGrid g, const double *__restrict__ rho, const doub
     else kap = opacity_law(g.k, law, vd * g.k.rho2cgs, Tl * g.k.t2si, parametric_raw) * g.k.opa2cu;
     opacity[l] = kap;
     const double tau = opacity_drop * 0.5 * kap * rho[l];
-    const double taueff = 0.375 * tau + taueff_c + div_fast(0.25, tau);
+    // Q- = 2 sigma T^3 / tau_eff, tau_eff = 3/8 tau + c + 1/(4 tau), as one quotient
     const double T3 = cube_rn(Tl);
-    qminus[l] = div_fast(2.0 * g.k.sigma_sb * T3, taueff);
+    qminus[l] = div_fast(2.0 * g.k.sigma_sb * T3 * tau, __fma_rn(__fma_rn(0.375, tau, taueff_c), tau, 0.25));
     const int ig = (i == 0) ? 1 : (i == nr - 1 ? nr - 2 : i);
     const double gradt = gradt_mag(g, T, ig, j, invdxtheta_r);
-    const double fac = div_fast(1.0, vd * kap);
-    const double s = div_fast(4.0 * gradt * fac, Tl);
+    // fac = 1 / (rho_mid kappa) and the limiter argument s = 4 |grad T| fac / T from one division
+    const double q = div_fast(1.0, vd * kap * Tl);
+    const double fac = q * Tl;
+    const double s = 4.0 * gradt * q;
     const double D = flux_limiter(s) * 16.0 * g.k.sigma_sb * T3 * fac;
     dcen[l] = D;
     dtl = div_fast(deltar2_r[i], D);
@@ -679,6 +680,24 @@ __global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__r
 // its absolute value added to the L1 norm, delta = resid * (omega/Ml) with
 // omega/Ml prepared once per solve by k_sor_resid0, the update, and the
 // change test delta > T*SORPRECISION taken from the sign of one FMA.
+// delta > tn * SORPRECISION (SORPRECISION = 1e-15, between 2^-50 and 2^-49).
+// For positive tn the binary exponents decide it on the integer pipe unless
+// they are 49 or 50 apart (or delta is zero or subnormal); those cases, and a
+// non-positive tn, take the sign of the exact difference.
+__device__ __forceinline__ bool sor_changed(double delta, double tn)
+{
+  const long long d64 = __double_as_longlong(delta), t64 = __double_as_longlong(tn);
+  if (t64 > 0x000FFFFFFFFFFFFFLL && t64 < 0x7FF0000000000000LL) {   // tn positive, normal, finite
+    if (d64 <= 0LL) return false;                                     // delta <= +0 (or negative)
+    const int diff = (int)(d64 >> 52) - (int)(t64 >> 52);
+    if ((d64 >> 52) != 0 && (d64 >> 52) != 0x7FF) {
+      if (diff >= -48) return true;
+      if (diff <= -51) return false;
+    }
+  }
+  return __double_as_longlong(__fma_rn(-tn, TH_SORPRECISION, delta)) > 0LL;
+}
+
 __global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict__ T, const double *__restrict__ ml,
                                                   const double *__restrict__ mlip, const double *__restrict__ mlim,
                                                   const double *__restrict__ mljp, const double *__restrict__ mljm,
@@ -712,8 +731,7 @@ __global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict_
         const double delta = resid * cw[q];
         const double tn = T[l] - delta;
         T[l] = tn;
-        // delta > tn * SORPRECISION, from the sign of the exact difference
-        ch += (__double_as_longlong(__fma_rn(-tn, TH_SORPRECISION, delta)) > 0LL) ? 1 : 0;
+        ch += sor_changed(delta, tn) ? 1 : 0;
       }
     }
   }
