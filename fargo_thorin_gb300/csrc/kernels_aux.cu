@@ -399,8 +399,9 @@ __global__ void k_pebble_substep1(DevGrid g, double *__restrict__ pvr, double *_
   const double t = tau[l];
   const double efac = exp(div_fast(-dt * Omega, t));
   double a = pvr[l], b = pvt[l];
-  if (i > 0) a = a * efac + gaccr[l] * dt + (vr[l] + div_fast((paccr[l] - gaccr[l]) * t, Omega)) * (1.0 - efac);
-  b = b * efac + gacct[l] * dt + (vt[l] + div_fast((pacct[l] - gacct[l]) * t, Omega)) * (1.0 - efac);
+  const double oinv = g.r.OmegaInv[i];               // x / Omega as x * OmegaInv
+  if (i > 0) a = a * efac + gaccr[l] * dt + (vr[l] + (paccr[l] - gaccr[l]) * t * oinv) * (1.0 - efac);
+  b = b * efac + gacct[l] * dt + (vt[l] + (pacct[l] - gacct[l]) * t * oinv) * (1.0 - efac);
   if (diffusion) {
     if (i >= 1) {
       const int lim = l - ns;
@@ -541,14 +542,14 @@ __global__ void __launch_bounds__(128) k_forces(DevGrid g, ForceArgs a, ForceRin
     const double mcell = a.rho[l] * g.r.Surf[i];
     const double H = a.cs[l] * omegainv * g.k.sqrt_adiabind_inv;
     const double H_avr = fr.H_avr[i];
-    int local = (div_fast(fabs(H - H_avr), H_avr) > 0.05) ? 1 : 0;
+    int local = (fabs(H - H_avr) > 0.05 * H_avr) ? 1 : 0;      // |H - H_avr| / H_avr > 0.05
     double Hcorr = 0.0, pH = 0.0, pmcell = 0.0;
     if (peb) {
       pmcell = a.pdens[l] * g.r.Surf[i];
       Hcorr = sqrt(div_fast(a.pebble_alpha, a.tau[l]));
       pH = H * Hcorr;
       const double p_H_avr = fr.p_H_avr[i];
-      if (div_fast(fabs(pH - p_H_avr), p_H_avr) > 0.05) local = 1;
+      if (fabs(pH - p_H_avr) > 0.05 * p_H_avr) local = 1;
     }
     double s2[MAXPL_DEV], integpl[MAXPL_DEV], p_integpl[MAXPL_DEV], hillcut[MAXPL_DEV];
     int with[MAXPL_DEV];

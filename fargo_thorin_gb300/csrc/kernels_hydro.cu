@@ -680,22 +680,25 @@ __global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__r
 // its absolute value added to the L1 norm, delta = resid * (omega/Ml) with
 // omega/Ml prepared once per solve by k_sor_resid0, the update, and the
 // change test delta > T*SORPRECISION taken from the sign of one FMA.
-// delta > tn * SORPRECISION (SORPRECISION = 1e-15, between 2^-50 and 2^-49).
-// For positive tn the binary exponents decide it on the integer pipe unless
-// they are 49 or 50 apart (or delta is zero or subnormal); those cases, and a
-// non-positive tn, take the sign of the exact difference.
-__device__ __forceinline__ bool sor_changed(double delta, double tn)
+// delta > tn * SORPRECISION (SORPRECISION = 1e-15, between 2^-50 and 2^-49)
+// with delta = resid * cw, cw = omega / Ml > 0.  When resid, cw and tn are
+// positive normal numbers well inside the exponent range, delta lies in
+// [2^(a+b), 2^(a+b+2)] for the exponents a, b of resid and cw, so the
+// exponents decide the test on the integer pipe unless a + b - t is within
+// -51..-49; those cases, and all unusual operands, take the exact sign test.
+__device__ __forceinline__ bool sor_changed(double resid, double cw, double tn)
 {
-  const long long d64 = __double_as_longlong(delta), t64 = __double_as_longlong(tn);
-  if (t64 > 0x000FFFFFFFFFFFFFLL && t64 < 0x7FF0000000000000LL) {   // tn positive, normal, finite
-    if (d64 <= 0LL) return false;                                     // delta <= +0 (or negative)
-    const int diff = (int)(d64 >> 52) - (int)(t64 >> 52);
-    if ((d64 >> 52) != 0 && (d64 >> 52) != 0x7FF) {
+  const long long r64 = __double_as_longlong(resid), c64 = __double_as_longlong(cw), t64 = __double_as_longlong(tn);
+  const int er = (int)(r64 >> 52), ec = (int)(c64 >> 52), et = (int)(t64 >> 52);
+  if (t64 > 0LL && et >= 100 && et < 0x7FF && c64 > 0LL && ec != 0 && ec < 0x7FF) {
+    if (r64 <= 0LL) return false;                      // resid <= +0: delta <= 0 < threshold
+    if (er != 0 && er != 0x7FF && er + ec - 1023 >= 100 && er + ec - 1023 < 0x7FF - 100) {
+      const int diff = er + ec - 1023 - et;
       if (diff >= -48) return true;
-      if (diff <= -51) return false;
+      if (diff <= -52) return false;
     }
   }
-  return __double_as_longlong(__fma_rn(-tn, TH_SORPRECISION, delta)) > 0LL;
+  return __double_as_longlong(__fma_rn(-tn, TH_SORPRECISION, resid * cw)) > 0LL;
 }
 
 __global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict__ T, const double *__restrict__ ml,
@@ -728,10 +731,10 @@ __global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict_
         const size_t q = pbase + k;
         const double resid = sor_resid_at(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm, q);
         a += fabs(resid);
-        const double delta = resid * cw[q];
-        const double tn = T[l] - delta;
+        const double c = cw[q];
+        const double tn = __fma_rn(-resid, c, T[l]);     // T -= omega resid / Ml
         T[l] = tn;
-        ch += sor_changed(delta, tn) ? 1 : 0;
+        ch += sor_changed(resid, c, tn) ? 1 : 0;
       }
     }
   }
@@ -896,12 +899,14 @@ __global__ void k_rad_update(DevGrid g, PtrPack8 qf, const double *__restrict__ 
   CELL_LOOP_2D
   const int lip = l + ns;
   const double dtheta = 2.0 * TH_PI / (double)ns;
-  const double ci = dt * dtheta * g.r.Rinf[i];
-  const double co = dt * dtheta * g.r.Rsup[i];
+  // the mass fluxes through the inner and outer faces are shared by all
+  // quantities: varq = q*_in fin - q*_out fout
+  const double fin = dt * dtheta * g.r.Rinf[i] * rhos[l] * vr[l];
+  const double fout = dt * dtheta * g.r.Rsup[i] * rhos[lip] * vr[lip];
+  const double is = g.r.InvSurf[i];
   for (int q = 0; q < io.n; q++) {
-    double varq = ci * qf.src[q][l] * rhos[l] * vr[l];
-    varq -= co * qf.src[q][lip] * rhos[lip] * vr[lip];
-    io.dst[q][l] = io.src[q][l] + varq * g.r.InvSurf[i];
+    const double varq = __fma_rn(qf.src[q][l], fin, -(qf.src[q][lip] * fout));
+    io.dst[q][l] = __fma_rn(varq, is, io.src[q][l]);
   }
 }
 
