@@ -132,6 +132,8 @@ __global__ void __launch_bounds__(256) k_cfl_cells(DevGrid g, const double *__re
   const int i = blockIdx.y + 1;                    // rings One_or_active .. Max_or_active-1
   const double dxrad = cr.dxrad[i], dxtheta = cr.dxtheta[i], mindx = cr.mindx[i];
   const double invdt5 = viscous ? div_fast(g.r.nu_med[i] * 4., cr.den5[i]) : 1e-30;
+  // the per-cell rates divide by ring constants: multiply by their reciprocals
+  const double idxrad = div_fast(1.0, dxrad), idxtheta = div_fast(1.0, dxtheta), imindx = div_fast(1.0, mindx);
   long long gas = 0, peb = 0;
   for (int m = 0; m < CFL_CPT; m++) {
     const int j = (blockIdx.x * CFL_CPT + m) * blockDim.x + threadIdx.x;
@@ -139,24 +141,24 @@ __global__ void __launch_bounds__(256) k_cfl_cells(DevGrid g, const double *__re
     const int l = j + i * ns, lip = l + ns;
     const int ljp = (j == ns - 1) ? i * ns : l + 1;
     const double vres = fast ? vt[l] - cr.vmoy[i] : vt[l];
-    const double invdt1 = div_fast(cs[l], mindx);
-    const double invdt2 = div_fast(fabs(vr[l]), dxrad);
-    const double invdt3 = div_fast(fabs(vres), dxtheta);
+    const double invdt1 = cs[l] * imindx;
+    const double invdt2 = fabs(vr[l]) * idxrad;
+    const double invdt3 = fabs(vres) * idxtheta;
     double dvr = vr[lip] - vr[l], dvt = vt[ljp] - vt[l];
     dvr = (dvr >= 0.0) ? 1e-10 : -dvr;
     dvt = (dvt >= 0.0) ? 1e-10 : -dvt;
-    const double a = div_fast(dvr, dxrad), b = div_fast(dvt, dxtheta);
+    const double a = dvr * idxrad, b = dvt * idxtheta;
     double invdt4 = (b > a) ? b : a;
     invdt4 *= 4.0 * TH_CVNR * TH_CVNR;
     const double sg = invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4 + invdt5 * invdt5;
     const long long bg = __double_as_longlong(sg);
     gas = bg > gas ? bg : gas;
     if (pebbles) {
-      const double p1 = div_fast(fabs(pvr[l]), dxrad);
+      const double p1 = fabs(pvr[l]) * idxrad;
       const double vrp = fast ? pvt[l] - cr.pvtmed[i] : pvt[l];
-      const double p2 = div_fast(fabs(vrp), dxtheta);
-      const double p3 = div_fast(fabs(pvr[l] - vr[l]), dxrad);
-      const double p4 = div_fast(fabs(pvt[l] - vt[l]), dxtheta);
+      const double p2 = fabs(vrp) * idxtheta;
+      const double p3 = fabs(pvr[l] - vr[l]) * idxrad;
+      const double p4 = fabs(pvt[l] - vt[l]) * idxtheta;
       const long long bp = __double_as_longlong(p1 * p1 + p2 * p2 + p3 * p3 + p4 * p4);
       peb = bp > peb ? bp : peb;
     }
@@ -354,6 +356,7 @@ __global__ void k_pebble_sources(DevGrid g, const double *__restrict__ pd, const
   CELL_LOOP_2D
   const double Omega = div_fast(1.0, g.r.OmegaInv[i]);
   const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+  const double otau = back_reaction ? div_fast(Omega, tau[l]) : 0.0;    // Omega / tau_s
   if (i >= 1) {
     const int lim = l - ns;
     const int ljp = (j == ns - 1) ? i * ns : l + 1;
@@ -362,13 +365,13 @@ __global__ void k_pebble_sources(DevGrid g, const double *__restrict__ pd, const
     vt2 = vt2 * vt2;
     paccr[l] = vt2 * g.r.InvRinf[i] + 0.5 * (pagr[l] + pagr[lim]);
     if (back_reaction) {
-      const double drag = div_fast(Omega * (pvr[l] - vr[l]), tau[l]);
+      const double drag = (pvr[l] - vr[l]) * otau;
       dragr[l] = 0.5 * (pd[l] + pd[lim]) * drag;
     }
   }
   pacct[l] = 0.5 * (pagt[l] + pagt[ljm]);
   if (back_reaction) {
-    const double drag = div_fast(Omega * (pvt[l] - vt[l]), tau[l]);
+    const double drag = (pvt[l] - vt[l]) * otau;
     dragt[l] = 0.5 * (pd[l] + pd[ljm]) * drag;
   }
 }

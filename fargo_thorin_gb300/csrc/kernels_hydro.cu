@@ -207,7 +207,7 @@ __global__ void k_qplus(DevGrid g, const double *__restrict__ vr, const double *
     const double nu = g.r.nu_med[i];
     double q;
     if (nu != 0.0) {
-      q = div_fast(div_fast(0.5, nu), rho[l]) * (s.trr * s.trr + 2.0 * s.trp * s.trp + s.tpp * s.tpp);
+      q = div_fast(0.5, nu * rho[l]) * (s.trr * s.trr + 2.0 * s.trp * s.trp + s.tpp * s.tpp);
       q += (2.0 / 9.0) * nu * rho[l] * s.divv * s.divv;
     } else {
       q = 0.0;
@@ -583,7 +583,7 @@ __global__ void k_matrix(DevGrid g, const double *__restrict__ rho, const double
   const double Dt_ljp = 0.5 * (dcen[ljp] + dcen[l]);
   const double B_ljp = Dt_ljp * idx2 * 2.0 * Hjp;
   const double bfac = div_fast(dt, rho[l] * g.k.cv);
-  const double afac = div_fast(bfac * g.r.InvDiffRsup[i] * 2.0 * H, g.r.Rmed[i]);
+  const double afac = bfac * g.r.InvDiffRsup[i] * 2.0 * H * g.r.InvRmed[i];
   const double Tl = T[l], qm = qminus[l];
   const size_t q = sor_pidx(i, j, ns >> 1);
   const double diag = 1.0 + divv[l] * gm1 * dt + 4.0 * bfac * qm + afac * (A_lip + A_l) + bfac * (B_ljp + B_l);
@@ -884,10 +884,11 @@ __global__ void k_rad_face(DevGrid g, PtrPack8 w, PtrPack8 dq, const double *__r
   const double v = vr[l];
   if (v > 0.0) {
     const double c = (g.r.Rmed[i] - g.r.Rmed[i - 1] - v * dt) * 0.5;
-    for (int q = 0; q < w.n; q++) w.dst[q][l] = w.src[q][l - ns] + c * dq.src[q][l - ns];
+    for (int q = 0; q < w.n; q++)
+      w.dst[q][l] = dq.src[q] ? w.src[q][l - ns] + c * dq.src[q][l - ns] : w.src[q][l - ns];
   } else {
     const double c = (g.r.Rmed[i + 1] - g.r.Rmed[i] + v * dt) * 0.5;
-    for (int q = 0; q < w.n; q++) w.dst[q][l] = w.src[q][l] - c * dq.src[q][l];
+    for (int q = 0; q < w.n; q++) w.dst[q][l] = dq.src[q] ? w.src[q][l] - c * dq.src[q][l] : w.src[q][l];
   }
 }
 
@@ -1020,10 +1021,17 @@ __global__ void __launch_bounds__(AZ_TMAX) k_azimuthal(DevGrid g, AziIO io, cons
       const double w = q[k] * rcp;
       s_a[t] = w;
       __syncthreads();
-      const double dq = azi_vl_slope_raw(s_a[tm], w, s_a[tp]);
-      s_b[t] = dq;
-      __syncthreads();
-      const double qs = up ? __fma_rn(cs, s_b[tm], s_a[tm]) : __fma_rn(-cs, dq, w);
+      double qs;
+      if (k < NQ - 1) {
+        const double dq = azi_vl_slope_raw(s_a[tm], w, s_a[tp]);
+        s_b[t] = dq;
+        __syncthreads();
+        qs = up ? __fma_rn(cs, s_b[tm], s_a[tm]) : __fma_rn(-cs, dq, w);
+      } else {
+        // the density's own quotient rho / (rho + 1e-20) is 1 to within
+        // 1e-20 / rho: its slope term is below rounding
+        qs = up ? s_a[tm] : w;
+      }
       const double F = qs * cf;
       s_c[t] = F;
       __syncthreads();
@@ -1078,13 +1086,12 @@ __global__ void k_velocities(DevGrid g, const double *__restrict__ rho, const do
     v = (v + lambda * 0.0) / (1.0 + lambda);
   }
   vr[l] = v;
-  vt[l] = div_fast(div_fast(tmp_[ljm] + tmm[l], rho[l] + rho[ljm] + 1e-15), rm) - rm * omega_frame;
+  vt[l] = div_fast(tmp_[ljm] + tmm[l], rho[l] + rho[ljm] + 1e-15) * g.r.InvRmed[i] - rm * omega_frame;
   if (temper) {
     const double r = rho[l], e = energy[l];
-    double tmp2 = div_fast(1.0, r * 1.0);
-    double tmp1 = e * 1.0 * gm1;
-    temper[l] = tmp1 * tmp2;
-    cs[l] = sqrt(div_fast(gg1 * fabs(e), r));
+    const double tmp2 = div_fast(1.0, r);
+    temper[l] = e * gm1 * tmp2;
+    cs[l] = sqrt(gg1 * fabs(e) * tmp2);
   }
 }
 
@@ -1252,7 +1259,10 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
   // slopes of the quotients and of rho (slot 7)
   PtrPack8 sl;
   int n = 0;
-  for (int k = 0; k < nq; k++) { sl.src[n] = S.w[qi[k]]; sl.dst[n] = S.d[qi[k]]; n++; }
+  // (the quotient rho / (rho + 1e-20) of the density is 1 to within
+  // 1e-20 / rho, so its slope term is below rounding and is left out)
+  for (int k = 0; k < nq; k++)
+    if (qi[k] != 5) { sl.src[n] = S.w[qi[k]]; sl.dst[n] = S.d[qi[k]]; n++; }
   sl.src[n] = *rho; sl.dst[n] = S.d[7]; n++;
   sl.n = n;
   k_rad_slope<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, sl);
@@ -1260,7 +1270,9 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
   // faces: quotients and rho
   PtrPack8 wf, dqf;
   n = 0;
-  for (int k = 0; k < nq; k++) { wf.src[n] = S.w[qi[k]]; wf.dst[n] = S.f[qi[k]]; dqf.src[n] = S.d[qi[k]]; n++; }
+  for (int k = 0; k < nq; k++) {
+    wf.src[n] = S.w[qi[k]]; wf.dst[n] = S.f[qi[k]]; dqf.src[n] = (qi[k] == 5) ? nullptr : S.d[qi[k]]; n++;
+  }
   wf.src[n] = *rho; wf.dst[n] = S.f[7]; dqf.src[n] = S.d[7]; n++;
   wf.n = dqf.n = n;
   k_rad_face<<<grid2d(ns, nr + 1, BX), BX, 0, s>>>(g, wf, dqf, vr, dt);
