@@ -39,7 +39,8 @@ __global__ void k_substep1(DevGrid g, const double *__restrict__ rho, const doub
   if (i >= 1) {
     const int lim = l - ns;
     const double plim = press ? press[lim] : gm1 * energy[lim];
-    double gradp = div_fast((pl - plim) * 2.0, rho[l] + rho[lim]) * g.r.InvDiffRmed[i];
+    const double ir2 = div_fast(2.0, rho[l] + rho[lim]);     // 2 / (rho_l + rho_lim), shared
+    double gradp = (pl - plim) * ir2 * g.r.InvDiffRmed[i];
     double vt2 = vtheta[l] + vtheta[ljp] + vtheta[lim] + vtheta[ljp - ns];
     vt2 = vt2 / 4.0 + g.r.Rinf[i] * omega_frame;
     vt2 = vt2 * vt2;
@@ -48,7 +49,7 @@ __global__ void k_substep1(DevGrid g, const double *__restrict__ rho, const doub
     if (pebbles) {
       double acc = tmp;
       if (back_reaction) {
-        tmp = div_fast(dragr[l] * 2.0, rho[l] + rho[lim]);
+        tmp = dragr[l] * ir2;
         v += dt * tmp;
         acc += tmp;
       }
@@ -59,14 +60,15 @@ __global__ void k_substep1(DevGrid g, const double *__restrict__ rho, const doub
   {
     const double invdxtheta = invdxtheta_r[i];
     const double pljm = press ? press[ljm] : gm1 * energy[ljm];
-    double gradp = div_fast((pl - pljm) * 2.0, rho[l] + rho[ljm]) * invdxtheta;
+    const double it2 = div_fast(2.0, rho[l] + rho[ljm]);     // 2 / (rho_l + rho_ljm), shared
+    double gradp = (pl - pljm) * it2 * invdxtheta;
     double tmp = -gradp + 0.5 * (agt[l] + agt[ljm]);
     double v = vtheta[l] + dt * tmp;
     v += dt * supp_torque[i];
     if (pebbles) {
       double acc = tmp + supp_torque[i];
       if (back_reaction) {
-        tmp = div_fast(dragt[l] * 2.0, rho[l] + rho[ljm]);
+        tmp = dragt[l] * it2;
         v += dt * tmp;
         acc += tmp;
       }
@@ -287,6 +289,30 @@ __device__ double opacity_BL94(double rho, double T)
     const double x = div_fast(k3 * T10, T10 + 1.0e22);
     const double x2 = x * x;
     k = sqrt(sqrt(t1 + x2 * x2));
+  } else if (T > 0.0 && rho > 0.0) {
+    // T <= TEMPB(i, j) compared as logarithms: ln T <= (ln(kappa_j / kappa_i)
+    // + (a_j - a_i) ln rho) / (b_i - b_j), one log each of rho and T; the
+    // regimes' power laws with integer powers, cbrt and sqrt
+    const double lr = log(rho), lT = log(T);
+    const double t34 = __fma_rn(-0.33333333333333337, lr, -205.62322045703002) * -0.037037037037037035;
+    const double t45 = __fma_rn(-0.3333333333333333, lr, -64.47238260383328) * -0.14285714285714285;
+    const double t56 = __fma_rn(0.6666666666666667, lr, 129.35023031577472) * 0.08;
+    const double t67 = __fma_rn(-1.0, lr, -47.51271976719674) * -0.4;
+    const double T2 = T * T;
+    if (lT <= t34) {
+      const double T3 = T2 * T, T6 = T3 * T3, T12 = T6 * T6;
+      k = div_fast(kappa[3] * rho, T12 * T12);                 // rho T^-24
+    } else if (lT <= t45) {
+      const double c = cbrt(rho);
+      k = kappa[4] * (c * c) * (T2 * T);                       // rho^(2/3) T^3
+    } else if (lT <= t56) {
+      const double T5 = T2 * T2 * T;
+      k = kappa[5] * cbrt(rho) * (T5 * T5);                    // rho^(1/3) T^10
+    } else if (lT <= t67) {
+      k = div_fast(kappa[6] * rho, T2 * sqrt(T));              // rho T^-2.5
+    } else {
+      k = kappa[7];
+    }
   } else if (T <= TEMPB(3, 4)) {
     k = kappa[3] * pow(rho, a[3]) * pow(T, b[3]);
   } else if ((T > TEMPB(3, 4)) && (T <= TEMPB(4, 5))) {
@@ -633,7 +659,9 @@ __device__ __forceinline__ bool sor_last_block(unsigned int *ticket, unsigned nb
   return last;
 }
 
+#ifndef SOR_CPT
 #define SOR_CPT 4        // cells of one colour per thread
+#endif
 #define SOR_BX 128       // threads per SOR block
 
 __global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__restrict__ T,
