@@ -123,6 +123,11 @@ struct thorin_disk {
   double *pdens, *pvrad, *pvtheta, *psize, *tau, *paccr, *pacct, *gaccr, *gacct, *dragr, *dragt, *macc;
   double *t_rho_gas, *t_e_gas, *t_rho_peb;
   TransportScratch ts;
+  // the pebble fluid's transport runs on its own stream with its own scratch,
+  // concurrently with SubStep2, the energy step and the gas transport
+  TransportScratch ts_peb;
+  cudaStream_t s_peb = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double *partials, *scal;
   int *iscal, *nshift, *heat_idx_d, *damp_rings_d;
   double *heat_val_d;
@@ -386,6 +391,28 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   d->ts.nshift = d->nshift;
   d->ts.vmed = d->ring[R_VMED];
   d->ts.vtemp = d->ring[R_VTEMP];
+  if (d->p.pebbles) {
+    TransportScratch &P = d->ts_peb;
+    P = TransportScratch{};
+    for (int q = 0; q < 4; q++) RCHK(dfield(d, &P.mom[q]));
+    for (int q = 0; q < 6; q++) RCHK(dfield(d, &P.w[q]));
+    // pebbles carry the four momenta (slots 0-3) and the density (slot 5,
+    // its slope in slot 7): no energy or tracer slots, no slope of the
+    // density quotient
+    for (int q = 0; q < 8; q++) {
+      const bool used = q < 4 || q == 5 || q == 7;
+      P.d[q] = P.f[q] = nullptr;
+      if (used && q != 5) RCHK(dfield(d, &P.d[q]));
+      if (used) RCHK(dfield(d, &P.f[q]));
+    }
+    P.w[6] = P.ext = P.ext_new = nullptr;
+    RCHK(dalloc(d, (void **)&P.nshift, n1 * sizeof(int)));
+    RCHK(dalloc(d, (void **)&P.vmed, n1 * sizeof(double)));
+    RCHK(dalloc(d, (void **)&P.vtemp, n1 * sizeof(double)));
+    CUCHK(cudaStreamCreateWithFlags(&d->s_peb, cudaStreamNonBlocking));
+    CUCHK(cudaEventCreateWithFlags(&d->ev_fork, cudaEventDisableTiming));
+    CUCHK(cudaEventCreateWithFlags(&d->ev_join, cudaEventDisableTiming));
+  }
   // reduction scratch: enough partials for every reduction kernel
   const size_t nb = (size_t)((d->ns + 127) / 128 + 2) * (size_t)(d->nr + 2);
   RCHK(dalloc(d, (void **)&d->partials, nb * (2 + 2 * MAXPL_DEV + 6) * sizeof(double)));
@@ -527,6 +554,12 @@ extern "C" int thorin_gpu_destroy(thorin_disk *d)
   cudaFreeHost(d->iscal_h);
   cudaFreeHost(d->csmean_h);
   for (int q = 0; q < 4; q++) cudaEventDestroy(d->ev[q]);
+  if (d->s_peb) {
+    cudaStreamSynchronize(d->s_peb);
+    cudaEventDestroy(d->ev_fork);
+    cudaEventDestroy(d->ev_join);
+    cudaStreamDestroy(d->s_peb);
+  }
   cudaStreamDestroy(d->s);
   delete d;
   return THORIN_OK;
@@ -1532,9 +1565,9 @@ static int energy_step(thorin_disk *d, double dt)
 }
 
 static void transport_fluid(thorin_disk *d, double **rho, double *vr, double *vt, double **energy, double **rho_scratch,
-                            double dt, int gas)
+                            double dt, int gas, const TransportScratch &scratch, cudaStream_t stream)
 {
-  TransportScratch S = d->ts;
+  TransportScratch S = scratch;
   S.rho_new = *rho_scratch;
   S.e_new = energy ? d->t_e_gas : nullptr;
   // the v_r damping of the boundary call after the transport is fused into
@@ -1543,7 +1576,7 @@ static void transport_fluid(thorin_disk *d, double **rho, double *vr, double *vt
   const int fused = p.damping && p.damp_vrad && !(p.open_inner || p.open_outer || p.non_reflecting || p.outer_source_mass);
   hydro_transport(d->g, rho, vr, vt, energy, (gas && p.label_advection) ? d->label : nullptr, S, dt, d->OmegaFrame,
                   p.fast_transport, gas && fused, d->drin, d->drout, gas ? d->temper : nullptr, d->cs, d->gm1, d->gg1,
-                  d->s);
+                  stream);
   std::swap(*rho, *rho_scratch);
   if (energy) std::swap(*energy, d->t_e_gas);
 }
@@ -1588,9 +1621,21 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
   const int kepler = (!p.damping) || (p.damping && p.damp_vrad);
   hydro_visc_update(d->g, d->vrad_int, d->vtheta_int, d->rho, d->trr, d->tpp, d->trp, dt, d->invdphi, kepler,
                     d->vkep_in - d->Rmed[0] * d->OmegaFrame, d->vkep_out - d->Rmed[d->nr - 1] * d->OmegaFrame, d->s);
-  if (p.pebbles)
+  if (p.pebbles) {
     aux_pebble_substep1(d->g, d->pvrad, d->pvtheta, d->tau, d->vrad, d->vtheta, d->paccr, d->pacct, d->gaccr, d->gacct,
                         d->rho, d->pdens, dt, p.diffusive_particles, p.schmidt_number, d->ring[R_INVDXTHETA], d->s);
+    // EvolvePebbleDisk (Pebbles.c:702-708).  From here on the pebble fields
+    // are read and written only by the pebble transport and the gas side
+    // touches none of them, so it runs on the pebble stream while the gas
+    // goes through SubStep2, the energy step and its own transport; the
+    // streams join before this call returns.
+    CUCHK(cudaEventRecord(d->ev_fork, d->s));
+    CUCHK(cudaStreamWaitEvent(d->s_peb, d->ev_fork, 0));
+    aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, d->s_peb);
+    transport_fluid(d, &d->pdens, d->pvrad, d->pvtheta, nullptr, &d->t_rho_peb, dt, 0, d->ts_peb, d->s_peb);
+    aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, d->s_peb);
+    CUCHK(cudaEventRecord(d->ev_join, d->s_peb));
+  }
   // SubStep2, ActualiseGas, ApplyBoundaryCondition
   hydro_substep2(d->g, d->rho, d->vrad_int, d->vtheta_int, d->energy, d->vrad_new, d->vtheta_new, d->energy_int, dt,
                  p.energy_eq, d->ring[R_INVDXTHETA], d->s);
@@ -1600,11 +1645,14 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
   int status = THORIN_OK;
   if (p.energy_eq) {
     int s = energy_step(d, dt);
-    if (s != THORIN_OK && s != THORIN_ERR_SOR_MAXIT) return s;
+    if (s != THORIN_OK && s != THORIN_ERR_SOR_MAXIT) {
+      if (p.pebbles) cudaStreamWaitEvent(d->s, d->ev_join, 0);
+      return s;
+    }
     status = s;
   }
   // Transport, ApplyBoundaryCondition, ComputeTemperatureField, ComputeSoundSpeed
-  transport_fluid(d, &d->rho, d->vrad, d->vtheta, p.energy_eq ? &d->energy : nullptr, &d->t_rho_gas, dt, 1);
+  transport_fluid(d, &d->rho, d->vrad, d->vtheta, p.energy_eq ? &d->energy : nullptr, &d->t_rho_gas, dt, 1, d->ts, d->s);
   CUCHK(cudaMemcpyAsync(d->nshift_h.data(), d->nshift, d->nr * sizeof(int), cudaMemcpyDeviceToHost, d->s));
   if ((damp && !p.damp_vrad) || p.open_inner || p.open_outer || p.non_reflecting || p.outer_source_mass) {
     // damping towards INIT / GASFLUX changes Sigma (and e): the boundary
@@ -1617,12 +1665,7 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
   if (p.alpha_flock) aux_ring_mean(d->g, d->temper, d->ring[R_TEMPMEAN], d->s);
   aux_viscosity_rings(d->g, d->vp, d->s);
   CUCHK(cudaMemcpyAsync(d->csmean_h, d->ring[R_CSMEAN], d->nr * sizeof(double), cudaMemcpyDeviceToHost, d->s));
-  // EvolvePebbleDisk (Pebbles.c:702-708)
-  if (p.pebbles) {
-    aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, d->s);
-    transport_fluid(d, &d->pdens, d->pvrad, d->pvtheta, nullptr, &d->t_rho_peb, dt, 0);
-    aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, d->s);
-  }
+  if (p.pebbles) CUCHK(cudaStreamWaitEvent(d->s, d->ev_join, 0));     // join the pebble transport
   KCHECK("hydro kernels");
   CUCHK(cudaMemcpyAsync(d->iscal_h + IS_CRASH, d->iscal + IS_CRASH, sizeof(int), cudaMemcpyDeviceToHost, d->s));
   d->PhysicalTime += dt;
