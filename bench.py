@@ -184,6 +184,36 @@ def warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, steps, stream, barr
             "threshold": "eps * L1 residual of the previous-temperature start, as the plain solve"}
 
 
+def ensemble_phase(n=16, seed=0, ndt=2):
+    """A drawn ensemble of n gas + pebble + embryo disks of uneven sizes
+    (Nrad in {128 .. 512}, Nsec = 3 Nrad): after one DT with the omega
+    calibration, the autotuner times every schedule on one DT each, then
+    ndt DTs run with the fastest.  Aggregate cell-updates/s of the ensemble
+    against the same disks one after the other."""
+    from fargo_thorin_gb300.ensemble import Ensemble
+    ens = Ensemble.drawn(n, seed=seed)
+    ens.step(8)
+    tune = ens.tune(max_workers=16, ndt=1)
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    upd = 0
+    for _ in range(ndt):
+        ens.step(tune["workers"], tune["order_code"])
+        upd += sum(d.nr * d.ns * d.stats().substeps for d in ens.disks)
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    sizes = sorted(d.nr for d in ens.disks)
+    out = {"disks": n, "nrad": sizes, "cells": ens.cells, "workers": tune["workers"], "order": tune["order"],
+           "value": upd / sec, "unit": UNIT, "ms_per_dt": 1e3 * sec / ndt,
+           "sequential_ms_per_dt": tune["sequential_ms_per_dt"],
+           "speedup_vs_sequential": tune["sequential_ms_per_dt"] / (1e3 * sec / ndt),
+           "schedule": "one host worker thread per concurrent disk, per-disk streams, autotuned worker count and order",
+           "timing": "wall clock with a device synchronisation on both sides"}
+    ens.close()
+    return out
+
+
 def run_gpu(args):
     import torch
     ws, rank, local = dist_env()
@@ -272,6 +302,9 @@ def run_gpu(args):
     # the same DTs again with the learned SOR warm start (device-timed)
     learned = warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, args.steps, stream, barrier, t_plain,
                                sweeps / max(solves, 1))
+    ens = None
+    if rank == 0 and not args.no_ensemble:
+        ens = ensemble_phase()
 
     if rank == 0:
         peak, peak_kind = peaks()
@@ -319,6 +352,7 @@ def run_gpu(args):
                          "algorithmic_bytes_per_launch": bytes_pass, "avg_launch_ms": sor_avg_ms},
             "fp64_roofline": fp64,
             "sor_warm_start": learned,
+            "ensemble": ens,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
@@ -426,6 +460,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the 16-disk ensemble measurement")
     ap.add_argument("--profile", action="store_true",
                     help="run --steps DTs inside cuProfilerStart/Stop for ncu; prints no bench line")
     ap.add_argument("--grid", type=int, nargs=2, metavar=("NRAD", "NSEC"), default=(NR, NS),

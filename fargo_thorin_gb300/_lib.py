@@ -61,6 +61,11 @@ SIGNATURES = {
     "thorin_warmnet_adam": (C.c_int, [_P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float]),
     "thorin_gpu_warmstart": (C.c_int, [_P, _P, C.c_int, C.c_float]),
     "thorin_gpu_warmstart_stats": (C.c_int, [_P, _P]),
+    # ensembles (include/thorin_ensemble.h)
+    "thorin_ensemble_algogas": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int, C.c_int, C.c_int,
+                                          C.POINTER(C.c_int)]),
+    "thorin_ensemble_tune": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int), _D, _D]),
     "thorin_selftest_umma": (C.c_int, [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.POINTER(C.c_float)]),
     "thorin_planet_from_elements": (C.c_int, [C.POINTER(ThorinPlanets), C.c_int] + [C.c_float] * 9),
 }

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libthorin_gpu.so")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["kernels_hydro.cu", "kernels_aux.cu", "thorin_api.cu", "thorin_noalloc.cu", "thorin_selftest.cu",
-           "warmnet.cu"]
+           "warmnet.cu", "thorin_ensemble.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=true", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2"]
 

@@ -1214,9 +1214,11 @@ void hydro_matrix(const DevGrid &g, const double *rho, const double *T, const do
 
 static dim3 sor_grid_pass(const DevGrid &g)
 {
-  static int occ = 0;                              // resident k_sor_pass blocks per multiprocessor
+  static std::atomic<int> occ_cache{0};            // resident k_sor_pass blocks per multiprocessor
+  int occ = occ_cache.load();
   if (occ == 0) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sor_pass, SOR_BX, 0) != cudaSuccess || occ < 1) occ = 1;
+    occ_cache.store(occ);
   }
   const int half = g.ns / 2;
   const long long ntiles = (long long)((half + SOR_BX * SOR_CPT - 1) / (SOR_BX * SOR_CPT)) * (g.nr - 2);

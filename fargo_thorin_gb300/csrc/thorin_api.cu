@@ -40,7 +40,7 @@ int wn_dims(const thorin_warmnet *n, int *nr, int *ns);
 #define SQRT2PI_INV (1.0 / sqrt(2.0 * H_PI))
 
 thread_local std::string g_last_error;
-long long g_thorin_launches = 0;
+std::atomic<long long> g_thorin_launches{0};
 
 #define CUCHK(call)                                                                     \
   do {                                                                                  \
@@ -698,7 +698,7 @@ extern "C" int thorin_gpu_get_stats(thorin_disk *d, thorin_stats *s)
   *s = d->st;
   s->physical_time = d->PhysicalTime;
   s->omega_frame = d->OmegaFrame;
-  s->kernel_launches = g_thorin_launches;
+  s->kernel_launches = g_thorin_launches.load();
   return THORIN_OK;
 }
 
@@ -1812,7 +1812,7 @@ extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
   }
   d->st.substeps = nsub;
   d->st.crashed = d->iscal_h[IS_CRASH];
-  d->st.kernel_launches = g_thorin_launches;
+  d->st.kernel_launches = g_thorin_launches.load();
   return status;
 }
 
@@ -1844,6 +1844,9 @@ extern "C" int thorin_gpu_set_timing(thorin_disk *d, int on)
   d->st.sor_passes = 0;
   return THORIN_OK;
 }
+
+// cells of a disk's grid (the ensemble scheduler orders disks by it)
+long long thorin_disk_cells(const thorin_disk *d) { return (long long)d->nr * d->ns; }
 
 extern "C" int thorin_gpu_get_stream(thorin_disk *d, void **stream)
 {

@@ -1,5 +1,6 @@
 // thorin_kernels.cuh -- argument structs and host launchers of the kernels.
 #pragma once
+#include <atomic>
 #include "thorin_dev.cuh"
 
 #define MAXPL_DEV 8            // planets handled by the force kernel (per-thread arrays)
@@ -96,8 +97,9 @@ struct AccArgs {
 };
 
 // Number of kernels launched by this library (host-side bookkeeping; every
-// launcher below adds the launches it issues).
-extern long long g_thorin_launches;
+// launcher below adds the launches it issues).  Atomic: disks of an ensemble
+// are advanced from several host threads.
+extern std::atomic<long long> g_thorin_launches;
 
 // kernels_hydro.cu
 void hydro_substep1(const DevGrid &g, const double *rho, const double *vrad, const double *vtheta,

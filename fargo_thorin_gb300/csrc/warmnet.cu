@@ -699,10 +699,10 @@ static int conv_launch(thorin_warmnet *n, const bf16 *in, const bf16 *wk, const 
                        int B, int H, int W, cudaStream_t s)
 {
   constexpr int SM = conv_smem<CIN, N>();
-  static bool attr = false;
-  if (!attr) {
+  static std::atomic<bool> attr{false};
+  if (!attr.load()) {
     WNCHK(cudaFuncSetAttribute(k_wn_conv<CIN, N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
-    attr = true;
+    attr.store(true);
   }
   const long long tiles = ((long long)B * H * W + 127) / 128;
   const int grid = (int)(tiles < 2LL * n->nsm ? tiles : 2LL * n->nsm);
@@ -717,10 +717,10 @@ static int wgrad_launch(thorin_warmnet *n, int layer, const bf16 *in, const bf16
                         cudaStream_t s)
 {
   using S = WgradShape<CIN, N>;
-  static bool attr = false;
-  if (!attr) {
+  static std::atomic<bool> attr{false};
+  if (!attr.load()) {
     WNCHK(cudaFuncSetAttribute(k_wn_wgrad<CIN, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM));
-    attr = true;
+    attr.store(true);
   }
   const long long chunks = ((long long)B * H * W + 127) / 128;
   const int grid = (int)(chunks < n->part_blocks ? chunks : n->part_blocks);

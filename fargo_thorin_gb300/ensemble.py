@@ -1,0 +1,100 @@
+"""Ensembles of independent disks on one GPU (C ABI of include/thorin_ensemble.h).
+
+Every disk is a full `GpuDisk` with its own streams; one ensemble step
+advances each disk by one DT on a pool of host worker threads, so the
+kernels of several disks share the GPU.  `tune` picks the worker count and
+order by timing real DTs.
+
+The drawn ensemble is the batched workload of the BASELINE configs: gas +
+pebble disks with Nrad in {128, 192, 256, 384, 512} and Nsec = 3 Nrad, alpha
+log-uniform in [1e-4, 1e-2], Sigma0 scaled log-uniform in [0.3, 3], aspect
+ratio uniform in [0.03, 0.07] and an embryo of 0 to 20 Earth masses at r = 1.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .disk import GpuDisk
+
+SIZES = (128, 192, 256, 384, 512)
+EARTH = 3.0e-6
+GIVEN, LARGEST = 0, 1
+
+
+def draw(rng: np.random.Generator) -> dict:
+    return {"nrad": int(rng.choice(SIZES)), "alpha": float(10.0 ** rng.uniform(-4.0, -2.0)),
+            "sigma_scale": float(10.0 ** rng.uniform(np.log10(0.3), np.log10(3.0))),
+            "aspect": float(rng.uniform(0.03, 0.07)), "mplanet": float(rng.uniform(0.0, 20.0) * EARTH)}
+
+
+def make_disk(spec: dict, seed: int = 0, nsec: int | None = None, sor_eps: float = 1e-8):
+    """A pebble + embryo disk of the drawn parameters in the measured initial
+    state (perturbed Sigma, v_r = 0, Sigma_p = 0.01 Sigma, Stokes 0.1)."""
+    from . import workloads
+    nr = spec["nrad"]
+    ns = nsec if nsec is not None else 3 * nr
+    p = workloads.params_for("disk1", nr, ns, sor_eps=sor_eps, AlphaViscosity=spec["alpha"],
+                             AspectRatio=spec["aspect"], Sigma0=5.0e-4 * spec["sigma_scale"])
+    d = GpuDisk(p)
+    d.init_default()
+    st = workloads.perturbed_state(p, {"dens": d.get(0), "temper": d.get(8)}, seed=seed)
+    d.set(0, st["dens"]); d.set(1, st["vrad"]); d.set(3, st["energy"])
+    d.set(4, st["pebdens"]); d.set(7, st["pebsize"])
+    d.refresh(2)
+    row = list(workloads.PLANET1)
+    row[0] = spec["mplanet"]
+    return p, d, workloads.make_planets(p, [tuple(row)])
+
+
+class Ensemble:
+    """A set of disks advanced together."""
+
+    def __init__(self, specs: list, seed: int = 0):
+        self.L = _lib.load()
+        self.specs = list(specs)
+        built = [make_disk(s, seed=seed + k) for k, s in enumerate(self.specs)]
+        self.params = [b[0] for b in built]
+        self.disks = [b[1] for b in built]
+        self.systems = [b[2] for b in built]
+        self._arrays()
+
+    @classmethod
+    def drawn(cls, n: int, seed: int = 0) -> "Ensemble":
+        rng = np.random.default_rng(seed)
+        return cls([draw(rng) for _ in range(n)], seed=seed)
+
+    def _arrays(self):
+        n = len(self.disks)
+        self._dp = (C.c_void_p * n)(*[d.h.value for d in self.disks])
+        self._sp = (C.c_void_p * n)(*[C.cast(C.pointer(s), C.c_void_p).value for s in self.systems])
+
+    @property
+    def cells(self) -> int:
+        return sum(d.nr * d.ns for d in self.disks)
+
+    def step(self, workers: int = 1, order: int = LARGEST) -> list:
+        """One DT of every disk; returns the per-disk status codes."""
+        n = len(self.disks)
+        st = (C.c_int * n)()
+        rc = self.L.thorin_ensemble_algogas(self._dp, self._sp, n, workers, order, st)
+        _lib.check(rc, "thorin_ensemble_algogas")
+        return list(st)
+
+    def tune(self, max_workers: int = 16, ndt: int = 1) -> dict:
+        bw, bo = C.c_int(), C.c_int()
+        bms, sms = C.c_double(), C.c_double()
+        _lib.check(self.L.thorin_ensemble_tune(self._dp, self._sp, len(self.disks), max_workers, ndt, C.byref(bw),
+                                               C.byref(bo), C.byref(bms), C.byref(sms)), "thorin_ensemble_tune")
+        return {"workers": bw.value, "order": "largest first" if bo.value == LARGEST else "given",
+                "order_code": bo.value, "ms_per_dt": bms.value, "sequential_ms_per_dt": sms.value}
+
+    def substeps(self) -> int:
+        return sum(d.stats().substeps for d in self.disks)
+
+    def close(self):
+        for d in self.disks:
+            d.close()
+        self.disks = []
