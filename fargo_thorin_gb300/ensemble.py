@@ -30,14 +30,17 @@ def draw(rng: np.random.Generator) -> dict:
             "aspect": float(rng.uniform(0.03, 0.07)), "mplanet": float(rng.uniform(0.0, 20.0) * EARTH)}
 
 
-def make_disk(spec: dict, seed: int = 0, nsec: int | None = None, sor_eps: float = 1e-8):
+def make_disk(spec: dict, seed: int = 0, nsec: int | None = None, sor_eps: float = 1e-8, sor_maxiters: int = 0):
     """A pebble + embryo disk of the drawn parameters in the measured initial
-    state (perturbed Sigma, v_r = 0, Sigma_p = 0.01 Sigma, Stokes 0.1)."""
+    state (perturbed Sigma, v_r = 0, Sigma_p = 0.01 Sigma, Stokes 0.1).
+    sor_maxiters > 0 caps the SOR iterations (the reference's cap is 100000)."""
     from . import workloads
     nr = spec["nrad"]
     ns = nsec if nsec is not None else 3 * nr
     p = workloads.params_for("disk1", nr, ns, sor_eps=sor_eps, AlphaViscosity=spec["alpha"],
                              AspectRatio=spec["aspect"], Sigma0=5.0e-4 * spec["sigma_scale"])
+    if sor_maxiters > 0:
+        p.sor_maxiters = sor_maxiters
     d = GpuDisk(p)
     d.init_default()
     st = workloads.perturbed_state(p, {"dens": d.get(0), "temper": d.get(8)}, seed=seed)
@@ -52,19 +55,45 @@ def make_disk(spec: dict, seed: int = 0, nsec: int | None = None, sor_eps: float
 class Ensemble:
     """A set of disks advanced together."""
 
-    def __init__(self, specs: list, seed: int = 0):
+    def __init__(self, specs: list, seed: int = 0, sor_maxiters: int = 0):
         self.L = _lib.load()
         self.specs = list(specs)
-        built = [make_disk(s, seed=seed + k) for k, s in enumerate(self.specs)]
+        built = [make_disk(s, seed=seed + k, sor_maxiters=sor_maxiters) for k, s in enumerate(self.specs)]
         self.params = [b[0] for b in built]
         self.disks = [b[1] for b in built]
         self.systems = [b[2] for b in built]
         self._arrays()
 
     @classmethod
-    def drawn(cls, n: int, seed: int = 0) -> "Ensemble":
+    def drawn(cls, n: int, seed: int = 0, sor_maxiters: int = 2000, tries: int = 8) -> "Ensemble":
+        """n drawn disks, each advanced by its first DT (with the SOR omega
+        calibration).  Some draws are not viable on the coarser grids: the
+        reference's own solver fails on them (no omega converges, or the
+        temperature turns NaN).  Those are replaced by fresh draws.  The cap
+        on SOR iterations makes such a failure quick."""
         rng = np.random.default_rng(seed)
-        return cls([draw(rng) for _ in range(n)], seed=seed)
+        specs, kept = [], []
+        k = 0
+        while len(kept) < n:
+            if k >= n * tries:
+                raise RuntimeError("ensemble: too many drawn disks failed their first DT")
+            spec = draw(rng)
+            p, d, s = make_disk(spec, seed=seed + k, sor_maxiters=sor_maxiters)
+            k += 1
+            rc = d.L.thorin_gpu_algogas(d.h, C.byref(s))
+            if rc == 0 and np.isfinite(d.get(8)).all():
+                specs.append(spec)
+                kept.append((p, d, s))
+            else:
+                d.close()
+        ens = cls.__new__(cls)
+        ens.L = _lib.load()
+        ens.specs = specs
+        ens.params = [b[0] for b in kept]
+        ens.disks = [b[1] for b in kept]
+        ens.systems = [b[2] for b in kept]
+        ens._arrays()
+        return ens
 
     def _arrays(self):
         n = len(self.disks)

@@ -32,7 +32,7 @@ def test_ensemble_rejects_bad_arguments():
 
 SPECS = [{"nrad": 32, "alpha": 1e-3, "sigma_scale": 1.0, "aspect": 0.05, "mplanet": 3e-5},
          {"nrad": 48, "alpha": 3e-4, "sigma_scale": 2.0, "aspect": 0.04, "mplanet": 1e-5},
-         {"nrad": 64, "alpha": 5e-3, "sigma_scale": 0.5, "aspect": 0.06, "mplanet": 0.0},
+         {"nrad": 64, "alpha": 1e-3, "sigma_scale": 1.0, "aspect": 0.05, "mplanet": 0.0},
          {"nrad": 40, "alpha": 1e-4, "sigma_scale": 1.5, "aspect": 0.07, "mplanet": 6e-5}]
 
 
