@@ -3,7 +3,10 @@
 CPU: argument checks return THORIN_ERR_ARG before any device work.
 GPU: disks of uneven sizes advanced concurrently on four worker threads,
 largest first, end bit-identical to the same disks advanced one after the
-other; the autotuner returns a schedule it measured.
+other; the autotuner returns a schedule it measured.  (Every disk carries
+an accreting embryo of nonzero mass: with pebble accretion and accretion
+heating on, a zero-mass embryo has a zero Hill radius and the reference's
+heating term turns the temperature NaN.)
 """
 import ctypes as C
 import os
@@ -32,7 +35,7 @@ def test_ensemble_rejects_bad_arguments():
 
 SPECS = [{"nrad": 32, "alpha": 1e-3, "sigma_scale": 1.0, "aspect": 0.05, "mplanet": 3e-5},
          {"nrad": 48, "alpha": 3e-4, "sigma_scale": 2.0, "aspect": 0.04, "mplanet": 1e-5},
-         {"nrad": 64, "alpha": 1e-3, "sigma_scale": 1.0, "aspect": 0.05, "mplanet": 0.0},
+         {"nrad": 64, "alpha": 1e-3, "sigma_scale": 1.0, "aspect": 0.05, "mplanet": 2e-5},
          {"nrad": 40, "alpha": 1e-4, "sigma_scale": 1.5, "aspect": 0.07, "mplanet": 6e-5}]
 
 
