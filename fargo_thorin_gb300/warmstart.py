@@ -231,9 +231,23 @@ if __name__ == "__main__":
     ap.add_argument("--init", default=None, help="start from this parameter file")
     ap.add_argument("--out", default=None, help="write the trained parameters here (.npy)")
     ap.add_argument("--eval-dts", type=int, default=2)
+    ap.add_argument("--forward", type=int, default=0,
+                    help="only time this many forward passes on random inputs (no training, no evaluation)")
     a = ap.parse_args()
     t0 = time.time()
     net = WarmNet(a.nrad, a.nsec, params=WarmNet.load_params(a.init) if a.init else None)
+    if a.forward > 0:
+        rng = np.random.default_rng(0)
+        x = np.zeros((1, a.nrad, a.nsec, INPUTS), np.float32)
+        x[..., :6] = rng.uniform(-1.0, 1.0, (1, a.nrad, a.nsec, 6))
+        bits = (np.ascontiguousarray(x).view(np.uint32) >> 16).astype(np.uint16)
+        net.forward(bits)
+        t1 = time.time()
+        for _ in range(a.forward):
+            net.forward(bits)
+        print(f"{a.forward} forward passes of {a.nrad}x{a.nsec} in {time.time() - t1:.3f} s "
+              f"(host copies included)", flush=True)
+        raise SystemExit(0)
     if a.disks > 0:
         train(net, a.disks, a.steps, lr=a.lr, seed=a.seed, lr_final=a.lr_final, log=print)
         print(f"trained in {time.time() - t0:.1f} s", flush=True)
