@@ -62,13 +62,20 @@ struct ConvArgs {
   int *err;
 };
 
+// The nine taps are staged and multiplied in three phases of three taps, so
+// that the operand tile is a third of the full im2col tile and several CTAs
+// share an SM (their staging overlaps each other's MMAs).
+constexpr int WN_TAPS_PER_PHASE = 3;
+
 template <int CIN, int N>
-constexpr int conv_smem() { return 9 * CIN * 128 * 2 + 9 * CIN * N * 2 + 128 + 128; }
+constexpr int conv_smem() { return WN_TAPS_PER_PHASE * CIN * 128 * 2 + 9 * CIN * N * 2 + 128 + 128; }
 
 template <int CIN, int N, int MODE>
 __global__ void __launch_bounds__(128) k_wn_conv(ConvArgs a)
 {
-  constexpr int K = 9 * CIN, KG = K / 8, A_BYTES = KG * 128 * 16, B_BYTES = KG * N * 16;
+  constexpr int K = 9 * CIN, KG = K / 8, B_BYTES = KG * N * 16;
+  constexpr int TP = WN_TAPS_PER_PHASE, KP = TP * CIN, A_BYTES = (KP / 8) * 128 * 16;
+  static_assert(9 % TP == 0 && KP % 16 == 0, "phases of whole MMA k-steps");
   constexpr uint32_t IDESC = umma::idesc_bf16(128, N);
   extern __shared__ unsigned char smem_raw[];
   unsigned char *sA = align128(smem_raw), *sB = sA + A_BYTES;
@@ -105,34 +112,38 @@ __global__ void __launch_bounds__(128) k_wn_conv(ConvArgs a)
       i = (int)(rem / a.W);
       j = (int)(rem - (long long)i * a.W);
     }
+#pragma unroll 1
+    for (int ph = 0; ph < 9 / TP && ok; ph++) {
 #pragma unroll
-    for (int t = 0; t < 9; t++) {
-      const int ii = i + t / 3 - 1;
-      int jj = j + t % 3 - 1;
-      jj = jj < 0 ? jj + a.W : (jj >= a.W ? jj - a.W : jj);
-      const bool v = live && ii >= 0 && ii < a.H;
-      const uint4 *src = (const uint4 *)(a.in + (((long long)b * a.H + (v ? ii : 0)) * a.W + jj) * CIN);
+      for (int tt = 0; tt < TP; tt++) {
+        const int t = ph * TP + tt;
+        const int ii = i + t / 3 - 1;
+        int jj = j + t % 3 - 1;
+        jj = jj < 0 ? jj + a.W : (jj >= a.W ? jj - a.W : jj);
+        const bool v = live && ii >= 0 && ii < a.H;
+        const uint4 *src = (const uint4 *)(a.in + (((long long)b * a.H + (v ? ii : 0)) * a.W + jj) * CIN);
 #pragma unroll
-      for (int c8 = 0; c8 < CIN / 8; c8++) {
-        const uint4 val = v ? src[c8] : make_uint4(0u, 0u, 0u, 0u);
-        *(uint4 *)(sA + (t * (CIN / 8) + c8) * 2048 + tid * 16) = val;
+        for (int c8 = 0; c8 < CIN / 8; c8++) {
+          const uint4 val = v ? src[c8] : make_uint4(0u, 0u, 0u, 0u);
+          *(uint4 *)(sA + (tt * (CIN / 8) + c8) * 2048 + tid * 16) = val;
+        }
       }
-    }
-    umma::fence_smem_async();
-    __syncthreads();
-    if (tid == 0) {
-      umma::fence_after_sync();
-      const uint32_t a0 = umma::smem_addr(sA), b0 = umma::smem_addr(sB);
+      umma::fence_smem_async();
+      __syncthreads();
+      if (tid == 0) {
+        umma::fence_after_sync();
+        const uint32_t a0 = umma::smem_addr(sA), b0 = umma::smem_addr(sB);
 #pragma unroll
-      for (int ks = 0; ks < K / 16; ks++)
-        umma::mma_bf16(tmem, umma::desc(a0 + ks * 4096, 2048, 128), umma::desc(b0 + ks * 2 * N * 16, N * 16, 128), IDESC,
-                       ks > 0);
-      umma::mma_commit(bar);
+        for (int ks = 0; ks < KP / 16; ks++)
+          umma::mma_bf16(tmem, umma::desc(a0 + ks * 4096, 2048, 128),
+                         umma::desc(b0 + (ph * (KP / 16) + ks) * 2 * N * 16, N * 16, 128), IDESC, ph > 0 || ks > 0);
+        umma::mma_commit(bar);
+      }
+      __syncwarp();
+      ok = umma::mbar_wait(bar, phase, WN_WAIT);      // the tile is free again once the MMAs are done
+      ok = __syncthreads_and(ok);
+      phase ^= 1u;
     }
-    __syncwarp();
-    ok = umma::mbar_wait(bar, phase, WN_WAIT);
-    ok = __syncthreads_and(ok);
-    phase ^= 1u;
     if (!ok) break;
     umma::fence_after_sync();
     float v[N];
@@ -353,40 +364,54 @@ __global__ void k_wn_pack(const float *__restrict__ w, int cin, int cout, int ci
   }
 }
 
-// 2x2 average pooling, bf16 [B][H][W][32] -> [B][H/2][W/2][32]
+// 2x2 average pooling, bf16 [B][H][W][32] -> [B][H/2][W/2][32]; one thread
+// per 8 channels of an output cell
 __global__ void k_wn_pool(const bf16 *__restrict__ a, bf16 *__restrict__ p, int B, int H, int W)
 {
-  const long long n = (long long)B * (H / 2) * (W / 2) * WN_C;
+  const long long n = (long long)B * (H / 2) * (W / 2) * (WN_C / 8);
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= n) return;
-  const int c = (int)(idx % WN_C);
-  long long q = idx / WN_C;
+  const int c8 = (int)(idx % (WN_C / 8));
+  long long q = idx / (WN_C / 8);
   const int j = (int)(q % (W / 2));
   q /= W / 2;
   const int i = (int)(q % (H / 2));
   const int b = (int)(q / (H / 2));
-  const bf16 *s = a + (((long long)b * H + 2 * i) * W + 2 * j) * WN_C + c;
-  const float v = (__bfloat162float(s[0]) + __bfloat162float(s[WN_C])) +
-                  (__bfloat162float(s[(long long)W * WN_C]) + __bfloat162float(s[(long long)W * WN_C + WN_C]));
-  p[idx] = __float2bfloat16_rn(0.25f * v);
+  const bf16 *s = a + (((long long)b * H + 2 * i) * W + 2 * j) * WN_C + 8 * c8;
+  const uint4 u0 = *(const uint4 *)s, u1 = *(const uint4 *)(s + WN_C), u2 = *(const uint4 *)(s + (long long)W * WN_C),
+              u3 = *(const uint4 *)(s + (long long)W * WN_C + WN_C);
+  const bf16 *h0 = (const bf16 *)&u0, *h1 = (const bf16 *)&u1, *h2 = (const bf16 *)&u2, *h3 = (const bf16 *)&u3;
+  uint4 out;
+  bf16 *ho = (bf16 *)&out;
+#pragma unroll
+  for (int e = 0; e < 8; e++)
+    ho[e] = __float2bfloat16_rn(0.25f * ((__bfloat162float(h0[e]) + __bfloat162float(h1[e])) +
+                                         (__bfloat162float(h2[e]) + __bfloat162float(h3[e]))));
+  *(uint4 *)(p + idx * 8) = out;
 }
 
-// u = up2(low) + skip, bf16 at the finer level [B][H][W][32]
+// u = up2(low) + skip, bf16 at the finer level [B][H][W][32]; one thread per
+// 8 channels of a cell
 __global__ void k_wn_upadd(const bf16 *__restrict__ low, const bf16 *__restrict__ skip, bf16 *__restrict__ u, int B,
                            int H, int W)
 {
-  const long long n = (long long)B * H * W * WN_C;
+  const long long n = (long long)B * H * W * (WN_C / 8);
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= n) return;
-  const int c = (int)(idx % WN_C);
-  long long q = idx / WN_C;
+  const int c8 = (int)(idx % (WN_C / 8));
+  long long q = idx / (WN_C / 8);
   const int j = (int)(q % W);
   q /= W;
   const int i = (int)(q % H);
   const int b = (int)(q / H);
-  const float v = __bfloat162float(low[(((long long)b * (H / 2) + i / 2) * (W / 2) + j / 2) * WN_C + c]) +
-                  __bfloat162float(skip[idx]);
-  u[idx] = __float2bfloat16_rn(v);
+  const uint4 lo = *(const uint4 *)(low + (((long long)b * (H / 2) + i / 2) * (W / 2) + j / 2) * WN_C + 8 * c8);
+  const uint4 sk = *(const uint4 *)(skip + idx * 8);
+  const bf16 *hl = (const bf16 *)&lo, *hs = (const bf16 *)&sk;
+  uint4 out;
+  bf16 *ho = (bf16 *)&out;
+#pragma unroll
+  for (int e = 0; e < 8; e++) ho[e] = __float2bfloat16_rn(__bfloat162float(hl[e]) + __bfloat162float(hs[e]));
+  *(uint4 *)(u + idx * 8) = out;
 }
 
 // bf16 gradient = g * (act > 0)
@@ -699,13 +724,17 @@ static int conv_launch(thorin_warmnet *n, const bf16 *in, const bf16 *wk, const 
                        int B, int H, int W, cudaStream_t s)
 {
   constexpr int SM = conv_smem<CIN, N>();
-  static std::atomic<bool> attr{false};
-  if (!attr.load()) {
+  static std::atomic<int> occ_cache{0};            // resident CTAs per SM at this shared-memory size
+  int occ = occ_cache.load();
+  if (occ == 0) {
     WNCHK(cudaFuncSetAttribute(k_wn_conv<CIN, N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
-    attr.store(true);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_wn_conv<CIN, N, MODE>, 128, SM) != cudaSuccess || occ < 1)
+      occ = 1;
+    occ_cache.store(occ);
   }
   const long long tiles = ((long long)B * H * W + 127) / 128;
-  const int grid = (int)(tiles < 2LL * n->nsm ? tiles : 2LL * n->nsm);
+  const long long wave = (long long)occ * n->nsm;     // persistent CTAs: one wave over the tiles
+  const int grid = (int)(tiles < wave ? tiles : wave);
   ConvArgs a{in, wk, bias, coutr, out, B, H, W, n->err};
   k_wn_conv<CIN, N, MODE><<<grid, 128, SM, s>>>(a);
   g_thorin_launches++;
@@ -757,11 +786,11 @@ static int wn_forward(thorin_warmnet *n, int B, cudaStream_t s)
   int h[4] = {H, H / 2, H / 4, H / 8}, w[4] = {W, W / 2, W / 4, W / 8};
   bf16 **A = n->act;
   auto pool = [&](const bf16 *a, bf16 *p, int lv) {
-    k_wn_pool<<<nblk((long long)B * h[lv + 1] * w[lv + 1] * WN_C), 256, 0, s>>>(a, p, B, h[lv], w[lv]);
+    k_wn_pool<<<nblk((long long)B * h[lv + 1] * w[lv + 1] * (WN_C / 8)), 256, 0, s>>>(a, p, B, h[lv], w[lv]);
     g_thorin_launches++;
   };
   auto upadd = [&](const bf16 *low, const bf16 *skip, bf16 *u, int lv) {
-    k_wn_upadd<<<nblk((long long)B * h[lv] * w[lv] * WN_C), 256, 0, s>>>(low, skip, u, B, h[lv], w[lv]);
+    k_wn_upadd<<<nblk((long long)B * h[lv] * w[lv] * (WN_C / 8)), 256, 0, s>>>(low, skip, u, B, h[lv], w[lv]);
     g_thorin_launches++;
   };
   RCHK_WN(conv_launch<16, 32, 0>(n, n->x, n->wk[0], bias_of(n, 0), 32, A[A0], B, h[0], w[0], s));
