@@ -62,10 +62,10 @@ struct ConvArgs {
   int *err;
 };
 
-// The nine taps are staged and multiplied in three phases of three taps, so
-// that the operand tile is a third of the full im2col tile and several CTAs
-// share an SM (their staging overlaps each other's MMAs).
-constexpr int WN_TAPS_PER_PHASE = 3;
+// Taps staged and multiplied per phase (9: the whole im2col tile at once).
+// Three phases of three taps let more CTAs share an SM but measured twice
+// as slow: each phase adds an MMA completion round trip to the tile.
+constexpr int WN_TAPS_PER_PHASE = 9;
 
 template <int CIN, int N>
 constexpr int conv_smem() { return WN_TAPS_PER_PHASE * CIN * 128 * 2 + 9 * CIN * N * 2 + 128 + 128; }
