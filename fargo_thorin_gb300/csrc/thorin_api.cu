@@ -15,10 +15,12 @@
 
 // learned SOR warm start (warmnet.cu)
 int wn_sor_predict(thorin_warmnet *n, int nr, int ns, double *T, const double *ml, const double *mlip,
-                   const double *mlim, const double *mljp, const double *mljm, const double *rhs, cudaStream_t s);
+                   const double *mlim, const double *mljp, const double *mljm, const double *rhs, const double *prev,
+                   cudaStream_t s);
 int wn_sor_train(thorin_warmnet *n, int nr, int ns, const double *tk, const double *tconv, const double *ml,
                  const double *mlip, const double *mlim, const double *mljp, const double *mljm, const double *rhs,
-                 float lr, double *scratch, cudaStream_t s);
+                 const double *prev, float lr, double *scratch, cudaStream_t s);
+int wn_record_update(int nr, int ns, const double *tconv, const double *tstart, double *prev, cudaStream_t s);
 int wn_last_loss(thorin_warmnet *n, double *loss);
 int wn_dims(const thorin_warmnet *n, int *nr, int *ns);
 
@@ -158,6 +160,7 @@ struct thorin_disk {
   int ws_mode = THORIN_WS_OFF;
   float ws_lr = 0.f;
   thorin_ws_stats ws_st = {0, 0, 0.0, 0.0, 0.0};
+  double *ws_prev = nullptr;     // the previous solve's update T_conv - T_start (network input)
   double heatsrc[THORIN_MAXPLANETS];
   int heatsrc_index[THORIN_MAXPLANETS], heatsrc_max;
   double gm1, gg1, drin, drout, invdphi, lr01, lr12, taueff_c, tirr4fac, rstar;
@@ -523,6 +526,10 @@ extern "C" int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode,
       g_last_error = "warmstart: the network's grid differs from the disk's";
       return THORIN_ERR_ARG;
     }
+  }
+  if (mode != THORIN_WS_OFF && !d->ws_prev) {
+    RCHK(dalloc(d, (void **)&d->ws_prev, (size_t)d->nr * d->ns * sizeof(double)));
+    CUCHK(cudaMemsetAsync(d->ws_prev, 0, (size_t)d->nr * d->ns * sizeof(double), d->s));
   }
   d->ws_net = mode == THORIN_WS_OFF ? nullptr : n;
   d->ws_mode = mode;
@@ -1430,7 +1437,11 @@ static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *ca
   hydro_sor_resid0(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, omega, d->sor, d->s);
   KCHECK("SOR residual kernel");
   if (learned && d->ws_net && d->ws_mode == THORIN_WS_PREDICT) {
-    RCHK(wn_sor_predict(d->ws_net, d->nr, d->ns, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->s));
+    // keep the start (for the update record after the solve), then move it
+    CUCHK(cudaMemcpyAsync(d->tbackup, d->temper, (size_t)d->nr * d->ns * sizeof(double), cudaMemcpyDeviceToDevice,
+                          d->s));
+    RCHK(wn_sor_predict(d->ws_net, d->nr, d->ns, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs,
+                        d->ws_prev, d->s));
     d->ws_st.predictions++;
   }
   int first = 1, chunk = hint > 0 ? hint : 4;
@@ -1550,9 +1561,11 @@ static int energy_step(thorin_disk *d, double dt)
   if (train) {
     // fit the network to this solve; energy_new is free until the energy is formed below
     RCHK(wn_sor_train(d->ws_net, d->nr, d->ns, d->tbackup, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm,
-                      d->rhs, d->ws_lr, d->energy_new, d->s));
+                      d->rhs, d->ws_prev, d->ws_lr, d->energy_new, d->s));
     d->ws_st.train_steps++;
   }
+  if (d->ws_net && d->ws_prev)        // this solve's update, an input of the next prediction
+    RCHK(wn_record_update(d->nr, d->ns, d->temper, d->tbackup, d->ws_prev, d->s));
   d->st.sor_calls++;
   d->st.sor_sweeps += Niter;
   d->st.sor_last_niter = Niter;

@@ -24,7 +24,7 @@ namespace {
 
 constexpr int WN_C = 32;          // feature channels
 constexpr int WN_NL = 8;          // layers: e0 e1 e2 e3 d2 d1 d0 out
-constexpr int WN_NIN = 6;         // input channels used
+constexpr int WN_NIN = 7;         // input channels used
 constexpr float WN_YSCALE = 32.f; // output unit, in residual scales
 constexpr long long WN_WAIT = 1LL << 26;  // mbarrier polls before giving up
 
@@ -549,15 +549,18 @@ __global__ void k_wn_scale(int nr, int ns, const double *__restrict__ T, SorSys 
   if (threadIdx.x == 0) part[gridDim.x + blockIdx.x] = sr;
 }
 
-// network input x[l][16] and the Jacobi step jac = -r / Ml
+// network input x[l][16] and the Jacobi step jac = -r / Ml.  Channels: the
+// Jacobi-scaled residual over its mean (clipped), the four neighbour weights
+// -M/Ml, the stiffness -log(1 - sum w) / 4, and the previous solve's update
+// in the output's units (clipped; zero before the first solve)
 __global__ void k_wn_features(int nr, int ns, const double *__restrict__ T, SorSys m, const double *__restrict__ scale,
-                              bf16 *__restrict__ x, double *__restrict__ jac)
+                              const double *__restrict__ prev, bf16 *__restrict__ x, double *__restrict__ jac)
 {
   const long long n = (long long)nr * ns;
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= n) return;
   const int i = (int)(q / ns), j = (int)(q % ns), l = (int)q;
-  float f[WN_NIN] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float f[WN_NIN] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   double jl = 0.0;
   if (i >= 1 && i <= nr - 2) {
     const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
@@ -570,6 +573,7 @@ __global__ void k_wn_features(int nr, int ns, const double *__restrict__ T, SorS
     const double w1 = -m.mlip[l] / ml, w2 = -m.mlim[l] / ml, w3 = -m.mljp[l] / ml, w4 = -m.mljm[l] / ml;
     f[1] = (float)w1; f[2] = (float)w2; f[3] = (float)w3; f[4] = (float)w4;
     f[5] = (float)(-log(fmax(1.0 - (((w1 + w2) + w3) + w4), 1e-6)) * 0.25);
+    if (prev && s > 0.0) f[6] = (float)fmin(fmax(prev[l] / (s * (double)WN_YSCALE), -16.0), 16.0);
   }
   jac[l] = jl;
   uint4 z[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
@@ -675,6 +679,14 @@ __global__ void k_wn_res_grad(int nr, int ns, const float *__restrict__ rs, SorS
 __global__ void k_wn_total(double *dscal, float wres, float wsup)
 {
   dscal[0] = (double)wres * dscal[4] + (double)wsup * dscal[5];
+}
+
+// the solve's update tconv - tstart (the previous-update input of the next solve)
+__global__ void k_wn_record(long long n, const double *__restrict__ tconv, const double *__restrict__ tstart,
+                            double *__restrict__ prev)
+{
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q < n) prev[q] = tconv[q] - tstart[q];
 }
 
 inline unsigned nblk(long long n, int bs = 256) { return (unsigned)((n + bs - 1) / bs); }
@@ -900,7 +912,8 @@ static int wn_check_err(thorin_warmnet *n)
 
 // T (start of the solve, or the current iterate) -> T + jac + network
 int wn_sor_predict(thorin_warmnet *n, int nr, int ns, double *T, const double *ml, const double *mlip,
-                   const double *mlim, const double *mljp, const double *mljm, const double *rhs, cudaStream_t s)
+                   const double *mlim, const double *mljp, const double *mljm, const double *rhs, const double *prev,
+                   cudaStream_t s)
 {
   // dscal: [2] mean |r/Ml| of the start, [3] mean |r|, [4] residual loss,
   // [5] supervised loss, [0] total loss; partials from dscal + 8
@@ -909,7 +922,7 @@ int wn_sor_predict(thorin_warmnet *n, int nr, int ns, double *T, const double *m
   const int sb = 2 * n->nsm;
   k_wn_scale<<<sb, 256, 0, s>>>(nr, ns, T, m, part);
   k_wn_sum<<<1, 32, 0, s>>>(part, sb, 1.0 / ((double)(nr - 2) * ns), n->dscal + 2);
-  k_wn_features<<<nblk((long long)nr * ns), 256, 0, s>>>(nr, ns, T, m, n->dscal + 2, n->x, n->jac);
+  k_wn_features<<<nblk((long long)nr * ns), 256, 0, s>>>(nr, ns, T, m, n->dscal + 2, prev, n->x, n->jac);
   g_thorin_launches += 3;
   RCHK_WN(wn_forward(n, 1, s));
   k_wn_apply<<<nblk((long long)(nr - 2) * ns), 256, 0, s>>>(nr, ns, T, n->jac, n->y, n->dscal + 2);
@@ -924,7 +937,7 @@ int wn_sor_predict(thorin_warmnet *n, int nr, int ns, double *T, const double *m
 // beyond the Jacobi step in the same units
 int wn_sor_train(thorin_warmnet *n, int nr, int ns, const double *tk, const double *tconv, const double *ml,
                  const double *mlip, const double *mlim, const double *mljp, const double *mljm, const double *rhs,
-                 float lr, double *scratch, cudaStream_t s)
+                 const double *prev, float lr, double *scratch, cudaStream_t s)
 {
   constexpr float WRES = 1.0f, WSUP = 0.1f;
   SorSys m{ml, mlip, mlim, mljp, mljm, rhs};
@@ -935,7 +948,7 @@ int wn_sor_train(thorin_warmnet *n, int nr, int ns, const double *tk, const doub
   k_wn_scale<<<sb, 256, 0, s>>>(nr, ns, tk, m, part);
   k_wn_sum<<<1, 32, 0, s>>>(part, sb, inv_n, n->dscal + 2);
   k_wn_sum<<<1, 32, 0, s>>>(part + sb, sb, inv_n, n->dscal + 3);
-  k_wn_features<<<nblk(cells), 256, 0, s>>>(nr, ns, tk, m, n->dscal + 2, n->x, n->jac);
+  k_wn_features<<<nblk(cells), 256, 0, s>>>(nr, ns, tk, m, n->dscal + 2, prev, n->x, n->jac);
   k_wn_target<<<nblk(cells), 256, 0, s>>>(nr, ns, tconv, tk, n->jac, n->dscal + 2, n->tgt);
   g_thorin_launches += 5;
   RCHK_WN(wn_forward(n, 1, s));
@@ -952,6 +965,16 @@ int wn_sor_train(thorin_warmnet *n, int nr, int ns, const double *tk, const doub
   RCHK_WN(wn_adam(n, lr, 0.9f, 0.999f, 1e-8f, 1.0f, s));
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? THORIN_OK : wn_fail("training kernels", e);
+}
+
+// prev = tconv - tstart over nr x ns cells
+int wn_record_update(int nr, int ns, const double *tconv, const double *tstart, double *prev, cudaStream_t s)
+{
+  const long long cells = (long long)nr * ns;
+  k_wn_record<<<nblk(cells), 256, 0, s>>>(cells, tconv, tstart, prev);
+  g_thorin_launches++;
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? THORIN_OK : wn_fail("record kernel", e);
 }
 
 // total, residual and supervised loss of the last training step

@@ -23,12 +23,12 @@ import numpy as np
 
 from . import _lib
 
-NPARAMS = 57537
+NPARAMS = 57825
 INPUTS = 16
 OFF, PREDICT, TRAIN = 0, 1, 2
 EARTH = 3.0e-6                         # Earth mass in solar masses
 # (cin, cout) per layer: e0 e1 e2 e3 d2 d1 d0 out
-LAYERS = [(6, 32)] + [(32, 32)] * 6 + [(32, 1)]
+LAYERS = [(7, 32)] + [(32, 32)] * 6 + [(32, 1)]
 
 
 def init_params(seed: int = 0) -> np.ndarray:
@@ -239,7 +239,7 @@ if __name__ == "__main__":
     if a.forward > 0:
         rng = np.random.default_rng(0)
         x = np.zeros((1, a.nrad, a.nsec, INPUTS), np.float32)
-        x[..., :6] = rng.uniform(-1.0, 1.0, (1, a.nrad, a.nsec, 6))
+        x[..., :7] = rng.uniform(-1.0, 1.0, (1, a.nrad, a.nsec, 7))
         bits = (np.ascontiguousarray(x).view(np.uint32) >> 16).astype(np.uint16)
         net.forward(bits)
         t1 = time.time()

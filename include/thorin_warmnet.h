@@ -14,15 +14,17 @@
  * Network (fixed): 4 levels, 3x3 convolutions periodic in azimuth and
  * zero-padded in radius, 32 channels, ReLU, 2x2 average pooling down and
  * nearest-neighbour upsampling with additive skips up, one output channel;
- * 57,537 FP32 master parameters, BF16 weights and activations, FP32
- * accumulation on the tensor cores.  Inputs per cell (6 of 16 channels):
+ * 57,825 FP32 master parameters, BF16 weights and activations, FP32
+ * accumulation on the tensor cores.  Inputs per cell (7 of 16 channels):
  * the Jacobi-scaled SOR residual of the start temperature (divided by its
  * grid mean and clipped to +-16), the four neighbour weights -M/Ml of the
- * SOR matrix and the local stiffness -log(1 - sum of the weights) / 4.
- * These carry Sigma, T_old, the heating, the opacity and the dt-scaled
- * diffusion coefficients through the matrix and right-hand side that they
- * build.  Output: the update beyond one Jacobi step, in units of 32 times
- * the residual scale.
+ * SOR matrix, the local stiffness -log(1 - sum of the weights) / 4, and the
+ * previous solve's update T_conv - T_start in the output's units (clipped;
+ * zero before the disk's first solve with the network attached).  These
+ * carry Sigma, T_old, the heating, the opacity and the dt-scaled diffusion
+ * coefficients through the matrix and right-hand side that they build.
+ * Output: the update beyond one Jacobi step, in units of 32 times the
+ * residual scale.
  */
 #ifndef THORIN_WARMNET_H
 #define THORIN_WARMNET_H
@@ -34,8 +36,8 @@
 extern "C" {
 #endif
 
-#define THORIN_WN_INPUTS   16    /* input channels per cell (6 used, rest zero) */
-#define THORIN_WN_NPARAMS  57537 /* FP32 parameters */
+#define THORIN_WN_INPUTS   16    /* input channels per cell (7 used, rest zero) */
+#define THORIN_WN_NPARAMS  57825 /* FP32 parameters */
 
 #define THORIN_WS_OFF      0     /* plain SOR (the reference's method)          */
 #define THORIN_WS_PREDICT  1     /* warm-start every SOR solve from the network */

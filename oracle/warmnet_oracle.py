@@ -18,7 +18,7 @@ from __future__ import annotations
 import numpy as np
 
 C = 32
-NIN = 6
+NIN = 7
 INPUTS = 16
 # (cin, cout) per layer: e0 e1 e2 e3 d2 d1 d0 out
 LAYERS = [(NIN, C)] + [(C, C)] * 6 + [(C, 1)]

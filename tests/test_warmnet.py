@@ -41,7 +41,7 @@ def _inputs(seed, B, H, W):
 
 
 def test_param_count_and_init():
-    assert WO.NPARAMS == WS.NPARAMS == 57537
+    assert WO.NPARAMS == WS.NPARAMS == 57825
     p = WS.init_params(3)
     assert p.dtype == np.float32 and p.size == WS.NPARAMS
     assert np.all(p[WO.OFFSETS[7]:] == 0.0)            # output layer starts at zero
