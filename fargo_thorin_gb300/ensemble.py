@@ -5,8 +5,8 @@ advances each disk by one DT on a pool of host worker threads, so the
 kernels of several disks share the GPU.  `tune` picks the worker count and
 order by timing real DTs.
 
-The drawn ensemble is the batched workload of the BASELINE configs: gas +
-pebble disks with Nrad in {128, 192, 256, 384, 512} and Nsec = 3 Nrad, alpha
+The drawn ensemble is the batched many-disk workload: gas + pebble disks
+with Nrad in {128, 192, 256, 384, 512} and Nsec = 3 Nrad, alpha
 log-uniform in [1e-4, 1e-2], Sigma0 scaled log-uniform in [0.3, 3], aspect
 ratio uniform in [0.03, 0.07] and an embryo of 0 to 20 Earth masses at r = 1.
 """
