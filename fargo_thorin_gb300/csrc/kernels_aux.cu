@@ -256,15 +256,15 @@ __global__ void k_damp_gas(DevGrid g, double *__restrict__ vrad, double *__restr
   const int l = j + i * ns;
   const double lambda = g.r.WaveKiller[i] * dt;
   const double vrad0 = damp_flux ? vr0r[i] : 0.0;
-  vrad[l] = (vrad[l] + lambda * vrad0) / (1.0 + lambda);
+  vrad[l] = div_fast(vrad[l] + lambda * vrad0, 1.0 + lambda);
   if (damp_init) {
     const double rho0 = g.r.SigmaMed[i], e0 = g.r.EnergyMed[i];
     const double vt0 = g.r.VthetaMed[i] - g.r.Rmed[i] * omega_frame;
-    rho[l] = (rho[l] + lambda * rho0) / (1.0 + lambda);
-    vtheta[l] = (vtheta[l] + lambda * vt0) / (1.0 + lambda);
-    if (energy_eq) energy[l] = (energy[l] + lambda * e0) / (1.0 + lambda);
+    rho[l] = div_fast(rho[l] + lambda * rho0, 1.0 + lambda);
+    vtheta[l] = div_fast(vtheta[l] + lambda * vt0, 1.0 + lambda);
+    if (energy_eq) energy[l] = div_fast(energy[l] + lambda * e0, 1.0 + lambda);
   }
-  if (damp_flux) rho[l] = (rho[l] + lambda * g.r.SigmaMed[i]) / (1.0 + lambda);
+  if (damp_flux) rho[l] = div_fast(rho[l] + lambda * g.r.SigmaMed[i], 1.0 + lambda);
 }
 
 void aux_damp_gas(const DevGrid &g, double *vrad, double *rho, double *vtheta, double *energy, const int *rings,
@@ -312,9 +312,9 @@ __global__ void k_damp_peb(DevGrid g, double *__restrict__ pd, double *__restric
   const double lambda = g.r.WaveKiller[i] * dt;
   const double d0 = g.r.PebDensInit[i], vr0 = g.r.PebVradInit[i];
   const double vt0 = g.r.PebVthetaInit[i] - g.r.Rmed[i] * omega_frame;
-  pd[l] = (pd[l] + lambda * d0) / (1.0 + lambda);
-  pvr[l] = (pvr[l] + lambda * vr0) / (1.0 + lambda);
-  pvt[l] = (pvt[l] + lambda * vt0) / (1.0 + lambda);
+  pd[l] = div_fast(pd[l] + lambda * d0, 1.0 + lambda);
+  pvr[l] = div_fast(pvr[l] + lambda * vr0, 1.0 + lambda);
+  pvt[l] = div_fast(pvt[l] + lambda * vt0, 1.0 + lambda);
 }
 
 void aux_damp_peb(const DevGrid &g, double *pd, double *pvr, double *pvt, const int *rings, int nrings, double dt,

@@ -927,7 +927,7 @@ __global__ void k_rad_update(DevGrid g, PtrPack8 qf, const double *__restrict__ 
   const int ns = g.ns;
   CELL_LOOP_2D
   const int lip = l + ns;
-  const double dtheta = 2.0 * TH_PI / (double)ns;
+  const double dtheta = g.k.dpns;
   // the mass fluxes through the inner and outer faces are shared by all
   // quantities: varq = q*_in fin - q*_out fout
   const double fin = dt * dtheta * g.r.Rinf[i] * rhos[l] * vr[l];
@@ -1014,10 +1014,12 @@ __global__ void __launch_bounds__(AZ_TMAX) k_azimuthal(DevGrid g, AziIO io, cons
   const int tm = (t == 0) ? 0 : t - 1, tp = (t == T - 1) ? t : t + 1;   // edge threads only feed the halo
   const size_t rowo = (size_t)i * ns;
   const double rmed = g.r.Rmed[i];
-  const double dxtheta = 2.0 * TH_PI / (double)ns * rmed;
-  const double invdxtheta = 1.0 / dxtheta;
+  // ring constants from tables (the same values as 2 pi / ns * Rmed, its
+  // inverse and 1 / Surf, without three divisions per thread)
+  const double dxtheta = g.k.dpns * rmed;
+  const double invdxtheta = g.r.InvDxtheta[i];
   const double dxrad = (g.r.Rsup[i] - g.r.Rinf[i]) * dt;
-  const double invsurf = 1.0 / g.r.Surf[i];
+  const double invsurf = g.r.InvSurf[i];
   double q[NQ];
 #pragma unroll
   for (int k = 0; k < NQ; k++) q[k] = io.src[k][rowo + j];
@@ -1111,7 +1113,7 @@ __global__ void k_velocities(DevGrid g, const double *__restrict__ rho, const do
   else v = div_fast(rmp[l - ns] + rmm[l], rho[l] + rho[l - ns] + 1e-20);
   if (damp_vrad && (rm < drin || rm > drout)) {
     const double lambda = g.r.WaveKiller[i] * dt;
-    v = (v + lambda * 0.0) / (1.0 + lambda);
+    v = div_fast(v + lambda * 0.0, 1.0 + lambda);
   }
   vr[l] = v;
   vt[l] = div_fast(tmp_[ljm] + tmm[l], rho[l] + rho[ljm] + 1e-15) * g.r.InvRmed[i] - rm * omega_frame;

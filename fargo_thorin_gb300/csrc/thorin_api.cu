@@ -321,6 +321,8 @@ static void build_grid(thorin_disk *d)
   r.csmean = R[R_CSMEAN]; r.tempmean = R[R_TEMPMEAN]; r.nu_med = R[R_NUMED]; r.nu_inf = R[R_NUINF];
   DevConst &k = g.k;
   const thorin_params &p = d->p;
+  k.dpns = 2.0 * H_PI / (double)d->ns;
+  r.InvDxtheta = R[R_INVDXTHETA];
   k.opa2cu = OPA2CU; k.t2si = T2SI; k.rho2cgs = RHO2CGS; k.sigma_sb = STEFANBOLTZMANN; k.sqrt2pi_inv = SQRT2PI_INV;
   k.pebbulkdens = p.pebble_bulk_dens / RHO2CGS;
   k.cv = 1.0 / (1.0 * (p.adiabind - 1.0));

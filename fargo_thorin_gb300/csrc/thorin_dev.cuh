@@ -32,6 +32,7 @@ struct DevConst {
   double opa2cu, t2si, rho2cgs, sigma_sb, sqrt2pi_inv, pebbulkdens, cv, sqrt_adiabind_inv;
   double evaptemp;           // EVAPORATIONTEMPERATURE / T2SI
   double sqrt3;              // sqrt(3.0)
+  double dpns;               // 2 pi / nsec, the azimuthal cell width in radians
   // OpacityTable SM03: the Malygin gas table (device copies)
   const double *sm_pgrid, *sm_tgrid, *sm_ross;
   int sm_rows, sm_cols;
@@ -41,6 +42,7 @@ struct DevConst {
 struct DevRings {
   const double *Rinf, *Rsup, *Rmed, *Surf, *InvRmed, *InvSurf, *InvDiffRmed, *InvDiffRsup, *InvRinf;
   const double *OmegaInv, *Rmed2, *WaveKiller;
+  const double *InvDxtheta;             // 1 / (2 pi / nsec * Rmed)
   const double *Rmed15, *Rinf15;        // pow(Rmed,1.5), pow(Rinf,1.5) (FViscosity)
   const double *costab, *sintab;         // cos/sin(2 pi j / nsec), nsec entries
   const double *SigmaMed, *EnergyMed, *VthetaMed;
