@@ -702,12 +702,15 @@ __global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__r
   }
 }
 
-// One colour pass of sweep n.  Each thread updates SOR_CPT cells of ring i
+// One colour pass of a sweep.  Each thread updates SOR_CPT cells of ring i
 // (k = base + m*blockDim, j = 2k + parity).  The pass is bound by the FP64
-// pipe, so each cell costs nine FP64 instructions: the residual as five FMAs,
-// its absolute value added to the L1 norm, delta = resid * (omega/Ml) with
-// omega/Ml prepared once per solve by k_sor_resid0, the update, and the
-// change test delta > T*SORPRECISION taken from the sign of one FMA.
+// pipe, so each cell costs eight FP64 instructions: the residual as five
+// FMAs, its absolute value added to the L1 norm, and the update
+// T - resid * (omega/Ml) as one FMA (omega/Ml prepared once per solve by
+// k_sor_resid0); the change test delta > T*SORPRECISION runs on the integer
+// pipe (sor_changed).  The sweep number is counted on the device (c.niter),
+// so the launches of a chunk of sweeps are identical and replay as one CUDA
+// graph.
 // delta > tn * SORPRECISION (SORPRECISION = 1e-15, between 2^-50 and 2^-49)
 // with delta = resid * cw, cw = omega / Ml > 0.  When resid, cw and tn are
 // positive normal numbers well inside the exponent range, delta lies in
@@ -733,7 +736,7 @@ __global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict_
                                                   const double *__restrict__ mlip, const double *__restrict__ mlim,
                                                   const double *__restrict__ mljp, const double *__restrict__ mljm,
                                                   const double *__restrict__ rhs, const double *__restrict__ cw,
-                                                  SorCtl c, double eps, int pass, int n, int maxiters)
+                                                  SorCtl c, double eps, int pass, int maxiters)
 {
   if (*((volatile int *)c.done)) return;
   const int ns = g.ns, half = ns >> 1;
@@ -812,6 +815,7 @@ __global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict_
   cs = block_reduce(cs, OpAddI(), 0);
   if (threadIdx.x == 0) {
     const double r0 = *c.normres0;
+    const int n = __ldcg(c.niter) + 1;             // this sweep's number (k_sor_resid0 set 0)
     *c.normres = s;
     *c.changed = cs;
     *c.niter = n;
@@ -1250,14 +1254,12 @@ void hydro_sor_resid0(const DevGrid &g, const double *T, const double *ml, const
 
 void hydro_sor_sweeps(const DevGrid &g, double *T, const double *ml, const double *mlip, const double *mlim,
                       const double *mljp, const double *mljm, const double *rhs, const double *cw, const SorCtl &c,
-                      double eps, int first, int count, int maxiters, cudaStream_t s)
+                      double eps, int count, int maxiters, cudaStream_t s)
 {
   const dim3 grid = sor_grid_pass(g);
-  for (int n = first; n < first + count && n <= maxiters; n++) {
-    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, cw, c, eps, 1, n, maxiters);
-    g_thorin_launches++;
-    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, cw, c, eps, 2, n, maxiters);
-    g_thorin_launches++;
+  for (int n = 0; n < count; n++) {
+    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, cw, c, eps, 1, maxiters);
+    k_sor_pass<<<grid, SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, cw, c, eps, 2, maxiters);
   }
 }
 

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 #include "thorin_kernels.cuh"
@@ -161,6 +162,8 @@ struct thorin_disk {
   float ws_lr = 0.f;
   thorin_ws_stats ws_st = {0, 0, 0.0, 0.0, 0.0};
   double *ws_prev = nullptr;     // the previous solve's update T_conv - T_start (network input)
+  // SOR chunks of n sweeps, captured once as CUDA graphs and replayed
+  std::map<int, cudaGraphExec_t> sor_graphs;
   double heatsrc[THORIN_MAXPLANETS];
   int heatsrc_index[THORIN_MAXPLANETS], heatsrc_max;
   double gm1, gg1, drin, drout, invdphi, lr01, lr12, taueff_c, tirr4fac, rstar;
@@ -562,6 +565,7 @@ extern "C" int thorin_gpu_destroy(thorin_disk *d)
   cudaFreeHost(d->scal_h);
   cudaFreeHost(d->iscal_h);
   cudaFreeHost(d->csmean_h);
+  for (auto &kv : d->sor_graphs) cudaGraphExecDestroy(kv.second);
   for (int q = 0; q < 4; q++) cudaEventDestroy(d->ev[q]);
   if (d->s_peb) {
     cudaStreamSynchronize(d->s_peb);
@@ -1429,6 +1433,30 @@ extern "C" int thorin_gpu_get_torques(thorin_disk *d, thorin_torque *out, int ma
   return THORIN_OK;
 }
 
+// `count` SOR sweeps on the disk's stream: a CUDA graph of the 2*count pass
+// launches, captured the first time this count is asked for.
+static int sor_chunk(thorin_disk *d, int count)
+{
+  cudaGraphExec_t ge;
+  auto it = d->sor_graphs.find(count);
+  if (it == d->sor_graphs.end()) {
+    cudaGraph_t gr;
+    CUCHK(cudaStreamBeginCapture(d->s, cudaStreamCaptureModeThreadLocal));
+    hydro_sor_sweeps(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, d->sor,
+                     d->p.sor_eps, count, d->p.sor_maxiters, d->s);
+    CUCHK(cudaStreamEndCapture(d->s, &gr));
+    const cudaError_t e = cudaGraphInstantiate(&ge, gr, 0);
+    cudaGraphDestroy(gr);
+    CUCHK(e);
+    d->sor_graphs[count] = ge;
+  } else {
+    ge = it->second;
+  }
+  CUCHK(cudaGraphLaunch(ge, d->s));
+  g_thorin_launches += 2LL * count;
+  return THORIN_OK;
+}
+
 // SuccessiveOverrelaxation driver: residual, then sweeps launched in chunks;
 // converged sweeps turn later launches into no-ops.
 static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *capped, bool learned = false)
@@ -1450,8 +1478,7 @@ static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *ca
   *capped = 0;
   for (;;) {
     if (d->timing) CUCHK(cudaEventRecord(d->ev[0], d->s));
-    hydro_sor_sweeps(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, d->sor, p.sor_eps,
-                     first, chunk, p.sor_maxiters, d->s);
+    RCHK(sor_chunk(d, chunk));
     KCHECK("SOR sweep kernels");
     if (d->timing) CUCHK(cudaEventRecord(d->ev[1], d->s));
     CUCHK(cudaMemcpyAsync(d->iscal_h + IS_SOR_DONE, d->sor.done, 2 * sizeof(int), cudaMemcpyDeviceToHost, d->s));

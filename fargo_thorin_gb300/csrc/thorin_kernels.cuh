@@ -136,9 +136,13 @@ int sor_blocks(const DevGrid &g);
 void hydro_sor_resid0(const DevGrid &g, const double *T, const double *ml, const double *mlip, const double *mlim,
                       const double *mljp, const double *mljm, const double *rhs, double *cw, double omega,
                       const SorCtl &c, cudaStream_t s);
+// `count` sweeps (two colour passes each).  The sweep number lives on the
+// device, so every call with the same count issues identical launches (the
+// caller may capture and replay them as a CUDA graph); the launch counter is
+// left to the caller.
 void hydro_sor_sweeps(const DevGrid &g, double *T, const double *ml, const double *mlip, const double *mlim,
                       const double *mljp, const double *mljm, const double *rhs, const double *cw, const SorCtl &c,
-                      double eps, int first, int count, int maxiters, cudaStream_t s);
+                      double eps, int count, int maxiters, cudaStream_t s);
 void hydro_energy_from_t(const DevGrid &g, const double *rho, double *T, double *enew, cudaStream_t s);
 void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, double **energy, double *label,
                      const TransportScratch &S, double dt, double omega_frame, int fast, int damp_vrad, double drin,
