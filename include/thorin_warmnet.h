@@ -69,7 +69,11 @@ int thorin_warmnet_gradient(thorin_warmnet *n, int batch, const uint16_t *x, con
 /* One Adam step with the last gradient, clipped to global norm max_norm. */
 int thorin_warmnet_adam(thorin_warmnet *n, float lr, float beta1, float beta2, float eps, float max_norm);
 
-/* Attach a network to a disk (same nrad x nsec) or detach it (mode
+/* A network holds one set of activation buffers: attach it to one disk at
+ * a time (in an ensemble advanced by several threads, give each disk its
+ * own network).
+ *
+ * Attach a network to a disk (same nrad x nsec) or detach it (mode
  * THORIN_WS_OFF, n may be NULL).  PREDICT: every SOR solve of the disk
  * starts from T_old + Jacobi step + network prediction (a cell whose
  * predicted temperature is not positive keeps T_old).  TRAIN: the solve is
