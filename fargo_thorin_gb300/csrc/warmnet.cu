@@ -50,8 +50,15 @@ __device__ __forceinline__ unsigned char *align128(unsigned char *p)
 // input channels of in[p + tap] * W, with in = 0 outside rings 0..H-1 and the
 // azimuth periodic.  MODE 0: bf16 [P][N] = relu(acc + bias); MODE 1: float
 // [P] = acc[0] + bias[0]; MODE 2: float [P][N] = acc.
-// A tile: [kg][128 cells][16 B] (LBO 2048, SBO 128); B: [kg][N][16 B]
-// (LBO N*16, SBO 128); wk is [N][9*CIN] (K index = tap*CIN + c).
+//
+// A tile is 128 consecutive cells of one ring.  The CTA stages the ring and
+// its two neighbours over the tile's 128 cells plus one halo cell on each
+// side (azimuth wrapped) once, as [c/8][ring r' = 0..2][cell p' = 0..129][16 B].
+// Each tap (dr, dphi) is then the same tile seen through a shifted
+// descriptor: rows m = cells p' = m + 1 + dphi of ring r' = 1 + dr, 8 cells
+// per core matrix (SBO 128 B), channel groups 3 * 130 * 16 B apart (LBO).  No
+// im2col copy: a tile stages 3 * 130 cells instead of 9 * 128.
+// B: [kg][N][16 B] (LBO N*16, SBO 128); wk is [N][9*CIN] (K = tap*CIN + c).
 struct ConvArgs {
   const bf16 *in;
   const bf16 *wk;
@@ -62,20 +69,16 @@ struct ConvArgs {
   int *err;
 };
 
-// Taps staged and multiplied per phase (9: the whole im2col tile at once).
-// Three phases of three taps let more CTAs share an SM but measured twice
-// as slow: each phase adds an MMA completion round trip to the tile.
-constexpr int WN_TAPS_PER_PHASE = 9;
+constexpr int WN_HALO_W = 130;                     // 128 cells + one halo cell each side
 
 template <int CIN, int N>
-constexpr int conv_smem() { return WN_TAPS_PER_PHASE * CIN * 128 * 2 + 9 * CIN * N * 2 + 128 + 128; }
+constexpr int conv_smem() { return (CIN / 8) * 3 * WN_HALO_W * 16 + 9 * CIN * N * 2 + 128 + 128; }
 
 template <int CIN, int N, int MODE>
 __global__ void __launch_bounds__(128) k_wn_conv(ConvArgs a)
 {
-  constexpr int K = 9 * CIN, KG = K / 8, B_BYTES = KG * N * 16;
-  constexpr int TP = WN_TAPS_PER_PHASE, KP = TP * CIN, A_BYTES = (KP / 8) * 128 * 16;
-  static_assert(9 % TP == 0 && KP % 16 == 0, "phases of whole MMA k-steps");
+  constexpr int K = 9 * CIN, KG = K / 8, C8 = CIN / 8;
+  constexpr int A_BYTES = C8 * 3 * WN_HALO_W * 16, B_BYTES = KG * N * 16, LBO_A = 3 * WN_HALO_W * 16;
   constexpr uint32_t IDESC = umma::idesc_bf16(128, N);
   extern __shared__ unsigned char smem_raw[];
   unsigned char *sA = align128(smem_raw), *sB = sA + A_BYTES;
@@ -98,56 +101,50 @@ __global__ void __launch_bounds__(128) k_wn_conv(ConvArgs a)
 #pragma unroll
   for (int n = 0; n < N; n++) bias[n] = (MODE != 2 && n < a.coutr) ? a.bias[n] : 0.f;
 
-  const long long HW = (long long)a.H * a.W, P = (long long)a.B * HW;
-  const long long ntiles = (P + 127) / 128;
+  const int tpr = (a.W + 127) / 128;                       // tiles per ring
+  const long long ntiles = (long long)a.B * a.H * tpr;
   uint32_t phase = 0;
   bool ok = true;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const long long p = tile * 128 + tid;
-    const bool live = p < P;
-    int b = 0, i = 0, j = 0;
-    if (live) {
-      b = (int)(p / HW);
-      const long long rem = p - (long long)b * HW;
-      i = (int)(rem / a.W);
-      j = (int)(rem - (long long)i * a.W);
+    const long long ring = tile / tpr;                     // b * H + i
+    const int p0 = (int)(tile - ring * tpr) * 128;
+    const int i = (int)(ring % a.H);
+    const long long rbase = ring - i;                      // b * H
+    // stage rings i-1, i, i+1 over cells p0-1 .. p0+128 (azimuth wrapped)
+    for (int ch = tid; ch < 3 * WN_HALO_W * C8; ch += 128) {
+      const int c8 = ch % C8, rest = ch / C8, pp = rest % WN_HALO_W, rr = rest / WN_HALO_W;
+      const int ii = i + rr - 1;
+      int jj = (p0 - 1 + pp) % a.W;
+      if (jj < 0) jj += a.W;
+      uint4 val = make_uint4(0u, 0u, 0u, 0u);
+      if (ii >= 0 && ii < a.H) val = *(const uint4 *)(a.in + ((rbase + ii) * a.W + jj) * CIN + c8 * 8);
+      *(uint4 *)(sA + ((c8 * 3 + rr) * WN_HALO_W + pp) * 16) = val;
     }
-#pragma unroll 1
-    for (int ph = 0; ph < 9 / TP && ok; ph++) {
+    umma::fence_smem_async();
+    __syncthreads();
+    if (tid == 0) {
+      umma::fence_after_sync();
+      const uint32_t a0 = umma::smem_addr(sA), b0 = umma::smem_addr(sB);
 #pragma unroll
-      for (int tt = 0; tt < TP; tt++) {
-        const int t = ph * TP + tt;
-        const int ii = i + t / 3 - 1;
-        int jj = j + t % 3 - 1;
-        jj = jj < 0 ? jj + a.W : (jj >= a.W ? jj - a.W : jj);
-        const bool v = live && ii >= 0 && ii < a.H;
-        const uint4 *src = (const uint4 *)(a.in + (((long long)b * a.H + (v ? ii : 0)) * a.W + jj) * CIN);
+      for (int t = 0; t < 9; t++) {
+        const int rr = t / 3, pp = t % 3;                  // ring 1 + dr, first cell 1 + dphi
 #pragma unroll
-        for (int c8 = 0; c8 < CIN / 8; c8++) {
-          const uint4 val = v ? src[c8] : make_uint4(0u, 0u, 0u, 0u);
-          *(uint4 *)(sA + (tt * (CIN / 8) + c8) * 2048 + tid * 16) = val;
-        }
+        for (int ks = 0; ks < CIN / 16; ks++)
+          umma::mma_bf16(tmem, umma::desc(a0 + ((2 * ks * 3 + rr) * WN_HALO_W + pp) * 16, LBO_A, 128),
+                         umma::desc(b0 + (t * (CIN / 16) + ks) * 2 * N * 16, N * 16, 128), IDESC, t > 0 || ks > 0);
       }
-      umma::fence_smem_async();
-      __syncthreads();
-      if (tid == 0) {
-        umma::fence_after_sync();
-        const uint32_t a0 = umma::smem_addr(sA), b0 = umma::smem_addr(sB);
-#pragma unroll
-        for (int ks = 0; ks < KP / 16; ks++)
-          umma::mma_bf16(tmem, umma::desc(a0 + ks * 4096, 2048, 128),
-                         umma::desc(b0 + (ph * (KP / 16) + ks) * 2 * N * 16, N * 16, 128), IDESC, ph > 0 || ks > 0);
-        umma::mma_commit(bar);
-      }
-      __syncwarp();
-      ok = umma::mbar_wait(bar, phase, WN_WAIT);      // the tile is free again once the MMAs are done
-      ok = __syncthreads_and(ok);
-      phase ^= 1u;
+      umma::mma_commit(bar);
     }
+    __syncwarp();
+    ok = umma::mbar_wait(bar, phase, WN_WAIT);
+    ok = __syncthreads_and(ok);
+    phase ^= 1u;
     if (!ok) break;
     umma::fence_after_sync();
     float v[N];
     umma::tmem_ld<N>(tmem + ((uint32_t)(warp * 32) << 16), v);
+    const bool live = p0 + tid < a.W;
+    const long long p = ring * a.W + p0 + tid;
     if (live) {
       if (MODE == 0) {
         uint4 *dst = (uint4 *)((bf16 *)a.out + p * N);
@@ -744,7 +741,7 @@ static int conv_launch(thorin_warmnet *n, const bf16 *in, const bf16 *wk, const 
       occ = 1;
     occ_cache.store(occ);
   }
-  const long long tiles = ((long long)B * H * W + 127) / 128;
+  const long long tiles = (long long)B * H * ((W + 127) / 128);
   const long long wave = (long long)occ * n->nsm;     // persistent CTAs: one wave over the tiles
   const int grid = (int)(tiles < wave ? tiles : wave);
   ConvArgs a{in, wk, bias, coutr, out, B, H, W, n->err};
