@@ -733,16 +733,18 @@ static int conv_launch(thorin_warmnet *n, const bf16 *in, const bf16 *wk, const 
                        int B, int H, int W, cudaStream_t s)
 {
   constexpr int SM = conv_smem<CIN, N>();
-  static std::atomic<int> occ_cache{0};            // resident CTAs per SM at this shared-memory size
-  int occ = occ_cache.load();
-  if (occ == 0) {
+  static std::atomic<bool> attr{false};
+  if (!attr.load()) {
     WNCHK(cudaFuncSetAttribute(k_wn_conv<CIN, N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_wn_conv<CIN, N, MODE>, 128, SM) != cudaSuccess || occ < 1)
-      occ = 1;
-    occ_cache.store(occ);
+    attr.store(true);
   }
+  // Four persistent CTAs per SM (44 KB of shared memory and 32 TMEM columns
+  // each): the occupancy calculator answers 1 for this kernel, and one CTA
+  // per SM leaves the tile's load -> MMA -> epilogue chain unhidden (3x
+  // slower measured); CTAs that do not fit simply start later.
+  constexpr long long per_sm = 4;
   const long long tiles = (long long)B * H * ((W + 127) / 128);
-  const long long wave = (long long)occ * n->nsm;     // persistent CTAs: one wave over the tiles
+  const long long wave = per_sm * n->nsm;
   const int grid = (int)(tiles < wave ? tiles : wave);
   ConvArgs a{in, wk, bias, coutr, out, B, H, W, n->err};
   k_wn_conv<CIN, N, MODE><<<grid, 128, SM, s>>>(a);
