@@ -537,7 +537,7 @@ __global__ void k_wn_scale(int nr, int ns, const double *__restrict__ T, SorSys 
     const int i = 1 + (int)(q / ns), j = (int)(q % ns), l = j + i * ns;
     const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
     const double r = sor_resid(T, m.ml, m.mlip, m.mlim, m.mljp, m.mljm, m.rhs, l, l + ns, l - ns, ljp, ljm);
-    s += fabs(r / m.ml[l]);
+    s += (double)fabsf((float)r / (float)m.ml[l]);       // a scale: FP32 is plenty
     sr += fabs(r);
   }
   s = block_reduce(s, OpAdd(), 0.0);
@@ -560,17 +560,21 @@ __global__ void k_wn_features(int nr, int ns, const double *__restrict__ T, SorS
   float f[WN_NIN] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   double jl = 0.0;
   if (i >= 1 && i <= nr - 2) {
+    // the residual needs FP64 (it cancels); everything after it only feeds
+    // bf16 inputs and the start of the solve, so it runs in FP32
     const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
-    const double ml = m.ml[l];
-    const double rj = sor_resid(T, m.ml, m.mlip, m.mlim, m.mljp, m.mljm, m.rhs, l, l + ns, l - ns, ljp, ljm) / ml;
-    jl = -rj;
+    const double r = sor_resid(T, m.ml, m.mlip, m.mlim, m.mljp, m.mljm, m.rhs, l, l + ns, l - ns, ljp, ljm);
+    const float iml = 1.0f / (float)m.ml[l];
+    const float rj = (float)r * iml;
+    jl = -(double)rj;
     const double s = *scale;
-    const double rs = s > 0.0 ? rj / s : 0.0;
-    f[0] = (float)fmin(fmax(rs, -16.0), 16.0);
-    const double w1 = -m.mlip[l] / ml, w2 = -m.mlim[l] / ml, w3 = -m.mljp[l] / ml, w4 = -m.mljm[l] / ml;
-    f[1] = (float)w1; f[2] = (float)w2; f[3] = (float)w3; f[4] = (float)w4;
-    f[5] = (float)(-log(fmax(1.0 - (((w1 + w2) + w3) + w4), 1e-6)) * 0.25);
-    if (prev && s > 0.0) f[6] = (float)fmin(fmax(prev[l] / (s * (double)WN_YSCALE), -16.0), 16.0);
+    const float is = s > 1e-30 ? (float)(1.0 / s) : 0.f;
+    f[0] = fminf(fmaxf(rj * is, -16.f), 16.f);
+    const float w1 = -(float)m.mlip[l] * iml, w2 = -(float)m.mlim[l] * iml, w3 = -(float)m.mljp[l] * iml,
+                w4 = -(float)m.mljm[l] * iml;
+    f[1] = w1; f[2] = w2; f[3] = w3; f[4] = w4;
+    f[5] = -logf(fmaxf(1.f - (((w1 + w2) + w3) + w4), 1e-6f)) * 0.25f;
+    if (prev) f[6] = fminf(fmaxf((float)prev[l] * is * (1.f / WN_YSCALE), -16.f), 16.f);
   }
   jac[l] = jl;
   uint4 z[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
