@@ -15,12 +15,12 @@
 #include "../../include/thorin_warmnet.h"
 
 // learned SOR warm start (warmnet.cu)
-int wn_sor_predict(thorin_warmnet *n, int nr, int ns, double *T, const double *ml, const double *mlip,
+int wn_sor_predict(thorin_warmnet *n, int nr, int ns, int fc, double *T, const double *ml, const double *mlip,
                    const double *mlim, const double *mljp, const double *mljm, const double *rhs, const double *prev,
-                   cudaStream_t s);
-int wn_sor_train(thorin_warmnet *n, int nr, int ns, const double *tk, const double *tconv, const double *ml,
+                   double *jac, cudaStream_t s);
+int wn_sor_train(thorin_warmnet *n, int nr, int ns, int fc, const double *tk, const double *tconv, const double *ml,
                  const double *mlip, const double *mlim, const double *mljp, const double *mljm, const double *rhs,
-                 const double *prev, float lr, double *scratch, cudaStream_t s);
+                 const double *prev, double *jac, float lr, double *scratch, cudaStream_t s);
 int wn_record_update(int nr, int ns, const double *tconv, const double *tstart, double *prev, cudaStream_t s);
 int wn_last_loss(thorin_warmnet *n, double *loss);
 int wn_dims(const thorin_warmnet *n, int *nr, int *ns);
@@ -162,6 +162,8 @@ struct thorin_disk {
   float ws_lr = 0.f;
   thorin_ws_stats ws_st = {0, 0, 0.0, 0.0, 0.0};
   double *ws_prev = nullptr;     // the previous solve's update T_conv - T_start (network input)
+  double *ws_jac = nullptr;      // the Jacobi step of the solve's start, per cell
+  int ws_f = 1;                  // disk cells per network cell along each axis (1 or 2)
   // SOR chunks of n sweeps, captured once as CUDA graphs and replayed
   std::map<int, cudaGraphExec_t> sor_graphs;
   double heatsrc[THORIN_MAXPLANETS];
@@ -524,18 +526,23 @@ extern "C" int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode,
     g_last_error = "warmstart: mode OFF/PREDICT/TRAIN, a network unless OFF, lr > 0 to train";
     return THORIN_ERR_ARG;
   }
+  int f = 1;
   if (n) {
     int nr = 0, ns = 0;
     wn_dims(n, &nr, &ns);
-    if (nr != d->nr || ns != d->ns) {
-      g_last_error = "warmstart: the network's grid differs from the disk's";
+    if (nr == d->nr && ns == d->ns) f = 1;
+    else if (2 * nr == d->nr && 2 * ns == d->ns) f = 2;
+    else {
+      g_last_error = "warmstart: the network's grid must be the disk's or half of it in both directions";
       return THORIN_ERR_ARG;
     }
   }
   if (mode != THORIN_WS_OFF && !d->ws_prev) {
     RCHK(dalloc(d, (void **)&d->ws_prev, (size_t)d->nr * d->ns * sizeof(double)));
+    RCHK(dalloc(d, (void **)&d->ws_jac, (size_t)d->nr * d->ns * sizeof(double)));
     CUCHK(cudaMemsetAsync(d->ws_prev, 0, (size_t)d->nr * d->ns * sizeof(double), d->s));
   }
+  d->ws_f = f;
   d->ws_net = mode == THORIN_WS_OFF ? nullptr : n;
   d->ws_mode = mode;
   d->ws_lr = lr;
@@ -1470,8 +1477,8 @@ static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *ca
     // keep the start (for the update record after the solve), then move it
     CUCHK(cudaMemcpyAsync(d->tbackup, d->temper, (size_t)d->nr * d->ns * sizeof(double), cudaMemcpyDeviceToDevice,
                           d->s));
-    RCHK(wn_sor_predict(d->ws_net, d->nr, d->ns, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs,
-                        d->ws_prev, d->s));
+    RCHK(wn_sor_predict(d->ws_net, d->nr, d->ns, d->ws_f, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm,
+                        d->rhs, d->ws_prev, d->ws_jac, d->s));
     d->ws_st.predictions++;
   }
   int first = 1, chunk = hint > 0 ? hint : 4;
@@ -1589,8 +1596,8 @@ static int energy_step(thorin_disk *d, double dt)
   RCHK(sor_solve(d, d->omega, d->Niterlast, &Niter, &capped, true));
   if (train) {
     // fit the network to this solve; energy_new is free until the energy is formed below
-    RCHK(wn_sor_train(d->ws_net, d->nr, d->ns, d->tbackup, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm,
-                      d->rhs, d->ws_prev, d->ws_lr, d->energy_new, d->s));
+    RCHK(wn_sor_train(d->ws_net, d->nr, d->ns, d->ws_f, d->tbackup, d->temper, d->ml, d->mlip, d->mlim, d->mljp,
+                      d->mljm, d->rhs, d->ws_prev, d->ws_jac, d->ws_lr, d->energy_new, d->s));
     d->ws_st.train_steps++;
   }
   if (d->ws_net && d->ws_prev)        // this solve's update, an input of the next prediction

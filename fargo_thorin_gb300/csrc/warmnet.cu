@@ -546,80 +546,116 @@ __global__ void k_wn_scale(int nr, int ns, const double *__restrict__ T, SorSys 
   if (threadIdx.x == 0) part[gridDim.x + blockIdx.x] = sr;
 }
 
-// network input x[l][16] and the Jacobi step jac = -r / Ml.  Channels: the
-// Jacobi-scaled residual over its mean (clipped), the four neighbour weights
-// -M/Ml, the stiffness -log(1 - sum w) / 4, and the previous solve's update
-// in the output's units (clipped; zero before the first solve)
-__global__ void k_wn_features(int nr, int ns, const double *__restrict__ T, SorSys m, const double *__restrict__ scale,
-                              const double *__restrict__ prev, bf16 *__restrict__ x, double *__restrict__ jac)
+// The network may run on a coarser grid than the disk: f x f disk cells
+// (f = 1 or 2) make one network cell.  Its inputs are the averages of the
+// fine cells' inputs, and its prediction is applied to each of them (nearest
+// upsampling).  The Jacobi step stays per fine cell.
+
+// One fine cell's inputs: the Jacobi-scaled residual over its mean
+// (clipped), the four neighbour weights -M/Ml, the stiffness
+// -log(1 - sum w) / 4 and the previous solve's update in the output's units
+// (clipped; zero before the first solve).  Returns the Jacobi step -r/Ml.
+// The residual needs FP64 (it cancels); the rest only feeds bf16 inputs and
+// the start of the solve, so it runs in FP32.
+__device__ __forceinline__ double wn_cell_inputs(int nr, int ns, int i, int j, const double *T, const SorSys &m,
+                                                 float is, const double *prev, float (&f)[WN_NIN])
 {
-  const long long n = (long long)nr * ns;
+  if (i < 1 || i > nr - 2) return 0.0;
+  const int l = j + i * ns;
+  const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+  const double r = sor_resid(T, m.ml, m.mlip, m.mlim, m.mljp, m.mljm, m.rhs, l, l + ns, l - ns, ljp, ljm);
+  const float iml = 1.0f / (float)m.ml[l];
+  const float rj = (float)r * iml;
+  f[0] += fminf(fmaxf(rj * is, -16.f), 16.f);
+  const float w1 = -(float)m.mlip[l] * iml, w2 = -(float)m.mlim[l] * iml, w3 = -(float)m.mljp[l] * iml,
+              w4 = -(float)m.mljm[l] * iml;
+  f[1] += w1; f[2] += w2; f[3] += w3; f[4] += w4;
+  f[5] += -logf(fmaxf(1.f - (((w1 + w2) + w3) + w4), 1e-6f)) * 0.25f;
+  if (prev) f[6] += fminf(fmaxf((float)prev[l] * is * (1.f / WN_YSCALE), -16.f), 16.f);
+  return -(double)rj;
+}
+
+// network input x[L][16] for each network cell L (the mean of its f x f
+// fine cells' inputs) and the Jacobi step jac of every fine cell
+__global__ void k_wn_features(int nr, int ns, int fc, const double *__restrict__ T, SorSys m,
+                              const double *__restrict__ scale, const double *__restrict__ prev, bf16 *__restrict__ x,
+                              double *__restrict__ jac)
+{
+  const int H = nr / fc, W = ns / fc;
+  const long long n = (long long)H * W;
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= n) return;
-  const int i = (int)(q / ns), j = (int)(q % ns), l = (int)q;
+  const int I = (int)(q / W), J = (int)(q % W);
+  const double s = *scale;
+  const float is = s > 1e-30 ? (float)(1.0 / s) : 0.f;
   float f[WN_NIN] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  double jl = 0.0;
-  if (i >= 1 && i <= nr - 2) {
-    // the residual needs FP64 (it cancels); everything after it only feeds
-    // bf16 inputs and the start of the solve, so it runs in FP32
-    const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
-    const double r = sor_resid(T, m.ml, m.mlip, m.mlim, m.mljp, m.mljm, m.rhs, l, l + ns, l - ns, ljp, ljm);
-    const float iml = 1.0f / (float)m.ml[l];
-    const float rj = (float)r * iml;
-    jl = -(double)rj;
-    const double s = *scale;
-    const float is = s > 1e-30 ? (float)(1.0 / s) : 0.f;
-    f[0] = fminf(fmaxf(rj * is, -16.f), 16.f);
-    const float w1 = -(float)m.mlip[l] * iml, w2 = -(float)m.mlim[l] * iml, w3 = -(float)m.mljp[l] * iml,
-                w4 = -(float)m.mljm[l] * iml;
-    f[1] = w1; f[2] = w2; f[3] = w3; f[4] = w4;
-    f[5] = -logf(fmaxf(1.f - (((w1 + w2) + w3) + w4), 1e-6f)) * 0.25f;
-    if (prev) f[6] = fminf(fmaxf((float)prev[l] * is * (1.f / WN_YSCALE), -16.f), 16.f);
-  }
-  jac[l] = jl;
+  for (int a = 0; a < fc; a++)
+    for (int b = 0; b < fc; b++) {
+      const int i = I * fc + a, j = J * fc + b;
+      jac[j + (long long)i * ns] = wn_cell_inputs(nr, ns, i, j, T, m, is, prev, f);
+    }
+  const float inv = 1.f / (float)(fc * fc);
   uint4 z[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
   bf16 *h = (bf16 *)z;
 #pragma unroll
-  for (int c = 0; c < WN_NIN; c++) h[c] = __float2bfloat16_rn(f[c]);
+  for (int c = 0; c < WN_NIN; c++) h[c] = __float2bfloat16_rn(f[c] * inv);
   uint4 *dst = (uint4 *)(x + q * THORIN_WN_INPUTS);
   dst[0] = z[0];
   dst[1] = z[1];
 }
 
-// T += jac + scale * YSCALE * y on the unknowns; a non-positive result keeps T
-__global__ void k_wn_apply(int nr, int ns, double *__restrict__ T, const double *__restrict__ jac,
+__device__ __forceinline__ long long wn_coarse(int i, int j, int ns, int fc)
+{
+  return (long long)(i / fc) * (ns / fc) + j / fc;
+}
+
+// T += jac + scale * YSCALE * y (y of the cell's network cell) on the
+// unknowns; a non-positive result keeps T
+__global__ void k_wn_apply(int nr, int ns, int fc, double *__restrict__ T, const double *__restrict__ jac,
                            const float *__restrict__ y, const double *__restrict__ scale)
 {
   const long long n = (long long)(nr - 2) * ns;
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= n) return;
   const long long l = q + ns;
-  const double t = T[l] + jac[l] + (*scale) * (double)WN_YSCALE * (double)y[l];
+  const int i = (int)(l / ns), j = (int)(l % ns);
+  const double t = T[l] + jac[l] + (*scale) * (double)WN_YSCALE * (double)y[wn_coarse(i, j, ns, fc)];
   if (t > 0.0) T[l] = t;
 }
 
-// training target (T_conv - T_k - jac) / (scale * YSCALE); zero off the unknowns
-__global__ void k_wn_target(int nr, int ns, const double *__restrict__ tconv, const double *__restrict__ tk,
+// training target of each network cell: the mean over its fine cells of
+// (T_conv - T_k - jac) / (scale * YSCALE), unknowns only
+__global__ void k_wn_target(int nr, int ns, int fc, const double *__restrict__ tconv, const double *__restrict__ tk,
                             const double *__restrict__ jac, const double *__restrict__ scale, float *__restrict__ tgt)
 {
-  const long long n = (long long)nr * ns;
+  const int H = nr / fc, W = ns / fc;
+  const long long n = (long long)H * W;
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= n) return;
-  const int i = (int)(q / ns);
+  const int I = (int)(q / W), J = (int)(q % W);
   const double s = *scale;
-  tgt[q] = (i >= 1 && i <= nr - 2 && s > 0.0) ? (float)((tconv[q] - tk[q] - jac[q]) / (s * (double)WN_YSCALE)) : 0.f;
+  double acc = 0.0;
+  for (int a = 0; a < fc; a++)
+    for (int b = 0; b < fc; b++) {
+      const int i = I * fc + a, j = J * fc + b;
+      const long long l = j + (long long)i * ns;
+      if (i >= 1 && i <= nr - 2) acc += tconv[l] - tk[l] - jac[l];
+    }
+  tgt[q] = s > 0.0 ? (float)(acc / ((double)(fc * fc) * s * (double)WN_YSCALE)) : 0.f;
 }
 
 // predicted start temperature: tp = T_k + jac + scale * YSCALE * y on the
 // unknowns, T_k on the boundary rings
-__global__ void k_wn_tpred(int nr, int ns, const double *__restrict__ tk, const double *__restrict__ jac,
+__global__ void k_wn_tpred(int nr, int ns, int fc, const double *__restrict__ tk, const double *__restrict__ jac,
                            const float *__restrict__ y, const double *__restrict__ scale, double *__restrict__ tp)
 {
   const long long n = (long long)nr * ns;
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= n) return;
-  const int i = (int)(q / ns);
-  tp[q] = (i >= 1 && i <= nr - 2) ? tk[q] + jac[q] + (*scale) * (double)WN_YSCALE * (double)y[q] : tk[q];
+  const int i = (int)(q / ns), j = (int)(q % ns);
+  tp[q] = (i >= 1 && i <= nr - 2)
+              ? tk[q] + jac[q] + (*scale) * (double)WN_YSCALE * (double)y[wn_coarse(i, j, ns, fc)]
+              : tk[q];
 }
 
 // rs = (A tp - rhs) / sr on the unknowns (zero elsewhere); partial sums of rs^2
@@ -644,28 +680,45 @@ __global__ void k_wn_res(int nr, int ns, const double *__restrict__ tp, SorSys m
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
-// output gradient of  wres * mean(rs^2) + wsup * mean((y - tgt)^2)  over the
-// unknowns: wres * 2/N * (scale * YSCALE / sr) * (A^T rs) + wsup * 2/N * (y - tgt),
-// as channel 0 of gy16; partial sums of (y - tgt)^2
+// gradient of wres * mean_fine(rs^2) with respect to each fine cell's
+// predicted update: wres * 2/N * (scale * YSCALE / sr) * (A^T rs)
 __global__ void k_wn_res_grad(int nr, int ns, const float *__restrict__ rs, SorSys m, const double *__restrict__ scale,
-                              const double *__restrict__ sr, const float *__restrict__ y, const float *__restrict__ tgt,
-                              float wres, float wsup, double inv_n, bf16 *__restrict__ gy16, double *__restrict__ part)
+                              const double *__restrict__ sr, float wres, double inv_n, float *__restrict__ gf)
 {
   const long long n = (long long)nr * ns;
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int i = (int)(q / ns), j = (int)(q % ns), l = (int)q;
+  float g = 0.f;
+  if (i >= 1 && i <= nr - 2 && *sr > 0.0) {
+    const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+    double at = m.ml[l] * rs[l] + m.mljm[ljp] * rs[ljp] + m.mljp[ljm] * rs[ljm];
+    if (i + 1 <= nr - 2) at += m.mlim[l + ns] * rs[l + ns];
+    if (i - 1 >= 1) at += m.mlip[l - ns] * rs[l - ns];
+    g = (float)(2.0 * inv_n * (double)wres * (*scale) * (double)WN_YSCALE / (*sr) * at);
+  }
+  gf[l] = g;
+}
+
+// output gradient of each network cell: the sum of its fine cells'
+// residual gradients plus wsup * 2/Nc * (y - tgt), as channel 0 of gy16;
+// partial sums of (y - tgt)^2
+__global__ void k_wn_out_grad(int nr, int ns, int fc, const float *__restrict__ gf, const float *__restrict__ y,
+                              const float *__restrict__ tgt, float wsup, double inv_nc, bf16 *__restrict__ gy16,
+                              double *__restrict__ part)
+{
+  const int H = nr / fc, W = ns / fc;
+  const long long n = (long long)H * W;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   double acc = 0.0;
   if (q < n) {
-    const int i = (int)(q / ns), j = (int)(q % ns), l = (int)q;
+    const int I = (int)(q / W), J = (int)(q % W);
     float g = 0.f;
-    if (i >= 1 && i <= nr - 2 && *sr > 0.0) {
-      const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
-      double at = m.ml[l] * rs[l] + m.mljm[ljp] * rs[ljp] + m.mljp[ljm] * rs[ljm];
-      if (i + 1 <= nr - 2) at += m.mlim[l + ns] * rs[l + ns];
-      if (i - 1 >= 1) at += m.mlip[l - ns] * rs[l - ns];
-      const double d = (double)y[l] - (double)tgt[l];
-      acc = d * d;
-      g = (float)(2.0 * inv_n * ((double)wres * (*scale) * (double)WN_YSCALE / (*sr) * at + (double)wsup * d));
-    }
+    for (int a = 0; a < fc; a++)
+      for (int b = 0; b < fc; b++) g += gf[(J * fc + b) + (long long)(I * fc + a) * ns];
+    const double d = (double)y[q] - (double)tgt[q];
+    acc = d * d;
+    g += (float)(2.0 * inv_nc * (double)wsup * d);
     uint4 z[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
     ((bf16 *)z)[0] = __float2bfloat16_rn(g);
     uint4 *dst = (uint4 *)(gy16 + q * 16);
@@ -708,7 +761,6 @@ struct thorin_warmnet {
   float *part;                           // weight-gradient partials
   int part_blocks;
   double *dscal;                         // [0] loss, [1] grad sq-norm, [2] residual scale, partials from 8
-  double *jac;                           // Jacobi step of the coupled disk
   int *err;
   int adam_t;
   int B;                                 // batch of the last forward
@@ -913,10 +965,11 @@ static int wn_check_err(thorin_warmnet *n)
 // ---------------------------------------------------------------------------
 // Disk coupling, called from the SOR driver on the disk's stream.
 
-// T (start of the solve, or the current iterate) -> T + jac + network
-int wn_sor_predict(thorin_warmnet *n, int nr, int ns, double *T, const double *ml, const double *mlip,
+// T (start of the solve) -> T + jac + network.  The network grid is
+// (nr/fc) x (ns/fc); jac has the disk's nr x ns cells.
+int wn_sor_predict(thorin_warmnet *n, int nr, int ns, int fc, double *T, const double *ml, const double *mlip,
                    const double *mlim, const double *mljp, const double *mljm, const double *rhs, const double *prev,
-                   cudaStream_t s)
+                   double *jac, cudaStream_t s)
 {
   // dscal: [2] mean |r/Ml| of the start, [3] mean |r|, [4] residual loss,
   // [5] supervised loss, [0] total loss; partials from dscal + 8
@@ -925,45 +978,46 @@ int wn_sor_predict(thorin_warmnet *n, int nr, int ns, double *T, const double *m
   const int sb = 2 * n->nsm;
   k_wn_scale<<<sb, 256, 0, s>>>(nr, ns, T, m, part);
   k_wn_sum<<<1, 32, 0, s>>>(part, sb, 1.0 / ((double)(nr - 2) * ns), n->dscal + 2);
-  k_wn_features<<<nblk((long long)nr * ns), 256, 0, s>>>(nr, ns, T, m, n->dscal + 2, prev, n->x, n->jac);
+  k_wn_features<<<nblk((long long)(nr / fc) * (ns / fc)), 256, 0, s>>>(nr, ns, fc, T, m, n->dscal + 2, prev, n->x, jac);
   g_thorin_launches += 3;
   RCHK_WN(wn_forward(n, 1, s));
-  k_wn_apply<<<nblk((long long)(nr - 2) * ns), 256, 0, s>>>(nr, ns, T, n->jac, n->y, n->dscal + 2);
+  k_wn_apply<<<nblk((long long)(nr - 2) * ns), 256, 0, s>>>(nr, ns, fc, T, jac, n->y, n->dscal + 2);
   g_thorin_launches++;
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? THORIN_OK : wn_fail("predict kernels", e);
 }
 
 // one training step on the solve that went from tk to tconv: loss = WRES *
-// mean((A T_pred - rhs)^2) / mean|r_k|^2 + WSUP * mean((y - target)^2) over the
-// unknowns, T_pred = tk + jac + scale * YSCALE * y, target the converged update
-// beyond the Jacobi step in the same units
-int wn_sor_train(thorin_warmnet *n, int nr, int ns, const double *tk, const double *tconv, const double *ml,
+// mean((A T_pred - rhs)^2) / mean|r_k|^2 over the disk's unknowns + WSUP *
+// mean((y - target)^2) over the network cells, T_pred = tk + jac + scale *
+// YSCALE * y, target the converged update beyond the Jacobi step in the same
+// units (averaged over each network cell)
+int wn_sor_train(thorin_warmnet *n, int nr, int ns, int fc, const double *tk, const double *tconv, const double *ml,
                  const double *mlip, const double *mlim, const double *mljp, const double *mljm, const double *rhs,
-                 const double *prev, float lr, double *scratch, cudaStream_t s)
+                 const double *prev, double *jac, float lr, double *scratch, cudaStream_t s)
 {
   constexpr float WRES = 1.0f, WSUP = 0.1f;
   SorSys m{ml, mlip, mlim, mljp, mljm, rhs};
   double *part = n->dscal + 8;
   const int sb = 2 * n->nsm;
-  const long long cells = (long long)nr * ns;
-  const double inv_n = 1.0 / ((double)(nr - 2) * ns);
+  const long long cells = (long long)nr * ns, ncells = (long long)(nr / fc) * (ns / fc);
+  const double inv_n = 1.0 / ((double)(nr - 2) * ns), inv_nc = 1.0 / (double)ncells;
   k_wn_scale<<<sb, 256, 0, s>>>(nr, ns, tk, m, part);
   k_wn_sum<<<1, 32, 0, s>>>(part, sb, inv_n, n->dscal + 2);
   k_wn_sum<<<1, 32, 0, s>>>(part + sb, sb, inv_n, n->dscal + 3);
-  k_wn_features<<<nblk(cells), 256, 0, s>>>(nr, ns, tk, m, n->dscal + 2, prev, n->x, n->jac);
-  k_wn_target<<<nblk(cells), 256, 0, s>>>(nr, ns, tconv, tk, n->jac, n->dscal + 2, n->tgt);
+  k_wn_features<<<nblk(ncells), 256, 0, s>>>(nr, ns, fc, tk, m, n->dscal + 2, prev, n->x, jac);
+  k_wn_target<<<nblk(ncells), 256, 0, s>>>(nr, ns, fc, tconv, tk, jac, n->dscal + 2, n->tgt);
   g_thorin_launches += 5;
   RCHK_WN(wn_forward(n, 1, s));
-  float *rs = n->gf[0];                       // free until the backward pass
-  k_wn_tpred<<<nblk(cells), 256, 0, s>>>(nr, ns, tk, n->jac, n->y, n->dscal + 2, scratch);
+  float *rs = n->gf[0], *gfine = n->gf[0] + cells;    // free until the backward pass (>= 8 * cells floats)
+  k_wn_tpred<<<nblk(cells), 256, 0, s>>>(nr, ns, fc, tk, jac, n->y, n->dscal + 2, scratch);
   k_wn_res<<<nblk(cells), 256, 0, s>>>(nr, ns, scratch, m, n->dscal + 3, rs, part);
   k_wn_sum<<<1, 32, 0, s>>>(part, (int)nblk(cells), inv_n, n->dscal + 4);
-  k_wn_res_grad<<<nblk(cells), 256, 0, s>>>(nr, ns, rs, m, n->dscal + 2, n->dscal + 3, n->y, n->tgt, WRES, WSUP, inv_n,
-                                            n->act[GY16], part);
-  k_wn_sum<<<1, 32, 0, s>>>(part, (int)nblk(cells), inv_n, n->dscal + 5);
+  k_wn_res_grad<<<nblk(cells), 256, 0, s>>>(nr, ns, rs, m, n->dscal + 2, n->dscal + 3, WRES, inv_n, gfine);
+  k_wn_out_grad<<<nblk(ncells), 256, 0, s>>>(nr, ns, fc, gfine, n->y, n->tgt, WSUP, inv_nc, n->act[GY16], part);
+  k_wn_sum<<<1, 32, 0, s>>>(part, (int)nblk(ncells), inv_nc, n->dscal + 5);
   k_wn_total<<<1, 1, 0, s>>>(n->dscal, WRES, WSUP);
-  g_thorin_launches += 6;
+  g_thorin_launches += 7;
   RCHK_WN(wn_backward(n, 1, s, false));
   RCHK_WN(wn_adam(n, lr, 0.9f, 0.999f, 1e-8f, 1.0f, s));
   const cudaError_t e = cudaGetLastError();
@@ -1054,7 +1108,6 @@ extern "C" int thorin_warmnet_create(int nrad, int nsec, int max_batch, thorin_w
   const size_t nd = 8 + (size_t)(nblk(P0) > 4096 ? nblk(P0) : 4096);
   if ((e = cudaMalloc((void **)&n->dscal, nd * sizeof(double))) != cudaSuccess) return fail(e);
   cudaMemset(n->dscal, 0, nd * sizeof(double));
-  if ((e = cudaMalloc((void **)&n->jac, (size_t)nrad * nsec * sizeof(double))) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc((void **)&n->err, sizeof(int))) != cudaSuccess) return fail(e);
   cudaMemset(n->err, 0, sizeof(int));
   pack_all(n, n->own);
@@ -1067,7 +1120,7 @@ extern "C" int thorin_warmnet_destroy(thorin_warmnet *n)
 {
   if (!n) return THORIN_OK;
   if (n->own) cudaStreamSynchronize(n->own);
-  void *ptrs[] = {n->w, n->g, n->m, n->v, n->x, n->y, n->tgt, n->part, n->dscal, n->jac, n->err};
+  void *ptrs[] = {n->w, n->g, n->m, n->v, n->x, n->y, n->tgt, n->part, n->dscal, n->err};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int l = 0; l < WN_NL; l++) {

@@ -46,13 +46,20 @@ def init_params(seed: int = 0) -> np.ndarray:
 
 
 class WarmNet:
-    """The network on the GPU, sized for batch images of nrad x nsec."""
+    """The network on the GPU for a disk of nrad x nsec cells.  With
+    factor 2 it runs on the half-resolution grid (each network cell averages
+    2 x 2 disk cells' inputs, and its prediction applies to all four).  nr,
+    ns are the network's grid, used by the raw forward and gradient calls."""
 
-    def __init__(self, nrad: int, nsec: int, max_batch: int = 1, params: np.ndarray | None = None):
+    def __init__(self, nrad: int, nsec: int, max_batch: int = 1, params: np.ndarray | None = None, factor: int = 1):
+        if factor not in (1, 2) or nrad % (8 * factor) or nsec % (8 * factor):
+            raise ValueError("factor 1 or 2, and nrad, nsec multiples of 8 * factor")
         self.L = _lib.load()
-        self.nr, self.ns, self.maxb = nrad, nsec, max_batch
+        self.factor = factor
+        self.disk_nr, self.disk_ns = nrad, nsec
+        self.nr, self.ns, self.maxb = nrad // factor, nsec // factor, max_batch
         self.h = C.c_void_p()
-        _lib.check(self.L.thorin_warmnet_create(nrad, nsec, max_batch, C.byref(self.h)), "thorin_warmnet_create")
+        _lib.check(self.L.thorin_warmnet_create(self.nr, self.ns, max_batch, C.byref(self.h)), "thorin_warmnet_create")
         self.set_params(init_params() if params is None else params)
 
     def close(self):
@@ -172,7 +179,7 @@ def train(net: WarmNet, ndisks: int, steps_per_disk: int, lr: float = 1e-3, seed
     for k in range(ndisks):
         rate = lr if lr_final is None or ndisks == 1 else lr * (lr_final / lr) ** (k / (ndisks - 1))
         draw = draw_disk(rng)
-        p, d, sys_ = make_training_disk(net.nr, net.ns, draw, seed=1000 * seed + k, dt_div=dt_div)
+        p, d, sys_ = make_training_disk(net.disk_nr, net.disk_ns, draw, seed=1000 * seed + k, dt_div=dt_div)
         attach(d, net, TRAIN, rate)
         for _ in range(steps_per_disk):
             d.algogas(sys_)
@@ -195,7 +202,7 @@ def compare_sweeps(net: WarmNet, draw: dict, ndt: int, seed: int = 12345, dt_div
     out = {}
     temps = {}
     for mode in (OFF, PREDICT):
-        p, d, sys_ = make_training_disk(net.nr, net.ns, draw, seed=seed, dt_div=dt_div)
+        p, d, sys_ = make_training_disk(net.disk_nr, net.disk_ns, draw, seed=seed, dt_div=dt_div)
         for _ in range(warm):
             d.algogas(sys_)
         attach(d, net if mode == PREDICT else None, mode)
@@ -225,6 +232,7 @@ if __name__ == "__main__":
     ap.add_argument("--nsec", type=int, default=3072)
     ap.add_argument("--disks", type=int, default=24)
     ap.add_argument("--steps", type=int, default=6, help="DTs per training disk")
+    ap.add_argument("--factor", type=int, default=1, help="disk cells per network cell along each axis (1 or 2)")
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--lr-final", type=float, default=1e-4)
     ap.add_argument("--seed", type=int, default=0)
@@ -235,17 +243,17 @@ if __name__ == "__main__":
                     help="only time this many forward passes on random inputs (no training, no evaluation)")
     a = ap.parse_args()
     t0 = time.time()
-    net = WarmNet(a.nrad, a.nsec, params=WarmNet.load_params(a.init) if a.init else None)
+    net = WarmNet(a.nrad, a.nsec, params=WarmNet.load_params(a.init) if a.init else None, factor=a.factor)
     if a.forward > 0:
         rng = np.random.default_rng(0)
-        x = np.zeros((1, a.nrad, a.nsec, INPUTS), np.float32)
-        x[..., :7] = rng.uniform(-1.0, 1.0, (1, a.nrad, a.nsec, 7))
+        x = np.zeros((1, net.nr, net.ns, INPUTS), np.float32)
+        x[..., :7] = rng.uniform(-1.0, 1.0, (1, net.nr, net.ns, 7))
         bits = (np.ascontiguousarray(x).view(np.uint32) >> 16).astype(np.uint16)
         net.forward(bits)
         t1 = time.time()
         for _ in range(a.forward):
             net.forward(bits)
-        print(f"{a.forward} forward passes of {a.nrad}x{a.nsec} in {time.time() - t1:.3f} s "
+        print(f"{a.forward} forward passes of {net.nr}x{net.ns} in {time.time() - t1:.3f} s "
               f"(host copies included)", flush=True)
         raise SystemExit(0)
     if a.disks > 0:

@@ -73,8 +73,11 @@ int thorin_warmnet_adam(thorin_warmnet *n, float lr, float beta1, float beta2, f
  * a time (in an ensemble advanced by several threads, give each disk its
  * own network).
  *
- * Attach a network to a disk (same nrad x nsec) or detach it (mode
- * THORIN_WS_OFF, n may be NULL).  PREDICT: every SOR solve of the disk
+ * Attach a network to a disk or detach it (mode
+ * THORIN_WS_OFF, n may be NULL).  The network's grid is the disk's nrad x
+ * nsec, or half of it in both directions: then each network cell takes the
+ * mean of its 2 x 2 disk cells' inputs and its prediction applies to all
+ * four, while the Jacobi step stays per disk cell.  PREDICT: every SOR solve of the disk
  * starts from T_old + Jacobi step + network prediction (a cell whose
  * predicted temperature is not positive keeps T_old).  TRAIN: the solve is
  * plain; afterwards one Adam step (learning rate lr, moments 0.9/0.999,
