@@ -1105,7 +1105,9 @@ extern "C" int thorin_warmnet_create(int nrad, int nsec, int max_batch, thorin_w
   }
   const size_t part = (size_t)n->part_blocks * (9 * WN_C * WN_C + WN_C);
   if ((e = cudaMalloc((void **)&n->part, part * sizeof(float))) != cudaSuccess) return fail(e);
-  const size_t nd = 8 + (size_t)(nblk(P0) > 4096 ? nblk(P0) : 4096);
+  // reduction partials: one per 256 cells of the largest grid a pass runs
+  // over, which for a disk coupled at half resolution is 4x the network's
+  const size_t nd = 8 + (size_t)(nblk(4 * P0) > 4096 ? nblk(4 * P0) : 4096);
   if ((e = cudaMalloc((void **)&n->dscal, nd * sizeof(double))) != cudaSuccess) return fail(e);
   cudaMemset(n->dscal, 0, nd * sizeof(double));
   if ((e = cudaMalloc((void **)&n->err, sizeof(int))) != cudaSuccess) return fail(e);
