@@ -141,7 +141,8 @@ def reduce_over_ranks(values, ops, device):
     return out
 
 
-WARMNET = os.path.join(ROOT, "fargo_thorin_gb300", "warmnet_disk1_1024x3072.npy")
+WARMNET = os.environ.get("THORIN_WARMNET", os.path.join(ROOT, "fargo_thorin_gb300", "warmnet_disk1_1024x3072.npy"))
+WARMNET_FACTOR = int(os.environ.get("THORIN_WARMNET_FACTOR", "1"))   # disk cells per network cell per axis
 
 
 def warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, steps, stream, barrier, t_plain, plain_per_solve):
@@ -152,7 +153,7 @@ def warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, steps, stream, barr
     from fargo_thorin_gb300 import warmstart as WS
     if not os.path.exists(WARMNET):
         return {"unavailable": "no trained network file"}
-    net = WS.WarmNet(NR, NS, params=WS.WarmNet.load_params(WARMNET))
+    net = WS.WarmNet(NR, NS, params=WS.WarmNet.load_params(WARMNET), factor=WARMNET_FACTOR)
     for f, v in snap.items():
         d.upload(f, v)
     d.set_sor_state(*snap_sor[:3])
@@ -179,7 +180,7 @@ def warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, steps, stream, barr
     return {"plain_sweeps_per_solve": plain_per_solve, "learned_sweeps_per_solve": per_solve,
             "sweeps_ratio_plain_over_learned": plain_per_solve / per_solve if per_solve else None,
             "learned_value": NR * NS * subs / (ms / 1e3), "learned_ms_per_step": ms / steps, "substeps": subs,
-            "network_applications": pred, "network": os.path.relpath(WARMNET, ROOT),
+            "network_applications": pred, "network": os.path.relpath(WARMNET, ROOT), "network_factor": WARMNET_FACTOR,
             "t_rel_l2_vs_plain": float(np.linalg.norm(t - t_plain) / np.linalg.norm(t_plain)),
             "threshold": "eps * L1 residual of the previous-temperature start, as the plain solve"}
 
