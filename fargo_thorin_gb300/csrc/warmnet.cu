@@ -604,9 +604,45 @@ __global__ void k_wn_features(int nr, int ns, int fc, const double *__restrict__
   dst[1] = z[1];
 }
 
-__device__ __forceinline__ long long wn_coarse(int i, int j, int ns, int fc)
+// Prolongation of the network's output to the disk's cells.  fc = 1: the
+// same cell.  fc = 2: bilinear between network-cell centres.  Disk cell i
+// sits at network coordinate (i - 1/2) / 2, so an even i takes 1/4 of
+// network cell i/2 - 1 and 3/4 of i/2, and an odd i takes 3/4 of (i-1)/2
+// and 1/4 of (i+1)/2.  Radially the index is clamped to the grid;
+// azimuthally it wraps.
+__device__ __forceinline__ void wn_up_1d(int i, int n, bool periodic, int (&k)[2], float (&w)[2])
 {
-  return (long long)(i / fc) * (ns / fc) + j / fc;
+  const int I = i >> 1;
+  if (i & 1) { k[0] = I; k[1] = I + 1; w[0] = 0.75f; w[1] = 0.25f; }
+  else       { k[0] = I - 1; k[1] = I; w[0] = 0.25f; w[1] = 0.75f; }
+  for (int a = 0; a < 2; a++) {
+    if (periodic) k[a] = (k[a] + n) % n;
+    else k[a] = k[a] < 0 ? 0 : (k[a] >= n ? n - 1 : k[a]);
+  }
+}
+
+__device__ __forceinline__ double wn_up(const float *y, int i, int j, int nr, int ns, int fc)
+{
+  if (fc == 1) return (double)y[(long long)i * ns + j];
+  const int H = nr / 2, W = ns / 2;
+  int ki[2], kj[2];
+  float wi[2], wj[2];
+  wn_up_1d(i, H, false, ki, wi);
+  wn_up_1d(j, W, true, kj, wj);
+  float v = 0.f;
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++) v += wi[a] * wj[b] * y[(long long)ki[a] * W + kj[b]];
+  return (double)v;
+}
+
+// weight with which disk index i reaches network index I (the transpose of
+// wn_up_1d)
+__device__ __forceinline__ float wn_up_weight(int i, int I, int n, bool periodic)
+{
+  int k[2];
+  float w[2];
+  wn_up_1d(i, n, periodic, k, w);
+  return (k[0] == I ? w[0] : 0.f) + (k[1] == I ? w[1] : 0.f);
 }
 
 // T += jac + scale * YSCALE * y (y of the cell's network cell) on the
@@ -619,7 +655,7 @@ __global__ void k_wn_apply(int nr, int ns, int fc, double *__restrict__ T, const
   if (q >= n) return;
   const long long l = q + ns;
   const int i = (int)(l / ns), j = (int)(l % ns);
-  const double t = T[l] + jac[l] + (*scale) * (double)WN_YSCALE * (double)y[wn_coarse(i, j, ns, fc)];
+  const double t = T[l] + jac[l] + (*scale) * (double)WN_YSCALE * wn_up(y, i, j, nr, ns, fc);
   if (t > 0.0) T[l] = t;
 }
 
@@ -653,9 +689,8 @@ __global__ void k_wn_tpred(int nr, int ns, int fc, const double *__restrict__ tk
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= n) return;
   const int i = (int)(q / ns), j = (int)(q % ns);
-  tp[q] = (i >= 1 && i <= nr - 2)
-              ? tk[q] + jac[q] + (*scale) * (double)WN_YSCALE * (double)y[wn_coarse(i, j, ns, fc)]
-              : tk[q];
+  tp[q] = (i >= 1 && i <= nr - 2) ? tk[q] + jac[q] + (*scale) * (double)WN_YSCALE * wn_up(y, i, j, nr, ns, fc)
+                                   : tk[q];
 }
 
 // rs = (A tp - rhs) / sr on the unknowns (zero elsewhere); partial sums of rs^2
@@ -700,9 +735,9 @@ __global__ void k_wn_res_grad(int nr, int ns, const float *__restrict__ rs, SorS
   gf[l] = g;
 }
 
-// output gradient of each network cell: the sum of its fine cells'
-// residual gradients plus wsup * 2/Nc * (y - tgt), as channel 0 of gy16;
-// partial sums of (y - tgt)^2
+// output gradient of each network cell: its fine cells' residual gradients
+// through the transpose of the prolongation, plus wsup * 2/Nc * (y - tgt),
+// as channel 0 of gy16; partial sums of (y - tgt)^2
 __global__ void k_wn_out_grad(int nr, int ns, int fc, const float *__restrict__ gf, const float *__restrict__ y,
                               const float *__restrict__ tgt, float wsup, double inv_nc, bf16 *__restrict__ gy16,
                               double *__restrict__ part)
@@ -714,8 +749,20 @@ __global__ void k_wn_out_grad(int nr, int ns, int fc, const float *__restrict__ 
   if (q < n) {
     const int I = (int)(q / W), J = (int)(q % W);
     float g = 0.f;
-    for (int a = 0; a < fc; a++)
-      for (int b = 0; b < fc; b++) g += gf[(J * fc + b) + (long long)(I * fc + a) * ns];
+    if (fc == 1) {
+      g = gf[q];
+    } else {
+      for (int i = 2 * I - 1; i <= 2 * I + 2; i++) {
+        if (i < 0 || i >= nr) continue;
+        const float wi = wn_up_weight(i, I, H, false);
+        if (wi == 0.f) continue;
+        for (int jj = 2 * J - 1; jj <= 2 * J + 2; jj++) {
+          const int j = (jj + ns) % ns;
+          const float wj = wn_up_weight(j, J, W, true);
+          if (wj != 0.f) g += wi * wj * gf[(long long)i * ns + j];
+        }
+      }
+    }
     const double d = (double)y[q] - (double)tgt[q];
     acc = d * d;
     g += (float)(2.0 * inv_nc * (double)wsup * d);
