@@ -153,31 +153,39 @@ def warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, steps, stream, barr
     from fargo_thorin_gb300 import warmstart as WS
     if not os.path.exists(WARMNET):
         return {"unavailable": "no trained network file"}
-    net = WS.WarmNet(NR, NS, params=WS.WarmNet.load_params(WARMNET), factor=WARMNET_FACTOR)
-    for f, v in snap.items():
-        d.upload(f, v)
-    d.set_sor_state(*snap_sor[:3])
-    d.set_time(snap_time)
-    sys_ = snap_sys.copy()
-    WS.attach(d, net, WS.PREDICT)
-    st0 = d.stats()
-    barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    subs = 0
-    for _ in range(steps):
-        d.algogas(sys_)
-        subs += d.stats().substeps
-    e1.record(stream)
-    barrier()
-    ms = e0.elapsed_time(e1)
-    st1 = d.stats()
-    pred = WS.stats(d).predictions
-    WS.attach(d, None, WS.OFF)
-    t = d.get(8)
-    net.close()
-    per_solve = (st1.sor_sweeps - st0.sor_sweeps) / max(st1.sor_calls - st0.sor_calls, 1)
+
+    def replay(params):
+        """the timed DTs again from the snapshot with a network attached"""
+        net = WS.WarmNet(NR, NS, params=params, factor=WARMNET_FACTOR)
+        for f, v in snap.items():
+            d.upload(f, v)
+        d.set_sor_state(*snap_sor[:3])
+        d.set_time(snap_time)
+        sys_ = snap_sys.copy()
+        WS.attach(d, net, WS.PREDICT)
+        st0 = d.stats()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        subs = 0
+        for _ in range(steps):
+            d.algogas(sys_)
+            subs += d.stats().substeps
+        e1.record(stream)
+        barrier()
+        st1 = d.stats()
+        pred = WS.stats(d).predictions
+        WS.attach(d, None, WS.OFF)
+        net.close()
+        return (e0.elapsed_time(e1), subs, pred,
+                (st1.sor_sweeps - st0.sor_sweeps) / max(st1.sor_calls - st0.sor_calls, 1), d.get(8))
+
+    # control: the same coupling with an untrained network (zero output
+    # layer), i.e. the previous temperature plus one Jacobi step
+    _, _, _, jacobi_per_solve, _ = replay(WS.init_params(0))
+    ms, subs, pred, per_solve, t = replay(WS.WarmNet.load_params(WARMNET))
     return {"plain_sweeps_per_solve": plain_per_solve, "learned_sweeps_per_solve": per_solve,
+            "jacobi_start_sweeps_per_solve": jacobi_per_solve,
             "sweeps_ratio_plain_over_learned": plain_per_solve / per_solve if per_solve else None,
             "learned_value": NR * NS * subs / (ms / 1e3), "learned_ms_per_step": ms / steps, "substeps": subs,
             "network_applications": pred, "network": os.path.relpath(WARMNET, ROOT), "network_factor": WARMNET_FACTOR,
