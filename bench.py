@@ -163,7 +163,7 @@ def warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, steps, stream, barr
         d.set_time(snap_time)
         sys_ = snap_sys.copy()
         WS.attach(d, net, WS.PREDICT)
-        st0 = d.stats()
+        st0, pred0 = d.stats(), WS.stats(d).predictions
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -174,7 +174,7 @@ def warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, steps, stream, barr
         e1.record(stream)
         barrier()
         st1 = d.stats()
-        pred = WS.stats(d).predictions
+        pred = WS.stats(d).predictions - pred0
         WS.attach(d, None, WS.OFF)
         net.close()
         return (e0.elapsed_time(e1), subs, pred,
