@@ -110,15 +110,30 @@ __global__ void __launch_bounds__(128) k_wn_conv(ConvArgs a)
     const int p0 = (int)(tile - ring * tpr) * 128;
     const int i = (int)(ring % a.H);
     const long long rbase = ring - i;                      // b * H
-    // stage rings i-1, i, i+1 over cells p0-1 .. p0+128 (azimuth wrapped)
-    for (int ch = tid; ch < 3 * WN_HALO_W * C8; ch += 128) {
-      const int c8 = ch % C8, rest = ch / C8, pp = rest % WN_HALO_W, rr = rest / WN_HALO_W;
-      const int ii = i + rr - 1;
-      int jj = (p0 - 1 + pp) % a.W;
-      if (jj < 0) jj += a.W;
-      uint4 val = make_uint4(0u, 0u, 0u, 0u);
-      if (ii >= 0 && ii < a.H) val = *(const uint4 *)(a.in + ((rbase + ii) * a.W + jj) * CIN + c8 * 8);
-      *(uint4 *)(sA + ((c8 * 3 + rr) * WN_HALO_W + pp) * 16) = val;
+    // stage rings i-1, i, i+1 over cells p0-1 .. p0+128 (azimuth wrapped):
+    // every load of the thread is issued before the first store, so their
+    // latencies overlap
+    constexpr int NCH = 3 * WN_HALO_W * C8, PER = (NCH + 127) / 128;
+    uint4 val[PER];
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+      const int ch = tid + 128 * k;
+      val[k] = make_uint4(0u, 0u, 0u, 0u);
+      if (ch < NCH) {
+        const int c8 = ch % C8, rest = ch / C8, pp = rest % WN_HALO_W, rr = rest / WN_HALO_W;
+        const int ii = i + rr - 1;
+        int jj = p0 - 1 + pp;
+        jj = jj < 0 ? jj + a.W : (jj >= a.W ? jj % a.W : jj);
+        if (ii >= 0 && ii < a.H) val[k] = __ldg((const uint4 *)(a.in + ((rbase + ii) * a.W + jj) * CIN + c8 * 8));
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+      const int ch = tid + 128 * k;
+      if (ch < NCH) {
+        const int c8 = ch % C8, rest = ch / C8, pp = rest % WN_HALO_W, rr = rest / WN_HALO_W;
+        *(uint4 *)(sA + ((c8 * 3 + rr) * WN_HALO_W + pp) * 16) = val[k];
+      }
     }
     umma::fence_smem_async();
     __syncthreads();
