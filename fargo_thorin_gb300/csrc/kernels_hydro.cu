@@ -672,7 +672,7 @@ __global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__r
 {
   const int ns = g.ns, half = ns >> 1;
   const int i = blockIdx.y + 1;
-  double a = 0.0;
+  double a = 0.0, aj = 0.0;
   for (int m = 0; m < SOR_CPT; m++) {
     const int j = blockIdx.x * blockDim.x * SOR_CPT + m * blockDim.x + threadIdx.x;
     if (j < ns) {
@@ -680,20 +680,32 @@ __global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__r
       const int ljp = (j == ns - 1) ? i * ns : l + 1;
       const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
       const size_t q = sor_pidx(i, j, half);
-      a += fabs(sor_resid_at(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm, q));
-      cw[q] = div_fast(omega, ml[q]);              // the sweeps' update is resid * omega / ml
+      const double r = fabs(sor_resid_at(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm, q));
+      const double w = div_fast(omega, ml[q]);     // the sweeps' update is resid * omega / ml
+      cw[q] = w;
+      a += r;
+      aj += r * w;                                 // omega |resid / Ml|: the warm start's input scale
     }
   }
   a = block_reduce(a, OpAdd(), 0.0);
+  aj = block_reduce(aj, OpAdd(), 0.0);
   const unsigned nb = gridDim.x * gridDim.y;
   const int b = blockIdx.x + blockIdx.y * gridDim.x;
-  if (threadIdx.x == 0) c.part[b] = a;
+  if (threadIdx.x == 0) {
+    c.part[b] = a;
+    c.part[nb + b] = aj;
+  }
   if (sor_last_block(c.ticket, nb)) {
     __threadfence();
-    double s = 0.0;
-    for (unsigned k = threadIdx.x; k < nb; k += blockDim.x) s += __ldcg(c.part + k);   // L2, past L1
+    double s = 0.0, sj = 0.0;
+    for (unsigned k = threadIdx.x; k < nb; k += blockDim.x) {
+      s += __ldcg(c.part + k);                     // L2, past L1
+      sj += __ldcg(c.part + nb + k);
+    }
     s = block_reduce(s, OpAdd(), 0.0);
+    sj = block_reduce(sj, OpAdd(), 0.0);
     if (threadIdx.x == 0) {
+      *c.jscale = sj;
       *c.normres0 = s;
       *c.done = 0;
       *c.niter = 0;

@@ -17,7 +17,7 @@
 // learned SOR warm start (warmnet.cu)
 int wn_sor_predict(thorin_warmnet *n, int nr, int ns, int fc, double *T, const double *ml, const double *mlip,
                    const double *mlim, const double *mljp, const double *mljm, const double *rhs, const double *prev,
-                   double *jac, cudaStream_t s);
+                   double *jac, const double *jscale, double omega, cudaStream_t s);
 int wn_sor_train(thorin_warmnet *n, int nr, int ns, int fc, const double *tk, const double *tconv, const double *ml,
                  const double *mlip, const double *mlim, const double *mljp, const double *mljm, const double *rhs,
                  const double *prev, double *jac, float lr, double *scratch, cudaStream_t s);
@@ -445,6 +445,7 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   d->sor.part = sp + 8;
   d->sor.normres0 = sp;
   d->sor.normres = sp + 1;
+  d->sor.jscale = sp + 2;
   d->sor.ipart = ip + 8;
   d->sor.done = ip;
   d->sor.niter = ip + 1;
@@ -1478,7 +1479,7 @@ static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *ca
     CUCHK(cudaMemcpyAsync(d->tbackup, d->temper, (size_t)d->nr * d->ns * sizeof(double), cudaMemcpyDeviceToDevice,
                           d->s));
     RCHK(wn_sor_predict(d->ws_net, d->nr, d->ns, d->ws_f, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm,
-                        d->rhs, d->ws_prev, d->ws_jac, d->s));
+                        d->rhs, d->ws_prev, d->ws_jac, d->sor.jscale, omega, d->s));
     d->ws_st.predictions++;
   }
   int first = 1, chunk = hint > 0 ? hint : 4;

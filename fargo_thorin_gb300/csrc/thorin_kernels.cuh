@@ -37,6 +37,7 @@ struct SorCtl {
   double *normres0;
   double *normres;
   int *changed;
+  double *jscale;         // sum over the start of |resid| * omega/Ml (k_sor_resid0)
 };
 
 // Transport scratch (device fields).

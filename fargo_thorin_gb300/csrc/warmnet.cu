@@ -1031,17 +1031,23 @@ static int wn_check_err(thorin_warmnet *n)
 // (nr/fc) x (ns/fc); jac has the disk's nr x ns cells.
 int wn_sor_predict(thorin_warmnet *n, int nr, int ns, int fc, double *T, const double *ml, const double *mlip,
                    const double *mlim, const double *mljp, const double *mljm, const double *rhs, const double *prev,
-                   double *jac, cudaStream_t s)
+                   double *jac, const double *jscale, double omega, cudaStream_t s)
 {
   // dscal: [2] mean |r/Ml| of the start, [3] mean |r|, [4] residual loss,
   // [5] supervised loss, [0] total loss; partials from dscal + 8
   SorSys m{ml, mlip, mlim, mljp, mljm, rhs};
   double *part = n->dscal + 8;
   const int sb = 2 * n->nsm;
-  k_wn_scale<<<sb, 256, 0, s>>>(nr, ns, T, m, part);
-  k_wn_sum<<<1, 32, 0, s>>>(part, sb, 1.0 / ((double)(nr - 2) * ns), n->dscal + 2);
+  if (jscale) {            // sum of omega |r / Ml| from the solve's own residual pass
+    k_wn_sum<<<1, 32, 0, s>>>(jscale, 1, 1.0 / (omega * (double)(nr - 2) * ns), n->dscal + 2);
+    g_thorin_launches += 1;
+  } else {
+    k_wn_scale<<<sb, 256, 0, s>>>(nr, ns, T, m, part);
+    k_wn_sum<<<1, 32, 0, s>>>(part, sb, 1.0 / ((double)(nr - 2) * ns), n->dscal + 2);
+    g_thorin_launches += 2;
+  }
   k_wn_features<<<nblk((long long)(nr / fc) * (ns / fc)), 256, 0, s>>>(nr, ns, fc, T, m, n->dscal + 2, prev, n->x, jac);
-  g_thorin_launches += 3;
+  g_thorin_launches += 1;
   RCHK_WN(wn_forward(n, 1, s));
   k_wn_apply<<<nblk((long long)(nr - 2) * ns), 256, 0, s>>>(nr, ns, fc, T, jac, n->y, n->dscal + 2);
   g_thorin_launches++;
