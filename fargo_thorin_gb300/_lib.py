@@ -42,6 +42,8 @@ SIGNATURES = {
     "thorin_integrals_static": (C.c_int, [_D, _D, _D, _D, _D, _D, _D, _D, C.c_int, C.c_int, C.c_double, _D, _P]),
     "thorin_selftest_division": (C.c_int, [C.c_longlong, C.c_ulonglong, C.c_double, C.POINTER(C.c_ulonglong),
                                            C.POINTER(C.c_ulonglong)]),
+    "thorin_selftest_slope_division": (C.c_int, [C.c_longlong, C.c_ulonglong, C.c_double,
+                                                 C.POINTER(C.c_ulonglong)]),
     "thorin_selftest_fp64_peak": (C.c_int, [_D]),
     "thorin_gpu_request_torques": (C.c_int, [_P]),
     "thorin_gpu_init_pebbles": (C.c_int, [_P]),

@@ -645,6 +645,36 @@ __device__ __forceinline__ double sor_resid_at(const double *T, const double *ml
   return __fma_rn(T[ljm], mljm[q], r);
 }
 
+#ifndef SOR_CPT
+#define SOR_CPT 4        // cells of one colour per thread
+#endif
+#define SOR_BX 128       // threads per SOR block
+
+// Block sums of the pass's L1 residual and "changed" count, result in
+// thread 0.  The FP64 pipe bounds the SOR pass, so the first level goes
+// through shared memory: warp 0 adds the SOR_BX / 32 values of its lane's
+// column, then one shuffle tree finishes.  That is SOR_BX / 32 + 4 warp-wide
+// FP64 adds per block instead of 5 (SOR_BX / 32 + 1).  Fixed order.
+__device__ __forceinline__ void sor_block_sums(double &a, int &c)
+{
+  __shared__ double sa[SOR_BX];
+  __shared__ int sc[SOR_BX];
+  sa[threadIdx.x] = a;
+  sc[threadIdx.x] = c;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double s = sa[threadIdx.x];
+    int t = sc[threadIdx.x];
+#pragma unroll
+    for (int k = 1; k < SOR_BX / 32; k++) {
+      s += sa[threadIdx.x + 32 * k];
+      t += sc[threadIdx.x + 32 * k];
+    }
+    a = warp_reduce(s, OpAdd());
+    c = warp_reduce(t, OpAddI());
+  }
+}
+
 // Sum of the block partials by the block holding the last ticket; every
 // block adds its partial first (no block ever waits on another).
 __device__ __forceinline__ bool sor_last_block(unsigned int *ticket, unsigned nb)
@@ -658,11 +688,6 @@ __device__ __forceinline__ bool sor_last_block(unsigned int *ticket, unsigned nb
   __syncthreads();
   return last;
 }
-
-#ifndef SOR_CPT
-#define SOR_CPT 4        // cells of one colour per thread
-#endif
-#define SOR_BX 128       // threads per SOR block
 
 __global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__restrict__ T,
                                                     const double *__restrict__ ml, const double *__restrict__ mlip,
@@ -680,7 +705,7 @@ __global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__r
       const int ljp = (j == ns - 1) ? i * ns : l + 1;
       const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
       const size_t q = sor_pidx(i, j, half);
-      const double r = fabs(sor_resid_at(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm, q));
+      const double r = abs_i(sor_resid_at(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm, q));
       const double w = div_fast(omega, ml[q]);     // the sweeps' update is resid * omega / ml
       cw[q] = w;
       a += r;
@@ -773,7 +798,7 @@ __global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict_
         const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
         const size_t q = pbase + k;
         const double resid = sor_resid_at(T, ml, mlip, mlim, mljp, mljm, rhs, l, l + ns, l - ns, ljp, ljm, q);
-        a += fabs(resid);
+        a += abs_i(resid);
         const double c = cw[q];
         const double tn = __fma_rn(-resid, c, T[l]);     // T -= omega resid / Ml
         T[l] = tn;
@@ -781,8 +806,8 @@ __global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict_
       }
     }
   }
-  a = block_reduce(a, OpAdd(), 0.0);
-  const int chs = block_reduce(ch, OpAddI(), 0);
+  sor_block_sums(a, ch);
+  const int chs = ch;
   const unsigned nb = gridDim.x;
   const int b = blockIdx.x;
   const int slot = col * nb + b;
@@ -904,7 +929,7 @@ __device__ __forceinline__ double vl_slope_r(const DevGrid &g, const double *q, 
   const double dqm = (q[l] - q[l - ns]) * g.r.InvDiffRmed[i];
   const double dqp = (q[l + ns] - q[l]) * g.r.InvDiffRmed[i + 1];
   const double p = dqp * dqm;
-  return (__double_as_longlong(p) > 0LL) ? div_fast(2.0 * p, dqp + dqm) : 0.0;   // p > 0.0
+  return (__double_as_longlong(p) > 0LL) ? div_slope(2.0 * p, dqp + dqm) : 0.0;  // p > 0.0
 }
 
 
@@ -1014,7 +1039,7 @@ __device__ __forceinline__ double azi_vl_slope_raw(double qm, double q0, double 
   const double s = dqp + dqm;
   const bool pos = __double_as_longlong(p) > 0LL;                 // p > 0.0
   const bool nz = (__double_as_longlong(s) << 1) != 0LL;          // s != 0.0
-  return (pos && nz) ? div_fast(p, s) : 0.0;
+  return (pos && nz) ? div_slope(p, s) : 0.0;
 }
 
 template <int NQ>

@@ -107,6 +107,33 @@ __device__ T block_reduce(T v, Op op, T identity)
   return v;
 }
 
+// Quotient for the van Leer slopes only.  The harmonic-mean slope
+// 2 dq- dq+ / (dq- + dq+) enters a face value as a correction of at most
+// half a cell width times the slope, beside the cell value itself, so a
+// relative error e of the slope moves the face value by at most
+// e |dq| dx / |q|.  The reciprocal estimate with one Newton-Raphson step,
+// y = y + y(1 - d y), times x is two FP64 instructions shorter than
+// div_fast; thorin_selftest_slope_division measures its distance from IEEE
+// division on the GPU.  Same exponent guard as div_fast.
+__device__ __forceinline__ double div_slope(double x, double d)
+{
+  const unsigned ex = ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
+  const unsigned ed = ((unsigned)__double2hiint(d) >> 20) & 0x7ffu;
+  if (((ex - 523u) < 1001u || ex == 0u) && (ed - 523u) < 1001u) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(d));
+    y = __fma_rn(y, __fma_rn(-d, y, 1.0), y);
+    return x * y;
+  }
+  return x / d;
+}
+
+// |x| by clearing the sign bit on the integer pipe (same bits as fabs).
+__device__ __forceinline__ double abs_i(double x)
+{
+  return __hiloint2double(__double2hiint(x) & 0x7fffffff, __double2loint(x));
+}
+
 // x^3 correctly rounded (Dekker two-product with fma): the reference uses
 // pow(T, 3.0) (EnergySources.c:95,590), which glibc returns correctly
 // rounded in all but vanishingly rare cases.

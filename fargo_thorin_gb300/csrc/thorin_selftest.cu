@@ -1,5 +1,5 @@
-// thorin_selftest.cu -- on-device check of the kernels' division routine
-// (div_fast) against IEEE division.
+// thorin_selftest.cu -- on-device checks of the kernels' division routines
+// (div_fast, div_slope) against IEEE division, and the FP64 FMA peak.
 #include <string>
 #include "thorin_kernels.cuh"
 
@@ -75,6 +75,42 @@ __global__ void __launch_bounds__(256) k_selftest_dfma(double *__restrict__ out,
     x4 = __fma_rn(x4, a, b); x5 = __fma_rn(x5, a, b); x6 = __fma_rn(x6, a, b); x7 = __fma_rn(x7, a, b);
   }
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+__global__ void k_selftest_slope_division(long long n, unsigned long long seed, double emax,
+                                          unsigned long long *__restrict__ out)
+{
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const double x = st_value(seed + 2ULL * (unsigned long long)t, emax);
+  const double d = st_value(seed + 2ULL * (unsigned long long)t + 1ULL, emax);
+  const long long a = __double_as_longlong(x / d), b = __double_as_longlong(div_slope(x, d));
+  const unsigned long long u = (unsigned long long)(a > b ? a - b : b - a);
+  if (u) atomicMax(out, u);
+}
+
+extern "C" int thorin_selftest_slope_division(long long n, unsigned long long seed, double max_exponent,
+                                              unsigned long long *max_ulp)
+{
+  if (n < 1 || !max_ulp || !(max_exponent >= 0.0 && max_exponent <= 1000.0)) {
+    g_last_error = "selftest_slope_division: n >= 1, 0 <= max_exponent <= 1000 and an output pointer required";
+    return THORIN_ERR_ARG;
+  }
+  unsigned long long *dev = nullptr, host = 0ULL;
+  cudaError_t e = cudaMalloc((void **)&dev, sizeof(host));
+  if (e == cudaSuccess) e = cudaMemset(dev, 0, sizeof(host));
+  if (e == cudaSuccess) {
+    k_selftest_slope_division<<<(unsigned)((n + 255) / 256), 256>>>(n, seed, max_exponent, dev);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(&host, dev, sizeof(host), cudaMemcpyDeviceToHost);
+  if (dev) cudaFree(dev);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("selftest_slope_division: ") + cudaGetErrorString(e);
+    return THORIN_ERR_CUDA;
+  }
+  *max_ulp = host;
+  return THORIN_OK;
 }
 
 extern "C" int thorin_selftest_fp64_peak(double *gflops)

@@ -347,6 +347,13 @@ int thorin_gpu_get_torques(thorin_disk *d, thorin_torque *out, int max, int *n);
 int thorin_selftest_division(long long n, unsigned long long seed, double max_exponent,
                              unsigned long long *mismatches, unsigned long long *max_ulp);
 
+/* Self-test of the van Leer slopes' shorter division (reciprocal estimate
+ * and one Newton-Raphson step, no correction) against IEEE division: n
+ * random quotients as above; returns the largest difference in ulps.  No
+ * counterpart in the reference. */
+int thorin_selftest_slope_division(long long n, unsigned long long seed, double max_exponent,
+                                   unsigned long long *max_ulp);
+
 /* FP64 fused multiply-add throughput of the current GPU in GFLOP/s (two
  * flops per FMA), measured with a short kernel of independent FMA chains:
  * the FP64-pipe ceiling for the roofline of the kernels.  No counterpart in

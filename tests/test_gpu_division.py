@@ -18,3 +18,17 @@ def test_division_matches_ieee(max_exponent, seed):
     _lib.check(lib.thorin_selftest_division(n, seed, max_exponent, C.byref(mis), C.byref(ulp)), "selftest_division")
     assert ulp.value <= 1
     assert mis.value <= n // 1000000
+
+
+@pytest.mark.parametrize("max_exponent,seed", [(40.0, 4), (300.0, 5)])
+def test_slope_division_bound(max_exponent, seed):
+    """The van Leer slopes' division (no Markstein correction) stays within
+    2^14 ulp of IEEE division, a relative error below 2^-38 (measured on
+    GB300: 8696 ulp at most in 2^26 quotients)."""
+    from fargo_thorin_gb300 import _lib
+    lib = _lib.load()
+    ulp = C.c_ulonglong()
+    _lib.check(lib.thorin_selftest_slope_division(1 << 26, seed, max_exponent, C.byref(ulp)),
+               "selftest_slope_division")
+    print("slope division: max", ulp.value, "ulp")
+    assert ulp.value <= 16384
