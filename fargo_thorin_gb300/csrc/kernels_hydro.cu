@@ -1032,9 +1032,10 @@ __global__ void __launch_bounds__(256) k_azi_rings(DevGrid g, const double *__re
 #define AZ_HALO 4
 #define AZ_TMAX 512
 
-__device__ __forceinline__ double azi_vl_slope_raw(double qm, double q0, double qp)
+// Slope from the differences dqm = q_j - q_{j-1} and dqp = q_{j+1} - q_j;
+// each thread forms its own dqm and reads dqp from its right neighbour.
+__device__ __forceinline__ double azi_vl_slope_d(double dqm, double dqp)
 {
-  const double dqm = q0 - qm, dqp = qp - q0;
   const double p = dqp * dqm;
   const double s = dqp + dqm;
   const bool pos = __double_as_longlong(p) > 0LL;                 // p > 0.0
@@ -1079,10 +1080,13 @@ __global__ void __launch_bounds__(AZ_TMAX) k_azimuthal(DevGrid g, AziIO io, cons
     const double rho = q[NQ - 1];
     s_a[t] = rho;
     __syncthreads();
-    const double drho = azi_vl_slope_raw(s_a[tm], rho, s_a[tp]);
-    s_b[t] = drho;
+    const double drm = rho - s_a[tm];
+    s_b[t] = drm;
     __syncthreads();
-    const double rs = up ? __fma_rn(cs, s_b[tm], s_a[tm]) : __fma_rn(-cs, drho, rho);
+    const double drho = azi_vl_slope_d(drm, s_b[tp]);
+    s_c[t] = drho;
+    __syncthreads();
+    const double rs = up ? __fma_rn(cs, s_c[tm], s_a[tm]) : __fma_rn(-cs, drho, rho);
     const double cf = dxrad * rs * v;              // flux = dxrad Q* RhoStar v
     const double rcp = div_fast(1.0, rho + 1e-20); // 1 / (RhoInt + 1e-20)
     __syncthreads();
@@ -1094,19 +1098,22 @@ __global__ void __launch_bounds__(AZ_TMAX) k_azimuthal(DevGrid g, AziIO io, cons
       __syncthreads();
       double qs;
       if (k < NQ - 1) {
-        const double dq = azi_vl_slope_raw(s_a[tm], w, s_a[tp]);
-        s_b[t] = dq;
+        const double dm = w - s_a[tm];
+        s_b[t] = dm;
         __syncthreads();
-        qs = up ? __fma_rn(cs, s_b[tm], s_a[tm]) : __fma_rn(-cs, dq, w);
+        const double dq = azi_vl_slope_d(dm, s_b[tp]);
+        s_c[t] = dq;
+        __syncthreads();
+        qs = up ? __fma_rn(cs, s_c[tm], s_a[tm]) : __fma_rn(-cs, dq, w);
       } else {
         // the density's own quotient rho / (rho + 1e-20) is 1 to within
         // 1e-20 / rho: its slope term is below rounding
         qs = up ? s_a[tm] : w;
       }
       const double F = qs * cf;
-      s_c[t] = F;
+      s_b[t] = F;                                  // every read of s_b is behind a barrier
       __syncthreads();
-      q[k] = __fma_rn(F - s_c[tp], invsurf, q[k]);
+      q[k] = __fma_rn(F - s_b[tp], invsurf, q[k]);
     }
   }
   const int x = t - AZ_HALO;
