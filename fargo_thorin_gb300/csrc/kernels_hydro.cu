@@ -856,9 +856,12 @@ __global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict_
     *c.normres = s;
     *c.changed = cs;
     *c.niter = n;
-    if (s < eps * r0 || s < TH_SORMIN || cs == 0) *c.done = 1;
-    else if (n >= maxiters) *c.done = 2;
+    const int dn = (s < eps * r0 || s < TH_SORMIN || cs == 0) ? 1 : (n >= maxiters ? 2 : 0);
+    if (dn) *c.done = dn;
     *c.ticket = 0u;
+    // the sweep loop of the graph ends with the first sweep that sets done;
+    // n >= maxiters always does, so the loop is finite
+    if (c.has_cond) cudaGraphSetConditional(c.cond, dn == 0 ? 1u : 0u);
   }
 }
 

@@ -8,7 +8,6 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
-#include <map>
 #include <string>
 #include <vector>
 #include "thorin_kernels.cuh"
@@ -164,8 +163,10 @@ struct thorin_disk {
   double *ws_prev = nullptr;     // the previous solve's update T_conv - T_start (network input)
   double *ws_jac = nullptr;      // the Jacobi step of the solve's start, per cell
   int ws_f = 1;                  // disk cells per network cell along each axis (1 or 2)
-  // SOR chunks of n sweeps, captured once as CUDA graphs and replayed
-  std::map<int, cudaGraphExec_t> sor_graphs;
+  // the SOR sweep loop: one CUDA graph whose WHILE node repeats the two
+  // colour passes until the completion step clears its condition
+  cudaGraphExec_t sor_loop = nullptr;
+  int sor_loop_k = 8;            // sweeps per run of the loop body
   double heatsrc[THORIN_MAXPLANETS];
   int heatsrc_index[THORIN_MAXPLANETS], heatsrc_max;
   double gm1, gg1, drin, drout, invdphi, lr01, lr12, taueff_c, tirr4fac, rstar;
@@ -451,6 +452,12 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   d->sor.niter = ip + 1;
   d->sor.changed = ip + 2;
   d->sor.ticket = d->ticket;
+  d->sor.cond = 0;
+  d->sor.has_cond = 0;
+  if (const char *ek = getenv("THORIN_SOR_LOOP_SWEEPS")) {
+    const int k = atoi(ek);
+    if (k >= 1 && k <= 64) d->sor_loop_k = k;
+  }
   const int ng = (sb + SOR_GROUP - 1) / SOR_GROUP;
   RCHK(dalloc(d, (void **)&d->sor.gpart, (size_t)ng * sizeof(double)));
   RCHK(dalloc(d, (void **)&d->sor.gipart, (size_t)ng * sizeof(int)));
@@ -573,7 +580,7 @@ extern "C" int thorin_gpu_destroy(thorin_disk *d)
   cudaFreeHost(d->scal_h);
   cudaFreeHost(d->iscal_h);
   cudaFreeHost(d->csmean_h);
-  for (auto &kv : d->sor_graphs) cudaGraphExecDestroy(kv.second);
+  if (d->sor_loop) cudaGraphExecDestroy(d->sor_loop);
   for (int q = 0; q < 4; q++) cudaEventDestroy(d->ev[q]);
   if (d->s_peb) {
     cudaStreamSynchronize(d->s_peb);
@@ -1443,33 +1450,58 @@ extern "C" int thorin_gpu_get_torques(thorin_disk *d, thorin_torque *out, int ma
 
 // `count` SOR sweeps on the disk's stream: a CUDA graph of the 2*count pass
 // launches, captured the first time this count is asked for.
-static int sor_chunk(thorin_disk *d, int count)
+// The sweep loop as one graph: a WHILE conditional node (default value 1 at
+// every launch) whose body is sor_loop_k red-black sweeps.  Each sweep's
+// completion step sets the condition from the exit tests (converged, or the
+// iteration cap): 0 with done, else 1.  Sweeps after the one that set done
+// return at once and leave the condition at 0, so one launch runs the sweeps
+// the solve needs plus fewer than sor_loop_k no-op sweeps, with no host round
+// trip.  A body of several sweeps keeps the loop's per-run restart, which
+// costs more than a kernel node of a linear graph, off most sweeps
+// (THORIN_SOR_LOOP_SWEEPS, 1..64, sets sor_loop_k; default 8, measured
+// level with 16 and ahead of 2 and 4 on the 1024x3072 disk).
+static int sor_loop_graph(thorin_disk *d)
 {
-  cudaGraphExec_t ge;
-  auto it = d->sor_graphs.find(count);
-  if (it == d->sor_graphs.end()) {
-    cudaGraph_t gr;
-    CUCHK(cudaStreamBeginCapture(d->s, cudaStreamCaptureModeThreadLocal));
-    hydro_sor_sweeps(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, d->sor,
-                     d->p.sor_eps, count, d->p.sor_maxiters, d->s);
-    CUCHK(cudaStreamEndCapture(d->s, &gr));
-    const cudaError_t e = cudaGraphInstantiate(&ge, gr, 0);
-    cudaGraphDestroy(gr);
-    CUCHK(e);
-    d->sor_graphs[count] = ge;
-  } else {
-    ge = it->second;
+  if (d->sor_loop) return THORIN_OK;
+  cudaGraph_t gr;
+  CUCHK(cudaGraphCreate(&gr, 0));
+  cudaGraphConditionalHandle h;
+  cudaGraphNodeParams np = {};
+  cudaGraphNode_t node;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, gr, 1u, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess) {
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    e = cudaGraphAddNode(&node, gr, nullptr, nullptr, 0, &np);
   }
-  CUCHK(cudaGraphLaunch(ge, d->s));
-  g_thorin_launches += 2LL * count;
+  if (e == cudaSuccess)
+    e = cudaStreamBeginCaptureToGraph(d->s, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    SorCtl c = d->sor;
+    c.cond = h;
+    c.has_cond = 1;
+    hydro_sor_sweeps(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, c,
+                     d->p.sor_eps, d->sor_loop_k, d->p.sor_maxiters, d->s);
+    cudaGraph_t body;
+    e = cudaStreamEndCapture(d->s, &body);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&d->sor_loop, gr, 0);
+  cudaGraphDestroy(gr);
+  if (e != cudaSuccess) {
+    d->sor_loop = nullptr;
+    g_last_error = std::string("SOR loop graph: ") + cudaGetErrorString(e);
+    return THORIN_ERR_CUDA;
+  }
   return THORIN_OK;
 }
 
-// SuccessiveOverrelaxation driver: residual, then sweeps launched in chunks;
-// converged sweeps turn later launches into no-ops.
-static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *capped, bool learned = false)
+// SuccessiveOverrelaxation driver: the start residual (and the learned warm
+// start), then the sweep loop graph; one read of the exit state per solve.
+static int sor_solve(thorin_disk *d, double omega, int *niter, int *capped, bool learned = false)
 {
-  const thorin_params &p = d->p;
   // normres0 and the threshold always come from the start temperature as
   // the reference has it; a learned start only moves T before the sweeps
   hydro_sor_resid0(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, omega, d->sor, d->s);
@@ -1482,32 +1514,28 @@ static int sor_solve(thorin_disk *d, double omega, int hint, int *niter, int *ca
                         d->rhs, d->ws_prev, d->ws_jac, d->sor.jscale, omega, d->s));
     d->ws_st.predictions++;
   }
-  int first = 1, chunk = hint > 0 ? hint : 4;
-  *capped = 0;
-  for (;;) {
-    if (d->timing) CUCHK(cudaEventRecord(d->ev[0], d->s));
-    RCHK(sor_chunk(d, chunk));
-    KCHECK("SOR sweep kernels");
-    if (d->timing) CUCHK(cudaEventRecord(d->ev[1], d->s));
-    CUCHK(cudaMemcpyAsync(d->iscal_h + IS_SOR_DONE, d->sor.done, 2 * sizeof(int), cudaMemcpyDeviceToHost, d->s));
-    CUCHK(cudaStreamSynchronize(d->s));
-    const int done = d->iscal_h[IS_SOR_DONE];
-    if (d->timing) {
-      float ms = 0.f;
-      CUCHK(cudaEventElapsedTime(&ms, d->ev[0], d->ev[1]));
-      d->st.sor_time_ms += ms;
-      const int did = done ? d->iscal_h[IS_SOR_DONE + 1] - first + 1 : chunk;
-      d->st.sor_passes += 2LL * (did > 0 ? did : 0);
-    }
-    if (done) {
-      *niter = d->iscal_h[IS_SOR_DONE + 1];
-      *capped = (done == 2);
-      return THORIN_OK;
-    }
-    first += chunk;
-    if (first > p.sor_maxiters) { *niter = p.sor_maxiters; *capped = 1; return THORIN_OK; }
-    chunk = chunk < 64 ? 2 * chunk : 64;
+  RCHK(sor_loop_graph(d));
+  if (d->timing) CUCHK(cudaEventRecord(d->ev[0], d->s));
+  CUCHK(cudaGraphLaunch(d->sor_loop, d->s));
+  KCHECK("SOR sweep kernels");
+  if (d->timing) CUCHK(cudaEventRecord(d->ev[1], d->s));
+  CUCHK(cudaMemcpyAsync(d->iscal_h + IS_SOR_DONE, d->sor.done, 2 * sizeof(int), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  const int done = d->iscal_h[IS_SOR_DONE], n = d->iscal_h[IS_SOR_DONE + 1];
+  if (!done || n < 1) {
+    g_last_error = "SOR loop ended without an exit decision";
+    return THORIN_ERR_CUDA;
   }
+  *niter = n;
+  *capped = (done == 2);
+  g_thorin_launches += 2LL * n;
+  if (d->timing) {
+    float ms = 0.f;
+    CUCHK(cudaEventElapsedTime(&ms, d->ev[0], d->ev[1]));
+    d->st.sor_time_ms += ms;
+    d->st.sor_passes += 2LL * n;
+  }
+  return THORIN_OK;
 }
 
 // IterateRelaxationParameter (EnergySources.c:340-403).
@@ -1525,7 +1553,7 @@ static int iterate_relaxation(thorin_disk *d)
   for (int outer = 0;; outer++) {
     if (outer >= 1000) { g_last_error = "omega calibration did not settle"; return THORIN_ERR_OMEGA; }
     for (int n = 0; n <= nsplit; n++) {
-      RCHK(sor_solve(d, omega, d->Niterbest < p.sor_maxiters ? d->Niterbest : 4, &Niter, &capped));
+      RCHK(sor_solve(d, omega, &Niter, &capped));
       d->st.sor_sweeps += Niter;
       if (Niter == d->Niterbest) count++;
       if (Niter < d->Niterbest) { d->Niterbest = Niter; d->omegabest = omega; }
@@ -1594,7 +1622,7 @@ static int energy_step(thorin_disk *d, double dt)
   const bool train = d->ws_net && d->ws_mode == THORIN_WS_TRAIN;
   const size_t tbytes = (size_t)d->nr * d->ns * sizeof(double);
   if (train) CUCHK(cudaMemcpyAsync(d->tbackup, d->temper, tbytes, cudaMemcpyDeviceToDevice, d->s));
-  RCHK(sor_solve(d, d->omega, d->Niterlast, &Niter, &capped, true));
+  RCHK(sor_solve(d, d->omega, &Niter, &capped, true));
   if (train) {
     // fit the network to this solve; energy_new is free until the energy is formed below
     RCHK(wn_sor_train(d->ws_net, d->nr, d->ns, d->ws_f, d->tbackup, d->temper, d->ml, d->mlip, d->mlim, d->mljp,

@@ -38,6 +38,10 @@ struct SorCtl {
   double *normres;
   int *changed;
   double *jscale;         // sum over the start of |resid| * omega/Ml (k_sor_resid0)
+  // Condition of the graph's WHILE node around the sweeps: the completion
+  // step sets it to 0 together with done (has_cond 0: no such node)
+  cudaGraphConditionalHandle cond;
+  int has_cond;
 };
 
 // Transport scratch (device fields).

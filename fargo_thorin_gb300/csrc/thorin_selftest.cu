@@ -1,5 +1,6 @@
 // thorin_selftest.cu -- on-device checks of the kernels' division routines
-// (div_fast, div_slope) against IEEE division, and the FP64 FMA peak.
+// (div_fast, div_slope) against IEEE division, conditional graph nodes, and
+// the FP64 FMA peak.
 #include <string>
 #include "thorin_kernels.cuh"
 
@@ -61,6 +62,89 @@ extern "C" int thorin_selftest_division(long long n, unsigned long long seed, do
   }
   *mismatches = host[0];
   *max_ulp = host[1];
+  return THORIN_OK;
+}
+
+// Conditional graph nodes as the SOR sweep loop uses them.  Every part is
+// bounded: an IF node runs its body at most once, and the WHILE check runs
+// only after the IF checks have shown that a kernel's condition value of 0
+// skips the body and 1 runs it.
+__global__ void k_st_setcond(cudaGraphConditionalHandle h, unsigned v)
+{
+  if (threadIdx.x == 0) cudaGraphSetConditional(h, v);
+}
+
+__global__ void k_st_count(int *c, cudaGraphConditionalHandle h, int limit, int loop)
+{
+  if (threadIdx.x == 0) {
+    const int n = ++c[0];
+    if (loop) cudaGraphSetConditional(h, n < limit ? 1u : 0u);
+  }
+}
+
+// One graph: k_st_setcond(v), then IF (body k_st_count) when loop == 0, or
+// WHILE with default 1 (body k_st_count, which clears the condition at
+// `limit`) when loop == 1.  Returns the count.
+static cudaError_t st_cond_graph(int loop, unsigned v, int limit, int *dev, int *count)
+{
+  cudaGraph_t g;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e != cudaSuccess) return e;
+  cudaGraphConditionalHandle h;
+  cudaGraphNode_t n1, n2, n3;
+  cudaGraphNodeParams np = {};
+  cudaKernelNodeParams kp = {};
+  void *a1[] = {&h, &v};
+  void *a2[] = {&dev, &h, &limit, &loop};
+  cudaGraphExec_t ge = nullptr;
+  e = cudaGraphConditionalHandleCreate(&h, g, loop ? 1u : 0u, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess && !loop) {
+    kp.func = (void *)k_st_setcond;
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(32);
+    kp.kernelParams = a1;
+    e = cudaGraphAddKernelNode(&n1, g, nullptr, 0, &kp);
+  }
+  if (e == cudaSuccess) {
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = loop ? cudaGraphCondTypeWhile : cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    e = cudaGraphAddNode(&n2, g, loop ? nullptr : &n1, nullptr, loop ? 0 : 1, &np);
+  }
+  if (e == cudaSuccess) {
+    kp.func = (void *)k_st_count;
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(32);
+    kp.kernelParams = a2;
+    e = cudaGraphAddKernelNode(&n3, np.conditional.phGraph_out[0], nullptr, 0, &kp);
+  }
+  if (e == cudaSuccess) e = cudaMemset(dev, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+  if (e == cudaSuccess) e = cudaGraphLaunch(ge, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(count, dev, sizeof(int), cudaMemcpyDeviceToHost);
+  if (ge) cudaGraphExecDestroy(ge);
+  cudaGraphDestroy(g);
+  return e;
+}
+
+extern "C" int thorin_selftest_graph_conditional(int *if_zero, int *if_one, int *while_count)
+{
+  if (!if_zero || !if_one || !while_count) {
+    g_last_error = "selftest_graph_conditional: output pointers required";
+    return THORIN_ERR_ARG;
+  }
+  *if_zero = *if_one = *while_count = -1;
+  int *dev = nullptr;
+  cudaError_t e = cudaMalloc((void **)&dev, sizeof(int));
+  if (e == cudaSuccess) e = st_cond_graph(0, 0u, 0, dev, if_zero);
+  if (e == cudaSuccess) e = st_cond_graph(0, 1u, 0, dev, if_one);
+  if (e == cudaSuccess && *if_zero == 0 && *if_one == 1) e = st_cond_graph(1, 1u, 5, dev, while_count);
+  if (dev) cudaFree(dev);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("selftest_graph_conditional: ") + cudaGetErrorString(e);
+    return THORIN_ERR_CUDA;
+  }
   return THORIN_OK;
 }
 

@@ -354,6 +354,13 @@ int thorin_selftest_division(long long n, unsigned long long seed, double max_ex
 int thorin_selftest_slope_division(long long n, unsigned long long seed, double max_exponent,
                                    unsigned long long *max_ulp);
 
+/* Self-test of the conditional CUDA graph nodes behind the SOR sweep loop:
+ * a kernel that sets an IF node's condition to 0 must skip its body
+ * (*if_zero = 0) and to 1 run it once (*if_one = 1); only then a WHILE node
+ * whose body clears the condition on its fifth run is launched
+ * (*while_count = 5; -1 when not run).  No counterpart in the reference. */
+int thorin_selftest_graph_conditional(int *if_zero, int *if_one, int *while_count);
+
 /* FP64 fused multiply-add throughput of the current GPU in GFLOP/s (two
  * flops per FMA), measured with a short kernel of independent FMA chains:
  * the FP64-pipe ceiling for the roofline of the kernels.  No counterpart in

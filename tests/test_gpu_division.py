@@ -32,3 +32,15 @@ def test_slope_division_bound(max_exponent, seed):
                "selftest_slope_division")
     print("slope division: max", ulp.value, "ulp")
     assert ulp.value <= 16384
+
+
+def test_graph_conditional_nodes():
+    """The SOR sweep loop is a WHILE graph node whose condition the last
+    sweep's completion step clears; this checks the mechanism in bounded
+    form first (IF nodes), then a WHILE node of five runs."""
+    from fargo_thorin_gb300 import _lib
+    lib = _lib.load()
+    a, b, w = C.c_int(), C.c_int(), C.c_int()
+    _lib.check(lib.thorin_selftest_graph_conditional(C.byref(a), C.byref(b), C.byref(w)),
+               "selftest_graph_conditional")
+    assert (a.value, b.value, w.value) == (0, 1, 5)
