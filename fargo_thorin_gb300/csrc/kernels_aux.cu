@@ -354,7 +354,7 @@ __global__ void k_pebble_sources(DevGrid g, const double *__restrict__ pd, const
 {
   const int ns = g.ns;
   CELL_LOOP_2D
-  const double Omega = div_fast(1.0, g.r.OmegaInv[i]);
+  const double Omega = g.r.Omega[i];
   const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
   const double otau = back_reaction ? div_fast(Omega, tau[l]) : 0.0;    // Omega / tau_s
   if (i >= 1) {
@@ -398,7 +398,7 @@ __global__ void k_pebble_substep1(DevGrid g, double *__restrict__ pvr, double *_
 {
   const int ns = g.ns;
   CELL_LOOP_2D
-  const double Omega = div_fast(1.0, g.r.OmegaInv[i]);
+  const double Omega = g.r.Omega[i];
   const double t = tau[l];
   const double efac = exp(div_fast(-dt * Omega, t));
   double a = pvr[l], b = pvt[l];
@@ -408,13 +408,13 @@ __global__ void k_pebble_substep1(DevGrid g, double *__restrict__ pvr, double *_
   if (diffusion) {
     if (i >= 1) {
       const int lim = l - ns;
-      double corr = -g.r.nu_inf[i] / schmidt;
+      double corr = div_fast(-g.r.nu_inf[i], schmidt);
       corr *= div_fast(rho[l] + rho[lim], pd[l] + pd[lim]);
       corr *= (div_fast(pd[l], rho[l]) - div_fast(pd[lim], rho[lim])) * g.r.InvDiffRmed[i];
       a += corr;
     }
     const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
-    double corr = -g.r.nu_med[i] / schmidt;
+    double corr = div_fast(-g.r.nu_med[i], schmidt);
     corr *= div_fast(rho[l] + rho[ljm], pd[l] + pd[ljm]);
     corr *= (div_fast(pd[l], rho[l]) - div_fast(pd[ljm], rho[ljm])) * invdxtheta_r[i];
     b += corr;
@@ -467,6 +467,7 @@ __global__ void k_force_rings(DevGrid g, ForceRings fr, int pebbles, double pebb
   }
   fr.H_avr[i] = H_avr;
   fr.sigma_avr[i] = sig;
+  fr.isigma_avr[i] = div_fast(1.0, sig);
   fr.integstar_avr[i] = ist;
   fr.p_H_avr[i] = p_H_avr;
   fr.p_integstar_avr[i] = p_int;
@@ -538,8 +539,7 @@ __global__ void __launch_bounds__(128) k_forces(DevGrid g, ForceArgs a, ForceRin
     if (j >= ns) break;
     const int l = j + i * ns;
     const double omegainv = g.r.OmegaInv[i], r2 = g.r.Rmed2[i];
-    double Rsup_Rinf2 = g.r.Rsup[i] - g.r.Rinf[i];
-    Rsup_Rinf2 *= Rsup_Rinf2;
+    const double Rsup_Rinf2 = fr.drsq[i];
     const double x = g.r.Rmed[i] * g.r.costab[j];
     const double y = g.r.Rmed[i] * g.r.sintab[j];
     const double mcell = a.rho[l] * g.r.Surf[i];
@@ -560,12 +560,10 @@ __global__ void __launch_bounds__(128) k_forces(DevGrid g, ForceArgs a, ForceRin
     for (int k = 0; k < npl; k++) {
       const DevPlanet P = a.pl[k];
       s2[k] = (x - P.x) * (x - P.x) + (y - P.y) * (y - P.y);
-      double c1 = 10.0 * P.Hpl; c1 *= c1;
-      double c2 = 5.0 * P.rhill; c2 *= c2;
       hillcut[k] = 1.0;
       integpl[k] = 0.0;
       p_integpl[k] = 0.0;
-      if (a.mass_taper == 1.0 && (s2[k] < c1 || s2[k] < c2)) {
+      if (a.full_mass && (s2[k] < P.near_h2 || s2[k] < P.near_hill2)) {
         local = 1;
         with[k] = 1;
         if (a.exclude_hill) {
@@ -577,23 +575,22 @@ __global__ void __launch_bounds__(128) k_forces(DevGrid g, ForceArgs a, ForceRin
       }
       if (s2[k] < P.rmorevert2) Nvert = 30;
     }
-    double sigma, integstar, p_integstar = 0.0;
+    double isig, integstar, p_integstar = 0.0;       // 1 / sigma from tables
     if (local) {
       if (Nvert == 10) {
-        sigma = a.sig10;
+        isig = a.isig10;
         vert_quad<10>(a.wq10, H, r2, Hcorr, pH, peb, npl, with, s2, Rsup_Rinf2, a.pl, integstar, p_integstar,
                       integpl, p_integpl);
       } else {
-        sigma = a.sig30;
+        isig = a.isig30;
         vert_quad<30>(a.wq30, H, r2, Hcorr, pH, peb, npl, with, s2, Rsup_Rinf2, a.pl, integstar, p_integstar,
                       integpl, p_integpl);
       }
     } else {
-      sigma = fr.sigma_avr[i];
+      isig = fr.isigma_avr[i];
       integstar = fr.integstar_avr[i];
       if (peb) p_integstar = fr.p_integstar_avr[i];
     }
-    const double isig = div_fast(1.0, sigma);
     double tmp = integstar * isig;
     double agr = -g.r.Rmed[i] * tmp;            // 0.0 + ar
     acc[0] += mcell * tmp * x;
@@ -657,7 +654,7 @@ __global__ void __launch_bounds__(128) k_forces(DevGrid g, ForceArgs a, ForceRin
   const int nq = 2 + 2 * npl;
   const int b = blockIdx.x + blockIdx.y * gridDim.x;
   for (int q = 0; q < nq; q++) {
-    const double v = block_reduce(acc[q], OpAdd(), 0.0);
+    const double v = block_reduce_smem<128>(acc[q], OpAdd());
     if (threadIdx.x == 0) a.part[(size_t)b * nq + q] = v;
   }
 }
@@ -710,7 +707,8 @@ void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr, dou
       w[m - 1] = exp(-(0.5 * (z * z)));
       sig += w[m - 1];
     }
-    if (pass) a.sig30 = sig; else a.sig10 = sig;
+    if (pass) { a.sig30 = sig; a.isig30 = 1.0 / sig; }
+    else { a.sig10 = sig; a.isig10 = 1.0 / sig; }
   }
   dim3 grid = grid2d(g.ns, g.nr, 128 * FORCE_CPT);
   k_forces<<<grid, 128, 0, s>>>(g, a, fr);

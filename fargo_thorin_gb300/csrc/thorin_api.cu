@@ -105,7 +105,8 @@ enum {  // ring arrays kept on the device
   R_WAVEKILLER, R_RMED15, R_RINF15, R_RSUP15, R_COSTAB, R_SINTAB, R_SIGMAMED, R_ENERGYMED, R_VTHETAMED, R_PEBDENS0,
   R_PEBVRAD0, R_PEBVTHETA0, R_CSMEAN, R_TEMPMEAN, R_NUMED, R_NUINF, R_INVDXTHETA, R_INVDXTHETA2, R_SUPPTORQUE,
   R_DELTAR2, R_CFLDXRAD, R_CFLDXTHETA, R_CFLMINDX, R_CFLDEN5, R_VMOY, R_PVTMED, R_HAVR, R_SIGAVR, R_ISTAVR, R_PHAVR,
-  R_PISTAVR, R_VMED, R_TAUAVR, R_VTEMP, R_DAMPVR0, R_CSISO, R_COOLT, R_QPLUSMED, R_COUNT
+  R_PISTAVR, R_VMED, R_TAUAVR, R_VTEMP, R_DAMPVR0, R_CSISO, R_COOLT, R_QPLUSMED, R_ISIGAVR, R_DRSQ, R_OMEGA,
+  R_COUNT
 };
 
 struct thorin_disk {
@@ -262,6 +263,12 @@ static int upload_all_rings(thorin_disk *d)
   RCHK(upload_ring(d, R_INVSURF, d->InvSurf)); RCHK(upload_ring(d, R_INVDIFFRMED, d->InvDiffRmed));
   RCHK(upload_ring(d, R_INVDIFFRSUP, d->InvDiffRsup)); RCHK(upload_ring(d, R_INVRINF, d->InvRinf));
   RCHK(upload_ring(d, R_OMEGAINV, d->OmegaInv)); RCHK(upload_ring(d, R_RMED2, d->Rmed2));
+  {
+    std::vector<double> om(n1, 0.0);           // Omega = 1 / OmegaInv, correctly rounded
+    for (int i = 0; i < n1; i++)
+      if (d->OmegaInv[i] != 0.0) om[i] = 1.0 / d->OmegaInv[i];
+    RCHK(upload_ring(d, R_OMEGA, om));
+  }
   RCHK(upload_ring(d, R_WAVEKILLER, d->WaveKiller));
   for (int i = 0; i < nr; i++) v[i] = pow(d->Rmed[i], 1.5);
   RCHK(upload_ring(d, R_RMED15, v));
@@ -279,7 +286,7 @@ static int upload_all_rings(thorin_disk *d)
   CUCHK(cudaMemcpyAsync(d->ring[R_SINTAB], sn.data(), ns * sizeof(double), cudaMemcpyHostToDevice, d->s));
   // per-ring expressions of SubStep1/2, ImplicitRadiativeDiffusion, DiffusionTimestep, ConditionCFL
   std::vector<double> a(n1, 0.0), b(n1, 0.0), st(n1, 0.0), dr2(n1, 0.0), cdx(n1, 0.0), cdt(n1, 0.0), cmin(n1, 0.0),
-      cden(n1, 0.0);
+      cden(n1, 0.0), drsq(n1, 0.0);
   for (int i = 0; i < nr; i++) {
     const double dxtheta = 2.0 * H_PI / (double)ns * d->Rmed[i];
     a[i] = 1.0 / dxtheta;
@@ -287,6 +294,7 @@ static int upload_all_rings(thorin_disk *d)
     st[i] = p.imposed_disk_drift * .5 * pow(d->Rmed[i], -2.5 + p.sigma_slope);
     double dr = d->Rsup[i] - d->Rinf[i];
     dr2[i] = dr * dr / 2.0;
+    drsq[i] = dr * dr;
     const double dxrad = d->Rsup[i] - d->Rinf[i];
     const double dxth = d->Rmed[i] * 2.0 * H_PI / (double)ns;
     cdx[i] = dxrad;
@@ -295,7 +303,7 @@ static int upload_all_rings(thorin_disk *d)
     cden[i] = pow(cmin[i], 2);
   }
   RCHK(upload_ring(d, R_INVDXTHETA, a)); RCHK(upload_ring(d, R_INVDXTHETA2, b));
-  RCHK(upload_ring(d, R_SUPPTORQUE, st)); RCHK(upload_ring(d, R_DELTAR2, dr2));
+  RCHK(upload_ring(d, R_SUPPTORQUE, st)); RCHK(upload_ring(d, R_DELTAR2, dr2)); RCHK(upload_ring(d, R_DRSQ, drsq));
   RCHK(upload_ring(d, R_CFLDXRAD, cdx)); RCHK(upload_ring(d, R_CFLDXTHETA, cdt));
   RCHK(upload_ring(d, R_CFLMINDX, cmin)); RCHK(upload_ring(d, R_CFLDEN5, cden));
   RCHK(upload_ring(d, R_SIGMAMED, d->SigmaMed)); RCHK(upload_ring(d, R_ENERGYMED, d->EnergyMed));
@@ -320,7 +328,7 @@ static void build_grid(thorin_disk *d)
   double **R = d->ring;
   r.Rinf = R[R_RINF]; r.Rsup = R[R_RSUP]; r.Rmed = R[R_RMED]; r.Surf = R[R_SURF]; r.InvRmed = R[R_INVRMED];
   r.InvSurf = R[R_INVSURF]; r.InvDiffRmed = R[R_INVDIFFRMED]; r.InvDiffRsup = R[R_INVDIFFRSUP];
-  r.InvRinf = R[R_INVRINF]; r.OmegaInv = R[R_OMEGAINV]; r.Rmed2 = R[R_RMED2]; r.WaveKiller = R[R_WAVEKILLER];
+  r.InvRinf = R[R_INVRINF]; r.OmegaInv = R[R_OMEGAINV]; r.Omega = R[R_OMEGA]; r.Rmed2 = R[R_RMED2]; r.WaveKiller = R[R_WAVEKILLER];
   r.Rmed15 = R[R_RMED15]; r.Rinf15 = R[R_RINF15]; r.costab = R[R_COSTAB]; r.sintab = R[R_SINTAB];
   r.SigmaMed = R[R_SIGMAMED]; r.EnergyMed = R[R_ENERGYMED]; r.VthetaMed = R[R_VTHETAMED];
   r.PebDensInit = R[R_PEBDENS0]; r.PebVradInit = R[R_PEBVRAD0]; r.PebVthetaInit = R[R_PEBVTHETA0];
@@ -339,6 +347,7 @@ static void build_grid(thorin_disk *d)
   d->cfl.den5 = R[R_CFLDEN5]; d->cfl.vmoy = R[R_VMOY]; d->cfl.pvtmed = R[R_PVTMED];
   d->fr.H_avr = R[R_HAVR]; d->fr.sigma_avr = R[R_SIGAVR]; d->fr.integstar_avr = R[R_ISTAVR];
   d->fr.p_H_avr = R[R_PHAVR]; d->fr.p_integstar_avr = R[R_PISTAVR]; d->fr.tau_avr = R[R_TAUAVR];
+  d->fr.isigma_avr = R[R_ISIGAVR]; d->fr.drsq = R[R_DRSQ];
 }
 
 static int check_supported(const thorin_params &p)
@@ -1353,6 +1362,10 @@ extern "C" int thorin_gpu_forces(thorin_disk *d, thorin_planets *sys, double mas
     P.rsm2 = rsm * rsm;
     P.rmorevert2 = 2.0 * P.rhill;
     P.rmorevert2 *= P.rmorevert2;
+    P.near_h2 = 10.0 * P.Hpl;
+    P.near_h2 *= P.near_h2;
+    P.near_hill2 = 5.0 * P.rhill;
+    P.near_hill2 *= P.near_hill2;
     if (p.indirect_term) {
       const double invdpl3 = 1.0 / (dpl * dpl * dpl);
       mpl *= mass_taper;
@@ -1368,6 +1381,7 @@ extern "C" int thorin_gpu_forces(thorin_disk *d, thorin_planets *sys, double mas
   a.pl = d->planets_d;
   a.npl = npl; a.pebbles = p.pebbles; a.exclude_hill = p.exclude_hill; a.pebble_gravity = p.pebble_gravity;
   a.mass_taper = mass_taper; a.pebble_alpha = p.pebble_alpha; a.hillcut = p.hillcut;
+  a.full_mass = (mass_taper == 1.0) ? 1 : 0;
   const double indx_pl = p.indirect_term ? -axs : 0.0, indy_pl = p.indirect_term ? -ays : 0.0;
   aux_forces(d->g, a, d->fr, indx_pl, indy_pl, d->scal, d->s);
   KCHECK("force kernels");

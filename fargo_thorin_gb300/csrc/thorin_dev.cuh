@@ -42,6 +42,7 @@ struct DevConst {
 struct DevRings {
   const double *Rinf, *Rsup, *Rmed, *Surf, *InvRmed, *InvSurf, *InvDiffRmed, *InvDiffRsup, *InvRinf;
   const double *OmegaInv, *Rmed2, *WaveKiller;
+  const double *Omega;                  // 1 / OmegaInv
   const double *InvDxtheta;             // 1 / (2 pi / nsec * Rmed)
   const double *Rmed15, *Rinf15;        // pow(Rmed,1.5), pow(Rinf,1.5) (FViscosity)
   const double *costab, *sintab;         // cos/sin(2 pi j / nsec), nsec entries
@@ -132,6 +133,29 @@ __device__ __forceinline__ double div_slope(double x, double d)
 __device__ __forceinline__ double abs_i(double x)
 {
   return __hiloint2double(__double2hiint(x) & 0x7fffffff, __double2loint(x));
+}
+
+// Block reduction for blocks of exactly NT threads through shared memory:
+// warp 0 folds the NT / 32 values of its lane's column, then one shuffle
+// tree finishes.  On the FP64 pipe that is NT/32 + 4 warp instructions
+// instead of the 5 (NT/32 + 1) of block_reduce.  Result valid in thread 0;
+// fixed order.  Safe to call repeatedly (the first barrier waits for the
+// previous call's readers).
+template <int NT, typename T, typename Op>
+__device__ __forceinline__ T block_reduce_smem(T v, Op op)
+{
+  static_assert(NT % 32 == 0 && NT <= 1024, "block of whole warps");
+  __shared__ T sh[NT];
+  __syncthreads();
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    T s = sh[threadIdx.x];
+#pragma unroll
+    for (int k = 1; k < NT / 32; k++) s = op(s, sh[threadIdx.x + 32 * k]);
+    v = warp_reduce(s, op);
+  }
+  return v;
 }
 
 // x^3 correctly rounded (Dekker two-product with fma): the reference uses

@@ -8,6 +8,7 @@
 // Planet data seen by the kernels (per-planet constants from the host).
 struct DevPlanet {
   double x, y, z, m, rhill, Hpl, smoothing2, rst2, rst3, rst4, rsm2, rmorevert2;
+  double near_h2, near_hill2;   // (10 Hpl)^2 and (5 rhill)^2: the vertical-quadrature zone
 };
 
 // Indices into the small device scalar buffer.
@@ -73,7 +74,11 @@ struct CflFinal {
   double deltaT, invdtreb_sq, minimum_step, maximum_step, first_step, twopi_cfl_ns;
 };
 
-struct ForceRings { double *H_avr, *sigma_avr, *integstar_avr, *p_H_avr, *p_integstar_avr, *tau_avr; };
+struct ForceRings {
+  double *H_avr, *sigma_avr, *integstar_avr, *p_H_avr, *p_integstar_avr, *tau_avr;
+  double *isigma_avr;          // 1 / sigma_avr
+  const double *drsq;          // (Rsup - Rinf)^2
+};
 
 struct ForceArgs {
   const double *rho, *cs, *tau, *pdens;
@@ -85,6 +90,8 @@ struct ForceArgs {
   // vertical quadrature weights exp(-z_m^2 / 2H^2) at z_m = (m - 1/2) 3H/N,
   // which do not depend on H, and their sums (filled by aux_forces)
   double wq10[10], wq30[30], sig10, sig30;
+  double isig10, isig30;      // 1 / sig10, 1 / sig30
+  int full_mass;              // mass_taper == 1.0
 };
 
 struct GasAccArgs {           // one planet of AccreteOntoPlanets (Planet.c:34-166)
