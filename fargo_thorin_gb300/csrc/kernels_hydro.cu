@@ -466,8 +466,8 @@ __device__ __forceinline__ double opacity_law(const DevConst &k, int law, double
   }
 }
 
-// |grad T| at a cell centre (TemperatureGradient, EnergySources.c:609-653).
-__device__ __forceinline__ double gradt_mag(const DevGrid &g, const double *T, int i, int j, const double *invdxtheta_r)
+// |grad T|^2 at a cell centre (TemperatureGradient, EnergySources.c:609-653).
+__device__ __forceinline__ double gradt_sq(const DevGrid &g, const double *T, int i, int j, const double *invdxtheta_r)
 {
   const int ns = g.ns, l = j + i * ns, lip = l + ns, lim = l - ns;
   const int ljp = (j == ns - 1) ? i * ns : l + 1;
@@ -479,12 +479,18 @@ __device__ __forceinline__ double gradt_mag(const DevGrid &g, const double *T, i
   double gt_ljp = (T[ljp] - T[l]) * invdx;
   double r = 0.5 * (gr_lip + gr_l);
   double t = 0.5 * (gt_ljp + gt_l);
-  return sqrt(r * r + t * t);
+  return r * r + t * t;
 }
 
-__device__ __forceinline__ double flux_limiter(double s)
+// FluxLimiterValue (EnergySources.c:684-698) of s = sqrt(g2) * c, from
+// s^2 = g2 c^2: below s = 2 the limiter 2 / (3 + sqrt(9 + 10 s^2)) needs only
+// s^2, which saves the square root of |grad T| in optically thick cells (the
+// limiter is continuous at s = 2, where both forms give 1/5).
+__device__ __forceinline__ double flux_limiter_sq(double g2, double c)
 {
-  if (s <= 2.0) return div_fast(2.0, 3.0 + sqrt(9.0 + 10.0 * s * s));
+  const double s2 = g2 * (c * c);
+  if (s2 <= 4.0) return div_fast(2.0, 3.0 + sqrt(9.0 + 10.0 * s2));
+  const double s = sqrt(g2) * c;
   return div_fast(10.0, 10.0 * s + 9.0 + sqrt(81.0 + 180.0 * s));
 }
 
@@ -520,12 +526,11 @@ __global__ void k_diffcoef(DevGrid g, const double *__restrict__ rho, const doub
     const double T3 = cube_rn(Tl);
     qminus[l] = div_fast(2.0 * g.k.sigma_sb * T3 * tau, __fma_rn(__fma_rn(0.375, tau, taueff_c), tau, 0.25));
     const int ig = (i == 0) ? 1 : (i == nr - 1 ? nr - 2 : i);
-    const double gradt = gradt_mag(g, T, ig, j, invdxtheta_r);
+    const double g2 = gradt_sq(g, T, ig, j, invdxtheta_r);
     // fac = 1 / (rho_mid kappa) and the limiter argument s = 4 |grad T| fac / T from one division
     const double q = div_fast(1.0, vd * kap * Tl);
     const double fac = q * Tl;
-    const double s = 4.0 * gradt * q;
-    const double D = flux_limiter(s) * 16.0 * g.k.sigma_sb * T3 * fac;
+    const double D = flux_limiter_sq(g2, 4.0 * q) * 16.0 * g.k.sigma_sb * T3 * fac;
     dcen[l] = D;
     if (__double_as_longlong(D) > 0LL) dmax = D;
     else dtl = div_fast(deltar2_r[i], D);

@@ -136,3 +136,27 @@ def test_gpu_vs_oracle_wide_rings(kind, nr, ns):
         for f in H.GAS + (H.PEB if p.pebbles else []) + ["energy"] + (["label"] if p.label_advection else []):
             assert H.rel_l2(d.get(H.FIELD_IDS[f])[:n], o.get(H.FIELD_IDS[f])[:n]) < 1e-11, f"{f} at DT {step}"
         assert abs(sg.x[0] - so.x[0]) < 1e-14 and abs(sg.vx[0] - so.vx[0]) < 1e-14
+
+
+def test_sor_direct_launches_match_graph_loop(monkeypatch):
+    """THORIN_SOR_DIRECT (the sweeps as plain launches, for kernel profilers)
+    runs the same kernels as the conditional-graph sweep loop: identical
+    fields and SOR counts, bit for bit."""
+    g = H.load("disk1_32x96")
+    p = H.case_params(g)
+    runs = []
+    for direct in ("0", "1"):
+        monkeypatch.setenv("THORIN_SOR_DIRECT", direct)
+        d = _gpu_disk(p)
+        d.init_default()
+        H.opacity_table(d, g)
+        H.start_state(d, p, {"dens": g["init_dens"].ravel(), "temper": g["init_temper"].ravel()})
+        s = workloads.make_planets(p, [tuple(g["planet"])])
+        niter = []
+        for _ in range(3):
+            d.algogas(s)
+            niter.append(d.stats().sor_last_niter)
+        runs.append((niter, [d.get(H.FIELD_IDS[f]).copy() for f in H.GAS + H.PEB + ["energy"]]))
+    assert runs[0][0] == runs[1][0]
+    for a, b in zip(runs[0][1], runs[1][1]):
+        np.testing.assert_array_equal(a, b)
