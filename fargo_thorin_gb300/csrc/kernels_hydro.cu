@@ -6,6 +6,7 @@
 // sums associate left to right exactly as written in the C source) so that,
 // compiled without FMA contraction, results match the reference bit for bit
 // wherever no transcendental function is involved.
+#include <cstdio>
 #include "thorin_kernels.cuh"
 
 #define CELL_LOOP_2D                                                        \
@@ -665,7 +666,9 @@ __device__ __forceinline__ double sor_resid_at(const double *T, const double *ml
 #ifndef SOR_CPT
 #define SOR_CPT 4        // cells of one colour per thread
 #endif
+#ifndef SOR_BX
 #define SOR_BX 128       // threads per SOR block
+#endif
 
 // Block sums of the pass's L1 residual and "changed" count, result in
 // thread 0.  The FP64 pipe bounds the SOR pass, so the first level goes
@@ -706,7 +709,7 @@ __device__ __forceinline__ bool sor_last_block(unsigned int *ticket, unsigned nb
   return last;
 }
 
-__global__ void __launch_bounds__(128) k_sor_resid0(DevGrid g, const double *__restrict__ T,
+__global__ void __launch_bounds__(SOR_BX) k_sor_resid0(DevGrid g, const double *__restrict__ T,
                                                     const double *__restrict__ ml, const double *__restrict__ mlip,
                                                     const double *__restrict__ mlim, const double *__restrict__ mljp,
                                                     const double *__restrict__ mljm, const double *__restrict__ rhs,
@@ -786,7 +789,7 @@ __device__ __forceinline__ bool sor_changed(double resid, double cw, double tn)
   return __double_as_longlong(__fma_rn(-tn, TH_SORPRECISION, resid * cw)) > 0LL;
 }
 
-__global__ void __launch_bounds__(128) k_sor_pass(DevGrid g, double *__restrict__ T, const double *__restrict__ ml,
+__global__ void __launch_bounds__(SOR_BX) k_sor_pass(DevGrid g, double *__restrict__ T, const double *__restrict__ ml,
                                                   const double *__restrict__ mlip, const double *__restrict__ mlim,
                                                   const double *__restrict__ mljp, const double *__restrict__ mljm,
                                                   const double *__restrict__ rhs, const double *__restrict__ cw,
@@ -1310,7 +1313,20 @@ static dim3 sor_grid_pass(const DevGrid &g)
   static std::atomic<int> occ_cache{0};            // resident k_sor_pass blocks per multiprocessor
   int occ = occ_cache.load();
   if (occ == 0) {
+#ifdef SOR_CARVEOUT
+    cudaFuncSetAttribute(k_sor_pass, cudaFuncAttributePreferredSharedMemoryCarveout, SOR_CARVEOUT);
+#endif
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sor_pass, SOR_BX, 0) != cudaSuccess || occ < 1) occ = 1;
+    // at most 1536 resident threads per SM: on the 1024x3072 disk the pass
+    // took 29.3 us with 12 blocks of 128 per SM (also with 6 of 256), 30.4 us
+    // with the 16 that fit, 31.6 us with 8
+    if (occ * SOR_BX > 1536) occ = 1536 / SOR_BX > 0 ? 1536 / SOR_BX : 1;
+#ifdef SOR_OCC
+    occ = SOR_OCC;
+#endif
+#ifdef SOR_PRINT_OCC
+    std::fprintf(stderr, "k_sor_pass: %d blocks per SM\n", occ);
+#endif
     occ_cache.store(occ);
   }
   const int half = g.ns / 2;
