@@ -584,15 +584,6 @@ __global__ void k_irradiation(DevGrid g, const double *__restrict__ rho, const d
   }
 }
 
-// The SOR coefficients are stored packed by colour: for ring i, the cells
-// of pass 1 (j = i-1 mod 2) then those of pass 2, each as k = j/2, so that a
-// colour pass reads them contiguously.
-__device__ __forceinline__ size_t sor_pidx(int i, int j, int half)
-{
-  const int c = (j ^ (i - 1)) & 1;
-  return (size_t)((i << 1) + c) * half + (j >> 1);
-}
-
 // Matrix of the linearised implicit energy equation
 // (ImplicitRadiativeDiffusion, EnergySources.c:256-297), plus the
 // reciprocal of the diagonal used by the SOR update.

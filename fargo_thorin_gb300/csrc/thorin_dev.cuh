@@ -135,6 +135,16 @@ __device__ __forceinline__ double abs_i(double x)
   return __hiloint2double(__double2hiint(x) & 0x7fffffff, __double2loint(x));
 }
 
+// The SOR coefficients (Ml, Mlip, Mlim, Mljp, Mljm, RHS) are stored packed
+// by colour: for ring i, the cells of pass 1 (j = i-1 mod 2) then those of
+// pass 2, each as k = j/2, so that a colour pass reads them contiguously.
+// Every reader of those arrays indexes them through sor_pidx.
+__device__ __forceinline__ size_t sor_pidx(int i, int j, int half)
+{
+  const int c = (j ^ (i - 1)) & 1;
+  return (size_t)((i << 1) + c) * half + (j >> 1);
+}
+
 // Block reduction for blocks of exactly NT threads through shared memory:
 // warp 0 folds the NT / 32 values of its lane's column, then one shuffle
 // tree finishes.  On the FP64 pipe that is NT/32 + 4 warp instructions

@@ -75,7 +75,7 @@ template <int CIN, int N>
 constexpr int conv_smem() { return (CIN / 8) * 3 * WN_HALO_W * 16 + 9 * CIN * N * 2 + 128 + 128; }
 
 template <int CIN, int N, int MODE>
-__global__ void __launch_bounds__(128) k_wn_conv(ConvArgs a)
+__global__ void __launch_bounds__(128, 4) k_wn_conv(ConvArgs a)
 {
   constexpr int K = 9 * CIN, KG = K / 8, C8 = CIN / 8;
   constexpr int A_BYTES = C8 * 3 * WN_HALO_W * 16, B_BYTES = KG * N * 16, LBO_A = 3 * WN_HALO_W * 16;
@@ -97,24 +97,24 @@ __global__ void __launch_bounds__(128) k_wn_conv(ConvArgs a)
   umma::fence_after_sync();
   const uint32_t tmem = *tslot;
 
-  float bias[N];
-#pragma unroll
-  for (int n = 0; n < N; n++) bias[n] = (MODE != 2 && n < a.coutr) ? a.bias[n] : 0.f;
+  // the bias is read in the epilogue (L1-resident), not held in registers
+  // beside the next tile's loads
+  auto bias = [&](int n) { return (MODE != 2 && n < a.coutr) ? __ldg(a.bias + n) : 0.f; };
 
   const int tpr = (a.W + 127) / 128;                       // tiles per ring
   const long long ntiles = (long long)a.B * a.H * tpr;
-  uint32_t phase = 0;
-  bool ok = true;
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const long long ring = tile / tpr;                     // b * H + i
+  // A tile stages rings i-1, i, i+1 over cells p0-1 .. p0+128 (azimuth
+  // wrapped).  The global loads of the next tile are issued into registers
+  // as soon as this tile's MMAs are issued, so their latency overlaps the
+  // MMA wait and the epilogue; every load of the thread is in flight before
+  // the first store.
+  constexpr int NCH = 3 * WN_HALO_W * C8, PER = (NCH + 127) / 128;
+  uint4 val[PER];
+  auto load_tile = [&](long long tile) {
+    const long long ring = tile / tpr;
     const int p0 = (int)(tile - ring * tpr) * 128;
     const int i = (int)(ring % a.H);
-    const long long rbase = ring - i;                      // b * H
-    // stage rings i-1, i, i+1 over cells p0-1 .. p0+128 (azimuth wrapped):
-    // every load of the thread is issued before the first store, so their
-    // latencies overlap
-    constexpr int NCH = 3 * WN_HALO_W * C8, PER = (NCH + 127) / 128;
-    uint4 val[PER];
+    const long long rbase = ring - i;
 #pragma unroll
     for (int k = 0; k < PER; k++) {
       const int ch = tid + 128 * k;
@@ -127,6 +127,13 @@ __global__ void __launch_bounds__(128) k_wn_conv(ConvArgs a)
         if (ii >= 0 && ii < a.H) val[k] = __ldg((const uint4 *)(a.in + ((rbase + ii) * a.W + jj) * CIN + c8 * 8));
       }
     }
+  };
+  uint32_t phase = 0;
+  bool ok = true;
+  if ((long long)blockIdx.x < ntiles) load_tile(blockIdx.x);
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long ring = tile / tpr;                     // b * H + i
+    const int p0 = (int)(tile - ring * tpr) * 128;
 #pragma unroll
     for (int k = 0; k < PER; k++) {
       const int ch = tid + 128 * k;
@@ -151,6 +158,7 @@ __global__ void __launch_bounds__(128) k_wn_conv(ConvArgs a)
       umma::mma_commit(bar);
     }
     __syncwarp();
+    if (tile + gridDim.x < ntiles) load_tile(tile + gridDim.x);   // registers only: sA is the MMA's until the wait
     ok = umma::mbar_wait(bar, phase, WN_WAIT);
     ok = __syncthreads_and(ok);
     phase ^= 1u;
@@ -168,12 +176,12 @@ __global__ void __launch_bounds__(128) k_wn_conv(ConvArgs a)
           __nv_bfloat162 h[4];
 #pragma unroll
           for (int e = 0; e < 4; e++)
-            h[e] = __floats2bfloat162_rn(fmaxf(v[8 * q + 2 * e] + bias[8 * q + 2 * e], 0.f),
-                                         fmaxf(v[8 * q + 2 * e + 1] + bias[8 * q + 2 * e + 1], 0.f));
+            h[e] = __floats2bfloat162_rn(fmaxf(v[8 * q + 2 * e] + bias(8 * q + 2 * e), 0.f),
+                                         fmaxf(v[8 * q + 2 * e + 1] + bias(8 * q + 2 * e + 1), 0.f));
           dst[q] = *(uint4 *)h;
         }
       } else if (MODE == 1) {
-        ((float *)a.out)[p] = v[0] + bias[0];
+        ((float *)a.out)[p] = v[0] + bias(0);
       } else {
         float4 *dst = (float4 *)((float *)a.out + p * N);
 #pragma unroll
@@ -530,17 +538,21 @@ __global__ void k_wn_adam(float *__restrict__ w, const float *__restrict__ g, fl
 }
 
 // ---------------------------------------------------------------------------
-// Coupling to the SOR system (rows 1..nr-2 are the unknowns).
-__device__ __forceinline__ double sor_resid(const double *T, const double *ml, const double *mlip, const double *mlim,
-                                            const double *mljp, const double *mljm, const double *rhs, int l, int lip,
-                                            int lim, int ljp, int ljm)
-{
-  return T[l] * ml[l] + T[lip] * mlip[l] + T[lim] * mlim[l] + T[ljp] * mljp[l] + T[ljm] * mljm[l] - rhs[l];
-}
-
+// Coupling to the SOR system (rows 1..nr-2 are the unknowns).  T is in the
+// grid layout (l = j + i*ns); the coefficients and the right-hand side are
+// colour-packed (sor_pidx), as k_matrix writes them.
 struct SorSys {
   const double *ml, *mlip, *mlim, *mljp, *mljm, *rhs;
 };
+
+// residual of cell (i, j), row l = j + i*ns, packed position q
+__device__ __forceinline__ double sor_resid(const double *T, const SorSys &m, int ns, int i, int j, size_t q)
+{
+  const int l = j + i * ns;
+  const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+  return T[l] * m.ml[q] + T[l + ns] * m.mlip[q] + T[l - ns] * m.mlim[q] + T[ljp] * m.mljp[q] + T[ljm] * m.mljm[q] -
+         m.rhs[q];
+}
 
 // partial sums over the unknowns of |r / Ml| (part[block]) and |r|
 // (part[grid + block]), grid-stride, block order
@@ -549,10 +561,10 @@ __global__ void k_wn_scale(int nr, int ns, const double *__restrict__ T, SorSys 
   double s = 0.0, sr = 0.0;
   const long long n = (long long)(nr - 2) * ns;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(q / ns), j = (int)(q % ns), l = j + i * ns;
-    const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
-    const double r = sor_resid(T, m.ml, m.mlip, m.mlim, m.mljp, m.mljm, m.rhs, l, l + ns, l - ns, ljp, ljm);
-    s += (double)fabsf((float)r / (float)m.ml[l]);       // a scale: FP32 is plenty
+    const int i = 1 + (int)(q / ns), j = (int)(q % ns);
+    const size_t pq = sor_pidx(i, j, ns >> 1);
+    const double r = sor_resid(T, m, ns, i, j, pq);
+    s += (double)fabsf((float)r / (float)m.ml[pq]);      // a scale: FP32 is plenty
     sr += fabs(r);
   }
   s = block_reduce(s, OpAdd(), 0.0);
@@ -577,13 +589,13 @@ __device__ __forceinline__ double wn_cell_inputs(int nr, int ns, int i, int j, c
 {
   if (i < 1 || i > nr - 2) return 0.0;
   const int l = j + i * ns;
-  const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
-  const double r = sor_resid(T, m.ml, m.mlip, m.mlim, m.mljp, m.mljm, m.rhs, l, l + ns, l - ns, ljp, ljm);
-  const float iml = 1.0f / (float)m.ml[l];
+  const size_t q = sor_pidx(i, j, ns >> 1);
+  const double r = sor_resid(T, m, ns, i, j, q);
+  const float iml = 1.0f / (float)m.ml[q];
   const float rj = (float)r * iml;
   f[0] += fminf(fmaxf(rj * is, -16.f), 16.f);
-  const float w1 = -(float)m.mlip[l] * iml, w2 = -(float)m.mlim[l] * iml, w3 = -(float)m.mljp[l] * iml,
-              w4 = -(float)m.mljm[l] * iml;
+  const float w1 = -(float)m.mlip[q] * iml, w2 = -(float)m.mlim[q] * iml, w3 = -(float)m.mljp[q] * iml,
+              w4 = -(float)m.mljm[q] * iml;
   f[1] += w1; f[2] += w2; f[3] += w3; f[4] += w4;
   f[5] += -logf(fmaxf(1.f - (((w1 + w2) + w3) + w4), 1e-6f)) * 0.25f;
   if (prev) f[6] += fminf(fmaxf((float)prev[l] * is * (1.f / WN_YSCALE), -16.f), 16.f);
@@ -719,8 +731,7 @@ __global__ void k_wn_res(int nr, int ns, const double *__restrict__ tp, SorSys m
     const int i = (int)(q / ns), j = (int)(q % ns), l = (int)q;
     float v = 0.f;
     if (i >= 1 && i <= nr - 2 && *sr > 0.0) {
-      const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
-      const double r = sor_resid(tp, m.ml, m.mlip, m.mlim, m.mljp, m.mljm, m.rhs, l, l + ns, l - ns, ljp, ljm) / *sr;
+      const double r = sor_resid(tp, m, ns, i, j, sor_pidx(i, j, ns >> 1)) / *sr;
       v = (float)r;
       acc = r * r;
     }
@@ -741,10 +752,15 @@ __global__ void k_wn_res_grad(int nr, int ns, const float *__restrict__ rs, SorS
   const int i = (int)(q / ns), j = (int)(q % ns), l = (int)q;
   float g = 0.f;
   if (i >= 1 && i <= nr - 2 && *sr > 0.0) {
-    const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
-    double at = m.ml[l] * rs[l] + m.mljm[ljp] * rs[ljp] + m.mljp[ljm] * rs[ljm];
-    if (i + 1 <= nr - 2) at += m.mlim[l + ns] * rs[l + ns];
-    if (i - 1 >= 1) at += m.mlip[l - ns] * rs[l - ns];
+    // (A^T rs)_l: column l of A holds Ml of row l and the neighbour rows'
+    // coefficients that point at l
+    const int half = ns >> 1;
+    const int jp = (j == ns - 1) ? 0 : j + 1, jm = (j == 0) ? ns - 1 : j - 1;
+    const int ljp = jp + i * ns, ljm = jm + i * ns;
+    double at = m.ml[sor_pidx(i, j, half)] * rs[l] + m.mljm[sor_pidx(i, jp, half)] * rs[ljp] +
+                m.mljp[sor_pidx(i, jm, half)] * rs[ljm];
+    if (i + 1 <= nr - 2) at += m.mlim[sor_pidx(i + 1, j, half)] * rs[l + ns];
+    if (i - 1 >= 1) at += m.mlip[sor_pidx(i - 1, j, half)] * rs[l - ns];
     g = (float)(2.0 * inv_n * (double)wres * (*scale) * (double)WN_YSCALE / (*sr) * at);
   }
   gf[l] = g;

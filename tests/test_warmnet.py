@@ -207,3 +207,60 @@ def test_trained_network_saves_sweeps_on_the_disk1_workload():
     print(r)
     assert r["learned"] < r["plain"]
     assert r["t_rel_l2"] < 1e-9
+
+
+@pytest.mark.gpu
+def test_training_residual_uses_the_disks_packed_system():
+    """The warm start reads the disk's SOR system, which k_matrix stores
+    colour-packed.  With a zero output layer the prediction is the start plus
+    one Jacobi step J = -r/Ml, and the training step records
+    mean((A (T0 + J) - rhs)^2) / mean|r0|^2 over the unknowns.  Recomputed
+    here from the oracle's system of the same solve (grid layout)."""
+    import oracle as O
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import harness as H
+    from fargo_thorin_gb300 import workloads
+    p = workloads.params_for("disk1", 32, 96)
+    o = O.OracleDisk(p)
+    o.init_default()
+    # 20% random structure in azimuth, so that cells of one ring have clearly
+    # different coefficients (on a near-axisymmetric disk, reading another
+    # cell of the same ring would go unnoticed)
+    rng = np.random.default_rng(5)
+    dens = o.get(H.FIELD_IDS["dens"]).copy()
+    temper = o.get(H.FIELD_IDS["temper"]).copy()
+    dens *= 1 + 0.2 * rng.uniform(-1, 1, dens.shape)
+    temper *= 1 + 0.2 * rng.uniform(-1, 1, temper.shape)
+    init = {"dens": dens, "temper": temper}
+    from fargo_thorin_gb300.disk import GpuDisk
+    d = GpuDisk(p)
+    d.init_default()
+    for x in (d, o):
+        H.start_state(x, p, init)
+    sg = workloads.make_planets(p, [workloads.PLANET1])
+    so = workloads.make_planets(p, [workloads.PLANET1])
+    d.algogas(sg)
+    o.algogas(so)
+    net = WS.WarmNet(32, 96, params=WS.init_params(0))
+    WS.attach(d, net, WS.TRAIN, 1e-30)
+    d.algogas(sg)
+    o.algogas(so)
+    got = WS.stats(d).last_res_loss
+    s = o.sor_system()
+    nr, ns = 32, 96
+    A = {k: s[k].reshape(-1, ns)[:nr] for k in ("ml", "mlip", "mlim", "mljp", "mljm", "rhs")}
+    T0 = s["tstart"].reshape(-1, ns)[:nr]
+
+    def resid(T):
+        r = (T * A["ml"] + np.roll(T, -1, axis=0) * A["mlip"] + np.roll(T, 1, axis=0) * A["mlim"]
+             + np.roll(T, -1, axis=1) * A["mljp"] + np.roll(T, 1, axis=1) * A["mljm"] - A["rhs"])
+        return r[1:nr - 1]
+
+    r0 = resid(T0)
+    T1 = T0.copy()
+    T1[1:nr - 1] -= r0 / A["ml"][1:nr - 1]
+    want = np.mean(resid(T1) ** 2) / np.mean(np.abs(r0)) ** 2
+    assert abs(got / want - 1) < 1e-3, (got, want)
+    WS.attach(d, None, WS.OFF)
+    net.close()
+    d.close()
