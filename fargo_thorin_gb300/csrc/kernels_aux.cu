@@ -549,7 +549,7 @@ __global__ void __launch_bounds__(128) k_forces(DevGrid g, ForceArgs a, ForceRin
     double Hcorr = 0.0, pH = 0.0, pmcell = 0.0;
     if (peb) {
       pmcell = a.pdens[l] * g.r.Surf[i];
-      Hcorr = sqrt(div_fast(a.pebble_alpha, a.tau[l]));
+      Hcorr = a.sqrt_pebble_alpha * rsqrt(a.tau[l]);        // sqrt(alpha / tau) without the division
       pH = H * Hcorr;
       const double p_H_avr = fr.p_H_avr[i];
       if (fabs(pH - p_H_avr) > 0.05 * p_H_avr) local = 1;

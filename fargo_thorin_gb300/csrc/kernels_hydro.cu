@@ -282,10 +282,10 @@ __device__ double opacity_BL94(double rho, double T)
   if (grains) {
     // k1 = kappa0 T^2, k2 = kappa1 T^-7, k3 = kappa2 T^0.5;
     // t1 = (k1^-2 + k2^-2)^-2, x = k3 / (1 + 1e22 T^-10), k = (t1 + x^4)^(1/4),
-    // rearranged to three divisions
+    // rearranged to two divisions
     const double T2 = T * T, T4 = T2 * T2, T5 = T4 * T, T7 = T5 * T2, T10 = T5 * T5;
     const double k3 = kappa[2] * sqrt(T);
-    const double ik = div_fast(1.0, 2.5e7 * div_fast(1.0, T4) + 2.5e-33 * (T7 * T7));   // 1 / (k1^-2 + k2^-2)
+    const double ik = div_fast(T4, __fma_rn(2.5e-33 * (T7 * T7), T4, 2.5e7));   // 1 / (k1^-2 + k2^-2) = T^4 / (2.5e7 + 2.5e-33 T^18)
     const double t1 = ik * ik;
     const double x = div_fast(k3 * T10, T10 + 1.0e22);
     const double x2 = x * x;

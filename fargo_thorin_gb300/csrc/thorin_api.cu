@@ -1384,6 +1384,7 @@ extern "C" int thorin_gpu_forces(thorin_disk *d, thorin_planets *sys, double mas
   a.npl = npl; a.pebbles = p.pebbles; a.exclude_hill = p.exclude_hill; a.pebble_gravity = p.pebble_gravity;
   a.mass_taper = mass_taper; a.pebble_alpha = p.pebble_alpha; a.hillcut = p.hillcut;
   a.full_mass = (mass_taper == 1.0) ? 1 : 0;
+  a.sqrt_pebble_alpha = sqrt(p.pebble_alpha);
   const double indx_pl = p.indirect_term ? -axs : 0.0, indy_pl = p.indirect_term ? -ays : 0.0;
   aux_forces(d->g, a, d->fr, indx_pl, indy_pl, d->scal, d->s);
   KCHECK("force kernels");

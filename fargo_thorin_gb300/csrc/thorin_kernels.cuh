@@ -87,6 +87,7 @@ struct ForceArgs {
   const DevPlanet *pl;
   int npl, pebbles, exclude_hill, pebble_gravity;
   double mass_taper, pebble_alpha, hillcut;
+  double sqrt_pebble_alpha;   // sqrt(pebble_alpha)
   // vertical quadrature weights exp(-z_m^2 / 2H^2) at z_m = (m - 1/2) 3H/N,
   // which do not depend on H, and their sums (filled by aux_forces)
   double wq10[10], wq30[30], sig10, sig30;
