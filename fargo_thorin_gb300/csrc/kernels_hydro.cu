@@ -752,13 +752,13 @@ __global__ void __launch_bounds__(SOR_BX) k_sor_resid0(DevGrid g, const double *
 
 // One colour pass of a sweep.  Each thread updates SOR_CPT cells of ring i
 // (k = base + m*blockDim, j = 2k + parity).  The pass is bound by the FP64
-// pipe, so each cell costs eight FP64 instructions: the residual as five
+// pipe, so each cell costs seven FP64 instructions: the residual as five
 // FMAs, its absolute value added to the L1 norm, and the update
 // T - resid * (omega/Ml) as one FMA (omega/Ml prepared once per solve by
 // k_sor_resid0); the change test delta > T*SORPRECISION runs on the integer
 // pipe (sor_changed).  The sweep number is counted on the device (c.niter),
-// so the launches of a chunk of sweeps are identical and replay as one CUDA
-// graph.
+// so every sweep is the same two launches: the body of the sweep loop's
+// WHILE graph node.
 // delta > tn * SORPRECISION (SORPRECISION = 1e-15, between 2^-50 and 2^-49)
 // with delta = resid * cw, cw = omega / Ml > 0.  When resid, cw and tn are
 // positive normal numbers well inside the exponent range, delta lies in
