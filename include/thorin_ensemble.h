@@ -34,7 +34,10 @@ int thorin_ensemble_algogas(thorin_disk *const *disks, thorin_planets *const *sy
  * both orders), timing each on the wall clock after a device
  * synchronisation.  It writes the fastest schedule and its milliseconds
  * per DT, and the one-worker, given-order time for reference.  The DTs are
- * real steps of the run. */
+ * real steps of the run, each candidate on the next ones, so call it once
+ * the disks are past their initial transient: while the cost per DT still
+ * falls, the first candidates (the one-worker time among them) see the
+ * costlier DTs. */
 int thorin_ensemble_tune(thorin_disk *const *disks, thorin_planets *const *systems, int n, int max_workers, int ndt,
                          int *best_workers, int *best_order, double *best_ms_per_dt, double *sequential_ms_per_dt);
 
