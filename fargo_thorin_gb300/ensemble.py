@@ -113,6 +113,11 @@ class Ensemble:
         return list(st)
 
     def tune(self, max_workers: int = 16, ndt: int = 1) -> dict:
+        """Time every schedule (worker counts 1, 2, 4, ... in both orders) on
+        real DTs and return the fastest.  Each schedule runs on the next DTs,
+        so tune once the disks are past their initial transient; the
+        one-worker time it reports is not a like-for-like baseline while the
+        cost per DT is still falling."""
         bw, bo = C.c_int(), C.c_int()
         bms, sms = C.c_double(), C.c_double()
         _lib.check(self.L.thorin_ensemble_tune(self._dp, self._sp, len(self.disks), max_workers, ndt, C.byref(bw),
