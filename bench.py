@@ -15,7 +15,13 @@ ABI with the state uploaded from pinned host buffers and downloaded back
 every step.
 
 --impl reference times the CPU restatement of the reference algorithm (the
-oracle, OpenMP over all host cores) on the same disk, one short DT per step.
+oracle, OpenMP over all host cores) on the same disk: the same warm-up DTs
+from t = 0 as the GPU arm, then the substeps of the DTs that follow, which
+are the first DTs of the GPU arm's timed region; a step of that arm is one
+CFL substep (a bounded sample of a DT, so that the run ends within a few
+minutes).  ``cpu_baseline`` in the GPU line runs the oracle from the GPU
+arm's own snapshot, i.e. on exactly the first timed DTs, and checks their
+substep and SOR sweep counts against the GPU's.
 With torchrun (N > 1) every rank advances its own replica (the disk does not
 shard); rank 0 prints the line.
 """
@@ -42,6 +48,11 @@ UNIT = "cell-updates/s"
 # Algorithmic bytes per cell of one full SOR sweep: T read + write, the five
 # matrix coefficients and the right-hand side (8 FP64 values).
 SOR_BYTES_PER_CELL_SWEEP = 64.0
+# Algorithmic bytes per cell of one hydro substep: the gas state (Sigma, v_r,
+# v_theta, e read and written, 64 B) and the pebble state (Sigma_p, v_r,p,
+# v_theta,p read and written, the size read, 56 B).
+STATE_BYTES_PER_CELL_SUBSTEP = 120.0
+WORKLOAD = f"disk1 {NR}x{NS} gas+pebbles+3e-5 embryo, BL94, SOR eps {SOR_EPS}"
 
 
 def dist_env():
@@ -279,9 +290,13 @@ def run_gpu(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     subs, sweeps0, calls0 = 0, d.stats().sor_sweeps, d.stats().sor_calls
+    per_dt = []                               # (substeps, SOR sweeps) of each timed DT
     for _ in range(args.steps):
+        w0 = d.stats().sor_sweeps
         d.algogas(sys_)
-        subs += d.stats().substeps
+        st_ = d.stats()
+        subs += st_.substeps
+        per_dt.append((st_.substeps, st_.sor_sweeps - w0))
     e1.record(stream)
     barrier()
     clk = clocks.stop()
@@ -363,13 +378,32 @@ def run_gpu(args):
                                    "instruction"}
         cpu = None
         if ws == 1 and not args.no_cpu_baseline:
-            cpu = cpu_baseline(d, sys_)
+            cpu = cpu_baseline(p, snap, snap_sor, snap_time, snap_sys, per_dt)
+        # the whole DT against both roofs: algorithmic bytes (state traffic of
+        # every substep plus 64 B per cell per SOR sweep) and FP64
+        # instructions (per-kernel ncu counts per cell, scaled to the DT)
+        step_s = ms_max / args.steps / 1e3
+        step_bytes = NR * NS * (STATE_BYTES_PER_CELL_SUBSTEP * subs + SOR_BYTES_PER_CELL_SWEEP * sweeps) / args.steps
+        step_roof = {"bound": "hbm", "achieved": step_bytes / step_s / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": step_bytes / step_s / 1e9 / peak, "algorithmic_bytes_per_step": step_bytes,
+                     "peak_kind": peak_kind}
+        step_fp64 = None
+        ff = os.path.join(ROOT, "profiles", "fp64_inst_per_cell_disk1.json")
+        if fp64 and os.path.exists(ff):
+            with open(ff) as f:
+                fc = json.load(f)
+            inst = NR * NS * (fc["hydro_per_cell_substep"] * subs + fc["sor_per_cell_sweep"] * sweeps) / args.steps
+            step_fp64 = {"bound": "fp64 pipe", "achieved": inst / step_s / 1e9, "peak": fp64["peak"],
+                         "unit": "G FP64 inst/s", "frac": inst / step_s / 1e9 / fp64["peak"],
+                         "fp64_inst_per_step": inst, "counts": os.path.relpath(ff, ROOT)}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"disk1 {NR}x{NS} gas+pebbles+3e-5 embryo, BL94, SOR eps {SOR_EPS}",
+            "config": {"workload": WORKLOAD,
                        "nrad": NR, "nsec": NS, "substeps": subs, "sor_sweeps_per_substep": sweeps / max(subs, 1),
+                       "timed_dts": f"DTs {args.warmup + 1}-{args.warmup + args.steps} from t = 0",
+                       "per_dt_substeps_sweeps": per_dt,
                        "step": "one DT of AlgoGas (all CFL substeps)", "l2": "inputs larger than L2 (1.7 GB state)",
                        "parallelism": "replicas" if ws > 1 else "single disk"},
             "clocks": clk,
@@ -381,6 +415,8 @@ def run_gpu(args):
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": bytes_pass, "avg_launch_ms": sor_avg_ms},
             "fp64_roofline": fp64,
+            "step_roofline": step_roof,
+            "step_fp64_roofline": step_fp64,
             "sor_warm_start": learned,
             "ensemble": ens,
             "cpu_baseline": cpu,
@@ -399,10 +435,10 @@ def _oracle():
     return O
 
 
-def oracle_disk(O, omp=True, dt_div=8):
+def oracle_disk(O, omp=True):
+    """The bench workload on the oracle, set up like make_disk()."""
     from fargo_thorin_gb300 import workloads
     p = workloads.params_for("disk1", NR, NS, sor_eps=SOR_EPS)
-    p.dt = p.dt / dt_div          # one short DT per step keeps a step near one substep
     o = O.OracleDisk(p, omp=omp)
     o.init_default()
     st = workloads.perturbed_state(p, {"dens": o.get(0), "temper": o.get(8)})
@@ -412,29 +448,42 @@ def oracle_disk(O, omp=True, dt_div=8):
     return p, o, workloads.make_planets(p, [workloads.PLANET1])
 
 
-def cpu_baseline(d, sys_gpu):
-    """The oracle (OpenMP, all host cores) on the same disk: SOR omega schedule
-    taken from the GPU run so that the bounded sample times steady-state
-    substeps, a few short DTs."""
+def cpu_baseline(p, snap, snap_sor, snap_time, snap_sys, per_dt, budget_s=20.0):
+    """The oracle (OpenMP, all host cores) from the GPU arm's own snapshot
+    taken after the warm-up: the same first timed DTs, as many as fit in
+    about budget_s seconds (at least one).  Their substep and SOR sweep
+    counts are compared with the GPU's."""
     O = _oracle()
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    p, o, s = oracle_disk(O)
-    om, dom, nl, _ = d.sor_state()
-    o.set_sor_state(om, dom, nl)
+    _, o, _ = oracle_disk(O)              # initial profiles and damping targets as on the GPU
+    for f, v in snap.items():
+        o.set(f, v)
+    o.refresh(0)                          # EOS of the snapshot's state
+    o.set_sor_state(*snap_sor[:3])
+    o.set_time(snap_time)
+    s = snap_sys.copy()
     t0 = time.perf_counter()
-    subs, steps = 0, 0
-    while time.perf_counter() - t0 < 15.0 and steps < 8:
+    mine = []
+    while len(mine) < len(per_dt) and (not mine or time.perf_counter() - t0 < budget_s):
+        w0 = o.stats().sor_sweeps
         o.algogas(s)
-        subs += o.stats().substeps
-        steps += 1
+        st = o.stats()
+        mine.append((st.substeps, st.sor_sweeps - w0))
     el = time.perf_counter() - t0
+    subs = sum(m[0] for m in mine)
+    sweeps = sum(m[1] for m in mine)
     return {"value": NR * NS * subs / el, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{subs} substeps ({steps} DT/8 steps) of the {NR}x{NS} disk after the SOR omega calibration, "
-                      f"{el:.1f} s"}
+            "sample": f"the first {len(mine)} timed DTs ({subs} substeps, {sweeps} SOR sweeps) of the {NR}x{NS} "
+                      f"disk from the GPU arm's snapshot, {el:.1f} s",
+            "sor_sweeps_per_substep": sweeps / max(subs, 1), "per_dt_substeps_sweeps": mine,
+            "same_dts_as_gpu": bool(mine == [tuple(x) for x in per_dt[:len(mine)]])}
 
 
 def run_reference(args):
+    """The oracle on all host cores: the GPU arm's warm-up DTs from t = 0,
+    then --steps substeps of the DTs that follow (the GPU arm's first timed
+    DTs), each substep one step."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
@@ -444,22 +493,32 @@ def run_reference(args):
     p, o, s = oracle_disk(O)
     for _ in range(args.warmup):
         o.algogas(s)
+    # advance whole DTs until --steps substeps are done; the oracle's step
+    # counter counts substeps, so time the DTs and keep the count
     t0 = time.perf_counter()
-    subs = 0
-    for _ in range(args.steps):
+    subs, dts, w0 = 0, [], o.stats().sor_sweeps
+    while subs < args.steps:
+        wd = o.stats().sor_sweeps
         o.algogas(s)
-        subs += o.stats().substeps
+        st = o.stats()
+        subs += st.substeps
+        dts.append((st.substeps, st.sor_sweeps - wd))
     el = time.perf_counter() - t0
+    sweeps = o.stats().sor_sweeps - w0
     value = NR * NS * subs / el
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": el * 1e3 / subs, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"disk1 {NR}x{NS} gas+pebbles+3e-5 embryo, BL94, SOR eps {SOR_EPS}", "nrad": NR,
-                   "nsec": NS, "substeps": subs, "step": "one DT/8 of AlgoGas", "implementation":
-                   "CPU restatement of the reference algorithm (oracle), OpenMP"},
+        "config": {"workload": WORKLOAD, "nrad": NR, "nsec": NS, "substeps": subs,
+                   "sor_sweeps_per_substep": sweeps / max(subs, 1),
+                   "timed_dts": f"DTs {args.warmup + 1}-{args.warmup + len(dts)} from t = 0 (the GPU arm's first "
+                                f"timed DTs)", "per_dt_substeps_sweeps": dts,
+                   "step": "one CFL substep of AlgoGas (whole DTs run until --steps substeps are done)",
+                   "implementation": "CPU restatement of the reference algorithm (oracle, bit-identical to the "
+                                     "reference binary), OpenMP"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{subs} substeps in {args.steps} DT/8 steps after {args.warmup} warm-up steps"},
+                         "sample": f"{subs} substeps ({len(dts)} whole DTs) after {args.warmup} warm-up DTs"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

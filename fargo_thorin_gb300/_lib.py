@@ -26,6 +26,7 @@ SIGNATURES = {
     "thorin_gpu_refresh": (C.c_int, [_P, C.c_int]),
     "thorin_gpu_set_profile": (C.c_int, [_P, C.c_int, _D]),
     "thorin_gpu_get_profile": (C.c_int, [_P, C.c_int, _D]),
+    "thorin_gpu_get_rings": (C.c_int, [_P, _D, _D, _D, _D]),
     "thorin_gpu_set_time": (C.c_int, [_P, C.c_double]),
     "thorin_gpu_cfl": (C.c_int, [_P, C.c_double, C.c_double, C.POINTER(C.c_int)]),
     "thorin_gpu_accrete": (C.c_int, [_P, C.POINTER(ThorinPlanets), C.c_double]),

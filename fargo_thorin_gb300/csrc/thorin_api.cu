@@ -691,6 +691,18 @@ extern "C" int thorin_gpu_get_profile(thorin_disk *d, int profile, double *host)
   return THORIN_OK;
 }
 
+extern "C" int thorin_gpu_get_rings(thorin_disk *d, double *rinf, double *rsup, double *rmed, double *surf)
+{
+  if (!d) return THORIN_ERR_ARG;
+  for (int i = 0; i < d->nr; i++) {
+    if (rinf) rinf[i] = d->Rinf[i];
+    if (rsup) rsup[i] = d->Rsup[i];
+    if (rmed) rmed[i] = d->Rmed[i];
+    if (surf) surf[i] = d->Surf[i];
+  }
+  return THORIN_OK;
+}
+
 extern "C" int thorin_gpu_set_time(thorin_disk *d, double t)
 {
   d->PhysicalTime = t;

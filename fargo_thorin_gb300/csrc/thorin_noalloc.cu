@@ -11,12 +11,16 @@
 // The per-ring partial sums live in a fixed file-scope device array sized
 // for the largest ring count the reference supports (MAX1D = 16384 rings,
 // src_main/types.h:65).  Its device address is looked up once per GPU, on
-// the first call made while that GPU is current; make that first call
-// before any stream capture.  Every call on a GPU reuses the same array and
+// the first call made while that GPU is current, and again whenever the
+// GPU's current context is not the one of the last look-up (a
+// cudaDeviceReset destroys the context and with it the array's old
+// address); make the first call, and the first after a reset, before any
+// stream capture.  Every call on a GPU reuses the same array and
 // overwrites each ring's slot before reading it, so nothing has to start at
 // zero; two calls whose kernels overlap on the same GPU (e.g. issued on
 // different streams without ordering) race on the array and must not be
 // made.
+#include <cuda.h>
 #include <mutex>
 #include <string>
 #include "thorin_kernels.cuh"
@@ -71,12 +75,40 @@ __global__ void __launch_bounds__(1024) k_integrals_rings_sum(const double *__re
 
 static std::mutex g_noalloc_mutex;
 static double *g_noalloc_ptr[64];
+static unsigned long long g_noalloc_ctx[64];    // context ID of each look-up (IDs are never reused)
 // Message of the last failure, read back through thorin_gpu_last_error().
 extern thread_local std::string g_last_error;
 #define g_noalloc_error g_last_error
 
+// ID of the calling thread's current CUDA context (0 if there is none).
+// The two driver calls are reached through the runtime's entry-point query,
+// so the library needs no link against the driver library (and still loads
+// on a machine without one).
+static unsigned long long current_context_id()
+{
+  typedef CUresult (*GetCurrentFn)(CUcontext *);
+  typedef CUresult (*GetIdFn)(CUcontext, unsigned long long *);
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void *f1 = nullptr, *f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return 0;
+    get_current = (GetCurrentFn)f1;
+    get_id = (GetIdFn)f2;
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
 // Device address of the partials array on the current GPU, looked up the
-// first time this GPU is seen.
+// first time this GPU is seen and again when its context has changed.
 static int noalloc_scratch(double **ptr)
 {
   int dev = 0;
@@ -84,7 +116,10 @@ static int noalloc_scratch(double **ptr)
   if (e != cudaSuccess) { g_noalloc_error = std::string("cudaGetDevice: ") + cudaGetErrorString(e); return THORIN_ERR_CUDA; }
   if (dev < 0 || dev >= 64) { g_noalloc_error = "device index out of range"; return THORIN_ERR_ARG; }
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
+  unsigned long long ctx = current_context_id();
+  if (!g_noalloc_ptr[dev] || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
+    // the look-up also makes the runtime set up the device's primary context
+    // when none is current yet
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_partials);
     if (e != cudaSuccess || !p) {
@@ -92,6 +127,7 @@ static int noalloc_scratch(double **ptr)
       return THORIN_ERR_CUDA;
     }
     g_noalloc_ptr[dev] = (double *)p;
+    g_noalloc_ctx[dev] = current_context_id();
   }
   *ptr = g_noalloc_ptr[dev];
   return THORIN_OK;

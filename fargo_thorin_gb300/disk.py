@@ -58,6 +58,13 @@ class GpuDisk:
         assert a.size == (self.nr + 1) * self.ns
         _lib.check(self.L.thorin_gpu_upload(self.h, fid, a.ctypes.data_as(C.POINTER(C.c_double))), "upload")
 
+    def rings(self):
+        """Rinf, Rsup, Rmed and Surf of the disk's grid (FillPolar1DArrays)."""
+        arrs = [np.zeros(self.nr) for _ in range(4)]
+        _lib.check(self.L.thorin_gpu_get_rings(self.h, *[a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs]),
+                   "get_rings")
+        return tuple(arrs)
+
     def set_opacity_table(self, rows, cols, pgrid, tgrid, planck, rosseland):
         """OpacityTable SM03 gas table (InitOpacities, Opacity2.c:247-297)."""
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (pgrid, tgrid, planck, rosseland)]

@@ -225,6 +225,12 @@ int thorin_gpu_refresh(thorin_disk *d, int flags);
 int thorin_gpu_set_profile(thorin_disk *d, int profile, const double *host);
 int thorin_gpu_get_profile(thorin_disk *d, int profile, double *host);
 
+/* The disk's ring geometry as FillPolar1DArrays builds it
+ * (src_main/SourceEuler.c:68-131): inner and outer interface radius, the
+ * cell-centre radius and the cell area of every ring (nrad doubles each;
+ * any pointer may be NULL).  Host copies. */
+int thorin_gpu_get_rings(thorin_disk *d, double *rinf, double *rsup, double *rmed, double *surf);
+
 /* Rotation rate of the frame, e.g. OmegaFrame of omegaframe.dat at a
  * restart (GetOmegaFrame, Output.c:280-310). */
 int thorin_gpu_set_frame(thorin_disk *d, double omega_frame);
@@ -306,7 +312,9 @@ int thorin_gpu_get_stream(thorin_disk *d, void **stream);
  * Limit: 1 <= nrad <= 16384 (the reference's MAX1D); larger grids are
  * rejected with THORIN_ERR_ARG.  The partial sums use one fixed device array
  * per GPU, found on the first call made while that GPU is current (make that
- * call before any stream capture); concurrent calls on one GPU race on it. */
+ * call before any stream capture) and found again when the GPU's context
+ * has changed since (after a cudaDeviceReset, say); concurrent calls on one
+ * GPU race on it. */
 int thorin_integrals_static(const double *rho, const double *vrad, const double *vtheta, const double *energy,
                             const double *surf, const double *rinf, const double *rsup, const double *rmed,
                             int nrad, int nsec, double omega_frame, double *out, void *stream);

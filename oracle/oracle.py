@@ -66,6 +66,8 @@ def lib(omp: bool = False):
         L.ora_sor_omega.restype = C.c_double
         L.ora_sor_omega.argtypes = [C.c_void_p]
         L.ora_set_sor_state.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int]
+        L.ora_get_sor_state.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_int)]
         _D = C.POINTER(C.c_double)
         L.ora_set_opacity_table.argtypes = [C.c_int, C.c_int, _D, _D, _D, _D]
         _libs[path] = L
@@ -123,6 +125,11 @@ class OracleDisk:
         vals = [C.c_double() for _ in range(5)]
         self.L.ora_integrals(self.h, *[C.byref(v) for v in vals])
         return tuple(v.value for v in vals)
+
+    def sor_state(self):
+        om, dom, nl = C.c_double(), C.c_double(), C.c_int()
+        self.L.ora_get_sor_state(self.h, C.byref(om), C.byref(dom), C.byref(nl))
+        return om.value, dom.value, nl.value
 
     def set_sor_state(self, omega: float, domega: float, niterlast: int):
         self.L.ora_set_sor_state(self.h, omega, domega, niterlast)

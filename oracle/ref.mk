@@ -1,9 +1,11 @@
-# Builds the reference FARGO_THORIN sequential binary straight from its sources
-# (no use of the reference's own build system) into oracle/_ref/.
-# Usage: make -f oracle/ref.mk REF=/path/to/reference [OMP=1]
+# Builds the reference FARGO_THORIN binary straight from its sources (no use
+# of the reference's own build system) into oracle/_ref/.
+# Usage: make -f oracle/ref.mk REF=<reference source tree> [OMP=1] [SOREPS=1e-8]
 # The REBOUND OpenGL viewer (display.c, glad.c) is compiled out in the
 # reference (OPENGL is empty) and is left out here.
-REF    ?= /root/reference
+ifeq ($(REF),)
+  $(error REF must name the reference source tree)
+endif
 OUT    ?= $(dir $(lastword $(MAKEFILE_LIST)))_ref
 CC     ?= gcc
 # -std=c99 keeps gcc from contracting a*b+c into FMAs, as the reference build does.
@@ -23,16 +25,29 @@ else
   SUFFIX :=
   XFLAGS := mpi_dummy.c
 endif
-# SOREPS is hard-coded in EnergySources.c; SOREPS_OVERRIDE builds a variant
-# with another tolerance by pre-defining it through a forced include.
+# SOREPS, the SOR tolerance, is a #define in EnergySources.c (line 23).  A
+# variant with another tolerance compiles that one file from a stream edit of
+# the source (sed to the compiler's standard input, no copy on disk) and the
+# rest unchanged.
 ifneq ($(SOREPS),)
   SUFFIX := $(SUFFIX)_soreps$(SOREPS)
-  SORDEF := -include $(OUT)/soreps$(SOREPS).h
+  SORMAIN := $(filter-out EnergySources.c,$(MAINSRC))
+  SOROBJ := $(abspath $(OUT))/EnergySources_soreps$(SOREPS)$(if $(filter 1,$(OMP)),_omp,).o
+else
+  SORMAIN := $(MAINSRC)
+  SOROBJ :=
 endif
 
 all: $(OUT)/thorin$(SUFFIX)
 
-$(OUT)/thorin$(SUFFIX): $(addprefix $(REF)/src_main/,$(MAINSRC)) $(addprefix $(REF)/src_reb/,$(REBSRC))
+ifneq ($(SOREPS),)
+$(SOROBJ): $(REF)/src_main/EnergySources.c
 	mkdir -p $(OUT)
-	cd $(REF)/src_main && $(CC) $(CFLAGS) $(SORDEF) -I../src_reb $(MAINSRC) $(XFLAGS) \
+	sed 's/^#define SOREPS .*/#define SOREPS $(SOREPS)/' $< | \
+	  $(CC) $(CFLAGS) $(if $(filter 1,$(OMP)),-fopenmp -DOPENMP,) -I$(REF)/src_main -I$(REF)/src_reb -x c -c - -o $@
+endif
+
+$(OUT)/thorin$(SUFFIX): $(addprefix $(REF)/src_main/,$(MAINSRC)) $(addprefix $(REF)/src_reb/,$(REBSRC)) $(SOROBJ)
+	mkdir -p $(OUT)
+	cd $(REF)/src_main && $(CC) $(CFLAGS) -I../src_reb $(SORMAIN) $(SOROBJ) $(XFLAGS) \
 	  $(addprefix ../src_reb/,$(REBSRC)) -o $(abspath $@) -lm

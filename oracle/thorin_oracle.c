@@ -2617,6 +2617,14 @@ void ora_integrals(ora_disk *d, double *mass, double *mom, double *energy, doubl
   *mass = m; *mom = 0.5 * am; *energy = e; *pmass = pm; *pmom = 0.5 * pam;
 }
 
+/* The SOR omega schedule: omega, its step and the last iteration count. */
+void ora_get_sor_state(const ora_disk *d, double *omega, double *domega, int *niterlast)
+{
+  *omega = d->omega;
+  *domega = d->domega;
+  *niterlast = d->Niterlast;
+}
+
 /* Continue an SOR omega schedule instead of calibrating it (used to time
  * steady-state substeps). */
 void ora_set_sor_state(ora_disk *d, double omega, double domega, int niterlast)

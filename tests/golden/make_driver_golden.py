@@ -13,7 +13,8 @@ oracle/_ref/thorin) the way a user does and records every file it writes:
 
 The planet sits at a = 1.05, off the ring interfaces, so that the different
 N-body integrators (REBOUND's IAS15 there, the library's RK4 here) give the
-same cells near the planet.  Usage: python tests/golden/make_driver_golden.py
+same cells near the planet.
+Usage: THORIN_REFERENCE=<reference tree> python tests/golden/make_driver_golden.py
 """
 from __future__ import annotations
 
@@ -32,7 +33,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from fargo_thorin_gb300 import workloads  # noqa: E402
 
-REF = os.environ.get("THORIN_REFERENCE", "/root/reference")
+REF = os.environ.get("THORIN_REFERENCE", "")
 THORIN = os.path.join(ROOT, "oracle", "_ref", "thorin")
 NR, NS = 20, 60
 
@@ -150,6 +151,8 @@ def make_run(kind):
 
 
 if __name__ == "__main__":
+    if not REF or not os.path.isdir(os.path.join(REF, "src_main")):
+        sys.exit("set THORIN_REFERENCE to the reference FARGO_THORIN source tree")
     subprocess.run(["make", "-s", "-f", os.path.join(ROOT, "oracle", "ref.mk"), f"REF={REF}"], check=True)
     make_init()
     make_run("disk0")

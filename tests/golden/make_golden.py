@@ -3,7 +3,7 @@
 Builds the reference's sequential binary from its sources with
 oracle/ref.mk (into oracle/_ref/), runs it on small disk set-ups and stores
 its outputs as .npz fixtures next to this script.  Needs the reference tree
-(default /root/reference, or $THORIN_REFERENCE); the fixtures it writes are
+(the directory $THORIN_REFERENCE names); the fixtures it writes are
 committed so that the tests never need the reference at run time.
 
 Each case runs the reference twice, like the measured workloads prescribe:
@@ -15,7 +15,7 @@ path.  Recorded: the initial dump, field dumps after chosen DTs, the -a
 integrals after every DT, the -d SOR iteration counts and CFL substep counts,
 and the planet state of the torque log (tqwk0.dat, written every DT).
 
-Usage: python tests/golden/make_golden.py [case ...]
+Usage: THORIN_REFERENCE=<reference tree> python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -33,14 +33,22 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from fargo_thorin_gb300 import workloads  # noqa: E402
 
-REF = os.environ.get("THORIN_REFERENCE", "/root/reference")
-THORIN = os.path.join(ROOT, "oracle", "_ref", "thorin")
+REF = os.environ.get("THORIN_REFERENCE", "")
+REF_OUT = os.path.join(ROOT, "oracle", "_ref")
 
-# name: (kind, nrad, nsec, ntot, ninterm, extra in.par lines, full-field snapshots?)
+# Stellar irradiation and its parameters as the reference's shipped
+# in_relax/in.par sets them (lines 9-21)
+IRRADIATION = ("StellarIrradiation YES\nOpacityDrop 0.6\nEffectiveTemperature 4370.0\nStellarRadius 1.5\n"
+               "DiscAlbedo 0.5\n")
+
+# name: (kind, nrad, nsec, ntot, ninterm, extra in.par lines, full-field snapshots?
+#        [, planet row [, command-line flags [, SOREPS of the reference build]]])
+# full: True = every output in full; "last" = the last output in full and
+# sampled rows + ring means before it; False = sampled rows + ring means only
 CASES = {
     "disk0_24x72": ("disk0", 24, 72, 4, 1, "", True),
     "disk1_32x96": ("disk1", 32, 96, 3, 1, "", True),
-    "disk0_128x384_200": ("disk0", 128, 384, 200, 100, "", False),
+    "disk0_128x384_200": ("disk0", 128, 384, 200, 100, "", "last"),
     "disk1_64x192_40": ("disk1", 64, 192, 40, 20, "", False),
     # in.par options beyond the two measured set-ups
     "iso_24x72": ("disk0", 24, 72, 6, 2, "EnergyEquation NO\nWriteTemperature YES\n", True),
@@ -68,6 +76,16 @@ CASES = {
     "sm03_24x72": ("disk0", 24, 72, 6, 2, "OpacityTable SM03\n", True),
     # command-line switch -c: one CFL per DT (and a DT long enough to need substeps)
     "sloppy_peb_32x96": ("disk1", 32, 96, 6, 2, "DT 0.4\n", True, None, "c"),
+    # the opacity laws and the stellar irradiation of the shipped examples
+    "zhu12irr_24x72": ("disk0", 24, 72, 6, 2, "OpacityTable ZHU12\n" + IRRADIATION, True),
+    "zhu12irr_peb_32x96": ("disk1", 32, 96, 6, 2, "OpacityTable ZHU12\n" + IRRADIATION, True),
+    "lp85_24x72": ("disk0", 24, 72, 6, 2, "OpacityTable LP85\n", True),
+    "lp85irr_24x72": ("disk0", 24, 72, 6, 2, "OpacityTable LP85\n" + IRRADIATION, True),
+    "constopa_24x72": ("disk0", 24, 72, 6, 2, "ParametricOpacity 2.0\n", True),
+    "bl94irr_24x72": ("disk0", 24, 72, 6, 2, IRRADIATION, True),
+    # the pebble + embryo disk at the SOR tolerance of the measured workload
+    # (SOREPS is a compile-time constant of the reference, EnergySources.c:23)
+    "disk1_48x144_eps8": ("disk1", 48, 144, 10, 5, "", True, None, "", "1e-8"),
 }
 
 
@@ -93,8 +111,12 @@ PEB = ["pebbledens", "pebblevrad", "pebblevtheta"]
 SAMPLE_ROWS_FRAC = [0.0, 0.3, 0.5, 0.75, 1.0]
 
 
-def build_reference():
-    subprocess.run(["make", "-s", "-f", os.path.join(ROOT, "oracle", "ref.mk"), f"REF={REF}"], check=True)
+def build_reference(soreps=""):
+    if not REF or not os.path.isdir(os.path.join(REF, "src_main")):
+        sys.exit("set THORIN_REFERENCE to the reference FARGO_THORIN source tree")
+    extra = [f"SOREPS={soreps}"] if soreps else []
+    subprocess.run(["make", "-s", "-f", os.path.join(ROOT, "oracle", "ref.mk"), f"REF={REF}", *extra], check=True)
+    return os.path.join(REF_OUT, "thorin" + (f"_soreps{soreps}" if soreps else ""))
 
 
 def read_dump(out, name, k, nr, ns):
@@ -134,6 +156,8 @@ def make_case(name):
     kind, nr, ns, ntot, ninterm, extra, full = CASES[name][:7]
     planet_override = CASES[name][7] if len(CASES[name]) > 7 else None
     flags = CASES[name][8] if len(CASES[name]) > 8 else ""
+    soreps = CASES[name][9] if len(CASES[name]) > 9 else ""
+    THORIN = build_reference(soreps)
     work = tempfile.mkdtemp(prefix="thorin_golden_")
     try:
         out = os.path.join(work, "out")
@@ -180,6 +204,8 @@ def make_case(name):
             log = run([THORIN, "-ad" + flags, "-s", "0", "in.par"], work)
         res = {"inpar": np.array(par), "planet": np.array(planet), "flags": np.array(flags), "nrad": nr, "nsec": ns,
                "ntot": ntot, "ninterm": ninterm, "kind": np.array(kind)}
+        if soreps:
+            res["soreps"] = float(soreps)
         for k, v in init.items():
             res["init_" + k] = v
         if table is not None:
@@ -189,10 +215,11 @@ def make_case(name):
         names = GAS + (PEB if kind == "disk1" else []) + (["label"] if "LabelAdvection YES" in extra else [])
         rows = sorted({min(nr - 1, int(round(f * (nr - 1)))) for f in SAMPLE_ROWS_FRAC})
         res["sample_rows"] = np.array(rows)
-        for k in range(1, ntot // ninterm + 1):
+        nout = ntot // ninterm
+        for k in range(1, nout + 1):
             for fname in names:
                 arr = read_dump(out, fname, k, nr, ns)
-                if full:
+                if full is True or (full == "last" and k == nout):
                     res[f"out{k}_{fname}"] = arr
                 else:
                     res[f"out{k}_{fname}_ringmean"] = arr.mean(axis=1)
@@ -207,6 +234,5 @@ def make_case(name):
 
 
 if __name__ == "__main__":
-    build_reference()
     for name in (sys.argv[1:] or list(CASES)):
         make_case(name)

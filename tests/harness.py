@@ -23,6 +23,8 @@ def load(name):
 
 def case_params(g, **kw):
     flags = str(g["flags"]) if "flags" in g.files else ""
+    if "soreps" in g.files:                           # a reference build with another SOR tolerance
+        kw.setdefault("sor_eps", float(g["soreps"]))
     p = derive(read_inpar(str(g["inpar"])), centrifugal_balance="b" in flags, sloppy_cfl="c" in flags, **kw)
     if p.corotating:                                  # the frame of planet 0 (main.c:161)
         corotating_frame(p, workloads.make_planets(p, [tuple(g["planet"])]))
@@ -59,3 +61,16 @@ def rel_l2(a, b):
     b = np.asarray(b, dtype=np.float64)
     nb = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
+
+
+def mass_momentum(rings, rho, vtheta, omega_frame=0.0):
+    """GasTotalMass and GasMomentum (src_main/SideEuler.c:26-60) of a density
+    and azimuthal velocity given as (nrad, nsec) arrays, summed by numpy; the
+    reference applies the same two sums to the pebble fluid.  rings = (Rinf,
+    Rsup, Rmed, Surf)."""
+    _, _, rmed, surf = (np.asarray(a)[:, None] for a in rings)
+    rho = np.asarray(rho)
+    vt = np.asarray(vtheta) + omega_frame * rmed
+    mass = float(np.sum(surf * rho))
+    mom = 0.5 * float(np.sum(surf * (rho + np.roll(rho, 1, axis=1)) * rmed * vt))
+    return mass, mom

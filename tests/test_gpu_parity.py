@@ -17,7 +17,8 @@ CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "
          "dampinit_24x72", "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
          "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72", "label_24x72",
          "corot_24x72", "corot_peb_32x96", "sm03_24x72",
-         "sloppy_peb_32x96"]
+         "sloppy_peb_32x96", "zhu12irr_24x72", "zhu12irr_peb_32x96", "lp85_24x72", "lp85irr_24x72", "constopa_24x72",
+         "bl94irr_24x72", "disk1_48x144_eps8"]
 TOL = 1e-10
 
 
@@ -65,11 +66,19 @@ def test_gpu_vs_reference_golden(name):
             assert np.isnan(t.torque_norm)
         elif ref[1] != 0.0:
             assert abs(t.torque_norm / t.torque / (ref[2] / ref[1]) - 1) < 1e-10
-        m, mom, e, _, _ = d.integrals()
+        m, mom, e, pm, pmom = d.integrals()
         assert abs(m / g["mass"][step - 1] - 1) < 1e-12
         assert abs(mom / g["momentum"][step - 1] - 1) < 1e-12
+        assert abs(e / g["energy"][step - 1] - 1) < 1e-12, f"total energy at DT {step}"
         if step % ninterm == 0:
             k = step // ninterm
+            if p.pebbles and f"out{k}_pebbledens" in g:
+                # pebble mass and angular momentum: the reference logs neither,
+                # so they are summed from its pebble field dumps
+                want = H.mass_momentum(d.rings(), g[f"out{k}_pebbledens"], g[f"out{k}_pebblevtheta"],
+                                         d.stats().omega_frame)
+                assert abs(pm / want[0] - 1) < 1e-12, f"pebble mass after {step} DT"
+                assert abs(pmom / want[1] - 1) < 1e-12, f"pebble angular momentum after {step} DT"
             for f in fields:
                 a = d.get(H.FIELD_IDS[f])[:n].reshape(nr, ns)
                 if f"out{k}_{f}" in g:
@@ -108,6 +117,10 @@ def test_gpu_vs_oracle_every_dt(name):
         for f in H.GAS + (H.PEB if p.pebbles else []) + ["energy"] + (["label"] if p.label_advection else []):
             assert H.rel_l2(d.get(H.FIELD_IDS[f])[:n], o.get(H.FIELD_IDS[f])[:n]) < 1e-11, f"{f} at DT {step}"
         assert abs(sg.x[0] - so.x[0]) < 1e-14 and abs(sg.vx[0] - so.vx[0]) < 1e-14
+        # gas mass, momentum and energy, pebble mass and momentum
+        for name_, a, b in zip(("mass", "momentum", "energy", "pebble mass", "pebble momentum"), d.integrals(),
+                               o.integrals()):
+            assert abs(a - b) <= 1e-12 * abs(b), f"{name_} at DT {step}"
 
 
 @pytest.mark.parametrize("kind,nr,ns", [("disk0", 20, 1536), ("disk1", 24, 1152)])
@@ -160,3 +173,72 @@ def test_sor_direct_launches_match_graph_loop(monkeypatch):
     assert runs[0][0] == runs[1][0]
     for a, b in zip(runs[0][1], runs[1][1]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("name,field,crashed", [("cooling_24x72", "energy", 1), ("cooling_24x72", "dens", 0),
+                                                ("disk1_32x96", "pebbledens", 1)])
+def test_detect_crash_matches_oracle(name, field, crashed):
+    """DetectCrash (src_main/SourceEuler.c:48-66, called at :272-274): one
+    negative cell uploaded from the host.  The reference overwrites the flag
+    -- density, then energy, then (with pebbles) the pebble density -- so
+    only the last test counts: a negative density alone with a positive
+    energy reports no crash.  The flag of the GPU path equals the oracle's,
+    and the run continues like the reference's (fields still within the
+    tolerance of the oracle)."""
+    g = H.load(name)
+    p = H.case_params(g)
+    d = _gpu_disk(p)
+    o = O.OracleDisk(p)
+    for x in (d, o):
+        x.init_default()
+        H.opacity_table(x, g)
+        H.start_state(x, p, {"dens": g["init_dens"].ravel(), "temper": g["init_temper"].ravel()})
+        f = x.get(H.FIELD_IDS[field])
+        l = 7 + (p.nrad // 2) * p.nsec
+        f[l] = -abs(f[l])
+        x.set(H.FIELD_IDS[field], f)
+    sg = workloads.make_planets(p, [tuple(g["planet"])])
+    so = workloads.make_planets(p, [tuple(g["planet"])])
+    d.algogas(sg)
+    assert o.algogas(so) == 0
+    assert o.stats().crashed == crashed
+    assert d.stats().crashed == crashed
+    n = p.nrad * p.nsec
+    for f in H.GAS + (H.PEB if p.pebbles else []):
+        assert H.rel_l2(d.get(H.FIELD_IDS[f])[:n], o.get(H.FIELD_IDS[f])[:n]) < 1e-11, f
+
+
+def test_gpu_vs_oracle_full_size_workload():
+    """The measured workload itself: the 1024x3072 pebble + embryo disk at
+    the SOR tolerance 1e-8, its first two DTs from t = 0 (the first one with
+    the omega calibration and the initial transient's 27 substeps), against
+    the oracle built with OpenMP.  FARGO shifts bit-exact, substep counts and
+    every SOR iteration count (calibration included) exact, fields within
+    relative L2 1e-10, gas and pebble integrals within 1e-12."""
+    import os
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    p = workloads.params_for("disk1", 1024, 3072, sor_eps=1e-8)
+    d = _gpu_disk(p)
+    o = O.OracleDisk(p, omp=True)
+    o.init_default()
+    init = {"dens": o.get(H.FIELD_IDS["dens"]).copy(), "temper": o.get(H.FIELD_IDS["temper"]).copy()}
+    d.init_default()
+    for x in (d, o):
+        H.start_state(x, p, init)
+    sg = workloads.make_planets(p, [workloads.PLANET1])
+    so = workloads.make_planets(p, [workloads.PLANET1])
+    n = p.nrad * p.nsec
+    for step in range(1, 3):
+        d.algogas(sg)
+        assert o.algogas(so) == 0
+        sd, st = d.stats(), o.stats()
+        assert sd.substeps == st.substeps, f"substeps at DT {step}"
+        assert sd.sor_sweeps == st.sor_sweeps and sd.sor_last_niter == st.sor_last_niter, f"SOR counts at DT {step}"
+        np.testing.assert_array_equal(d.nshift(), o.nshift())
+        for f in H.GAS + H.PEB + ["energy"]:
+            assert H.rel_l2(d.get(H.FIELD_IDS[f])[:n], o.get(H.FIELD_IDS[f])[:n]) < TOL, f"{f} at DT {step}"
+        for name_, a, b in zip(("mass", "momentum", "energy", "pebble mass", "pebble momentum"), d.integrals(),
+                               o.integrals()):
+            assert abs(a - b) <= 1e-12 * abs(b), f"{name_} at DT {step}"
+        assert abs(sg.x[0] - so.x[0]) < 1e-13 and abs(sg.vx[0] - so.vx[0]) < 1e-13
+    d.close()

@@ -17,7 +17,8 @@ CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "
          "dampinit_24x72", "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
          "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72", "label_24x72",
          "corot_24x72", "corot_peb_32x96", "sm03_24x72",
-         "sloppy_peb_32x96"]
+         "sloppy_peb_32x96", "zhu12irr_24x72", "zhu12irr_peb_32x96", "lp85_24x72", "lp85irr_24x72", "constopa_24x72",
+         "bl94irr_24x72", "disk1_48x144_eps8"]
 
 
 def _run(name, force_planet=True):
@@ -71,11 +72,21 @@ def test_oracle_bit_exact_vs_reference(name):
             assert st.substeps == g["substeps"][step - 1]
         if counts and len(g["sor_niter"]):          # no SOR in isothermal runs
             assert st.sor_last_niter == g["sor_niter"][step - 1]
-        m, mom, e, _, _ = d.integrals()
+        m, mom, e, pm, pmom = d.integrals()
         _same(np.array([m, mom, e]), np.array([g["mass"][step - 1], g["momentum"][step - 1], g["energy"][step - 1]]),
               f"integrals after {step} DT", exact)
         if step % ninterm == 0:
             k = step // ninterm
+            if p.pebbles and f"out{k}_pebbledens" in g:
+                # the reference logs no pebble integrals: sum its pebble dumps
+                radii = d.radii()
+                rinf, rsup = radii[:-1], radii[1:]
+                rmed = 2.0 / 3.0 * (rsup ** 3 - rinf ** 3) / (rsup ** 2 - rinf ** 2)
+                surf = np.pi * (rsup ** 2 - rinf ** 2) / ns
+                want = H.mass_momentum((rinf, rsup, rmed, surf), g[f"out{k}_pebbledens"], g[f"out{k}_pebblevtheta"],
+                                       d.stats().omega_frame)
+                assert abs(pm / want[0] - 1) < 1e-12, f"pebble mass after {step} DT"
+                assert abs(pmom / want[1] - 1) < 1e-12, f"pebble momentum after {step} DT"
             for f in fields:
                 a = d.get(H.FIELD_IDS[f])[:n].reshape(nr, ns)
                 if f"out{k}_{f}" in g:

@@ -16,20 +16,9 @@ import numpy as np
 import pytest
 
 import harness as H
-import oracle as O
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12       # summation order differs from the regular entry point
-
-
-def _ring_arrays(p):
-    """Rinf, Rsup, Rmed, Surf with the expressions of FillPolar1DArrays."""
-    radii = O.OracleDisk(p).radii()
-    rinf, rsup = radii[:-1].copy(), radii[1:].copy()
-    rmed = 2.0 / 3.0 * (rsup * rsup * rsup - rinf * rinf * rinf)
-    rmed = rmed / (rsup * rsup - rinf * rinf)
-    surf = 3.14159265358979323844 * (rsup * rsup - rinf * rinf) / float(p.nsec)
-    return rinf, rsup, rmed, surf
 
 
 def test_static_integrals_match_regular_entry_point():
@@ -44,7 +33,8 @@ def test_static_integrals_match_regular_entry_point():
     sys_ = workloads.make_planets(p, [tuple(g["planet"])])
     L = _lib.load()
     dev = torch.device("cuda", 0)
-    rinf, rsup, rmed, surf = (torch.tensor(a, dtype=torch.float64, device=dev) for a in _ring_arrays(p))
+    # the disk's own ring geometry (FillPolar1DArrays), as the regular entry point uses it
+    rinf, rsup, rmed, surf = (torch.tensor(a, dtype=torch.float64, device=dev) for a in d.rings())
     out = torch.full((3,), float("nan"), dtype=torch.float64, device=dev)
     ptr = lambda t: C.cast(t.data_ptr(), C.POINTER(C.c_double))
     for call in range(2):
