@@ -15,13 +15,11 @@ ABI with the state uploaded from pinned host buffers and downloaded back
 every step.
 
 --impl reference times the CPU restatement of the reference algorithm (the
-oracle, OpenMP over all host cores) on the same disk: the same warm-up DTs
-from t = 0 as the GPU arm, then the substeps of the DTs that follow, which
-are the first DTs of the GPU arm's timed region; a step of that arm is one
-CFL substep (a bounded sample of a DT, so that the run ends within a few
-minutes).  ``cpu_baseline`` in the GPU line runs the oracle from the GPU
-arm's own snapshot, i.e. on exactly the first timed DTs, and checks their
-substep and SOR sweep counts against the GPU's.
+oracle, OpenMP over all host cores) on the same disk and the same DTs: the
+GPU arm's warm-up DTs from t = 0, then its --steps timed DTs (about 4 s per
+DT on 16 Grace cores).  ``cpu_baseline`` in the GPU line runs the oracle from
+the GPU arm's own snapshot, i.e. on the first timed DTs, for about 20 s, and
+checks their substep and SOR sweep counts against the GPU's.
 With torchrun (N > 1) every rank advances its own replica (the disk does not
 shard); rank 0 prints the line.
 """
@@ -482,8 +480,7 @@ def cpu_baseline(p, snap, snap_sor, snap_time, snap_sys, per_dt, budget_s=20.0):
 
 def run_reference(args):
     """The oracle on all host cores: the GPU arm's warm-up DTs from t = 0,
-    then --steps substeps of the DTs that follow (the GPU arm's first timed
-    DTs), each substep one step."""
+    then its --steps timed DTs, each DT one step."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
@@ -493,11 +490,9 @@ def run_reference(args):
     p, o, s = oracle_disk(O)
     for _ in range(args.warmup):
         o.algogas(s)
-    # advance whole DTs until --steps substeps are done; the oracle's step
-    # counter counts substeps, so time the DTs and keep the count
     t0 = time.perf_counter()
     subs, dts, w0 = 0, [], o.stats().sor_sweeps
-    while subs < args.steps:
+    for _ in range(args.steps):
         wd = o.stats().sor_sweeps
         o.algogas(s)
         st = o.stats()
@@ -508,17 +503,17 @@ def run_reference(args):
     value = NR * NS * subs / el
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": el * 1e3 / subs, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "nrad": NR, "nsec": NS, "substeps": subs,
                    "sor_sweeps_per_substep": sweeps / max(subs, 1),
-                   "timed_dts": f"DTs {args.warmup + 1}-{args.warmup + len(dts)} from t = 0 (the GPU arm's first "
-                                f"timed DTs)", "per_dt_substeps_sweeps": dts,
-                   "step": "one CFL substep of AlgoGas (whole DTs run until --steps substeps are done)",
+                   "timed_dts": f"DTs {args.warmup + 1}-{args.warmup + args.steps} from t = 0",
+                   "per_dt_substeps_sweeps": dts, "step": "one DT of AlgoGas (all CFL substeps)",
                    "implementation": "CPU restatement of the reference algorithm (oracle, bit-identical to the "
                                      "reference binary), OpenMP"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{subs} substeps ({len(dts)} whole DTs) after {args.warmup} warm-up DTs"},
+                         "sample": f"{args.steps} DTs ({subs} substeps, {sweeps} SOR sweeps) after {args.warmup} "
+                                   f"warm-up DTs, {el:.1f} s"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -32,6 +32,9 @@ SIGNATURES = {
     "thorin_gpu_accrete": (C.c_int, [_P, C.POINTER(ThorinPlanets), C.c_double]),
     "thorin_gpu_forces": (C.c_int, [_P, C.POINTER(ThorinPlanets), C.c_double, _D, _D, _D]),
     "thorin_gpu_hydro": (C.c_int, [_P, C.c_double]),
+    "thorin_advance_from_disk": (C.c_int, [_P, C.POINTER(ThorinPlanets), C.c_double, _D, _D, _D]),
+    "thorin_gpu_correct_vtheta": (C.c_int, [_P, C.c_double]),
+    "thorin_gpu_stokes": (C.c_int, [_P]),
     "thorin_gpu_algogas": (C.c_int, [_P, C.POINTER(ThorinPlanets)]),
     "thorin_gpu_integrals": (C.c_int, [_P, _D, _D, _D, _D, _D]),
     "thorin_gpu_get_nshift": (C.c_int, [_P, C.POINTER(C.c_int)]),

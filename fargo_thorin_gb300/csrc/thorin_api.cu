@@ -1184,7 +1184,7 @@ extern "C" int thorin_gpu_cfl(thorin_disk *d, double dt_remaining, double invdtr
   if (p.pebbles) aux_stokes(d->g, d->rho, d->psize, d->tau, d->s);       // PebbleStokesNumbers
   CflFinal f;
   memset(&f, 0, sizeof(f));
-  f.pebbles = p.pebbles && !d->sloppy_pass;   // SloppyCFL: CriticalCharTime is never called (rate 0)
+  f.pebbles = p.pebbles && !d->sloppy_pass && !p.sloppy_cfl;   // SloppyCFL: CriticalCharTime is never called (rate 0)
   f.first_call = d->cfl_first;
   f.deltaT = dt_remaining;
   f.invdtreb_sq = invdtreb_sq;
@@ -1199,6 +1199,14 @@ extern "C" int thorin_gpu_cfl(thorin_disk *d, double dt_remaining, double invdtr
   CUCHK(cudaMemcpyAsync(d->iscal_h, d->iscal, sizeof(int) * IS_COUNT, cudaMemcpyDeviceToHost, d->s));
   CUCHK(cudaStreamSynchronize(d->s));
   *n_sub = d->iscal_h[IS_NSUB];
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_stokes(thorin_disk *d)
+{
+  if (!d) return THORIN_ERR_ARG;
+  if (d->p.pebbles) aux_stokes(d->g, d->rho, d->psize, d->tau, d->s);
+  KCHECK("Stokes kernel");
   return THORIN_OK;
 }
 
@@ -1814,6 +1822,24 @@ static void advance_from_disk(thorin_disk *d, thorin_planets *sys, double dt, co
     sys->vx[k] += dt * ind[0];
     sys->vy[k] += dt * ind[1];
   }
+}
+
+extern "C" int thorin_advance_from_disk(const thorin_disk *d, thorin_planets *sys, double dt, const double indirect[2],
+                                        const double *ring_rho, const double *ring_cs)
+{
+  if (!d || !sys || !indirect || !ring_rho || !ring_cs || sys->nb > MAXPL_DEV) return THORIN_ERR_ARG;
+  advance_from_disk(const_cast<thorin_disk *>(d), sys, dt, indirect, ring_rho, ring_cs);
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_correct_vtheta(thorin_disk *d, double domega)
+{
+  if (!d) return THORIN_ERR_ARG;
+  aux_correct_vtheta(d->g, d->vtheta, domega, d->s);
+  if (d->p.pebbles) aux_correct_vtheta(d->g, d->pvtheta, domega, d->s);
+  KCHECK("CorrectVtheta kernel");
+  d->OmegaFrame += domega;
+  return THORIN_OK;
 }
 
 // StokesDrag + AdvanceSystemFromDrag (Drag.c:17-119): the drag of the gas in

@@ -247,6 +247,11 @@ int thorin_gpu_set_time(thorin_disk *d, double physical_time);
  * for the remaining interval dt_remaining. */
 int thorin_gpu_cfl(thorin_disk *d, double dt_remaining, double invdtreb_sq, int *n_sub);
 
+/* PebbleStokesNumbers alone (Pebbles.c:280-300), for the substeps of a
+ * SloppyCFL run, where thorin_gpu_cfl is called once per DT
+ * (SourceEuler.c:221-235).  Without pebbles it does nothing. */
+int thorin_gpu_stokes(thorin_disk *d);
+
 /* InitHeating + AccretePebblesOntoPlanets + Heating1 + EvaporatePebbles
  * (Planet.c:222-258, Pebbles.c:353-539, Pebbles.c:834-864).  Updates the
  * planets' masses and velocities in sys. */
@@ -265,6 +270,18 @@ int thorin_gpu_forces(thorin_disk *d, thorin_planets *sys, double mass_taper,
  * SOR, transport, EOS refresh, pebble transport (SourceEuler.c:270-313).
  * Advances the clock by dt. */
 int thorin_gpu_hydro(thorin_disk *d, double dt);
+
+/* AdvanceSystemFromDisk with DampingTW04 (Pframeforce.c:514-603): kicks the
+ * velocities of the planets that feel the disk by dt times the disk and
+ * indirect accelerations of the last thorin_gpu_forces call, which also
+ * returned indirect, ring_rho and ring_cs.  Host arithmetic only. */
+int thorin_advance_from_disk(const thorin_disk *d, thorin_planets *sys, double dt, const double indirect[2],
+                             const double *ring_rho, const double *ring_cs);
+
+/* CorrectVtheta and CorrectPebblesVtheta (SideEuler.c:505-519) of a
+ * corotating frame whose rate changes by domega: v_theta -= domega * Rmed
+ * for the gas (and the pebbles), and OmegaFrame += domega. */
+int thorin_gpu_correct_vtheta(thorin_disk *d, double domega);
 
 /* ---- whole-DT driver ---- */
 
