@@ -9,6 +9,7 @@ import re
 import subprocess
 import sys
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -152,3 +153,72 @@ def test_reference_arm_nonzero_rank_exits():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference"], env=env,
                        capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_ensemble_partition_is_disjoint_balanced_and_deterministic():
+    from fargo_thorin_gb300.sharding import partition
+    rng = np.random.default_rng(3)
+    nr = rng.choice([128, 192, 256, 384, 512], size=64)
+    cells = [int(3 * n * n) for n in nr]
+    for world in (1, 2, 3, 4, 8):
+        shards = partition(cells, world)
+        flat = sorted(k for s in shards for k in s)
+        assert flat == list(range(len(cells)))                  # every disk exactly once
+        loads = [sum(cells[k] for k in s) for s in shards]
+        # LPT bound: no rank exceeds the mean load by more than the largest disk
+        assert max(loads) <= sum(cells) / world + max(cells)
+        assert partition(cells, world) == shards                # same answer on every rank
+
+
+class _StubDisk:
+    """A host stand-in for a GPU disk: one DT = a fixed number of substeps."""
+
+    def __init__(self, cells, substeps):
+        self.cells, self.substeps = cells, substeps
+
+    def step(self):
+        return self.cells * self.substeps
+
+
+def _shard_rank(rank, ws, port, cells, q):
+    import time
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    sys.path.insert(0, ROOT)
+    from fargo_thorin_gb300 import sharding
+    mine = sharding.shard_of(cells, rank, ws)
+    disks = [_StubDisk(cells[k], 2 + k % 3) for k in mine]
+    t0 = time.perf_counter()
+    upd = sum(d.step() for d in disks)
+    local = {"disks": len(disks), "cells": sum(d.cells for d in disks), "cell_updates": upd,
+             "seconds": time.perf_counter() - t0 + 1e-3 * (rank + 1), "indices": mine}
+    got = sharding.gather_metrics(local)
+    dist.destroy_process_group()
+    q.put((rank, got))
+
+
+def test_sharded_ensemble_gathers_metrics_gloo():
+    """Two ranks take disjoint shards of an ensemble and gather their
+    metrics on the host; no data-path collective is involved."""
+    import multiprocessing as mp
+    from fargo_thorin_gb300.sharding import combine
+    cells = [3 * n * n for n in (128, 512, 256, 384, 192, 512, 128, 256, 384)]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29600 + os.getpid() % 1000
+    procs = [ctx.Process(target=_shard_rank, args=(r, 2, port, cells, q)) for r in range(2)]
+    for pr in procs:
+        pr.start()
+    res = dict(q.get(timeout=120) for _ in procs)
+    for pr in procs:
+        pr.join(60)
+        assert pr.exitcode == 0
+    assert res[0] == res[1]                                     # every rank sees the same gather
+    metrics = res[0]
+    idx = metrics[0]["indices"] + metrics[1]["indices"]
+    assert sorted(idx) == list(range(len(cells))) and not set(metrics[0]["indices"]) & set(metrics[1]["indices"])
+    tot = combine(metrics)
+    assert tot["disks"] == len(cells)
+    assert tot["cell_updates"] == sum(c * (2 + k % 3) for k, c in enumerate(cells))
+    assert tot["seconds"] == max(m["seconds"] for m in metrics)
