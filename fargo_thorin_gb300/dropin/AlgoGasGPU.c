@@ -30,7 +30,7 @@
 
 /* switches the reference keeps as globals outside its headers */
 extern boolean OpenInner, OpenOuter, NonReflecting, OuterSourceMass, FastTransport, IsDisk, Corotating;
-extern boolean Indirect_Term, Restart, DumpTorqueNow;
+extern boolean Indirect_Term, Restart, DumpTorqueNow, GuidingCenter;
 extern int begin_i;
 extern real ScalingFactor;
 
@@ -149,6 +149,7 @@ static void params_from_reference(thorin_params *p)
   p->centrifugal_balance = CentrifugalBalance;
   p->label_advection = AdvecteLabel;
   p->corotating = Corotating;
+  p->guiding_center = GuidingCenter;
 }
 
 /* A raw field file of the output directory (nrad x nsec doubles, the layout

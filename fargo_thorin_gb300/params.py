@@ -161,7 +161,7 @@ class ThorinParams(C.Structure):
         ("evaporation_rate", C.c_double), ("evaporation_temperature", C.c_double), ("heating_delay", C.c_int),
         ("parametric_accretion", C.c_double), ("prescribed_accretion", C.c_int),
         ("sor_eps", C.c_double), ("sor_maxiters", C.c_int), ("centrifugal_balance", C.c_int),
-        ("label_advection", C.c_int), ("corotating", C.c_int),
+        ("label_advection", C.c_int), ("corotating", C.c_int), ("guiding_center", C.c_int),
     ]
 
     def as_dict(self):
@@ -264,9 +264,8 @@ def derive(v: dict, *, sor_eps: float = SOREPS, sor_maxiters: int = SORMAXITERS,
     p.planetary_density = v["PLANETARYDENSITY"]
     p.aerodynamic_drag = int(_yes(v["AERODYNAMICDRAG"], "Y"))
     p.omega_frame = v["OMEGAFRAME"]
-    if _yes(v["FRAME"], "G"):
-        raise ValueError("Frame GuidingCenter is not supported (fixed or corotating frames only)")
-    p.corotating = int(_yes(v["FRAME"], "C"))
+    p.guiding_center = int(_yes(v["FRAME"], "G"))          # Interpret.c:165-169
+    p.corotating = int(_yes(v["FRAME"], "C") or p.guiding_center)
     p.fast_transport = int(not _yes(v["TRANSPORT"], "S"))
     ib, ob = v["INNERBOUNDARY"], v["OUTERBOUNDARY"]
     p.open_inner = int(_yes(ib, "O"))
@@ -326,15 +325,53 @@ def read_planet_config(text: str):
     return out
 
 
+def orbit_elements(m, x, y, z, vx, vy, vz):
+    """Semi-major axis, eccentricity, inclination and mean anomaly of a body
+    of mass m about a unit-mass primary at rest at the origin (G = 1), as
+    REBOUND's reb_tools_particle_to_orbit defines them (src_reb/tools.c:
+    578-686; Murray & Dermott ch. 2)."""
+    def acos_ratio(num, den, sign):
+        c = num / den if den != 0.0 else math.nan
+        if -1.0 < c < 1.0:
+            v = math.acos(c)
+            return -v if sign < 0.0 else v
+        return math.pi if c <= -1.0 else 0.0
+    mu = m + 1.0
+    d = math.sqrt(x * x + y * y + z * z)
+    v2 = vx * vx + vy * vy + vz * vz
+    vc2 = mu / d
+    a = -mu / (v2 - 2.0 * vc2)
+    hx, hy, hz = y * vz - z * vy, z * vx - x * vz, x * vy - y * vx
+    h = math.sqrt(hx * hx + hy * hy + hz * hz)
+    vr = (x * vx + y * vy + z * vz) / d
+    rvr, muinv, vd2 = d * vr, 1.0 / mu, v2 - vc2
+    ex, ey, ez = (muinv * (vd2 * x - rvr * vx), muinv * (vd2 * y - rvr * vy), muinv * (vd2 * z - rvr * vz))
+    e = math.sqrt(ex * ex + ey * ey + ez * ez)
+    inc = acos_ratio(hz, h, 1.0)
+    if e < 1.0:
+        ea = acos_ratio(1.0 - d / a, e, vr)
+        mean = ea - e * math.sin(ea)
+    else:
+        ea = math.acosh((1.0 - d / a) / e)
+        ea = -ea if vr < 0.0 else ea
+        mean = e * math.sinh(ea) - ea
+    return a, e, inc, mean
+
+
 def corotating_frame(p: ThorinParams, planets) -> None:
     """Frame COROTATING: the run starts in the frame of planet 0, rotating at
-    its angular speed (x vy - y vx) / (x^2 + y^2) (GetPsysInfo FREQUENCY,
+    its angular speed (x vy - y vx) / (x^2 + y^2); Frame GUIDINGCENTER: at
+    the mean motion sqrt((1 + m) / a^3) of its orbit (GetPsysInfo FREQUENCY,
     Psys.c:195-262; main.c:161)."""
     if p.corotating:
         if planets.nb < 1:
             raise ValueError("Frame COROTATING needs a planet")
         x, y, vx, vy = planets.x[0], planets.y[0], planets.vx[0], planets.vy[0]
-        p.omega_frame = (x * vy - y * vx) / (x * x + y * y)
+        if p.guiding_center:
+            a = orbit_elements(planets.mass[0], x, y, planets.z[0], vx, vy, planets.vz[0])[0]
+            p.omega_frame = math.sqrt((planets.mass[0] + 1.0) / (a * a * a))
+        else:
+            p.omega_frame = (x * vy - y * vx) / (x * x + y * y)
 
 
 def read_opacity_table(path: str):

@@ -150,6 +150,9 @@ typedef struct thorin_params {
   int    label_advection;        /* LabelAdvection YES: a passive tracer    */
   int    corotating;             /* Frame COROTATING: the frame follows planet 0
                                     (omega_frame starts at its angular speed) */
+  int    guiding_center;         /* Frame GUIDINGCENTER (implies corotating): the
+                                    frame follows planet 0's guiding centre when its
+                                    orbit is eccentric and inclined (Psys.c:195-262) */
 } thorin_params;
 
 /* The planetary system as seen by the hydro loop (src_main/types.h:96-115). */

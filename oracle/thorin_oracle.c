@@ -2508,6 +2508,55 @@ static void RotatePsys(thorin_planets *sys, double angle)   /* Psys.c:336-355 */
 /* ------------------------------------------------------------------ */
 /* AlgoGas: SourceEuler.c:210-317 (fixed frame, SloppyCFL off).  Returns a
  * THORIN_* status. */
+/* The point whose angle a corotating frame follows (GetPsysInfo and
+ * GetPsysInfoFromRsim, Psys.c:195-330): planet 0 itself, or with Frame
+ * GUIDINGCENTER and an orbit both eccentric and inclined (e, inc > 1e-8),
+ * its guiding centre a (cos, sin)(M + periapsis angle) cos(inc).  a, e, inc
+ * and the mean anomaly M are REBOUND's reb_tools_particle_to_orbit
+ * (src_reb/tools.c:578-686) for a unit-mass primary at rest at the origin
+ * and G = 1. */
+static double frame_acos(double num, double den, double sign)   /* acos2, tools.c:563-576 */
+{
+  double c = num / den;
+  if (c > -1.0 && c < 1.0) {
+    double v = acos(c);
+    return sign < 0.0 ? -v : v;
+  }
+  return (c <= -1.0) ? M_PI : 0.0;
+}
+
+static void frame_point(int guiding_center, const thorin_planets *sys, double *xc, double *yc)
+{
+  double x = sys->x[0], y = sys->y[0], z = sys->z[0], vx = sys->vx[0], vy = sys->vy[0], vz = sys->vz[0];
+  double m = sys->mass[0] + 1.0;
+  *xc = x;
+  *yc = y;
+  if (!guiding_center) return;
+  double d = sqrt(x * x + y * y + z * z);
+  double v2 = vx * vx + vy * vy + vz * vz, vc2 = m / d;
+  double a = -m / (v2 - 2.0 * vc2);
+  double hx = y * vz - z * vy, hy = z * vx - x * vz, hz = x * vy - y * vx;
+  double h = sqrt(hx * hx + hy * hy + hz * hz);
+  double vr = (x * vx + y * vy + z * vz) / d, rvr = d * vr, muinv = 1.0 / m, vd2 = v2 - vc2;
+  double ex = muinv * (vd2 * x - rvr * vx), ey = muinv * (vd2 * y - rvr * vy), ez = muinv * (vd2 * z - rvr * vz);
+  double e = sqrt(ex * ex + ey * ey + ez * ez);
+  double inc = frame_acos(hz, h, 1.0), M;
+  if (e < 1.0) {
+    double ea = frame_acos(1.0 - d / a, e, vr);
+    M = ea - e * sin(ea);
+  } else {
+    double ea = acosh((1.0 - d / a) / e);
+    if (vr < 0.0) ea = -ea;
+    M = e * sinh(ea) - ea;
+  }
+  if (e > 1e-8 && inc > 1e-8) {
+    double Ax = vy * hz - vz * hy - m * x / d, Ay = vz * hx - vx * hz - m * y / d;
+    double pa = (Ax * Ax + Ay * Ay > 0.0) ? atan2(Ay, Ax) : atan2(y, x);
+    *xc = a * cos(M + pa) * cos(inc);
+    *yc = a * sin(M + pa) * cos(inc);
+  }
+}
+
 int ora_algogas(ora_disk *d, thorin_planets *sys)
 {
   const thorin_params *p = &d->p;
@@ -2529,13 +2578,15 @@ int ora_algogas(ora_disk *d, thorin_planets *sys)
     if (p->prescribed_accretion) ParametricAccretion(d, sys, dt);
     if (p->pebbles) { AccretePebblesOntoPlanets(d, sys, dt); EvaporatePebbles(d, dt); }
     dtemp += dt;
-    double xmark = sys->x[0], ymark = sys->y[0];              /* GetPsysInfo (MARK), Psys.c:240-244 */
+    double xmark, ymark;                                       /* GetPsysInfo (MARK), Psys.c:240-244 */
+    frame_point(p->guiding_center, sys, &xmark, &ymark);
     FillForcesArrays(d, sys);
     AdvanceSystemFromDisk(d, sys, dt);
     if (p->aerodynamic_drag) AdvanceSystemFromDrag(d, sys, dt);
     AdvanceSystemNbody(sys, dt);
     if (p->corotating) {                                       /* SourceEuler.c:261-267 */
-      double x = sys->x[0], y = sys->y[0];
+      double x, y;
+      frame_point(p->guiding_center, sys, &x, &y);             /* GetPsysInfoFromRsim (GET), Psys.c:313-322 */
       double d2 = sqrt(x * x + y * y), d1 = sqrt(xmark * xmark + ymark * ymark);
       double cross = xmark * y - x * ymark;
       double OmegaNew = asin(cross / (d1 * d2)) / dt;         /* GetPsysInfo (GET), Psys.c:245-254 */

@@ -86,6 +86,11 @@ CASES = {
     # the pebble + embryo disk at the SOR tolerance of the measured workload
     # (SOREPS is a compile-time constant of the reference, EnergySources.c:23)
     "disk1_48x144_eps8": ("disk1", 48, 144, 10, 5, "", True, None, "", "1e-8"),
+    # the guiding-centre frame follows an eccentric, inclined planet
+    "gc_24x72": ("disk0", 24, 72, 6, 2, "Frame GUIDINGCENTER\nPlanetsFeelDisk YES\n", True,
+                 (1.0e-5, 0.0, 0.0, 1.05, 0.03, 1.0, 0.0, 0.0, 30.0)),
+    "gc_peb_32x96": ("disk1", 32, 96, 6, 2, "Frame GUIDINGCENTER\n", True,
+                     (3.0e-5, 0.0, 0.0, 1.05, 0.03, 1.0, 0.0, 0.0, 30.0)),
 }
 
 

@@ -18,7 +18,7 @@ CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "
          "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72", "label_24x72",
          "corot_24x72", "corot_peb_32x96", "sm03_24x72",
          "sloppy_peb_32x96", "zhu12irr_24x72", "zhu12irr_peb_32x96", "lp85_24x72", "lp85irr_24x72", "constopa_24x72",
-         "bl94irr_24x72", "disk1_48x144_eps8"]
+         "bl94irr_24x72", "disk1_48x144_eps8", "gc_24x72", "gc_peb_32x96"]
 TOL = 1e-10
 
 
@@ -91,7 +91,8 @@ def test_gpu_vs_reference_golden(name):
 @pytest.mark.parametrize("name", ["disk0_24x72", "disk1_32x96", "disk1_64x192_40", "iso_peb_32x96", "dampinit_24x72",
                                   "gasflux_24x72", "frame_24x72", "open_24x72", "nonrefl_24x72", "srcmass_24x72",
                                   "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72",
-                                  "label_24x72", "corot_24x72", "corot_peb_32x96", "sm03_24x72",
+                                  "label_24x72", "corot_24x72", "corot_peb_32x96", "sm03_24x72", "gc_24x72",
+                                  "gc_peb_32x96", "zhu12irr_peb_32x96", "lp85irr_24x72", "constopa_24x72",
          "sloppy_peb_32x96"])
 def test_gpu_vs_oracle_every_dt(name):
     """GPU and oracle run the same host N-body code, so they share the planet

@@ -79,10 +79,24 @@ def test_bad_options_rejected_before_cuda(lib):
     assert "nsec even" in lib.thorin_gpu_last_error().decode()
 
 
-def test_guiding_centre_frame_refused():
+def test_guiding_centre_frame_is_corotating():
+    """Frame GUIDINGCENTER sets both switches (Interpret.c:165-169), and the
+    orbital elements behind its frame rate invert the planet set-up."""
     text = workloads.inpar_text("disk0", 24, 72) + "\nFrame GUIDINGCENTER\n"
-    with pytest.raises(ValueError, match="GuidingCenter"):
-        P.derive(P.read_inpar(text))
+    p = P.derive(P.read_inpar(text))
+    assert p.corotating == 1 and p.guiding_center == 1
+    m, a, e, inc_deg, f_deg = 1e-5, 1.05, 0.02, 0.5, 30.0
+    st = workloads.planet_from_elements(m, 0.0, 0.0, a, e, inc_deg, 0.0, 0.0, f_deg)
+    a2, e2, inc2, mean = P.orbit_elements(st["mass"], st["x"], st["y"], st["z"], st["vx"], st["vy"], st["vz"])
+    a32, e32 = float(np.float32(a)), float(np.float32(e))     # the planet file is read as C floats
+    assert abs(a2 - a32) < 1e-13 and abs(e2 - e32) < 1e-13
+    assert abs(inc2 - float(np.float32(inc_deg)) * np.pi / 180.0) < 1e-13
+    f = float(np.float32(f_deg)) * np.pi / 180.0               # true -> eccentric -> mean anomaly
+    ea = 2.0 * np.arctan(np.sqrt((1 - e32) / (1 + e32)) * np.tan(f / 2.0))
+    assert abs(mean - (ea - e32 * np.sin(ea))) < 1e-12
+    sys_ = workloads.make_planets(p, [(m, 0.0, 0.0, a, e, inc_deg, 0.0, 0.0, f_deg)])
+    P.corotating_frame(p, sys_)
+    assert abs(p.omega_frame - np.sqrt((1.0 + sys_.mass[0]) / a2 ** 3)) < 1e-15
 
 
 def test_corotating_frame_rate():

@@ -18,7 +18,7 @@ CASES = ["disk0_24x72", "disk1_32x96", "disk0_128x384_200", "disk1_64x192_40", "
          "cooling_24x72", "gasacc_24x72", "paracc_32x96", "drag_24x72", "cbal_24x72", "label_24x72",
          "corot_24x72", "corot_peb_32x96", "sm03_24x72",
          "sloppy_peb_32x96", "zhu12irr_24x72", "zhu12irr_peb_32x96", "lp85_24x72", "lp85irr_24x72", "constopa_24x72",
-         "bl94irr_24x72", "disk1_48x144_eps8"]
+         "bl94irr_24x72", "disk1_48x144_eps8", "gc_24x72", "gc_peb_32x96"]
 
 
 def _run(name, force_planet=True):
@@ -45,7 +45,7 @@ def _run(name, force_planet=True):
 # frame, the planet's position in the later substeps of a multi-substep DT
 # -- the fields differ in the last bit (relative 1e-16 per DT), so these
 # cases are compared within 1e-12 instead of bit for bit.
-NBODY_FRAME = {"corot_24x72", "corot_peb_32x96", "sloppy_peb_32x96"}
+NBODY_FRAME = {"corot_24x72", "corot_peb_32x96", "sloppy_peb_32x96", "gc_24x72", "gc_peb_32x96"}
 
 
 def _same(a, b, err_msg, exact=True):
