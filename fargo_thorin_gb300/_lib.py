@@ -49,6 +49,7 @@ SIGNATURES = {
     "thorin_selftest_slope_division": (C.c_int, [C.c_longlong, C.c_ulonglong, C.c_double,
                                                  C.POINTER(C.c_ulonglong)]),
     "thorin_selftest_graph_conditional": (C.c_int, [C.POINTER(C.c_int)] * 3),
+    "thorin_selftest_graph_nested": (C.c_int, [C.POINTER(C.c_int)] * 2),
     "thorin_selftest_fp64_peak": (C.c_int, [_D]),
     "thorin_gpu_request_torques": (C.c_int, [_P]),
     "thorin_gpu_init_pebbles": (C.c_int, [_P]),

@@ -148,6 +148,98 @@ extern "C" int thorin_selftest_graph_conditional(int *if_zero, int *if_one, int 
   return THORIN_OK;
 }
 
+// Nested conditional nodes, as a whole-DT graph would use them: an outer
+// WHILE node (the substep loop) whose body holds an inner WHILE node (the
+// SOR sweep loop).  Both loops are bounded: the outer body resets the inner
+// counter, sets the inner condition to 1 and counts itself, clearing its own
+// condition at outer_limit; the inner body counts, clearing its condition at
+// inner_limit.  (A handle's default value is assigned once per launch of the
+// whole graph, not at each run of the body that holds it, so a nested loop
+// must be re-armed by a kernel before it.)  c[0] = outer runs, c[1] = inner
+// runs in this outer run, c[2] = inner runs in all.
+__global__ void k_st_outer(int *c, cudaGraphConditionalHandle h, int limit, cudaGraphConditionalHandle hin)
+{
+  if (threadIdx.x == 0) {
+    const int n = ++c[0];
+    c[1] = 0;
+    cudaGraphSetConditional(hin, 1u);
+    cudaGraphSetConditional(h, n < limit ? 1u : 0u);
+  }
+}
+
+__global__ void k_st_inner(int *c, cudaGraphConditionalHandle h, int limit)
+{
+  if (threadIdx.x == 0) {
+    const int n = ++c[1];
+    c[2]++;
+    cudaGraphSetConditional(h, n < limit ? 1u : 0u);
+  }
+}
+
+extern "C" int thorin_selftest_graph_nested(int *outer, int *inner_total)
+{
+  if (!outer || !inner_total) {
+    g_last_error = "selftest_graph_nested: output pointers required";
+    return THORIN_ERR_ARG;
+  }
+  *outer = *inner_total = -1;
+  int *dev = nullptr, host[3] = {0, 0, 0};
+  int olim = 3, ilim = 4;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
+  cudaGraphConditionalHandle ho, hi;
+  cudaGraphNodeParams po = {}, pi = {};
+  cudaKernelNodeParams kp = {};
+  cudaGraphNode_t no, nk, ni, nik;
+  void *ao[] = {&dev, &ho, &olim, &hi};
+  void *ai[] = {&dev, &hi, &ilim};
+  cudaError_t e = cudaMalloc((void **)&dev, 3 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(dev, 0, 3 * sizeof(int));
+  if (e == cudaSuccess) e = cudaGraphCreate(&g, 0);
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&ho, g, 1u, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess) {
+    po.type = cudaGraphNodeTypeConditional;
+    po.conditional.handle = ho;
+    po.conditional.type = cudaGraphCondTypeWhile;
+    po.conditional.size = 1;
+    e = cudaGraphAddNode(&no, g, nullptr, nullptr, 0, &po);
+  }
+  cudaGraph_t body = (e == cudaSuccess) ? po.conditional.phGraph_out[0] : nullptr;
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hi, body, 1u, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess) {
+    kp.func = (void *)k_st_outer;
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(32);
+    kp.kernelParams = ao;
+    e = cudaGraphAddKernelNode(&nk, body, nullptr, 0, &kp);
+  }
+  if (e == cudaSuccess) {
+    pi.type = cudaGraphNodeTypeConditional;
+    pi.conditional.handle = hi;
+    pi.conditional.type = cudaGraphCondTypeWhile;
+    pi.conditional.size = 1;
+    e = cudaGraphAddNode(&ni, body, &nk, nullptr, 1, &pi);
+  }
+  if (e == cudaSuccess) {
+    kp.func = (void *)k_st_inner;
+    kp.kernelParams = ai;
+    e = cudaGraphAddKernelNode(&nik, pi.conditional.phGraph_out[0], nullptr, 0, &kp);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+  if (e == cudaSuccess) e = cudaGraphLaunch(ge, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(host, dev, sizeof(host), cudaMemcpyDeviceToHost);
+  if (ge) cudaGraphExecDestroy(ge);
+  if (g) cudaGraphDestroy(g);
+  if (dev) cudaFree(dev);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("selftest_graph_nested: ") + cudaGetErrorString(e);
+    return THORIN_ERR_CUDA;
+  }
+  *outer = host[0];
+  *inner_total = host[2];
+  return THORIN_OK;
+}
+
 // FP64 fused multiply-add throughput of the current GPU: eight independent
 // FMA chains per thread, one wave of blocks per multiprocessor times eight.
 __global__ void __launch_bounds__(256) k_selftest_dfma(double *__restrict__ out, int iters, double a, double b)

@@ -389,6 +389,11 @@ int thorin_selftest_slope_division(long long n, unsigned long long seed, double 
  * (*while_count = 5; -1 when not run).  No counterpart in the reference. */
 int thorin_selftest_graph_conditional(int *if_zero, int *if_one, int *while_count);
 
+/* Nested conditional graph nodes (a WHILE node inside a WHILE node's body),
+ * bounded: an outer loop of 3 runs, each running an inner loop of 4.  On
+ * success outer = 3 and inner_total = 12.  No counterpart in the reference. */
+int thorin_selftest_graph_nested(int *outer, int *inner_total);
+
 /* FP64 fused multiply-add throughput of the current GPU in GFLOP/s (two
  * flops per FMA), measured with a short kernel of independent FMA chains:
  * the FP64-pipe ceiling for the roofline of the kernels.  No counterpart in

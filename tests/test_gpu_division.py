@@ -44,3 +44,13 @@ def test_graph_conditional_nodes():
     _lib.check(lib.thorin_selftest_graph_conditional(C.byref(a), C.byref(b), C.byref(w)),
                "selftest_graph_conditional")
     assert (a.value, b.value, w.value) == (0, 1, 5)
+
+
+def test_graph_nested_conditional_nodes():
+    """A WHILE node inside a WHILE node's body (the substep loop around the
+    SOR sweep loop of a whole-DT graph), bounded: 3 outer runs of 4 inner."""
+    from fargo_thorin_gb300 import _lib
+    lib = _lib.load()
+    o, i = C.c_int(), C.c_int()
+    _lib.check(lib.thorin_selftest_graph_nested(C.byref(o), C.byref(i)), "selftest_graph_nested")
+    assert (o.value, i.value) == (3, 12)
