@@ -51,6 +51,17 @@ void aux_ring_means(const DevGrid &g, const double *f0, double *o0, const double
   g_thorin_launches++;
 }
 
+__global__ void k_set_ctl(double *__restrict__ ctl, CtlSet v)
+{
+  if (threadIdx.x < (unsigned)v.n) ctl[v.idx[threadIdx.x]] = v.val[threadIdx.x];
+}
+
+void aux_set_ctl(double *ctl, const CtlSet &v, cudaStream_t s)
+{
+  k_set_ctl<<<1, 32, 0, s>>>(ctl, v);
+  g_thorin_launches++;
+}
+
 void aux_ring_mean(const DevGrid &g, const double *f, double *out, cudaStream_t s)
 {
   aux_ring_means(g, f, out, nullptr, nullptr, 0, g.nr, s);
@@ -175,6 +186,9 @@ __global__ void __launch_bounds__(256) k_cfl_cells(DevGrid g, const double *__re
 __global__ void __launch_bounds__(1024) k_cfl_final(DevGrid g, const double *__restrict__ part, CflRings cr, CflFinal f,
                             double *__restrict__ scal, int *__restrict__ iscal)
 {
+  // the remaining part of the DT and MinStepForRebound's rate come from the
+  // disk's control block; so does the CFL's substep length, written back
+  const double deltaT = g.ctl[CTL_DELTAT], invdtreb_sq = g.ctl[CTL_INVDTREB];
   double mg = 0.0, mp = -1.0e30, shear = 1e30;
   for (int b = threadIdx.x; b < f.nb; b += blockDim.x) {
     const double a = part[2 * b], c = part[2 * b + 1];
@@ -190,8 +204,8 @@ __global__ void __launch_bounds__(1024) k_cfl_final(DevGrid g, const double *__r
   shear = block_reduce(shear, OpMin(), 1e30);
   if (threadIdx.x == 0) {
     double newdt;
-    if (!f.pebbles) newdt = TH_CFLSECURITY / sqrt(mg + f.invdtreb_sq);
-    else newdt = TH_CFLSECURITY / sqrt(mg + mp + f.invdtreb_sq);
+    if (!f.pebbles) newdt = TH_CFLSECURITY / sqrt(mg + invdtreb_sq);
+    else newdt = TH_CFLSECURITY / sqrt(mg + mp + invdtreb_sq);
     if (newdt > 1e30) newdt = 1e30;
     if (shear < newdt) newdt = shear;
     const double dts = scal[SC_DTSTELLAR];
@@ -201,10 +215,12 @@ __global__ void __launch_bounds__(1024) k_cfl_final(DevGrid g, const double *__r
     }
     newdt = (newdt < f.maximum_step) ? newdt : f.maximum_step;
     if (f.first_call && f.first_step > 0.0) newdt = f.first_step;
-    if (f.deltaT < newdt) newdt = f.deltaT;
+    if (deltaT < newdt) newdt = deltaT;
     scal[SC_NEWDT] = newdt;
     scal[SC_INVDTPEB] = mp;
-    iscal[IS_NSUB] = (int)(ceil(f.deltaT / newdt));
+    const int n = (int)(ceil(deltaT / newdt));
+    iscal[IS_NSUB] = n;
+    g.ctl[CTL_DT] = deltaT / (double)n;
   }
 }
 
@@ -225,8 +241,9 @@ void aux_cfl(const DevGrid &g, const double *vr, const double *vt, const double 
 
 // ---------------------------------------------------------------------------
 // EvaporatePebbles (Pebbles.c:834-864).
-__global__ void k_evaporate(DevGrid g, const double *__restrict__ T, double *__restrict__ pdens, double facc)
+__global__ void k_evaporate(DevGrid g, const double *__restrict__ T, double *__restrict__ pdens)
 {
+  const double facc = g.ctl[CTL_FACC_EVAP];
   const int ns = g.ns;
   CELL_LOOP_2D
   if (T[l] > g.k.evaptemp) {
@@ -236,9 +253,9 @@ __global__ void k_evaporate(DevGrid g, const double *__restrict__ T, double *__r
   }
 }
 
-void aux_evaporate(const DevGrid &g, const double *T, double *pdens, double facc, cudaStream_t s)
+void aux_evaporate(const DevGrid &g, const double *T, double *pdens, cudaStream_t s)
 {
-  k_evaporate<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, T, pdens, facc);
+  k_evaporate<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, T, pdens);
   g_thorin_launches++;
 }
 
@@ -246,9 +263,9 @@ void aux_evaporate(const DevGrid &g, const double *T, double *pdens, double facc
 // Damping boundaries (DampingBoundary, SideEuler.c:368-419, and DampPebbles,
 // SideEuler.c:423-456).  Only rings inside the damping zones are launched.
 __global__ void k_damp_gas(DevGrid g, double *__restrict__ vrad, double *__restrict__ rho, double *__restrict__ vtheta,
-                           double *__restrict__ energy, const int *__restrict__ rings, const double *__restrict__ vr0r,
-                           double dt, double omega_frame, int damp_init, int damp_flux, int energy_eq)
+                           double *__restrict__ energy, const int *__restrict__ rings, const double *__restrict__ vr0r, int damp_init, int damp_flux, int energy_eq)
 {
+  const double dt = g.ctl[CTL_DT], omega_frame = g.ctl[CTL_OMEGA_FRAME];
   const int ns = g.ns;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= ns) return;
@@ -268,11 +285,11 @@ __global__ void k_damp_gas(DevGrid g, double *__restrict__ vrad, double *__restr
 }
 
 void aux_damp_gas(const DevGrid &g, double *vrad, double *rho, double *vtheta, double *energy, const int *rings,
-                  int nrings, const double *vr0r, double dt, double omega_frame, int damp_init, int damp_flux,
+                  int nrings, const double *vr0r, int damp_init, int damp_flux,
                   int energy_eq, cudaStream_t s)
 {
   if (nrings <= 0) return;
-  k_damp_gas<<<grid2d(g.ns, nrings, BX), BX, 0, s>>>(g, vrad, rho, vtheta, energy, rings, vr0r, dt, omega_frame,
+  k_damp_gas<<<grid2d(g.ns, nrings, BX), BX, 0, s>>>(g, vrad, rho, vtheta, energy, rings, vr0r,
                                                      damp_init, damp_flux, energy_eq);
   g_thorin_launches++;
 }
@@ -302,8 +319,9 @@ void aux_iso_eos(const DevGrid &g, const double *rho, const double *csr, double 
 }
 
 __global__ void k_damp_peb(DevGrid g, double *__restrict__ pd, double *__restrict__ pvr, double *__restrict__ pvt,
-                           const int *__restrict__ rings, double dt, double omega_frame)
+                           const int *__restrict__ rings)
 {
+  const double dt = g.ctl[CTL_DT], omega_frame = g.ctl[CTL_OMEGA_FRAME];
   const int ns = g.ns;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= ns) return;
@@ -317,11 +335,10 @@ __global__ void k_damp_peb(DevGrid g, double *__restrict__ pd, double *__restric
   pvt[l] = div_fast(pvt[l] + lambda * vt0, 1.0 + lambda);
 }
 
-void aux_damp_peb(const DevGrid &g, double *pd, double *pvr, double *pvt, const int *rings, int nrings, double dt,
-                  double omega_frame, cudaStream_t s)
+void aux_damp_peb(const DevGrid &g, double *pd, double *pvr, double *pvt, const int *rings, int nrings, cudaStream_t s)
 {
   if (nrings <= 0) return;
-  k_damp_peb<<<grid2d(g.ns, nrings, BX), BX, 0, s>>>(g, pd, pvr, pvt, rings, dt, omega_frame);
+  k_damp_peb<<<grid2d(g.ns, nrings, BX), BX, 0, s>>>(g, pd, pvr, pvt, rings);
   g_thorin_launches++;
 }
 
@@ -350,8 +367,9 @@ __global__ void k_pebble_sources(DevGrid g, const double *__restrict__ pd, const
                                  const double *__restrict__ vr, const double *__restrict__ vt,
                                  const double *__restrict__ pagr, const double *__restrict__ pagt,
                                  double *__restrict__ paccr, double *__restrict__ pacct, double *__restrict__ dragr,
-                                 double *__restrict__ dragt, double omega_frame, int back_reaction)
+                                 double *__restrict__ dragt, int back_reaction)
 {
+  const double omega_frame = g.ctl[CTL_OMEGA_FRAME];
   const int ns = g.ns;
   CELL_LOOP_2D
   const double Omega = g.r.Omega[i];
@@ -378,11 +396,11 @@ __global__ void k_pebble_sources(DevGrid g, const double *__restrict__ pd, const
 
 void aux_pebble_sources(const DevGrid &g, const double *pd, const double *pvr, const double *pvt, const double *tau,
                         const double *vr, const double *vt, const double *pagr, const double *pagt, double *paccr,
-                        double *pacct, double *dragr, double *dragt, double omega_frame, int back_reaction,
+                        double *pacct, double *dragr, double *dragt, int back_reaction,
                         cudaStream_t s)
 {
   k_pebble_sources<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, pd, pvr, pvt, tau, vr, vt, pagr, pagt, paccr, pacct, dragr,
-                                                         dragt, omega_frame, back_reaction);
+                                                         dragt, back_reaction);
   g_thorin_launches++;
 }
 
@@ -393,9 +411,10 @@ __global__ void k_pebble_substep1(DevGrid g, double *__restrict__ pvr, double *_
                                   const double *__restrict__ vt, const double *__restrict__ paccr,
                                   const double *__restrict__ pacct, const double *__restrict__ gaccr,
                                   const double *__restrict__ gacct, const double *__restrict__ rho,
-                                  const double *__restrict__ pd, double dt, int diffusion, double schmidt,
+                                  const double *__restrict__ pd, int diffusion, double schmidt,
                                   const double *__restrict__ invdxtheta_r)
 {
+  const double dt = g.ctl[CTL_DT];
   const int ns = g.ns;
   CELL_LOOP_2D
   const double Omega = g.r.Omega[i];
@@ -425,11 +444,10 @@ __global__ void k_pebble_substep1(DevGrid g, double *__restrict__ pvr, double *_
 
 void aux_pebble_substep1(const DevGrid &g, double *pvr, double *pvt, const double *tau, const double *vr, const double *vt,
                          const double *paccr, const double *pacct, const double *gaccr, const double *gacct,
-                         const double *rho, const double *pd, double dt, int diffusion, double schmidt,
+                         const double *rho, const double *pd, int diffusion, double schmidt,
                          const double *invdxtheta_r, cudaStream_t s)
 {
-  k_pebble_substep1<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, pvr, pvt, tau, vr, vt, paccr, pacct, gaccr, gacct, rho, pd,
-                                                          dt, diffusion, schmidt, invdxtheta_r);
+  k_pebble_substep1<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, pvr, pvt, tau, vr, vt, paccr, pacct, gaccr, gacct, rho, pd, diffusion, schmidt, invdxtheta_r);
   g_thorin_launches++;
 }
 
@@ -529,6 +547,8 @@ __device__ __forceinline__ void vert_quad(const double (&wq)[NV], double H, doub
 
 __global__ void __launch_bounds__(128) k_forces(DevGrid g, ForceArgs a, ForceRings fr)
 {
+  const double mass_taper = g.ctl[CTL_MASS_TAPER];
+  const int full_mass = (mass_taper == 1.0) ? 1 : 0;
   const int ns = g.ns;
   const int i = blockIdx.y;
   const int npl = a.npl, peb = a.pebbles;
@@ -563,7 +583,7 @@ __global__ void __launch_bounds__(128) k_forces(DevGrid g, ForceArgs a, ForceRin
       hillcut[k] = 1.0;
       integpl[k] = 0.0;
       p_integpl[k] = 0.0;
-      if (a.full_mass && (s2[k] < P.near_h2 || s2[k] < P.near_hill2)) {
+      if (full_mass && (s2[k] < P.near_h2 || s2[k] < P.near_hill2)) {
         local = 1;
         with[k] = 1;
         if (a.exclude_hill) {
@@ -621,7 +641,7 @@ __global__ void __launch_bounds__(128) k_forces(DevGrid g, ForceArgs a, ForceRin
           if (a.pebble_gravity) { if (a.exclude_hill) tmp *= hillcut[k]; acc[3 + 2 * k] += pmcell * tmp; }
         }
       } else {
-        mpl *= a.mass_taper;
+        mpl *= mass_taper;
         double d2 = s2[k] + P.z * P.z + P.smoothing2, iv = rsqrt(d2), id3 = iv * iv * iv;
         tmp = (x - P.x) * id3;
         ax += -mpl * tmp;
@@ -677,9 +697,9 @@ __global__ void __launch_bounds__(1024) k_forces_final(const double *__restrict_
 
 // Indirect term added to every cell (Pframeforce.c:488-509).
 __global__ void k_forces_indirect(DevGrid g, double *__restrict__ agr, double *__restrict__ agt,
-                                  double *__restrict__ pagr, double *__restrict__ pagt, const double *__restrict__ scal,
-                                  double indx_pl, double indy_pl, int pebbles)
+                                  double *__restrict__ pagr, double *__restrict__ pagt, const double *__restrict__ scal, int pebbles)
 {
+  const double indx_pl = g.ctl[CTL_INDX_PL], indy_pl = g.ctl[CTL_INDY_PL];
   const int ns = g.ns;
   CELL_LOOP_2D
   const double axi = scal[SC_INDX] + indx_pl, ayi = scal[SC_INDY] + indy_pl;
@@ -691,7 +711,7 @@ __global__ void k_forces_indirect(DevGrid g, double *__restrict__ agr, double *_
   if (pebbles) { pagr[l] += ar; pagt[l] += at; }
 }
 
-void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr, double indx_pl, double indy_pl,
+void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr,
                 double *scal, cudaStream_t s)
 {
   if (a0.pebbles) aux_ring_means(g, a0.tau, fr.tau_avr, nullptr, nullptr, 0, g.nr, s);
@@ -715,7 +735,7 @@ void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr, dou
   g_thorin_launches++;
   k_forces_final<<<1, 1024, 0, s>>>(a0.part, grid.x * grid.y, 2 + 2 * a0.npl, scal);
   g_thorin_launches++;
-  k_forces_indirect<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, a0.agr, a0.agt, a0.pagr, a0.pagt, scal, indx_pl, indy_pl,
+  k_forces_indirect<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, a0.agr, a0.agt, a0.pagr, a0.pagt, scal,
                                                           a0.pebbles);
   g_thorin_launches++;
 }
@@ -760,8 +780,10 @@ __device__ double column_mass(double a, double b, double Hpeb)
 // acc[] scalars: 0 Reff, 1 vrel, 2 Mt, 3 limiter.
 #define ACC_BX 256
 
-__global__ void __launch_bounds__(ACC_BX) k_acc_tau(DevGrid g, AccArgs a)
+__global__ void __launch_bounds__(ACC_BX) k_acc_tau(DevGrid g, const AccArgs *__restrict__ ap)
 {
+  const AccArgs &a = *ap;
+  if ((int)blockIdx.x >= a.nb) return;           // grid sized for the widest annulus
   const int ncells = (a.imax - a.imin + 1) * g.ns;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   double t = (q < ncells) ? a.tau[(size_t)a.imin * g.ns + q] : 0.0;
@@ -769,8 +791,10 @@ __global__ void __launch_bounds__(ACC_BX) k_acc_tau(DevGrid g, AccArgs a)
   if (threadIdx.x == 0) a.part[blockIdx.x] = t;
 }
 
-__global__ void __launch_bounds__(ACC_BX) k_acc_reff(DevGrid g, AccArgs a, int nb)
+__global__ void __launch_bounds__(ACC_BX) k_acc_reff(DevGrid g, const AccArgs *__restrict__ ap)
 {
+  const AccArgs &a = *ap;
+  const int nb = a.nb;
   const int ns = g.ns;
   __shared__ double sh[2];
   if (threadIdx.x == 0) {                    // vt1D at the two rings bracketing the planet
@@ -801,8 +825,10 @@ __global__ void __launch_bounds__(ACC_BX) k_acc_reff(DevGrid g, AccArgs a, int n
   }
 }
 
-__global__ void __launch_bounds__(ACC_BX) k_acc_upper(DevGrid g, AccArgs a)
+__global__ void __launch_bounds__(ACC_BX) k_acc_upper(DevGrid g, const AccArgs *__restrict__ ap)
 {
+  const AccArgs &a = *ap;
+  if ((int)blockIdx.x >= a.nb) return;           // grid sized for the widest annulus
   const int ns = g.ns;
   const int ncells = (a.imax - a.imin + 1) * ns;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -834,8 +860,10 @@ __global__ void __launch_bounds__(ACC_BX) k_acc_upper(DevGrid g, AccArgs a)
   }
 }
 
-__global__ void __launch_bounds__(ACC_BX) k_acc_limiter(AccArgs a, int nb, double pi, double sqrt2pi_inv)
+__global__ void __launch_bounds__(ACC_BX) k_acc_limiter(const AccArgs *__restrict__ ap, double pi, double sqrt2pi_inv)
 {
+  const AccArgs &a = *ap;
+  const int nb = a.nb;
   double v[4] = {0.0, 0.0, 0.0, 0.0};
   for (int b = threadIdx.x; b < nb; b += blockDim.x)
     for (int k = 0; k < 4; k++) v[k] += a.part[4 * b + k];
@@ -855,8 +883,10 @@ __global__ void __launch_bounds__(ACC_BX) k_acc_limiter(AccArgs a, int nb, doubl
   }
 }
 
-__global__ void __launch_bounds__(ACC_BX) k_acc_apply(DevGrid g, AccArgs a)
+__global__ void __launch_bounds__(ACC_BX) k_acc_apply(DevGrid g, const AccArgs *__restrict__ ap)
 {
+  const AccArgs &a = *ap;
+  if ((int)blockIdx.x >= a.nb) return;           // grid sized for the widest annulus
   const int ns = g.ns;
   const int ncells = (a.imax - a.imin + 1) * ns;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -886,8 +916,10 @@ __global__ void __launch_bounds__(ACC_BX) k_acc_apply(DevGrid g, AccArgs a)
   }
 }
 
-__global__ void __launch_bounds__(ACC_BX) k_acc_sum(AccArgs a, int nb, double *__restrict__ scal)
+__global__ void __launch_bounds__(ACC_BX) k_acc_sum(const AccArgs *__restrict__ ap, double *__restrict__ scal)
 {
+  const AccArgs &a = *ap;
+  const int nb = a.nb;
   double v[3] = {0.0, 0.0, 0.0};
   for (int b = threadIdx.x; b < nb; b += blockDim.x)
     for (int k = 0; k < 3; k++) v[k] += a.part[3 * b + k];
@@ -901,21 +933,34 @@ int aux_accrete_blocks(const DevGrid &g, int imin, int imax)
   return (ncells + ACC_BX - 1) / ACC_BX;
 }
 
-void aux_accrete(const DevGrid &g, const AccArgs &a, double *scal, cudaStream_t s)
+__global__ void k_set_accargs(AccArgs a, AccArgs *__restrict__ dst)
 {
-  const int nb = aux_accrete_blocks(g, a.imin, a.imax);
+  if (threadIdx.x == 0) *dst = a;
+}
+
+void aux_accrete(const DevGrid &g, const AccArgs &a0, AccArgs *a_dev, double *scal, cudaStream_t s)
+{
+  AccArgs a = a0;
+  a.nb = aux_accrete_blocks(g, a.imin, a.imax);
+  k_set_accargs<<<1, 32, 0, s>>>(a, a_dev);
+  g_thorin_launches++;
   aux_ring_means(g, a.vt, a.acc + 4, nullptr, nullptr, a.iflow, (a.iflow + 1 < g.nr) ? 2 : 1, s);
-  k_acc_tau<<<nb, ACC_BX, 0, s>>>(g, a);
+  aux_accrete_kernels(g, a_dev, a.nb, scal, s);
+}
+
+void aux_accrete_kernels(const DevGrid &g, const AccArgs *a_dev, int nb_grid, double *scal, cudaStream_t s)
+{
+  k_acc_tau<<<nb_grid, ACC_BX, 0, s>>>(g, a_dev);
   g_thorin_launches++;
-  k_acc_reff<<<1, ACC_BX, 0, s>>>(g, a, nb);
+  k_acc_reff<<<1, ACC_BX, 0, s>>>(g, a_dev);
   g_thorin_launches++;
-  k_acc_upper<<<nb, ACC_BX, 0, s>>>(g, a);
+  k_acc_upper<<<nb_grid, ACC_BX, 0, s>>>(g, a_dev);
   g_thorin_launches++;
-  k_acc_limiter<<<1, ACC_BX, 0, s>>>(a, nb, TH_PI, g.k.sqrt2pi_inv);
+  k_acc_limiter<<<1, ACC_BX, 0, s>>>(a_dev, TH_PI, g.k.sqrt2pi_inv);
   g_thorin_launches++;
-  k_acc_apply<<<nb, ACC_BX, 0, s>>>(g, a);
+  k_acc_apply<<<nb_grid, ACC_BX, 0, s>>>(g, a_dev);
   g_thorin_launches++;
-  k_acc_sum<<<1, ACC_BX, 0, s>>>(a, nb, scal);
+  k_acc_sum<<<1, ACC_BX, 0, s>>>(a_dev, scal);
   g_thorin_launches++;
 }
 
@@ -1155,8 +1200,9 @@ void aux_outer_source_mass(const DevGrid &g, double *rho, double *vr, double pen
 __global__ void k_parametric_cooling(DevGrid g, const double *__restrict__ rho, const double *__restrict__ eint,
                                      const double *__restrict__ qplus, const double *__restrict__ divv,
                                      const double *__restrict__ coolt, const double *__restrict__ qplusmed,
-                                     double *__restrict__ enew, double dt, double gm1)
+                                     double *__restrict__ enew, double gm1)
 {
+  const double dt = g.ctl[CTL_DT];
   const int ns = g.ns;
   CELL_LOOP_2D
   const double tc = coolt[i], sm = g.r.SigmaMed[i];
@@ -1167,10 +1213,10 @@ __global__ void k_parametric_cooling(DevGrid g, const double *__restrict__ rho, 
 }
 
 void aux_parametric_cooling(const DevGrid &g, const double *rho, const double *eint, const double *qplus,
-                            const double *divv, const double *coolt, const double *qplusmed, double *enew, double dt,
+                            const double *divv, const double *coolt, const double *qplusmed, double *enew,
                             double gm1, cudaStream_t s)
 {
-  k_parametric_cooling<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, eint, qplus, divv, coolt, qplusmed, enew, dt, gm1);
+  k_parametric_cooling<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, eint, qplus, divv, coolt, qplusmed, enew, gm1);
   g_thorin_launches++;
 }
 

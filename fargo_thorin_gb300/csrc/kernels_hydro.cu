@@ -28,10 +28,10 @@ __global__ void k_substep1(DevGrid g, const double *__restrict__ rho, const doub
                            const double *__restrict__ agr, const double *__restrict__ agt,
                            const double *__restrict__ dragr, const double *__restrict__ dragt,
                            double *__restrict__ vradint, double *__restrict__ vthetaint,
-                           double *__restrict__ gaccr, double *__restrict__ gacct,
-                           double dt, double omega_frame, double gm1, int pebbles, int back_reaction,
+                           double *__restrict__ gaccr, double *__restrict__ gacct, double gm1, int pebbles, int back_reaction,
                            const double *__restrict__ supp_torque, const double *__restrict__ invdxtheta_r)
 {
+  const double dt = g.ctl[CTL_DT], omega_frame = g.ctl[CTL_OMEGA_FRAME];
   const int ns = g.ns;
   CELL_LOOP_2D
   const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
@@ -126,9 +126,10 @@ __global__ void k_stress(DevGrid g, const double *__restrict__ vr, const double 
 // ImposeKeplerianEdges (Viscosity.c:221-260).
 __global__ void k_visc_update(DevGrid g, double *__restrict__ vr, double *__restrict__ vt,
                               const double *__restrict__ rho, const double *__restrict__ trr,
-                              const double *__restrict__ tpp, const double *__restrict__ trp, double dt,
+                              const double *__restrict__ tpp, const double *__restrict__ trp,
                               double invdphi, int kepler_edges, double vkep_in, double vkep_out)
 {
+  const double dt = g.ctl[CTL_DT];
   const int ns = g.ns, nr = g.nr;
   CELL_LOOP_2D
   const int ljp = (j == ns - 1) ? i * ns : l + 1;
@@ -163,9 +164,9 @@ __device__ __forceinline__ double avisc(double dv, double rho)
 
 __global__ void k_substep2(DevGrid g, const double *__restrict__ rho, const double *__restrict__ vr,
                            const double *__restrict__ vt, const double *__restrict__ energy,
-                           double *__restrict__ vrnew, double *__restrict__ vtnew, double *__restrict__ eint,
-                           double dt, int energy_eq, const double *__restrict__ invdxtheta_r)
+                           double *__restrict__ vrnew, double *__restrict__ vtnew, double *__restrict__ eint, int energy_eq, const double *__restrict__ invdxtheta_r)
 {
+  const double dt = g.ctl[CTL_DT];
   const int ns = g.ns, nr = g.nr;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y;
@@ -591,11 +592,11 @@ __global__ void k_matrix(DevGrid g, const double *__restrict__ rho, const double
                          const double *__restrict__ cs, const double *__restrict__ dcen, const double *__restrict__ divv,
                          const double *__restrict__ qminus, const double *__restrict__ qplus, const double *__restrict__ qirr,
                          double *__restrict__ ml, double *__restrict__ mlip, double *__restrict__ mlim,
-                         double *__restrict__ mljp, double *__restrict__ mljm, double *__restrict__ rhs,
-                         double dt, double gm1, const double *__restrict__ invdxtheta2_r,
+                         double *__restrict__ mljp, double *__restrict__ mljm, double *__restrict__ rhs, double gm1, const double *__restrict__ invdxtheta2_r,
                          int irradiation, int nheat, const int *__restrict__ heat_idx,
                          const double *__restrict__ heat_val)
 {
+  const double dt = g.ctl[CTL_DT];
   const int ns = g.ns;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y + 1;                   // rings 1 .. nr-2
@@ -704,8 +705,9 @@ __global__ void __launch_bounds__(SOR_BX) k_sor_resid0(DevGrid g, const double *
                                                     const double *__restrict__ ml, const double *__restrict__ mlip,
                                                     const double *__restrict__ mlim, const double *__restrict__ mljp,
                                                     const double *__restrict__ mljm, const double *__restrict__ rhs,
-                                                    double *__restrict__ cw, double omega, SorCtl c)
+                                                    double *__restrict__ cw, SorCtl c)
 {
+  const double omega = g.ctl[CTL_SOR_OMEGA];
   const int ns = g.ns, half = ns >> 1;
   const int i = blockIdx.y + 1;
   double a = 0.0, aj = 0.0;
@@ -905,8 +907,9 @@ __global__ void k_energy_from_t(DevGrid g, const double *__restrict__ rho, doubl
 __global__ void k_rad_prep(DevGrid g, int nq, const double *__restrict__ rho, const double *__restrict__ vr,
                            const double *__restrict__ vt, const double *__restrict__ energy, double *rmp, double *rmm,
                            double *tmp_, double *tmm, double *w0, double *w1, double *w2, double *w3, double *we,
-                           double *wr, double omega_frame, const double *__restrict__ label, double *ext, double *wx)
+                           double *wr, const double *__restrict__ label, double *ext, double *wx)
 {
+  const double omega_frame = g.ctl[CTL_OMEGA_FRAME];
   const int ns = g.ns;
   CELL_LOOP_2D
   const int ljp = (j == ns - 1) ? i * ns : l + 1;
@@ -979,8 +982,9 @@ __global__ void k_rad_slope(DevGrid g, PtrPack8 pk)
 
 // ComputeStarRad (TransportEuler.c:232-273): upwind face values at the inner
 // face of ring i (faces 0 and nr are zero).
-__global__ void k_rad_face(DevGrid g, PtrPack8 w, PtrPack8 dq, const double *__restrict__ vr, double dt)
+__global__ void k_rad_face(DevGrid g, PtrPack8 w, PtrPack8 dq, const double *__restrict__ vr)
 {
+  const double dt = g.ctl[CTL_DT];
   const int ns = g.ns, nr = g.nr;
   CELL_LOOP_2D
   if (i == 0 || i == nr) {
@@ -1000,8 +1004,9 @@ __global__ void k_rad_face(DevGrid g, PtrPack8 w, PtrPack8 dq, const double *__r
 
 // VanLeerRadial update (TransportEuler.c:384-415).
 __global__ void k_rad_update(DevGrid g, PtrPack8 qf, const double *__restrict__ rhos, const double *__restrict__ vr,
-                             PtrPack8 io, double dt)
+                             PtrPack8 io)
 {
+  const double dt = g.ctl[CTL_DT];
   const int ns = g.ns;
   CELL_LOOP_2D
   const int lip = l + ns;
@@ -1024,10 +1029,11 @@ __global__ void k_rad_update(DevGrid g, PtrPack8 qf, const double *__restrict__ 
 // Ntilde + 1/2 lies within 1e-9 of an integer, the ring is summed again left
 // to right, the reference's order, so that the integer shift is exactly the
 // reference's.
-__global__ void __launch_bounds__(256) k_azi_rings(DevGrid g, const double *__restrict__ vt, double dt,
+__global__ void __launch_bounds__(256) k_azi_rings(DevGrid g, const double *__restrict__ vt,
                                                    int *__restrict__ nshift, double *__restrict__ vmed,
                                                    double *__restrict__ vtemp)
 {
+  const double dt = g.ctl[CTL_DT];
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (i >= g.nr) return;                           // whole warp
   const int ns = g.ns;
@@ -1081,10 +1087,11 @@ __device__ __forceinline__ double azi_vl_slope_d(double dqm, double dqp)
 }
 
 template <int NQ>
-__global__ void __launch_bounds__(AZ_TMAX) k_azimuthal(DevGrid g, AziIO io, const double *__restrict__ vt, double dt,
+__global__ void __launch_bounds__(AZ_TMAX) k_azimuthal(DevGrid g, AziIO io, const double *__restrict__ vt,
                                                      int fast, const int *__restrict__ nshift,
                                                      const double *__restrict__ vmed, const double *__restrict__ vtemp)
 {
+  const double dt = g.ctl[CTL_DT];
   __shared__ double s_a[AZ_TMAX], s_b[AZ_TMAX], s_c[AZ_TMAX];
   const int ns = g.ns, i = blockIdx.y, t = threadIdx.x, T = blockDim.x;
   const int seg = T - 2 * AZ_HALO;
@@ -1184,11 +1191,11 @@ static int azi_block(int ns)
 // ComputeSoundSpeed).
 __global__ void k_velocities(DevGrid g, const double *__restrict__ rho, const double *__restrict__ rmp,
                              const double *__restrict__ rmm, const double *__restrict__ tmp_,
-                             const double *__restrict__ tmm, double *__restrict__ vr, double *__restrict__ vt,
-                             double omega_frame, int damp_vrad, double dt, double drin, double drout,
+                             const double *__restrict__ tmm, double *__restrict__ vr, double *__restrict__ vt, int damp_vrad, double drin, double drout,
                              const double *__restrict__ energy, double *__restrict__ temper, double *__restrict__ cs,
                              double gm1, double gg1)
 {
+  const double dt = g.ctl[CTL_DT], omega_frame = g.ctl[CTL_OMEGA_FRAME];
   const int ns = g.ns;
   CELL_LOOP_2D
   const int ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
@@ -1215,11 +1222,11 @@ __global__ void k_velocities(DevGrid g, const double *__restrict__ rho, const do
 void hydro_substep1(const DevGrid &g, const double *rho, const double *vrad, const double *vtheta,
                     const double *energy, const double *press, const double *agr, const double *agt,
                     const double *dragr, const double *dragt, double *vradint, double *vthetaint, double *gaccr,
-                    double *gacct, double dt, double omega_frame, double gm1, int pebbles, int back_reaction,
+                    double *gacct, double gm1, int pebbles, int back_reaction,
                     const double *supp_torque, const double *invdxtheta_r, cudaStream_t s)
 {
   k_substep1<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, rho, vrad, vtheta, energy, press, agr, agt, dragr, dragt, vradint,
-                                                   vthetaint, gaccr, gacct, dt, omega_frame, gm1, pebbles,
+                                                   vthetaint, gaccr, gacct, gm1, pebbles,
                                                    back_reaction, supp_torque, invdxtheta_r);
   g_thorin_launches++;
 }
@@ -1232,18 +1239,18 @@ void hydro_stress(const DevGrid &g, const double *vr, const double *vt, const do
 }
 
 void hydro_visc_update(const DevGrid &g, double *vr, double *vt, const double *rho, const double *trr, const double *tpp,
-                       const double *trp, double dt, double invdphi, int kepler, double vkin, double vkout,
+                       const double *trp, double invdphi, int kepler, double vkin, double vkout,
                        cudaStream_t s)
 {
-  k_visc_update<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, vr, vt, rho, trr, tpp, trp, dt, invdphi, kepler, vkin, vkout);
+  k_visc_update<<<grid2d(g.ns, g.nr, BX), BX, 0, s>>>(g, vr, vt, rho, trr, tpp, trp, invdphi, kepler, vkin, vkout);
   g_thorin_launches++;
 }
 
 void hydro_substep2(const DevGrid &g, const double *rho, const double *vr, const double *vt, const double *energy,
-                    double *vrnew, double *vtnew, double *eint, double dt, int energy_eq, const double *invdxtheta_r,
+                    double *vrnew, double *vtnew, double *eint, int energy_eq, const double *invdxtheta_r,
                     cudaStream_t s)
 {
-  k_substep2<<<grid2d(g.ns, g.nr + 1, BX), BX, 0, s>>>(g, rho, vr, vt, energy, vrnew, vtnew, eint, dt, energy_eq,
+  k_substep2<<<grid2d(g.ns, g.nr + 1, BX), BX, 0, s>>>(g, rho, vr, vt, energy, vrnew, vtnew, eint, energy_eq,
                                                        invdxtheta_r);
   g_thorin_launches++;
 }
@@ -1287,13 +1294,13 @@ void hydro_irradiation(const DevGrid &g, const double *rho, const double *cs, co
 
 void hydro_matrix(const DevGrid &g, const double *rho, const double *T, const double *cs, const double *dcen,
                   const double *divv, const double *qminus, const double *qplus, const double *qirr, double *ml,
-                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs, double dt,
+                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs,
                   double gm1, const double *invdxtheta2_r, int irradiation, int nheat, const int *heat_idx,
                   const double *heat_val, cudaStream_t s)
 {
   if (g.nr < 3) return;
   k_matrix<<<grid2d(g.ns, g.nr - 2, BX), BX, 0, s>>>(g, rho, T, cs, dcen, divv, qminus, qplus, qirr, ml, mlip, mlim, mljp,
-                                                     mljm, rhs, dt, gm1, invdxtheta2_r, irradiation, nheat, heat_idx,
+                                                     mljm, rhs, gm1, invdxtheta2_r, irradiation, nheat, heat_idx,
                                                      heat_val);
   g_thorin_launches++;
 }
@@ -1339,10 +1346,10 @@ int sor_blocks(const DevGrid &g)
 }
 
 void hydro_sor_resid0(const DevGrid &g, const double *T, const double *ml, const double *mlip, const double *mlim,
-                      const double *mljp, const double *mljm, const double *rhs, double *cw, double omega,
+                      const double *mljp, const double *mljm, const double *rhs, double *cw,
                       const SorCtl &c, cudaStream_t s)
 {
-  k_sor_resid0<<<sor_grid_resid(g), SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, cw, omega, c);
+  k_sor_resid0<<<sor_grid_resid(g), SOR_BX, 0, s>>>(g, T, ml, mlip, mlim, mljp, mljm, rhs, cw, c);
   g_thorin_launches++;
 }
 
@@ -1368,7 +1375,7 @@ void hydro_energy_from_t(const DevGrid &g, const double *rho, double *T, double 
 // are swapped with the updated buffers and vr/vt hold the new velocities.
 
 void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, double **energy, double *label,
-                     const TransportScratch &S, double dt, double omega_frame, int fast, int damp_vrad, double drin,
+                     const TransportScratch &S, int fast, int damp_vrad, double drin,
                      double drout, double *temper, double *cs, double gm1, double gg1, cudaStream_t s)
 {
   const int ns = g.ns, nr = g.nr;
@@ -1381,8 +1388,7 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
   if (label) qi[nq++] = 6;
   qi[nq++] = 5;
   k_rad_prep<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, nq, *rho, vr, vt, energy ? *energy : nullptr, S.mom[0], S.mom[1],
-                                               S.mom[2], S.mom[3], S.w[0], S.w[1], S.w[2], S.w[3], S.w[4], S.w[5],
-                                               omega_frame, label, S.ext, S.w[6]);
+                                               S.mom[2], S.mom[3], S.w[0], S.w[1], S.w[2], S.w[3], S.w[4], S.w[5], label, S.ext, S.w[6]);
   g_thorin_launches++;
   // slopes of the quotients and of rho (slot 7)
   PtrPack8 sl;
@@ -1403,7 +1409,7 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
   }
   wf.src[n] = *rho; wf.dst[n] = S.f[7]; dqf.src[n] = S.d[7]; n++;
   wf.n = dqf.n = n;
-  k_rad_face<<<grid2d(ns, nr + 1, BX), BX, 0, s>>>(g, wf, dqf, vr, dt);
+  k_rad_face<<<grid2d(ns, nr + 1, BX), BX, 0, s>>>(g, wf, dqf, vr);
   g_thorin_launches++;
   // flux divergence into the quotient buffers, which are free by now
   PtrPack8 qf, io;
@@ -1416,11 +1422,11 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
     n++;
   }
   qf.n = io.n = n;
-  k_rad_update<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, qf, S.f[7], vr, io, dt);
+  k_rad_update<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, qf, S.f[7], vr, io);
   g_thorin_launches++;
   // azimuthal step back into the momenta, the new energy, the tracer and
   // the new density
-  k_azi_rings<<<(nr * 32 + 255) / 256, 256, 0, s>>>(g, vt, dt, S.nshift, S.vmed, S.vtemp);
+  k_azi_rings<<<(nr * 32 + 255) / 256, 256, 0, s>>>(g, vt, S.nshift, S.vmed, S.vtemp);
   g_thorin_launches++;
   AziIO az;
   for (int k = 0; k < nq; k++) {
@@ -1431,13 +1437,12 @@ void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, dou
   az.n = nq;
   const int T = azi_block(ns);
   const dim3 grid((ns + T - 2 * AZ_HALO - 1) / (T - 2 * AZ_HALO), nr);
-  if (nq == 7) k_azimuthal<7><<<grid, T, 0, s>>>(g, az, vt, dt, fast, S.nshift, S.vmed, S.vtemp);
-  else if (nq == 6) k_azimuthal<6><<<grid, T, 0, s>>>(g, az, vt, dt, fast, S.nshift, S.vmed, S.vtemp);
-  else k_azimuthal<5><<<grid, T, 0, s>>>(g, az, vt, dt, fast, S.nshift, S.vmed, S.vtemp);
+  if (nq == 7) k_azimuthal<7><<<grid, T, 0, s>>>(g, az, vt, fast, S.nshift, S.vmed, S.vtemp);
+  else if (nq == 6) k_azimuthal<6><<<grid, T, 0, s>>>(g, az, vt, fast, S.nshift, S.vmed, S.vtemp);
+  else k_azimuthal<5><<<grid, T, 0, s>>>(g, az, vt, fast, S.nshift, S.vmed, S.vtemp);
   g_thorin_launches++;
   // velocities from the transported momenta
-  k_velocities<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, S.rho_new, S.mom[0], S.mom[1], S.mom[2], S.mom[3], vr, vt,
-                                                 omega_frame, damp_vrad, dt, drin, drout,
+  k_velocities<<<grid2d(ns, nr, BX), BX, 0, s>>>(g, S.rho_new, S.mom[0], S.mom[1], S.mom[2], S.mom[3], vr, vt, damp_vrad, drin, drout,
                                                  energy ? S.e_new : nullptr, energy ? temper : nullptr, cs, gm1, gg1);
   g_thorin_launches++;
   if (label) {

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <string>
 #include <vector>
 #include "thorin_kernels.cuh"
@@ -136,6 +137,8 @@ struct thorin_disk {
   double *heat_val_d;
   unsigned int *ticket;
   DevPlanet *planets_d;
+  double *ctl;                       // control block (CTL_*), also d->g.ctl
+  AccArgs *acc_args_d;               // pebble accretion arguments on the device
   SorCtl sor;
   CflRings cfl;
   ForceRings fr;
@@ -378,6 +381,9 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
     RCHK(dalloc(d, (void **)&d->ring[q], n * sizeof(double)));
   }
   build_grid(d);
+  RCHK(dalloc(d, (void **)&d->ctl, CTL_COUNT * sizeof(double)));
+  d->g.ctl = d->ctl;
+  RCHK(dalloc(d, (void **)&d->acc_args_d, sizeof(AccArgs)));
   double **F[] = {&d->rho, &d->vrad, &d->vtheta, &d->energy, &d->vrad_new, &d->vtheta_new, &d->energy_new,
                   &d->vrad_int, &d->vtheta_int, &d->energy_int, &d->cs, &d->temper, &d->qplus, &d->qminus,
                   &d->opacity, &d->divv, &d->trr, &d->trp, &d->tpp, &d->agr, &d->agt, &d->dcen, &d->ml, &d->mlip,
@@ -1176,6 +1182,15 @@ extern "C" int thorin_planet_from_elements(thorin_planets *sys, int k, float mas
   return THORIN_OK;
 }
 
+// Writes control-block values (stream-ordered) for the kernels that follow.
+static void set_ctl(thorin_disk *d, std::initializer_list<std::pair<int, double>> kv, cudaStream_t s = nullptr)
+{
+  CtlSet v;
+  v.n = 0;
+  for (const auto &e : kv) { v.idx[v.n] = e.first; v.val[v.n] = e.second; v.n++; }
+  aux_set_ctl(d->ctl, v, s ? s : d->s);
+}
+
 // ---------------------------------------------------------------------------
 // Substep pieces
 extern "C" int thorin_gpu_cfl(thorin_disk *d, double dt_remaining, double invdtreb_sq, int *n_sub)
@@ -1186,8 +1201,7 @@ extern "C" int thorin_gpu_cfl(thorin_disk *d, double dt_remaining, double invdtr
   memset(&f, 0, sizeof(f));
   f.pebbles = p.pebbles && !d->sloppy_pass && !p.sloppy_cfl;   // SloppyCFL: CriticalCharTime is never called (rate 0)
   f.first_call = d->cfl_first;
-  f.deltaT = dt_remaining;
-  f.invdtreb_sq = invdtreb_sq;
+  set_ctl(d, {{CTL_DELTAT, dt_remaining}, {CTL_INVDTREB, invdtreb_sq}});
   f.minimum_step = p.minimum_step;
   f.maximum_step = p.maximum_step;
   f.first_step = p.first_step;
@@ -1252,6 +1266,11 @@ static void heating1(thorin_disk *d, double Mp, double dMp, double Xp, double Yp
 extern "C" int thorin_gpu_accrete(thorin_disk *d, thorin_planets *sys, double dt)
 {
   const thorin_params &p = d->p;
+  {
+    double facc = p.evaporation_rate * dt;                         // EvaporatePebbles' fraction
+    if (facc > 1.0) facc = 1.0;
+    set_ctl(d, {{CTL_DT, dt}, {CTL_OMEGA_FRAME, d->OmegaFrame}, {CTL_FACC_EVAP, facc}});
+  }
   for (int k = 0; k < sys->nb; k++) { d->heatsrc[k] = 0.0; d->heatsrc_index[k] = -1; }   // InitHeating
   // AccreteOntoPlanets (Planet.c:34-166)
   for (int k = 0; k < sys->nb; k++) {
@@ -1332,7 +1351,7 @@ extern "C" int thorin_gpu_accrete(thorin_disk *d, thorin_planets *sys, double dt
     a.imin = imin; a.imax = imax;
     double dMp = 0, dPx = 0, dPy = 0;
     if (imin <= imax) {
-      aux_accrete(d->g, a, d->scal, d->s);
+      aux_accrete(d->g, a, d->acc_args_d, d->scal, d->s);
       KCHECK("accretion kernel");
       CUCHK(cudaMemcpyAsync(d->scal_h + SC_ACC_DM, d->scal + SC_ACC_DM, 3 * sizeof(double), cudaMemcpyDeviceToHost, d->s));
       CUCHK(cudaStreamSynchronize(d->s));
@@ -1345,11 +1364,8 @@ extern "C" int thorin_gpu_accrete(thorin_disk *d, thorin_planets *sys, double dt
     sys->vx[k] = PX / M;
     sys->vy[k] = PY / M;
   }
-  if (p.evaporation_rate > 0.0) {                                  // EvaporatePebbles
-    double facc = p.evaporation_rate * dt;
-    if (facc > 1.0) facc = 1.0;
-    aux_evaporate(d->g, d->temper, d->pdens, facc, d->s);
-  }
+  if (p.evaporation_rate > 0.0)                                    // EvaporatePebbles
+    aux_evaporate(d->g, d->temper, d->pdens, d->s);
   return THORIN_OK;
 }
 
@@ -1402,11 +1418,11 @@ extern "C" int thorin_gpu_forces(thorin_disk *d, thorin_planets *sys, double mas
   a.part = d->partials;
   a.pl = d->planets_d;
   a.npl = npl; a.pebbles = p.pebbles; a.exclude_hill = p.exclude_hill; a.pebble_gravity = p.pebble_gravity;
-  a.mass_taper = mass_taper; a.pebble_alpha = p.pebble_alpha; a.hillcut = p.hillcut;
-  a.full_mass = (mass_taper == 1.0) ? 1 : 0;
+  a.pebble_alpha = p.pebble_alpha; a.hillcut = p.hillcut;
   a.sqrt_pebble_alpha = sqrt(p.pebble_alpha);
   const double indx_pl = p.indirect_term ? -axs : 0.0, indy_pl = p.indirect_term ? -ays : 0.0;
-  aux_forces(d->g, a, d->fr, indx_pl, indy_pl, d->scal, d->s);
+  set_ctl(d, {{CTL_MASS_TAPER, mass_taper}, {CTL_INDX_PL, indx_pl}, {CTL_INDY_PL, indy_pl}});
+  aux_forces(d->g, a, d->fr, d->scal, d->s);
   KCHECK("force kernels");
   // DampingTW04 needs the ring means of Sigma (and c_s) at each planet
   for (int k = 0; k < npl; k++) {
@@ -1541,7 +1557,8 @@ static int sor_solve(thorin_disk *d, double omega, int *niter, int *capped, bool
 {
   // normres0 and the threshold always come from the start temperature as
   // the reference has it; a learned start only moves T before the sweeps
-  hydro_sor_resid0(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, omega, d->sor, d->s);
+  set_ctl(d, {{CTL_SOR_OMEGA, omega}});
+  hydro_sor_resid0(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, d->sor, d->s);
   KCHECK("SOR residual kernel");
   if (learned && d->ws_net && d->ws_mode == THORIN_WS_PREDICT) {
     // keep the start (for the update record after the solve), then move it
@@ -1632,7 +1649,7 @@ static int energy_step(thorin_disk *d, double dt)
   hydro_qplus(d->g, d->vrad, d->vtheta, d->rho, d->divv, d->qplus, d->invdphi, d->lr01, d->lr12, d->s);
   if (p.parametric_cooling) {
     aux_parametric_cooling(d->g, d->rho, d->energy_int, d->qplus, d->divv, d->ring[R_COOLT], d->ring[R_QPLUSMED],
-                           d->energy_new, dt, d->gm1, d->s);
+                           d->energy_new, d->gm1, d->s);
     KCHECK("cooling kernel");
     std::swap(d->energy, d->energy_new);
     return THORIN_OK;
@@ -1658,7 +1675,7 @@ static int energy_step(thorin_disk *d, double dt)
     }
   }
   hydro_matrix(d->g, d->rho, d->temper, d->cs, d->dcen, d->divv, d->qminus, d->qplus, d->qirr, d->ml, d->mlip, d->mlim,
-               d->mljp, d->mljm, d->rhs, dt, d->gm1, d->ring[R_INVDXTHETA2], p.stellar_irradiation, nheat,
+               d->mljp, d->mljm, d->rhs, d->gm1, d->ring[R_INVDXTHETA2], p.stellar_irradiation, nheat,
                d->heat_idx_d, d->heat_val_d, d->s);
   KCHECK("energy kernels");
   if (d->sor_first) {
@@ -1704,7 +1721,7 @@ static void transport_fluid(thorin_disk *d, double **rho, double *vr, double *vt
   // the velocity kernel when it is the only boundary condition
   const thorin_params &p = d->p;
   const int fused = p.damping && p.damp_vrad && !(p.open_inner || p.open_outer || p.non_reflecting || p.outer_source_mass);
-  hydro_transport(d->g, rho, vr, vt, energy, (gas && p.label_advection) ? d->label : nullptr, S, dt, d->OmegaFrame,
+  hydro_transport(d->g, rho, vr, vt, energy, (gas && p.label_advection) ? d->label : nullptr, S,
                   p.fast_transport, gas && fused, d->drin, d->drout, gas ? d->temper : nullptr, d->cs, d->gm1, d->gg1,
                   stream);
   std::swap(*rho, *rho_scratch);
@@ -1714,6 +1731,7 @@ static void transport_fluid(thorin_disk *d, double **rho, double *vr, double *vt
 extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
 {
   const thorin_params &p = d->p;
+  set_ctl(d, {{CTL_DT, dt}, {CTL_OMEGA_FRAME, d->OmegaFrame}});
   const int damp = p.damping;
   auto boundary = [&]() {                // ApplyBoundaryCondition (SideEuler.c:490-503)
     if (p.open_inner) aux_open_inner(d->g, d->rho, d->vrad, d->energy, p.energy_eq, p.damp_flux, p.gasflux, d->s);
@@ -1729,8 +1747,7 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
     if (p.outer_source_mass)
       aux_outer_source_mass(d->g, d->rho, d->vrad, p.imposed_disk_drift * pow((d->Rinf[d->nr - 1] / 1.0), -p.sigma_slope),
                             d->s);
-    if (damp) aux_damp_gas(d->g, d->vrad, d->rho, d->vtheta, d->energy, d->damp_rings_d, d->ndamp, d->ring[R_DAMPVR0],
-                           dt, d->OmegaFrame, p.damp_init, p.damp_flux, p.energy_eq, d->s);
+    if (damp) aux_damp_gas(d->g, d->vrad, d->rho, d->vtheta, d->energy, d->damp_rings_d, d->ndamp, d->ring[R_DAMPVR0], p.damp_init, p.damp_flux, p.energy_eq, d->s);
   };
   // ApplyBoundaryCondition, DetectCrash, ComputePressureField (SourceEuler.c:271-292)
   boundary();
@@ -1739,21 +1756,21 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
   if (!p.energy_eq) aux_iso_eos(d->g, d->rho, nullptr, d->cs, d->press, d->temper, 0, 1, 0, d->s);
   // SourceTermsPebbles (Pebbles.c:550-613)
   if (p.pebbles) {
-    aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, d->s);
+    aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, d->s);
     aux_pebble_sources(d->g, d->pdens, d->pvrad, d->pvtheta, d->tau, d->vrad, d->vtheta, d->pagr, d->pagt, d->paccr,
-                       d->pacct, d->dragr, d->dragt, d->OmegaFrame, p.back_reaction, d->s);
+                       d->pacct, d->dragr, d->dragt, p.back_reaction, d->s);
   }
   // SubStep1 with viscous terms (SourceEuler.c:319-415)
   hydro_substep1(d->g, d->rho, d->vrad, d->vtheta, d->energy, p.energy_eq ? nullptr : d->press, d->agr, d->agt, d->dragr, d->dragt, d->vrad_int,
-                 d->vtheta_int, d->gaccr, d->gacct, dt, d->OmegaFrame, d->gm1, p.pebbles, p.back_reaction,
+                 d->vtheta_int, d->gaccr, d->gacct, d->gm1, p.pebbles, p.back_reaction,
                  d->ring[R_SUPPTORQUE], d->ring[R_INVDXTHETA], d->s);
   hydro_stress(d->g, d->vrad_int, d->vtheta_int, d->rho, d->divv, d->trr, d->tpp, d->trp, d->invdphi, d->s);
   const int kepler = (!p.damping) || (p.damping && p.damp_vrad);
-  hydro_visc_update(d->g, d->vrad_int, d->vtheta_int, d->rho, d->trr, d->tpp, d->trp, dt, d->invdphi, kepler,
+  hydro_visc_update(d->g, d->vrad_int, d->vtheta_int, d->rho, d->trr, d->tpp, d->trp, d->invdphi, kepler,
                     d->vkep_in - d->Rmed[0] * d->OmegaFrame, d->vkep_out - d->Rmed[d->nr - 1] * d->OmegaFrame, d->s);
   if (p.pebbles) {
     aux_pebble_substep1(d->g, d->pvrad, d->pvtheta, d->tau, d->vrad, d->vtheta, d->paccr, d->pacct, d->gaccr, d->gacct,
-                        d->rho, d->pdens, dt, p.diffusive_particles, p.schmidt_number, d->ring[R_INVDXTHETA], d->s);
+                        d->rho, d->pdens, p.diffusive_particles, p.schmidt_number, d->ring[R_INVDXTHETA], d->s);
     // EvolvePebbleDisk (Pebbles.c:702-708).  From here on the pebble fields
     // are read and written only by the pebble transport and the gas side
     // touches none of them, so it runs on the pebble stream while the gas
@@ -1761,13 +1778,13 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
     // streams join before this call returns.
     CUCHK(cudaEventRecord(d->ev_fork, d->s));
     CUCHK(cudaStreamWaitEvent(d->s_peb, d->ev_fork, 0));
-    aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, d->s_peb);
+    aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, d->s_peb);
     transport_fluid(d, &d->pdens, d->pvrad, d->pvtheta, nullptr, &d->t_rho_peb, dt, 0, d->ts_peb, d->s_peb);
-    aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, dt, d->OmegaFrame, d->s_peb);
+    aux_damp_peb(d->g, d->pdens, d->pvrad, d->pvtheta, d->damp_rings_d, d->ndamp, d->s_peb);
     CUCHK(cudaEventRecord(d->ev_join, d->s_peb));
   }
   // SubStep2, ActualiseGas, ApplyBoundaryCondition
-  hydro_substep2(d->g, d->rho, d->vrad_int, d->vtheta_int, d->energy, d->vrad_new, d->vtheta_new, d->energy_int, dt,
+  hydro_substep2(d->g, d->rho, d->vrad_int, d->vtheta_int, d->energy, d->vrad_new, d->vtheta_new, d->energy_int,
                  p.energy_eq, d->ring[R_INVDXTHETA], d->s);
   std::swap(d->vrad, d->vrad_new);
   std::swap(d->vtheta, d->vtheta_new);

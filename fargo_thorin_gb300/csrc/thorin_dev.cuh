@@ -53,11 +53,34 @@ struct DevRings {
   double *nu_med, *nu_inf;               // FViscosity(Rmed[i]), FViscosity(Rinf[i])
 };
 
+// The disk's control block: scalars that change from one substep to the
+// next.  Kernels read them from device memory instead of taking them as
+// arguments, so that the launches of a substep do not depend on host values
+// and a whole DT can be captured and replayed as one CUDA graph.  The host
+// path writes them (k_set_ctl) before the kernels that read them; the graph
+// path computes them on the device.
+enum {
+  CTL_DT = 0,            // substep length dt
+  CTL_OMEGA_FRAME,       // OmegaFrame
+  CTL_MASS_TAPER,        // MassTaper (SourceEuler.c:230-231)
+  CTL_SOR_OMEGA,         // relaxation parameter of the current SOR solve
+  CTL_FACC_EVAP,         // EvaporatePebbles' fraction min(EVAPORATIONRATE dt, 1)
+  CTL_INDX_PL,           // indirect acceleration of the planets (x, y)
+  CTL_INDY_PL,
+  CTL_DELTAT,            // the DT's remaining interval DT - dtemp (ConditionCFL)
+  CTL_INVDTREB,          // MinStepForRebound's rate invdtreb_sq
+  CTL_TIME,              // PhysicalTime
+  CTL_DTEMP,             // time advanced so far in this DT
+  CTL_SOR_DOMEGA,        // omega schedule step (EnergySources.c:298-317)
+  CTL_COUNT = 32
+};
+
 struct DevGrid {
   int nr, ns;
   int nsm;                               // multiprocessors of the disk's GPU
   DevRings r;
   DevConst k;
+  double *ctl;                           // control block (CTL_*), CTL_COUNT doubles
 };
 
 __device__ __forceinline__ int jp_of(int j, int ns) { return (j == ns - 1) ? 0 : j + 1; }

@@ -86,13 +86,12 @@ struct ForceArgs {
   double *part;               // [nblocks][2 + 2*npl]
   const DevPlanet *pl;
   int npl, pebbles, exclude_hill, pebble_gravity;
-  double mass_taper, pebble_alpha, hillcut;
+  double pebble_alpha, hillcut;   // the mass taper is read from the control block
   double sqrt_pebble_alpha;   // sqrt(pebble_alpha)
   // vertical quadrature weights exp(-z_m^2 / 2H^2) at z_m = (m - 1/2) 3H/N,
   // which do not depend on H, and their sums (filled by aux_forces)
   double wq10[10], wq30[30], sig10, sig30;
   double isig10, isig30;      // 1 / sig10, 1 / sig30
-  int full_mass;              // mass_taper == 1.0
 };
 
 struct GasAccArgs {           // one planet of AccreteOntoPlanets (Planet.c:34-166)
@@ -107,6 +106,7 @@ struct AccArgs {
   const double *pvr, *pvt, *tau, *cs, *vt;
   double Xp, Yp, Zp, VXp, VYp, VZp, Mp, Rp, Rhill, Omegap, Rp15, omega_frame, dt, pebble_alpha, frac;
   int imin, imax, iflow;
+  int nb;                     // blocks over the annulus imin..imax (aux_accrete_blocks)
 };
 
 // Number of kernels launched by this library (host-side bookkeeping; every
@@ -117,16 +117,16 @@ extern std::atomic<long long> g_thorin_launches;
 // kernels_hydro.cu
 void hydro_substep1(const DevGrid &g, const double *rho, const double *vrad, const double *vtheta,
                     const double *energy, const double *press, const double *agr, const double *agt, const double *dragr, const double *dragt,
-                    double *vradint, double *vthetaint, double *gaccr, double *gacct, double dt, double omega_frame,
+                    double *vradint, double *vthetaint, double *gaccr, double *gacct,
                     double gm1, int pebbles, int back_reaction, const double *supp_torque, const double *invdxtheta_r,
                     cudaStream_t s);
 void hydro_stress(const DevGrid &g, const double *vr, const double *vt, const double *rho, double *divv, double *trr,
                   double *tpp, double *trp, double invdphi, cudaStream_t s);
 void hydro_visc_update(const DevGrid &g, double *vr, double *vt, const double *rho, const double *trr, const double *tpp,
-                       const double *trp, double dt, double invdphi, int kepler, double vkin, double vkout,
+                       const double *trp, double invdphi, int kepler, double vkin, double vkout,
                        cudaStream_t s);
 void hydro_substep2(const DevGrid &g, const double *rho, const double *vr, const double *vt, const double *energy,
-                    double *vrnew, double *vtnew, double *eint, double dt, int energy_eq, const double *invdxtheta_r,
+                    double *vrnew, double *vtnew, double *eint, int energy_eq, const double *invdxtheta_r,
                     cudaStream_t s);
 void hydro_qplus(const DevGrid &g, const double *vr, const double *vt, const double *rho, double *divv, double *qplus,
                  double invdphi, double lr01, double lr12, cudaStream_t s);
@@ -142,12 +142,12 @@ void hydro_irradiation(const DevGrid &g, const double *rho, const double *cs, co
                        const double *rinf15, const double *rsup15, cudaStream_t s);
 void hydro_matrix(const DevGrid &g, const double *rho, const double *T, const double *cs, const double *dcen,
                   const double *divv, const double *qminus, const double *qplus, const double *qirr, double *ml,
-                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs, double dt,
+                  double *mlip, double *mlim, double *mljp, double *mljm, double *rhs,
                   double gm1, const double *invdxtheta2_r, int irradiation, int nheat, const int *heat_idx,
                   const double *heat_val, cudaStream_t s);
 int sor_blocks(const DevGrid &g);
 void hydro_sor_resid0(const DevGrid &g, const double *T, const double *ml, const double *mlip, const double *mlim,
-                      const double *mljp, const double *mljm, const double *rhs, double *cw, double omega,
+                      const double *mljp, const double *mljm, const double *rhs, double *cw,
                       const SorCtl &c, cudaStream_t s);
 // `count` sweeps (two colour passes each).  The sweep number lives on the
 // device, so every call with the same count issues identical launches (the
@@ -158,7 +158,7 @@ void hydro_sor_sweeps(const DevGrid &g, double *T, const double *ml, const doubl
                       double eps, int count, int maxiters, cudaStream_t s);
 void hydro_energy_from_t(const DevGrid &g, const double *rho, double *T, double *enew, cudaStream_t s);
 void hydro_transport(const DevGrid &g, double **rho, double *vr, double *vt, double **energy, double *label,
-                     const TransportScratch &S, double dt, double omega_frame, int fast, int damp_vrad, double drin,
+                     const TransportScratch &S, int fast, int damp_vrad, double drin,
                      double drout, double *temper, double *cs, double gm1, double gg1, cudaStream_t s);
 
 // kernels_aux.cu
@@ -171,9 +171,9 @@ void aux_stokes(const DevGrid &g, const double *rho, const double *psize, double
 void aux_cfl(const DevGrid &g, const double *vr, const double *vt, const double *cs, const double *pvr, const double *pvt,
              const CflRings &cr, int pebbles, int fast, int viscous, double *part, const CflFinal &f0, double *scal,
              int *iscal, cudaStream_t s);
-void aux_evaporate(const DevGrid &g, const double *T, double *pdens, double facc, cudaStream_t s);
+void aux_evaporate(const DevGrid &g, const double *T, double *pdens, cudaStream_t s);
 void aux_damp_gas(const DevGrid &g, double *vrad, double *rho, double *vtheta, double *energy, const int *rings,
-                  int nrings, const double *vr0r, double dt, double omega_frame, int damp_init, int damp_flux,
+                  int nrings, const double *vr0r, int damp_init, int damp_flux,
                   int energy_eq, cudaStream_t s);
 void aux_open_inner(const DevGrid &g, double *rho, double *vr, double *energy, int energy_eq, int damp_flux,
                     double gasflux, cudaStream_t s);
@@ -182,7 +182,7 @@ void aux_open_outer(const DevGrid &g, double *rho, double *vr, double *energy, i
 void aux_nonreflecting(const DevGrid &g, double *rho, double *vr, double *energy, const double *cs, cudaStream_t s);
 void aux_outer_source_mass(const DevGrid &g, double *rho, double *vr, double penul_vr, cudaStream_t s);
 void aux_parametric_cooling(const DevGrid &g, const double *rho, const double *eint, const double *qplus,
-                            const double *divv, const double *coolt, const double *qplusmed, double *enew, double dt,
+                            const double *divv, const double *coolt, const double *qplusmed, double *enew,
                             double gm1, cudaStream_t s);
 void aux_gas_accrete(const DevGrid &g, double *dens, const double *vrad, const double *vtheta, const double *cs,
                      const GasAccArgs &a, double *out, cudaStream_t s);
@@ -191,20 +191,27 @@ void aux_drag_cell(const double *rho, const double *cs, const double *vrad, cons
 void aux_correct_vtheta(const DevGrid &g, double *vt, double domega, cudaStream_t s);
 void aux_iso_eos(const DevGrid &g, const double *rho, const double *csr, double *cs, double *press, double *temper,
                  int set_cs, int set_press, int set_temper, cudaStream_t s);
-void aux_damp_peb(const DevGrid &g, double *pd, double *pvr, double *pvt, const int *rings, int nrings, double dt,
-                  double omega_frame, cudaStream_t s);
+void aux_damp_peb(const DevGrid &g, double *pd, double *pvr, double *pvt, const int *rings, int nrings, cudaStream_t s);
 void aux_crash(const DevGrid &g, const double *f, int *flag, cudaStream_t s);
 void aux_pebble_sources(const DevGrid &g, const double *pd, const double *pvr, const double *pvt, const double *tau,
                         const double *vr, const double *vt, const double *pagr, const double *pagt, double *paccr,
-                        double *pacct, double *dragr, double *dragt, double omega_frame, int back_reaction,
+                        double *pacct, double *dragr, double *dragt, int back_reaction,
                         cudaStream_t s);
 void aux_pebble_substep1(const DevGrid &g, double *pvr, double *pvt, const double *tau, const double *vr, const double *vt,
                          const double *paccr, const double *pacct, const double *gaccr, const double *gacct,
-                         const double *rho, const double *pd, double dt, int diffusion, double schmidt,
+                         const double *rho, const double *pd, int diffusion, double schmidt,
                          const double *invdxtheta_r, cudaStream_t s);
-void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr, double indx_pl, double indy_pl,
+void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr,
                 double *scal, cudaStream_t s);
-void aux_accrete(const DevGrid &g, const AccArgs &a, double *scal, cudaStream_t s);
+// AccArgs go to the device first (a_dev), the kernels read them there.
+void aux_accrete(const DevGrid &g, const AccArgs &a, AccArgs *a_dev, double *scal, cudaStream_t s);
+// The accretion kernels alone over a grid of nb_grid blocks (at least the
+// annulus' aux_accrete_blocks; blocks beyond it return at once), arguments
+// and the two ring means of v_theta already on the device.
+void aux_accrete_kernels(const DevGrid &g, const AccArgs *a_dev, int nb_grid, double *scal, cudaStream_t s);
+// Control block writes (host path): up to 6 (index, value) pairs.
+struct CtlSet { int n; int idx[6]; double val[6]; };
+void aux_set_ctl(double *ctl, const CtlSet &v, cudaStream_t s);
 int aux_accrete_blocks(const DevGrid &g, int imin, int imax);
 void aux_integrals(const DevGrid &g, const double *rho, const double *vr, const double *vt, const double *e,
                    const double *pd, const double *pvt, double omega_frame, int pebbles, double *part, double *scal,
