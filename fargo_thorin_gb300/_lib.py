@@ -36,6 +36,11 @@ SIGNATURES = {
     "thorin_gpu_correct_vtheta": (C.c_int, [_P, C.c_double]),
     "thorin_gpu_stokes": (C.c_int, [_P]),
     "thorin_gpu_algogas": (C.c_int, [_P, C.POINTER(ThorinPlanets)]),
+    "thorin_gpu_algogas_graph": (C.c_int, [_P, C.POINTER(ThorinPlanets)]),
+    "thorin_gpu_graph_supported": (C.c_int, [_P, C.POINTER(ThorinPlanets)]),
+    "thorin_gpu_set_launch_shape": (C.c_int, [_P, C.c_int, C.c_int]),
+    "thorin_gpu_get_launch_shape": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "thorin_ensemble_algogas_graph": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int, C.POINTER(C.c_int)]),
     "thorin_gpu_integrals": (C.c_int, [_P, _D, _D, _D, _D, _D]),
     "thorin_gpu_get_nshift": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "thorin_gpu_get_stats": (C.c_int, [_P, C.POINTER(ThorinStats)]),

@@ -18,7 +18,10 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libthorin_gpu.so")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["kernels_hydro.cu", "kernels_aux.cu", "thorin_api.cu", "thorin_noalloc.cu", "thorin_selftest.cu",
-           "warmnet.cu", "thorin_ensemble.cu"]
+           "warmnet.cu", "thorin_ensemble.cu", "thorin_graph.cu"]
+# the control kernels of the device-resident DT repeat host arithmetic and
+# are compiled, like the host code, without FMA contraction
+NO_FMA = {"thorin_graph.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=true", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2"]
 
@@ -48,7 +51,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_v: bool = False) -> 
         o = os.path.join(BUILD, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            cmd = [nv, *ARCH, *FLAGS, *(["-Xptxas", "-v"] if ptxas_v else []), "-c", s, "-o", o]
+            flags = [f.replace("--fmad=true", "--fmad=false") for f in FLAGS] if src in NO_FMA else FLAGS
+            cmd = [nv, *ARCH, *flags, *(["-Xptxas", "-v"] if ptxas_v else []), "-c", s, "-o", o]
             jobs.append(cmd)
 
     def run(cmd):

@@ -2,6 +2,7 @@
 // damping boundaries, disk forces with their reductions, pebble accretion,
 // conservation integrals.
 #include "thorin_kernels.cuh"
+#include "thorin_graph.cuh"
 
 static inline dim3 grid2d(int ns, int rows, int bx) { return dim3((ns + bx - 1) / bx, rows); }
 static const int BX = 128;
@@ -20,6 +21,15 @@ static const int BX = 128;
 // last bits.  The only integer decision fed by a ring mean, the FARGO shift,
 // re-sums its ring in order when the mean lands near a rounding tie (see
 // k_azimuthal).  Output index is relative to ring0.
+// One warp's fixed-tree sum of a ring (all lanes return it).
+__device__ __forceinline__ double warp_ring_sum(const double *__restrict__ row, int ns, int lane)
+{
+  double a = 0.0;
+  for (int j = lane; j < ns; j += 32) a += row[j];
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(TH_FULL, a, o);
+  return a;
+}
+
 __global__ void __launch_bounds__(256) k_ring_means(int ns, const double *__restrict__ f0,
                                                     const double *__restrict__ f1, double *__restrict__ o0,
                                                     double *__restrict__ o1, int ring0, int nrings, int nf)
@@ -27,19 +37,33 @@ __global__ void __launch_bounds__(256) k_ring_means(int ns, const double *__rest
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (w >= nrings) return;                         // whole warp
   const size_t base = (size_t)(ring0 + w) * ns;
-  double a0 = 0.0, a1 = 0.0;
-  for (int j = lane; j < ns; j += 32) {
-    a0 += f0[base + j];
-    if (nf > 1) a1 += f1[base + j];
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    a0 += __shfl_xor_sync(TH_FULL, a0, o);
-    if (nf > 1) a1 += __shfl_xor_sync(TH_FULL, a1, o);
-  }
+  const double a0 = warp_ring_sum(f0 + base, ns, lane);
+  const double a1 = (nf > 1) ? warp_ring_sum(f1 + base, ns, lane) : 0.0;
   if (lane == 0) {
     o0[w] = a0 / (double)ns;
     if (nf > 1) o1[w] = a1 / (double)ns;
   }
+}
+
+// The same ring means at rings chosen on the device: ring info[slot] and,
+// with two, info[slot + 1] rings from there (else one ring when
+// info[slot] >= 0, none when it is negative).
+__global__ void __launch_bounds__(64) k_ring_means_at(int ns, const double *__restrict__ f, double *__restrict__ o,
+                                                      const int *__restrict__ info, int slot, int two)
+{
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ring0 = info[slot];
+  const int nrings = two ? info[slot + 1] : (ring0 >= 0 ? 1 : 0);
+  if (ring0 < 0 || w >= nrings) return;
+  const double a = warp_ring_sum(f + (size_t)(ring0 + w) * ns, ns, lane);
+  if (lane == 0) o[w] = a / (double)ns;
+}
+
+void graph_ring_means_at(const DevGrid &g, const double *f, double *out, const int *ring_info, int slot, int two_slots,
+                         cudaStream_t s)
+{
+  k_ring_means_at<<<1, 64, 0, s>>>(g.ns, f, out, ring_info, slot, two_slots);
+  g_thorin_launches++;
 }
 
 void aux_ring_means(const DevGrid &g, const double *f0, double *o0, const double *f1, double *o1, int ring0, int nrings,
@@ -778,7 +802,6 @@ __device__ double column_mass(double a, double b, double Hpeb)
 // by a one-block kernel that sums the block partials in a fixed order and
 // does the scalar steps of the reference.
 // acc[] scalars: 0 Reff, 1 vrel, 2 Mt, 3 limiter.
-#define ACC_BX 256
 
 __global__ void __launch_bounds__(ACC_BX) k_acc_tau(DevGrid g, const AccArgs *__restrict__ ap)
 {
@@ -795,6 +818,7 @@ __global__ void __launch_bounds__(ACC_BX) k_acc_reff(DevGrid g, const AccArgs *_
 {
   const AccArgs &a = *ap;
   const int nb = a.nb;
+  if (nb == 0) return;                       // no annulus (only the device-resident DT launches this)
   const int ns = g.ns;
   __shared__ double sh[2];
   if (threadIdx.x == 0) {                    // vt1D at the two rings bracketing the planet
@@ -864,6 +888,7 @@ __global__ void __launch_bounds__(ACC_BX) k_acc_limiter(const AccArgs *__restric
 {
   const AccArgs &a = *ap;
   const int nb = a.nb;
+  if (nb == 0) return;
   double v[4] = {0.0, 0.0, 0.0, 0.0};
   for (int b = threadIdx.x; b < nb; b += blockDim.x)
     for (int k = 0; k < 4; k++) v[k] += a.part[4 * b + k];

@@ -1306,27 +1306,35 @@ void hydro_matrix(const DevGrid &g, const double *rho, const double *T, const do
 }
 
 
-static dim3 sor_grid_pass(const DevGrid &g)
+// Resident k_sor_pass blocks per multiprocessor that fit (occupancy API),
+// found once.
+static int sor_occ_max()
 {
-  static std::atomic<int> occ_cache{0};            // resident k_sor_pass blocks per multiprocessor
+  static std::atomic<int> occ_cache{0};
   int occ = occ_cache.load();
   if (occ == 0) {
 #ifdef SOR_CARVEOUT
     cudaFuncSetAttribute(k_sor_pass, cudaFuncAttributePreferredSharedMemoryCarveout, SOR_CARVEOUT);
 #endif
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sor_pass, SOR_BX, 0) != cudaSuccess || occ < 1) occ = 1;
-    // at most 1536 resident threads per SM: on the 1024x3072 disk the pass
-    // took 29.3 us with 12 blocks of 128 per SM (also with 6 of 256), 30.4 us
-    // with the 16 that fit, 31.6 us with 8
-    if (occ * SOR_BX > 1536) occ = 1536 / SOR_BX > 0 ? 1536 / SOR_BX : 1;
-#ifdef SOR_OCC
-    occ = SOR_OCC;
-#endif
-#ifdef SOR_PRINT_OCC
-    std::fprintf(stderr, "k_sor_pass: %d blocks per SM\n", occ);
-#endif
     occ_cache.store(occ);
   }
+  return occ;
+}
+
+// One wave of resident blocks striding over the (ring, tile) tiles, with at
+// most g.sor_tpsm threads per multiprocessor (default 1536: on the 1024x3072
+// disk the pass took 29.3 us with 12 blocks of 128 per SM, 30.4 us with the
+// 16 that fit, 31.6 us with 8; the ensemble autotuner may pick another cap
+// per disk).
+static dim3 sor_grid_pass(const DevGrid &g, bool capped = true)
+{
+  int occ = sor_occ_max();
+  const int tpsm = g.sor_tpsm > 0 ? g.sor_tpsm : 1536;
+  if (capped && occ * SOR_BX > tpsm) occ = tpsm / SOR_BX > 0 ? tpsm / SOR_BX : 1;
+#ifdef SOR_OCC
+  occ = SOR_OCC;
+#endif
   const int half = g.ns / 2;
   const long long ntiles = (long long)((half + SOR_BX * SOR_CPT - 1) / (SOR_BX * SOR_CPT)) * (g.nr - 2);
   const long long wave = (long long)g.nsm * occ;
@@ -1340,7 +1348,7 @@ static dim3 sor_grid_resid(const DevGrid &g)
 
 int sor_blocks(const DevGrid &g)
 {
-  const dim3 a = sor_grid_pass(g), b = sor_grid_resid(g);
+  const dim3 a = sor_grid_pass(g, false), b = sor_grid_resid(g);
   const int na = a.x * a.y, nb = b.x * b.y;
   return na > nb ? na : nb;
 }

@@ -12,6 +12,8 @@
 #include <string>
 #include <vector>
 #include "thorin_kernels.cuh"
+#include "thorin_planet.cuh"
+#include "thorin_graph.cuh"
 #include "../../include/thorin_warmnet.h"
 
 // learned SOR warm start (warmnet.cu)
@@ -138,6 +140,19 @@ struct thorin_disk {
   unsigned int *ticket;
   DevPlanet *planets_d;
   double *ctl;                       // control block (CTL_*), also d->g.ctl
+  PlConst plc;                       // constants of the planet side (thorin_planet.cuh)
+  // device-resident DT (thorin_gpu_algogas_graph): the instantiated graph of
+  // one DT, the planets and counters it keeps on the device, and the state
+  // of the capture that builds it
+  cudaGraphExec_t dt_graph = nullptr;
+  thorin_planets *sys_d = nullptr, *sys_h = nullptr;   // device copy, pinned staging copy
+  GraphStats *gst_d = nullptr, *gst_h = nullptr;
+  int *ring_info_d = nullptr;
+  double *ctl_h = nullptr;           // pinned staging of the control block
+  int graph_npl = -1;                // planets the graph was built for
+  int capturing = 0;                 // launches are being captured into the DT graph
+  StepDev capS;
+  cudaGraph_t capture_sor_body = nullptr;   // body of the SOR loop node, filled after the substep capture
   AccArgs *acc_args_d;               // pebble accretion arguments on the device
   SorCtl sor;
   CflRings cfl;
@@ -325,6 +340,7 @@ static void build_grid(thorin_disk *d)
 {
   DevGrid &g = d->g;
   g.nr = d->nr; g.ns = d->ns;
+  g.sor_tpsm = 1536;
   int dev = 0;
   g.nsm = 1;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&g.nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -480,6 +496,23 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   RCHK(dalloc(d, (void **)&d->sor.gipart, (size_t)ng * sizeof(int)));
   RCHK(dalloc(d, (void **)&d->sor.gticket, (size_t)ng * SOR_TSTRIDE * sizeof(unsigned int)));
   fill_rings(d);
+  {
+    PlConst &c = d->plc;                 // constants of the planet side of a substep
+    const thorin_params &q = d->p;
+    c.nr = d->nr; c.ns = d->ns;
+    c.rin = d->Rinf[0]; c.rout = d->Rsup[d->nr - 1];
+    c.plrho = q.planetary_density / RHO2CGS;
+    c.tdelay = 4.0 * q.dt * (double)q.heating_delay;
+    c.thickness_smoothing = q.thickness_smoothing;
+    c.sqrt_adiabind_inv = 1.0 / sqrt(q.adiabind);
+    c.adiabind = q.adiabind;
+    c.pebble_alpha = q.pebble_alpha;
+    c.vertical_damping = q.vertical_damping;
+    c.mass_taper_param = q.mass_taper;
+    c.indirect_term = q.indirect_term;
+    c.accret_heating = q.accret_heating;
+    c.feel_disk_any = q.feel_disk;
+  }
   // damping rings (rows with Rmed outside [DRin, DRout])
   std::vector<int> rings;
   for (int i = 0; i < d->nr; i++)
@@ -598,6 +631,10 @@ extern "C" int thorin_gpu_destroy(thorin_disk *d)
   cudaFreeHost(d->iscal_h);
   cudaFreeHost(d->csmean_h);
   if (d->sor_loop) cudaGraphExecDestroy(d->sor_loop);
+  if (d->dt_graph) cudaGraphExecDestroy(d->dt_graph);
+  if (d->sys_h) cudaFreeHost(d->sys_h);
+  if (d->gst_h) cudaFreeHost(d->gst_h);
+  if (d->ctl_h) cudaFreeHost(d->ctl_h);
   for (int q = 0; q < 4; q++) cudaEventDestroy(d->ev[q]);
   if (d->s_peb) {
     cudaStreamSynchronize(d->s_peb);
@@ -1078,84 +1115,9 @@ extern "C" int thorin_gpu_init_pebbles(thorin_disk *d)
 // Host N-body step standing in for REBOUND's IAS15 (ReboundInterface.c:
 // 262-325): heliocentric -> barycentric, star + planets with mutual gravity
 // over dt (classical RK4 with 256 substeps), back to heliocentric.
-static void nbody_accel(int n, const double *m, const double *x, double *a)
-{
-  for (int i = 0; i < 3 * n; i++) a[i] = 0.0;
-  for (int i = 0; i < n; i++)
-    for (int j = i + 1; j < n; j++) {
-      double dx = x[3 * j] - x[3 * i], dy = x[3 * j + 1] - x[3 * i + 1], dz = x[3 * j + 2] - x[3 * i + 2];
-      double r2 = dx * dx + dy * dy + dz * dz, r = sqrt(r2), ir3 = 1.0 / (r2 * r);
-      a[3 * i] += 1.0 * m[j] * dx * ir3; a[3 * i + 1] += 1.0 * m[j] * dy * ir3; a[3 * i + 2] += 1.0 * m[j] * dz * ir3;
-      a[3 * j] -= 1.0 * m[i] * dx * ir3; a[3 * j + 1] -= 1.0 * m[i] * dy * ir3; a[3 * j + 2] -= 1.0 * m[i] * dz * ir3;
-    }
-}
 
-static void nbody_step(thorin_planets *sys, double dt)
-{
-  const int n = sys->nb + 1;
-  std::vector<double> m(n), x(3 * n), v(3 * n), k1x(3 * n), k1v(3 * n), xt(3 * n), ax(3 * n), sx(3 * n), sv(3 * n);
-  m[0] = 1.0;
-  for (int c = 0; c < 3; c++) { x[c] = 0.0; v[c] = 0.0; }
-  for (int k = 0; k < sys->nb; k++) {
-    m[k + 1] = sys->mass[k];
-    x[3 * k + 3] = sys->x[k]; x[3 * k + 4] = sys->y[k]; x[3 * k + 5] = sys->z[k];
-    v[3 * k + 3] = sys->vx[k]; v[3 * k + 4] = sys->vy[k]; v[3 * k + 5] = sys->vz[k];
-  }
-  double M = 0, cx[3] = {0, 0, 0}, cv[3] = {0, 0, 0};
-  for (int i = 0; i < n; i++) {
-    M += m[i];
-    for (int c = 0; c < 3; c++) { cx[c] += m[i] * x[3 * i + c]; cv[c] += m[i] * v[3 * i + c]; }
-  }
-  for (int i = 0; i < n; i++)
-    for (int c = 0; c < 3; c++) { x[3 * i + c] -= cx[c] / M; v[3 * i + c] -= cv[c] / M; }
-  const int nsteps = 256;
-  const double h = dt / nsteps;
-  static const double wts[4] = {1.0, 2.0, 2.0, 1.0}, cs[4] = {0.0, 0.5, 0.5, 1.0};
-  for (int s = 0; s < nsteps; s++) {
-    for (int q = 0; q < 3 * n; q++) { sx[q] = 0; sv[q] = 0; k1x[q] = 0; k1v[q] = 0; }
-    for (int stage = 0; stage < 4; stage++) {
-      for (int q = 0; q < 3 * n; q++) xt[q] = x[q] + cs[stage] * h * k1x[q];
-      nbody_accel(n, m.data(), xt.data(), ax.data());
-      for (int q = 0; q < 3 * n; q++) {
-        double vx = v[q] + cs[stage] * h * k1v[q];
-        k1x[q] = vx; k1v[q] = ax[q];
-        sx[q] += wts[stage] * k1x[q]; sv[q] += wts[stage] * k1v[q];
-      }
-    }
-    for (int q = 0; q < 3 * n; q++) { x[q] += h / 6.0 * sx[q]; v[q] += h / 6.0 * sv[q]; }
-  }
-  for (int k = 0; k < sys->nb; k++) {
-    sys->x[k] = x[3 * k + 3] - x[0]; sys->y[k] = x[3 * k + 4] - x[1]; sys->z[k] = x[3 * k + 5] - x[2];
-    sys->vx[k] = v[3 * k + 3] - v[0]; sys->vy[k] = v[3 * k + 4] - v[1]; sys->vz[k] = v[3 * k + 5] - v[2];
-  }
-}
 
-static double min_step_for_rebound(const thorin_planets *sys)   // ReboundInterface.c:360-385
-{
-  double dt = 1.e30;
-  for (int i = 0; i < sys->nb; i++)
-    for (int j = i + 1; j < sys->nb; j++) {
-      double dx = sys->x[i] - sys->x[j], dy = sys->y[i] - sys->y[j], dz = sys->z[i] - sys->z[j];
-      double dvx = sys->vx[i] - sys->vx[j], dvy = sys->vy[i] - sys->vy[j], dvz = sys->vz[i] - sys->vz[j];
-      double r2 = dx * dx + dy * dy + dz * dz, rv = dx * dvx + dy * dvy + dz * dvz;
-      double dtnew = fabs(r2 / rv);
-      if (dtnew < dt) dt = dtnew;
-    }
-  dt *= 0.25;
-  dt *= dt;
-  return 1.0 / dt;
-}
 
-static void rotate_psys(thorin_planets *sys, double angle)      // Psys.c:336-355
-{
-  double sint = sin(angle), cost = cos(angle);
-  for (int k = 0; k < sys->nb; k++) {
-    double xt = sys->x[k], yt = sys->y[k];
-    sys->x[k] = xt * cost + yt * sint; sys->y[k] = -xt * sint + yt * cost;
-    xt = sys->vx[k]; yt = sys->vy[k];
-    sys->vx[k] = xt * cost + yt * sint; sys->vy[k] = -xt * sint + yt * cost;
-  }
-}
 
 extern "C" int thorin_planet_from_elements(thorin_planets *sys, int k, float mass, float gas, float solid, float a,
                                            float e, float inc, float Omega, float omega, float f)
@@ -1193,21 +1155,34 @@ static void set_ctl(thorin_disk *d, std::initializer_list<std::pair<int, double>
 
 // ---------------------------------------------------------------------------
 // Substep pieces
-extern "C" int thorin_gpu_cfl(thorin_disk *d, double dt_remaining, double invdtreb_sq, int *n_sub)
+// ConditionCFL's fixed arguments (the interval and the rebound rate are in
+// the control block).
+static CflFinal cfl_args(const thorin_disk *d)
 {
   const thorin_params &p = d->p;
-  if (p.pebbles) aux_stokes(d->g, d->rho, d->psize, d->tau, d->s);       // PebbleStokesNumbers
   CflFinal f;
   memset(&f, 0, sizeof(f));
   f.pebbles = p.pebbles && !d->sloppy_pass && !p.sloppy_cfl;   // SloppyCFL: CriticalCharTime is never called (rate 0)
   f.first_call = d->cfl_first;
-  set_ctl(d, {{CTL_DELTAT, dt_remaining}, {CTL_INVDTREB, invdtreb_sq}});
   f.minimum_step = p.minimum_step;
   f.maximum_step = p.maximum_step;
   f.first_step = p.first_step;
   f.twopi_cfl_ns = 2.0 * H_PI * 0.5 / (double)d->ns;
+  return f;
+}
+
+static void cfl_launches(thorin_disk *d)
+{
+  const thorin_params &p = d->p;
+  if (p.pebbles) aux_stokes(d->g, d->rho, d->psize, d->tau, d->s);       // PebbleStokesNumbers
   aux_cfl(d->g, d->vrad, d->vtheta, d->cs, d->pvrad, d->pvtheta, d->cfl, p.pebbles, p.fast_transport,
-          (p.viscosity_alpha || p.viscosity != 0.0), d->partials, f, d->scal, d->iscal, d->s);
+          (p.viscosity_alpha || p.viscosity != 0.0), d->partials, cfl_args(d), d->scal, d->iscal, d->s);
+}
+
+extern "C" int thorin_gpu_cfl(thorin_disk *d, double dt_remaining, double invdtreb_sq, int *n_sub)
+{
+  set_ctl(d, {{CTL_DELTAT, dt_remaining}, {CTL_INVDTREB, invdtreb_sq}});
+  cfl_launches(d);
   d->cfl_first = 0;
   KCHECK("cfl kernels");
   CUCHK(cudaMemcpyAsync(d->iscal_h, d->iscal, sizeof(int) * IS_COUNT, cudaMemcpyDeviceToHost, d->s));
@@ -1224,44 +1199,21 @@ extern "C" int thorin_gpu_stokes(thorin_disk *d)
   return THORIN_OK;
 }
 
-static int ring_of(const thorin_disk *d, double r)         // "while (Rsup[i] < r) i++"
-{
-  int i = 0;
-  while (i < d->nr - 1 && d->Rsup[i] < r) i++;
-  return i;
-}
 
-static double global_ifrac(const thorin_disk *d, double r)  // GetGlobalIFrac, LowTasks.c:21-31
+
+static int ring_of(const thorin_disk *d, double r) { return pl_ring_of(d->Rsup.data(), d->nr, r); }
+static double global_ifrac(const thorin_disk *d, double r) { return pl_global_ifrac(d->GlobalRmed.data(), d->nr, r); }
+static void heating1(thorin_disk *d, double Mp, double dMp, double Xp, double Yp, double dt, int k)
 {
-  int i = 0;
-  if (r < d->GlobalRmed[0]) return 0.0;
-  if (r > d->GlobalRmed[d->nr - 1]) return (double)d->nr - 1.0;
-  while (d->GlobalRmed[i] <= r) i++;
-  return (double)i + (r - d->GlobalRmed[i - 1]) / (d->GlobalRmed[i] - d->GlobalRmed[i - 1]) - 1.0;
+  int idx;
+  double add;
+  if (pl_heating1(d->plc, d->Rsup.data(), d->Surf.data(), d->PhysicalTime, Mp, dMp, Xp, Yp, dt, &idx, &add)) {
+    d->heatsrc_index[k] = idx;
+    d->heatsrc[k] += add;
+  }
 }
 
 // Heating1 (Planet.c:222-247): accretion luminosity into the planet's cell.
-static void heating1(thorin_disk *d, double Mp, double dMp, double Xp, double Yp, double dt, int k)
-{
-  const thorin_params &p = d->p;
-  const int nr = d->nr, ns = d->ns;
-  const double Rperp = sqrt(Xp * Xp + Yp * Yp);
-  if (Rperp < d->Rinf[0] || Rperp > d->Rsup[nr - 1]) return;
-  const double tdelay = 4.0 * p.dt * (double)p.heating_delay;
-  double taper = d->PhysicalTime / tdelay;
-  if (taper > 1.0) taper = 1.0;
-  const double plrho = p.planetary_density / RHO2CGS;
-  const double plradius = pow(3.0 * Mp / (4.0 * H_PI * plrho), 1.0 / 3.0);
-  const double L = Mp * dMp / dt / plradius;
-  double ang = atan2(Yp, Xp);
-  if (ang < 0.0) ang += 2.0 * H_PI;
-  int i = 0;
-  while (d->Rsup[i] < Rperp) i++;
-  int j = (int)floor((double)ns / 2.0 / H_PI * ang + 0.5);
-  if (j == ns) j = 0;
-  d->heatsrc_index[k] = j + i * ns;
-  d->heatsrc[k] += L * taper / d->Surf[i];
-}
 
 extern "C" int thorin_gpu_accrete(thorin_disk *d, thorin_planets *sys, double dt)
 {
@@ -1329,26 +1281,9 @@ extern "C" int thorin_gpu_accrete(thorin_disk *d, thorin_planets *sys, double dt
     a.vt = d->vtheta;
     a.part = d->partials;
     a.acc = d->scal + 64;
-    a.Xp = sys->x[k]; a.Yp = sys->y[k]; a.Zp = sys->z[k];
-    a.VXp = sys->vx[k]; a.VYp = sys->vy[k]; a.VZp = sys->vz[k];
-    a.Mp = sys->mass[k];
-    double Rp = a.Xp * a.Xp + a.Yp * a.Yp;
-    const double Rp3D = sqrt(Rp + a.Zp * a.Zp);
-    Rp = sqrt(Rp);
-    a.Rp = Rp;
-    a.Rhill = Rp3D * pow(1.0 / 3.0 * a.Mp, 1.0 / 3.0);
-    a.Omegap = pow(Rp, -1.5);
-    a.Rp15 = pow(Rp, 1.5);
-    const double ifrac = global_ifrac(d, Rp);
-    a.frac = ifrac - floor(ifrac);
-    a.iflow = (int)ifrac;
-    a.omega_frame = d->OmegaFrame;
-    a.dt = dt;
-    a.pebble_alpha = p.pebble_alpha;
-    int imax = d->nr - 1, imin = 0;
-    while (d->Rinf[imax] > (Rp + a.Rhill) && imax >= imin) imax--;
-    while (d->Rsup[imin] < (Rp - a.Rhill) && imin <= imax) imin++;
-    a.imin = imin; a.imax = imax;
+    pl_pebble_acc_prep(d->plc, d->Rinf.data(), d->Rsup.data(), d->GlobalRmed.data(), sys, k, d->OmegaFrame, dt,
+                       ACC_BX, &a);
+    const int imin = a.imin, imax = a.imax;
     double dMp = 0, dPx = 0, dPy = 0;
     if (imin <= imax) {
       aux_accrete(d->g, a, d->acc_args_d, d->scal, d->s);
@@ -1358,15 +1293,28 @@ extern "C" int thorin_gpu_accrete(thorin_disk *d, thorin_planets *sys, double dt
       dMp = d->scal_h[SC_ACC_DM]; dPx = d->scal_h[SC_ACC_DPX]; dPy = d->scal_h[SC_ACC_DPY];
     }
     if (p.accret_heating) heating1(d, a.Mp, dMp, a.Xp, a.Yp, dt, k);
-    double PX = a.VXp * a.Mp + dPx, PY = a.VYp * a.Mp + dPy, M = a.Mp + dMp;
-    sys->mass[k] = M;
-    sys->solid[k] = sys->solid[k] + dMp;
-    sys->vx[k] = PX / M;
-    sys->vy[k] = PY / M;
+    pl_pebble_acc_finish(sys, k, a, dMp, dPx, dPy);
   }
   if (p.evaporation_rate > 0.0)                                    // EvaporatePebbles
     aux_evaporate(d->g, d->temper, d->pdens, d->s);
   return THORIN_OK;
+}
+
+// FillForcesArrays' fixed arguments for npl planets (their constants are in
+// d->planets_d, the mass taper and the planets' indirect term in the
+// control block).
+static ForceArgs force_args(const thorin_disk *d, int npl)
+{
+  const thorin_params &p = d->p;
+  ForceArgs a;
+  a.rho = d->rho; a.cs = d->cs; a.tau = d->tau; a.pdens = d->pdens;
+  a.agr = d->agr; a.agt = d->agt; a.pagr = d->pagr; a.pagt = d->pagt;
+  a.part = d->partials;
+  a.pl = d->planets_d;
+  a.npl = npl; a.pebbles = p.pebbles; a.exclude_hill = p.exclude_hill; a.pebble_gravity = p.pebble_gravity;
+  a.pebble_alpha = p.pebble_alpha; a.hillcut = p.hillcut;
+  a.sqrt_pebble_alpha = sqrt(p.pebble_alpha);
+  return a;
 }
 
 extern "C" int thorin_gpu_forces(thorin_disk *d, thorin_planets *sys, double mass_taper, double indirect[2],
@@ -1378,51 +1326,12 @@ extern "C" int thorin_gpu_forces(thorin_disk *d, thorin_planets *sys, double mas
   DevPlanet pl[MAXPL_DEV];
   double axs = 0.0, ays = 0.0;
   CUCHK(cudaStreamSynchronize(d->s));        // csmean_h is current
-  for (int k = 0; k < npl; k++) {
-    const double xpl = sys->x[k], ypl = sys->y[k], zpl = sys->z[k];
-    double mpl = sys->mass[k];
-    const double dpl = sqrt(xpl * xpl + ypl * ypl + zpl * zpl);
-    DevPlanet &P = pl[k];
-    P.x = xpl; P.y = ypl; P.z = zpl; P.m = mpl;
-    P.rhill = dpl * pow((1.0 / 3.0 * mpl), 1.0 / 3.0);
-    // ThicknessSmoothing (Force.c:75-102): ring-mean c_s at the planet's ring
-    double smoothing = 0.0;
-    const double r = sqrt(xpl * xpl + ypl * ypl);
-    if (r >= d->Rinf[0] && r <= d->Rsup[d->nr - 1]) {
-      const int i = ring_of(d, r);
-      smoothing = p.thickness_smoothing * (d->csmean_h[i] * d->OmegaInv[i] * (1.0 / sqrt(p.adiabind)));
-    }
-    P.Hpl = smoothing / p.thickness_smoothing;
-    P.smoothing2 = smoothing * smoothing;
-    const double rst = 0.5 * P.rhill;
-    P.rst2 = rst * rst; P.rst3 = P.rst2 * rst; P.rst4 = P.rst3 * rst;
-    const double rsm = 0.05 * P.rhill;
-    P.rsm2 = rsm * rsm;
-    P.rmorevert2 = 2.0 * P.rhill;
-    P.rmorevert2 *= P.rmorevert2;
-    P.near_h2 = 10.0 * P.Hpl;
-    P.near_h2 *= P.near_h2;
-    P.near_hill2 = 5.0 * P.rhill;
-    P.near_hill2 *= P.near_hill2;
-    if (p.indirect_term) {
-      const double invdpl3 = 1.0 / (dpl * dpl * dpl);
-      mpl *= mass_taper;
-      axs += mpl * invdpl3 * xpl;
-      ays += mpl * invdpl3 * ypl;
-    }
-  }
+  for (int k = 0; k < npl; k++)
+    pl_force_planet(d->plc, d->Rsup.data(), d->csmean_h, d->OmegaInv.data(), sys, k, mass_taper, &pl[k], &axs, &ays);
   if (npl > 0) CUCHK(cudaMemcpyAsync(d->planets_d, pl, npl * sizeof(DevPlanet), cudaMemcpyHostToDevice, d->s));
-  ForceArgs a;
-  a.rho = d->rho; a.cs = d->cs; a.tau = d->tau; a.pdens = d->pdens;
-  a.agr = d->agr; a.agt = d->agt; a.pagr = d->pagr; a.pagt = d->pagt;
-  a.part = d->partials;
-  a.pl = d->planets_d;
-  a.npl = npl; a.pebbles = p.pebbles; a.exclude_hill = p.exclude_hill; a.pebble_gravity = p.pebble_gravity;
-  a.pebble_alpha = p.pebble_alpha; a.hillcut = p.hillcut;
-  a.sqrt_pebble_alpha = sqrt(p.pebble_alpha);
   const double indx_pl = p.indirect_term ? -axs : 0.0, indy_pl = p.indirect_term ? -ays : 0.0;
   set_ctl(d, {{CTL_MASS_TAPER, mass_taper}, {CTL_INDX_PL, indx_pl}, {CTL_INDY_PL, indy_pl}});
-  aux_forces(d->g, a, d->fr, d->scal, d->s);
+  aux_forces(d->g, force_args(d, npl), d->fr, d->scal, d->s);
   KCHECK("force kernels");
   // DampingTW04 needs the ring means of Sigma (and c_s) at each planet
   for (int k = 0; k < npl; k++) {
@@ -1643,6 +1552,8 @@ static int iterate_relaxation(thorin_disk *d)
 
 // SubStep3 + ImplicitRadiativeDiffusion (SourceEuler.c:508-586,
 // EnergySources.c:201-335).  Leaves the new energy in d->energy.
+static int capture_sor(thorin_disk *d);
+
 static int energy_step(thorin_disk *d, double dt)
 {
   const thorin_params &p = d->p;
@@ -1667,7 +1578,9 @@ static int energy_step(thorin_disk *d, double dt)
     hydro_irradiation(d->g, d->rho, d->cs, d->opacity, d->flaring, d->qirr, d->rstar, d->tirr4fac, p.opacity_drop,
                       d->taueff_c, d->ring[R_RINF15], d->ring[R_RSUP15], d->s);
   int nheat = 0;
-  if (p.accret_heating || p.gas_accret_heating) {
+  if (d->capturing) {
+    nheat = d->capS.accret_heating ? d->capS.npl : 0;      // written on the device by the accretion step
+  } else if (p.accret_heating || p.gas_accret_heating) {
     nheat = d->heatsrc_max;
     if (nheat > 0) {
       CUCHK(cudaMemcpyAsync(d->heat_idx_d, d->heatsrc_index, nheat * sizeof(int), cudaMemcpyHostToDevice, d->s));
@@ -1678,6 +1591,12 @@ static int energy_step(thorin_disk *d, double dt)
                d->mljp, d->mljm, d->rhs, d->gm1, d->ring[R_INVDXTHETA2], p.stellar_irradiation, nheat,
                d->heat_idx_d, d->heat_val_d, d->s);
   KCHECK("energy kernels");
+  if (d->capturing) {                  // device-resident DT: schedule, solve loop and counters on the device
+    RCHK(capture_sor(d));
+    hydro_energy_from_t(d->g, d->rho, d->temper, d->energy_new, d->s);
+    std::swap(d->energy, d->energy_new);
+    return THORIN_OK;
+  }
   if (d->sor_first) {
     d->sor_first = 0;
     RCHK(iterate_relaxation(d));
@@ -1731,7 +1650,7 @@ static void transport_fluid(thorin_disk *d, double **rho, double *vr, double *vt
 extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
 {
   const thorin_params &p = d->p;
-  set_ctl(d, {{CTL_DT, dt}, {CTL_OMEGA_FRAME, d->OmegaFrame}});
+  if (!d->capturing) set_ctl(d, {{CTL_DT, dt}, {CTL_OMEGA_FRAME, d->OmegaFrame}});
   const int damp = p.damping;
   auto boundary = [&]() {                // ApplyBoundaryCondition (SideEuler.c:490-503)
     if (p.open_inner) aux_open_inner(d->g, d->rho, d->vrad, d->energy, p.energy_eq, p.damp_flux, p.gasflux, d->s);
@@ -1800,7 +1719,8 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
   }
   // Transport, ApplyBoundaryCondition, ComputeTemperatureField, ComputeSoundSpeed
   transport_fluid(d, &d->rho, d->vrad, d->vtheta, p.energy_eq ? &d->energy : nullptr, &d->t_rho_gas, dt, 1, d->ts, d->s);
-  CUCHK(cudaMemcpyAsync(d->nshift_h.data(), d->nshift, d->nr * sizeof(int), cudaMemcpyDeviceToHost, d->s));
+  if (!d->capturing)
+    CUCHK(cudaMemcpyAsync(d->nshift_h.data(), d->nshift, d->nr * sizeof(int), cudaMemcpyDeviceToHost, d->s));
   if ((damp && !p.damp_vrad) || p.open_inner || p.open_outer || p.non_reflecting || p.outer_source_mass) {
     // damping towards INIT / GASFLUX changes Sigma (and e): the boundary
     // call, then ComputeTemperatureField and ComputeSoundSpeed
@@ -1811,9 +1731,11 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
   aux_ring_mean(d->g, d->cs, d->ring[R_CSMEAN], d->s);
   if (p.alpha_flock) aux_ring_mean(d->g, d->temper, d->ring[R_TEMPMEAN], d->s);
   aux_viscosity_rings(d->g, d->vp, d->s);
-  CUCHK(cudaMemcpyAsync(d->csmean_h, d->ring[R_CSMEAN], d->nr * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  if (!d->capturing)
+    CUCHK(cudaMemcpyAsync(d->csmean_h, d->ring[R_CSMEAN], d->nr * sizeof(double), cudaMemcpyDeviceToHost, d->s));
   if (p.pebbles) CUCHK(cudaStreamWaitEvent(d->s, d->ev_join, 0));     // join the pebble transport
   KCHECK("hydro kernels");
+  if (d->capturing) return status;     // clock and crash flag stay on the device
   CUCHK(cudaMemcpyAsync(d->iscal_h + IS_CRASH, d->iscal + IS_CRASH, sizeof(int), cudaMemcpyDeviceToHost, d->s));
   d->PhysicalTime += dt;
   d->st.last_dt = dt;
@@ -1824,21 +1746,7 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
 static void advance_from_disk(thorin_disk *d, thorin_planets *sys, double dt, const double ind[2], const double *rrho,
                               const double *rcs)
 {
-  for (int k = 0; k < sys->nb; k++) {
-    if (!sys->feel_disk[k]) continue;
-    const double x = sys->x[k], y = sys->y[k], z = sys->z[k], vz = sys->vz[k], m = sys->mass[k];
-    double damp = 0.0;
-    const double r = sqrt(x * x + y * y);
-    if ((d->p.vertical_damping > 0.0) && (r >= d->Rinf[0] && r <= d->Rsup[d->nr - 1])) {
-      const double cs4inv = pow(rcs[k], -4.0), Omega = pow(r, -1.5);
-      damp = d->p.vertical_damping * m * rrho[k] * Omega * cs4inv * (-2.176 * vz - 0.871 * z * Omega);
-    }
-    sys->vx[k] += dt * sys->ax[k];
-    sys->vy[k] += dt * sys->ay[k];
-    sys->vz[k] += dt * (sys->az[k] + damp);
-    sys->vx[k] += dt * ind[0];
-    sys->vy[k] += dt * ind[1];
-  }
+  pl_advance_from_disk(d->plc, sys, dt, ind, rrho, rcs);
 }
 
 extern "C" int thorin_advance_from_disk(const thorin_disk *d, thorin_planets *sys, double dt, const double indirect[2],
@@ -1980,10 +1888,9 @@ extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
     dt = DT / (double)n;
   }
   while (dtemp < 0.999999999 * DT) {
-    d->MassTaper = d->PhysicalTime / (p.mass_taper * 2.0 * H_MPI);
-    d->MassTaper = (d->MassTaper > 1.0 ? 1.0 : pow(sin(d->MassTaper * H_MPI / 2.0), 2.0));
+    d->MassTaper = pl_mass_taper(d->PhysicalTime, p.mass_taper);
     if (!p.sloppy_cfl) {
-      const double invdtreb_sq = min_step_for_rebound(sys);
+      const double invdtreb_sq = pl_min_step_for_rebound(sys);
       int n;
       RCHK(thorin_gpu_cfl(d, DT - dtemp, invdtreb_sq, &n));
       dt = (DT - dtemp) / (double)n;
@@ -1998,7 +1905,7 @@ extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
     RCHK(thorin_gpu_forces(d, sys, d->MassTaper, ind, rrho, rcs));
     advance_from_disk(d, sys, dt, ind, rrho, rcs);
     if (p.aerodynamic_drag) RCHK(thorin_gpu_drag(d, sys, dt));
-    nbody_step(sys, dt);
+    pl_nbody_step(sys, dt);
     if (p.corotating) {
       // GetPsysInfo (GET): the angle planet 0 (or its guiding centre) moved
       // through; the frame follows it and the azimuthal velocities are
@@ -2013,7 +1920,7 @@ extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
       if (p.pebbles) aux_correct_vtheta(d->g, d->pvtheta, domega, d->s);
       d->OmegaFrame = OmegaNew;
     }
-    rotate_psys(sys, d->OmegaFrame * dt);
+    pl_rotate(sys, d->OmegaFrame * dt);
     int s = thorin_gpu_hydro(d, dt);
     if (s != THORIN_OK && s != THORIN_ERR_SOR_MAXIT) return s;
     if (s != THORIN_OK) status = s;
@@ -2030,6 +1937,328 @@ extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
   d->st.crashed = d->iscal_h[IS_CRASH];
   d->st.kernel_launches = g_thorin_launches.load();
   return status;
+}
+
+// ---------------------------------------------------------------------------
+// Device-resident DT: one CUDA graph per disk runs a whole DT of AlgoGas.
+//
+//   [k_g_dt_begin] -> WHILE(h_sub) {  one substep:
+//       k_g_sub_begin, Stokes numbers, CFL (dt into the control block),
+//       InitHeating, per planet: accretion set-up, v_theta ring means,
+//       accretion kernels, Heating1 + planet update; evaporation,
+//       force constants, FillForcesArrays, DampingTW04 ring means,
+//       planet kick + N-body step + rotation,
+//       the hydro substep of the host path (pebble transport on a parallel
+//       branch) with the SOR solve as   k_g_sor_begin, residual,
+//       WHILE(h_sor) { sweeps }, k_g_sor_end,
+//       copies that put the state back into the buffers the next run of the
+//       body reads, k_g_sub_end (clock, counters, loop condition)  }
+//
+// The launches are the host path's own, captured with the control block in
+// place of host values.  Pointer swaps of the host path (ActualiseGas, the
+// transport's output buffers) would change buffers between runs of the loop
+// body, so the body ends by copying each state field back into the buffer it
+// started in.  The first DT of a disk (omega calibration) runs on the host
+// path; planets are kept on the device for the DT.
+
+// Inserts the SOR sweep loop into the capture: the omega schedule, the start
+// residual, a WHILE node whose body (captured later into d->capS) holds the
+// sweeps, then the counters.
+static int capture_sor(thorin_disk *d)
+{
+  StepDev &S = d->capS;
+  graph_sor_begin(S, d->s);
+  hydro_sor_resid0(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, d->sor, d->s);
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t cg;
+  const cudaGraphNode_t *deps = nullptr;
+  const cudaGraphEdgeData *edges = nullptr;
+  size_t ndeps = 0;
+  CUCHK(cudaStreamGetCaptureInfo(d->s, &cs, nullptr, &cg, &deps, &edges, &ndeps));
+  if (cs != cudaStreamCaptureStatusActive) { g_last_error = "SOR loop outside a capture"; return THORIN_ERR_STATE; }
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = S.h_sor;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  CUCHK(cudaGraphAddNode(&node, cg, deps, edges, ndeps, &np));
+  d->capture_sor_body = np.conditional.phGraph_out[0];
+  CUCHK(cudaStreamUpdateCaptureDependencies(d->s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  graph_sor_end(S, d->s);
+  return THORIN_OK;
+}
+
+// Inserts a WHILE node with handle h into the capture of stream s; returns
+// its body graph.
+static int capture_while(cudaStream_t s, cudaGraphConditionalHandle h, cudaGraph_t *body)
+{
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t cg;
+  const cudaGraphNode_t *deps = nullptr;
+  const cudaGraphEdgeData *edges = nullptr;
+  size_t ndeps = 0;
+  CUCHK(cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, &edges, &ndeps));
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  CUCHK(cudaGraphAddNode(&node, cg, deps, edges, ndeps, &np));
+  *body = np.conditional.phGraph_out[0];
+  CUCHK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  return THORIN_OK;
+}
+
+// The launches of one substep (the loop body), on d->s.
+static int capture_substep(thorin_disk *d)
+{
+  const thorin_params &p = d->p;
+  StepDev &S = d->capS;
+  const int npl = S.npl;
+  graph_sub_begin(S, d->s);
+  cfl_launches(d);
+  if (p.pebbles) {
+    graph_acc_init(S, d->s);
+    const int nb_max = aux_accrete_blocks(d->g, 0, d->nr - 1);
+    for (int k = 0; k < npl; k++) {
+      graph_acc_prep(S, k, d->s);
+      graph_ring_means_at(d->g, d->vtheta, d->scal + 64 + 4, d->ring_info_d, 0, 1, d->s);
+      aux_accrete_kernels(d->g, d->acc_args_d, nb_max, d->scal, d->s);
+      graph_acc_finish(S, k, d->s);
+    }
+    if (p.evaporation_rate > 0.0) aux_evaporate(d->g, d->temper, d->pdens, d->s);
+  }
+  graph_force_prep(S, d->s);
+  aux_forces(d->g, force_args(d, npl), d->fr, d->scal, d->s);
+  for (int k = 0; k < npl; k++)
+    graph_ring_means_at(d->g, d->rho, d->scal + SC_PLANET_A + 2 * MAXPL_DEV + k, d->ring_info_d, 2 + k, 0, d->s);
+  graph_planet_step(S, d->s);
+  // the hydro substep, with the buffers' roles restored at the end
+  double *const f0[5] = {d->rho, d->vrad, d->vtheta, d->energy, d->pdens};
+  double *const sc0[6] = {d->vrad_new, d->vtheta_new, d->energy_new, d->t_rho_gas, d->t_e_gas, d->t_rho_peb};
+  const int rc = thorin_gpu_hydro(d, 0.0);
+  double *f1[5] = {d->rho, d->vrad, d->vtheta, d->energy, d->pdens};
+  const size_t bytes = d->fsize * sizeof(double);
+  for (int q = 0; q < 5; q++)
+    if (f1[q] && f1[q] != f0[q]) CUCHK(cudaMemcpyAsync(f0[q], f1[q], bytes, cudaMemcpyDeviceToDevice, d->s));
+  d->rho = f0[0]; d->vrad = f0[1]; d->vtheta = f0[2]; d->energy = f0[3]; d->pdens = f0[4];
+  d->vrad_new = sc0[0]; d->vtheta_new = sc0[1]; d->energy_new = sc0[2];
+  d->t_rho_gas = sc0[3]; d->t_e_gas = sc0[4]; d->t_rho_peb = sc0[5];
+  if (rc != THORIN_OK) return rc;
+  graph_sub_end(S, d->s);
+  KCHECK("device-resident substep");
+  return THORIN_OK;
+}
+
+// Options the device-resident DT covers; the others stay on the host path.
+static const char *graph_unsupported(const thorin_disk *d, const thorin_planets *sys)
+{
+  const thorin_params &p = d->p;
+  if (p.sloppy_cfl) return "SloppyCFL";
+  if (p.corotating) return "corotating frames";
+  if (p.accretion_rate > 0.0) return "gas accretion onto planets";
+  if (p.prescribed_accretion) return "ParametricAccretion";
+  if (p.aerodynamic_drag) return "AerodynamicDrag";
+  if (!p.energy_eq || p.parametric_cooling) return "runs without SOR radiative diffusion";
+  if (d->ws_net) return "the learned SOR warm start";
+  if (d->sor_direct) return "THORIN_SOR_DIRECT";
+  if (sys->nb > MAXPL_DEV) return "more than 8 planets";
+  return nullptr;
+}
+
+static int build_dt_graph(thorin_disk *d, int npl)
+{
+  const thorin_params &p = d->p;
+  if (d->dt_graph) { cudaGraphExecDestroy(d->dt_graph); d->dt_graph = nullptr; }
+  if (!d->sys_d) {
+    RCHK(dalloc(d, (void **)&d->sys_d, sizeof(thorin_planets)));
+    RCHK(dalloc(d, (void **)&d->gst_d, sizeof(GraphStats)));
+    RCHK(dalloc(d, (void **)&d->ring_info_d, (2 + MAXPL_DEV) * sizeof(int)));
+    CUCHK(cudaMallocHost((void **)&d->sys_h, sizeof(thorin_planets)));
+    CUCHK(cudaMallocHost((void **)&d->gst_h, sizeof(GraphStats)));
+    CUCHK(cudaMallocHost((void **)&d->ctl_h, CTL_COUNT * sizeof(double)));
+  }
+  // the accretion arguments' device pointers (the scalars are set per planet)
+  AccArgs a;
+  memset(&a, 0, sizeof(a));
+  a.pdens = d->pdens; a.macc = d->macc; a.pvr = d->pvrad; a.pvt = d->pvtheta; a.tau = d->tau; a.cs = d->cs;
+  a.vt = d->vtheta;
+  a.part = d->partials;
+  a.acc = d->scal + 64;
+  CUCHK(cudaMemcpyAsync(d->acc_args_d, &a, sizeof(a), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  StepDev &S = d->capS;
+  S.g = d->g; S.c = d->plc; S.sys = d->sys_d; S.scal = d->scal; S.iscal = d->iscal; S.acc = d->acc_args_d;
+  S.ring_info = d->ring_info_d; S.pl = d->planets_d; S.heat_idx = d->heat_idx_d; S.heat_val = d->heat_val_d;
+  S.st = d->gst_d; S.sor = d->sor; S.DT = p.dt; S.evaporation_rate = p.evaporation_rate; S.npl = npl;
+  S.pebbles = p.pebbles; S.accret_heating = p.pebbles && p.accret_heating; S.indirect_term = p.indirect_term;
+  cudaGraph_t G = nullptr, body = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int rc = THORIN_OK;
+  cudaError_t e = cudaGraphCreate(&G, 0);
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&S.h_sub, G, 1u, cudaGraphCondAssignDefault);
+  // top level: counters, then the substep loop
+  if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(d->s, G, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    graph_dt_begin(S, d->s);
+    rc = capture_while(d->s, S.h_sub, &body);
+    cudaGraph_t tmp;
+    const cudaError_t e2 = cudaStreamEndCapture(d->s, &tmp);
+    if (rc == THORIN_OK && e2 != cudaSuccess) e = e2;
+  }
+  // the substep body, with the SOR loop's node inside it
+  if (e == cudaSuccess && rc == THORIN_OK) e = cudaGraphConditionalHandleCreate(&S.h_sor, body, 1u, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess && rc == THORIN_OK) e = cudaStreamBeginCaptureToGraph(d->s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess && rc == THORIN_OK) {
+    d->capturing = 1;
+    d->capture_sor_body = nullptr;
+    rc = capture_substep(d);
+    d->capturing = 0;
+    cudaGraph_t tmp;
+    const cudaError_t e2 = cudaStreamEndCapture(d->s, &tmp);
+    if (rc == THORIN_OK && e2 != cudaSuccess) e = e2;
+    if (rc == THORIN_OK && e == cudaSuccess && !d->capture_sor_body) { g_last_error = "no SOR loop in the substep"; rc = THORIN_ERR_STATE; }
+  }
+  // the sweeps inside the SOR loop
+  if (e == cudaSuccess && rc == THORIN_OK) e = cudaStreamBeginCaptureToGraph(d->s, d->capture_sor_body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess && rc == THORIN_OK) {
+    SorCtl c = d->sor;
+    c.cond = S.h_sor;
+    c.has_cond = 1;
+    hydro_sor_sweeps(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, c, p.sor_eps,
+                     d->sor_loop_k, p.sor_maxiters, d->s);
+    cudaGraph_t tmp;
+    e = cudaStreamEndCapture(d->s, &tmp);
+  }
+  if (e == cudaSuccess && rc == THORIN_OK) e = cudaGraphInstantiate(&exec, G, 0);
+  if (G) cudaGraphDestroy(G);
+  cudaGetLastError();
+  if (rc != THORIN_OK) return rc;
+  if (e != cudaSuccess) {
+    g_last_error = std::string("device-resident DT graph: ") + cudaGetErrorString(e);
+    return THORIN_ERR_CUDA;
+  }
+  d->dt_graph = exec;
+  d->graph_npl = npl;
+  return THORIN_OK;
+}
+
+// Uploads what the graph reads (planets, clock, frame, omega schedule) and
+// launches one DT on the disk's stream; thorin_gpu_graph_finish reads back.
+static int graph_launch(thorin_disk *d, const thorin_planets *sys)
+{
+  if (!d->dt_graph || d->graph_npl != sys->nb) RCHK(build_dt_graph(d, sys->nb));
+  *d->sys_h = *sys;
+  CUCHK(cudaMemcpyAsync(d->sys_d, d->sys_h, sizeof(thorin_planets), cudaMemcpyHostToDevice, d->s));
+  set_ctl(d, {{CTL_TIME, d->PhysicalTime}, {CTL_OMEGA_FRAME, d->OmegaFrame}, {CTL_SOR_OMEGA, d->omega},
+              {CTL_SOR_DOMEGA, d->domega}});
+  d->gst_h->niterlast = d->Niterlast;
+  CUCHK(cudaMemcpyAsync(&d->gst_d->niterlast, &d->gst_h->niterlast, sizeof(int), cudaMemcpyHostToDevice, d->s));
+  if (d->timing) CUCHK(cudaEventRecord(d->ev[2], d->s));
+  CUCHK(cudaGraphLaunch(d->dt_graph, d->s));
+  if (d->timing) CUCHK(cudaEventRecord(d->ev[3], d->s));
+  CUCHK(cudaMemcpyAsync(d->sys_h, d->sys_d, sizeof(thorin_planets), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaMemcpyAsync(d->gst_h, d->gst_d, sizeof(GraphStats), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaMemcpyAsync(d->ctl_h, d->ctl, CTL_COUNT * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaMemcpyAsync(d->nshift_h.data(), d->nshift, d->nr * sizeof(int), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaMemcpyAsync(d->csmean_h, d->ring[R_CSMEAN], d->nr * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  return THORIN_OK;
+}
+
+static int graph_finish(thorin_disk *d, thorin_planets *sys)
+{
+  CUCHK(cudaStreamSynchronize(d->s));
+  const GraphStats &g = *d->gst_h;
+  *sys = *d->sys_h;
+  d->PhysicalTime = d->ctl_h[CTL_TIME];
+  d->omega = d->ctl_h[CTL_SOR_OMEGA];
+  d->domega = d->ctl_h[CTL_SOR_DOMEGA];
+  d->Niterlast = g.niterlast;
+  d->MassTaper = d->ctl_h[CTL_MASS_TAPER];
+  d->st.substeps = g.nsub;
+  d->st.crashed = g.crashed;
+  d->st.sor_calls += g.sor_calls;
+  d->st.sor_sweeps += g.sor_sweeps;
+  if (g.sor_calls) { d->st.sor_last_niter = g.sor_last_niter; d->st.sor_omega = g.omega_used; }
+  d->st.last_dt = d->ctl_h[CTL_DT];
+  d->st.kernel_launches = g_thorin_launches.load();
+  if (d->timing) {
+    float ms = 0.f;
+    CUCHK(cudaEventElapsedTime(&ms, d->ev[2], d->ev[3]));
+    d->st.step_time_ms = ms;
+  }
+  if (g.error == 1) { g_last_error = "SOR loop ended without an exit decision"; return THORIN_ERR_CUDA; }
+  if (g.error == 2) { g_last_error = "substep bound of the device-resident DT reached"; return THORIN_ERR_STATE; }
+  if (g.error == 3) { g_last_error = "non-positive substep length"; return THORIN_ERR_STATE; }
+  return g.capped ? THORIN_ERR_SOR_MAXIT : THORIN_OK;
+}
+
+extern "C" int thorin_gpu_set_launch_shape(thorin_disk *d, int sor_loop_sweeps, int sor_threads_per_sm)
+{
+  if (!d || sor_loop_sweeps < 1 || sor_loop_sweeps > 64 || sor_threads_per_sm < 128 || sor_threads_per_sm > 2048 ||
+      sor_threads_per_sm % 128) {
+    g_last_error = "launch shape: 1..64 sweeps per loop body, 128..2048 SOR threads per SM in steps of 128";
+    return THORIN_ERR_ARG;
+  }
+  CUCHK(cudaStreamSynchronize(d->s));
+  d->sor_loop_k = sor_loop_sweeps;
+  d->g.sor_tpsm = sor_threads_per_sm;
+  if (d->sor_loop) { cudaGraphExecDestroy(d->sor_loop); d->sor_loop = nullptr; }
+  if (d->dt_graph) { cudaGraphExecDestroy(d->dt_graph); d->dt_graph = nullptr; }
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_get_launch_shape(thorin_disk *d, int *sor_loop_sweeps, int *sor_threads_per_sm)
+{
+  if (!d || !sor_loop_sweeps || !sor_threads_per_sm) return THORIN_ERR_ARG;
+  *sor_loop_sweeps = d->sor_loop_k;
+  *sor_threads_per_sm = d->g.sor_tpsm;
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_graph_supported(thorin_disk *d, const thorin_planets *sys)
+{
+  if (!d || !sys) return THORIN_ERR_ARG;
+  const char *why = graph_unsupported(d, sys);
+  if (why) { g_last_error = std::string("device-resident DT: not with ") + why; return THORIN_ERR_ARG; }
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_algogas_graph(thorin_disk *d, thorin_planets *sys)
+{
+  RCHK(thorin_gpu_graph_supported(d, sys));
+  // the first DT calibrates omega and takes the first CFL on the host path
+  if (d->sor_first || d->cfl_first) return thorin_gpu_algogas(d, sys);
+  RCHK(graph_launch(d, sys));
+  return graph_finish(d, sys);
+}
+
+// One DT of n disks: every disk's graph is launched on its own stream before
+// the first is waited for, so the disks run side by side on the GPU.
+extern "C" int thorin_ensemble_algogas_graph(thorin_disk **disks, thorin_planets **systems, int n, int *status)
+{
+  if (!disks || !systems || n < 1) return THORIN_ERR_ARG;
+  for (int k = 0; k < n; k++)
+    if (!disks[k] || !systems[k]) return THORIN_ERR_ARG;
+  int worst = THORIN_OK;
+  std::vector<int> launched(n, 0);
+  for (int k = 0; k < n; k++) {
+    thorin_disk *d = disks[k];
+    int rc = thorin_gpu_graph_supported(d, systems[k]);
+    if (rc == THORIN_OK && (d->sor_first || d->cfl_first)) rc = thorin_gpu_algogas(d, systems[k]);
+    else if (rc == THORIN_OK) { rc = graph_launch(d, systems[k]); launched[k] = (rc == THORIN_OK); }
+    if (status) status[k] = rc;
+    if (rc != THORIN_OK && rc != THORIN_ERR_SOR_MAXIT) worst = rc;
+  }
+  for (int k = 0; k < n; k++) {
+    if (!launched[k]) continue;
+    const int rc = graph_finish(disks[k], systems[k]);
+    if (status) status[k] = rc;
+    if (rc != THORIN_OK && rc != THORIN_ERR_SOR_MAXIT) worst = rc;
+  }
+  return worst;
 }
 
 extern "C" int thorin_gpu_get_sor_state(thorin_disk *d, double *omega, double *domega, int *niterlast, int *calibrated)

@@ -81,6 +81,7 @@ struct DevGrid {
   DevRings r;
   DevConst k;
   double *ctl;                           // control block (CTL_*), CTL_COUNT doubles
+  int sor_tpsm;                          // SOR pass: resident threads per multiprocessor (0: 1536)
 };
 
 __device__ __forceinline__ int jp_of(int j, int ns) { return (j == ns - 1) ? 0 : j + 1; }

@@ -4,6 +4,7 @@
 #include "thorin_dev.cuh"
 
 #define MAXPL_DEV 8            // planets handled by the force kernel (per-thread arrays)
+#define ACC_BX 256             // threads per block of the pebble accretion kernels
 
 // Planet data seen by the kernels (per-planet constants from the host).
 struct DevPlanet {

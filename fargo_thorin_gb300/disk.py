@@ -82,6 +82,23 @@ class GpuDisk:
     def algogas(self, sys_: ThorinPlanets) -> int:
         return _lib.check(self.L.thorin_gpu_algogas(self.h, C.byref(sys_)), "thorin_gpu_algogas", ok=(0, 4))
 
+    def algogas_graph(self, sys_: ThorinPlanets) -> int:
+        """One DT as a single CUDA graph launch (the disk's first DT runs
+        through algogas, which calibrates the SOR omega)."""
+        return _lib.check(self.L.thorin_gpu_algogas_graph(self.h, C.byref(sys_)), "thorin_gpu_algogas_graph",
+                          ok=(0, 4))
+
+    def graph_supported(self, sys_: ThorinPlanets) -> bool:
+        return self.L.thorin_gpu_graph_supported(self.h, C.byref(sys_)) == 0
+
+    def set_launch_shape(self, sor_loop_sweeps: int, sor_threads_per_sm: int):
+        _lib.check(self.L.thorin_gpu_set_launch_shape(self.h, sor_loop_sweeps, sor_threads_per_sm), "set_launch_shape")
+
+    def launch_shape(self):
+        a, b = C.c_int(), C.c_int()
+        _lib.check(self.L.thorin_gpu_get_launch_shape(self.h, C.byref(a), C.byref(b)), "get_launch_shape")
+        return a.value, b.value
+
     def integrals(self):
         vals = [C.c_double() for _ in range(5)]
         _lib.check(self.L.thorin_gpu_integrals(self.h, *[C.byref(v) for v in vals]), "integrals")

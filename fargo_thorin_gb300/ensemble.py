@@ -112,6 +112,15 @@ class Ensemble:
         _lib.check(rc, "thorin_ensemble_algogas")
         return list(st)
 
+    def step_graph(self) -> list:
+        """One DT of every disk, each as one device-resident DT graph, all
+        launched before any is waited for; returns the status codes."""
+        n = len(self.disks)
+        st = (C.c_int * n)()
+        rc = self.L.thorin_ensemble_algogas_graph(self._dp, self._sp, n, st)
+        _lib.check(rc, "thorin_ensemble_algogas_graph", ok=(0, 4))
+        return list(st)
+
     def tune(self, max_workers: int = 16, ndt: int = 1) -> dict:
         """Time every schedule (worker counts 1, 2, 4, ... in both orders) on
         real DTs and return the fastest.  Each schedule runs on the next DTs,

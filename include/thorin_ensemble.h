@@ -41,6 +41,13 @@ int thorin_ensemble_algogas(thorin_disk *const *disks, thorin_planets *const *sy
 int thorin_ensemble_tune(thorin_disk *const *disks, thorin_planets *const *systems, int n, int max_workers, int ndt,
                          int *best_workers, int *best_order, double *best_ms_per_dt, double *sequential_ms_per_dt);
 
+/* One DT of every disk as device-resident DT graphs (thorin_gpu_algogas_graph),
+ * all launched on the disks' own streams from the calling thread before any
+ * is waited for, so that the disks run side by side with no host round trip
+ * inside the DT.  A disk's first DT runs on the host path (omega
+ * calibration).  status[k] as for thorin_ensemble_algogas. */
+int thorin_ensemble_algogas_graph(thorin_disk **disks, thorin_planets **systems, int n, int *status);
+
 #ifdef __cplusplus
 }
 #endif

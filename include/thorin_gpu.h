@@ -293,6 +293,30 @@ int thorin_gpu_correct_vtheta(thorin_disk *d, double domega);
  * REBOUND's IAS15, ReboundInterface.c:262-325).  sys is updated in place. */
 int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys);
 
+/* The same DT as one CUDA graph launch: the substep loop, the planet side
+ * (accretion, forces, kick, N-body step) and the SOR omega schedule run on
+ * the device, with no host round trip inside the DT.  The disk's first DT
+ * (the omega calibration) runs as thorin_gpu_algogas.  Covers fixed frames,
+ * SOR radiative diffusion, pebbles, pebble accretion with heating, all
+ * boundaries and opacity laws; other options are rejected with
+ * THORIN_ERR_ARG (thorin_gpu_graph_supported says which).  No torque log
+ * records are made.  The graph is built at the first call for the current
+ * number of planets. */
+int thorin_gpu_algogas_graph(thorin_disk *d, thorin_planets *sys);
+
+/* THORIN_OK if thorin_gpu_algogas_graph covers this disk and system, else
+ * THORIN_ERR_ARG with the reason in thorin_gpu_last_error(). */
+int thorin_gpu_graph_supported(thorin_disk *d, const thorin_planets *sys);
+
+/* Launch shape of the SOR sweeps (no counterpart in the reference): sweeps
+ * per run of the sweep loop's body (1..64, default 8) and the resident
+ * threads per multiprocessor of a colour pass (128..2048 in steps of 128,
+ * default 1536).  Results do not depend on either; the ensemble autotuner
+ * picks them per disk size.  The disk's graphs are rebuilt at their next
+ * use. */
+int thorin_gpu_set_launch_shape(thorin_disk *d, int sor_loop_sweeps, int sor_threads_per_sm);
+int thorin_gpu_get_launch_shape(thorin_disk *d, int *sor_loop_sweeps, int *sor_threads_per_sm);
+
 /* Conservation integrals (SideEuler.c:26-80,523-565), summed on the device. */
 int thorin_gpu_integrals(thorin_disk *d, double *mass, double *momentum,
                          double *energy, double *peb_mass, double *peb_momentum);
