@@ -153,6 +153,8 @@ struct thorin_disk {
   int capturing = 0;                 // launches are being captured into the DT graph
   StepDev capS;
   cudaGraph_t capture_sor_body = nullptr;   // body of the SOR loop node, filled after the substep capture
+  cudaStream_t s_pl = nullptr;       // the planet step's branch of the substep graph
+  cudaEvent_t ev_pl_fork = nullptr, ev_pl_join = nullptr;
   AccArgs *acc_args_d;               // pebble accretion arguments on the device
   SorCtl sor;
   CflRings cfl;
@@ -635,6 +637,12 @@ extern "C" int thorin_gpu_destroy(thorin_disk *d)
   if (d->sys_h) cudaFreeHost(d->sys_h);
   if (d->gst_h) cudaFreeHost(d->gst_h);
   if (d->ctl_h) cudaFreeHost(d->ctl_h);
+  if (d->s_pl) {
+    cudaStreamSynchronize(d->s_pl);
+    cudaEventDestroy(d->ev_pl_fork);
+    cudaEventDestroy(d->ev_pl_join);
+    cudaStreamDestroy(d->s_pl);
+  }
   for (int q = 0; q < 4; q++) cudaEventDestroy(d->ev[q]);
   if (d->s_peb) {
     cudaStreamSynchronize(d->s_peb);
@@ -1947,7 +1955,7 @@ extern "C" int thorin_gpu_algogas(thorin_disk *d, thorin_planets *sys)
 //       InitHeating, per planet: accretion set-up, v_theta ring means,
 //       accretion kernels, Heating1 + planet update; evaporation,
 //       force constants, FillForcesArrays, DampingTW04 ring means,
-//       planet kick + N-body step + rotation,
+//       planet kick + N-body step + rotation (a branch beside the hydro),
 //       the hydro substep of the host path (pebble transport on a parallel
 //       branch) with the SOR solve as   k_g_sor_begin, residual,
 //       WHILE(h_sor) { sweeps }, k_g_sor_end,
@@ -2034,7 +2042,12 @@ static int capture_substep(thorin_disk *d)
   aux_forces(d->g, force_args(d, npl), d->fr, d->scal, d->s);
   for (int k = 0; k < npl; k++)
     graph_ring_means_at(d->g, d->rho, d->scal + SC_PLANET_A + 2 * MAXPL_DEV + k, d->ring_info_d, 2 + k, 0, d->s);
-  graph_planet_step(S, d->s);
+  // the planet kick and N-body step run beside the hydro substep, which does
+  // not read the planets; the next substep's CFL waits for them
+  CUCHK(cudaEventRecord(d->ev_pl_fork, d->s));
+  CUCHK(cudaStreamWaitEvent(d->s_pl, d->ev_pl_fork, 0));
+  graph_planet_step(S, d->s_pl);
+  CUCHK(cudaEventRecord(d->ev_pl_join, d->s_pl));
   // the hydro substep, with the buffers' roles restored at the end
   double *const f0[5] = {d->rho, d->vrad, d->vtheta, d->energy, d->pdens};
   double *const sc0[6] = {d->vrad_new, d->vtheta_new, d->energy_new, d->t_rho_gas, d->t_e_gas, d->t_rho_peb};
@@ -2046,6 +2059,7 @@ static int capture_substep(thorin_disk *d)
   d->rho = f0[0]; d->vrad = f0[1]; d->vtheta = f0[2]; d->energy = f0[3]; d->pdens = f0[4];
   d->vrad_new = sc0[0]; d->vtheta_new = sc0[1]; d->energy_new = sc0[2];
   d->t_rho_gas = sc0[3]; d->t_e_gas = sc0[4]; d->t_rho_peb = sc0[5];
+  CUCHK(cudaStreamWaitEvent(d->s, d->ev_pl_join, 0));
   if (rc != THORIN_OK) return rc;
   graph_sub_end(S, d->s);
   KCHECK("device-resident substep");
@@ -2079,6 +2093,9 @@ static int build_dt_graph(thorin_disk *d, int npl)
     CUCHK(cudaMallocHost((void **)&d->sys_h, sizeof(thorin_planets)));
     CUCHK(cudaMallocHost((void **)&d->gst_h, sizeof(GraphStats)));
     CUCHK(cudaMallocHost((void **)&d->ctl_h, CTL_COUNT * sizeof(double)));
+    CUCHK(cudaStreamCreateWithFlags(&d->s_pl, cudaStreamNonBlocking));
+    CUCHK(cudaEventCreateWithFlags(&d->ev_pl_fork, cudaEventDisableTiming));
+    CUCHK(cudaEventCreateWithFlags(&d->ev_pl_join, cudaEventDisableTiming));
   }
   // the accretion arguments' device pointers (the scalars are set per planet)
   AccArgs a;

@@ -78,11 +78,19 @@ PL_HD double pl_min_step_for_rebound(const thorin_planets *sys)
 // over dt (classical RK4 with 256 substeps), back to heliocentric.
 #define PL_NMAX (MAXPL_DEV + 1)
 
-PL_HD void pl_nbody_accel(int n, const double *m, const double *x, double *a)
+// Bodies 0..N-1 (0 the star) with compile-time N: the loops unroll fully, so
+// that on the device the state stays in registers (a one-thread kernel with
+// its arrays in local memory spends most of its time waiting on loads).  The
+// host path runs the same template, so the arithmetic and its order agree.
+template <int N>
+PL_HD void pl_nbody_accel_n(const double *m, const double *x, double *a)
 {
-  for (int i = 0; i < 3 * n; i++) a[i] = 0.0;
-  for (int i = 0; i < n; i++)
-    for (int j = i + 1; j < n; j++) {
+#pragma unroll
+  for (int i = 0; i < 3 * N; i++) a[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < N; i++)
+#pragma unroll
+    for (int j = i + 1; j < N; j++) {
       double dx = x[3 * j] - x[3 * i], dy = x[3 * j + 1] - x[3 * i + 1], dz = x[3 * j + 2] - x[3 * i + 2];
       double r2 = dx * dx + dy * dy + dz * dz, r = sqrt(r2), ir3 = 1.0 / (r2 * r);
       a[3 * i] += 1.0 * m[j] * dx * ir3; a[3 * i + 1] += 1.0 * m[j] * dy * ir3; a[3 * i + 2] += 1.0 * m[j] * dz * ir3;
@@ -90,44 +98,71 @@ PL_HD void pl_nbody_accel(int n, const double *m, const double *x, double *a)
     }
 }
 
-PL_HD void pl_nbody_step(thorin_planets *sys, double dt)
+template <int N>
+PL_HD void pl_nbody_step_n(thorin_planets *sys, double dt)
 {
-  const int n = sys->nb + 1;
-  double m[PL_NMAX], x[3 * PL_NMAX], v[3 * PL_NMAX], k1x[3 * PL_NMAX], k1v[3 * PL_NMAX], xt[3 * PL_NMAX];
-  double ax[3 * PL_NMAX], sx[3 * PL_NMAX], sv[3 * PL_NMAX];
+  double m[N], x[3 * N], v[3 * N], k1x[3 * N], k1v[3 * N], xt[3 * N], ax[3 * N], sx[3 * N], sv[3 * N];
   m[0] = 1.0;
+#pragma unroll
   for (int c = 0; c < 3; c++) { x[c] = 0.0; v[c] = 0.0; }
-  for (int k = 0; k < sys->nb; k++) {
+#pragma unroll
+  for (int k = 0; k < N - 1; k++) {
     m[k + 1] = sys->mass[k];
     x[3 * k + 3] = sys->x[k]; x[3 * k + 4] = sys->y[k]; x[3 * k + 5] = sys->z[k];
     v[3 * k + 3] = sys->vx[k]; v[3 * k + 4] = sys->vy[k]; v[3 * k + 5] = sys->vz[k];
   }
   double M = 0, cx[3] = {0, 0, 0}, cv[3] = {0, 0, 0};
-  for (int i = 0; i < n; i++) {
+#pragma unroll
+  for (int i = 0; i < N; i++) {
     M += m[i];
+#pragma unroll
     for (int c = 0; c < 3; c++) { cx[c] += m[i] * x[3 * i + c]; cv[c] += m[i] * v[3 * i + c]; }
   }
-  for (int i = 0; i < n; i++)
+#pragma unroll
+  for (int i = 0; i < N; i++)
+#pragma unroll
     for (int c = 0; c < 3; c++) { x[3 * i + c] -= cx[c] / M; v[3 * i + c] -= cv[c] / M; }
   const int nsteps = 256;
   const double h = dt / nsteps;
   const double wts[4] = {1.0, 2.0, 2.0, 1.0}, cs[4] = {0.0, 0.5, 0.5, 1.0};
   for (int s = 0; s < nsteps; s++) {
-    for (int q = 0; q < 3 * n; q++) { sx[q] = 0; sv[q] = 0; k1x[q] = 0; k1v[q] = 0; }
+#pragma unroll
+    for (int q = 0; q < 3 * N; q++) { sx[q] = 0; sv[q] = 0; k1x[q] = 0; k1v[q] = 0; }
+#pragma unroll
     for (int stage = 0; stage < 4; stage++) {
-      for (int q = 0; q < 3 * n; q++) xt[q] = x[q] + cs[stage] * h * k1x[q];
-      pl_nbody_accel(n, m, xt, ax);
-      for (int q = 0; q < 3 * n; q++) {
+#pragma unroll
+      for (int q = 0; q < 3 * N; q++) xt[q] = x[q] + cs[stage] * h * k1x[q];
+      pl_nbody_accel_n<N>(m, xt, ax);
+#pragma unroll
+      for (int q = 0; q < 3 * N; q++) {
         double vx = v[q] + cs[stage] * h * k1v[q];
         k1x[q] = vx; k1v[q] = ax[q];
         sx[q] += wts[stage] * k1x[q]; sv[q] += wts[stage] * k1v[q];
       }
     }
-    for (int q = 0; q < 3 * n; q++) { x[q] += h / 6.0 * sx[q]; v[q] += h / 6.0 * sv[q]; }
+#pragma unroll
+    for (int q = 0; q < 3 * N; q++) { x[q] += h / 6.0 * sx[q]; v[q] += h / 6.0 * sv[q]; }
   }
-  for (int k = 0; k < sys->nb; k++) {
+#pragma unroll
+  for (int k = 0; k < N - 1; k++) {
     sys->x[k] = x[3 * k + 3] - x[0]; sys->y[k] = x[3 * k + 4] - x[1]; sys->z[k] = x[3 * k + 5] - x[2];
     sys->vx[k] = v[3 * k + 3] - v[0]; sys->vy[k] = v[3 * k + 4] - v[1]; sys->vz[k] = v[3 * k + 5] - v[2];
+  }
+}
+
+// The N-body step for the star and sys->nb (at most MAXPL_DEV) planets.
+PL_HD void pl_nbody_step(thorin_planets *sys, double dt)
+{
+  switch (sys->nb) {
+  case 0: break;
+  case 1: pl_nbody_step_n<2>(sys, dt); break;
+  case 2: pl_nbody_step_n<3>(sys, dt); break;
+  case 3: pl_nbody_step_n<4>(sys, dt); break;
+  case 4: pl_nbody_step_n<5>(sys, dt); break;
+  case 5: pl_nbody_step_n<6>(sys, dt); break;
+  case 6: pl_nbody_step_n<7>(sys, dt); break;
+  case 7: pl_nbody_step_n<8>(sys, dt); break;
+  default: pl_nbody_step_n<9>(sys, dt); break;
   }
 }
 
