@@ -202,49 +202,40 @@ def warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, steps, stream, barr
             "threshold": "eps * L1 residual of the previous-temperature start, as the plain solve"}
 
 
-def ensemble_phase(n=16, seed=0, ndt=2, settle=3):
-    """A drawn ensemble of n gas + pebble + embryo disks of uneven sizes
-    (Nrad in {128 .. 512}, Nsec = 3 Nrad).  After each disk's first DT (with
-    the omega calibration) and `settle` more DTs past the initial transient,
-    the autotuner picks the schedule.  Then the same ndt DTs, from one
-    snapshot of every disk, run with that schedule and with the disks one
-    after the other: aggregate cell-updates/s and the speed-up on identical
-    work (the substeps and SOR sweeps of both runs are checked equal)."""
-    import torch
-    from fargo_thorin_gb300.ensemble import Ensemble, GIVEN, LARGEST
+def ensemble_phase(n=64, seed=0, ndt=2, settle=3):
+    """The batched ensemble: n drawn gas + pebble + embryo disks of uneven
+    sizes (Nrad in {128, 192, 256, 384, 512}, Nsec = 3 Nrad; alpha, Sigma0,
+    h and the embryo mass drawn per disk).  After each disk's first DT (the
+    omega calibration) and `settle` DTs as device-resident DT graphs, the
+    autotuner picks the schedule (graph mode or a host thread pool, then the
+    SOR launch shape per disk size) on one DT from a snapshot of every disk.
+    The same ndt DTs from that snapshot then run with the chosen schedule
+    and with the disks one after the other on the host path: aggregate
+    cell-updates/s and the speed-up on identical work (the substeps and SOR
+    sweeps of both runs are checked equal)."""
+    from fargo_thorin_gb300.ensemble import Ensemble
     ens = Ensemble.drawn(n, seed=seed)           # each disk has done its first DT
     for _ in range(settle):
-        ens.step(n, LARGEST)
-    tune = ens.tune(max_workers=16, ndt=1)
-    snaps = [({f: d.get(f) for f in SNAPSHOT_FIELDS}, d.sor_state(), d.stats().physical_time, s.copy())
-             for d, s in zip(ens.disks, ens.systems)]
-
-    def run(workers, order):
-        for d, s, (fields, sor, t, sy) in zip(ens.disks, ens.systems, snaps):
-            for f, v in fields.items():
-                d.upload(f, v)
-            d.set_sor_state(*sor[:3])
-            d.set_time(t)
-            C.memmove(C.byref(s), C.byref(sy), C.sizeof(s))
-        sw0 = sum(d.stats().sor_sweeps for d in ens.disks)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        upd = 0
-        for _ in range(ndt):
-            ens.step(workers, order)
-            upd += sum(d.nr * d.ns * d.stats().substeps for d in ens.disks)
-        torch.cuda.synchronize()
-        return time.perf_counter() - t0, upd, sum(d.stats().sor_sweeps for d in ens.disks) - sw0
-
-    sec, upd, sweeps = run(tune["workers"], tune["order_code"])
-    sec1, upd1, sweeps1 = run(1, GIVEN)
+        ens.step_graph()
+    snaps = ens.snapshot()
+    tune = ens.tune_schedule(snaps)
+    ens.restore(snaps)
+    best = ens.run_schedule(tune["schedule"], ndt)
+    ens.restore(snaps)
+    seq = ens.run_schedule({"mode": "sequential"}, ndt)
+    sched = tune["schedule"]
     sizes = sorted(d.nr for d in ens.disks)
-    out = {"disks": n, "nrad": sizes, "cells": ens.cells, "workers": tune["workers"], "order": tune["order"],
-           "value": upd / sec, "unit": UNIT, "ms_per_dt": 1e3 * sec / ndt,
-           "sequential_ms_per_dt": 1e3 * sec1 / ndt, "speedup_vs_sequential": sec1 / sec,
-           "same_work": bool(upd == upd1 and sweeps == sweeps1), "settle_dts": settle,
-           "schedule": "one host worker thread per concurrent disk, per-disk streams, autotuned worker count and order",
-           "timing": "wall clock with a device synchronisation on both sides; both runs replay the same DTs "
+    out = {"disks": len(ens.disks), "nrad": sizes, "cells": ens.cells,
+           "schedule": {"mode": sched["mode"], "workers": sched.get("workers"),
+                        "sor_launch_shapes": {str(k): list(v) for k, v in sched.get("shapes", {}).items()}},
+           "value": best["cell_updates"] / best["seconds"], "unit": UNIT, "ms_per_dt": 1e3 * best["seconds"] / ndt,
+           "sequential_ms_per_dt": 1e3 * seq["seconds"] / ndt,
+           "speedup_vs_sequential": seq["seconds"] / best["seconds"],
+           "same_work": bool(best["cell_updates"] == seq["cell_updates"] and best["sweeps"] == seq["sweeps"]),
+           "settle_dts": settle, "tuner_trials": tune["trials"],
+           "graph": "one CUDA graph per disk and DT (substep loop, planet side and SOR schedule on the device), "
+                    "all disks launched on their own streams before any is waited for",
+           "timing": "wall clock with a device synchronisation on both sides; every run replays the same DTs "
                      "from one snapshot of every disk"}
     ens.close()
     return out
@@ -544,7 +535,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-ensemble", action="store_true", help="skip the 16-disk ensemble measurement")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-disk ensemble measurement")
     ap.add_argument("--profile", action="store_true",
                     help="run --steps DTs inside cuProfilerStart/Stop for ncu; prints no bench line")
     ap.add_argument("--grid", type=int, nargs=2, metavar=("NRAD", "NSEC"), default=(NR, NS),

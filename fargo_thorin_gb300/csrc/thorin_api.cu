@@ -165,7 +165,7 @@ struct thorin_disk {
   // host ring arrays
   std::vector<double> Radii, GlobalRmed, Rinf, Rsup, Rmed, Surf, InvRmed, InvSurf, InvDiffRmed, InvDiffRsup, InvRinf,
       OmegaInv, Rmed2, WaveKiller, SigmaMed, SigmaInf, EnergyMed, VthetaMed, PebDensInit, PebVradInit, PebVthetaInit;
-  std::vector<int> nshift_h;
+  int *nshift_h = nullptr;           // pinned: the per-substep copy must not block the host
   int ndamp;
   // scalars carried between substeps (static variables in the reference)
   double PhysicalTime, PhysicalTimeInitial, OmegaFrame, MassTaper;
@@ -574,7 +574,8 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   for (int q = 0; q < 4; q++) CUCHK(cudaEventCreate(&d->ev[q]));
   d->timing = 0;
   CUCHK(cudaStreamSynchronize(d->s));
-  d->nshift_h.assign(d->nr, 0);
+  CUCHK(cudaMallocHost((void **)&d->nshift_h, (size_t)d->nr * sizeof(int)));
+  memset(d->nshift_h, 0, (size_t)d->nr * sizeof(int));
   *out = d;
   return THORIN_OK;
 }
@@ -632,6 +633,7 @@ extern "C" int thorin_gpu_destroy(thorin_disk *d)
   cudaFreeHost(d->scal_h);
   cudaFreeHost(d->iscal_h);
   cudaFreeHost(d->csmean_h);
+  if (d->nshift_h) cudaFreeHost(d->nshift_h);
   if (d->sor_loop) cudaGraphExecDestroy(d->sor_loop);
   if (d->dt_graph) cudaGraphExecDestroy(d->dt_graph);
   if (d->sys_h) cudaFreeHost(d->sys_h);
@@ -763,6 +765,8 @@ extern "C" int thorin_gpu_set_time(thorin_disk *d, double t)
 
 extern "C" int thorin_gpu_get_nshift(thorin_disk *d, int *host)
 {
+  if (!d || !host) return THORIN_ERR_ARG;
+  CUCHK(cudaStreamSynchronize(d->s));      // the last transport's copy has landed
   for (int i = 0; i < d->nr; i++) host[i] = d->nshift_h[i];
   return THORIN_OK;
 }
@@ -1728,7 +1732,7 @@ extern "C" int thorin_gpu_hydro(thorin_disk *d, double dt)
   // Transport, ApplyBoundaryCondition, ComputeTemperatureField, ComputeSoundSpeed
   transport_fluid(d, &d->rho, d->vrad, d->vtheta, p.energy_eq ? &d->energy : nullptr, &d->t_rho_gas, dt, 1, d->ts, d->s);
   if (!d->capturing)
-    CUCHK(cudaMemcpyAsync(d->nshift_h.data(), d->nshift, d->nr * sizeof(int), cudaMemcpyDeviceToHost, d->s));
+    CUCHK(cudaMemcpyAsync(d->nshift_h, d->nshift, d->nr * sizeof(int), cudaMemcpyDeviceToHost, d->s));
   if ((damp && !p.damp_vrad) || p.open_inner || p.open_outer || p.non_reflecting || p.outer_source_mass) {
     // damping towards INIT / GASFLUX changes Sigma (and e): the boundary
     // call, then ComputeTemperatureField and ComputeSoundSpeed
@@ -2179,7 +2183,7 @@ static int graph_launch(thorin_disk *d, const thorin_planets *sys)
   CUCHK(cudaMemcpyAsync(d->sys_h, d->sys_d, sizeof(thorin_planets), cudaMemcpyDeviceToHost, d->s));
   CUCHK(cudaMemcpyAsync(d->gst_h, d->gst_d, sizeof(GraphStats), cudaMemcpyDeviceToHost, d->s));
   CUCHK(cudaMemcpyAsync(d->ctl_h, d->ctl, CTL_COUNT * sizeof(double), cudaMemcpyDeviceToHost, d->s));
-  CUCHK(cudaMemcpyAsync(d->nshift_h.data(), d->nshift, d->nr * sizeof(int), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaMemcpyAsync(d->nshift_h, d->nshift, d->nr * sizeof(int), cudaMemcpyDeviceToHost, d->s));
   CUCHK(cudaMemcpyAsync(d->csmean_h, d->ring[R_CSMEAN], d->nr * sizeof(double), cudaMemcpyDeviceToHost, d->s));
   return THORIN_OK;
 }

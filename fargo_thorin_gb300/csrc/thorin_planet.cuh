@@ -30,22 +30,46 @@ struct PlConst {
   int indirect_term, accret_heating, feel_disk_any;
 };
 
+// The reference finds rings by linear scans ("while (Rsup[i] < r) i++").  On
+// the increasing ring radii a bisection finds the same index; in a
+// one-thread device kernel it takes log2(nr) dependent loads instead of up
+// to nr.
+
+// First i in [lo, hi) with a[i] >= r (hi if none); a increasing.
+PL_HD int pl_first_ge(const double *a, int lo, int hi, double r)
+{
+  while (lo < hi) {
+    const int mid = lo + (hi - lo) / 2;
+    if (a[mid] < r) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// First i in [lo, hi) with a[i] > r (hi if none); a increasing.
+PL_HD int pl_first_gt(const double *a, int lo, int hi, double r)
+{
+  while (lo < hi) {
+    const int mid = lo + (hi - lo) / 2;
+    if (a[mid] <= r) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
 // "while (Rsup[i] < r) i++", bounded at the last ring (ThicknessSmoothing's
 // and DampingTW04's ring search).
 PL_HD int pl_ring_of(const double *Rsup, int nr, double r)
 {
-  int i = 0;
-  while (i < nr - 1 && Rsup[i] < r) i++;
-  return i;
+  return pl_first_ge(Rsup, 0, nr - 1, r);
 }
 
 // GetGlobalIFrac (LowTasks.c:21-31) on the cell-centre radii.
 PL_HD double pl_global_ifrac(const double *Rmed, int nr, double r)
 {
-  int i = 0;
   if (r < Rmed[0]) return 0.0;
   if (r > Rmed[nr - 1]) return (double)nr - 1.0;
-  while (Rmed[i] <= r) i++;
+  const int i = pl_first_gt(Rmed, 0, nr, r);            // "while (Rmed[i] <= r) i++"
   return (double)i + (r - Rmed[i - 1]) / (Rmed[i] - Rmed[i - 1]) - 1.0;
 }
 
@@ -215,8 +239,7 @@ PL_HD int pl_heating1(const PlConst &c, const double *Rsup, const double *Surf, 
   const double L = Mp * dMp / dt / plradius;
   double ang = atan2(Yp, Xp);
   if (ang < 0.0) ang += 2.0 * PL_PI;
-  int i = 0;
-  while (Rsup[i] < Rperp) i++;
+  const int i = pl_first_ge(Rsup, 0, c.nr, Rperp);        // "while (Rsup[i] < Rperp) i++"
   int j = (int)floor((double)ns / 2.0 / PL_PI * ang + 0.5);
   if (j == ns) j = 0;
   *idx = j + i * ns;
@@ -246,12 +269,12 @@ PL_HD void pl_pebble_acc_prep(const PlConst &c, const double *Rinf, const double
   a->omega_frame = omega_frame;
   a->dt = dt;
   a->pebble_alpha = c.pebble_alpha;
-  // the reference tests the radius before the bound (Pebbles.c:408-409) and
-  // so reads Rinf[-1] for a planet inside the inner edge; the bound comes
-  // first here, which changes nothing for a planet inside the disk
-  int imax = c.nr - 1, imin = 0;
-  while (imax >= imin && Rinf[imax] > (Rp + a->Rhill)) imax--;
-  while (imin <= imax && Rsup[imin] < (Rp - a->Rhill)) imin++;
+  // Pebbles.c:408-409: "while (Rinf[imax] > Rp + Rhill) imax--" from the
+  // last ring, then "while (Rsup[imin] < Rp - Rhill) imin++" from the first,
+  // not past imax (for a planet inside the inner edge the reference's scan
+  // reads Rinf[-1]; the bisection stops at imax = -1)
+  const int imax = pl_first_gt(Rinf, 0, c.nr, Rp + a->Rhill) - 1;
+  const int imin = pl_first_ge(Rsup, 0, imax + 1, Rp - a->Rhill);
   a->imin = imin; a->imax = imax;
   a->nb = (imin <= imax) ? ((imax - imin + 1) * c.ns + acc_bx - 1) / acc_bx : 0;
 }

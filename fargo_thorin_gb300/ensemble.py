@@ -24,6 +24,11 @@ EARTH = 3.0e-6
 GIVEN, LARGEST = 0, 1
 
 
+def _sync():
+    import torch
+    torch.cuda.synchronize()
+
+
 def draw(rng: np.random.Generator) -> dict:
     return {"nrad": int(rng.choice(SIZES)), "alpha": float(10.0 ** rng.uniform(-4.0, -2.0)),
             "sigma_scale": float(10.0 ** rng.uniform(np.log10(0.3), np.log10(3.0))),
@@ -133,6 +138,86 @@ class Ensemble:
                                                C.byref(bo), C.byref(bms), C.byref(sms)), "thorin_ensemble_tune")
         return {"workers": bw.value, "order": "largest first" if bo.value == LARGEST else "given",
                 "order_code": bo.value, "ms_per_dt": bms.value, "sequential_ms_per_dt": sms.value}
+
+    # -- snapshots and the schedule autotuner of the device-resident DTs --
+
+    SNAP_FIELDS = (0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 11)   # state, temperature, sound speed, Stokes number
+
+    def snapshot(self) -> list:
+        """Every disk's state, SOR schedule, clock and planets (host copies)."""
+        return [({f: d.get(f) for f in self.SNAP_FIELDS}, d.sor_state(), d.stats().physical_time, s.copy())
+                for d, s in zip(self.disks, self.systems)]
+
+    def restore(self, snaps: list):
+        for d, s, (fields, sor, t, sy) in zip(self.disks, self.systems, snaps):
+            for f, v in fields.items():
+                d.upload(f, v)
+            d.set_sor_state(*sor[:3])
+            d.set_time(t)
+            C.memmove(C.byref(s), C.byref(sy), C.sizeof(s))
+
+    def run_schedule(self, sched: dict, ndt: int = 1) -> dict:
+        """ndt DTs of the ensemble with a schedule: {"mode": "graph"} (every
+        disk one DT graph, all launched before any is waited for) or
+        {"mode": "pool", "workers": w} (host path on w threads, largest
+        first) or {"mode": "sequential"}; with sched["shapes"] = {nrad:
+        (sweeps per loop body, SOR threads per SM)} set first.  Wall time
+        with a device synchronisation on both sides."""
+        import time
+        for d in self.disks:
+            shape = sched.get("shapes", {}).get(d.nr, (8, 1536))
+            if d.launch_shape() != tuple(shape):
+                d.set_launch_shape(*shape)
+        sw0 = sum(d.stats().sor_sweeps for d in self.disks)
+        _sync()
+        t0 = time.perf_counter()
+        upd = 0
+        for _ in range(ndt):
+            if sched["mode"] == "graph":
+                self.step_graph()
+            elif sched["mode"] == "pool":
+                self.step(sched["workers"], LARGEST)
+            else:
+                self.step(1, GIVEN)
+            upd += sum(d.nr * d.ns * d.stats().substeps for d in self.disks)
+        _sync()
+        sec = time.perf_counter() - t0
+        return {"seconds": sec, "cell_updates": upd, "sweeps": sum(d.stats().sor_sweeps for d in self.disks) - sw0}
+
+    def tune_schedule(self, snaps: list, shapes=((8, 1536), (16, 1536), (8, 1024), (16, 2048)),
+                      pool_workers=(8, 16, 32)) -> dict:
+        """Autotuner: every candidate runs the same DT from the snapshot.
+        First the mode (graph, or a host thread pool of each worker count);
+        then, in graph mode, the SOR launch shape of each disk size in turn
+        (sweeps per run of the sweep loop, resident threads per SM of a
+        colour pass), keeping a size's best before the next size is tried.
+        Returns the schedule and the time of every candidate."""
+        trials = []
+
+        def time_of(sched):
+            self.restore(snaps)
+            r = self.run_schedule(sched)
+            trials.append({"schedule": {k: v for k, v in sched.items() if k != "shapes"},
+                           "shapes": {str(k): list(v) for k, v in sched.get("shapes", {}).items()},
+                           "ms": 1e3 * r["seconds"]})
+            return r["seconds"]
+
+        best = {"mode": "graph", "shapes": {}}
+        best_t = time_of(best)
+        for w in pool_workers:
+            cand = {"mode": "pool", "workers": w, "shapes": {}}
+            t = time_of(cand)
+            if t < best_t:
+                best, best_t = cand, t
+        if best["mode"] == "graph":
+            for nr in sorted({d.nr for d in self.disks}, reverse=True):
+                for shape in shapes[1:]:
+                    cand = {"mode": "graph", "shapes": dict(best["shapes"])}
+                    cand["shapes"][nr] = shape
+                    t = time_of(cand)
+                    if t < best_t:
+                        best, best_t = cand, t
+        return {"schedule": best, "ms_per_dt": 1e3 * best_t, "trials": trials}
 
     def substeps(self) -> int:
         return sum(d.stats().substeps for d in self.disks)

@@ -151,3 +151,29 @@ def test_ensemble_graph_matches_single_disks():
         one.close()
         for a, b in zip(together[k], alone):
             np.testing.assert_array_equal(a, b)
+
+
+def test_schedule_tuner_replays_identical_work():
+    """The autotuner times every candidate schedule on the same DT from a
+    snapshot; the chosen schedule and the sequential host path then do the
+    same substeps and SOR sweeps on the same DTs, and end with the same
+    fields to 1e-12."""
+    from fargo_thorin_gb300.ensemble import Ensemble
+    specs = [{"nrad": 32, "alpha": 1e-3, "sigma_scale": 1.0, "aspect": 0.05, "mplanet": 3e-5},
+             {"nrad": 48, "alpha": 3e-4, "sigma_scale": 2.0, "aspect": 0.04, "mplanet": 1e-5},
+             {"nrad": 64, "alpha": 1e-3, "sigma_scale": 1.0, "aspect": 0.05, "mplanet": 2e-5}]
+    ens = Ensemble(specs, seed=7)
+    ens.step(1)
+    snaps = ens.snapshot()
+    tune = ens.tune_schedule(snaps, shapes=((8, 1536), (4, 768)), pool_workers=(2,))
+    assert tune["schedule"]["mode"] in ("graph", "pool") and len(tune["trials"]) >= 2
+    ens.restore(snaps)
+    a = ens.run_schedule(tune["schedule"], 2)
+    fa = [d.get(0) for d in ens.disks]
+    ens.restore(snaps)
+    b = ens.run_schedule({"mode": "sequential"}, 2)
+    fb = [d.get(0) for d in ens.disks]
+    assert a["cell_updates"] == b["cell_updates"] and a["sweeps"] == b["sweeps"]
+    for x, y in zip(fa, fb):
+        assert H.rel_l2(x, y) < 1e-12
+    ens.close()
