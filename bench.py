@@ -170,6 +170,7 @@ def warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, steps, stream, barr
             d.upload(f, v)
         d.set_sor_state(*snap_sor[:3])
         d.set_time(snap_time)
+        d.refresh(4)                      # ring means of the restored c_s
         sys_ = snap_sys.copy()
         WS.attach(d, net, WS.PREDICT)
         st0, pred0 = d.stats(), WS.stats(d).predictions
@@ -306,6 +307,7 @@ def run_gpu(args):
         d.upload(f, v)
     d.set_sor_state(*snap_sor[:3])
     d.set_time(snap_time)
+    d.refresh(4)                          # ring means of the restored c_s
     sys_ = snap_sys.copy()
     sweeps_e0 = d.stats().sor_sweeps
     n = (NR + 1) * NS

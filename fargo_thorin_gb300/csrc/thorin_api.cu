@@ -1070,6 +1070,16 @@ extern "C" int thorin_gpu_refresh(thorin_disk *d, int flags)
 {
   const thorin_params &p = d->p;
   const int nr = d->nr;
+  if (flags == THORIN_REFRESH_RING_MEANS) {
+    // a state put back as it was at the end of a DT (fields, c_s and T
+    // included): the ring means and viscosities the next substep reads
+    aux_ring_mean(d->g, d->cs, d->ring[R_CSMEAN], d->s);
+    if (p.alpha_flock) aux_ring_mean(d->g, d->temper, d->ring[R_TEMPMEAN], d->s);
+    aux_viscosity_rings(d->g, d->vp, d->s);
+    CUCHK(cudaMemcpyAsync(d->csmean_h, d->ring[R_CSMEAN], d->nr * sizeof(double), cudaMemcpyDeviceToHost, d->s));
+    CUCHK(cudaStreamSynchronize(d->s));
+    return THORIN_OK;
+  }
   if (flags & THORIN_REFILL_GAS) {
     std::vector<double> m;
     RCHK(ring_means_host(d, d->rho, m));                    // RefillSigma, Theo.c:33-57

@@ -154,6 +154,7 @@ class Ensemble:
                 d.upload(f, v)
             d.set_sor_state(*sor[:3])
             d.set_time(t)
+            d.refresh(4)                  # THORIN_REFRESH_RING_MEANS: ring means of the restored c_s
             C.memmove(C.byref(s), C.byref(sy), C.sizeof(s))
 
     def run_schedule(self, sched: dict, ndt: int = 1) -> dict:

@@ -222,6 +222,11 @@ int thorin_gpu_download(thorin_disk *d, int field, double *host);
  * BckpFieldsForBC (Pebbles.c:208-232). */
 #define THORIN_REFILL_GAS     1
 #define THORIN_REFILL_PEBBLES 2
+/* Alone (not combined with the others): only the ring means of c_s (and
+ * of T) and the viscosity per ring, from the resident c_s and T, as the end
+ * of a substep leaves them; for a state restored from a snapshot taken
+ * between DTs that includes c_s and T. */
+#define THORIN_REFRESH_RING_MEANS 4
 int thorin_gpu_refresh(thorin_disk *d, int flags);
 
 /* Ring profiles (nrad doubles each). */
