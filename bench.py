@@ -154,7 +154,7 @@ WARMNET = os.environ.get("THORIN_WARMNET", os.path.join(ROOT, "fargo_thorin_gb30
 WARMNET_FACTOR = int(os.environ.get("THORIN_WARMNET_FACTOR", "1"))   # disk cells per network cell per axis
 
 
-def warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, steps, stream, barrier, t_plain, plain_per_solve):
+def warm_start_phase(d, snapd, snap_sys, steps, stream, barrier, t_plain, plain_per_solve):
     """Replay the timed DTs with the trained network attached in PREDICT
     mode: SOR sweeps per solve against the plain run, the throughput, and the
     temperature difference after the DTs (both meet the same threshold)."""
@@ -166,11 +166,7 @@ def warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, steps, stream, barr
     def replay(params):
         """the timed DTs again from the snapshot with a network attached"""
         net = WS.WarmNet(NR, NS, params=params, factor=WARMNET_FACTOR)
-        for f, v in snap.items():
-            d.upload(f, v)
-        d.set_sor_state(*snap_sor[:3])
-        d.set_time(snap_time)
-        d.refresh(4)                      # ring means of the restored c_s
+        d.restore(snapd)
         sys_ = snap_sys.copy()
         WS.attach(d, net, WS.PREDICT)
         st0, pred0 = d.stats(), WS.stats(d).predictions
@@ -259,9 +255,8 @@ def run_gpu(args):
     stream = torch.cuda.ExternalStream(d.stream())
     # snapshot of the whole disk state, so that the end-to-end phase below
     # repeats exactly the DTs of the device-timed phase
-    snap = {f: d.get(f) for f in SNAPSHOT_FIELDS}
-    snap_sor = d.sor_state()
-    snap_time = d.stats().physical_time
+    snapd = d.snapshot(SNAPSHOT_FIELDS)
+    snap = snapd["fields"]
     snap_sys = sys_.copy()
     d.set_timing(True)
     launches0 = d.stats().kernel_launches
@@ -303,11 +298,7 @@ def run_gpu(args):
 
     # end to end through the C ABI with host buffers (pinned), from the same
     # starting state: the same DTs, substeps and SOR sweeps as above
-    for f, v in snap.items():
-        d.upload(f, v)
-    d.set_sor_state(*snap_sor[:3])
-    d.set_time(snap_time)
-    d.refresh(4)                          # ring means of the restored c_s
+    d.restore(snapd)
     sys_ = snap_sys.copy()
     sweeps_e0 = d.stats().sor_sweeps
     n = (NR + 1) * NS
@@ -333,7 +324,7 @@ def run_gpu(args):
     e2e_value = NR * NS * esubs_all / e_max
 
     # the same DTs again with the learned SOR warm start (device-timed)
-    learned = warm_start_phase(d, snap, snap_sor, snap_time, snap_sys, args.steps, stream, barrier, t_plain,
+    learned = warm_start_phase(d, snapd, snap_sys, args.steps, stream, barrier, t_plain,
                                sweeps / max(solves, 1))
     ens = None
     if rank == 0 and not args.no_ensemble:
@@ -369,7 +360,7 @@ def run_gpu(args):
                                    "instruction"}
         cpu = None
         if ws == 1 and not args.no_cpu_baseline:
-            cpu = cpu_baseline(p, snap, snap_sor, snap_time, snap_sys, per_dt)
+            cpu = cpu_baseline(p, snapd, snap_sys, per_dt)
         # the whole DT against both roofs: algorithmic bytes (state traffic of
         # every substep plus 64 B per cell per SOR sweep) and FP64
         # instructions (per-kernel ncu counts per cell, scaled to the DT)
@@ -439,7 +430,7 @@ def oracle_disk(O, omp=True):
     return p, o, workloads.make_planets(p, [workloads.PLANET1])
 
 
-def cpu_baseline(p, snap, snap_sor, snap_time, snap_sys, per_dt, budget_s=20.0):
+def cpu_baseline(p, snapd, snap_sys, per_dt, budget_s=20.0):
     """The oracle (OpenMP, all host cores) from the GPU arm's own snapshot
     taken after the warm-up: the same first timed DTs, as many as fit in
     about budget_s seconds (at least one).  Their substep and SOR sweep
@@ -448,11 +439,12 @@ def cpu_baseline(p, snap, snap_sor, snap_time, snap_sys, per_dt, budget_s=20.0):
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     _, o, _ = oracle_disk(O)              # initial profiles and damping targets as on the GPU
-    for f, v in snap.items():
+    for f, v in snapd["fields"].items():
         o.set(f, v)
     o.refresh(0)                          # EOS of the snapshot's state
-    o.set_sor_state(*snap_sor[:3])
-    o.set_time(snap_time)
+    o.set_sor_state(*snapd["sor"][:3])
+    o.set_time(snapd["time"])
+    o.set_dt_stellar(snapd["dt_stellar"])
     s = snap_sys.copy()
     t0 = time.perf_counter()
     mine = []

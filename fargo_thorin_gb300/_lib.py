@@ -47,6 +47,8 @@ SIGNATURES = {
     "thorin_gpu_get_sor_state": (C.c_int, [_P, _D, _D, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "thorin_gpu_set_sor_state": (C.c_int, [_P, C.c_double, C.c_double, C.c_int]),
     "thorin_gpu_set_timing": (C.c_int, [_P, C.c_int]),
+    "thorin_gpu_get_dt_stellar": (C.c_int, [_P, _D]),
+    "thorin_gpu_set_dt_stellar": (C.c_int, [_P, C.c_double]),
     "thorin_gpu_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "thorin_integrals_static": (C.c_int, [_D, _D, _D, _D, _D, _D, _D, _D, C.c_int, C.c_int, C.c_double, _D, _P]),
     "thorin_selftest_division": (C.c_int, [C.c_longlong, C.c_ulonglong, C.c_double, C.POINTER(C.c_ulonglong),

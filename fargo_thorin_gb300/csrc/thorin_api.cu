@@ -2312,6 +2312,27 @@ extern "C" int thorin_gpu_set_sor_state(thorin_disk *d, double omega, double dom
   return THORIN_OK;
 }
 
+// The one scalar a DT hands to the next besides the fields and the omega
+// schedule: DiffusionTimestep's dt_stellar of the last energy step, which
+// bounds the next CFL (SourceEuler.c:680-690).
+extern "C" int thorin_gpu_get_dt_stellar(thorin_disk *d, double *dt_stellar)
+{
+  if (!d || !dt_stellar) return THORIN_ERR_ARG;
+  CUCHK(cudaMemcpyAsync(d->scal_h + SC_DTSTELLAR, d->scal + SC_DTSTELLAR, sizeof(double), cudaMemcpyDeviceToHost, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  *dt_stellar = d->scal_h[SC_DTSTELLAR];
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_set_dt_stellar(thorin_disk *d, double dt_stellar)
+{
+  if (!d) return THORIN_ERR_ARG;
+  d->scal_h[SC_DTSTELLAR] = dt_stellar;
+  CUCHK(cudaMemcpyAsync(d->scal + SC_DTSTELLAR, d->scal_h + SC_DTSTELLAR, sizeof(double), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaStreamSynchronize(d->s));
+  return THORIN_OK;
+}
+
 extern "C" int thorin_gpu_set_timing(thorin_disk *d, int on)
 {
   if (!d) return THORIN_ERR_ARG;

@@ -135,6 +135,28 @@ class GpuDisk:
     def set_sor_state(self, omega: float, domega: float, niterlast: int):
         _lib.check(self.L.thorin_gpu_set_sor_state(self.h, omega, domega, niterlast), "set_sor_state")
 
+    def dt_stellar(self) -> float:
+        v = C.c_double()
+        _lib.check(self.L.thorin_gpu_get_dt_stellar(self.h, C.byref(v)), "get_dt_stellar")
+        return v.value
+
+    def set_dt_stellar(self, v: float):
+        _lib.check(self.L.thorin_gpu_set_dt_stellar(self.h, v), "set_dt_stellar")
+
+    def snapshot(self, fields) -> dict:
+        """The state a later DT starts from: the given fields (with c_s and
+        T), the SOR omega schedule, the clock and dt_stellar."""
+        return {"fields": {f: self.get(f) for f in fields}, "sor": self.sor_state(),
+                "time": self.stats().physical_time, "dt_stellar": self.dt_stellar()}
+
+    def restore(self, snap: dict):
+        for f, v in snap["fields"].items():
+            self.upload(f, v)
+        self.set_sor_state(*snap["sor"][:3])
+        self.set_time(snap["time"])
+        self.set_dt_stellar(snap["dt_stellar"])
+        self.refresh(4)                   # THORIN_REFRESH_RING_MEANS
+
     def set_timing(self, on: bool):
         _lib.check(self.L.thorin_gpu_set_timing(self.h, 1 if on else 0), "set_timing")
 

@@ -144,17 +144,12 @@ class Ensemble:
     SNAP_FIELDS = (0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 11)   # state, temperature, sound speed, Stokes number
 
     def snapshot(self) -> list:
-        """Every disk's state, SOR schedule, clock and planets (host copies)."""
-        return [({f: d.get(f) for f in self.SNAP_FIELDS}, d.sor_state(), d.stats().physical_time, s.copy())
-                for d, s in zip(self.disks, self.systems)]
+        """Every disk's state (GpuDisk.snapshot) and planets (host copies)."""
+        return [(d.snapshot(self.SNAP_FIELDS), s.copy()) for d, s in zip(self.disks, self.systems)]
 
     def restore(self, snaps: list):
-        for d, s, (fields, sor, t, sy) in zip(self.disks, self.systems, snaps):
-            for f, v in fields.items():
-                d.upload(f, v)
-            d.set_sor_state(*sor[:3])
-            d.set_time(t)
-            d.refresh(4)                  # THORIN_REFRESH_RING_MEANS: ring means of the restored c_s
+        for d, s, (snap, sy) in zip(self.disks, self.systems, snaps):
+            d.restore(snap)
             C.memmove(C.byref(s), C.byref(sy), C.sizeof(s))
 
     def run_schedule(self, sched: dict, ndt: int = 1) -> dict:

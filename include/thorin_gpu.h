@@ -343,6 +343,13 @@ int thorin_gpu_set_sor_state(thorin_disk *d, double omega, double domega, int ni
  * library's stream (counters in thorin_stats). */
 int thorin_gpu_set_timing(thorin_disk *d, int on);
 
+/* DiffusionTimestep's dt_stellar (EnergySources.c:833), which the last
+ * energy step leaves for the next CFL (SourceEuler.c:680-690): with the
+ * fields and the SOR state, what a snapshot between DTs must carry for the
+ * next DT to repeat. */
+int thorin_gpu_get_dt_stellar(thorin_disk *d, double *dt_stellar);
+int thorin_gpu_set_dt_stellar(thorin_disk *d, double dt_stellar);
+
 /* The CUDA stream all work of this disk is issued on (cudaStream_t). */
 int thorin_gpu_get_stream(thorin_disk *d, void **stream);
 

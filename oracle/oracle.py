@@ -66,6 +66,7 @@ def lib(omp: bool = False):
         L.ora_sor_omega.restype = C.c_double
         L.ora_sor_omega.argtypes = [C.c_void_p]
         L.ora_set_sor_state.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int]
+        L.ora_set_dt_stellar.argtypes = [C.c_void_p, C.c_double]
         L.ora_get_sor_state.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                         C.POINTER(C.c_int)]
         _D = C.POINTER(C.c_double)
@@ -125,6 +126,9 @@ class OracleDisk:
         vals = [C.c_double() for _ in range(5)]
         self.L.ora_integrals(self.h, *[C.byref(v) for v in vals])
         return tuple(v.value for v in vals)
+
+    def set_dt_stellar(self, v: float):
+        self.L.ora_set_dt_stellar(self.h, v)
 
     def sor_state(self):
         om, dom, nl = C.c_double(), C.c_double(), C.c_int()

@@ -2668,6 +2668,9 @@ void ora_integrals(ora_disk *d, double *mass, double *mom, double *energy, doubl
   *mass = m; *mom = 0.5 * am; *energy = e; *pmass = pm; *pmom = 0.5 * pam;
 }
 
+/* DiffusionTimestep's dt_stellar carried from one DT to the next. */
+void ora_set_dt_stellar(ora_disk *d, double v) { d->dt_stellar = v; }
+
 /* The SOR omega schedule: omega, its step and the last iteration count. */
 void ora_get_sor_state(const ora_disk *d, double *omega, double *domega, int *niterlast)
 {
