@@ -148,12 +148,14 @@ struct thorin_disk {
   thorin_planets *sys_d = nullptr, *sys_h = nullptr;   // device copy, pinned staging copy
   GraphStats *gst_d = nullptr, *gst_h = nullptr;
   int *ring_info_d = nullptr;
+  AccArgs *acc_args_g = nullptr;     // the graph's own accretion arguments (its buffers' pointers)
   double *ctl_h = nullptr;           // pinned staging of the control block
   int graph_npl = -1;                // planets the graph was built for
   int capturing = 0;                 // launches are being captured into the DT graph
   StepDev capS;
   cudaGraph_t capture_sor_body = nullptr;   // body of the SOR loop node, filled after the substep capture
   cudaStream_t s_pl = nullptr;       // the planet step's branch of the substep graph
+  double *cap_ptr[11] = {};          // the buffers the DT graph was captured with (graph_roles order)
   cudaEvent_t ev_pl_fork = nullptr, ev_pl_join = nullptr;
   AccArgs *acc_args_d;               // pebble accretion arguments on the device
   SorCtl sor;
@@ -2047,7 +2049,7 @@ static int capture_substep(thorin_disk *d)
     for (int k = 0; k < npl; k++) {
       graph_acc_prep(S, k, d->s);
       graph_ring_means_at(d->g, d->vtheta, d->scal + 64 + 4, d->ring_info_d, 0, 1, d->s);
-      aux_accrete_kernels(d->g, d->acc_args_d, nb_max, d->scal, d->s);
+      aux_accrete_kernels(d->g, S.acc, nb_max, d->scal, d->s);
       graph_acc_finish(S, k, d->s);
     }
     if (p.evaporation_rate > 0.0) aux_evaporate(d->g, d->temper, d->pdens, d->s);
@@ -2080,6 +2082,15 @@ static int capture_substep(thorin_disk *d)
   return THORIN_OK;
 }
 
+// The state fields and their scratch partners, whose buffers the host path
+// swaps (ActualiseGas, the transport's output buffers).
+static void graph_roles(thorin_disk *d, double **r[11])
+{
+  double **q[11] = {&d->rho, &d->vrad, &d->vtheta, &d->energy, &d->pdens, &d->vrad_new, &d->vtheta_new,
+                    &d->energy_new, &d->t_rho_gas, &d->t_e_gas, &d->t_rho_peb};
+  for (int k = 0; k < 11; k++) r[k] = q[k];
+}
+
 // Options the device-resident DT covers; the others stay on the host path.
 static const char *graph_unsupported(const thorin_disk *d, const thorin_planets *sys)
 {
@@ -2104,6 +2115,7 @@ static int build_dt_graph(thorin_disk *d, int npl)
     RCHK(dalloc(d, (void **)&d->sys_d, sizeof(thorin_planets)));
     RCHK(dalloc(d, (void **)&d->gst_d, sizeof(GraphStats)));
     RCHK(dalloc(d, (void **)&d->ring_info_d, (2 + MAXPL_DEV) * sizeof(int)));
+    RCHK(dalloc(d, (void **)&d->acc_args_g, sizeof(AccArgs)));
     CUCHK(cudaMallocHost((void **)&d->sys_h, sizeof(thorin_planets)));
     CUCHK(cudaMallocHost((void **)&d->gst_h, sizeof(GraphStats)));
     CUCHK(cudaMallocHost((void **)&d->ctl_h, CTL_COUNT * sizeof(double)));
@@ -2111,17 +2123,19 @@ static int build_dt_graph(thorin_disk *d, int npl)
     CUCHK(cudaEventCreateWithFlags(&d->ev_pl_fork, cudaEventDisableTiming));
     CUCHK(cudaEventCreateWithFlags(&d->ev_pl_join, cudaEventDisableTiming));
   }
-  // the accretion arguments' device pointers (the scalars are set per planet)
+  // the accretion arguments' device pointers (the scalars are set per
+  // planet): the buffers the graph is captured with, in a block of the
+  // graph's own (the host path rewrites acc_args_d with its current buffers)
   AccArgs a;
   memset(&a, 0, sizeof(a));
   a.pdens = d->pdens; a.macc = d->macc; a.pvr = d->pvrad; a.pvt = d->pvtheta; a.tau = d->tau; a.cs = d->cs;
   a.vt = d->vtheta;
   a.part = d->partials;
   a.acc = d->scal + 64;
-  CUCHK(cudaMemcpyAsync(d->acc_args_d, &a, sizeof(a), cudaMemcpyHostToDevice, d->s));
+  CUCHK(cudaMemcpyAsync(d->acc_args_g, &a, sizeof(a), cudaMemcpyHostToDevice, d->s));
   CUCHK(cudaStreamSynchronize(d->s));
   StepDev &S = d->capS;
-  S.g = d->g; S.c = d->plc; S.sys = d->sys_d; S.scal = d->scal; S.iscal = d->iscal; S.acc = d->acc_args_d;
+  S.g = d->g; S.c = d->plc; S.sys = d->sys_d; S.scal = d->scal; S.iscal = d->iscal; S.acc = d->acc_args_g;
   S.ring_info = d->ring_info_d; S.pl = d->planets_d; S.heat_idx = d->heat_idx_d; S.heat_val = d->heat_val_d;
   S.st = d->gst_d; S.sor = d->sor; S.DT = p.dt; S.evaporation_rate = p.evaporation_rate; S.npl = npl;
   S.pebbles = p.pebbles; S.accret_heating = p.pebbles && p.accret_heating; S.indirect_term = p.indirect_term;
@@ -2173,6 +2187,9 @@ static int build_dt_graph(thorin_disk *d, int npl)
   }
   d->dt_graph = exec;
   d->graph_npl = npl;
+  double **roles[11];
+  graph_roles(d, roles);
+  for (int k = 0; k < 11; k++) d->cap_ptr[k] = *roles[k];
   return THORIN_OK;
 }
 
@@ -2181,6 +2198,17 @@ static int build_dt_graph(thorin_disk *d, int npl)
 static int graph_launch(thorin_disk *d, const thorin_planets *sys)
 {
   if (!d->dt_graph || d->graph_npl != sys->nb) RCHK(build_dt_graph(d, sys->nb));
+  // the host path swaps buffers between the state fields and their scratch
+  // partners; the graph reads the buffers it was captured with, so the state
+  // goes back into those first (each field's buffers are its own, so no copy
+  // overwrites another field)
+  double **roles[11];
+  graph_roles(d, roles);
+  const size_t bytes = d->fsize * sizeof(double);
+  for (int k = 0; k < 5; k++)
+    if (*roles[k] && *roles[k] != d->cap_ptr[k])
+      CUCHK(cudaMemcpyAsync(d->cap_ptr[k], *roles[k], bytes, cudaMemcpyDeviceToDevice, d->s));
+  for (int k = 0; k < 11; k++) *roles[k] = d->cap_ptr[k];
   *d->sys_h = *sys;
   CUCHK(cudaMemcpyAsync(d->sys_d, d->sys_h, sizeof(thorin_planets), cudaMemcpyHostToDevice, d->s));
   set_ctl(d, {{CTL_TIME, d->PhysicalTime}, {CTL_OMEGA_FRAME, d->OmegaFrame}, {CTL_SOR_OMEGA, d->omega},

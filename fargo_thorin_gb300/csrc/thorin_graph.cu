@@ -95,7 +95,11 @@ __global__ void k_g_force_prep(StepDev S)
                     &ays);
     const double x = S.sys->x[k], y = S.sys->y[k];
     const double r = sqrt(x * x + y * y);
-    S.ring_info[2 + k] = (r >= S.c.rin && r <= S.c.rout) ? pl_ring_of(S.g.r.Rsup, S.c.nr, r) : -1;
+    const int i = (r >= S.c.rin && r <= S.c.rout) ? pl_ring_of(S.g.r.Rsup, S.c.nr, r) : -1;
+    S.ring_info[2 + k] = i;
+    // the planet step runs beside the hydro substep, which rewrites the
+    // ring means of c_s at its end: DampingTW04's value is taken now
+    S.scal[SC_RCS + k] = (i >= 0) ? S.g.r.csmean[i] : 0.0;
   }
   ctl[CTL_INDX_PL] = S.indirect_term ? -axs : 0.0;
   ctl[CTL_INDY_PL] = S.indirect_term ? -ays : 0.0;
@@ -113,7 +117,7 @@ __global__ void k_g_planet_step(StepDev S)
     sys->ay[k] = S.scal[SC_PLANET_A + 2 * k + 1];
     const int i = S.ring_info[2 + k];
     rrho[k] = (i >= 0) ? S.scal[SC_PLANET_A + 2 * MAXPL_DEV + k] : 0.0;
-    rcs[k] = (i >= 0) ? S.g.r.csmean[i] : 0.0;
+    rcs[k] = (i >= 0) ? S.scal[SC_RCS + k] : 0.0;
   }
   const double dt = S.g.ctl[CTL_DT];
   const double ind[2] = {S.scal[SC_INDX], S.scal[SC_INDY]};

@@ -19,7 +19,8 @@ enum {
   SC_PLANET_A = 32,           // 2 per planet: ax, ay (then the ring means of Sigma for DampingTW04)
   SC_TORQUE = 56,             // 2 per planet: ring means of Sigma either side of the planet (UpdateLog)
   SC_GASACC = 80,             // dM, dPx, dPy of the gas accretion onto one planet
-  SC_DRAGCELL = 84            // 6 values of the planet's cell for the aerodynamic drag
+  SC_DRAGCELL = 84,           // 6 values of the planet's cell for the aerodynamic drag
+  SC_RCS = 96                 // device-resident DT: ring mean of c_s at each planet, taken before the hydro
 };
 enum { IS_NSUB = 0, IS_SOR_DONE, IS_SOR_NITER, IS_SOR_CHANGED, IS_CRASH, IS_COUNT };
 

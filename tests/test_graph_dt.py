@@ -177,3 +177,25 @@ def test_schedule_tuner_replays_identical_work():
     for x, y in zip(fa, fb):
         assert H.rel_l2(x, y) < 1e-12
     ens.close()
+
+
+def test_graph_and_host_dts_interleave():
+    """Host-path DTs swap the buffers of the state fields; a graph DT after
+    them still reads the current state: host, graph, host, graph DTs end
+    where four host DTs end (counts exact, fields within 1e-12)."""
+    g = H.load("disk1_32x96")
+    p = H.case_params(g)
+    a, b = _disk(p), _disk(p)
+    for d in (a, b):
+        _start(d, p, g)
+    sa = workloads.make_planets(p, [tuple(g["planet"])])
+    sb = workloads.make_planets(p, [tuple(g["planet"])])
+    n = p.nrad * p.nsec
+    for step in range(8):
+        a.algogas(sa)
+        (b.algogas if step in (0, 1, 3, 6) else b.algogas_graph)(sb)
+        assert a.stats().substeps == b.stats().substeps and a.stats().sor_sweeps == b.stats().sor_sweeps
+        for f in FIELDS:
+            assert H.rel_l2(b.get(H.FIELD_IDS[f])[:n], a.get(H.FIELD_IDS[f])[:n]) < 1e-12, (f, step)
+    a.close()
+    b.close()
