@@ -296,6 +296,28 @@ def run_gpu(args):
     total_updates = NR * NS * subs_all
     value = total_updates / (ms_max / 1e3)
 
+    # the same DTs as device-resident DT graphs (one graph launch per DT)
+    graph = None
+    if d.graph_supported(snap_sys):
+        d.restore(snapd)
+        gsys = snap_sys.copy()
+        gsw0 = d.stats().sor_sweeps
+        barrier()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        gsubs = 0
+        for _ in range(args.steps):
+            d.algogas_graph(gsys)
+            gsubs += d.stats().substeps
+        g1.record(stream)
+        barrier()
+        gms = g0.elapsed_time(g1)
+        gsweeps = d.stats().sor_sweeps - gsw0
+        graph = {"value": NR * NS * gsubs / (gms / 1e3), "ms_per_step": gms / args.steps, "substeps": gsubs,
+                 "sor_sweeps": gsweeps, "same_work_as_value": bool(gsubs == subs and gsweeps == sweeps),
+                 "t_rel_l2_vs_value": float(np.linalg.norm(d.get(8) - t_plain) / np.linalg.norm(t_plain)),
+                 "mode": "one CUDA graph launch per DT: substep loop, planet side and SOR schedule on the device"}
+
     # end to end through the C ABI with host buffers (pinned), from the same
     # starting state: the same DTs, substeps and SOR sweeps as above
     d.restore(snapd)
@@ -397,6 +419,7 @@ def run_gpu(args):
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": bytes_pass, "avg_launch_ms": sor_avg_ms},
             "fp64_roofline": fp64,
+            "graph_dt": graph,
             "step_roofline": step_roof,
             "step_fp64_roofline": step_fp64,
             "sor_warm_start": learned,

@@ -19,7 +19,7 @@
 // learned SOR warm start (warmnet.cu)
 int wn_sor_predict(thorin_warmnet *n, int nr, int ns, int fc, double *T, const double *ml, const double *mlip,
                    const double *mlim, const double *mljp, const double *mljm, const double *rhs, const double *prev,
-                   double *jac, const double *jscale, double omega, cudaStream_t s);
+                   double *jac, const double *jscale, double omega, const double *omega_dev, cudaStream_t s);
 int wn_sor_train(thorin_warmnet *n, int nr, int ns, int fc, const double *tk, const double *tconv, const double *ml,
                  const double *mlip, const double *mlim, const double *mljp, const double *mljm, const double *rhs,
                  const double *prev, double *jac, float lr, double *scratch, cudaStream_t s);
@@ -606,6 +606,10 @@ extern "C" int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode,
     CUCHK(cudaMemsetAsync(d->ws_prev, 0, (size_t)d->nr * d->ns * sizeof(double), d->s));
   }
   d->ws_f = f;
+  if (d->dt_graph && (d->ws_net != (mode == THORIN_WS_OFF ? nullptr : n) || d->ws_mode != mode)) {
+    cudaGraphExecDestroy(d->dt_graph);            // the DT graph holds the warm start's launches or not
+    d->dt_graph = nullptr;
+  }
   d->ws_net = mode == THORIN_WS_OFF ? nullptr : n;
   d->ws_mode = mode;
   d->ws_lr = lr;
@@ -1498,7 +1502,7 @@ static int sor_solve(thorin_disk *d, double omega, int *niter, int *capped, bool
     CUCHK(cudaMemcpyAsync(d->tbackup, d->temper, (size_t)d->nr * d->ns * sizeof(double), cudaMemcpyDeviceToDevice,
                           d->s));
     RCHK(wn_sor_predict(d->ws_net, d->nr, d->ns, d->ws_f, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm,
-                        d->rhs, d->ws_prev, d->ws_jac, d->sor.jscale, omega, d->s));
+                        d->rhs, d->ws_prev, d->ws_jac, d->sor.jscale, omega, nullptr, d->s));
     d->ws_st.predictions++;
   }
   if (d->timing) CUCHK(cudaEventRecord(d->ev[0], d->s));
@@ -1993,6 +1997,13 @@ static int capture_sor(thorin_disk *d)
   StepDev &S = d->capS;
   graph_sor_begin(S, d->s);
   hydro_sor_resid0(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, d->sor, d->s);
+  const bool predict = d->ws_net && d->ws_mode == THORIN_WS_PREDICT;
+  if (predict) {          // the learned warm start moves T before the sweeps, as on the host path
+    CUCHK(cudaMemcpyAsync(d->tbackup, d->temper, (size_t)d->nr * d->ns * sizeof(double), cudaMemcpyDeviceToDevice,
+                          d->s));
+    RCHK(wn_sor_predict(d->ws_net, d->nr, d->ns, d->ws_f, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm,
+                        d->rhs, d->ws_prev, d->ws_jac, d->sor.jscale, 0.0, d->ctl + CTL_SOR_OMEGA, d->s));
+  }
   cudaStreamCaptureStatus cs;
   cudaGraph_t cg;
   const cudaGraphNode_t *deps = nullptr;
@@ -2010,6 +2021,8 @@ static int capture_sor(thorin_disk *d)
   d->capture_sor_body = np.conditional.phGraph_out[0];
   CUCHK(cudaStreamUpdateCaptureDependencies(d->s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
   graph_sor_end(S, d->s);
+  if (predict && d->ws_prev)           // this solve's update, an input of the next prediction
+    RCHK(wn_record_update(d->nr, d->ns, d->temper, d->tbackup, d->ws_prev, d->s));
   return THORIN_OK;
 }
 
@@ -2101,7 +2114,7 @@ static const char *graph_unsupported(const thorin_disk *d, const thorin_planets 
   if (p.prescribed_accretion) return "ParametricAccretion";
   if (p.aerodynamic_drag) return "AerodynamicDrag";
   if (!p.energy_eq || p.parametric_cooling) return "runs without SOR radiative diffusion";
-  if (d->ws_net) return "the learned SOR warm start";
+  if (d->ws_net && d->ws_mode == THORIN_WS_TRAIN) return "warm-start training";
   if (d->sor_direct) return "THORIN_SOR_DIRECT";
   if (sys->nb > MAXPL_DEV) return "more than 8 planets";
   return nullptr;
@@ -2239,6 +2252,7 @@ static int graph_finish(thorin_disk *d, thorin_planets *sys)
   d->st.substeps = g.nsub;
   d->st.crashed = g.crashed;
   d->st.sor_calls += g.sor_calls;
+  if (d->ws_net && d->ws_mode == THORIN_WS_PREDICT) d->ws_st.predictions += g.sor_calls;
   d->st.sor_sweeps += g.sor_sweeps;
   if (g.sor_calls) { d->st.sor_last_niter = g.sor_last_niter; d->st.sor_omega = g.omega_used; }
   d->st.last_dt = d->ctl_h[CTL_DT];

@@ -514,6 +514,17 @@ __global__ void k_wn_sum(const double *__restrict__ part, int n, double scale, d
   if (threadIdx.x == 0) *out = s * scale;
 }
 
+// the same with scale = 1 / (omega a b), omega read from the device (the
+// device-resident DT's control block)
+__global__ void k_wn_sum_omega(const double *__restrict__ part, int n, const double *__restrict__ omega, double a,
+                               double b, double *__restrict__ out)
+{
+  double s = 0.0;
+  for (int k = threadIdx.x; k < n; k += 32) s += part[k];
+  s = warp_reduce(s, OpAdd());
+  if (threadIdx.x == 0) *out = s * (1.0 / (*omega * a * b));
+}
+
 __global__ void k_wn_sqnorm(const float *__restrict__ g, int n, double *__restrict__ part)
 {
   double s = 0.0;
@@ -1047,14 +1058,17 @@ static int wn_check_err(thorin_warmnet *n)
 // (nr/fc) x (ns/fc); jac has the disk's nr x ns cells.
 int wn_sor_predict(thorin_warmnet *n, int nr, int ns, int fc, double *T, const double *ml, const double *mlip,
                    const double *mlim, const double *mljp, const double *mljm, const double *rhs, const double *prev,
-                   double *jac, const double *jscale, double omega, cudaStream_t s)
+                   double *jac, const double *jscale, double omega, const double *omega_dev, cudaStream_t s)
 {
   // dscal: [2] mean |r/Ml| of the start, [3] mean |r|, [4] residual loss,
   // [5] supervised loss, [0] total loss; partials from dscal + 8
   SorSys m{ml, mlip, mlim, mljp, mljm, rhs};
   double *part = n->dscal + 8;
   const int sb = 2 * n->nsm;
-  if (jscale) {            // sum of omega |r / Ml| from the solve's own residual pass
+  if (jscale && omega_dev) {   // omega on the device (device-resident DT)
+    k_wn_sum_omega<<<1, 32, 0, s>>>(jscale, 1, omega_dev, (double)(nr - 2), (double)ns, n->dscal + 2);
+    g_thorin_launches += 1;
+  } else if (jscale) {      // sum of omega |r / Ml| from the solve's own residual pass
     k_wn_sum<<<1, 32, 0, s>>>(jscale, 1, 1.0 / (omega * (double)(nr - 2) * ns), n->dscal + 2);
     g_thorin_launches += 1;
   } else {

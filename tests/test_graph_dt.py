@@ -199,3 +199,34 @@ def test_graph_and_host_dts_interleave():
             assert H.rel_l2(b.get(H.FIELD_IDS[f])[:n], a.get(H.FIELD_IDS[f])[:n]) < 1e-12, (f, step)
     a.close()
     b.close()
+
+
+def test_graph_dt_with_learned_warm_start():
+    """The warm start's prediction (network on the tensor cores) inside the
+    device-resident DT gives the host path's result: same SOR counts,
+    temperature within 1e-12."""
+    from fargo_thorin_gb300 import warmstart as WS
+    g = H.load("disk1_32x96")
+    p = H.case_params(g)
+    rng = np.random.default_rng(3)
+    params = WS.init_params(1)
+    import warmnet_oracle as WO
+    params[WO.OFFSETS[7]:] = rng.standard_normal(params.size - WO.OFFSETS[7]).astype(np.float32) * 0.01
+    out = []
+    for use_graph in (False, True):
+        d = _disk(p)
+        _start(d, p, g)
+        s = workloads.make_planets(p, [tuple(g["planet"])])
+        d.algogas(s)                                    # calibration DT without the network
+        net = WS.WarmNet(p.nrad, p.nsec, params=params)
+        WS.attach(d, net, WS.PREDICT)
+        counts = []
+        for _ in range(3):
+            (d.algogas_graph if use_graph else d.algogas)(s)
+            counts.append((d.stats().substeps, d.stats().sor_sweeps))
+        out.append((counts, d.get(H.FIELD_IDS["temper"]), WS.stats(d).predictions))
+        WS.attach(d, None, WS.OFF)
+        net.close()
+        d.close()
+    assert out[0][0] == out[1][0] and out[0][2] == out[1][2] > 0
+    assert H.rel_l2(out[1][1], out[0][1]) < 1e-12
