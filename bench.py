@@ -238,6 +238,65 @@ def ensemble_phase(n=64, seed=0, ndt=2, settle=3):
     return out
 
 
+def combined_phase(n_each=8, ndt=1, settle=1, seed=11):
+    """The combined workload: 2 n_each gas + pebble + embryo disks, n_each of
+    1024x3072 and n_each of 2048x6144 rings x sectors, with drawn alpha,
+    Sigma0, aspect ratio and embryo mass, FP64 hydro, SOR tolerance 1e-8.
+    Every disk starts from the omega schedule calibrated on the 1024x3072
+    bench disk, takes its first DT and `settle` more as device-resident DT
+    graphs (all disks together); from one snapshot of every disk the same
+    ndt DTs then run (a) batched: every disk a
+    device-resident DT graph, all launched together, each with the learned
+    SOR warm start attached, and (b) plain: the disks one after the other on
+    the host path without the network.  Cell-updates/s, the speed-up of (a)
+    over (b) and the SOR sweeps per solve of both."""
+    from fargo_thorin_gb300 import warmstart as WS
+    from fargo_thorin_gb300.ensemble import Ensemble
+    t_setup = time.perf_counter()
+    # the omega schedule of a calibrated 1024x3072 disk (the bench workload's
+    # first DT) seeds every disk
+    _, d0, s0 = make_disk()
+    d0.algogas(s0)
+    sor0 = d0.sor_state()[:3]
+    d0.close()
+    ens = Ensemble.drawn_sizes([1024] * n_each + [2048] * n_each, seed=seed, sor_state=sor0)
+    for _ in range(settle):
+        ens.step_graph()
+    snaps = ens.snapshot()
+    t_setup = time.perf_counter() - t_setup
+    params = WS.WarmNet.load_params(WARMNET) if os.path.exists(WARMNET) else None
+    nets = []
+    if params is not None:
+        for dd in ens.disks:
+            net = WS.WarmNet(dd.nr, dd.ns, params=params)
+            WS.attach(dd, net, WS.PREDICT)
+            nets.append(net)
+    ens.restore(snaps)
+    calls0 = sum(dd.stats().sor_calls for dd in ens.disks)
+    a = ens.run_schedule({"mode": "graph"}, ndt)
+    a_calls = sum(dd.stats().sor_calls for dd in ens.disks) - calls0
+    for dd, net in zip(ens.disks, nets):
+        WS.attach(dd, None, WS.OFF)
+        net.close()
+    ens.restore(snaps)
+    calls0 = sum(dd.stats().sor_calls for dd in ens.disks)
+    b = ens.run_schedule({"mode": "sequential"}, ndt)
+    b_calls = sum(dd.stats().sor_calls for dd in ens.disks) - calls0
+    out = {"disks": len(ens.disks), "grids": f"{n_each} x 1024x3072 + {n_each} x 2048x6144", "cells": ens.cells,
+           "dts": ndt, "value": a["cell_updates"] / a["seconds"], "unit": UNIT,
+           "ms_per_dt": 1e3 * a["seconds"] / ndt, "sequential_plain_value": b["cell_updates"] / b["seconds"],
+           "sequential_plain_ms_per_dt": 1e3 * b["seconds"] / ndt,
+           "speedup_vs_sequential_plain": (a["cell_updates"] / a["seconds"]) / (b["cell_updates"] / b["seconds"]),
+           "sweeps_per_solve_batched_learned": a["sweeps"] / max(a_calls, 1),
+           "sweeps_per_solve_sequential_plain": b["sweeps"] / max(b_calls, 1),
+           "warm_start": os.path.relpath(WARMNET, ROOT) if params is not None else None,
+           "setup_s": t_setup, "settle_dts": settle,
+           "timing": "wall clock with a device synchronisation on both sides; both runs replay the same DTs from "
+                     "one snapshot of every disk"}
+    ens.close()
+    return out
+
+
 def run_gpu(args):
     import torch
     ws, rank, local = dist_env()

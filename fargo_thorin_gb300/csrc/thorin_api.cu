@@ -2242,6 +2242,7 @@ static int graph_launch(thorin_disk *d, const thorin_planets *sys)
 static int graph_finish(thorin_disk *d, thorin_planets *sys)
 {
   CUCHK(cudaStreamSynchronize(d->s));
+  d->cfl_first = 0;
   const GraphStats &g = *d->gst_h;
   *sys = *d->sys_h;
   d->PhysicalTime = d->ctl_h[CTL_TIME];
@@ -2291,6 +2292,11 @@ extern "C" int thorin_gpu_get_launch_shape(thorin_disk *d, int *sor_loop_sweeps,
   return THORIN_OK;
 }
 
+static bool graph_host_dt(const thorin_disk *d)
+{
+  return d->sor_first || (d->cfl_first && d->p.first_step > 0.0);
+}
+
 extern "C" int thorin_gpu_graph_supported(thorin_disk *d, const thorin_planets *sys)
 {
   if (!d || !sys) return THORIN_ERR_ARG;
@@ -2302,8 +2308,9 @@ extern "C" int thorin_gpu_graph_supported(thorin_disk *d, const thorin_planets *
 extern "C" int thorin_gpu_algogas_graph(thorin_disk *d, thorin_planets *sys)
 {
   RCHK(thorin_gpu_graph_supported(d, sys));
-  // the first DT calibrates omega and takes the first CFL on the host path
-  if (d->sor_first || d->cfl_first) return thorin_gpu_algogas(d, sys);
+  // the omega calibration of a disk's first solve runs on the host path (so
+  // does a first DT with FirstStep set, which only the first CFL reads)
+  if (graph_host_dt(d)) return thorin_gpu_algogas(d, sys);
   RCHK(graph_launch(d, sys));
   return graph_finish(d, sys);
 }
@@ -2320,7 +2327,7 @@ extern "C" int thorin_ensemble_algogas_graph(thorin_disk **disks, thorin_planets
   for (int k = 0; k < n; k++) {
     thorin_disk *d = disks[k];
     int rc = thorin_gpu_graph_supported(d, systems[k]);
-    if (rc == THORIN_OK && (d->sor_first || d->cfl_first)) rc = thorin_gpu_algogas(d, systems[k]);
+    if (rc == THORIN_OK && graph_host_dt(d)) rc = thorin_gpu_algogas(d, systems[k]);
     else if (rc == THORIN_OK) { rc = graph_launch(d, systems[k]); launched[k] = (rc == THORIN_OK); }
     if (status) status[k] = rc;
     if (rc != THORIN_OK && rc != THORIN_ERR_SOR_MAXIT) worst = rc;

@@ -70,6 +70,50 @@ class Ensemble:
         self._arrays()
 
     @classmethod
+    def drawn_sizes(cls, sizes: list, seed: int = 0, sor_maxiters: int = 20000, tries: int = 4,
+                    sor_state=None) -> "Ensemble":
+        """Disks of the given ring counts (Nsec = 3 Nrad) with drawn alpha,
+        Sigma0, aspect ratio and embryo mass, each advanced by its first DT;
+        a draw whose first DT fails is replaced by another of the same size.
+        With sor_state = (omega, domega, niterlast) the disks start from that
+        omega schedule instead of the reference's calibration of the first
+        solve (IterateRelaxationParameter, whose cold SOR solves take
+        thousands of sweeps on the largest grids), and their first DTs run
+        together as device-resident DT graphs."""
+        rng = np.random.default_rng(seed)
+        specs, kept = [], []
+        for k, nr in enumerate(sizes):
+            for attempt in range(tries):
+                spec = draw(rng)
+                spec["nrad"] = int(nr)
+                p, d, s = make_disk(spec, seed=seed + 100 * k + attempt, sor_maxiters=sor_maxiters)
+                if sor_state is not None:
+                    d.set_sor_state(*sor_state)
+                    specs.append(spec)
+                    kept.append((p, d, s))
+                    break
+                rc = d.L.thorin_gpu_algogas(d.h, C.byref(s))
+                if rc == 0 and np.isfinite(d.get(8)).all():
+                    specs.append(spec)
+                    kept.append((p, d, s))
+                    break
+                d.close()
+            else:
+                raise RuntimeError(f"ensemble: no viable draw of a disk with {nr} rings")
+        ens = cls.__new__(cls)
+        ens.L = _lib.load()
+        ens.specs = specs
+        ens.params = [b[0] for b in kept]
+        ens.disks = [b[1] for b in kept]
+        ens.systems = [b[2] for b in kept]
+        ens._arrays()
+        if sor_state is not None:
+            st = ens.step_graph()
+            if any(x not in (0, 4) for x in st):
+                raise RuntimeError(f"ensemble: first DTs failed: {st}")
+        return ens
+
+    @classmethod
     def drawn(cls, n: int, seed: int = 0, sor_maxiters: int = 2000, tries: int = 8) -> "Ensemble":
         """n drawn disks, each advanced by its first DT (with the SOR omega
         calibration).  Some draws are not viable on the coarser grids: the
@@ -114,7 +158,7 @@ class Ensemble:
         n = len(self.disks)
         st = (C.c_int * n)()
         rc = self.L.thorin_ensemble_algogas(self._dp, self._sp, n, workers, order, st)
-        _lib.check(rc, "thorin_ensemble_algogas")
+        _lib.check(rc, "thorin_ensemble_algogas", ok=(0, 4))       # 4: a solve reached the iteration cap
         return list(st)
 
     def step_graph(self) -> list:
