@@ -612,6 +612,9 @@ def main():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-disk ensemble measurement")
+    ap.add_argument("--combined", action="store_true",
+                    help="only the combined 16-disk workload (1024x3072 and 2048x6144 grids, batched with the learned "
+                         "warm start against plain sequential; about 10 minutes); prints its JSON line")
     ap.add_argument("--profile", action="store_true",
                     help="run --steps DTs inside cuProfilerStart/Stop for ncu; prints no bench line")
     ap.add_argument("--grid", type=int, nargs=2, metavar=("NRAD", "NSEC"), default=(NR, NS),
@@ -619,6 +622,11 @@ def main():
     args = ap.parse_args()
     if args.profile:
         run_profile(args, *args.grid)
+        return
+    if args.combined:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"metric": "combined workload", **combined_phase()}), flush=True)
         return
     if args.warmup < 3:
         args.warmup = 3
