@@ -186,11 +186,39 @@ def warm_start_phase(d, snapd, snap_sys, steps, stream, barrier, t_plain, plain_
         return (e0.elapsed_time(e1), subs, pred,
                 (st1.sor_sweeps - st0.sor_sweeps) / max(st1.sor_calls - st0.sor_calls, 1), d.get(8))
 
+    def replay_extrapolated(order=2):
+        """the timed DTs again, each solve started from the extrapolated update"""
+        d.restore(snapd)
+        sys_ = snap_sys.copy()
+        WS.set_order(d, order)
+        WS.attach(d, None, WS.EXTRAPOLATE)
+        st0 = d.stats()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        subs = 0
+        for _ in range(steps):
+            d.algogas(sys_)
+            subs += d.stats().substeps
+        e1.record(stream)
+        barrier()
+        st1 = d.stats()
+        WS.attach(d, None, WS.OFF)
+        ms = e0.elapsed_time(e1)
+        per = (st1.sor_sweeps - st0.sor_sweeps) / max(st1.sor_calls - st0.sor_calls, 1)
+        t = d.get(8)
+        return {"order": order, "sweeps_per_solve": per, "sweeps_ratio_plain_over_extrapolated": plain_per_solve / per,
+                "value": NR * NS * subs / (ms / 1e3), "ms_per_step": ms / steps, "substeps": subs,
+                "t_rel_l2_vs_plain": float(np.linalg.norm(t - t_plain) / np.linalg.norm(t_plain)),
+                "start": "T_old + dt (2 r_1 - r_2), r_k = (T_conv - T_start) / dt of the k-th last solve"}
+
+    extrapolated = replay_extrapolated()
     # control: the same coupling with an untrained network (zero output
     # layer), i.e. the previous temperature plus one Jacobi step
     _, _, _, jacobi_per_solve, _ = replay(WS.init_params(0))
     ms, subs, pred, per_solve, t = replay(WS.WarmNet.load_params(WARMNET))
-    return {"plain_sweeps_per_solve": plain_per_solve, "learned_sweeps_per_solve": per_solve,
+    return {"plain_sweeps_per_solve": plain_per_solve, "extrapolated": extrapolated,
+            "learned_sweeps_per_solve": per_solve,
             "jacobi_start_sweeps_per_solve": jacobi_per_solve,
             "sweeps_ratio_plain_over_learned": plain_per_solve / per_solve if per_solve else None,
             "learned_value": NR * NS * subs / (ms / 1e3), "learned_ms_per_step": ms / steps, "substeps": subs,

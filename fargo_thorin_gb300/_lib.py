@@ -76,6 +76,7 @@ SIGNATURES = {
     "thorin_warmnet_adam": (C.c_int, [_P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float]),
     "thorin_gpu_warmstart": (C.c_int, [_P, _P, C.c_int, C.c_float]),
     "thorin_gpu_warmstart_stats": (C.c_int, [_P, _P]),
+    "thorin_gpu_warmstart_order": (C.c_int, [_P, C.c_int]),
     # ensembles (include/thorin_ensemble.h)
     "thorin_ensemble_algogas": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int, C.c_int, C.c_int,
                                           C.POINTER(C.c_int)]),

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <initializer_list>
 #include <string>
 #include <vector>
@@ -23,7 +24,10 @@ int wn_sor_predict(thorin_warmnet *n, int nr, int ns, int fc, double *T, const d
 int wn_sor_train(thorin_warmnet *n, int nr, int ns, int fc, const double *tk, const double *tconv, const double *ml,
                  const double *mlip, const double *mlim, const double *mljp, const double *mljm, const double *rhs,
                  const double *prev, double *jac, float lr, double *scratch, cudaStream_t s);
-int wn_record_update(int nr, int ns, const double *tconv, const double *tstart, double *prev, cudaStream_t s);
+int wn_record_update(int nr, int ns, const double *tconv, const double *tstart, double *hist, int nh,
+                     const double *dt, double *dts, cudaStream_t s);
+int ws_extrapolate(int nr, int ns, double *T, const double *hist, int order, const double *dt, const double *dts,
+                   cudaStream_t s);
 int wn_last_loss(thorin_warmnet *n, double *loss);
 int wn_dims(const thorin_warmnet *n, int *nr, int *ns);
 
@@ -183,7 +187,13 @@ struct thorin_disk {
   int ws_mode = THORIN_WS_OFF;
   float ws_lr = 0.f;
   thorin_ws_stats ws_st = {0, 0, 0.0, 0.0, 0.0};
-  double *ws_prev = nullptr;     // the previous solve's update T_conv - T_start (network input)
+  // the last ws_nh solves' updates T_conv - T_start, newest first (slot 0
+  // is the network's input), and their time steps (THORIN_WS_MAX_ORDER
+  // device doubles, 0 = not recorded)
+  double *ws_prev = nullptr;
+  double *ws_dts = nullptr;
+  int ws_nh = 0;                 // slots of ws_prev
+  int ws_order = 2;              // order of the extrapolated start
   double *ws_jac = nullptr;      // the Jacobi step of the solve's start, per cell
   int ws_f = 1;                  // disk cells per network cell along each axis (1 or 2)
   // the SOR sweep loop: one CUDA graph whose WHILE node repeats the two
@@ -582,13 +592,41 @@ extern "C" int thorin_gpu_create(const thorin_params *pin, thorin_disk **out)
   return THORIN_OK;
 }
 
+// Update history of the warm start with at least nh slots (zeroed, no time
+// step recorded); a larger history replaces the old one.
+static int ws_history(thorin_disk *d, int nh)
+{
+  const size_t cells = (size_t)d->nr * d->ns;
+  if (!d->ws_jac) {
+    RCHK(dalloc(d, (void **)&d->ws_jac, cells * sizeof(double)));
+    RCHK(dalloc(d, (void **)&d->ws_dts, THORIN_WS_MAX_ORDER * sizeof(double)));
+  }
+  if (nh <= d->ws_nh) return THORIN_OK;
+  if (d->ws_prev) {
+    d->allocs.erase(std::find(d->allocs.begin(), d->allocs.end(), (void *)d->ws_prev));
+    CUCHK(cudaStreamSynchronize(d->s));
+    cudaFree(d->ws_prev);
+    d->ws_prev = nullptr;
+  }
+  if (d->dt_graph) {                               // the DT graph holds the old history's address
+    cudaGraphExecDestroy(d->dt_graph);
+    d->dt_graph = nullptr;
+  }
+  RCHK(dalloc(d, (void **)&d->ws_prev, (size_t)nh * cells * sizeof(double)));
+  CUCHK(cudaMemsetAsync(d->ws_dts, 0, THORIN_WS_MAX_ORDER * sizeof(double), d->s));
+  d->ws_nh = nh;
+  return THORIN_OK;
+}
+
 extern "C" int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode, float lr)
 {
-  if (!d || mode < THORIN_WS_OFF || mode > THORIN_WS_TRAIN || (mode != THORIN_WS_OFF && !n) ||
+  if (!d || mode < THORIN_WS_OFF || mode > THORIN_WS_EXTRAPOLATE ||
+      ((mode == THORIN_WS_PREDICT || mode == THORIN_WS_TRAIN) && !n) ||
       (mode == THORIN_WS_TRAIN && !(lr > 0.f))) {
-    g_last_error = "warmstart: mode OFF/PREDICT/TRAIN, a network unless OFF, lr > 0 to train";
+    g_last_error = "warmstart: mode OFF/PREDICT/TRAIN/EXTRAPOLATE, a network to predict or train, lr > 0 to train";
     return THORIN_ERR_ARG;
   }
+  if (mode == THORIN_WS_EXTRAPOLATE || mode == THORIN_WS_OFF) n = nullptr;
   int f = 1;
   if (n) {
     int nr = 0, ns = 0;
@@ -600,19 +638,34 @@ extern "C" int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode,
       return THORIN_ERR_ARG;
     }
   }
-  if (mode != THORIN_WS_OFF && !d->ws_prev) {
-    RCHK(dalloc(d, (void **)&d->ws_prev, (size_t)d->nr * d->ns * sizeof(double)));
-    RCHK(dalloc(d, (void **)&d->ws_jac, (size_t)d->nr * d->ns * sizeof(double)));
-    CUCHK(cudaMemsetAsync(d->ws_prev, 0, (size_t)d->nr * d->ns * sizeof(double), d->s));
-  }
+  if (mode != THORIN_WS_OFF)
+    RCHK(ws_history(d, mode == THORIN_WS_EXTRAPOLATE ? d->ws_order : 1));
+  if (mode != d->ws_mode && d->ws_dts)             // nothing recorded in the new mode yet
+    CUCHK(cudaMemsetAsync(d->ws_dts, 0, THORIN_WS_MAX_ORDER * sizeof(double), d->s));
   d->ws_f = f;
-  if (d->dt_graph && (d->ws_net != (mode == THORIN_WS_OFF ? nullptr : n) || d->ws_mode != mode)) {
+  if (d->dt_graph && (d->ws_net != n || d->ws_mode != mode)) {
     cudaGraphExecDestroy(d->dt_graph);            // the DT graph holds the warm start's launches or not
     d->dt_graph = nullptr;
   }
-  d->ws_net = mode == THORIN_WS_OFF ? nullptr : n;
+  d->ws_net = n;
   d->ws_mode = mode;
   d->ws_lr = lr;
+  return THORIN_OK;
+}
+
+extern "C" int thorin_gpu_warmstart_order(thorin_disk *d, int order)
+{
+  if (!d || order < 1 || order > THORIN_WS_MAX_ORDER) {
+    g_last_error = "warmstart order: 1 .. THORIN_WS_MAX_ORDER";
+    return THORIN_ERR_ARG;
+  }
+  if (order == d->ws_order) return THORIN_OK;
+  d->ws_order = order;
+  if (d->ws_mode == THORIN_WS_EXTRAPOLATE) RCHK(ws_history(d, order));
+  if (d->dt_graph) {                               // the order is baked into the DT graph's launch
+    cudaGraphExecDestroy(d->dt_graph);
+    d->dt_graph = nullptr;
+  }
   return THORIN_OK;
 }
 
@@ -1504,6 +1557,11 @@ static int sor_solve(thorin_disk *d, double omega, int *niter, int *capped, bool
     RCHK(wn_sor_predict(d->ws_net, d->nr, d->ns, d->ws_f, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm,
                         d->rhs, d->ws_prev, d->ws_jac, d->sor.jscale, omega, nullptr, d->s));
     d->ws_st.predictions++;
+  } else if (learned && d->ws_mode == THORIN_WS_EXTRAPOLATE) {
+    CUCHK(cudaMemcpyAsync(d->tbackup, d->temper, (size_t)d->nr * d->ns * sizeof(double), cudaMemcpyDeviceToDevice,
+                          d->s));
+    RCHK(ws_extrapolate(d->nr, d->ns, d->temper, d->ws_prev, d->ws_order, d->ctl + CTL_DT, d->ws_dts, d->s));
+    d->ws_st.predictions++;
   }
   if (d->timing) CUCHK(cudaEventRecord(d->ev[0], d->s));
   if (d->sor_direct) {
@@ -1645,8 +1703,8 @@ static int energy_step(thorin_disk *d, double dt)
                       d->mljm, d->rhs, d->ws_prev, d->ws_jac, d->ws_lr, d->energy_new, d->s));
     d->ws_st.train_steps++;
   }
-  if (d->ws_net && d->ws_prev)        // this solve's update, an input of the next prediction
-    RCHK(wn_record_update(d->nr, d->ns, d->temper, d->tbackup, d->ws_prev, d->s));
+  if (d->ws_mode != THORIN_WS_OFF && d->ws_prev)   // this solve's update, an input of the next prediction
+    RCHK(wn_record_update(d->nr, d->ns, d->temper, d->tbackup, d->ws_prev, d->ws_nh, d->ctl + CTL_DT, d->ws_dts, d->s));
   d->st.sor_calls++;
   d->st.sor_sweeps += Niter;
   d->st.sor_last_niter = Niter;
@@ -1998,11 +2056,15 @@ static int capture_sor(thorin_disk *d)
   graph_sor_begin(S, d->s);
   hydro_sor_resid0(d->g, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, d->sor, d->s);
   const bool predict = d->ws_net && d->ws_mode == THORIN_WS_PREDICT;
-  if (predict) {          // the learned warm start moves T before the sweeps, as on the host path
+  const bool extrap = d->ws_mode == THORIN_WS_EXTRAPOLATE;
+  if (predict || extrap) {  // the warm start moves T before the sweeps, as on the host path
     CUCHK(cudaMemcpyAsync(d->tbackup, d->temper, (size_t)d->nr * d->ns * sizeof(double), cudaMemcpyDeviceToDevice,
                           d->s));
-    RCHK(wn_sor_predict(d->ws_net, d->nr, d->ns, d->ws_f, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm,
-                        d->rhs, d->ws_prev, d->ws_jac, d->sor.jscale, 0.0, d->ctl + CTL_SOR_OMEGA, d->s));
+    if (predict)
+      RCHK(wn_sor_predict(d->ws_net, d->nr, d->ns, d->ws_f, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm,
+                          d->rhs, d->ws_prev, d->ws_jac, d->sor.jscale, 0.0, d->ctl + CTL_SOR_OMEGA, d->s));
+    else
+      RCHK(ws_extrapolate(d->nr, d->ns, d->temper, d->ws_prev, d->ws_order, d->ctl + CTL_DT, d->ws_dts, d->s));
   }
   cudaStreamCaptureStatus cs;
   cudaGraph_t cg;
@@ -2021,8 +2083,8 @@ static int capture_sor(thorin_disk *d)
   d->capture_sor_body = np.conditional.phGraph_out[0];
   CUCHK(cudaStreamUpdateCaptureDependencies(d->s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
   graph_sor_end(S, d->s);
-  if (predict && d->ws_prev)           // this solve's update, an input of the next prediction
-    RCHK(wn_record_update(d->nr, d->ns, d->temper, d->tbackup, d->ws_prev, d->s));
+  if ((predict || extrap) && d->ws_prev)   // this solve's update, an input of the next prediction
+    RCHK(wn_record_update(d->nr, d->ns, d->temper, d->tbackup, d->ws_prev, d->ws_nh, d->ctl + CTL_DT, d->ws_dts, d->s));
   return THORIN_OK;
 }
 
@@ -2253,7 +2315,8 @@ static int graph_finish(thorin_disk *d, thorin_planets *sys)
   d->st.substeps = g.nsub;
   d->st.crashed = g.crashed;
   d->st.sor_calls += g.sor_calls;
-  if (d->ws_net && d->ws_mode == THORIN_WS_PREDICT) d->ws_st.predictions += g.sor_calls;
+  if ((d->ws_net && d->ws_mode == THORIN_WS_PREDICT) || d->ws_mode == THORIN_WS_EXTRAPOLATE)
+    d->ws_st.predictions += g.sor_calls;
   d->st.sor_sweeps += g.sor_sweeps;
   if (g.sor_calls) { d->st.sor_last_niter = g.sor_last_niter; d->st.sor_omega = g.omega_used; }
   d->st.last_dt = d->ctl_h[CTL_DT];

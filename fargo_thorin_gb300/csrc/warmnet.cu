@@ -27,6 +27,7 @@ constexpr int WN_NL = 8;          // layers: e0 e1 e2 e3 d2 d1 d0 out
 constexpr int WN_NIN = 7;         // input channels used
 constexpr float WN_YSCALE = 32.f; // output unit, in residual scales
 constexpr long long WN_WAIT = 1LL << 26;  // mbarrier polls before giving up
+constexpr int WS_MAXORDER = THORIN_WS_MAX_ORDER;   // longest extrapolated start
 
 struct LayerDef {
   int cin, cout, cinp, coutp;
@@ -824,12 +825,45 @@ __global__ void k_wn_total(double *dscal, float wres, float wsup)
   dscal[0] = (double)wres * dscal[4] + (double)wsup * dscal[5];
 }
 
-// the solve's update tconv - tstart (the previous-update input of the next solve)
+// the solve's update tconv - tstart (the previous-update input of the next
+// solve) into hist[0] and the time step it was made with into dts[0]; the
+// older nh - 1 updates and time steps move one slot back first
 __global__ void k_wn_record(long long n, const double *__restrict__ tconv, const double *__restrict__ tstart,
-                            double *__restrict__ prev)
+                            double *__restrict__ hist, int nh, const double *__restrict__ dt, double *__restrict__ dts)
 {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q < n) prev[q] = tconv[q] - tstart[q];
+  if (q < n) {
+    for (int k = nh - 1; k > 0; k--) hist[k * n + q] = hist[(k - 1) * n + q];
+    hist[q] = tconv[q] - tstart[q];
+  }
+  if (q == 0 && dts) {
+    for (int k = nh - 1; k > 0; k--) dts[k] = dts[k - 1];
+    dts[0] = *dt;
+  }
+}
+
+// Coefficients of the backward-difference extrapolation to the next point of
+// an evenly spaced sequence from its last m values (m = 1..WS_MAXORDER):
+// c_k = (-1)^k binom(m, k+1), e.g. 2, -1 (linear) and 3, -3, 1 (quadratic).
+struct WsCoef { double c[WS_MAXORDER][WS_MAXORDER]; };
+
+// Extrapolated start on the unknowns: this solve's dt times the update rate
+// u / dt extrapolated from the last m recorded solves (m = the order, fewer
+// while fewer are recorded; nothing before the first).  A non-positive
+// result keeps T.
+__global__ void k_ws_extrapolate(int nr, int ns, double *__restrict__ T, const double *__restrict__ hist, int order,
+                                 const double *__restrict__ dt, const double *__restrict__ dts, WsCoef cf)
+{
+  const long long n = (long long)(nr - 2) * ns, cells = (long long)nr * ns;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  int m = 0;
+  while (m < order && dts[m] > 0.0) m++;
+  if (q >= n || m == 0) return;
+  const long long l = q + ns;
+  double rate = 0.0;
+  for (int k = 0; k < m; k++) rate += cf.c[m - 1][k] * (hist[k * cells + l] / dts[k]);
+  const double t = T[l] + *dt * rate;
+  if (t > 0.0) T[l] = t;
 }
 
 inline unsigned nblk(long long n, int bs = 256) { return (unsigned)((n + bs - 1) / bs); }
@@ -1122,14 +1156,36 @@ int wn_sor_train(thorin_warmnet *n, int nr, int ns, int fc, const double *tk, co
   return e == cudaSuccess ? THORIN_OK : wn_fail("training kernels", e);
 }
 
-// prev = tconv - tstart over nr x ns cells
-int wn_record_update(int nr, int ns, const double *tconv, const double *tstart, double *prev, cudaStream_t s)
+// hist[0] = tconv - tstart over nr x ns cells and dts[0] = *dt, after the
+// older nh - 1 entries move one slot back
+int wn_record_update(int nr, int ns, const double *tconv, const double *tstart, double *hist, int nh,
+                     const double *dt, double *dts, cudaStream_t s)
 {
   const long long cells = (long long)nr * ns;
-  k_wn_record<<<nblk(cells), 256, 0, s>>>(cells, tconv, tstart, prev);
+  k_wn_record<<<nblk(cells), 256, 0, s>>>(cells, tconv, tstart, hist, nh, dt, dts);
   g_thorin_launches++;
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? THORIN_OK : wn_fail("record kernel", e);
+}
+
+// T (start of the solve) -> T + dt * (update rate extrapolated from the
+// last `order` recorded solves)
+int ws_extrapolate(int nr, int ns, double *T, const double *hist, int order, const double *dt, const double *dts,
+                   cudaStream_t s)
+{
+  if (order < 1 || order > WS_MAXORDER) return THORIN_ERR_ARG;
+  WsCoef cf = {};
+  for (int m = 1; m <= WS_MAXORDER; m++) {
+    double b = 1.0;                                 // binom(m, k + 1), built up along k
+    for (int k = 0; k < m; k++) {
+      b = b * (double)(m - k) / (double)(k + 1);
+      cf.c[m - 1][k] = (k & 1) ? -b : b;
+    }
+  }
+  k_ws_extrapolate<<<nblk((long long)(nr - 2) * ns), 256, 0, s>>>(nr, ns, T, hist, order, dt, dts, cf);
+  g_thorin_launches++;
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? THORIN_OK : wn_fail("extrapolation kernel", e);
 }
 
 // total, residual and supervised loss of the last training step

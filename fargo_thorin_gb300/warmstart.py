@@ -25,7 +25,7 @@ from . import _lib
 
 NPARAMS = 57825
 INPUTS = 16
-OFF, PREDICT, TRAIN = 0, 1, 2
+OFF, PREDICT, TRAIN, EXTRAPOLATE = 0, 1, 2, 3
 EARTH = 3.0e-6                         # Earth mass in solar masses
 # (cin, cout) per layer: e0 e1 e2 e3 d2 d1 d0 out
 LAYERS = [(7, 32)] + [(32, 32)] * 6 + [(32, 1)]
@@ -126,9 +126,16 @@ class WarmNet:
 
 
 def attach(disk, net: WarmNet | None, mode: int, lr: float = 0.0):
-    """Attach net to disk (PREDICT or TRAIN) or detach (OFF)."""
+    """Attach net to disk (PREDICT or TRAIN), start every solve from the
+    previous solve's update (EXTRAPOLATE, net None) or detach (OFF)."""
     h = net.h if net is not None else C.c_void_p()
     _lib.check(disk.L.thorin_gpu_warmstart(disk.h, h, mode, lr), "thorin_gpu_warmstart")
+
+
+def set_order(disk, order: int):
+    """Order of the EXTRAPOLATE start (1 .. 4): the update rate of the last
+    `order` solves extrapolated to the next one."""
+    _lib.check(disk.L.thorin_gpu_warmstart_order(disk.h, order), "thorin_gpu_warmstart_order")
 
 
 class WsStats(C.Structure):

@@ -42,6 +42,8 @@ extern "C" {
 #define THORIN_WS_OFF      0     /* plain SOR (the reference's method)          */
 #define THORIN_WS_PREDICT  1     /* warm-start every SOR solve from the network */
 #define THORIN_WS_TRAIN    2     /* plain SOR; each solve then trains the net   */
+#define THORIN_WS_EXTRAPOLATE 3  /* start from T_old + the extrapolated update  */
+#define THORIN_WS_MAX_ORDER 4    /* longest extrapolation (recorded solves)      */
 
 typedef struct thorin_warmnet thorin_warmnet;
 
@@ -85,8 +87,20 @@ int thorin_warmnet_adam(thorin_warmnet *n, float lr, float beta1, float beta2, f
  * start temperature T_k is
  *   mean((A T_pred - rhs)^2) / mean|A T_k - rhs|^2 + 0.1 mean((y - target)^2)
  * over the unknowns, T_pred = T_k + Jacobi step + the prediction and target
- * the converged update beyond the Jacobi step in the network's units. */
+ * the converged update beyond the Jacobi step in the network's units.
+ * EXTRAPOLATE (no network, n ignored): every SOR solve starts from
+ *   T_old + dt * r,
+ * r the update rate (T_conv - T_start) / dt of the last m solves extrapolated
+ * to this one as an evenly spaced sequence (m = the order, 2 unless set:
+ * r = 2 r_1 - r_2; order 1 takes r = r_1, order 3 r = 3 r_1 - 3 r_2 + r_3).
+ * While fewer than m solves are recorded since attaching the order is what
+ * they allow, and the first solve starts from T_old.  A cell whose start is
+ * not positive keeps T_old.  In every mode the exit tests and the threshold
+ * (eps times the L1 residual of T_old) are the plain solve's. */
 int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode, float lr);
+
+/* Order of the EXTRAPOLATE start, 1 .. THORIN_WS_MAX_ORDER (default 2). */
+int thorin_gpu_warmstart_order(thorin_disk *d, int order);
 
 /* Layout check of the tensor-core path: D[128][32] = A[128][64] * B[32][64]^T
  * with bf16 bit patterns a, b (row-major) and FP32 d, on one CTA. */
