@@ -276,8 +276,9 @@ def combined_phase(n_each=8, ndt=1, settle=1, seed=11):
     ndt DTs then run (a) batched: every disk a
     device-resident DT graph, all launched together, each with the learned
     SOR warm start attached, and (b) plain: the disks one after the other on
-    the host path without the network.  Cell-updates/s, the speed-up of (a)
-    over (b) and the SOR sweeps per solve of both."""
+    the host path without the network, and (c) as (a) with the extrapolated
+    SOR start in place of the network.  Cell-updates/s, the speed-ups of (a)
+    and (c) over (b) and the SOR sweeps per solve of each."""
     from fargo_thorin_gb300 import warmstart as WS
     from fargo_thorin_gb300.ensemble import Ensemble
     t_setup = time.perf_counter()
@@ -306,6 +307,15 @@ def combined_phase(n_each=8, ndt=1, settle=1, seed=11):
     for dd, net in zip(ens.disks, nets):
         WS.attach(dd, None, WS.OFF)
         net.close()
+    # (c) batched with the extrapolated start instead of the network
+    ens.restore(snaps)
+    for dd in ens.disks:
+        WS.attach(dd, None, WS.EXTRAPOLATE)
+    calls0 = sum(dd.stats().sor_calls for dd in ens.disks)
+    c = ens.run_schedule({"mode": "graph"}, ndt)
+    c_calls = sum(dd.stats().sor_calls for dd in ens.disks) - calls0
+    for dd in ens.disks:
+        WS.attach(dd, None, WS.OFF)
     ens.restore(snaps)
     calls0 = sum(dd.stats().sor_calls for dd in ens.disks)
     b = ens.run_schedule({"mode": "sequential"}, ndt)
@@ -317,6 +327,10 @@ def combined_phase(n_each=8, ndt=1, settle=1, seed=11):
            "speedup_vs_sequential_plain": (a["cell_updates"] / a["seconds"]) / (b["cell_updates"] / b["seconds"]),
            "sweeps_per_solve_batched_learned": a["sweeps"] / max(a_calls, 1),
            "sweeps_per_solve_sequential_plain": b["sweeps"] / max(b_calls, 1),
+           "batched_extrapolated": {"value": c["cell_updates"] / c["seconds"], "ms_per_dt": 1e3 * c["seconds"] / ndt,
+                                    "speedup_vs_sequential_plain": (c["cell_updates"] / c["seconds"]) /
+                                                                   (b["cell_updates"] / b["seconds"]),
+                                    "sweeps_per_solve": c["sweeps"] / max(c_calls, 1)},
            "warm_start": os.path.relpath(WARMNET, ROOT) if params is not None else None,
            "setup_s": t_setup, "settle_dts": settle,
            "timing": "wall clock with a device synchronisation on both sides; both runs replay the same DTs from "

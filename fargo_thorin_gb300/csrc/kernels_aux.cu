@@ -769,27 +769,34 @@ void aux_forces(const DevGrid &g, const ForceArgs &a0, const ForceRings &fr,
 // The annulus [imin, imax] holding the Hill sphere is searched; cells within
 // the effective accretion radius give up pebbles up to the model rate.
 
-__device__ double trapzd_col(int n, double a, double b, double H2, double *state)
+// Trapzd and IntegrateColumnMass (Pebbles.c:302-349) for one cell, evaluated
+// by a whole warp: the it = 2^(n-2) midpoints of level n are spread over the
+// lanes (lane k takes points k, k + 32, ...), point j at a + (j + 1/2)
+// spacing, and the level's sum is an xor butterfly over the lanes' partial
+// sums, so every lane holds the same bits of the integral and takes the same
+// exit.  The levels, the refinement integral = (integral + (b - a) sum / it)
+// / 2 and the exit test after level 5 are the reference's; only the order of
+// the midpoint sum and the rounding of the abscissae differ from its
+// sequential loop (x += spacing), by relative amounts of order 1e-16.  Before
+// this the reference's loop ran in one thread per cell, up to 2^14
+// dependent exponentials each.
+__device__ double column_mass_warp(double a, double b, double Hpeb)
 {
-  if (n == 1) {
-    *state = 0.5 * (b - a) * (exp(-0.5 * a * a / H2) + exp(-0.5 * b * b / H2));
-    return *state;
-  }
-  int it = 1;
-  for (int j = 1; j < n - 1; j++) it <<= 1;
-  const double iter = it, spacing = (b - a) / iter;
-  double x = a + 0.5 * spacing, sum = 0.0;
-  for (int j = 1; j <= it; j++) { sum += exp(-0.5 * x * x / H2); x += spacing; }
-  *state = 0.5 * (*state + (b - a) * sum / iter);
-  return *state;
-}
-
-__device__ double column_mass(double a, double b, double Hpeb)
-{
-  double integral = 0.0, iold = 0.0, st = 0.0;
+  const int lane = threadIdx.x & 31;
   const double H2 = Hpeb * Hpeb;
-  for (int n = 1; n <= 16; n++) {
-    integral = trapzd_col(n, a, b, H2, &st);
+  double integral = 0.5 * (b - a) * (exp(div_fast(-0.5 * a * a, H2)) + exp(div_fast(-0.5 * b * b, H2)));
+  double iold = integral;
+  for (int n = 2; n <= 16; n++) {
+    const int it = 1 << (n - 2);
+    const double iter = it, spacing = (b - a) / iter;
+    double sum = 0.0;
+    for (int j = lane; j < it; j += 32) {
+      const double x = a + ((double)j + 0.5) * spacing;
+      sum += exp(div_fast(-0.5 * x * x, H2));
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) sum += __shfl_xor_sync(TH_FULL, sum, o);
+    integral = 0.5 * (integral + (b - a) * sum / iter);
     if (n > 5)
       if (fabs(integral - iold) < 1.0e-4 * fabs(iold) || (integral == 0.0 && iold == 0.0)) return integral;
     iold = integral;
@@ -849,30 +856,83 @@ __global__ void __launch_bounds__(ACC_BX) k_acc_reff(DevGrid g, const AccArgs *_
   }
 }
 
+// Annulus cell q (0 .. (imax - imin + 1) ns - 1) of the accretion step: true
+// when its midplane distance to the planet is within the effective accretion
+// radius, with the pebble scale height and the column's ends inside the
+// sphere (Pebbles.c:445-453).  The operations are spelled out as
+// round-to-nearest intrinsics so that the two kernels that call this get the
+// same bits.
+__device__ __forceinline__ bool acc_cell(const DevGrid &g, const AccArgs &a, int q, int &i, int &l, double &Hpeb,
+                                         double &zmin, double &zmax)
+{
+  const int ns = g.ns;
+  i = a.imin + q / ns;
+  const int j = q - (q / ns) * ns;
+  l = j + i * ns;
+  const double Reff = a.acc[0], Reff2 = __dmul_rn(Reff, Reff);
+  const double dx = __dsub_rn(__dmul_rn(g.r.Rmed[i], g.r.costab[j]), a.Xp);
+  const double dy = __dsub_rn(__dmul_rn(g.r.Rmed[i], g.r.sintab[j]), a.Yp);
+  const double R2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+  if (!(R2 <= Reff2)) return false;
+  const double H = __dmul_rn(__dmul_rn(a.cs[l], g.r.OmegaInv[i]), g.k.sqrt_adiabind_inv);
+  Hpeb = __dmul_rn(H, __dsqrt_rn(__ddiv_rn(a.pebble_alpha, a.tau[l])));
+  const double h = __dsqrt_rn(__dsub_rn(Reff2, R2));
+  zmin = __dsub_rn(a.Zp, h);
+  zmax = __dadd_rn(a.Zp, h);
+  return true;
+}
+
+// Column integrals of the annulus cells inside the sphere (IntegrateColumnMass
+// of Pebbles.c:456), one warp per cell, into macc[l] (zero outside the
+// accretion step).  Warp w of the grid takes the annulus cells w, w + W,
+// w + 2W, ... (W warps in all), 32 of them tested at a time, so the cells of
+// the sphere, which lie together around the planet, fall on many
+// multiprocessors.
+__global__ void __launch_bounds__(ACC_BX) k_acc_column(DevGrid g, const AccArgs *__restrict__ ap)
+{
+  const AccArgs &a = *ap;
+  if (a.nb == 0) return;                         // no annulus
+  const int ncells = (a.imax - a.imin + 1) * g.ns;
+  const int lane = threadIdx.x & 31;
+  const int nw = gridDim.x * (ACC_BX / 32);
+  const int gw = blockIdx.x * (ACC_BX / 32) + (threadIdx.x >> 5);
+  for (long long base = gw; base < ncells; base += 32LL * nw) {   // warp-uniform
+    const long long c = base + (long long)lane * nw;
+    int i = 0, l = 0;
+    double Hpeb = 0.0, zmin = 0.0, zmax = 0.0;
+    const bool inside = c < ncells && acc_cell(g, a, (int)c, i, l, Hpeb, zmin, zmax);
+    unsigned bal = __ballot_sync(TH_FULL, inside);
+    while (bal) {
+      const int src = __ffs(bal) - 1;
+      bal &= bal - 1u;
+      const double cm = column_mass_warp(__shfl_sync(TH_FULL, zmin, src), __shfl_sync(TH_FULL, zmax, src),
+                                         __shfl_sync(TH_FULL, Hpeb, src));
+      if (lane == src) a.macc[l] = cm;
+    }
+  }
+}
+
+// Upper limit of the mass each annulus cell inside the sphere can give up
+// (Pebbles.c:454-462), from its column integral (k_acc_column), and the
+// block partials of the limit, the scale height, the pebble density and the
+// cell count.
 __global__ void __launch_bounds__(ACC_BX) k_acc_upper(DevGrid g, const AccArgs *__restrict__ ap)
 {
   const AccArgs &a = *ap;
   if ((int)blockIdx.x >= a.nb) return;           // grid sized for the widest annulus
-  const int ns = g.ns;
-  const int ncells = (a.imax - a.imin + 1) * ns;
+  const int ncells = (a.imax - a.imin + 1) * g.ns;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  const double Reff = a.acc[0], Reff2 = Reff * Reff;
   double dmu = 0.0, hpm = 0.0, pdm = 0.0, nc = 0.0;
-  if (q < ncells) {
-    const int i = a.imin + q / ns, j = q - (q / ns) * ns, l = j + i * ns;
-    const double xc = g.r.Rmed[i] * g.r.costab[j], yc = g.r.Rmed[i] * g.r.sintab[j];
-    const double R2 = (xc - a.Xp) * (xc - a.Xp) + (yc - a.Yp) * (yc - a.Yp);
-    if (R2 <= Reff2) {
-      const double H = a.cs[l] * g.r.OmegaInv[i] * g.k.sqrt_adiabind_inv;
-      const double Hpeb = H * sqrt(a.pebble_alpha / a.tau[l]);
-      const double zmin = a.Zp - sqrt(Reff2 - R2), zmax = a.Zp + sqrt(Reff2 - R2);
-      const double mcell = g.r.Surf[i] * a.pdens[l];
-      const double vdp = a.pdens[l] / Hpeb * g.k.sqrt2pi_inv;
-      double dM = vdp * g.r.Surf[i] * column_mass(zmin, zmax, Hpeb);
-      if (dM > mcell) dM = 0.99999999 * mcell;
-      a.macc[l] = dM;
-      dmu = dM; hpm = Hpeb; pdm = a.pdens[l]; nc = 1.0;
-    }
+  int i = 0, l = 0;
+  double Hpeb = 0.0, zmin = 0.0, zmax = 0.0;
+  if (q < ncells && acc_cell(g, a, q, i, l, Hpeb, zmin, zmax)) {
+    const double pd = a.pdens[l];
+    const double mcell = g.r.Surf[i] * pd;
+    const double vdp = pd / Hpeb * g.k.sqrt2pi_inv;
+    double dM = vdp * g.r.Surf[i] * a.macc[l];
+    if (dM > mcell) dM = 0.99999999 * mcell;
+    a.macc[l] = dM;
+    dmu = dM; hpm = Hpeb; pdm = pd; nc = 1.0;
   }
   dmu = block_reduce(dmu, OpAdd(), 0.0);
   hpm = block_reduce(hpm, OpAdd(), 0.0);
@@ -978,6 +1038,8 @@ void aux_accrete_kernels(const DevGrid &g, const AccArgs *a_dev, int nb_grid, do
   k_acc_tau<<<nb_grid, ACC_BX, 0, s>>>(g, a_dev);
   g_thorin_launches++;
   k_acc_reff<<<1, ACC_BX, 0, s>>>(g, a_dev);
+  g_thorin_launches++;
+  k_acc_column<<<2 * g.nsm, ACC_BX, 0, s>>>(g, a_dev);
   g_thorin_launches++;
   k_acc_upper<<<nb_grid, ACC_BX, 0, s>>>(g, a_dev);
   g_thorin_launches++;

@@ -1118,19 +1118,24 @@ __global__ void __launch_bounds__(AZ_TMAX) k_azimuthal(DevGrid g, AziIO io, cons
     const double ksi = v * dt;
     const bool up = ksi > 0.0;                     // upwind cell of the left face is j-1
     // face value q* = q_up +/- (dxtheta -/+ ksi) dq_up with the slope dq kept
-    // without its 1/dxtheta factor, which goes into cs instead
-    const double cs = (up ? (dxtheta - ksi) : (dxtheta + ksi)) * invdxtheta;
+    // without its 1/dxtheta factor, which goes into cs instead.  The upwind
+    // choice differs between neighbouring cells, so it selects operands
+    // (integer moves) and every face value is one FMA, fma(+/-cs, dq_up,
+    // q_up), rather than two predicated ones.
+    const double cs = (dxtheta + (up ? -ksi : ksi)) * invdxtheta;
+    const double csg = __hiloint2double(__double2hiint(cs) ^ (up ? 0 : (int)0x80000000), __double2loint(cs));
     // RhoStar at the left face (ComputeStarTheta of the density)
     const double rho = q[NQ - 1];
     s_a[t] = rho;
     __syncthreads();
-    const double drm = rho - s_a[tm];
+    const double rho_m = s_a[tm];
+    const double drm = rho - rho_m;
     s_b[t] = drm;
     __syncthreads();
     const double drho = azi_vl_slope_d(drm, s_b[tp]);
     s_c[t] = drho;
     __syncthreads();
-    const double rs = up ? __fma_rn(cs, s_c[tm], s_a[tm]) : __fma_rn(-cs, drho, rho);
+    const double rs = __fma_rn(csg, up ? s_c[tm] : drho, up ? rho_m : rho);
     const double cf = dxrad * rs * v;              // flux = dxrad Q* RhoStar v
     const double rcp = div_fast(1.0, rho + 1e-20); // 1 / (RhoInt + 1e-20)
     __syncthreads();
@@ -1140,19 +1145,20 @@ __global__ void __launch_bounds__(AZ_TMAX) k_azimuthal(DevGrid g, AziIO io, cons
       const double w = q[k] * rcp;
       s_a[t] = w;
       __syncthreads();
+      const double w_m = s_a[tm];
       double qs;
       if (k < NQ - 1) {
-        const double dm = w - s_a[tm];
+        const double dm = w - w_m;
         s_b[t] = dm;
         __syncthreads();
         const double dq = azi_vl_slope_d(dm, s_b[tp]);
         s_c[t] = dq;
         __syncthreads();
-        qs = up ? __fma_rn(cs, s_c[tm], s_a[tm]) : __fma_rn(-cs, dq, w);
+        qs = __fma_rn(csg, up ? s_c[tm] : dq, up ? w_m : w);
       } else {
         // the density's own quotient rho / (rho + 1e-20) is 1 to within
         // 1e-20 / rho: its slope term is below rounding
-        qs = up ? s_a[tm] : w;
+        qs = up ? w_m : w;
       }
       const double F = qs * cf;
       s_b[t] = F;                                  // every read of s_b is behind a barrier
