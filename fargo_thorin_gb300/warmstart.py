@@ -205,9 +205,10 @@ def compare_sweeps(net: WarmNet, draw: dict, ndt: int, seed: int = 12345, dt_div
     """SOR sweeps per solve of the same disk run plain and with the network
     (PREDICT), after `warm` DTs that include the omega calibration.  Also
     returns the relative L2 difference of the temperatures after the first
-    compared DT (both solves meet the same residual threshold)."""
+    compared DT and after the last (both solves meet the same residual
+    threshold)."""
     out = {}
-    temps = {}
+    temps, lasts = {}, {}
     for mode in (OFF, PREDICT):
         p, d, sys_ = make_training_disk(net.disk_nr, net.disk_ns, draw, seed=seed, dt_div=dt_div)
         for _ in range(warm):
@@ -219,6 +220,7 @@ def compare_sweeps(net: WarmNet, draw: dict, ndt: int, seed: int = 12345, dt_div
             d.algogas(sys_)
             if k == 0:
                 temps[mode] = d.get(8)
+        lasts[mode] = d.get(8)
         s1 = d.stats()
         out["plain" if mode == OFF else "learned"] = (s1.sor_sweeps - sweeps0) / max(s1.sor_calls - calls0, 1)
         out["solves"] = s1.sor_calls - calls0
@@ -228,6 +230,8 @@ def compare_sweeps(net: WarmNet, draw: dict, ndt: int, seed: int = 12345, dt_div
         d.close()
     a, b = temps[OFF], temps[PREDICT]
     out["t_rel_l2"] = float(np.linalg.norm(a - b) / np.linalg.norm(a))
+    a, b = lasts[OFF], lasts[PREDICT]
+    out["t_rel_l2_last"] = float(np.linalg.norm(a - b) / np.linalg.norm(a))
     return out
 
 

@@ -210,6 +210,20 @@ def test_trained_network_saves_sweeps_on_the_disk1_workload():
 
 
 @pytest.mark.gpu
+@pytest.mark.skipif(not os.path.exists(WEIGHTS), reason="no trained network file")
+def test_learned_start_stays_on_the_plain_solution_over_several_dts():
+    """Over 5 DTs (40 solves) of the disk1 workload the learned start's
+    temperatures stay within 1e-9 of the plain run's: every solve meets the
+    plain solve's threshold, so the difference does not grow with the DTs."""
+    from fargo_thorin_gb300 import workloads
+    net = WS.WarmNet(1024, 3072, params=WS.WarmNet.load_params(WEIGHTS))
+    r = WS.compare_sweeps(net, {"alpha": 1.0e-3, "aspect": 0.05, "mplanet": workloads.PLANET1[0]}, ndt=5, warm=2)
+    print(r)
+    assert r["learned"] < r["plain"]
+    assert r["t_rel_l2"] < 1e-9 and r["t_rel_l2_last"] < 1e-9
+
+
+@pytest.mark.gpu
 def test_training_residual_uses_the_disks_packed_system():
     """The warm start reads the disk's SOR system, which k_matrix stores
     colour-packed.  With a zero output layer the prediction is the start plus
