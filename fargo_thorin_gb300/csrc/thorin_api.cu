@@ -27,7 +27,8 @@ int wn_sor_train(thorin_warmnet *n, int nr, int ns, int fc, const double *tk, co
 int wn_record_update(int nr, int ns, const double *tconv, const double *tstart, double *hist, int nh,
                      const double *dt, double *dts, cudaStream_t s);
 int ws_extrapolate(int nr, int ns, double *T, const double *hist, int order, const double *dt, const double *dts,
-                   cudaStream_t s);
+                   const double *ml, const double *mlip, const double *mlim, const double *mljp, const double *mljm,
+                   const double *rhs, double *scratch, double *part, double *step, int nsm, cudaStream_t s);
 int wn_last_loss(thorin_warmnet *n, double *loss);
 int wn_dims(const thorin_warmnet *n, int *nr, int *ns);
 
@@ -186,12 +187,14 @@ struct thorin_disk {
   thorin_warmnet *ws_net = nullptr;
   int ws_mode = THORIN_WS_OFF;
   float ws_lr = 0.f;
-  thorin_ws_stats ws_st = {0, 0, 0.0, 0.0, 0.0};
+  thorin_ws_stats ws_st = {0, 0, 0.0, 0.0, 0.0, 0.0};
   // the last ws_nh solves' updates T_conv - T_start, newest first (slot 0
   // is the network's input), and their time steps (THORIN_WS_MAX_ORDER
   // device doubles, 0 = not recorded)
   double *ws_prev = nullptr;
   double *ws_dts = nullptr;
+  double *ws_part = nullptr;     // block partials of the extrapolated start's step length (4 nsm + 2)
+  double *ws_step = nullptr;     // its step length and the running sum of the steps
   int ws_nh = 0;                 // slots of ws_prev
   int ws_order = 2;              // order of the extrapolated start
   double *ws_jac = nullptr;      // the Jacobi step of the solve's start, per cell
@@ -600,6 +603,8 @@ static int ws_history(thorin_disk *d, int nh)
   if (!d->ws_jac) {
     RCHK(dalloc(d, (void **)&d->ws_jac, cells * sizeof(double)));
     RCHK(dalloc(d, (void **)&d->ws_dts, THORIN_WS_MAX_ORDER * sizeof(double)));
+    RCHK(dalloc(d, (void **)&d->ws_part, (size_t)(4 * d->g.nsm + 2) * sizeof(double)));
+    RCHK(dalloc(d, (void **)&d->ws_step, 2 * sizeof(double)));
   }
   if (nh <= d->ws_nh) return THORIN_OK;
   if (d->ws_prev) {
@@ -680,6 +685,7 @@ extern "C" int thorin_gpu_warmstart_stats(thorin_disk *d, thorin_ws_stats *out)
     d->ws_st.last_res_loss = l[1];
     d->ws_st.last_sup_loss = l[2];
   }
+  if (d->ws_step) CUCHK(cudaMemcpy(&d->ws_st.step_sum, d->ws_step + 1, sizeof(double), cudaMemcpyDeviceToHost));
   *out = d->ws_st;
   return THORIN_OK;
 }
@@ -1560,7 +1566,8 @@ static int sor_solve(thorin_disk *d, double omega, int *niter, int *capped, bool
   } else if (learned && d->ws_mode == THORIN_WS_EXTRAPOLATE) {
     CUCHK(cudaMemcpyAsync(d->tbackup, d->temper, (size_t)d->nr * d->ns * sizeof(double), cudaMemcpyDeviceToDevice,
                           d->s));
-    RCHK(ws_extrapolate(d->nr, d->ns, d->temper, d->ws_prev, d->ws_order, d->ctl + CTL_DT, d->ws_dts, d->s));
+    RCHK(ws_extrapolate(d->nr, d->ns, d->temper, d->ws_prev, d->ws_order, d->ctl + CTL_DT, d->ws_dts, d->ml, d->mlip,
+                          d->mlim, d->mljp, d->mljm, d->rhs, d->ws_jac, d->ws_part, d->ws_step, d->g.nsm, d->s));
     d->ws_st.predictions++;
   }
   if (d->timing) CUCHK(cudaEventRecord(d->ev[0], d->s));
@@ -2064,7 +2071,8 @@ static int capture_sor(thorin_disk *d)
       RCHK(wn_sor_predict(d->ws_net, d->nr, d->ns, d->ws_f, d->temper, d->ml, d->mlip, d->mlim, d->mljp, d->mljm,
                           d->rhs, d->ws_prev, d->ws_jac, d->sor.jscale, 0.0, d->ctl + CTL_SOR_OMEGA, d->s));
     else
-      RCHK(ws_extrapolate(d->nr, d->ns, d->temper, d->ws_prev, d->ws_order, d->ctl + CTL_DT, d->ws_dts, d->s));
+      RCHK(ws_extrapolate(d->nr, d->ns, d->temper, d->ws_prev, d->ws_order, d->ctl + CTL_DT, d->ws_dts, d->ml, d->mlip,
+                          d->mlim, d->mljp, d->mljm, d->rhs, d->ws_jac, d->ws_part, d->ws_step, d->g.nsm, d->s));
   }
   cudaStreamCaptureStatus cs;
   cudaGraph_t cg;

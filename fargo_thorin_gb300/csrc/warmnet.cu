@@ -847,22 +847,76 @@ __global__ void k_wn_record(long long n, const double *__restrict__ tconv, const
 // c_k = (-1)^k binom(m, k+1), e.g. 2, -1 (linear) and 3, -3, 1 (quadratic).
 struct WsCoef { double c[WS_MAXORDER][WS_MAXORDER]; };
 
-// Extrapolated start on the unknowns: this solve's dt times the update rate
-// u / dt extrapolated from the last m recorded solves (m = the order, fewer
-// while fewer are recorded; nothing before the first).  A non-positive
-// result keeps T.
-__global__ void k_ws_extrapolate(int nr, int ns, double *__restrict__ T, const double *__restrict__ hist, int order,
-                                 const double *__restrict__ dt, const double *__restrict__ dts, WsCoef cf)
+// The extrapolated update u = dt r over all cells, r the update rate u_k /
+// dt_k of the last m recorded solves extrapolated to this one (m = the
+// order, fewer while fewer are recorded; u = 0 before the first).
+__global__ void k_ws_delta(long long cells, const double *__restrict__ hist, int order, const double *__restrict__ dt,
+                           const double *__restrict__ dts, WsCoef cf, double *__restrict__ u)
 {
-  const long long n = (long long)(nr - 2) * ns, cells = (long long)nr * ns;
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= cells) return;
   int m = 0;
   while (m < order && dts[m] > 0.0) m++;
-  if (q >= n || m == 0) return;
-  const long long l = q + ns;
   double rate = 0.0;
-  for (int k = 0; k < m; k++) rate += cf.c[m - 1][k] * (hist[k * cells + l] / dts[k]);
-  const double t = T[l] + *dt * rate;
+  for (int k = 0; k < m; k++) rate += cf.c[m - 1][k] * (hist[k * cells + q] / dts[k]);
+  u[q] = *dt * rate;
+}
+
+// Step length along u that minimises the L2 norm of the residual
+// R(T + s u) = R(T) + s A u over the unknowns: block partials of
+// sum R(T) (A u) and sum (A u)^2, grid-stride, fixed order.
+__global__ void k_ws_line(int nr, int ns, const double *__restrict__ T, const double *__restrict__ u, SorSys m,
+                          double *__restrict__ part)
+{
+  double ra = 0.0, aa = 0.0;
+  const long long n = (long long)(nr - 2) * ns;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(k / ns), j = (int)(k % ns);
+    const size_t pq = sor_pidx(i, j, ns >> 1);
+    const double r = sor_resid(T, m, ns, i, j, pq);
+    const int l = j + i * ns;
+    const int ljp = (j == ns - 1) ? i * ns : l + 1, ljm = (j == 0) ? i * ns + ns - 1 : l - 1;
+    const double au = u[l] * m.ml[pq] + u[l + ns] * m.mlip[pq] + u[l - ns] * m.mlim[pq] + u[ljp] * m.mljp[pq] +
+                      u[ljm] * m.mljm[pq];
+    ra += r * au;
+    aa += au * au;
+  }
+  ra = block_reduce(ra, OpAdd(), 0.0);
+  if (threadIdx.x == 0) part[blockIdx.x] = ra;
+  aa = block_reduce(aa, OpAdd(), 0.0);
+  if (threadIdx.x == 0) part[gridDim.x + blockIdx.x] = aa;
+}
+
+// s = -sum R (A u) / sum (A u)^2, kept in [0, 2] (0 when A u vanishes);
+// out[0] = s, out[1] += s (a running sum for the statistics)
+__global__ void k_ws_step(const double *__restrict__ part, int nb, double *__restrict__ out)
+{
+  double ra = 0.0, aa = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    ra += part[b];
+    aa += part[nb + b];
+  }
+  ra = block_reduce(ra, OpAdd(), 0.0);
+  __syncthreads();
+  aa = block_reduce(aa, OpAdd(), 0.0);
+  if (threadIdx.x == 0) {
+    double st = aa > 0.0 ? -ra / aa : 0.0;
+    st = st > 2.0 ? 2.0 : (st > 0.0 ? st : 0.0);     // also maps NaN to 0
+    out[0] = st;
+    out[1] += st;
+  }
+}
+
+// T += s u on the unknowns; a non-positive result keeps T
+__global__ void k_ws_apply(int nr, int ns, double *__restrict__ T, const double *__restrict__ u,
+                           const double *__restrict__ step)
+{
+  const long long n = (long long)(nr - 2) * ns;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const double st = *step;
+  if (q >= n || st == 0.0) return;
+  const long long l = q + ns;
+  const double t = __fma_rn(st, u[l], T[l]);
   if (t > 0.0) T[l] = t;
 }
 
@@ -1168,10 +1222,12 @@ int wn_record_update(int nr, int ns, const double *tconv, const double *tstart, 
   return e == cudaSuccess ? THORIN_OK : wn_fail("record kernel", e);
 }
 
-// T (start of the solve) -> T + dt * (update rate extrapolated from the
-// last `order` recorded solves)
+// T (start of the solve) -> T + s u: u the update extrapolated from the last
+// `order` recorded solves (into scratch), s the step that minimises the L2
+// residual along u (part: 4 nsm + 2 doubles; step: s and its running sum).
 int ws_extrapolate(int nr, int ns, double *T, const double *hist, int order, const double *dt, const double *dts,
-                   cudaStream_t s)
+                   const double *ml, const double *mlip, const double *mlim, const double *mljp, const double *mljm,
+                   const double *rhs, double *scratch, double *part, double *step, int nsm, cudaStream_t s)
 {
   if (order < 1 || order > WS_MAXORDER) return THORIN_ERR_ARG;
   WsCoef cf = {};
@@ -1182,10 +1238,16 @@ int ws_extrapolate(int nr, int ns, double *T, const double *hist, int order, con
       cf.c[m - 1][k] = (k & 1) ? -b : b;
     }
   }
-  k_ws_extrapolate<<<nblk((long long)(nr - 2) * ns), 256, 0, s>>>(nr, ns, T, hist, order, dt, dts, cf);
-  g_thorin_launches++;
+  const long long cells = (long long)nr * ns;
+  const SorSys m{ml, mlip, mlim, mljp, mljm, rhs};
+  const int nb = 2 * nsm;
+  k_ws_delta<<<nblk(cells), 256, 0, s>>>(cells, hist, order, dt, dts, cf, scratch);
+  k_ws_line<<<nb, 256, 0, s>>>(nr, ns, T, scratch, m, part);
+  k_ws_step<<<1, 256, 0, s>>>(part, nb, step);
+  k_ws_apply<<<nblk((long long)(nr - 2) * ns), 256, 0, s>>>(nr, ns, T, scratch, step);
+  g_thorin_launches += 4;
   const cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? THORIN_OK : wn_fail("extrapolation kernel", e);
+  return e == cudaSuccess ? THORIN_OK : wn_fail("extrapolation kernels", e);
 }
 
 // total, residual and supervised loss of the last training step

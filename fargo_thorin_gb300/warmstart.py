@@ -140,7 +140,7 @@ def set_order(disk, order: int):
 
 class WsStats(C.Structure):
     _fields_ = [("predictions", C.c_longlong), ("train_steps", C.c_longlong), ("last_loss", C.c_double),
-                ("last_res_loss", C.c_double), ("last_sup_loss", C.c_double)]
+                ("last_res_loss", C.c_double), ("last_sup_loss", C.c_double), ("step_sum", C.c_double)]
 
 
 def stats(disk) -> WsStats:

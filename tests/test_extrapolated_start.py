@@ -75,6 +75,31 @@ def test_extrapolated_start_meets_the_same_threshold_with_fewer_sweeps():
     d.close()
 
 
+def test_step_length_keeps_the_start_no_worse_in_a_transient():
+    """From the set-up's start (the first DTs are a fast transient, where
+    extrapolating the last updates overshoots) the residual-minimising step
+    keeps the extrapolated start's solves within a few sweeps of the plain
+    ones, and on the settled disk it stays near 1 (the plain extrapolation)."""
+    d, sys0 = _settled_disk(settle=1)
+    snap = d.snapshot(SNAP)
+    plain = _replay(d, snap, sys0, WS.OFF, 2)
+    s0 = WS.stats(d).step_sum
+    ext = _replay(d, snap, sys0, WS.EXTRAPOLATE, 2)
+    steps = (WS.stats(d).step_sum - s0) / max(ext["predictions"], 1)
+    print(plain["sweeps"], ext["sweeps"], steps)
+    assert ext["sweeps"] <= plain["sweeps"] + 2
+    assert _rel(ext["T"], plain["T"]) < 1e-9
+    d.close()
+    d, sys0 = _settled_disk()
+    snap = d.snapshot(SNAP)
+    s0 = WS.stats(d).step_sum
+    ext = _replay(d, snap, sys0, WS.EXTRAPOLATE, 4)
+    steps = (WS.stats(d).step_sum - s0) / max(ext["predictions"] - 1, 1)   # the first solve has no update
+    print("settled mean step", steps)
+    assert 0.5 < steps < 1.5
+    d.close()
+
+
 def test_linear_extrapolation_beats_the_previous_update():
     """Order 2 (the rate extrapolated linearly) against order 1 (the last
     update's rate) on the same DTs."""
