@@ -656,7 +656,8 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-disk ensemble measurement")
     ap.add_argument("--combined", action="store_true",
                     help="only the combined 16-disk workload (1024x3072 and 2048x6144 grids, batched with the learned "
-                         "warm start against plain sequential; about 10 minutes); prints its JSON line")
+                         "and with the extrapolated SOR start against plain sequential; about 15 minutes); prints its "
+                         "JSON line")
     ap.add_argument("--profile", action="store_true",
                     help="run --steps DTs inside cuProfilerStart/Stop for ncu; prints no bench line")
     ap.add_argument("--grid", type=int, nargs=2, metavar=("NRAD", "NSEC"), default=(NR, NS),
