@@ -28,7 +28,8 @@ int wn_record_update(int nr, int ns, const double *tconv, const double *tstart, 
                      const double *dt, double *dts, cudaStream_t s);
 int ws_extrapolate(int nr, int ns, double *T, const double *hist, int order, const double *dt, const double *dts,
                    const double *ml, const double *mlip, const double *mlim, const double *mljp, const double *mljm,
-                   const double *rhs, double *scratch, double *part, double *step, int nsm, cudaStream_t s);
+                   const double *rhs, const double *cw, const double *omega, double *scratch, double *vq,
+                   double *part, double *step, int nsm, cudaStream_t s);
 int wn_last_loss(thorin_warmnet *n, double *loss);
 int wn_dims(const thorin_warmnet *n, int *nr, int *ns);
 
@@ -194,6 +195,7 @@ struct thorin_disk {
   double *ws_prev = nullptr;
   double *ws_dts = nullptr;
   double *ws_part = nullptr;     // block partials of the extrapolated start's step length (4 nsm + 2)
+  double *ws_vq = nullptr;       // its per-cell terms of the Jacobi step (2 fields)
   double *ws_step = nullptr;     // its step length and the running sum of the steps
   int ws_nh = 0;                 // slots of ws_prev
   int ws_order = 2;              // order of the extrapolated start
@@ -645,6 +647,8 @@ extern "C" int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode,
   }
   if (mode != THORIN_WS_OFF)
     RCHK(ws_history(d, mode == THORIN_WS_EXTRAPOLATE ? d->ws_order : 1));
+  if (mode == THORIN_WS_EXTRAPOLATE && !d->ws_vq)
+    RCHK(dalloc(d, (void **)&d->ws_vq, 2 * (size_t)d->nr * d->ns * sizeof(double)));
   if (mode != d->ws_mode && d->ws_dts)             // nothing recorded in the new mode yet
     CUCHK(cudaMemsetAsync(d->ws_dts, 0, THORIN_WS_MAX_ORDER * sizeof(double), d->s));
   d->ws_f = f;
@@ -1567,7 +1571,8 @@ static int sor_solve(thorin_disk *d, double omega, int *niter, int *capped, bool
     CUCHK(cudaMemcpyAsync(d->tbackup, d->temper, (size_t)d->nr * d->ns * sizeof(double), cudaMemcpyDeviceToDevice,
                           d->s));
     RCHK(ws_extrapolate(d->nr, d->ns, d->temper, d->ws_prev, d->ws_order, d->ctl + CTL_DT, d->ws_dts, d->ml, d->mlip,
-                          d->mlim, d->mljp, d->mljm, d->rhs, d->ws_jac, d->ws_part, d->ws_step, d->g.nsm, d->s));
+                          d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, d->ctl + CTL_SOR_OMEGA, d->ws_jac,
+                          d->ws_vq, d->ws_part, d->ws_step, d->g.nsm, d->s));
     d->ws_st.predictions++;
   }
   if (d->timing) CUCHK(cudaEventRecord(d->ev[0], d->s));
@@ -2072,7 +2077,8 @@ static int capture_sor(thorin_disk *d)
                           d->rhs, d->ws_prev, d->ws_jac, d->sor.jscale, 0.0, d->ctl + CTL_SOR_OMEGA, d->s));
     else
       RCHK(ws_extrapolate(d->nr, d->ns, d->temper, d->ws_prev, d->ws_order, d->ctl + CTL_DT, d->ws_dts, d->ml, d->mlip,
-                          d->mlim, d->mljp, d->mljm, d->rhs, d->ws_jac, d->ws_part, d->ws_step, d->g.nsm, d->s));
+                          d->mlim, d->mljp, d->mljm, d->rhs, d->sor_cw, d->ctl + CTL_SOR_OMEGA, d->ws_jac,
+                          d->ws_vq, d->ws_part, d->ws_step, d->g.nsm, d->s));
   }
   cudaStreamCaptureStatus cs;
   cudaGraph_t cg;

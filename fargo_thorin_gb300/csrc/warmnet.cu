@@ -864,12 +864,18 @@ __global__ void k_ws_delta(long long cells, const double *__restrict__ hist, int
 
 // Step length along u that minimises the L2 norm of the residual
 // R(T + s u) = R(T) + s A u over the unknowns: block partials of
-// sum R(T) (A u) and sum (A u)^2, grid-stride, fixed order.
+// sum R(T) (A u) and sum (A u)^2, grid-stride, fixed order.  Each unknown
+// also gets what the start then needs for one Jacobi step from T + s u:
+// with R(T + s u)/Ml = q0 + s qa (q = R cw / omega, cw = omega / Ml from the
+// solve's own start pass), v = u - qa and q0 go to vq[0..cells) and
+// vq[cells..2 cells).
 __global__ void k_ws_line(int nr, int ns, const double *__restrict__ T, const double *__restrict__ u, SorSys m,
+                          const double *__restrict__ cw, const double *__restrict__ omega, double *__restrict__ vq,
                           double *__restrict__ part)
 {
   double ra = 0.0, aa = 0.0;
-  const long long n = (long long)(nr - 2) * ns;
+  const long long n = (long long)(nr - 2) * ns, cells = (long long)nr * ns;
+  const double iw = 1.0 / *omega;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
     const int i = 1 + (int)(k / ns), j = (int)(k % ns);
     const size_t pq = sor_pidx(i, j, ns >> 1);
@@ -880,6 +886,9 @@ __global__ void k_ws_line(int nr, int ns, const double *__restrict__ T, const do
                       u[ljm] * m.mljm[pq];
     ra += r * au;
     aa += au * au;
+    const double iml = cw[pq] * iw;                 // 1 / Ml
+    vq[l] = u[l] - au * iml;
+    vq[cells + l] = r * iml;
   }
   ra = block_reduce(ra, OpAdd(), 0.0);
   if (threadIdx.x == 0) part[blockIdx.x] = ra;
@@ -907,16 +916,17 @@ __global__ void k_ws_step(const double *__restrict__ part, int nb, double *__res
   }
 }
 
-// T += s u on the unknowns; a non-positive result keeps T
-__global__ void k_ws_apply(int nr, int ns, double *__restrict__ T, const double *__restrict__ u,
-                           const double *__restrict__ step)
+// T -> T + s u - R(T + s u) / Ml = T + s v - q0 on the unknowns, once a
+// solve is recorded (the first solve after attaching starts from T); a
+// non-positive result keeps T
+__global__ void k_ws_apply(int nr, int ns, double *__restrict__ T, const double *__restrict__ vq,
+                           const double *__restrict__ step, const double *__restrict__ dts)
 {
-  const long long n = (long long)(nr - 2) * ns;
+  const long long n = (long long)(nr - 2) * ns, cells = (long long)nr * ns;
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const double st = *step;
-  if (q >= n || st == 0.0) return;
+  if (q >= n || !(dts[0] > 0.0)) return;
   const long long l = q + ns;
-  const double t = __fma_rn(st, u[l], T[l]);
+  const double t = __fma_rn(*step, vq[l], T[l]) - vq[cells + l];
   if (t > 0.0) T[l] = t;
 }
 
@@ -1222,12 +1232,15 @@ int wn_record_update(int nr, int ns, const double *tconv, const double *tstart, 
   return e == cudaSuccess ? THORIN_OK : wn_fail("record kernel", e);
 }
 
-// T (start of the solve) -> T + s u: u the update extrapolated from the last
-// `order` recorded solves (into scratch), s the step that minimises the L2
-// residual along u (part: 4 nsm + 2 doubles; step: s and its running sum).
+// T (start of the solve) -> T + s u followed by one Jacobi step: u the
+// update extrapolated from the last `order` recorded solves (into scratch),
+// s the step that minimises the L2 residual along u (part: 4 nsm + 2
+// doubles; step: s and its running sum; vq: 2 nr ns doubles; cw = omega/Ml
+// and omega of the solve).
 int ws_extrapolate(int nr, int ns, double *T, const double *hist, int order, const double *dt, const double *dts,
                    const double *ml, const double *mlip, const double *mlim, const double *mljp, const double *mljm,
-                   const double *rhs, double *scratch, double *part, double *step, int nsm, cudaStream_t s)
+                   const double *rhs, const double *cw, const double *omega, double *scratch, double *vq,
+                   double *part, double *step, int nsm, cudaStream_t s)
 {
   if (order < 1 || order > WS_MAXORDER) return THORIN_ERR_ARG;
   WsCoef cf = {};
@@ -1242,9 +1255,9 @@ int ws_extrapolate(int nr, int ns, double *T, const double *hist, int order, con
   const SorSys m{ml, mlip, mlim, mljp, mljm, rhs};
   const int nb = 2 * nsm;
   k_ws_delta<<<nblk(cells), 256, 0, s>>>(cells, hist, order, dt, dts, cf, scratch);
-  k_ws_line<<<nb, 256, 0, s>>>(nr, ns, T, scratch, m, part);
+  k_ws_line<<<nb, 256, 0, s>>>(nr, ns, T, scratch, m, cw, omega, vq, part);
   k_ws_step<<<1, 256, 0, s>>>(part, nb, step);
-  k_ws_apply<<<nblk((long long)(nr - 2) * ns), 256, 0, s>>>(nr, ns, T, scratch, step);
+  k_ws_apply<<<nblk((long long)(nr - 2) * ns), 256, 0, s>>>(nr, ns, T, vq, step, dts);
   g_thorin_launches += 4;
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? THORIN_OK : wn_fail("extrapolation kernels", e);

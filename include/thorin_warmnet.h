@@ -89,17 +89,17 @@ int thorin_warmnet_adam(thorin_warmnet *n, float lr, float beta1, float beta2, f
  * over the unknowns, T_pred = T_k + Jacobi step + the prediction and target
  * the converged update beyond the Jacobi step in the network's units.
  * EXTRAPOLATE (no network, n ignored): every SOR solve starts from
- *   T_old + s u,   u = dt * r,
- * r the update rate (T_conv - T_start) / dt of the last m solves extrapolated
- * to this one as an evenly spaced sequence (m = the order, 2 unless set:
- * r = 2 r_1 - r_2; order 1 takes r = r_1, order 3 r = 3 r_1 - 3 r_2 + r_3),
- * and s in [0, 2] the step that minimises the L2 norm of the residual along
- * u (s = 1 is the plain extrapolation; s near 0 where u does not help, as in
- * fast transients).  While fewer than m solves are recorded since attaching
- * the order is what they allow, and the first solve starts from T_old.  A
- * cell whose start is not positive keeps T_old.  In every mode the exit
- * tests and the threshold (eps times the L1 residual of T_old) are the plain
- * solve's. */
+ *   T_s - R(T_s) / Ml,   T_s = T_old + s u,   u = dt * r,
+ * i.e. one Jacobi step from T_s, with r the update rate
+ * (T_conv - T_start) / dt of the last m solves extrapolated to this one as
+ * an evenly spaced sequence (m = the order, 2 unless set: r = 2 r_1 - r_2;
+ * order 1 takes r = r_1, order 3 r = 3 r_1 - 3 r_2 + r_3), and s in [0, 2]
+ * the step that minimises the L2 norm of the residual R along u (s = 1 is
+ * the plain extrapolation; s near 0 where u does not help, as in fast
+ * transients).  While fewer than m solves are recorded since attaching the
+ * order is what they allow, and the first solve starts from T_old.  A cell
+ * whose start is not positive keeps T_old.  In every mode the exit tests and
+ * the threshold (eps times the L1 residual of T_old) are the plain solve's. */
 int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode, float lr);
 
 /* Order of the EXTRAPOLATE start, 1 .. THORIN_WS_MAX_ORDER (default 2). */
