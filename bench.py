@@ -210,7 +210,8 @@ def warm_start_phase(d, snapd, snap_sys, steps, stream, barrier, t_plain, plain_
         return {"order": order, "sweeps_per_solve": per, "sweeps_ratio_plain_over_extrapolated": plain_per_solve / per,
                 "value": NR * NS * subs / (ms / 1e3), "ms_per_step": ms / steps, "substeps": subs,
                 "t_rel_l2_vs_plain": float(np.linalg.norm(t - t_plain) / np.linalg.norm(t_plain)),
-                "start": "T_old + dt (2 r_1 - r_2), r_k = (T_conv - T_start) / dt of the k-th last solve"}
+                "start": "one Jacobi step from T_old + s dt (2 r_1 - r_2), r_k = (T_conv - T_start) / dt of the k-th "
+                         "last solve, s minimising the L2 residual along it"}
 
     extrapolated = replay_extrapolated()
     # control: the same coupling with an untrained network (zero output
