@@ -22,6 +22,7 @@
  */
 #include "fargo.h"
 #include "thorin_gpu.h"
+#include "thorin_warmnet.h"
 
 #ifndef THORIN_DROPIN_SOREPS
 #define THORIN_DROPIN_SOREPS 1.0e-6      /* SOREPS, EnergySources.c:23 */
@@ -243,6 +244,17 @@ static void dropin_init(PolarGrid *Rho, PolarGrid *Vrad, PolarGrid *Vtheta, Pola
   CALL(thorin_gpu_set_time(g_disk, PhysicalTime));
   CALL(thorin_gpu_set_frame(g_disk, OmegaFrame));
   CALL(thorin_gpu_refresh(g_disk, 0));   /* EOS of the uploaded state */
+  {
+    /* opt-in, no reference counterpart: THORIN_SOR_EXTRAPOLATE=<order 1..4>
+     * starts every SOR solve from the extrapolated update (the exit tests
+     * and the threshold stay SuccessiveOverrelaxation's; only the number of
+     * sweeps changes) */
+    const char *ex = getenv("THORIN_SOR_EXTRAPOLATE");
+    if (ex && atoi(ex) > 0) {
+      CALL(thorin_gpu_warmstart_order(g_disk, atoi(ex)));
+      CALL(thorin_gpu_warmstart(g_disk, NULL, THORIN_WS_EXTRAPOLATE, 0.f));
+    }
+  }
   g_iter = begin_i;
 }
 

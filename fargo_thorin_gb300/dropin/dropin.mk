@@ -32,7 +32,7 @@ $(OUT)/main.o: $(REF)/src_main/main.c
 	mkdir -p $(OUT)
 	$(CC) $(CFLAGS) $(INC) -DAlgoGas=AlgoGasGPU -c $< -o $@
 
-$(OUT)/AlgoGasGPU.o: $(HERE)/AlgoGasGPU.c $(PKG)/../include/thorin_gpu.h
+$(OUT)/AlgoGasGPU.o: $(HERE)/AlgoGasGPU.c $(PKG)/../include/thorin_gpu.h $(PKG)/../include/thorin_warmnet.h
 	mkdir -p $(OUT)
 	$(CC) $(CFLAGS) $(INC) $(SORDEF) -c $< -o $@
 
