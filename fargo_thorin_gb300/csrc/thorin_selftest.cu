@@ -381,6 +381,46 @@ __global__ void __launch_bounds__(128) k_selftest_umma(const uint16_t *__restric
   if (warp == 0) umma::tmem_dealloc(tmem, 32);
 }
 
+// The bounded mbarrier wait of the tensor-core kernels (umma::mbar_wait),
+// made to run out: thread 0 waits for a phase of a barrier that nothing
+// arrives at, with `polls` polls, and records the outcome in out[0] (1: it
+// gave up); then it arrives itself and waits again, which must succeed
+// (out[1] = 1).  The kernel returns normally either way.
+__global__ void k_selftest_bounded_wait(long long polls, int *__restrict__ out)
+{
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  umma::mbar_init(&bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  out[0] = umma::mbar_wait(&bar, 0u, polls) ? 0 : 1;
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(umma::smem_addr(&bar)) : "memory");
+  out[1] = umma::mbar_wait(&bar, 0u, polls) ? 1 : 0;
+}
+
+extern "C" int thorin_selftest_bounded_wait(long long polls, int *timed_out, int *completed_after_arrival)
+{
+  if (polls < 1 || polls > (1LL << 20) || !timed_out || !completed_after_arrival) {
+    g_last_error = "selftest_bounded_wait: 1 <= polls <= 2^20 and two output pointers required";
+    return THORIN_ERR_ARG;
+  }
+  int *dev = nullptr, host[2] = {0, 0};
+  cudaError_t e = cudaMalloc((void **)&dev, sizeof(host));
+  if (e == cudaSuccess) e = cudaMemset(dev, 0, sizeof(host));
+  if (e == cudaSuccess) {
+    k_selftest_bounded_wait<<<1, 32>>>(polls, dev);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(host, dev, sizeof(host), cudaMemcpyDeviceToHost);
+  if (dev) cudaFree(dev);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("selftest_bounded_wait: ") + cudaGetErrorString(e);
+    return THORIN_ERR_CUDA;
+  }
+  *timed_out = host[0];
+  *completed_after_arrival = host[1];
+  return THORIN_OK;
+}
+
 extern "C" int thorin_selftest_umma(const uint16_t *a, const uint16_t *b, float *d)
 {
   if (!a || !b || !d) {

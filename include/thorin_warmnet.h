@@ -109,6 +109,13 @@ int thorin_gpu_warmstart_order(thorin_disk *d, int order);
  * with bf16 bit patterns a, b (row-major) and FP32 d, on one CTA. */
 int thorin_selftest_umma(const uint16_t *a, const uint16_t *b, float *d);
 
+/* Self-test of the bounded mbarrier wait behind every tensor-core
+ * completion: a wait for a barrier that nothing arrives at gives up after
+ * `polls` polls (*timed_out = 1) and the kernel returns normally; after an
+ * arrival the same wait completes (*completed_after_arrival = 1).  The
+ * network kernels turn such a give-up into THORIN_ERR_TIMEOUT. */
+int thorin_selftest_bounded_wait(long long polls, int *timed_out, int *completed_after_arrival);
+
 /* Counters of the attached network's use on this disk. */
 typedef struct thorin_ws_stats {
   long long predictions;   /* network applications inside SOR solves   */
