@@ -649,7 +649,7 @@ extern "C" int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode,
     RCHK(ws_history(d, mode == THORIN_WS_EXTRAPOLATE ? d->ws_order : 1));
   if (mode == THORIN_WS_EXTRAPOLATE && !d->ws_vq)
     RCHK(dalloc(d, (void **)&d->ws_vq, 2 * (size_t)d->nr * d->ns * sizeof(double)));
-  if (mode != d->ws_mode && d->ws_dts)             // nothing recorded in the new mode yet
+  if (d->ws_dts)                                   // every attach starts without recorded updates
     CUCHK(cudaMemsetAsync(d->ws_dts, 0, THORIN_WS_MAX_ORDER * sizeof(double), d->s));
   d->ws_f = f;
   if (d->dt_graph && (d->ws_net != n || d->ws_mode != mode)) {

@@ -98,8 +98,11 @@ int thorin_warmnet_adam(thorin_warmnet *n, float lr, float beta1, float beta2, f
  * the plain extrapolation; s near 0 where u does not help, as in fast
  * transients).  While fewer than m solves are recorded since attaching the
  * order is what they allow, and the first solve starts from T_old.  A cell
- * whose start is not positive keeps T_old.  In every mode the exit tests and
- * the threshold (eps times the L1 residual of T_old) are the plain solve's. */
+ * whose start is not positive keeps T_old.  The recorded updates belong to
+ * the disk, not to its fields: after restoring other fields, attach the mode
+ * again (every attach starts without recorded updates) so that the next
+ * solves do not extrapolate from updates of another state.  In every mode the exit tests and the
+ * threshold (eps times the L1 residual of T_old) are the plain solve's. */
 int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode, float lr);
 
 /* Order of the EXTRAPOLATE start, 1 .. THORIN_WS_MAX_ORDER (default 2). */
