@@ -82,6 +82,7 @@ SIGNATURES = {
                                           C.POINTER(C.c_int)]),
     "thorin_ensemble_tune": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
                                        C.POINTER(C.c_int), _D, _D]),
+    "thorin_warmstart_coefficients": (C.c_int, [C.c_int, _D]),
     "thorin_selftest_bounded_wait": (C.c_int, [C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "thorin_selftest_umma": (C.c_int, [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.POINTER(C.c_float)]),
     "thorin_planet_from_elements": (C.c_int, [C.POINTER(ThorinPlanets), C.c_int] + [C.c_float] * 9),

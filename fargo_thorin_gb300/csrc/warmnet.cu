@@ -1232,6 +1232,17 @@ int wn_record_update(int nr, int ns, const double *tconv, const double *tstart, 
   return e == cudaSuccess ? THORIN_OK : wn_fail("record kernel", e);
 }
 
+extern "C" int thorin_warmstart_coefficients(int order, double *c)
+{
+  if (order < 1 || order > WS_MAXORDER || !c) return THORIN_ERR_ARG;
+  double b = 1.0;                                   // binom(order, k + 1), built up along k
+  for (int k = 0; k < order; k++) {
+    b = b * (double)(order - k) / (double)(k + 1);
+    c[k] = (k & 1) ? -b : b;
+  }
+  return THORIN_OK;
+}
+
 // T (start of the solve) -> T + s u followed by one Jacobi step: u the
 // update extrapolated from the last `order` recorded solves (into scratch),
 // s the step that minimises the L2 residual along u (part: 4 nsm + 2
@@ -1244,13 +1255,7 @@ int ws_extrapolate(int nr, int ns, double *T, const double *hist, int order, con
 {
   if (order < 1 || order > WS_MAXORDER) return THORIN_ERR_ARG;
   WsCoef cf = {};
-  for (int m = 1; m <= WS_MAXORDER; m++) {
-    double b = 1.0;                                 // binom(m, k + 1), built up along k
-    for (int k = 0; k < m; k++) {
-      b = b * (double)(m - k) / (double)(k + 1);
-      cf.c[m - 1][k] = (k & 1) ? -b : b;
-    }
-  }
+  for (int m = 1; m <= WS_MAXORDER; m++) thorin_warmstart_coefficients(m, cf.c[m - 1]);
   const long long cells = (long long)nr * ns;
   const SorSys m{ml, mlip, mlim, mljp, mljm, rhs};
   const int nb = 2 * nsm;

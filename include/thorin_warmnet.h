@@ -108,6 +108,12 @@ int thorin_gpu_warmstart(thorin_disk *d, thorin_warmnet *n, int mode, float lr);
 /* Order of the EXTRAPOLATE start, 1 .. THORIN_WS_MAX_ORDER (default 2). */
 int thorin_gpu_warmstart_order(thorin_disk *d, int order);
 
+/* The weights c[0..order) of the last `order` update rates in the
+ * extrapolated rate r = sum_k c[k] r_(k+1): backward differences to the next
+ * point of an evenly spaced sequence, c[k] = (-1)^k binom(order, k+1)
+ * (2, -1 for order 2).  Host only; no GPU needed. */
+int thorin_warmstart_coefficients(int order, double *c);
+
 /* Layout check of the tensor-core path: D[128][32] = A[128][64] * B[32][64]^T
  * with bf16 bit patterns a, b (row-major) and FP32 d, on one CTA. */
 int thorin_selftest_umma(const uint16_t *a, const uint16_t *b, float *d);

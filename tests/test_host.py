@@ -45,6 +45,26 @@ def test_header_functions_exported(lib):
         assert n in _lib.SIGNATURES, f"{n} has no ctypes signature"
 
 
+def test_extrapolation_weights(lib):
+    """The extrapolated SOR start's weights of the last update rates are the
+    backward differences of an evenly spaced sequence: they reproduce
+    polynomials of degree order-1 exactly at the next point."""
+    import math
+    for order in range(1, 5):
+        c = (C.c_double * order)()
+        assert lib.thorin_warmstart_coefficients(order, c) == 0
+        want = [(-1) ** k * math.comb(order, k + 1) for k in range(order)]
+        assert list(c) == want
+        # samples p(-1), p(-2), ... of a degree order-1 polynomial extrapolate to p(0)
+        for deg in range(order):
+            coef = [0.3 * (d + 1) for d in range(deg + 1)]
+            p = lambda x: sum(a * x ** d for d, a in enumerate(coef))
+            assert abs(sum(c[k] * p(-(k + 1)) for k in range(order)) - p(0)) < 1e-12
+    c = (C.c_double * 5)()
+    assert lib.thorin_warmstart_coefficients(0, c) != 0
+    assert lib.thorin_warmstart_coefficients(5, c) != 0
+
+
 def test_params_default_matches_struct(lib):
     """thorin_params_default fills the grid size and the SOR controls the same
     way the Python in.par path does for an empty file plus mandatory keys."""
